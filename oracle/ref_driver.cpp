@@ -1,0 +1,384 @@
+// Dump driver for the reference Omega_h build (oracle/_ref).  Builds a
+// seeded box workload with the reference's own build_box, runs one adapt
+// pass (refine_by_size -> coarsen_by_size -> swap_edges when the minimum
+// quality is below min_quality_desired, as src/Omega_h_adapt.cpp:173-210
+// sequences them) and writes every per-stage intermediate array plus the
+// mesh after each operator as raw little-endian files with a manifest.
+//
+// This is test infrastructure: it produces golden fixtures and is never
+// linked into the product.
+//
+//   ref_driver DIM N METRIC SEED MIN_QUAL_ALLOWED OUTDIR
+#include <Omega_h_adapt.hpp>
+#include <Omega_h_adj.hpp>
+#include <Omega_h_array_ops.hpp>
+#include <Omega_h_build.hpp>
+#include <Omega_h_coarsen.hpp>
+#include <Omega_h_collapse.hpp>
+#include <Omega_h_file.hpp>
+#include <Omega_h_hilbert.hpp>
+#include <Omega_h_indset.hpp>
+#include <Omega_h_library.hpp>
+#include <Omega_h_map.hpp>
+#include <Omega_h_mark.hpp>
+#include <Omega_h_mesh.hpp>
+#include <Omega_h_metric.hpp>
+#include <Omega_h_modify.hpp>
+#include <Omega_h_quality.hpp>
+#include <Omega_h_refine.hpp>
+#include <Omega_h_refine_qualities.hpp>
+#include <Omega_h_shape.hpp>
+#include <Omega_h_swap.hpp>
+#include <Omega_h_swap3d.hpp>
+#include <Omega_h_swap3d_loop.hpp>
+#include <Omega_h_swap3d_tables.hpp>
+#include <Omega_h_timer.hpp>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "ohg_workload.hpp"
+
+using namespace Omega_h;
+
+static std::string g_out;
+static FILE* g_manifest = nullptr;
+
+template <typename T>
+static const char* dtype_name();
+template <>
+const char* dtype_name<I8>() { return "i1"; }
+template <>
+const char* dtype_name<I32>() { return "i4"; }
+template <>
+const char* dtype_name<I64>() { return "i8"; }
+template <>
+const char* dtype_name<Real>() { return "f8"; }
+
+template <typename T>
+static void dump(std::string const& name, Read<T> a) {
+  HostRead<T> h(a);
+  std::string path = g_out + "/" + name + ".bin";
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (h.size()) std::fwrite(h.data(), sizeof(T), size_t(h.size()), f);
+  std::fclose(f);
+  std::fprintf(g_manifest, "%s %s %d\n", name.c_str(), dtype_name<T>(),
+      int(h.size()));
+}
+
+static void dump_scalar(std::string const& name, double v) {
+  dump(name, Reals({v}));
+}
+
+static void dump_mesh(Mesh* mesh, std::string const& p) {
+  int dim = mesh->dim();
+  dump_scalar(p + "nents", mesh->nverts());
+  for (int d = 1; d <= dim; ++d) {
+    dump(p + "ev2v_" + std::to_string(d), mesh->ask_verts_of(d));
+    auto down = mesh->ask_down(d, d - 1);
+    dump(p + "down_" + std::to_string(d), down.ab2b);
+    if (d > 1) dump(p + "downcodes_" + std::to_string(d), down.codes);
+  }
+  for (int d = 0; d <= dim; ++d) {
+    auto s = std::to_string(d);
+    dump(p + "global_" + s, mesh->globals(d));
+    dump(p + "class_dim_" + s, mesh->get_array<I8>(d, "class_dim"));
+    dump(p + "class_id_" + s, mesh->get_array<I32>(d, "class_id"));
+  }
+  dump(p + "coords", mesh->coords());
+  dump(p + "metric", mesh->get_array<Real>(VERT, "metric"));
+  if (mesh->has_tag(EDGE, "length"))
+    dump(p + "length", mesh->get_array<Real>(EDGE, "length"));
+  if (mesh->has_tag(dim, "quality"))
+    dump(p + "quality", mesh->get_array<Real>(dim, "quality"));
+}
+
+static void dump_adjacency(Mesh* mesh, std::string const& p) {
+  int dim = mesh->dim();
+  for (int lo = 0; lo < dim; ++lo) {
+    for (int hi = lo + 1; hi <= dim; ++hi) {
+      auto s = std::to_string(lo) + std::to_string(hi);
+      auto up = mesh->ask_up(lo, hi);
+      dump(p + "up_a2ab_" + s, up.a2ab);
+      dump(p + "up_ab2b_" + s, up.ab2b);
+      dump(p + "up_codes_" + s, up.codes);
+    }
+  }
+  if (dim == 3) {
+    auto t2e = mesh->ask_down(3, 1);
+    dump(p + "down31", t2e.ab2b);
+    dump(p + "downcodes31", t2e.codes);
+  }
+  for (int d = 0; d <= 1; ++d) {
+    auto star = mesh->ask_star(d);
+    dump(p + "star_a2ab_" + std::to_string(d), star.a2ab);
+    dump(p + "star_ab2b_" + std::to_string(d), star.ab2b);
+  }
+  auto dual = mesh->ask_dual();
+  dump(p + "dual_a2ab", dual.a2ab);
+  dump(p + "dual_ab2b", dual.ab2b);
+}
+
+static double seconds_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0)
+      .count();
+}
+
+// refine stage intermediates, following refine_by_size/refine_ghosted
+// (src/Omega_h_refine.cpp:17-41,92-100)
+static void dump_refine_stage(Mesh* mesh, AdaptOpts const& opts) {
+  auto lengths = mesh->ask_lengths();
+  auto cands = each_gt(lengths, opts.max_length_desired);
+  dump("r_cands", cands);
+  if (get_max(cands) != 1) return;
+  auto cands2edges = collect_marked(cands);
+  dump("r_cands2edges", cands2edges);
+  dump("r_midmetrics", get_mident_metrics(mesh, EDGE, cands2edges,
+                           mesh->get_array<Real>(VERT, "metric")));
+  auto cand_quals = refine_qualities(mesh, cands2edges);
+  dump("r_cand_quals", cand_quals);
+  auto good = each_geq_to(cand_quals, opts.min_quality_allowed);
+  if (get_max(good) != 1) return;
+  auto nedges = mesh->nedges();
+  auto initial = map_onto(good, cands2edges, nedges, I8(0), 1);
+  auto edge_quals = map_onto(cand_quals, cands2edges, nedges, 0.0, 1);
+  auto keys = find_indset(mesh, EDGE, edge_quals, initial);
+  dump("r_keys", keys);
+  dump("r_rep2md", get_rep2md_order_adapt(mesh, EDGE, VERT, keys));
+}
+
+// coarsen stage intermediates, following coarsen_by_size, coarsen_verts,
+// coarsen_element_based1 and coarsen_ghosted (src/Omega_h_coarsen.cpp:29-104,
+// 174-208)
+static void dump_coarsen_stage(Mesh* mesh, AdaptOpts const& opts) {
+  auto lengths = mesh->ask_lengths();
+  auto edge_is_cand = each_lt(lengths, opts.min_length_desired);
+  dump("c_edge_is_cand", edge_is_cand);
+  if (get_max(edge_is_cand) != 1) return;
+  auto vert_marks = mark_down(mesh, EDGE, VERT, edge_is_cand);
+  dump("c_vert_marks", vert_marks);
+  auto ev2v = mesh->ask_verts_of(EDGE);
+  auto nedges = mesh->nedges();
+  HostRead<LO> hev2v(ev2v);
+  HostRead<I8> hvm(vert_marks);
+  HostWrite<I8> hcodes(nedges);
+  for (LO e = 0; e < nedges; ++e) {
+    I8 code = DONT_COLLAPSE;
+    for (Int eev = 0; eev < 2; ++eev)
+      if (hvm[hev2v[e * 2 + eev]]) code = do_collapse(code, eev);
+    hcodes[e] = code;
+  }
+  Read<I8> edge_codes(hcodes.write());
+  dump("c_edge_codes", edge_codes);
+  auto cands2edges = collect_marked(each_neq_to(edge_codes, I8(DONT_COLLAPSE)));
+  auto cand_codes = read(unmap(cands2edges, edge_codes, 1));
+  cand_codes = check_collapse_class(mesh, cands2edges, cand_codes);
+  dump("c_class_codes", cand_codes);
+  if (get_max(cand_codes) <= DONT_COLLAPSE) return;
+  edge_codes = map_onto(cand_codes, cands2edges, nedges, I8(DONT_COLLAPSE), 1);
+  cands2edges = collect_marked(each_neq_to(edge_codes, I8(DONT_COLLAPSE)));
+  cand_codes = read(unmap(cands2edges, edge_codes, 1));
+  dump("c_cands2edges0", cands2edges);
+  cand_codes = check_collapse_exposure(mesh, cands2edges, cand_codes);
+  dump("c_expo_codes", cand_codes);
+  auto filt = [&](Reals* quals) {
+    auto keep = each_neq_to(cand_codes, I8(DONT_COLLAPSE));
+    auto new2old = collect_marked(keep);
+    cands2edges = unmap(new2old, cands2edges, 1);
+    cand_codes = unmap(new2old, cand_codes, 1);
+    if (quals) *quals = unmap(new2old, *quals, 2);
+  };
+  filt(nullptr);
+  dump("c_cands2edges1", cands2edges);
+  cand_codes = prevent_coarsen_overshoot(
+      mesh, opts.max_length_desired, cands2edges, cand_codes);
+  dump("c_over_codes", cand_codes);
+  filt(nullptr);
+  dump("c_cands2edges2", cands2edges);
+  if (cands2edges.size() == 0) return;
+  auto quals = coarsen_qualities(mesh, cands2edges, cand_codes);
+  dump("c_quals", quals);
+  cand_codes = filter_coarsen_min_qual(cand_codes, quals, opts.min_quality_allowed);
+  dump("c_minq_codes", cand_codes);
+  filt(&quals);
+  dump("c_cands2edges3", cands2edges);
+  dump("c_cand_codes3", cand_codes);
+  if (cands2edges.size() == 0) return;
+  Read<I8> verts_are_cands;
+  Reals vert_quals;
+  Read<GO> vert_rails;
+  choose_rails(mesh, cands2edges, cand_codes, quals, &verts_are_cands,
+      &vert_quals, &vert_rails);
+  dump("c_verts_are_cands", verts_are_cands);
+  dump("c_vert_quals", vert_quals);
+  dump("c_vert_rails", vert_rails);
+  auto keys = find_indset(mesh, VERT, vert_quals, verts_are_cands);
+  dump("c_keys", keys);
+  auto keys2verts = collect_marked(keys);
+  LOs rails2edges;
+  Read<I8> rail_col_dirs;
+  find_rails(mesh, keys2verts, vert_rails, &rails2edges, &rail_col_dirs);
+  dump("c_rails2edges", rails2edges);
+  dump("c_rail_col_dirs", rail_col_dirs);
+  auto dead = mark_dead_ents(mesh, rails2edges, rail_col_dirs);
+  for (int d = 1; d <= mesh->dim(); ++d)
+    dump("c_dead_" + std::to_string(d), dead[d]);
+}
+
+// swap stage intermediates, following swap_part1 and swap3d_ghosted
+// (src/Omega_h_swap.cpp:14-43, src/Omega_h_swap3d.cpp:14-37)
+static void dump_swap_stage(Mesh* mesh, AdaptOpts const& opts) {
+  auto elems_are_cands =
+      mark_sliver_layers(mesh, opts.min_quality_desired, opts.nsliver_layers);
+  dump("s_elem_cands", elems_are_cands);
+  auto edges_are_cands = mark_down(mesh, mesh->dim(), EDGE, elems_are_cands);
+  auto inter = mark_by_class_dim(mesh, EDGE, mesh->dim());
+  edges_are_cands = land_each(edges_are_cands, inter);
+  dump("s_edge_cands", edges_are_cands);
+  if (get_max(edges_are_cands) <= 0) return;
+  auto cands2edges = collect_marked(edges_are_cands);
+  Reals cand_quals;
+  Read<I8> cand_configs;
+  swap3d_qualities(mesh, opts, cands2edges, &cand_quals, &cand_configs);
+  dump("s_cands2edges", cands2edges);
+  dump("s_cand_quals", cand_quals);
+  dump("s_cand_configs", cand_configs);
+  auto keep = filter_swap_improve(mesh, cands2edges, cand_quals);
+  dump("s_keep", keep);
+  filter_swap(keep, &cands2edges, &cand_quals);
+  if (cands2edges.size() == 0) return;
+  auto is_cand = mark_image(cands2edges, mesh->nedges());
+  auto edge_quals = map_onto(cand_quals, cands2edges, mesh->nedges(), -1.0, 1);
+  auto keys = find_indset(mesh, EDGE, edge_quals, is_cand);
+  dump("s_keys", keys);
+}
+
+static void dump_swap_tables() {
+  std::vector<I32> t;
+  for (int n = 3; n <= 7; ++n) {
+    int nmesh = swap3d::swap_mesh_counts[n];
+    int ntri = swap3d::swap_mesh_sizes[n];
+    int nuniq = 0;
+    for (int i = 0; i < nmesh * ntri; ++i)
+      nuniq = std::max(nuniq, swap3d::swap_meshes[n][i] + 1);
+    t.push_back(n);
+    t.push_back(nmesh);
+    t.push_back(ntri);
+    t.push_back(nuniq);
+    for (int u = 0; u < nuniq; ++u)
+      for (int k = 0; k < 3; ++k) t.push_back(swap3d::swap_triangles[n][u][k]);
+    for (int i = 0; i < nmesh * ntri; ++i) t.push_back(swap3d::swap_meshes[n][i]);
+    int ne = swap3d::nedges[n];
+    t.push_back(ne);
+    int nuedge = 0;
+    if (ne) {
+      for (int m = 0; m < nmesh; ++m)
+        for (int e = 0; e < ne; ++e)
+          nuedge = std::max(nuedge, swap3d::edges2unique[n][m][e] + 1);
+    }
+    t.push_back(nuedge);
+    for (int u = 0; u < nuedge; ++u)
+      for (int k = 0; k < 2; ++k) t.push_back(swap3d::unique_edges[n][u][k]);
+    for (int m = 0; m < nmesh; ++m)
+      for (int e = 0; e < ne; ++e) t.push_back(swap3d::edges2unique[n][m][e]);
+  }
+  HostWrite<I32> h(LO(t.size()));
+  for (size_t i = 0; i < t.size(); ++i) h[LO(i)] = t[i];
+  dump("swap3d_tables", Read<I32>(h.write()));
+}
+
+int main(int argc, char** argv) {
+  if (argc < 7) {
+    std::fprintf(stderr,
+        "usage: %s DIM N METRIC SEED MIN_QUAL_ALLOWED OUTDIR [nopass]\n",
+        argv[0]);
+    return 2;
+  }
+  int dim = std::atoi(argv[1]);
+  int n = std::atoi(argv[2]);
+  int metric_kind = std::atoi(argv[3]);
+  unsigned long long seed = std::strtoull(argv[4], nullptr, 10);
+  double mqa = std::atof(argv[5]);
+  g_out = argv[6];
+  bool stages = argc < 8 || std::string(argv[7]) != "nostages";
+  g_manifest = std::fopen((g_out + "/manifest.txt").c_str(), "w");
+  auto lib = Library(&argc, &argv);
+  auto t0 = std::chrono::steady_clock::now();
+  auto mesh = build_box(lib.world(), OMEGA_H_SIMPLEX, 1., 1., dim == 3 ? 1. : 0.,
+      n, n, dim == 3 ? n : 0);
+  double t_build = seconds_since(t0);
+  // seeded jitter of interior vertices, then the analytic metric
+  auto coords = mesh.coords();
+  auto vcd = mesh.get_array<I8>(VERT, "class_dim");
+  HostWrite<Real> hc(deep_copy(coords));
+  HostRead<I8> hcd(vcd);
+  for (LO v = 0; v < mesh.nverts(); ++v) {
+    if (hcd[v] != dim) continue;
+    for (int j = 0; j < dim; ++j)
+      hc[v * dim + j] += ohg::workload::jitter(seed, v, j, dim, n);
+  }
+  mesh.set_coords(Reals(hc.write()));
+  ohg::workload::MetricParams mp;
+  mp.kind = metric_kind;
+  if (metric_kind == ohg::workload::METRIC_SHOCK)
+    ohg::workload::shock_normal(seed, mp.normal);
+  int ncomp = dim == 3 ? 6 : 3;
+  HostWrite<Real> hm(mesh.nverts() * ncomp);
+  HostRead<Real> hc2(mesh.coords());
+  for (LO v = 0; v < mesh.nverts(); ++v)
+    ohg::workload::metric_at(mp, dim, &hc2[v * dim], &hm[v * ncomp]);
+  mesh.add_tag(VERT, "metric", ncomp, Reals(hm.write()));
+
+  AdaptOpts opts(&mesh);
+  opts.min_quality_allowed = mqa;
+  opts.verbosity = SILENT;
+  dump_scalar("opts",
+      0.0);  // placeholder so the manifest always has an entry
+  dump("opts_values", Reals({opts.min_length_desired, opts.max_length_desired,
+                          opts.max_length_allowed, opts.min_quality_allowed,
+                          opts.min_quality_desired, Real(opts.nsliver_layers)}));
+  if (stages) {
+    dump_mesh(&mesh, "in_");
+    dump_adjacency(&mesh, "in_");
+    dump("in_length_fresh", measure_edges_metric(&mesh));
+    dump("in_quality_fresh", measure_qualities(&mesh));
+    dump("in_hilbert_perm", hilbert::sort_coords(mesh.coords(), dim));
+    if (dim == 3) dump_swap_tables();
+  }
+  // one adapt pass
+  double t_ref = 0, t_coa = 0, t_swp = 0;
+  mesh.set_parting(OMEGA_H_GHOSTED);
+  if (stages) dump_refine_stage(&mesh, opts);
+  auto t1 = std::chrono::steady_clock::now();
+  bool did_refine = refine_by_size(&mesh, opts);
+  t_ref = seconds_since(t1);
+  if (stages) dump_mesh(&mesh, "r_out_");
+  mesh.set_parting(OMEGA_H_GHOSTED);
+  if (stages) dump_coarsen_stage(&mesh, opts);
+  t1 = std::chrono::steady_clock::now();
+  bool did_coarsen = coarsen_by_size(&mesh, opts);
+  t_coa = seconds_since(t1);
+  if (stages) dump_mesh(&mesh, "c_out_");
+  mesh.set_parting(OMEGA_H_GHOSTED);
+  double minq = get_min(mesh.ask_qualities());
+  bool did_swap = false;
+  if (minq < opts.min_quality_desired && dim == 3) {
+    if (stages) dump_swap_stage(&mesh, opts);
+    t1 = std::chrono::steady_clock::now();
+    did_swap = swap_edges(&mesh, opts);
+    t_swp = seconds_since(t1);
+  }
+  dump("pass_flags", LOs({did_refine, did_coarsen, did_swap}));
+  dump_mesh(&mesh, "out_");
+  std::fclose(g_manifest);
+  std::printf(
+      "build %.4f refine %.4f coarsen %.4f swap %.4f pass %.4f "
+      "flags %d %d %d minq %.6f elems_in %d elems_out %d\n",
+      t_build, t_ref, t_coa, t_swp, t_ref + t_coa + t_swp, int(did_refine),
+      int(did_coarsen), int(did_swap), minq,
+      int(std::pow(double(n), dim) * (dim == 3 ? 6 : 2)), int(mesh.nelems()));
+  return 0;
+}

@@ -1,0 +1,111 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs ``oracle/_ref/ref_driver`` (the reference Omega_h library compiled from
+its own sources by ``oracle/ref.mk``) on seeded box workloads and stores
+
+* ``<case>.npz``: every per-stage intermediate array and the mesh before and
+  after each operator of one adapt pass (small cases);
+* ``<case>_digest.json``: sha256 digests of every integer array and
+  sum/min/max/strided samples of every real array (full-size cases, whose raw
+  arrays are too large to commit).
+
+On one rank the reference's global numbers are always 0..n-1 (checked here),
+so ``global_*`` arrays are dropped from the fixtures.
+
+Usage (needs the reference sources, i.e. only in the build container)::
+
+    python tests/golden/make_golden.py [--ref /path/to/omega_h] [case ...]
+"""
+import argparse
+import hashlib
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+# name: (dim, n, metric kind, seed, min_quality_allowed, full fixture?)
+CASES = {
+    # the 8^3 isotropic box (3072 tets, 729 verts), min_quality_allowed 0.3
+    "box8_iso": (3, 8, 0, 12345, 0.3, True),
+    # 12^3 shock metric: exercises refine, coarsen and swap
+    "box12_shock": (3, 12, 1, 7, 0.2, True),
+    # 12^3 boundary layer (aspect up to 1000:1): refine, coarsen and swap
+    "box12_blayer": (3, 12, 2, 3, 0.2, True),
+    # 64^3 shock metric (1,572,864 tets, 274,625 verts): digests only
+    "box64_shock": (3, 64, 1, 2024, 0.2, False),
+}
+
+
+def build_ref(ref):
+    subprocess.run(["make", "-f", "oracle/ref.mk", f"REF={ref}", "-j8"],
+                   cwd=ROOT, check=True, stdout=subprocess.DEVNULL)
+
+
+def run_case(name, spec):
+    dim, n, kind, seed, mqa, full = spec
+    with tempfile.TemporaryDirectory() as tmp:
+        args = [os.path.join(ROOT, "oracle/_ref/ref_driver"), str(dim), str(n),
+                str(kind), str(seed), str(mqa), tmp]
+        out = subprocess.run(args, check=True, capture_output=True, text=True)
+        arrs = {}
+        with open(os.path.join(tmp, "manifest.txt")) as f:
+            for line in f:
+                key, dt, count = line.split()
+                a = np.fromfile(os.path.join(tmp, key + ".bin"), dtype=np.dtype(dt))
+                assert a.size == int(count), key
+                arrs[key] = a
+    for key in list(arrs):
+        if "global_" in key:
+            assert np.array_equal(arrs[key], np.arange(arrs[key].size)), key
+            del arrs[key]
+        elif "ev2v_1" in key:
+            assert np.array_equal(arrs[key], arrs[key.replace("ev2v_1", "down_1")])
+            del arrs[key]
+    meta = {"case": name, "dim": dim, "n": n, "metric": kind, "seed": seed,
+            "min_quality_allowed": mqa, "driver_stdout": out.stdout.strip()}
+    if full:
+        arrs["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+    else:
+        digests = {}
+        for key, a in arrs.items():
+            if a.dtype.kind == "f":
+                idx = np.linspace(0, a.size - 1, num=min(a.size, 1024)).astype(np.int64) \
+                    if a.size else np.zeros(0, np.int64)
+                digests[key] = {"dtype": a.dtype.str, "count": int(a.size),
+                                "sum": math.fsum(a.tolist()) if a.size else 0.0,
+                                "min": float(a.min()) if a.size else 0.0,
+                                "max": float(a.max()) if a.size else 0.0,
+                                "sample_idx": idx.tolist(),
+                                "sample": a[idx].tolist()}
+            else:
+                digests[key] = {"dtype": a.dtype.str, "count": int(a.size),
+                                "sha256": hashlib.sha256(
+                                    np.ascontiguousarray(a).tobytes()).hexdigest()}
+        meta["arrays"] = digests
+        with open(os.path.join(HERE, name + "_digest.json"), "w") as f:
+            json.dump(meta, f)
+    print(name, out.stdout.strip())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("cases", nargs="*")
+    a = ap.parse_args()
+    if not os.path.isdir(a.ref):
+        sys.exit(f"reference sources not found at {a.ref}")
+    build_ref(a.ref)
+    for name in a.cases or CASES:
+        run_case(name, CASES[name])
+
+
+if __name__ == "__main__":
+    main()
