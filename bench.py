@@ -1,0 +1,315 @@
+"""Throughput of one adapt pass (refine -> coarsen -> swap) on the 64^3 box
+(1,572,864 tets, 274,625 verts) with the anisotropic shock metric, in mesh
+elements per second per pass.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one pass over a fresh device copy of the seeded input mesh.
+`value` is timed with CUDA events on the library's stream around the pass
+only (inputs resident in HBM); `e2e` goes through the C ABI from pinned host
+buffers: upload of the mesh arrays, ohg_mesh_from_arrays, the pass and the
+download of the adapted mesh, wall clock with device synchronisation.
+Between timed steps L2 is flushed by writing a 256 MiB buffer.  With N > 1
+(torchrun) every rank adapts its own replica: the pass does not shard.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "box64_shock_pass", "dim": 3, "n": 64, "metric": "shock", "metric_kind": 1,
+            "seed": 2024, "min_quality_allowed": 0.2, "elements": 1572864, "verts": 274625}
+METRIC = "elements/s per adapt pass"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _oracle_driver():
+    path = os.path.join(ROOT, "oracle", "_build", "oracle_driver")
+    if not os.path.exists(path):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j4"], check=True,
+                       stdout=subprocess.DEVNULL)
+    return path
+
+
+def _oracle_pass_seconds(n=None):
+    """Times one pass of the oracle restatement (serial C++) on the workload."""
+    w = WORKLOAD
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([_oracle_driver(), str(w["dim"]), str(n or w["n"]), str(w["metric_kind"]),
+                            str(w["seed"]), str(w["min_quality_allowed"]), d, "time"],
+                           capture_output=True, text=True, check=True)
+    toks = r.stdout.split()
+    return float(toks[toks.index("pass") + 1])
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    w = WORKLOAD
+    for _ in range(args.warmup):
+        _oracle_pass_seconds(n=8)  # small untimed warm-up of the same code
+    times = [_oracle_pass_seconds() for _ in range(args.steps)]
+    total = sum(times)
+    value = w["elements"] * len(times) / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "elements/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {k: w[k] for k in ("workload", "dim", "n", "metric", "seed",
+                                         "min_quality_allowed", "elements")},
+            "cpu_baseline": {"value": value, "unit": "elements/s", "cores": 1, "kind": "port",
+                             "sample": "one full adapt pass of the 64^3 shock box per step, "
+                                       "serial oracle restatement of the reference "
+                                       "(reference sources are not on this machine)"},
+            "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import omega_h_gb300.build as b
+    if rank == 0:
+        b.build()
+    if world > 1:
+        torch.distributed.barrier()
+    from omega_h_gb300 import _lib
+    from omega_h_gb300.mesh import Context, Mesh, adapt_opts
+    w = WORKLOAD
+    ctx = Context(local)
+    sp = ctypes.c_void_p()
+    _lib.call("ohg_context_stream", ctx.handle, ctypes.byref(sp))
+    lib_stream = torch.cuda.ExternalStream(sp.value, device=dev)
+    base = Mesh.build_box(ctx, w["dim"], w["n"])
+    base.apply_workload(w["n"], w["seed"], w["metric_kind"])
+    opts = adapt_opts(w["dim"], min_quality_allowed=w["min_quality_allowed"])
+    nelems = base.nelems()
+    assert nelems == w["elements"]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def clone(m):
+        h = ctypes.c_void_p()
+        _lib.call("ohg_mesh_clone", m.handle, ctypes.byref(h))
+        return Mesh(ctx, h)
+
+    def one_pass(timed):
+        m = clone(base)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        st = m.adapt_pass(opts)
+        e1.record(lib_stream)
+        torch.cuda.synchronize()
+        m.close()
+        return e0.elapsed_time(e1), st
+
+    for _ in range(args.warmup):
+        one_pass(False)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches()
+    ms, stats = [], None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, stats = one_pass(True)
+            ms.append(t)
+    torch.cuda.synchronize()
+    gpu_launches = ctx.launches() - launches0
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * nelems * args.steps / (total_ms / 1e3)
+
+    # ---- e2e through the C ABI from pinned host buffers
+    names = ["down_1", "down_2", "downcodes_2", "down_3", "downcodes_3", "coords", "metric"] + \
+            [f"class_dim_{d}" for d in range(4)] + [f"class_id_{d}" for d in range(4)]
+    host = {k: base.get(k).cpu().pin_memory() for k in names}
+    nents = (ctypes.c_int * 4)(*[base.nents(d) for d in range(4)])
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+
+    def e2e_step():
+        devs = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+        torch.cuda.synchronize()
+        P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        down = (ctypes.c_void_p * 4)(None, P(devs["down_1"]), P(devs["down_2"]), P(devs["down_3"]))
+        codes = (ctypes.c_void_p * 4)(None, None, P(devs["downcodes_2"]), P(devs["downcodes_3"]))
+        cdim = (ctypes.c_void_p * 4)(*[P(devs[f"class_dim_{d}"]) for d in range(4)])
+        cid = (ctypes.c_void_p * 4)(*[P(devs[f"class_id_{d}"]) for d in range(4)])
+        h = ctypes.c_void_p()
+        _lib.call("ohg_mesh_from_arrays", ctx.handle, 3, nents, down, codes, cdim, cid,
+                  P(devs["coords"]), P(devs["metric"]), ctypes.byref(h))
+        m = Mesh(ctx, h)
+        m.adapt_pass(opts)
+        outs = [m.get(k).cpu() for k in names]
+        d2h = sum(t.numel() * t.element_size() for t in outs)
+        m.close()
+        return d2h
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        d2h = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * nelems * args.steps / e2e_s
+
+    # ---- roofline of the stage kernels, each timed alone with CUDA events on
+    # the library stream, L2 flushed before every launch
+    peak, peak_kind = _peaks()
+    m = clone(base)
+    kernels = {}
+    for stage in ("lengths", "qualities", "coarsen_qualities", "refine_qualities"):
+        avg = ctypes.c_float()
+        nb = ctypes.c_double()
+        _lib.call("ohg_time_stage", m.handle, stage.encode(), 10, ctypes.byref(avg),
+                  ctypes.byref(nb))
+        kernels[stage] = {"ms": avg.value, "alg_bytes": nb.value,
+                          "gbs": nb.value / (avg.value / 1e3) / 1e9 if avg.value > 0 else None}
+    m.close()
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    achieved = kernels[dom]["gbs"]
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        t = _oracle_pass_seconds()
+        cpu = {"value": w["elements"] / t, "unit": "elements/s", "cores": 1, "kind": "port",
+               "sample": "one full adapt pass of the 64^3 shock box (1,572,864 tets) by the serial "
+                         "oracle restatement of the reference"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {k: w[k] for k in ("workload", "dim", "n", "metric", "seed",
+                                             "min_quality_allowed", "elements")} |
+                          {"l2": "flushed (256 MiB write) before every timed step",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "pass": {k: stats[k] for k in ("did_refine", "did_coarsen", "did_swap",
+                                               "nelems_out", "refine_keys", "coarsen_keys",
+                                               "swap_keys", "indset_rounds", "ms_refine",
+                                               "ms_coarsen", "ms_swap")},
+                "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "roofline": {"kernel": dom, "bound": "hbm",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "traffic": None, "algorithmic_bytes": kernels[dom]["alg_bytes"],
+                             "stages": kernels},
+                "cpu_baseline": cpu, "gpu_launches": gpu_launches, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/* omega_h_gb300: GB300 (sm_103a) implementation of the per-pass core of
+ * Omega_h::adapt() — metric edge lengths, cavity qualities for refine,
+ * coarsen and 3D edge swap, the independent-set selection and the
+ * adjacency rebuild — behind a C ABI over device pointers.
+ *
+ * Every function returns an ohg status code (OHG_OK on success); the
+ * message of the last failure on the calling thread is ohg_last_error().
+ * Arrays named *_dev are device pointers owned by the caller; sizes are in
+ * elements.  Integer formats follow the reference: LO = int32, GO = int64,
+ * Real = double, alignment codes = int8 laid out as
+ * which_down<<3 | rotation<<1 | flip (src/Omega_h_align.hpp:44-51).
+ * Calls on one context are ordered on that context's stream and return after
+ * the device work finished.
+ */
+#ifndef OHG_H
+#define OHG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  OHG_OK = 0,
+  OHG_ERR_CUDA = 1,          /* a CUDA runtime call failed */
+  OHG_ERR_BOUNDS = 2,        /* an index outside its array */
+  OHG_ERR_LOOP_TOO_BIG = 3,  /* an edge ring larger than a kernel supports */
+  OHG_ERR_NO_MATCH = 4,      /* reflect_down found no unique matching entity */
+  OHG_ERR_TIMEOUT = 5,       /* an iterative selection did not converge */
+  OHG_ERR_OOM = 6,           /* device allocation failed */
+  OHG_ERR_ADMISSION = 7,     /* request exceeds the admission budget */
+  OHG_ERR_INVALID = 8,       /* bad argument */
+  OHG_ERR_NUMERIC = 9,       /* degenerate metric eigen-decomposition */
+  OHG_ERR_TOPOLOGY = 10      /* mesh topology inconsistent with the operation */
+};
+
+typedef struct ohg_context ohg_context;
+typedef struct ohg_mesh ohg_mesh;
+
+/* The AdaptOpts fields used by one pass (src/Omega_h_adapt.hpp:50-77). */
+typedef struct ohg_adapt_opts {
+  double min_length_desired;
+  double max_length_desired;
+  double max_length_allowed;
+  double min_quality_allowed;
+  double min_quality_desired;
+  int nsliver_layers;
+} ohg_adapt_opts;
+
+typedef struct ohg_pass_stats {
+  int did_refine, did_coarsen, did_swap;
+  int nelems_in, nelems_out;
+  int refine_keys, coarsen_keys, swap_keys;
+  int indset_rounds;
+  double min_quality;
+  float ms_refine, ms_coarsen, ms_swap;
+} ohg_pass_stats;
+
+const char* ohg_last_error(void);
+
+/* ---- context: one device, one stream, one stream-ordered memory pool ---- */
+int ohg_context_create(int device, ohg_context** out);
+int ohg_context_destroy(ohg_context* ctx);
+/* number of kernels this library has launched on the context */
+int ohg_context_launches(ohg_context* ctx, unsigned long long* out);
+/* the context's cudaStream_t, for callers that order their own work on it */
+int ohg_context_stream(ohg_context* ctx, void** stream_out);
+
+/* ---- meshes ---- */
+/* build_box on the unit square/cube with n subdivisions per axis, Hilbert
+ * renumbered and classified (build_box, src/Omega_h_build.cpp:136-149) */
+int ohg_build_box(ohg_context* ctx, int dim, int n, ohg_mesh** out);
+/* seeded jitter of interior vertices (uniform +-0.15/n per axis) and an
+ * analytic metric: 0 isotropic h=0.05+0.1|x0-0.5|, 1 shock, 2 boundary
+ * layer, 3 isotropic sine */
+int ohg_mesh_apply_workload(ohg_mesh* mesh, int n, unsigned long long seed, int metric_kind);
+/* build_from_elems_and_coords (src/Omega_h_build.cpp:100-105): elements to
+ * vertices plus coordinates and metric, all device arrays copied in */
+int ohg_mesh_from_elems(ohg_context* ctx, int dim, int nverts, int nelems,
+                        const int* ev2v_dev, const double* coords_dev,
+                        const double* metric_dev, ohg_mesh** out);
+/* A mesh from its stored arrays, as an Omega_h::Mesh holds them: for each
+ * dimension d = 1..dim the downward adjacency d -> d-1 (down_dev[d], with
+ * alignment codes codes_dev[d] for d >= 2), classification per dimension,
+ * vertex coordinates and metric (Mesh::set_ents, src/Omega_h_mesh.cpp:87-95;
+ * tags "class_dim", "class_id", "coordinates", "metric").  nents[d] entities
+ * of each dimension; arrays are copied in. */
+int ohg_mesh_from_arrays(ohg_context* ctx, int dim, const int* nents,
+                         const int* const* down_dev, const signed char* const* codes_dev,
+                         const signed char* const* class_dim_dev,
+                         const int* const* class_id_dev, const double* coords_dev,
+                         const double* metric_dev, ohg_mesh** out);
+/* a device copy of a mesh's stored arrays (derived adjacencies are not copied) */
+int ohg_mesh_clone(ohg_mesh* mesh, ohg_mesh** out);
+int ohg_mesh_destroy(ohg_mesh* mesh);
+int ohg_mesh_dim(ohg_mesh* mesh, int* out);
+int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);
+/* Size in bytes of a named mesh array, then a copy of it into caller device
+ * memory.  Names: coords, metric, length, quality, ev2v_<d>, down_<d>,
+ * downcodes_<d>, class_dim_<d>, class_id_<d>, global_<d>, up_a2ab_<lo><hi>,
+ * up_ab2b_<lo><hi>, up_codes_<lo><hi>, down31, downcodes31,
+ * star_a2ab_<d>, star_ab2b_<d>, dual_a2ab, dual_ab2b (Mesh::ask_adj,
+ * src/Omega_h_mesh.cpp:347-357; tags, src/Omega_h_mesh.hpp:62-78) */
+int ohg_mesh_array_bytes(ohg_mesh* mesh, const char* name, long long* nbytes);
+int ohg_mesh_get_array(ohg_mesh* mesh, const char* name, void* dst_dev, long long capacity_bytes);
+/* replaces vertex coordinates or metric ("coords" | "metric") */
+int ohg_mesh_set_array(ohg_mesh* mesh, const char* name, const void* src_dev, long long nbytes);
+
+/* ---- the pass ---- */
+/* AdaptOpts::AdaptOpts(Int dim) defaults (src/Omega_h_adapt.cpp:52-85) */
+int ohg_adapt_opts_default(int dim, ohg_adapt_opts* out);
+/* refine_by_size -> coarsen_by_size -> swap_edges when the minimum element
+ * quality is below min_quality_desired (src/Omega_h_adapt.cpp:173-210) */
+int ohg_adapt_pass(ohg_mesh* mesh, const ohg_adapt_opts* opts, ohg_pass_stats* stats);
+/* one operator each; *did = whether the mesh changed
+ * (src/Omega_h_refine.hpp:8, src/Omega_h_coarsen.hpp:44, src/Omega_h_swap.hpp:14) */
+int ohg_refine_by_size(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
+int ohg_coarsen_by_size(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
+int ohg_swap_edges(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
+
+/* ---- stage kernels on a mesh ---- */
+/* measure_edges_metric (src/Omega_h_shape.cpp:28-44); a2e_dev NULL = all */
+int ohg_measure_edges_metric(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
+/* measure_qualities (src/Omega_h_quality.cpp:25-44); a2e_dev NULL = all */
+int ohg_measure_qualities(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
+/* get_mident_metrics for edges (src/Omega_h_metric.cpp:73-101): 6 per edge */
+int ohg_get_mident_metrics(ohg_mesh* mesh, const int* edges_dev, int n, double* out_dev);
+/* refine_qualities (src/Omega_h_refine_qualities.cpp:88-107) */
+int ohg_refine_qualities(ohg_mesh* mesh, const int* cands2edges_dev, int n, double* out_dev);
+/* check_collapse_class / check_collapse_exposure (src/Omega_h_collapse.hpp:30-33) */
+int ohg_check_collapse_class(ohg_mesh* mesh, const int* cands2edges_dev, int n,
+                             const signed char* codes_dev, signed char* out_dev);
+int ohg_check_collapse_exposure(ohg_mesh* mesh, const int* cands2edges_dev, int n,
+                                const signed char* codes_dev, signed char* out_dev);
+/* prevent_coarsen_overshoot (src/Omega_h_coarsen.hpp:20-21) */
+int ohg_prevent_coarsen_overshoot(ohg_mesh* mesh, double max_length, const int* cands2edges_dev,
+                                  int n, const signed char* codes_dev, signed char* out_dev);
+/* coarsen_qualities (src/Omega_h_coarsen.hpp:15): 2 per candidate, -1 where
+ * that direction does not collapse */
+int ohg_coarsen_qualities(ohg_mesh* mesh, const int* cands2edges_dev, int n,
+                          const signed char* codes_dev, double* out2_dev);
+/* choose_rails (src/Omega_h_coarsen.hpp:24-26): per-vertex outputs */
+int ohg_choose_rails(ohg_mesh* mesh, const int* cands2edges_dev, int n,
+                     const signed char* codes_dev, const double* quals2_dev,
+                     signed char* vert_cands_dev, double* vert_quals_dev,
+                     long long* vert_rails_dev);
+/* mark_sliver_layers (src/Omega_h_mark.hpp:23) */
+int ohg_mark_sliver_layers(ohg_mesh* mesh, double qual_ceil, int nlayers, signed char* out_dev);
+/* swap3d_qualities (src/Omega_h_swap3d.hpp:9-10) */
+int ohg_swap3d_qualities(ohg_mesh* mesh, double max_length_allowed, const int* cands2edges_dev,
+                         int n, double* quals_dev, signed char* configs_dev);
+/* find_indset over the mesh's star graph (src/Omega_h_indset.hpp:11-14) */
+int ohg_find_indset(ohg_mesh* mesh, int ent_dim, const double* quality_dev,
+                    const signed char* candidates_dev, signed char* out_dev, int* rounds);
+
+/* Times one stage kernel alone on this mesh: "lengths" (all edges),
+ * "qualities" (all elements), "refine_qualities" (every edge a candidate),
+ * "coarsen_qualities" (every edge, both directions).  Each of reps launches
+ * is bracketed by CUDA events on the context stream after a 256 MiB write
+ * that evicts L2; *avg_ms is the mean launch time and *alg_bytes the
+ * compulsory bytes of one launch (each input array read once, each output
+ * written once).  A measurement hook with no counterpart in the reference. */
+int ohg_time_stage(ohg_mesh* mesh, const char* stage, int reps, float* avg_ms, double* alg_bytes);
+
+/* ---- graph-level kernels (no mesh) ---- */
+/* invert_adj (src/Omega_h_adj.cpp:231-263): outputs nlows+1, nhigh*k, nhigh*k */
+int ohg_invert_adj(ohg_context* ctx, const int* hl2l_dev, const signed char* codes_dev,
+                   int nhigh, int nlows_per_high, int nlows, int* a2ab_dev, int* ab2b_dev,
+                   signed char* codes_out_dev);
+/* reflect_down (src/Omega_h_adj.cpp:424-441) given the low entities' vertices
+ * and the vertex-to-low upward adjacency; outputs nhigh*nlows_per_high */
+int ohg_reflect_down(ohg_context* ctx, const int* hv2v_dev, int nhigh, int high_dim,
+                     int low_dim, const int* lv2v_dev, int nlows, const int* v2l_a2ab_dev,
+                     const int* v2l_ab2b_dev, const signed char* v2l_codes_dev, int nverts,
+                     int* hl2l_dev, signed char* codes_out_dev);
+/* find_indset on an explicit graph (src/Omega_h_indset.cpp:17-34), entity
+ * numbers as global numbers */
+int ohg_find_indset_graph(ohg_context* ctx, int n, const int* xadj_dev, const int* adj_dev,
+                          const double* quality_dev, const signed char* candidates_dev,
+                          signed char* out_dev, int* rounds);
+/* sort_by_keys (src/Omega_h_sort.cpp:71-92): stable lexicographic sort of n
+ * tuples of width int32 (key_bytes 4) or int64 (key_bytes 8) keys */
+int ohg_sort_by_keys(ohg_context* ctx, const void* keys_dev, int n, int width, int key_bytes,
+                     int* perm_dev);
+/* hilbert::sort_coords (src/Omega_h_hilbert.cpp:52-55) */
+int ohg_hilbert_sort(ohg_context* ctx, const double* coords_dev, int n, int dim, int* perm_dev);
+/* offset_scan (src/Omega_h_int_scan.cpp:10-20): n+1 outputs */
+int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,51 @@
+// The per-pass adapt operators on a device-resident mesh.
+#pragma once
+#include "ohg_mesh.cuh"
+
+namespace ohg {
+
+struct AdaptOpts {
+  double min_length_desired, max_length_desired, max_length_allowed;
+  double min_quality_allowed, min_quality_desired;
+  int nsliver_layers = 4;
+  explicit AdaptOpts(int dim);  // src/Omega_h_adapt.cpp:52-85
+};
+
+struct PassStats {
+  int did_refine = 0, did_coarsen = 0, did_swap = 0;
+  LO nelems_in = 0, nelems_out = 0;
+  LO refine_keys = 0, coarsen_keys = 0, swap_keys = 0;
+  int indset_rounds = 0;
+  double min_quality = 0;
+  float ms_refine = 0, ms_coarsen = 0, ms_swap = 0;
+};
+
+// independent set over a conflict graph (src/Omega_h_indset.cpp,
+// src/Omega_h_indset_inline.hpp); quality ties broken by entity number,
+// which is the global number on one device
+Arr<I8> find_indset(const Adj& graph, LO n, const Arr<double>& quality, const Arr<I8>& cands,
+                    int* rounds);
+Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& quality, const Arr<I8>& cands,
+                    int* rounds = nullptr);
+
+// stage kernels (each fills caller memory of the stated size)
+void refine_qualities(Mesh& m, const LO* cands2edges, LO n, const double* midmetrics,
+                      double* out);
+void check_collapse_class(Mesh& m, const LO* c2e, LO n, const I8* codes_in, I8* codes_out);
+void check_collapse_exposure(Mesh& m, const LO* c2e, LO n, const I8* codes_in, I8* codes_out);
+void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e, LO n,
+                               const I8* codes_in, I8* codes_out);
+void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* out2);
+void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,
+                  I8* vert_cands, double* vert_quals, GO* vert_rails);
+Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers);
+void swap3d_qualities(Mesh& m, double max_length_allowed, const LO* c2e, LO n, double* quals,
+                      I8* configs);
+
+bool refine_by_size(Mesh& m, const AdaptOpts& o, PassStats* st);
+bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st);
+bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st);
+// refine -> coarsen -> swap when min quality < min_quality_desired
+PassStats adapt_pass(Mesh& m, const AdaptOpts& o);
+
+}  // namespace ohg

@@ -1,0 +1,161 @@
+// Runtime layer of the GB300 adapt-pass library: typed, reference-counted
+// device arrays allocated stream-ordered from the device memory pool, a
+// per-context stream and device status word, and the element-wise launch
+// helper used by the bookkeeping kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace ohg {
+
+typedef std::int32_t LO;
+typedef std::int64_t GO;
+typedef std::int8_t I8;
+
+enum { VERT = 0, EDGE = 1, FACE = 2, REGION = 3 };
+
+// status bits raised by kernels into the context's device status word
+enum StatusBits : int {
+  ST_NO_MATCH = 1,      // reflect_down found no (or two) matching entities
+  ST_LOOP_TOO_BIG = 2,  // an edge ring had more tets than a kernel's bound
+  ST_BOUNDS = 4,        // an index fell outside its array
+  ST_NUMERIC = 8,       // a degenerate eigen solve or non-finite value
+  ST_TOPOLOGY = 16,     // an edge ring that does not close
+};
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+#define OHG_CUDA(call)                                                 \
+  do {                                                                 \
+    cudaError_t ohg_e_ = (call);                                       \
+    if (ohg_e_ != cudaSuccess) ::ohg::cuda_fail(ohg_e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int* d_status = nullptr;  // device status word
+  int* h_pinned = nullptr;  // pinned host scratch for small reads
+  std::uint64_t launches = 0;
+  explicit Ctx(int dev);
+  ~Ctx();
+  Ctx(const Ctx&) = delete;
+  Ctx& operator=(const Ctx&) = delete;
+  void sync();
+  // reads and clears the device status word (synchronises the stream)
+  int take_status();
+};
+
+// The calling thread's current context; library entry points set it.
+Ctx& ctx();
+void set_ctx(Ctx* c);
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  ~Buf();
+};
+
+template <class T>
+struct Arr {
+  std::shared_ptr<Buf> buf;
+  T* ptr = nullptr;
+  LO n = 0;
+  Arr() = default;
+  explicit Arr(LO count) { alloc(count); }
+  void alloc(LO count);
+  T* data() const { return ptr; }
+  LO size() const { return n; }
+  bool empty() const { return n == 0; }
+  // wraps memory owned by someone else (no free)
+  static Arr wrap(T* p, LO count) {
+    Arr a;
+    a.ptr = p;
+    a.n = count;
+    return a;
+  }
+};
+
+void* dev_alloc(size_t bytes);
+
+template <class T>
+void Arr<T>::alloc(LO count) {
+  n = count;
+  buf = std::make_shared<Buf>();
+  size_t bytes = size_t(count > 0 ? count : 1) * sizeof(T);
+  buf->p = dev_alloc(bytes);
+  buf->bytes = bytes;
+  buf->stream = ctx().stream;
+  ptr = static_cast<T*>(buf->p);
+}
+
+// ------------------------------------------------------------ launches
+constexpr int kBlock = 256;
+
+template <class F>
+__global__ void k_for(LO n, F f) {
+  LO i = LO(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) f(i);
+}
+
+template <class F>
+inline void pfor(LO n, F f) {
+  if (n <= 0) return;
+  Ctx& c = ctx();
+  k_for<<<(n + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(n, f);
+  ++c.launches;
+}
+
+// device status helper
+__device__ inline void raise_status(int* st, int bits) { atomicOr(st, bits); }
+
+// ------------------------------------------------------------ host <-> device
+template <class T>
+Arr<T> to_device(const std::vector<T>& h) {
+  Arr<T> a(LO(h.size()));
+  if (!h.empty())
+    OHG_CUDA(cudaMemcpyAsync(a.data(), h.data(), h.size() * sizeof(T),
+                             cudaMemcpyHostToDevice, ctx().stream));
+  return a;
+}
+template <class T>
+std::vector<T> to_host(const Arr<T>& a) {
+  std::vector<T> h(size_t(a.size()));
+  if (a.size())
+    OHG_CUDA(cudaMemcpyAsync(h.data(), a.data(), h.size() * sizeof(T),
+                             cudaMemcpyDeviceToHost, ctx().stream));
+  ctx().sync();
+  return h;
+}
+// one element read (synchronises)
+template <class T>
+T get_elem(const Arr<T>& a, LO i) {
+  T v;
+  OHG_CUDA(cudaMemcpyAsync(&v, a.data() + i, sizeof(T), cudaMemcpyDeviceToHost,
+                           ctx().stream));
+  ctx().sync();
+  return v;
+}
+template <class T>
+Arr<T> copy_arr(const Arr<T>& a) {
+  Arr<T> b(a.size());
+  if (a.size())
+    OHG_CUDA(cudaMemcpyAsync(b.data(), a.data(), size_t(a.size()) * sizeof(T),
+                             cudaMemcpyDeviceToDevice, ctx().stream));
+  return b;
+}
+
+}  // namespace ohg

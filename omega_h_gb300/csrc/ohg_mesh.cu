@@ -1,0 +1,805 @@
+// Adjacency derivation, box construction, Hilbert renumbering, box
+// classification and the measurement kernels.
+#include <cfloat>
+
+#include "ohg_math.cuh"
+#include "ohg_mesh.cuh"
+#include "ohg_workload.hpp"
+
+namespace ohg {
+
+// ------------------------------------------------------------ invert_adj
+// Upward adjacency from a downward one (src/Omega_h_adj.cpp:231-263).
+// Degrees by atomics, offsets by scan, slots by atomics, then each row is
+// insertion-sorted by the high entity's use index so rows list high entities
+// in increasing order, the order the reference obtains with
+// sort_by_high_index.
+Adj invert_adj(const Adj& down, int k, LO nlows) {
+  LO nhl = down.ab2b.size();
+  Arr<LO> deg = fill<LO>(nlows, 0);
+  const LO* hl2l = down.ab2b.data();
+  LO* dg = deg.data();
+  pfor(nhl, [=] __device__(LO hl) { atomicAdd(&dg[hl2l[hl]], 1); });
+  Adj up;
+  up.a2ab = offset_scan(deg);
+  up.has_a2ab = true;
+  up.ab2b = Arr<LO>(nhl);
+  up.codes = Arr<I8>(nhl);
+  up.has_codes = true;
+  Arr<LO> pos = fill<LO>(nlows, 0);
+  const LO* off = up.a2ab.data();
+  LO* ps = pos.data();
+  LO* lh2hl = up.ab2b.data();
+  pfor(nhl, [=] __device__(LO hl) {
+    LO l = hl2l[hl];
+    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl;
+  });
+  const I8* dc = down.has_codes ? down.codes.data() : nullptr;
+  I8* codes = up.codes.data();
+  pfor(nlows, [=] __device__(LO l) {
+    LO b = off[l], e = off[l + 1];
+    for (LO j = b + 1; j < e; ++j) {
+      LO x = lh2hl[j];
+      LO i = j - 1;
+      while (i >= b && lh2hl[i] > x) {
+        lh2hl[i + 1] = lh2hl[i];
+        --i;
+      }
+      lh2hl[i + 1] = x;
+    }
+    for (LO j = b; j < e; ++j) {
+      LO hl = lh2hl[j];
+      int wd = hl % k;
+      if (dc) {
+        I8 c = dc[hl];
+        codes[j] = make_code(code_is_flipped(c), code_rotation(c), wd);
+      } else {
+        codes[j] = make_code(false, 0, wd);
+      }
+      lh2hl[j] = hl / k;
+    }
+  });
+  return up;
+}
+
+Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
+  int nvh = hd + 1, nvl = ld + 1, nlh = simplex_degree(hd, ld);
+  Arr<LO> uv2v(nh * nlh * nvl);
+  const LO* h = hv2v.data();
+  LO* u = uv2v.data();
+  pfor(nh * nlh, [=] __device__(LO hu) {
+    LO hh = hu / nlh;
+    int uu = hu % nlh;
+    for (int uv = 0; uv < nvl; ++uv) u[hu * nvl + uv] = h[hh * nvh + down_template(hd, ld, uu, uv)];
+  });
+  return uv2v;
+}
+
+// reflect_down / find_matches (src/Omega_h_adj.cpp:297-441): one thread per
+// use scans the upward list of the use's first vertex
+Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld) {
+  int nvh = hd + 1, nlh = simplex_degree(hd, ld), deg = ld + 1;
+  LO na = nh * nlh;
+  Adj out;
+  out.ab2b = Arr<LO>(na);
+  if (ld > 0) {
+    out.codes = Arr<I8>(na);
+    out.has_codes = true;
+  }
+  const LO* h = hv2v.data();
+  const LO* lv = lv2v.data();
+  const LO* va = v2l.a2ab.data();
+  const LO* vb = v2l.ab2b.data();
+  const I8* vc = v2l.codes.data();
+  LO* o = out.ab2b.data();
+  I8* oc = ld > 0 ? out.codes.data() : nullptr;
+  int* st = ctx().d_status;
+  pfor(na, [=] __device__(LO a) {
+    LO hh = a / nlh;
+    int uu = a % nlh;
+    LO av[3];
+    for (int j = 0; j < deg; ++j) av[j] = h[hh * nvh + down_template(hd, ld, uu, j)];
+    LO fv = av[0];
+    int found = 0;
+    for (LO x = va[fv]; x < va[fv + 1]; ++x) {
+      LO b = vb[x];
+      int wd = code_which_down(vc[x]);
+      const LO* bv = lv + LO(b) * deg;
+      I8 mc = 0;
+      bool match = false;
+      if (deg == 2) {
+        if (av[1] == bv[1 - wd]) {
+          mc = make_code(false, wd, 0);
+          match = true;
+        }
+      } else {
+        if (av[1] == bv[(wd + 1) % 3] && av[2] == bv[(wd + 2) % 3]) {
+          mc = make_code(false, rotation_to_first(3, wd), 0);
+          match = true;
+        } else if (av[1] == bv[(wd + 2) % 3] && av[2] == bv[(wd + 1) % 3]) {
+          mc = make_code(true, rotation_to_first(3, wd), 0);
+          match = true;
+        }
+      }
+      if (match) {
+        ++found;
+        o[a] = b;
+        if (oc) oc[a] = mc;
+      }
+    }
+    if (found != 1) {
+      raise_status(st, ST_NO_MATCH);
+      if (!found) o[a] = 0;
+    }
+  });
+  return out;
+}
+
+// transit (src/Omega_h_adj.cpp:443-510)
+Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh) {
+  int md = ld + 1;
+  int nmh = simplex_degree(hd, md), nlm = simplex_degree(md, ld), nlh = simplex_degree(hd, ld);
+  Adj out;
+  out.ab2b = Arr<LO>(nh * nlh);
+  if (ld == 1) {
+    out.codes = Arr<I8>(nh * nlh);
+    out.has_codes = true;
+  }
+  const LO* hm = h2m.ab2b.data();
+  const I8* hmc = h2m.codes.data();
+  const LO* ml = m2l.ab2b.data();
+  const I8* mlc = ld == 1 ? m2l.codes.data() : nullptr;
+  LO* o = out.ab2b.data();
+  I8* oc = ld == 1 ? out.codes.data() : nullptr;
+  pfor(nh * nlh, [=] __device__(LO x) {
+    LO h = x / nlh;
+    int hl = x % nlh;
+    UpTemplate ut = up_template0(hd, ld, hl);
+    LO m = hm[h * nmh + ut.up];
+    I8 hm2m = invert_alignment(nlm, hmc[h * nmh + ut.up]);
+    int mli = align_index(nlm, ld, ut.which_down, hm2m);
+    o[x] = ml[m * nlm + mli];
+    if (oc) {
+      bool f = code_is_flipped(hm2m) ^ (code_rotation(mlc[m * nlm + mli]) == 1) ^ ut.is_flipped;
+      oc[x] = make_code(false, f, 0);
+    }
+  });
+  return out;
+}
+
+// ------------------------------------------------------------ stars, dual
+static Adj verts_across_edges(const Adj& e2v, const Adj& v2e) {
+  Adj g;
+  g.a2ab = v2e.a2ab;
+  g.has_a2ab = true;
+  g.ab2b = Arr<LO>(v2e.ab2b.size());
+  const LO* ev = e2v.ab2b.data();
+  const LO* ve = v2e.ab2b.data();
+  const I8* vc = v2e.codes.data();
+  LO* o = g.ab2b.data();
+  pfor(v2e.ab2b.size(), [=] __device__(LO x) {
+    o[x] = ev[LO(ve[x]) * 2 + (1 - code_which_down(vc[x]))];
+  });
+  return g;
+}
+static Adj edges_across_tris(const Adj& f2e, const Adj& e2f, LO ne) {
+  Adj g;
+  Arr<LO> deg(ne);
+  const LO* ea = e2f.a2ab.data();
+  LO* dg = deg.data();
+  pfor(ne, [=] __device__(LO e) { dg[e] = 2 * (ea[e + 1] - ea[e]); });
+  g.a2ab = offset_scan(deg);
+  g.has_a2ab = true;
+  g.ab2b = Arr<LO>(last(g.a2ab));
+  const LO* ga = g.a2ab.data();
+  const LO* ef = e2f.ab2b.data();
+  const I8* efc = e2f.codes.data();
+  const LO* fe = f2e.ab2b.data();
+  LO* o = g.ab2b.data();
+  pfor(ne, [=] __device__(LO e) {
+    LO kk = ga[e];
+    for (LO x = ea[e]; x < ea[e + 1]; ++x) {
+      LO f = ef[x];
+      int ffe = code_which_down(efc[x]);
+      o[kk++] = fe[f * 3 + (ffe + 1) % 3];
+      o[kk++] = fe[f * 3 + (ffe + 2) % 3];
+    }
+  });
+  return g;
+}
+static Adj edges_across_tets(const Adj& r2e, const Adj& e2r) {
+  Adj g;
+  g.a2ab = e2r.a2ab;
+  g.has_a2ab = true;
+  g.ab2b = Arr<LO>(e2r.ab2b.size());
+  const LO* er = e2r.ab2b.data();
+  const I8* erc = e2r.codes.data();
+  const LO* re = r2e.ab2b.data();
+  LO* o = g.ab2b.data();
+  pfor(e2r.ab2b.size(), [=] __device__(LO x) {
+    o[x] = re[LO(er[x]) * 6 + opposite_template(3, 1, code_which_down(erc[x]))];
+  });
+  return g;
+}
+static Adj add_edges(const Adj& g1, const Adj& g2, LO nv) {
+  Adj g;
+  Arr<LO> deg(nv);
+  const LO* a1 = g1.a2ab.data();
+  const LO* a2 = g2.a2ab.data();
+  LO* dg = deg.data();
+  pfor(nv, [=] __device__(LO v) { dg[v] = (a1[v + 1] - a1[v]) + (a2[v + 1] - a2[v]); });
+  g.a2ab = offset_scan(deg);
+  g.has_a2ab = true;
+  g.ab2b = Arr<LO>(last(g.a2ab));
+  const LO* ga = g.a2ab.data();
+  const LO* b1 = g1.ab2b.data();
+  const LO* b2 = g2.ab2b.data();
+  LO* o = g.ab2b.data();
+  pfor(nv, [=] __device__(LO v) {
+    LO kk = ga[v];
+    for (LO j = a1[v]; j < a1[v + 1]; ++j) o[kk++] = b1[j];
+    for (LO j = a2[v]; j < a2[v + 1]; ++j) o[kk++] = b2[j];
+  });
+  return g;
+}
+static Adj elements_across_sides(int dim, const Adj& e2s, const Adj& s2e, LO ne) {
+  int nse = dim + 1;
+  const LO* es = e2s.ab2b.data();
+  const LO* sa = s2e.a2ab.data();
+  const LO* sb = s2e.ab2b.data();
+  Arr<LO> deg(ne);
+  LO* dg = deg.data();
+  pfor(ne, [=] __device__(LO e) {
+    int n = 0;
+    for (int k = 0; k < nse; ++k) {
+      LO s = es[e * nse + k];
+      if (sa[s + 1] - sa[s] >= 2) ++n;
+    }
+    dg[e] = n;
+  });
+  Adj g;
+  g.a2ab = offset_scan(deg);
+  g.has_a2ab = true;
+  g.ab2b = Arr<LO>(last(g.a2ab));
+  const LO* ga = g.a2ab.data();
+  LO* o = g.ab2b.data();
+  pfor(ne, [=] __device__(LO e) {
+    LO kk = ga[e];
+    for (int k = 0; k < nse; ++k) {
+      LO s = es[e * nse + k];
+      if (sa[s + 1] - sa[s] >= 2) {
+        LO x = sa[s];
+        if (sb[x] == e) ++x;
+        o[kk++] = sb[x];
+      }
+    }
+  });
+  return g;
+}
+
+void Mesh::set_ents(int d, Adj down) {
+  nents[d] = down.ab2b.size() / simplex_degree(d, d - 1);
+  adj[{d, d - 1}] = std::move(down);
+}
+
+void Mesh::drop_cache() {
+  for (auto it = adj.begin(); it != adj.end();) {
+    if (it->first.second == it->first.first - 1)
+      ++it;
+    else
+      it = adj.erase(it);
+  }
+}
+
+// Mesh::derive_adj (src/Omega_h_mesh.cpp:307-345)
+const Adj& Mesh::ask_adj(int from, int to) {
+  auto it = adj.find({from, to});
+  if (it != adj.end()) return it->second;
+  Adj d;
+  if (from < to) {
+    d = invert_adj(ask_adj(to, from), simplex_degree(to, from), nents[from]);
+  } else if (to < from) {
+    const Adj& h2m = ask_adj(from, to + 1);
+    const Adj& m2l = ask_adj(to + 1, to);
+    d = transit(h2m, m2l, from, to, nents[from]);
+  } else if (from == dim) {
+    d = elements_across_sides(dim, ask_adj(dim, dim - 1), ask_adj(dim - 1, dim), nents[dim]);
+  } else if (from == VERT) {
+    d = verts_across_edges(ask_adj(EDGE, VERT), ask_adj(VERT, EDGE));
+  } else {
+    d = edges_across_tris(ask_adj(FACE, EDGE), ask_adj(EDGE, FACE), nents[EDGE]);
+    if (dim == 3) {
+      Adj t = edges_across_tets(ask_adj(REGION, EDGE), ask_adj(EDGE, REGION));
+      d = add_edges(d, t, nents[EDGE]);
+    }
+  }
+  return adj[{from, to}] = std::move(d);
+}
+
+// ------------------------------------------------------------ find_unique
+// (src/Omega_h_adj.cpp:68-153): canonical rotation of each use, stable
+// lexicographic sort, keep the last use of each run in its own orientation
+Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
+  Arr<LO> uv2v = form_uses(hv2v, nh, hd, ld);
+  int deg = ld + 1;
+  LO nu = uv2v.size() / deg;
+  Arr<LO> canon(uv2v.size());
+  const LO* u = uv2v.data();
+  LO* cn = canon.data();
+  pfor(nu, [=] __device__(LO x) {
+    const LO* in = u + x * deg;
+    int min_j = 0;
+    LO min_v = in[0];
+    for (int j = 1; j < deg; ++j)
+      if (in[j] < min_v) {
+        min_j = j;
+        min_v = in[j];
+      }
+    int rot = rotation_to_first(deg, min_j);
+    LO tmp[3];
+    for (int j = 0; j < deg; ++j) tmp[rotate_index(deg, j, rot)] = in[j];
+    if (deg == 3 && tmp[2] < tmp[1]) {
+      LO t = tmp[1];
+      tmp[1] = tmp[2];
+      tmp[2] = t;
+    }
+    for (int j = 0; j < deg; ++j) cn[x * deg + j] = tmp[j];
+  });
+  Arr<LO> s2u = sort_by_keys(canon, deg);
+  Arr<I8> jumps(nu);
+  const LO* s = s2u.data();
+  I8* jp = jumps.data();
+  pfor(nu, [=] __device__(LO i) {
+    if (i == nu - 1) {
+      jp[i] = 1;
+      return;
+    }
+    LO e0 = s[i], e1 = s[i + 1];
+    I8 j = 0;
+    for (int k = 0; k < deg; ++k)
+      if (cn[e0 * deg + k] != cn[e1 * deg + k]) j = 1;
+    jp[i] = j;
+  });
+  Arr<LO> e2s = collect_marked(jumps);
+  LO ne = e2s.size();
+  Arr<LO> out(ne * deg);
+  const LO* es = e2s.data();
+  LO* o = out.data();
+  pfor(ne, [=] __device__(LO e) {
+    LO uu = s[es[e]];
+    for (int k = 0; k < deg; ++k) o[e * deg + k] = u[uu * deg + k];
+  });
+  return out;
+}
+
+// ------------------------------------------------------------ box
+// tets_from_hexes (Dompierre et al. case analysis, src/Omega_h_simplify.cpp:20-230)
+__device__ __forceinline__ void hex_rot_fwd(LO* v, int n) {
+  // the reference's in-place rotation: every slot copies its predecessor's
+  // already updated value
+  LO tmp = v[n - 1];
+  for (int i = 0; i < n - 1; ++i) v[i + 1] = v[i];
+  v[0] = tmp;
+}
+__device__ int hex_case(const LO* hv, LO* hh) {
+  for (int i = 0; i < 8; ++i) hh[i] = hv[i];
+  int min_i = 0;
+  for (int i = 1; i < 8; ++i)
+    if (hh[i] < hh[min_i]) min_i = i;
+  int r = (4 - (min_i % 4)) % 4;
+  for (int t = 0; t < r; ++t) hex_rot_fwd(hh, 4);
+  for (int t = 0; t < r; ++t) hex_rot_fwd(hh + 4, 4);
+  if (min_i >= 4) {
+    const int fp[4][2] = {{0, 4}, {3, 5}, {1, 7}, {2, 6}};
+    for (int i = 0; i < 4; ++i) {
+      LO t = hh[fp[i][0]];
+      hh[fp[i][0]] = hh[fp[i][1]];
+      hh[fp[i][1]] = t;
+    }
+  }
+  const int bf[3][4] = {{6, 5, 1, 2}, {6, 2, 3, 7}, {6, 7, 4, 5}};
+  int di[3];
+  for (int i = 0; i < 3; ++i) {
+    LO a = min(hh[bf[i][0]], hh[bf[i][2]]), b = min(hh[bf[i][1]], hh[bf[i][3]]);
+    di[i] = a < b;
+  }
+  int nd = di[0] + di[1] + di[2];
+  int face = -1;
+  if (nd == 1)
+    for (int i = 0; i < 3; ++i)
+      if (di[i]) face = i;
+  if (nd == 2)
+    for (int i = 0; i < 3; ++i)
+      if (!di[i]) face = i;
+  if (face >= 0) {
+    const int ring[6] = {1, 2, 3, 7, 5, 4};
+    LO tmp[6];
+    for (int i = 0; i < 6; ++i) tmp[i] = hh[ring[i]];
+    int nt = ((3 - face) % 3) * 2;
+    for (int t = 0; t < nt; ++t) hex_rot_fwd(tmp, 6);
+    for (int i = 0; i < 6; ++i) hh[ring[i]] = tmp[i];
+  }
+  return nd;
+}
+__constant__ int c_hex_tmpl[4][6][4] = {
+    {{0, 1, 2, 5}, {0, 2, 7, 5}, {0, 2, 3, 7}, {0, 5, 7, 4}, {2, 7, 5, 6}, {0, 0, 0, 0}},
+    {{0, 5, 7, 4}, {0, 1, 7, 5}, {1, 6, 7, 5}, {0, 7, 2, 3}, {0, 7, 1, 2}, {1, 7, 6, 2}},
+    {{0, 4, 5, 6}, {0, 3, 7, 6}, {0, 7, 4, 6}, {0, 1, 2, 5}, {0, 3, 6, 2}, {0, 6, 5, 2}},
+    {{0, 2, 3, 6}, {0, 3, 7, 6}, {0, 7, 4, 6}, {0, 5, 6, 4}, {1, 5, 6, 0}, {1, 6, 2, 0}}};
+
+static Arr<LO> box_elems(int dim, int n, Arr<double>* coords) {
+  if (dim == 3) {
+    LO nvx = n + 1, nvxy = nvx * nvx, nv = nvxy * nvx, nxy = n * n, nh = nxy * n;
+    double dx = 1.0 / n;
+    *coords = Arr<double>(nv * 3);
+    double* c = coords->data();
+    pfor(nv, [=] __device__(LO v) {
+      LO ij = v % nvxy, k = v / nvxy, i = ij % nvx, j = ij / nvx;
+      c[v * 3 + 0] = i * dx;
+      c[v * 3 + 1] = j * dx;
+      c[v * 3 + 2] = k * dx;
+    });
+    Arr<LO> hv(nh * 8);
+    LO* h = hv.data();
+    pfor(nh, [=] __device__(LO x) {
+      LO ij = x % nxy, k = x / nxy, i = ij % n, j = ij / n;
+      LO* o = h + x * 8;
+      o[0] = (k + 0) * nvxy + (j + 0) * nvx + (i + 0);
+      o[1] = (k + 0) * nvxy + (j + 0) * nvx + (i + 1);
+      o[2] = (k + 0) * nvxy + (j + 1) * nvx + (i + 1);
+      o[3] = (k + 0) * nvxy + (j + 1) * nvx + (i + 0);
+      o[4] = (k + 1) * nvxy + (j + 0) * nvx + (i + 0);
+      o[5] = (k + 1) * nvxy + (j + 0) * nvx + (i + 1);
+      o[6] = (k + 1) * nvxy + (j + 1) * nvx + (i + 1);
+      o[7] = (k + 1) * nvxy + (j + 1) * nvx + (i + 0);
+    });
+    Arr<LO> cnt(nh);
+    LO* ct = cnt.data();
+    pfor(nh, [=] __device__(LO x) {
+      LO hh[8];
+      ct[x] = hex_case(h + x * 8, hh) == 0 ? 5 : 6;
+    });
+    Arr<LO> off = offset_scan(cnt);
+    Arr<LO> tv(last(off) * 4);
+    const LO* of = off.data();
+    LO* t = tv.data();
+    pfor(nh, [=] __device__(LO x) {
+      LO hh[8];
+      int nd = hex_case(h + x * 8, hh);
+      int nt = nd == 0 ? 5 : 6;
+      for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < 4; ++j) t[(of[x] + i) * 4 + j] = hh[c_hex_tmpl[nd][i][j]];
+    });
+    return tv;
+  }
+  LO nvx = n + 1, nv = nvx * nvx, nq = n * n;
+  double dx = 1.0 / n;
+  *coords = Arr<double>(nv * 2);
+  double* c = coords->data();
+  pfor(nv, [=] __device__(LO v) {
+    c[v * 2 + 0] = (v % nvx) * dx;
+    c[v * 2 + 1] = (v / nvx) * dx;
+  });
+  Arr<LO> tv(nq * 6);
+  LO* t = tv.data();
+  pfor(nq, [=] __device__(LO q) {
+    LO i = q % n, j = q / n;
+    // the minimum vertex of a box quad is already first: no rotation
+    LO qq[4] = {(j + 0) * nvx + (i + 0), (j + 0) * nvx + (i + 1), (j + 1) * nvx + (i + 1),
+                (j + 1) * nvx + (i + 0)};
+    const int qt[2][3] = {{0, 1, 2}, {2, 3, 0}};
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 3; ++b) t[(q * 2 + a) * 3 + b] = qq[qt[a][b]];
+  });
+  return tv;
+}
+
+static void add_ents2verts(Mesh& m, int d, const Arr<LO>& ev2v, LO ne) {
+  if (d == 1) {
+    Adj a;
+    a.ab2b = ev2v;
+    m.set_ents(1, std::move(a));
+  } else {
+    const Arr<LO>& lv2v = m.ask_verts_of(d - 1);
+    const Adj& v2l = m.ask_up(0, d - 1);
+    m.set_ents(d, reflect_down(ev2v, ne, lv2v, v2l, d, d - 1));
+  }
+}
+
+Mesh build_box(int dim, int n) {
+  Arr<double> coords;
+  Arr<LO> ev2v = box_elems(dim, n, &coords);
+  Mesh m;
+  m.dim = dim;
+  m.nents[0] = coords.size() / dim;
+  LO nel = ev2v.size() / (dim + 1);
+  for (int md = 1; md < dim; ++md) {
+    Arr<LO> mv = find_unique(ev2v, nel, dim, md);
+    add_ents2verts(m, md, mv, mv.size() / (md + 1));
+  }
+  add_ents2verts(m, dim, ev2v, nel);
+  m.coords = coords;
+  reorder_by_hilbert(m);
+  classify_box(m, n);
+  return m;
+}
+
+// ------------------------------------------------------------ Hilbert
+// Skilling, "Programming the Hilbert curve" (AIP Conf. Proc. 707, 2004):
+// axes -> transpose form, then bit-interleave into dim 64-bit keys
+__device__ void hilbert_axes_to_transpose(std::uint64_t* X, int b, int n) {
+  std::uint64_t M = std::uint64_t(1) << (b - 1), P, Q, t;
+  for (Q = M; Q > 1; Q >>= 1) {
+    P = Q - 1;
+    for (int i = 0; i < n; i++) {
+      if (X[i] & Q)
+        X[0] ^= P;
+      else {
+        t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  for (int i = 1; i < n; i++) X[i] ^= X[i - 1];
+  t = 0;
+  for (Q = M; Q > 1; Q >>= 1)
+    if (X[n - 1] & Q) t ^= Q - 1;
+  for (int i = 0; i < n; i++) X[i] ^= t;
+}
+
+Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim) {
+  double mn[3], mx[3];
+  for (int j = 0; j < dim; ++j) {
+    Arr<double> comp(n);
+    const double* c = coords.data();
+    double* o = comp.data();
+    pfor(n, [=] __device__(LO i) { o[i] = c[i * dim + j]; });
+    mn[j] = min_f64(comp);
+    mx[j] = max_f64(comp);
+  }
+  // bounding box made equilateral, affine map into the unit box
+  // (src/Omega_h_bbox.hpp:65-79)
+  double maxl = mx[0] - mn[0];
+  for (int j = 1; j < dim; ++j) maxl = max2d(maxl, mx[j] - mn[j]);
+  double s0 = 0, s1 = 0, s2 = 0, t0 = 0, t1 = 0, t2 = 0;
+  double s[3], t[3];
+  for (int j = 0; j < dim; ++j) {
+    double hi = mn[j] + maxl;
+    s[j] = 1.0 / (hi - mn[j]);
+    t[j] = -(s[j] * mn[j]);
+  }
+  s0 = s[0];
+  s1 = s[1];
+  t0 = t[0];
+  t1 = t[1];
+  if (dim == 3) {
+    s2 = s[2];
+    t2 = t[2];
+  }
+  Arr<GO> keys(n * dim);
+  const double* c = coords.data();
+  GO* k = keys.data();
+  pfor(n, [=] __device__(LO i) {
+    const int nbits = 52;
+    double ss[3] = {s0, s1, s2}, tt[3] = {t0, t1, t2};
+    std::uint64_t X[3], Y[3];
+    for (int j = 0; j < dim; ++j) {
+      double u = ss[j] * c[i * dim + j];
+      u = u + tt[j];
+      double z = min2d(max2d(u, 0.0), 1.0) * 4503599627370496.0;  // 2^52
+      X[j] = std::uint64_t(z);
+      if (X[j] >= (std::uint64_t(1) << nbits)) X[j] = (std::uint64_t(1) << nbits) - 1;
+    }
+    hilbert_axes_to_transpose(X, nbits, dim);
+    for (int j = 0; j < dim; ++j) Y[j] = 0;
+    for (int b = 0; b < nbits * dim; ++b)
+      Y[b / nbits] |= (((X[b % dim] >> (nbits - 1 - (b / dim))) & 1) << (nbits - 1 - (b % nbits)));
+    for (int j = 0; j < dim; ++j) k[i * dim + j] = GO(Y[j]);
+  });
+  return keys;
+}
+Arr<LO> hilbert_sort(const Arr<double>& coords, LO n, int dim) {
+  return sort_by_keys64(hilbert_keys(coords, n, dim), dim);
+}
+
+// reorder_by_hilbert + unmap_mesh (src/Omega_h_reorder.cpp:19-64,
+// src/Omega_h_unmap_mesh.cpp:108-136): vertices in Hilbert order, every other
+// entity ordered by its first vertex's new number, then by old number
+void reorder_by_hilbert(Mesh& m) {
+  int dim = m.dim;
+  LO nv = m.nverts();
+  Arr<LO> new2old[4];
+  new2old[0] = hilbert_sort(m.coords, nv, dim);
+  Arr<LO> old2new_v(nv);
+  {
+    const LO* p = new2old[0].data();
+    LO* o = old2new_v.data();
+    pfor(nv, [=] __device__(LO i) { o[p[i]] = i; });
+  }
+  for (int d = 1; d <= dim; ++d) {
+    const Arr<LO>& ev2v = m.ask_verts_of(d);
+    int deg = d + 1;
+    LO ne = m.nents[d];
+    // key = new number of the first vertex; stable sort keeps old order
+    Arr<LO> key(ne);
+    const LO* ev = ev2v.data();
+    const LO* o2n = old2new_v.data();
+    LO* kk = key.data();
+    pfor(ne, [=] __device__(LO e) { kk[e] = o2n[ev[e * deg]]; });
+    new2old[d] = sort_by_keys(key, 1);
+  }
+  Mesh nm;
+  nm.dim = dim;
+  nm.nents[0] = nv;
+  nm.coords = unmap(new2old[0], m.coords, dim);
+  Arr<LO> old2new_low = old2new_v;
+  for (int d = 1; d <= dim; ++d) {
+    const Adj& od = m.ask_down(d, d - 1);
+    int deg = simplex_degree(d, d - 1);
+    LO ne = m.nents[d];
+    Adj nd;
+    nd.ab2b = unmap(new2old[d], od.ab2b, deg);
+    LO* nb = nd.ab2b.data();
+    const LO* o2n = old2new_low.data();
+    pfor(ne * deg, [=] __device__(LO x) { nb[x] = o2n[nb[x]]; });
+    if (od.has_codes) {
+      nd.codes = unmap(new2old[d], od.codes, deg);
+      nd.has_codes = true;
+    }
+    nm.set_ents(d, std::move(nd));
+    Arr<LO> o2n2(ne);
+    const LO* p = new2old[d].data();
+    LO* o = o2n2.data();
+    pfor(ne, [=] __device__(LO i) { o[p[i]] = i; });
+    old2new_low = o2n2;
+  }
+  m = std::move(nm);
+}
+
+// classify_box (src/Omega_h_box.cpp:105-160) on the unit square/cube
+void classify_box(Mesh& m, int n) {
+  int dim = m.dim;
+  double dist = 1.0 / double(n * 32);
+  for (int d = 0; d <= dim; ++d) {
+    LO ne = m.nents[d];
+    m.class_id[d] = Arr<LO>(ne);
+    m.class_dim[d] = Arr<I8>(ne);
+    const LO* ev = d ? m.ask_verts_of(d).data() : nullptr;
+    const double* c = m.coords.data();
+    LO* ci = m.class_id[d].data();
+    I8* cd = m.class_dim[d].data();
+    int deg = d + 1;
+    pfor(ne, [=] __device__(LO e) {
+      int id = 0, cdim = 0;
+      for (int j = dim - 1; j >= 0; --j) {
+        double x;
+        if (d == 0) {
+          x = c[e * dim + j];
+        } else {
+          double comp = 0;
+          for (int k = 0; k < deg; ++k) comp += c[LO(ev[e * deg + k]) * dim + j];
+          comp /= deg;
+          x = comp;
+        }
+        id *= 3;
+        if (x > (1.0 - dist)) {
+          id += 2;
+        } else if (x > dist) {
+          id += 1;
+          ++cdim;
+        }
+      }
+      ci[e] = id;
+      cd[e] = I8(cdim);
+    });
+  }
+}
+
+// seeded jitter of interior vertices and the analytic metric field (host
+// side: input construction only)
+void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
+  int dim = m.dim, mc = m.mcomp();
+  std::vector<double> c = to_host(m.coords);
+  std::vector<I8> cd = to_host(m.class_dim[0]);
+  LO nv = m.nverts();
+  for (LO v = 0; v < nv; ++v) {
+    if (cd[v] != dim) continue;
+    for (int j = 0; j < dim; ++j) c[size_t(v) * dim + j] += workload::jitter(seed, v, j, dim, n);
+  }
+  workload::MetricParams mp;
+  mp.kind = kind;
+  if (kind == workload::METRIC_SHOCK) workload::shock_normal(seed, mp.normal);
+  std::vector<double> met(size_t(nv) * mc);
+  for (LO v = 0; v < nv; ++v) workload::metric_at(mp, dim, &c[size_t(v) * dim], &met[size_t(v) * mc]);
+  m.coords = to_device(c);
+  m.metric = to_device(met);
+  m.has_length = m.has_quality = false;
+}
+
+// ------------------------------------------------------------ measurement
+// measure_edges_metric (src/Omega_h_shape.cpp:7-49): one thread per edge
+void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out) {
+  const LO* ev = m.ask_verts_of(1).data();
+  const double* c = m.coords.data();
+  const double* mt = m.metric.data();
+  int dim = m.dim, mc = m.mcomp();
+  pfor(na, [=] __device__(LO a) {
+    LO e = a2e ? a2e[a] : a;
+    LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
+    out[a] = dim == 3 ? edge_length3(c + v0 * 3, c + v1 * 3, mt + v0 * mc, mt + v1 * mc)
+                      : edge_length2(c + v0 * 2, c + v1 * 2, mt + v0 * mc, mt + v1 * mc);
+  });
+}
+
+__device__ __forceinline__ double elem_quality_dev(int dim, const double* c, const double* mt,
+                                                   const LO* v) {
+  if (dim == 3) {
+    V3 p[4];
+    M3 ms[4];
+    for (int i = 0; i < 4; ++i) {
+      for (int j = 0; j < 3; ++j) p[i].x[j] = c[LO(v[i]) * 3 + j];
+      ms[i] = symm3(mt + LO(v[i]) * 6);
+    }
+    return tet_quality(p, ms[maxdet_index3(ms, 4)]);
+  }
+  double p[3][2];
+  int best = 0;
+  double bd = det2p(mt + LO(v[0]) * 3);
+  for (int i = 0; i < 3; ++i) {
+    p[i][0] = c[LO(v[i]) * 2];
+    p[i][1] = c[LO(v[i]) * 2 + 1];
+    if (i) {
+      double d = det2p(mt + LO(v[i]) * 3);
+      if (d > bd) {
+        best = i;
+        bd = d;
+      }
+    }
+  }
+  return tri_quality(p, mt + LO(v[best]) * 3);
+}
+
+// measure_qualities (src/Omega_h_quality.cpp:7-53): one thread per element
+void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
+  int dim = m.dim;
+  const LO* ev = m.ask_verts_of(dim).data();
+  const double* c = m.coords.data();
+  const double* mt = m.metric.data();
+  pfor(na, [=] __device__(LO a) {
+    LO e = a2e ? a2e[a] : a;
+    out[a] = elem_quality_dev(dim, c, mt, ev + e * (dim + 1));
+  });
+}
+
+// get_mident_metrics (src/Omega_h_metric.cpp:56-104) for edges
+void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
+  const LO* ev = m.ask_verts_of(1).data();
+  const double* mt = m.metric.data();
+  int* st = ctx().d_status;
+  if (m.dim != 3) throw Error(8, "mident_metrics: 2D metrics are not supported yet");
+  pfor(n, [=] __device__(LO a) {
+    LO e = edges ? edges[a] : a;
+    if (!average_metric3(mt + LO(ev[e * 2]) * 6, mt + LO(ev[e * 2 + 1]) * 6, out + a * 6))
+      raise_status(st, ST_NUMERIC);
+  });
+}
+
+const Arr<double>& Mesh::ask_lengths() {
+  if (!has_length) {
+    length = Arr<double>(nedges());
+    measure_edges_metric(*this, nullptr, nedges(), length.data());
+    has_length = true;
+  }
+  return length;
+}
+const Arr<double>& Mesh::ask_qualities() {
+  if (!has_quality) {
+    quality = Arr<double>(nelems());
+    measure_qualities(*this, nullptr, nelems(), quality.data());
+    has_quality = true;
+  }
+  return quality;
+}
+
+}  // namespace ohg

@@ -1,0 +1,66 @@
+// Device-resident simplex mesh: the stored downward adjacencies, vertex
+// fields, classification and the lazily derived adjacency cache
+// (the roles of Omega_h::Mesh, src/Omega_h_mesh.hpp:36-177, and
+// src/Omega_h_mesh.cpp:307-357).
+#pragma once
+#include "ohg_prims.cuh"
+
+namespace ohg {
+
+struct Adj {
+  Arr<LO> a2ab, ab2b;
+  Arr<I8> codes;
+  bool has_a2ab = false, has_codes = false;
+};
+
+inline int simplex_degree(int from, int to) {
+  static const int t[4][4] = {{1, -1, -1, -1}, {2, 1, -1, -1}, {3, 3, 1, -1}, {4, 6, 4, 1}};
+  return t[from][to];
+}
+
+struct Mesh {
+  int dim = 3;
+  LO nents[4] = {0, 0, 0, 0};
+  Arr<double> coords;  // dim per vertex
+  Arr<double> metric;  // 6 (3D) or 3 (2D) per vertex, packed symmetric
+  Arr<I8> class_dim[4];
+  Arr<LO> class_id[4];
+  bool has_length = false, has_quality = false;
+  Arr<double> length, quality;
+  std::map<std::pair<int, int>, Adj> adj;
+
+  int mcomp() const { return dim == 3 ? 6 : 3; }
+  LO nverts() const { return nents[0]; }
+  LO nedges() const { return nents[1]; }
+  LO nelems() const { return nents[dim]; }
+  void set_ents(int d, Adj down);
+  const Adj& ask_adj(int from, int to);
+  const Adj& ask_down(int from, int to) { return ask_adj(from, to); }
+  const Adj& ask_up(int from, int to) { return ask_adj(from, to); }
+  const Arr<LO>& ask_verts_of(int d) { return ask_adj(d, 0).ab2b; }
+  const Arr<double>& ask_lengths();
+  const Arr<double>& ask_qualities();
+  void drop_cache();  // forget derived adjacencies (keeps stored down ones)
+};
+
+// adjacency derivation (src/Omega_h_adj.cpp)
+Adj invert_adj(const Adj& down, int nlows_per_high, LO nlows);
+Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld);
+Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh);
+Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld);
+Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld);
+
+// construction: box mesh, Hilbert renumbering, box classification
+Mesh build_box(int dim, int n);
+Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim);
+Arr<LO> hilbert_sort(const Arr<double>& coords, LO n, int dim);
+void reorder_by_hilbert(Mesh& m);
+void classify_box(Mesh& m, int n);
+void apply_workload(Mesh& m, int n, std::uint64_t seed, int metric_kind);
+
+// measurement kernels
+void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out);
+void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out);
+void mident_metrics(Mesh& m, const LO* edges, LO n, double* out);
+
+}  // namespace ohg

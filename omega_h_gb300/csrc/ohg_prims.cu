@@ -1,0 +1,372 @@
+// Scan, compaction, reduction and radix-sort kernels.
+#include <cfloat>
+
+#include "ohg_prims.cuh"
+
+namespace ohg {
+
+// ------------------------------------------------------------ runtime
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "CUDA error %d (%s) in %s at %s:%d", int(e),
+                cudaGetErrorString(e), what, file, line);
+  throw Error(e == cudaErrorMemoryAllocation ? 6 : 1, buf);
+}
+
+static thread_local Ctx* g_ctx = nullptr;
+Ctx& ctx() {
+  if (!g_ctx) throw Error(8, "no current ohg context");
+  return *g_ctx;
+}
+void set_ctx(Ctx* c) { g_ctx = c; }
+
+Ctx::Ctx(int dev) : device(dev) {
+  OHG_CUDA(cudaSetDevice(dev));
+  OHG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  OHG_CUDA(cudaMalloc(&d_status, sizeof(int)));
+  OHG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
+  OHG_CUDA(cudaMallocHost(&h_pinned, 64));
+  cudaMemPool_t pool;
+  OHG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  std::uint64_t thr = ~std::uint64_t(0);
+  OHG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+}
+Ctx::~Ctx() {
+  cudaStreamSynchronize(stream);
+  cudaFree(d_status);
+  cudaFreeHost(h_pinned);
+  cudaStreamDestroy(stream);
+}
+void Ctx::sync() { OHG_CUDA(cudaStreamSynchronize(stream)); }
+int Ctx::take_status() {
+  OHG_CUDA(cudaMemcpyAsync(h_pinned, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  OHG_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int), stream));
+  sync();
+  return h_pinned[0];
+}
+
+void* dev_alloc(size_t bytes) {
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, ctx().stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(6, "device allocation of " + std::to_string(bytes) + " bytes failed");
+  }
+  return p;
+}
+Buf::~Buf() {
+  if (p) cudaFreeAsync(p, stream);
+}
+
+// ------------------------------------------------------------ scan
+// Three-phase exclusive scan: tile sums, scan of tile sums, tile scans.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <class T>
+__global__ void k_tile_sums(const T* in, LO n, LO* sums) {
+  __shared__ LO warp_sums[kScanThreads / 32];
+  LO base = LO(blockIdx.x) * kScanTile;
+  LO s = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    LO i = base + k * kScanThreads + threadIdx.x;
+    if (i < n) s += LO(in[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < kScanThreads / 32 ? warp_sums[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s;
+  }
+}
+
+// single block: exclusive scan of nb tile sums in place, total into *total
+__global__ void k_scan_sums(LO* sums, LO nb, LO* total) {
+  __shared__ LO tsum[1024];
+  LO per = (nb + blockDim.x - 1) / blockDim.x;
+  LO b0 = LO(threadIdx.x) * per;
+  LO s = 0;
+  for (LO k = 0; k < per; ++k)
+    if (b0 + k < nb) s += sums[b0 + k];
+  tsum[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    LO run = 0;
+    for (unsigned t = 0; t < blockDim.x; ++t) {
+      LO v = tsum[t];
+      tsum[t] = run;
+      run += v;
+    }
+    *total = run;
+  }
+  __syncthreads();
+  LO run = tsum[threadIdx.x];
+  for (LO k = 0; k < per; ++k)
+    if (b0 + k < nb) {
+      LO v = sums[b0 + k];
+      sums[b0 + k] = run;
+      run += v;
+    }
+}
+
+template <class T>
+__global__ void k_tile_scan(const T* in, LO n, const LO* sums, LO* out, const LO* total) {
+  __shared__ LO warp_tot[kScanThreads / 32];
+  LO base = LO(blockIdx.x) * kScanTile + LO(threadIdx.x) * kScanItems;
+  LO v[kScanItems];
+  LO s = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    LO i = base + k;
+    v[k] = i < n ? LO(in[i]) : 0;
+    s += v[k];
+  }
+  // block-exclusive scan of thread sums
+  LO incl = s;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    LO y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    LO w = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
+    LO wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      LO y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+  }
+  __syncthreads();
+  LO run = sums[blockIdx.x] + warp_tot[warp] + incl - s;
+  for (int k = 0; k < kScanItems; ++k) {
+    LO i = base + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
+}
+
+template <class T>
+static void scan_impl(const T* in, LO n, LO* out) {
+  Ctx& c = ctx();
+  if (n == 0) {
+    OHG_CUDA(cudaMemsetAsync(out, 0, sizeof(LO), c.stream));
+    return;
+  }
+  LO nb = (n + kScanTile - 1) / kScanTile;
+  Arr<LO> sums(nb + 1);
+  k_tile_sums<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data());
+  k_scan_sums<<<1, 1024, 0, c.stream>>>(sums.data(), nb, sums.data() + nb);
+  k_tile_scan<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), out, sums.data() + nb);
+  c.launches += 3;
+}
+
+void offset_scan_into(const LO* counts, LO n, LO* out) { scan_impl(counts, n, out); }
+void offset_scan_into(const I8* counts, LO n, LO* out) { scan_impl(counts, n, out); }
+Arr<LO> offset_scan(const Arr<LO>& counts) {
+  Arr<LO> out(counts.size() + 1);
+  scan_impl(counts.data(), counts.size(), out.data());
+  return out;
+}
+Arr<LO> offset_scan(const Arr<I8>& counts) {
+  Arr<LO> out(counts.size() + 1);
+  scan_impl(counts.data(), counts.size(), out.data());
+  return out;
+}
+
+LO last(const Arr<LO>& a) { return get_elem(a, a.size() - 1); }
+
+Arr<LO> collect_marked(const Arr<I8>& marks) {
+  LO n = marks.size();
+  Arr<I8> nz(n);
+  const I8* m = marks.data();
+  I8* z = nz.data();
+  pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
+  Arr<LO> offs = offset_scan(nz);
+  LO cnt = last(offs);
+  Arr<LO> out(cnt);
+  const LO* o = offs.data();
+  LO* d = out.data();
+  pfor(n, [=] __device__(LO i) {
+    if (m[i]) d[o[i]] = i;
+  });
+  return out;
+}
+LO count_marked(const Arr<I8>& marks) {
+  LO n = marks.size();
+  Arr<I8> nz(n);
+  const I8* m = marks.data();
+  I8* z = nz.data();
+  pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
+  return last(offset_scan(nz));
+}
+
+// ------------------------------------------------------------ reductions
+template <class T, class Op>
+__global__ void k_reduce(const T* in, LO n, T init, Op op, T* out) {
+  __shared__ T sh[kBlock];
+  T acc = init;
+  for (LO i = LO(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += LO(gridDim.x) * blockDim.x)
+    acc = op(acc, in[i]);
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (int(threadIdx.x) < s) sh[threadIdx.x] = op(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+template <class T, class Op>
+static T reduce(const Arr<T>& a, T init, Op op) {
+  Ctx& c = ctx();
+  LO n = a.size();
+  int nb = int(std::min<LO>(1024, (n + kBlock - 1) / kBlock));
+  if (nb < 1) nb = 1;
+  Arr<T> part(nb);
+  k_reduce<<<nb, kBlock, 0, c.stream>>>(a.data(), n, init, op, part.data());
+  Arr<T> fin(1);
+  k_reduce<<<1, kBlock, 0, c.stream>>>(part.data(), LO(nb), init, op, fin.data());
+  c.launches += 2;
+  return get_elem(fin, 0);
+}
+struct MaxOp {
+  template <class T>
+  __device__ T operator()(T a, T b) const { return (a < b) ? b : a; }
+};
+struct MinOp {
+  template <class T>
+  __device__ T operator()(T a, T b) const { return (b < a) ? b : a; }
+};
+I8 max_i8(const Arr<I8>& a) { return reduce<I8>(a, I8(-128), MaxOp()); }
+LO max_lo(const Arr<LO>& a) { return reduce<LO>(a, LO(-2147483647 - 1), MaxOp()); }
+double min_f64(const Arr<double>& a) { return reduce<double>(a, DBL_MAX, MinOp()); }
+double max_f64(const Arr<double>& a) { return reduce<double>(a, -DBL_MAX, MaxOp()); }
+
+// ------------------------------------------------------------ radix sort
+// Stable LSD radix sort of (32-bit digit source, value) pairs, 4-bit digits.
+// Each block owns a tile of kRsItems consecutive items per thread; ranks
+// inside a tile come from per-thread digit counts scanned across threads, so
+// equal digits keep their input order.
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 8;
+constexpr int kRsTile = kRsThreads * kRsItems;
+constexpr int kRsBins = 16;
+
+__global__ void k_rs_hist(const std::uint32_t* keys, LO n, int shift, LO* hist, LO nb) {
+  __shared__ LO h[kRsBins];
+  if (threadIdx.x < kRsBins) h[threadIdx.x] = 0;
+  __syncthreads();
+  LO base = LO(blockIdx.x) * kRsTile + LO(threadIdx.x) * kRsItems;
+  for (int k = 0; k < kRsItems; ++k) {
+    LO i = base + k;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kRsBins - 1)], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < kRsBins) hist[LO(threadIdx.x) * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_rs_scatter(const std::uint32_t* keys, const LO* vals, LO n, int shift,
+                             const LO* offs, LO nb, std::uint32_t* okeys, LO* ovals) {
+  __shared__ LO cnt[kRsBins][kRsThreads + 1];
+  LO base = LO(blockIdx.x) * kRsTile + LO(threadIdx.x) * kRsItems;
+  LO c[kRsBins];
+  for (int d = 0; d < kRsBins; ++d) c[d] = 0;
+  for (int k = 0; k < kRsItems; ++k) {
+    LO i = base + k;
+    if (i < n) c[(keys[i] >> shift) & (kRsBins - 1)]++;
+  }
+  for (int d = 0; d < kRsBins; ++d) cnt[d][threadIdx.x] = c[d];
+  __syncthreads();
+  if (threadIdx.x < kRsBins) {
+    LO run = offs[LO(threadIdx.x) * nb + blockIdx.x];
+    for (int t = 0; t < kRsThreads; ++t) {
+      LO v = cnt[threadIdx.x][t];
+      cnt[threadIdx.x][t] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  for (int d = 0; d < kRsBins; ++d) c[d] = cnt[d][threadIdx.x];
+  for (int k = 0; k < kRsItems; ++k) {
+    LO i = base + k;
+    if (i < n) {
+      std::uint32_t key = keys[i];
+      int d = (key >> shift) & (kRsBins - 1);
+      LO pos = c[d]++;
+      okeys[pos] = key;
+      ovals[pos] = vals[i];
+    }
+  }
+}
+
+// sorts vals by keys[0..n) on bits [0, nbits), stably; both arrays permuted
+static void radix_pass_pairs(Arr<std::uint32_t>& keys, Arr<LO>& vals, int nbits) {
+  Ctx& c = ctx();
+  LO n = keys.size();
+  if (n <= 1) return;
+  LO nb = (n + kRsTile - 1) / kRsTile;
+  Arr<LO> hist(kRsBins * nb);
+  Arr<LO> offs(kRsBins * nb + 1);
+  Arr<std::uint32_t> k2(n);
+  Arr<LO> v2(n);
+  for (int shift = 0; shift < nbits; shift += 4) {
+    k_rs_hist<<<nb, kRsThreads, 0, c.stream>>>(keys.data(), n, shift, hist.data(), nb);
+    offset_scan_into(hist.data(), kRsBins * nb, offs.data());
+    k_rs_scatter<<<nb, kRsThreads, 0, c.stream>>>(keys.data(), vals.data(), n, shift,
+                                                   offs.data(), nb, k2.data(), v2.data());
+    c.launches += 2;
+    std::swap(keys, k2);
+    std::swap(vals, v2);
+  }
+}
+
+static int bits_needed(std::uint64_t maxv) {
+  int b = 0;
+  while (b < 64 && (maxv >> b) != 0) ++b;
+  return b;
+}
+
+// LSD over tuple components from last to first; each component gathered
+// through the current permutation, sorted stably on its significant bits
+Arr<LO> sort_by_keys(const Arr<LO>& keys, int w) {
+  LO n = keys.size() / w;
+  Arr<LO> perm = iota(n);
+  LO mx = max_lo(keys);
+  int nbits = bits_needed(std::uint64_t(mx < 0 ? 0xffffffffu : std::uint32_t(mx)));
+  if (nbits == 0) return perm;
+  for (int comp = w - 1; comp >= 0; --comp) {
+    Arr<std::uint32_t> k(n);
+    const LO* src = keys.data();
+    const LO* p = perm.data();
+    std::uint32_t* kd = k.data();
+    pfor(n, [=] __device__(LO i) { kd[i] = std::uint32_t(src[LO(p[i]) * w + comp]); });
+    radix_pass_pairs(k, perm, nbits);
+  }
+  return perm;
+}
+
+Arr<LO> sort_by_keys64(const Arr<GO>& keys, int w) {
+  LO n = keys.size() / w;
+  Arr<LO> perm = iota(n);
+  for (int comp = w - 1; comp >= 0; --comp) {
+    for (int half = 0; half < 2; ++half) {
+      Arr<std::uint32_t> k(n);
+      const GO* src = keys.data();
+      const LO* p = perm.data();
+      std::uint32_t* kd = k.data();
+      pfor(n, [=] __device__(LO i) {
+        std::uint64_t v = std::uint64_t(src[LO(p[i]) * w + comp]);
+        kd[i] = half == 0 ? std::uint32_t(v & 0xffffffffu) : std::uint32_t(v >> 32);
+      });
+      radix_pass_pairs(k, perm, 32);
+    }
+  }
+  return perm;
+}
+
+}  // namespace ohg

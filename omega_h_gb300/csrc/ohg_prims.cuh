@@ -1,0 +1,85 @@
+// Array primitives on device arrays: scans, compaction, reductions, stable
+// radix sorts and gathers/scatters (the roles of src/Omega_h_int_scan.cpp,
+// src/Omega_h_map.cpp, src/Omega_h_sort.cpp and src/Omega_h_reduce.hpp).
+#pragma once
+#include "ohg_common.cuh"
+
+namespace ohg {
+
+// exclusive prefix sum of counts, n+1 outputs (offset_scan,
+// src/Omega_h_int_scan.cpp:10-20)
+Arr<LO> offset_scan(const Arr<LO>& counts);
+Arr<LO> offset_scan(const Arr<I8>& counts);
+// same, into caller memory of n+1 entries
+void offset_scan_into(const LO* counts, LO n, LO* out);
+void offset_scan_into(const I8* counts, LO n, LO* out);
+
+// indices of nonzero marks (collect_marked, src/Omega_h_map.cpp:174-185)
+Arr<LO> collect_marked(const Arr<I8>& marks);
+LO count_marked(const Arr<I8>& marks);
+
+LO last(const Arr<LO>& a);
+
+// reductions (synchronise the stream)
+I8 max_i8(const Arr<I8>& a);
+double min_f64(const Arr<double>& a);
+double max_f64(const Arr<double>& a);
+LO max_lo(const Arr<LO>& a);
+
+// stable permutation sort of n tuples of width w, lexicographic
+// (sort_by_keys, src/Omega_h_sort.cpp:71-92); LSD radix sort
+Arr<LO> sort_by_keys(const Arr<LO>& keys, int width);
+Arr<LO> sort_by_keys64(const Arr<GO>& keys, int width);
+
+template <class T>
+Arr<T> fill(LO n, T v) {
+  Arr<T> a(n);
+  T* p = a.data();
+  pfor(n, [=] __device__(LO i) { p[i] = v; });
+  return a;
+}
+inline Arr<LO> iota(LO n) {
+  Arr<LO> a(n);
+  LO* p = a.data();
+  pfor(n, [=] __device__(LO i) { p[i] = i; });
+  return a;
+}
+// a[i*w+j] = b[a2b[i]*w+j]  (unmap)
+template <class T>
+Arr<T> unmap(const Arr<LO>& a2b, const Arr<T>& b, int w) {
+  Arr<T> a(a2b.size() * w);
+  const LO* m = a2b.data();
+  const T* src = b.data();
+  T* dst = a.data();
+  pfor(a2b.size(), [=] __device__(LO i) {
+    LO k = m[i];
+    for (int j = 0; j < w; ++j) dst[i * w + j] = src[LO(k) * w + j];
+  });
+  return a;
+}
+// b[a2b[i]*w+j] = a[i*w+j]  (map_into)
+template <class T>
+void map_into(const Arr<T>& a, const Arr<LO>& a2b, Arr<T>& b, int w) {
+  const LO* m = a2b.data();
+  const T* src = a.data();
+  T* dst = b.data();
+  pfor(a2b.size(), [=] __device__(LO i) {
+    LO k = m[i];
+    for (int j = 0; j < w; ++j) dst[LO(k) * w + j] = src[i * w + j];
+  });
+}
+template <class T>
+Arr<T> map_onto(const Arr<T>& a, const Arr<LO>& a2b, LO nb, T init, int w) {
+  Arr<T> b = fill<T>(nb * w, init);
+  map_into(a, a2b, b, w);
+  return b;
+}
+inline Arr<I8> mark_image(const Arr<LO>& a2b, LO nb) {
+  Arr<I8> out = fill<I8>(nb, 0);
+  const LO* m = a2b.data();
+  I8* o = out.data();
+  pfor(a2b.size(), [=] __device__(LO i) { o[m[i]] = 1; });
+  return out;
+}
+
+}  // namespace ohg

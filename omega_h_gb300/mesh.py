@@ -1,0 +1,224 @@
+"""Host-side mirror of the Omega_h Mesh / Read<T> / AdaptOpts interface on
+the adapt path, over the C ABI.  Device arrays are torch CUDA tensors; the
+computation is the CUDA library's (no CPU path exists).
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+# dtype of every named mesh array (see ohg_mesh_get_array in include/ohg.h)
+_F64 = ("coords", "metric", "length", "quality")
+
+
+def array_dtype(name):
+    if name in _F64:
+        return torch.float64
+    if name.startswith(("class_dim_", "downcodes", "up_codes_")):
+        return torch.int8
+    if name.startswith("global_"):
+        return torch.int64
+    return torch.int32
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+class Context:
+    """One device, one stream (ohg_context)."""
+
+    def __init__(self, device=0):
+        self.device = device
+        h = ctypes.c_void_p()
+        _lib.call("ohg_context_create", device, ctypes.byref(h))
+        self.handle = h
+
+    def launches(self):
+        v = ctypes.c_ulonglong()
+        _lib.call("ohg_context_launches", self.handle, ctypes.byref(v))
+        return v.value
+
+    def close(self):
+        if self.handle:
+            _lib.call("ohg_context_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def adapt_opts(dim, **overrides):
+    """AdaptOpts(dim) defaults (src/Omega_h_adapt.cpp:52-85) with overrides."""
+    o = _lib.AdaptOpts()
+    _lib.call("ohg_adapt_opts_default", dim, ctypes.byref(o))
+    for k, v in overrides.items():
+        setattr(o, k, v)
+    return o
+
+
+class Mesh:
+    """A device-resident simplex mesh (ohg_mesh)."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    @classmethod
+    def build_box(cls, ctx, dim, n):
+        """build_box on the unit square/cube, Hilbert-ordered and classified."""
+        h = ctypes.c_void_p()
+        _lib.call("ohg_build_box", ctx.handle, dim, n, ctypes.byref(h))
+        return cls(ctx, h)
+
+    @classmethod
+    def from_elems(cls, ctx, dim, ev2v, coords, metric):
+        h = ctypes.c_void_p()
+        nverts = coords.numel() // dim
+        _lib.call("ohg_mesh_from_elems", ctx.handle, dim, nverts, ev2v.numel() // (dim + 1),
+                  _ptr(ev2v), _ptr(coords), _ptr(metric), ctypes.byref(h))
+        return cls(ctx, h)
+
+    def apply_workload(self, n, seed, metric_kind):
+        _lib.call("ohg_mesh_apply_workload", self.handle, n, seed, metric_kind)
+
+    @property
+    def dim(self):
+        v = ctypes.c_int()
+        _lib.call("ohg_mesh_dim", self.handle, ctypes.byref(v))
+        return v.value
+
+    def nents(self, d):
+        v = ctypes.c_int()
+        _lib.call("ohg_mesh_nents", self.handle, d, ctypes.byref(v))
+        return v.value
+
+    def nelems(self):
+        return self.nents(self.dim)
+
+    def get(self, name):
+        """A copy of a named mesh array as a CUDA tensor."""
+        nb = ctypes.c_longlong()
+        _lib.call("ohg_mesh_array_bytes", self.handle, name.encode(), ctypes.byref(nb))
+        dt = array_dtype(name)
+        t = torch.empty(nb.value // torch.tensor([], dtype=dt).element_size(), dtype=dt,
+                        device=f"cuda:{self.ctx.device}")
+        _lib.call("ohg_mesh_get_array", self.handle, name.encode(), _ptr(t), nb.value)
+        return t
+
+    def set(self, name, t):
+        t = t.contiguous()
+        _lib.call("ohg_mesh_set_array", self.handle, name.encode(), _ptr(t),
+                  t.numel() * t.element_size())
+
+    def adapt_pass(self, opts=None):
+        o = opts or adapt_opts(self.dim)
+        s = _lib.PassStats()
+        _lib.call("ohg_adapt_pass", self.handle, ctypes.byref(o), ctypes.byref(s))
+        return s.as_dict()
+
+    def _op(self, fname, opts):
+        o = opts or adapt_opts(self.dim)
+        did = ctypes.c_int()
+        _lib.call(fname, self.handle, ctypes.byref(o), ctypes.byref(did))
+        return bool(did.value)
+
+    def refine_by_size(self, opts=None):
+        return self._op("ohg_refine_by_size", opts)
+
+    def coarsen_by_size(self, opts=None):
+        return self._op("ohg_coarsen_by_size", opts)
+
+    def swap_edges(self, opts=None):
+        return self._op("ohg_swap_edges", opts)
+
+    # ---- stage kernels --------------------------------------------------
+    def _dev(self):
+        return f"cuda:{self.ctx.device}"
+
+    def measure_edges_metric(self, a2e=None):
+        n = a2e.numel() if a2e is not None else self.nents(1)
+        out = torch.empty(n, dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_measure_edges_metric", self.handle, _ptr(a2e), n, _ptr(out))
+        return out
+
+    def measure_qualities(self, a2e=None):
+        n = a2e.numel() if a2e is not None else self.nelems()
+        out = torch.empty(n, dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_measure_qualities", self.handle, _ptr(a2e), n, _ptr(out))
+        return out
+
+    def mident_metrics(self, edges):
+        out = torch.empty(edges.numel() * 6, dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_get_mident_metrics", self.handle, _ptr(edges), edges.numel(), _ptr(out))
+        return out
+
+    def refine_qualities(self, c2e):
+        out = torch.empty(c2e.numel(), dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_refine_qualities", self.handle, _ptr(c2e), c2e.numel(), _ptr(out))
+        return out
+
+    def check_collapse_class(self, c2e, codes):
+        out = torch.empty_like(codes)
+        _lib.call("ohg_check_collapse_class", self.handle, _ptr(c2e), c2e.numel(), _ptr(codes), _ptr(out))
+        return out
+
+    def check_collapse_exposure(self, c2e, codes):
+        out = torch.empty_like(codes)
+        _lib.call("ohg_check_collapse_exposure", self.handle, _ptr(c2e), c2e.numel(), _ptr(codes),
+                  _ptr(out))
+        return out
+
+    def prevent_coarsen_overshoot(self, max_length, c2e, codes):
+        out = torch.empty_like(codes)
+        _lib.call("ohg_prevent_coarsen_overshoot", self.handle, max_length, _ptr(c2e), c2e.numel(),
+                  _ptr(codes), _ptr(out))
+        return out
+
+    def coarsen_qualities(self, c2e, codes):
+        out = torch.empty(c2e.numel() * 2, dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_coarsen_qualities", self.handle, _ptr(c2e), c2e.numel(), _ptr(codes), _ptr(out))
+        return out
+
+    def choose_rails(self, c2e, codes, quals2):
+        nv = self.nents(0)
+        vc = torch.empty(nv, dtype=torch.int8, device=self._dev())
+        vq = torch.empty(nv, dtype=torch.float64, device=self._dev())
+        vr = torch.empty(nv, dtype=torch.int64, device=self._dev())
+        _lib.call("ohg_choose_rails", self.handle, _ptr(c2e), c2e.numel(), _ptr(codes), _ptr(quals2),
+                  _ptr(vc), _ptr(vq), _ptr(vr))
+        return vc, vq, vr
+
+    def mark_sliver_layers(self, qual_ceil, nlayers):
+        out = torch.empty(self.nelems(), dtype=torch.int8, device=self._dev())
+        _lib.call("ohg_mark_sliver_layers", self.handle, qual_ceil, nlayers, _ptr(out))
+        return out
+
+    def swap3d_qualities(self, max_length_allowed, c2e):
+        q = torch.empty(c2e.numel(), dtype=torch.float64, device=self._dev())
+        cf = torch.empty(c2e.numel(), dtype=torch.int8, device=self._dev())
+        _lib.call("ohg_swap3d_qualities", self.handle, max_length_allowed, _ptr(c2e), c2e.numel(),
+                  _ptr(q), _ptr(cf))
+        return q, cf
+
+    def find_indset(self, ent_dim, quality, candidates):
+        out = torch.empty_like(candidates)
+        r = ctypes.c_int()
+        _lib.call("ohg_find_indset", self.handle, ent_dim, _ptr(quality), _ptr(candidates), _ptr(out),
+                  ctypes.byref(r))
+        return out, r.value
+
+    def close(self):
+        if self.handle:
+            _lib.call("ohg_mesh_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,125 @@
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+# golden case name -> (dim, n, metric kind, seed, min_quality_allowed)
+SMALL_CASES = {
+    "box8_iso": (3, 8, 0, 12345, 0.3),
+    "box12_shock": (3, 12, 1, 7, 0.2),
+    "box12_blayer": (3, 12, 2, 3, 0.2),
+}
+BIG_CASE = ("box64_shock", (3, 64, 1, 2024, 0.2))
+# arrays that are metadata, not per-stage outputs
+SKIP_KEYS = ("meta_json", "swap3d_tables", "opts", "opts_values", "r_rep2md")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+def load_golden(case):
+    z = np.load(os.path.join(GOLDEN, case + ".npz"))
+    return {k: z[k] for k in z.files}
+
+
+def load_digest(case):
+    with open(os.path.join(GOLDEN, case + "_digest.json")) as f:
+        return json.load(f)
+
+
+def load_dump_dir(d):
+    out = {}
+    with open(os.path.join(d, "manifest.txt")) as f:
+        for line in f:
+            name, dt, count = line.split()
+            out[name] = np.fromfile(os.path.join(d, name + ".bin"), dtype=np.dtype(dt))
+            assert out[name].size == int(count)
+    return out
+
+
+@pytest.fixture(scope="session")
+def oracle_driver():
+    """Builds the oracle restatement (test infrastructure) and returns the
+    path of its driver."""
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j4"], check=True,
+                   stdout=subprocess.DEVNULL)
+    return os.path.join(ROOT, "oracle", "_build", "oracle_driver")
+
+
+def run_oracle(driver, spec, mode=""):
+    dim, n, kind, seed, mqa = spec
+    with tempfile.TemporaryDirectory() as d:
+        args = [driver, str(dim), str(n), str(kind), str(seed), str(mqa), d]
+        if mode:
+            args.append(mode)
+        r = subprocess.run(args, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        return load_dump_dir(d)
+
+
+def compare_arrays(expected, got, keys=None, rtol=1e-12):
+    """Bit-exact for integer arrays, relative error <= rtol for reals.
+    Returns (list of failures, max real relative error, count of real
+    values that are not bitwise equal)."""
+    fails = []
+    maxerr = 0.0
+    nreal_diff = 0
+    for k in keys or expected:
+        if k.startswith(SKIP_KEYS):
+            continue
+        if k not in got:
+            fails.append(f"{k}: missing")
+            continue
+        a, b = np.asarray(expected[k]), np.asarray(got[k])
+        if a.shape != b.shape:
+            fails.append(f"{k}: shape {a.shape} vs {b.shape}")
+            continue
+        if a.dtype.kind == "f":
+            if a.size:
+                err = float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-300)))
+                maxerr = max(maxerr, err)
+                nreal_diff += int(np.sum(a != b))
+                if not err <= rtol:
+                    fails.append(f"{k}: max rel err {err:.3e}")
+        else:
+            nd = int(np.sum(a != b.astype(a.dtype)))
+            if nd:
+                fails.append(f"{k}: {nd}/{a.size} integers differ, first at {np.nonzero(a != b)[0][:4]}")
+    return fails, maxerr, nreal_diff
+
+
+def compare_digest(digest, got, rtol=1e-12):
+    import hashlib
+    fails = []
+    for k, v in digest["arrays"].items():
+        if k not in got:
+            continue
+        a = np.ascontiguousarray(got[k])
+        if a.size != v["count"]:
+            fails.append(f"{k}: count {a.size} vs {v['count']}")
+            continue
+        if "sha256" in v:
+            h = hashlib.sha256(a.astype(np.dtype(v["dtype"])).tobytes()).hexdigest()
+            if h != v["sha256"]:
+                fails.append(f"{k}: sha256 differs")
+        elif a.size:
+            idx = np.array(v["sample_idx"], dtype=np.int64)
+            s = np.array(v["sample"])
+            err = float(np.max(np.abs(a[idx] - s) / np.maximum(np.abs(s), 1e-300)))
+            if not err <= rtol:
+                fails.append(f"{k}: sampled rel err {err:.3e}")
+            for stat in ("min", "max"):
+                e = abs(getattr(a, stat)() - v[stat]) / max(abs(v[stat]), 1e-300)
+                if not e <= rtol:
+                    fails.append(f"{k}: {stat} rel err {e:.3e}")
+    return fails

@@ -1,0 +1,27 @@
+"""The oracle restatement against the reference's own outputs (golden
+fixtures generated by tests/golden/make_golden.py from the reference built
+from source).  CPU only."""
+import pytest
+
+from conftest import (BIG_CASE, SMALL_CASES, compare_arrays, compare_digest, load_digest,
+                      load_golden, run_oracle)
+
+
+@pytest.mark.parametrize("case", sorted(SMALL_CASES))
+def test_oracle_matches_reference_per_stage(oracle_driver, case):
+    golden = load_golden(case)
+    got = run_oracle(oracle_driver, SMALL_CASES[case])
+    fails, maxerr, ndiff = compare_arrays(golden, got)
+    assert not fails, fails[:10]
+    # the restatement keeps the reference's operation order: reals are
+    # bitwise identical on this platform
+    assert maxerr == 0.0 and ndiff == 0
+
+
+def test_oracle_full_size_pass_matches_reference_digest(oracle_driver):
+    name, spec = BIG_CASE
+    got = run_oracle(oracle_driver, spec, mode="nostages")
+    digest = load_digest(name)
+    fails = compare_digest(digest, got)
+    assert not fails, fails[:10]
+    assert list(got["pass_flags"]) == [0, 1, 1]
