@@ -3,7 +3,9 @@ import ctypes
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libohg.so")
+# OHG_CHECKED=1 selects the bounds-checked build of the same library
+LIB_PATH = os.path.join(_HERE, "libohg_checked.so" if os.environ.get("OHG_CHECKED") == "1"
+                        else "libohg.so")
 
 c_int, c_double, c_void_p, c_char_p = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_char_p
 c_ll, c_ull = ctypes.c_longlong, ctypes.c_ulonglong

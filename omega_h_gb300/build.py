@@ -13,6 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libohg.so")
+# bounds-checked variant: every device array subscript is checked and each
+# launch is followed by a synchronising check that names its source line
+LIB_CHECKED = os.path.join(HERE, "libohg_checked.so")
 SOURCES = ["ohg_prims.cu", "ohg_mesh.cu", "ohg_adapt.cu", "ohg_capi.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -28,32 +31,36 @@ def _newest_dep_mtime():
     return t
 
 
-def _compile(src):
-    obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-    cmd = [NVCC, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(src, checked=False):
+    bdir = BUILD + ("_checked" if checked else "")
+    obj = os.path.join(bdir, src.replace(".cu", ".o"))
+    extra = ["-DOHG_CHECKED"] if checked else []
+    cmd = [NVCC, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
     return obj
 
 
-def build(force=False, verbose=False):
-    """Compile and link libohg.so unless it is newer than every source."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_dep_mtime():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, checked=False):
+    """Compile and link libohg.so (or the checked variant) unless it is newer
+    than every source."""
+    lib = LIB_CHECKED if checked else LIB
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _newest_dep_mtime():
+        return lib
+    os.makedirs(BUILD + ("_checked" if checked else ""), exist_ok=True)
     with concurrent.futures.ThreadPoolExecutor(len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, checked), SOURCES))
+    tmp = lib + ".tmp"
     cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv)

@@ -19,32 +19,39 @@ AdaptOpts::AdaptOpts(int dim) {
   nsliver_layers = 4;
 }
 
-__device__ __forceinline__ double elem_quality_v(int dim, const double* c, const double* mt,
-                                                 const LO* v) {
+typedef View<const double> RV;
+typedef View<const LO> LV;
+
+__device__ __forceinline__ double elem_quality_v(int dim, RV c, RV mt, const LO* v) {
   if (dim == 3) {
     V3 p[4];
     M3 ms[4];
     for (int i = 0; i < 4; ++i) {
-      for (int j = 0; j < 3; ++j) p[i].x[j] = c[LO(v[i]) * 3 + j];
-      ms[i] = symm3(mt + LO(v[i]) * 6);
+      for (int j = 0; j < 3; ++j) p[i].x[j] = c[v[i] * 3 + j];
+      ms[i] = symm3(&mt[v[i] * 6]);
     }
     return tet_quality(p, ms[maxdet_index3(ms, 4)]);
   }
   double p[3][2];
   int best = 0;
-  double bd = det2p(mt + LO(v[0]) * 3);
+  double bd = det2p(&mt[v[0] * 3]);
   for (int i = 0; i < 3; ++i) {
-    p[i][0] = c[LO(v[i]) * 2];
-    p[i][1] = c[LO(v[i]) * 2 + 1];
+    p[i][0] = c[v[i] * 2];
+    p[i][1] = c[v[i] * 2 + 1];
     if (i) {
-      double d = det2p(mt + LO(v[i]) * 3);
+      double d = det2p(&mt[v[i] * 3]);
       if (d > bd) {
         best = i;
         bd = d;
       }
     }
   }
-  return tri_quality(p, mt + LO(v[best]) * 3);
+  return tri_quality(p, &mt[v[best] * 3]);
+}
+
+__device__ __forceinline__ double edge_len_v(int dim, RV c, RV mt, int mc, LO a, LO b) {
+  return dim == 3 ? edge_length3(&c[a * 3], &c[b * 3], &mt[a * mc], &mt[b * mc])
+                  : edge_length2(&c[a * 2], &c[b * 2], &mt[a * mc], &mt[b * mc]);
 }
 
 // ------------------------------------------------------------ indset
@@ -55,21 +62,23 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
                     int* rounds_out) {
   Ctx& c = ctx();
   Arr<I8> a(n), b(n);
-  const I8* cd = cands.data();
-  I8* s0 = a.data();
-  pfor(n, [=] __device__(LO i) { s0[i] = cd[i] ? UNKNOWN : NOT_IN; });
+  auto cd = cview(cands);
+  {
+    auto s0 = view(a);
+    pfor(n, [=] __device__(LO i) { s0[i] = cd[i] ? UNKNOWN : NOT_IN; });
+  }
   Arr<int> flag(1);
-  int* fl = flag.data();
-  const LO* xa = g.a2ab.data();
-  const LO* xb = g.ab2b.data();
-  const double* q = quality.data();
+  auto fl = view(flag);
+  auto xa = cview(g.a2ab);
+  auto xb = cview(g.ab2b);
+  auto q = cview(quality);
   int rounds = 0;
   int any = count_marked(cands) > 0;
   while (any) {
     if (rounds >= kMaxIndsetRounds) throw Error(5, "independent set did not converge");
-    OHG_CUDA(cudaMemsetAsync(fl, 0, sizeof(int), c.stream));
-    const I8* old = a.data();
-    I8* nw = b.data();
+    OHG_CUDA(cudaMemsetAsync(flag.data(), 0, sizeof(int), c.stream));
+    auto old = cview(a);
+    auto nw = view(b);
     pfor(n, [=] __device__(LO v) {
       I8 sv = old[v];
       if (sv != UNKNOWN) {
@@ -90,7 +99,7 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
         bool less = (qu != qv) ? (qu < qv) : (u < v);
         if (!less) {
           nw[v] = UNKNOWN;
-          *fl = 1;
+          fl[0] = 1;
           return;
         }
       }
@@ -98,7 +107,7 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
     });
     std::swap(a, b);
     ++rounds;
-    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flag.data(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
     any = c.h_pinned[0];
   }
@@ -112,11 +121,11 @@ Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& q, const Arr<I8>& cands, 
 
 // ------------------------------------------------------------ marks
 static Arr<I8> mark_up(Mesh& m, int ld, int hd, const Arr<I8>& lm) {
-  const LO* hl = m.ask_down(hd, ld).ab2b.data();
+  auto hl = cview(m.ask_down(hd, ld).ab2b);
   int deg = simplex_degree(hd, ld);
   Arr<I8> out(m.nents[hd]);
-  const I8* l = lm.data();
-  I8* o = out.data();
+  auto l = cview(lm);
+  auto o = view(out);
   pfor(m.nents[hd], [=] __device__(LO h) {
     I8 r = 0;
     for (int k = 0; k < deg; ++k)
@@ -127,11 +136,11 @@ static Arr<I8> mark_up(Mesh& m, int ld, int hd, const Arr<I8>& lm) {
 }
 static Arr<I8> mark_down(Mesh& m, int hd, int ld, const Arr<I8>& hm) {
   const Adj& l2h = m.ask_up(ld, hd);
-  const LO* a = l2h.a2ab.data();
-  const LO* b = l2h.ab2b.data();
-  const I8* h = hm.data();
+  auto a = cview(l2h.a2ab);
+  auto b = cview(l2h.ab2b);
+  auto h = cview(hm);
   Arr<I8> out(m.nents[ld]);
-  I8* o = out.data();
+  auto o = view(out);
   pfor(m.nents[ld], [=] __device__(LO l) {
     I8 r = 0;
     for (LO x = a[l]; x < a[l + 1]; ++x)
@@ -153,34 +162,32 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
                                    const Arr<LO>& keys2kds, const Arr<LO>& keys2prods,
                                    const Arr<LO>& prod_verts2verts,
                                    const Arr<LO>& old_lows2new_lows) {
-  int dim = om.dim;
   LO nkeys = keys2kds.size();
   ModifyOut out;
   LO nold = om.nents[ent_dim];
-  Arr<I8> mods_ent;
   if (ent_dim >= key_dim) {
     Arr<I8> km = mark_image(keys2kds, om.nents[key_dim]);
-    mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
+    Arr<I8> mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
     Arr<I8> same(nold);
-    const I8* me = mods_ent.data();
-    I8* sm = same.data();
+    auto me = cview(mods_ent);
+    auto sm = view(same);
     pfor(nold, [=] __device__(LO e) { sm[e] = !me[e]; });
     out.same2old = collect_marked(same);
   } else {
     out.same2old = iota(nold);
   }
-  // representatives (get_mods2reps)
-  Arr<LO> reps(nkeys);
-  {
-    const LO* kd = keys2kds.data();
-    LO* r = reps.data();
-    if (key_dim == ent_dim) {
-      r = nullptr;
-      reps = keys2kds;
-    } else if (ent_dim > key_dim) {
+  // representatives (get_mods2reps, src/Omega_h_modify.cpp:163-195)
+  Arr<LO> reps;
+  if (key_dim == ent_dim) {
+    reps = keys2kds;
+  } else {
+    reps = Arr<LO>(nkeys);
+    auto kd = cview(keys2kds);
+    auto r = view(reps);
+    if (ent_dim > key_dim) {
       const Adj& up = om.ask_up(key_dim, ent_dim);
-      const LO* ua = up.a2ab.data();
-      const LO* ub = up.ab2b.data();
+      auto ua = cview(up.a2ab);
+      auto ub = cview(up.ab2b);
       int* stw = ctx().d_status;
       pfor(nkeys, [=] __device__(LO k) {
         LO b = ua[kd[k]];
@@ -192,18 +199,20 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
         }
       });
     } else {
-      const LO* dn = om.ask_down(key_dim, ent_dim).ab2b.data();
+      auto dn = cview(om.ask_down(key_dim, ent_dim).ab2b);
       int deg = simplex_degree(key_dim, ent_dim);
-      pfor(nkeys, [=] __device__(LO k) { r[k] = dn[LO(kd[k]) * deg]; });
+      pfor(nkeys, [=] __device__(LO k) { r[k] = dn[kd[k] * deg]; });
     }
   }
+  // get_rep_counts (src/Omega_h_modify.cpp:210-243): integer sums, so the
+  // atomics give a deterministic result
   Arr<LO> counts = fill<LO>(nold, 0);
   {
-    LO* ct = counts.data();
-    const LO* s2o = out.same2old.data();
+    auto ct = view(counts);
+    auto s2o = cview(out.same2old);
     pfor(out.same2old.size(), [=] __device__(LO i) { ct[s2o[i]] = 1; });
-    const LO* r = reps.data();
-    const LO* kp = keys2prods.data();
+    auto r = cview(reps);
+    auto kp = cview(keys2prods);
     pfor(nkeys, [=] __device__(LO k) { atomicAdd(&ct[r[k]], kp[k + 1] - kp[k]); });
   }
   Arr<LO> offs = offset_scan(counts);
@@ -214,20 +223,21 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     // get_rep2md_order (src/Omega_h_modify.cpp:283-338)
     order = fill<LO>(om.nents[key_dim], -1);
     Arr<LO> md2mod = fill<LO>(om.nents[key_dim], -1);
-    LO* m2m = md2mod.data();
-    const LO* kd = keys2kds.data();
+    auto m2m = view(md2mod);
+    auto kd = cview(keys2kds);
     pfor(nkeys, [=] __device__(LO k) { m2m[kd[k]] = k; });
     const Adj& r2m = om.ask_up(ent_dim, key_dim);
-    const LO* ra = r2m.a2ab.data();
-    const LO* rb = r2m.ab2b.data();
-    const I8* rc = r2m.codes.data();
-    const LO* kp = keys2prods.data();
-    LO* ord = order.data();
+    auto ra = cview(r2m.a2ab);
+    auto rb = cview(r2m.ab2b);
+    auto rc = cview(r2m.codes);
+    auto kp = cview(keys2prods);
+    auto ord = view(order);
+    auto m2mc = cview(md2mod);
     pfor(nold, [=] __device__(LO rep) {
       LO offset = 0;
       for (LO x = ra[rep]; x < ra[rep + 1]; ++x) {
         LO md = rb[x];
-        LO mod = m2m[md];
+        LO mod = m2mc[md];
         if (mod >= 0 && code_which_down(rc[x]) == 0) {
           ord[md] = offset;
           offset += kp[mod + 1] - kp[mod];
@@ -238,16 +248,16 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   out.same2new = unmap(out.same2old, offs, 1);
   out.prods2new = Arr<LO>(last(keys2prods));
   {
-    const LO* of = offs.data();
-    const LO* r = reps.data();
-    const LO* kp = keys2prods.data();
-    const LO* kd = keys2kds.data();
-    const LO* ord = has_order ? order.data() : nullptr;
-    LO* p2n = out.prods2new.data();
+    auto of = cview(offs);
+    auto r = cview(reps);
+    auto kp = cview(keys2prods);
+    auto kd = cview(keys2kds);
+    auto ord = cview(order);
+    auto p2n = view(out.prods2new);
     int self = has_order ? 1 : 0;
     pfor(nkeys, [=] __device__(LO k) {
       LO offset = of[r[k]] + self;
-      if (ord) offset += ord[kd[k]];
+      if (has_order) offset += ord[kd[k]];
       for (LO p = kp[k]; p < kp[k + 1]; ++p) p2n[p] = offset++;
     });
   }
@@ -256,30 +266,40 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     nm.nents[0] = nnew;
     return out;
   }
+  // modify_conn (src/Omega_h_modify.cpp:20-70)
   int ld = ent_dim - 1;
   int deg = simplex_degree(ent_dim, ld);
   const Adj& od = om.ask_down(ent_dim, ld);
   Adj nd;
   // zero-filled so that every slot holds a valid index even if a caller's
-  // keys were not independent (the writes below then overlap)
+  // keys were not independent (the writes below would then overlap)
   nd.ab2b = fill<LO>(nnew * deg, 0);
   LO nprods = out.prods2new.size();
   Adj pd;
   if (ld > VERT) {
-    pd = reflect_down(prod_verts2verts, nprods, nm.ask_verts_of(ld), nm.ask_up(VERT, ld), ent_dim,
-                      ld);
+    const Arr<LO>& lv2v = nm.ask_verts_of(ld);
+    const Adj& v2l = nm.ask_up(VERT, ld);
+    pd = reflect_down(prod_verts2verts, nprods, lv2v, v2l, ent_dim, ld);
   } else {
     pd.ab2b = prod_verts2verts;
   }
   map_into(pd.ab2b, out.prods2new, nd.ab2b, deg);
   {
-    const LO* s2o = out.same2old.data();
-    const LO* s2n = out.same2new.data();
-    const LO* ob = od.ab2b.data();
-    const LO* l2n = old_lows2new_lows.data();
-    LO* nb = nd.ab2b.data();
+    auto s2o = cview(out.same2old);
+    auto s2n = cview(out.same2new);
+    auto ob = cview(od.ab2b);
+    auto l2n = cview(old_lows2new_lows);
+    auto nb = view(nd.ab2b);
+    int* stw = ctx().d_status;
     pfor(out.same2old.size(), [=] __device__(LO i) {
-      for (int k = 0; k < deg; ++k) nb[LO(s2n[i]) * deg + k] = l2n[ob[LO(s2o[i]) * deg + k]];
+      for (int k = 0; k < deg; ++k) {
+        LO l = l2n[ob[s2o[i] * deg + k]];
+        if (l < 0) {
+          raise_status(stw, ST_TOPOLOGY);
+          l = 0;
+        }
+        nb[s2n[i] * deg + k] = l;
+      }
     });
   }
   if (ld > VERT) {
@@ -297,12 +317,12 @@ template <class T>
 static Arr<T> xfer(const Arr<T>& old, const ModifyOut& mo, LO nnew, const Arr<T>& prod, int w) {
   Arr<T> nd(nnew * w);
   if (prod.size()) map_into(prod, mo.prods2new, nd, w);
-  const LO* s2o = mo.same2old.data();
-  const LO* s2n = mo.same2new.data();
-  const T* o = old.data();
-  T* d = nd.data();
+  auto s2o = cview(mo.same2old);
+  auto s2n = cview(mo.same2new);
+  auto o = cview(old);
+  auto d = view(nd);
   pfor(mo.same2old.size(), [=] __device__(LO i) {
-    for (int j = 0; j < w; ++j) d[LO(s2n[i]) * w + j] = o[LO(s2o[i]) * w + j];
+    for (int j = 0; j < w; ++j) d[s2n[i] * w + j] = o[s2o[i] * w + j];
   });
   return nd;
 }
@@ -326,16 +346,19 @@ static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& m
 // ------------------------------------------------------------ refine
 // refine_qualities_tmpl (src/Omega_h_refine_qualities.cpp:34-86): one thread
 // per candidate edge, two child simplices per adjacent element
-void refine_qualities(Mesh& m, const LO* c2e, LO n, const double* mid, double* out) {
-  int dim = m.dim;
-  const LO* ev = m.ask_verts_of(1).data();
-  const LO* cv = m.ask_verts_of(dim).data();
+void refine_qualities(Mesh& m, const LO* c2e_p, LO n, const double* mid_p, double* out_p) {
+  int dim = m.dim, mc = m.mcomp();
+  auto ev = cview(m.ask_verts_of(1));
+  auto cv = cview(m.ask_verts_of(dim));
   const Adj& e2c = m.ask_up(1, dim);
-  const LO* ea = e2c.a2ab.data();
-  const LO* eb = e2c.ab2b.data();
-  const I8* ec = e2c.codes.data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto ea = cview(e2c.a2ab);
+  auto eb = cview(e2c.ab2b);
+  auto ec = cview(e2c.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto mid = cview(mid_p, n * mc);
+  auto out = view(out_p, n);
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
@@ -346,12 +369,11 @@ void refine_qualities(Mesh& m, const LO* c2e, LO n, const double* mid, double* o
       LO el = eb[x];
       I8 code = ec[x];
       int cce = code_which_down(code), rot = code_rotation(code);
-      const LO* ccv2v = cv + el * (dim + 1);
       for (int eev = 0; eev < 2; ++eev) {
         int ccv = down_template(dim, 1, cce, eev ^ rot);
         int ccs = opposite_template(dim, 0, ccv);
         LO sv[3];
-        for (int k = 0; k < dim; ++k) sv[k] = ccv2v[down_template(dim, dim - 1, ccs, k)];
+        for (int k = 0; k < dim; ++k) sv[k] = cv[el * (dim + 1) + down_template(dim, dim - 1, ccs, k)];
         double q;
         if (dim == 3) {
           LO t = sv[1];
@@ -360,23 +382,23 @@ void refine_qualities(Mesh& m, const LO* c2e, LO n, const double* mid, double* o
           V3 p[4];
           M3 ms[4];
           for (int i = 0; i < 3; ++i) {
-            for (int j = 0; j < 3; ++j) p[i].x[j] = c[LO(sv[i]) * 3 + j];
-            ms[i] = symm3(mt + LO(sv[i]) * 6);
+            for (int j = 0; j < 3; ++j) p[i].x[j] = c[sv[i] * 3 + j];
+            ms[i] = symm3(&mt[sv[i] * 6]);
           }
           for (int j = 0; j < 3; ++j) p[3].x[j] = midp[j];
-          ms[3] = symm3(mid + LO(cand) * 6);
+          ms[3] = symm3(&mid[cand * 6]);
           q = tet_quality(p, ms[maxdet_index3(ms, 4)]);
         } else {
           double p[3][2];
           const double* mm[3];
           for (int i = 0; i < 2; ++i) {
-            p[i][0] = c[LO(sv[i]) * 2];
-            p[i][1] = c[LO(sv[i]) * 2 + 1];
-            mm[i] = mt + LO(sv[i]) * 3;
+            p[i][0] = c[sv[i] * 2];
+            p[i][1] = c[sv[i] * 2 + 1];
+            mm[i] = &mt[sv[i] * 3];
           }
           p[2][0] = midp[0];
           p[2][1] = midp[1];
-          mm[2] = mid + LO(cand) * 3;
+          mm[2] = &mid[cand * 3];
           int best = 0;
           double bd = det2p(mm[0]);
           for (int i = 1; i < 3; ++i) {
@@ -402,51 +424,52 @@ static void refine_products(Mesh& m, int ed, const Arr<LO>& k2e, const Arr<LO>& 
                             const Arr<LO>& ov2nv, Arr<LO>& k2p, Arr<LO>& pv2v) {
   int dim = m.dim;
   LO nkeys = k2e.size();
-  const LO* ke = k2e.data();
-  const LO* km = k2mid.data();
-  const LO* o2n = ov2nv.data();
-  const LO* ev = m.ask_verts_of(1).data();
-  const LO *pa = nullptr, *pb = nullptr, *ca = nullptr, *cb = nullptr;
-  const I8 *pc = nullptr, *cc = nullptr;
-  const LO *pdv = nullptr, *cdv = nullptr;
+  auto ke = cview(k2e);
+  auto km = cview(k2mid);
+  auto o2n = cview(ov2nv);
+  auto ev = cview(m.ask_verts_of(1));
+  LV pa = {nullptr, 0}, pb = {nullptr, 0}, ca = {nullptr, 0}, cb = {nullptr, 0};
+  LV pdv = {nullptr, 0}, cdv = {nullptr, 0};
+  View<const I8> pc = {nullptr, 0}, cc = {nullptr, 0};
   if (ed > EDGE) {
     const Adj& e2d = m.ask_up(1, ed);
-    pa = e2d.a2ab.data();
-    pb = e2d.ab2b.data();
-    pc = e2d.codes.data();
-    pdv = m.ask_verts_of(ed).data();
+    pa = cview(e2d.a2ab);
+    pb = cview(e2d.ab2b);
+    pc = cview(e2d.codes);
+    pdv = cview(m.ask_verts_of(ed));
   }
   int cd = ed + 1;
-  if (ed < dim) {
+  bool cuts = ed < dim;
+  if (cuts) {
     const Adj& e2c = m.ask_up(1, cd);
-    ca = e2c.a2ab.data();
-    cb = e2c.ab2b.data();
-    cc = e2c.codes.data();
-    cdv = m.ask_verts_of(cd).data();
+    ca = cview(e2c.a2ab);
+    cb = cview(e2c.ab2b);
+    cc = cview(e2c.codes);
+    cdv = cview(m.ask_verts_of(cd));
   }
   Arr<LO> cnt(nkeys);
-  LO* ct = cnt.data();
+  auto ct = view(cnt);
   pfor(nkeys, [=] __device__(LO k) {
     LO e = ke[k];
     LO np = ed == EDGE ? 2 : 2 * (pa[e + 1] - pa[e]);
-    if (ed < dim) np += ca[e + 1] - ca[e];
+    if (cuts) np += ca[e + 1] - ca[e];
     ct[k] = np;
   });
   k2p = offset_scan(cnt);
   int nppv = ed + 1;
   pv2v = Arr<LO>(last(k2p) * nppv);
-  const LO* kp = k2p.data();
-  LO* pv = pv2v.data();
+  auto kp = cview(k2p);
+  auto pv = view(pv2v);
   pfor(nkeys, [=] __device__(LO k) {
     LO e = ke[k];
     LO prod = kp[k];
     LO mid = km[k];
     if (ed == EDGE) {
-      LO* o = pv + prod * 2;
-      o[0] = o2n[ev[e * 2]];
-      o[1] = mid;
-      o[2] = mid;
-      o[3] = o2n[ev[e * 2 + 1]];
+      LO b = prod * 2;
+      pv[b + 0] = o2n[ev[e * 2]];
+      pv[b + 1] = mid;
+      pv[b + 2] = mid;
+      pv[b + 3] = o2n[ev[e * 2 + 1]];
       prod += 2;
     } else {
       for (LO x = pa[e]; x < pa[e + 1]; ++x) {
@@ -455,56 +478,59 @@ static void refine_products(Mesh& m, int ed, const Arr<LO>& k2e, const Arr<LO>& 
         for (int eev = 0; eev < 2; ++eev) {
           int ddv = down_template(ed, 1, dde, eev ^ rot);
           int dds = opposite_template(ed, 0, ddv);
-          LO* o = pv + prod * nppv;
-          for (int k2 = 0; k2 < ed; ++k2) o[k2] = o2n[pdv[dom * (ed + 1) + down_template(ed, ed - 1, dds, k2)]];
-          o[ed] = mid;
+          LO tmp[4];
+          for (int k2 = 0; k2 < ed; ++k2)
+            tmp[k2] = o2n[pdv[dom * (ed + 1) + down_template(ed, ed - 1, dds, k2)]];
+          tmp[ed] = mid;
           if (ed == 3) {
-            LO t = o[1];
-            o[1] = o[2];
-            o[2] = t;
+            LO t = tmp[1];
+            tmp[1] = tmp[2];
+            tmp[2] = t;
           }
+          for (int k2 = 0; k2 <= ed; ++k2) pv[prod * nppv + k2] = tmp[k2];
           ++prod;
         }
       }
     }
-    if (ed < dim) {
+    if (cuts) {
       for (LO x = ca[e]; x < ca[e + 1]; ++x) {
         LO dom = cb[x];
         int ddt = opposite_template(cd, 1, code_which_down(cc[x]));
-        LO* o = pv + prod * nppv;
         for (int k2 = 0; k2 < cd - 1; ++k2)
-          o[k2] = o2n[cdv[dom * (cd + 1) + down_template(cd, cd - 2, ddt, k2)]];
-        o[cd - 1] = mid;
+          pv[prod * nppv + k2] = o2n[cdv[dom * (cd + 1) + down_template(cd, cd - 2, ddt, k2)]];
+        pv[prod * nppv + cd - 1] = mid;
         ++prod;
       }
     }
   });
 }
 
+// class tags: pairs inherit their split d-entity, cuts their (d+1)-entity
+// (transfer_inherit_refine, src/Omega_h_transfer.cpp:213-263)
 template <class T>
 static void inherit_refine(Mesh& m, int d, const Arr<LO>& k2e, const Arr<LO>& k2p,
                            const Arr<T>* data, Arr<T>& prod) {
-  // class tags: pairs inherit their split d-entity, cuts their (d+1)-entity
-  // (transfer_inherit_refine, src/Omega_h_transfer.cpp:213-263)
   int dim = m.dim;
   LO nkeys = k2e.size();
-  const LO* ke = k2e.data();
-  const LO* kp = k2p.data();
-  const LO *pa = nullptr, *pb = nullptr, *ca = nullptr, *cb = nullptr;
+  auto ke = cview(k2e);
+  auto kp = cview(k2p);
+  LV pa = {nullptr, 0}, pb = {nullptr, 0}, ca = {nullptr, 0}, cb = {nullptr, 0};
   if (d > EDGE) {
     const Adj& a = m.ask_up(1, d);
-    pa = a.a2ab.data();
-    pb = a.ab2b.data();
+    pa = cview(a.a2ab);
+    pb = cview(a.ab2b);
   }
-  if (d + 1 > EDGE && d < dim) {
+  bool cuts = d < dim, cut_is_edge = d + 1 == EDGE;
+  if (cuts && !cut_is_edge) {
     const Adj& a = m.ask_up(1, d + 1);
-    ca = a.a2ab.data();
-    cb = a.ab2b.data();
+    ca = cview(a.a2ab);
+    cb = cview(a.ab2b);
   }
-  const T* pdat = d > VERT ? data[d].data() : nullptr;
-  const T* cdat = d < dim ? data[d + 1].data() : nullptr;
-  const T* edat = data[1].data();
-  T* o = prod.data();
+  View<const T> pdat = {nullptr, 0}, cdat = {nullptr, 0};
+  if (d > VERT) pdat = cview(data[d]);
+  if (cuts) cdat = cview(data[d + 1]);
+  auto edat = cview(data[1]);
+  auto o = view(prod);
   pfor(nkeys, [=] __device__(LO k) {
     LO e = ke[k];
     LO p = kp[k];
@@ -517,8 +543,8 @@ static void inherit_refine(Mesh& m, int d, const Arr<LO>& k2e, const Arr<LO>& k2
         o[p++] = pdat[pb[x]];
       }
     }
-    if (d < dim) {
-      if (d + 1 == EDGE) {
+    if (cuts) {
+      if (cut_is_edge) {
         o[p++] = cdat[e];
       } else {
         for (LO x = ca[e]; x < ca[e + 1]; ++x) o[p++] = cdat[cb[x]];
@@ -540,17 +566,17 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<I8>& cands, PassStats*
   Arr<double> eq = fill<double>(ne, 0.0);
   Arr<int> anyg = fill<int>(1, 0);
   {
-    const LO* ce = c2e.data();
-    const double* q = cq.data();
-    I8* in = initial.data();
-    double* e = eq.data();
-    int* ag = anyg.data();
+    auto ce = cview(c2e);
+    auto q = cview(cq);
+    auto in = view(initial);
+    auto e = view(eq);
+    auto ag = view(anyg);
     double mqa = o.min_quality_allowed;
     pfor(nc, [=] __device__(LO i) {
       bool g = q[i] >= mqa;
       in[ce[i]] = g;
       e[ce[i]] = q[i];
-      if (g) *ag = 1;
+      if (g) ag[0] = 1;
     });
   }
   if (!get_elem(anyg, 0)) return false;
@@ -583,16 +609,16 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<I8>& cands, PassStats*
     nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
     if (d == VERT) {
       Arr<double> pc(nkeys * dim);
-      const LO* ev = m.ask_verts_of(1).data();
-      const LO* ke = k2e.data();
-      const double* c = m.coords.data();
-      double* p = pc.data();
+      auto ev = cview(m.ask_verts_of(1));
+      auto ke = cview(k2e);
+      auto c = cview(m.coords);
+      auto p = view(pc);
       pfor(nkeys, [=] __device__(LO k) {
         LO e = ke[k];
         for (int j = 0; j < dim; ++j) {
           double comp = 0;
-          comp += c[LO(ev[e * 2]) * dim + j];
-          comp += c[LO(ev[e * 2 + 1]) * dim + j];
+          comp += c[ev[e * 2] * dim + j];
+          comp += c[ev[e * 2 + 1] * dim + j];
           comp /= 2;
           p[k * dim + j] = comp;
         }
@@ -612,8 +638,8 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<I8>& cands, PassStats*
 bool refine_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   const Arr<double>& len = m.ask_lengths();
   Arr<I8> cands(len.size());
-  const double* l = len.data();
-  I8* c = cands.data();
+  auto l = cview(len);
+  auto c = view(cands);
   double mx = o.max_length_desired;
   pfor(len.size(), [=] __device__(LO i) { c[i] = l[i] > mx; });
   if (count_marked(cands) == 0) return false;
@@ -625,10 +651,13 @@ __device__ __forceinline__ bool collapses(I8 code, int v) { return (code & (1 <<
 __device__ __forceinline__ I8 dont_collapse(I8 code, int v) { return I8(code & ~(1 << v)); }
 
 // check_collapse_class (src/Omega_h_check_collapse.cpp:10-45)
-void check_collapse_class(Mesh& m, const LO* c2e, LO n, const I8* ci, I8* co) {
-  const LO* ev = m.ask_verts_of(1).data();
-  const I8* vcd = m.class_dim[0].data();
-  const I8* ecd = m.class_dim[1].data();
+void check_collapse_class(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8* co_p) {
+  auto ev = cview(m.ask_verts_of(1));
+  auto vcd = cview(m.class_dim[0]);
+  auto ecd = cview(m.class_dim[1]);
+  auto c2e = cview(c2e_p, n);
+  auto ci = cview(ci_p, n);
+  auto co = view(co_p, n);
   pfor(n, [=] __device__(LO c) {
     I8 code = ci[c];
     LO e = c2e[c];
@@ -644,18 +673,19 @@ void check_collapse_class(Mesh& m, const LO* c2e, LO n, const I8* ci, I8* co) {
 }
 
 // check_collapse_exposure (src/Omega_h_check_collapse.cpp:69-119)
-void check_collapse_exposure(Mesh& m, const LO* c2e, LO n, const I8* ci, I8* co) {
+void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8* co_p) {
   Arr<I8> tmp(n);
-  const I8* in = ci;
+  auto c2e = cview(c2e_p, n);
+  View<const I8> in = cview(ci_p, n);
   for (int cd = 2; cd <= m.dim; ++cd) {
-    I8* out = cd == m.dim ? co : tmp.data();
+    View<I8> out = cd == m.dim ? view(co_p, n) : view(tmp);
     const Adj& e2c = m.ask_up(1, cd);
-    const LO* ea = e2c.a2ab.data();
-    const LO* eb = e2c.ab2b.data();
-    const I8* ecc = e2c.codes.data();
-    const LO* cs = m.ask_down(cd, cd - 1).ab2b.data();
-    const I8* cdim = m.class_dim[cd].data();
-    const I8* sdim = m.class_dim[cd - 1].data();
+    auto ea = cview(e2c.a2ab);
+    auto eb = cview(e2c.ab2b);
+    auto ecc = cview(e2c.codes);
+    auto cs = cview(m.ask_down(cd, cd - 1).ab2b);
+    auto cdim = cview(m.class_dim[cd]);
+    auto sdim = cview(m.class_dim[cd - 1]);
     int nccs = simplex_degree(cd, cd - 1);
     pfor(n, [=] __device__(LO c) {
       I8 code = in[c];
@@ -673,21 +703,24 @@ void check_collapse_exposure(Mesh& m, const LO* c2e, LO n, const I8* ci, I8* co)
       }
       out[c] = code;
     });
-    in = out;
+    in = {out.p, out.n};
   }
 }
 
 // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
-void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e, LO n, const I8* ci,
-                               I8* co) {
-  const LO* ev = m.ask_verts_of(1).data();
+void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n,
+                               const I8* ci_p, I8* co_p) {
+  auto ev = cview(m.ask_verts_of(1));
   const Adj& v2e = m.ask_up(0, 1);
-  const LO* va = v2e.a2ab.data();
-  const LO* vb = v2e.ab2b.data();
-  const I8* vc = v2e.codes.data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
   int dim = m.dim, mc = m.mcomp();
+  auto c2e = cview(c2e_p, n);
+  auto ci = cview(ci_p, n);
+  auto co = view(co_p, n);
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     I8 code = ci[cand];
@@ -701,9 +734,7 @@ void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e, LO n, 
         LO nv[2];
         nv[ein] = v_onto;
         nv[eout] = ev[e2 * 2 + eout];
-        double len = dim == 3 ? edge_length3(c + nv[0] * 3, c + nv[1] * 3, mt + nv[0] * mc, mt + nv[1] * mc)
-                              : edge_length2(c + nv[0] * 2, c + nv[1] * 2, mt + nv[0] * mc, mt + nv[1] * mc);
-        if (len >= max_length) {
+        if (edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length) {
           code = dont_collapse(code, col);
           break;
         }
@@ -714,16 +745,19 @@ void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e, LO n, 
 }
 
 // coarsen_qualities_tmpl (src/Omega_h_coarsen_qualities.cpp:15-63)
-void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* q2) {
+void coarsen_qualities(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, double* q2_p) {
   int dim = m.dim;
-  const LO* ev = m.ask_verts_of(1).data();
-  const LO* cv = m.ask_verts_of(dim).data();
+  auto ev = cview(m.ask_verts_of(1));
+  auto cv = cview(m.ask_verts_of(dim));
   const Adj& v2c = m.ask_up(0, dim);
-  const LO* va = v2c.a2ab.data();
-  const LO* vb = v2c.ab2b.data();
-  const I8* vc = v2c.codes.data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto va = cview(v2c.a2ab);
+  auto vb = cview(v2c.ab2b);
+  auto vc = cview(v2c.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto codes = cview(codes_p, n);
+  auto q2 = view(q2_p, n * 2);
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     I8 code = codes[cand];
@@ -741,7 +775,7 @@ void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* q2
         for (int k = 0; k <= dim; ++k)
           if (k != ccv_col && vv[k] == v_onto) dies = true;
         if (dies) continue;
-        vv[ccv_col] = v_onto;
+        vv[ccv_col & 3] = v_onto;
         minq = min2d(minq, elem_quality_v(dim, c, mt, vv));
       }
       q2[cand * 2 + col] = minq;
@@ -750,17 +784,27 @@ void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* q2
 }
 
 // choose_rails (src/Omega_h_collapse_rail.cpp:15-67)
-void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,
-                  I8* vcand, double* vqual, GO* vrail) {
+void choose_rails(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, const double* quals2_p,
+                  I8* vcand_p, double* vqual_p, GO* vrail_p) {
+  LO nv = m.nverts();
   Arr<LO> e2c = fill<LO>(m.nedges(), -1);
-  LO* ec = e2c.data();
-  pfor(n, [=] __device__(LO i) { ec[c2e[i]] = i; });
+  auto c2e = cview(c2e_p, n);
+  {
+    auto ec = view(e2c);
+    pfor(n, [=] __device__(LO i) { ec[c2e[i]] = i; });
+  }
   const Adj& v2e = m.ask_up(0, 1);
-  const LO* va = v2e.a2ab.data();
-  const LO* vb = v2e.ab2b.data();
-  const I8* vc = v2e.codes.data();
-  const double* len = m.ask_lengths().data();
-  pfor(m.nverts(), [=] __device__(LO v) {
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto len = cview(m.ask_lengths());
+  auto ec = cview(e2c);
+  auto codes = cview(codes_p, n);
+  auto quals2 = cview(quals2_p, n * 2);
+  auto vcand = view(vcand_p, nv);
+  auto vqual = view(vqual_p, nv);
+  auto vrail = view(vrail_p, nv);
+  pfor(nv, [=] __device__(LO v) {
     bool is_cand = false;
     GO best_g = -1;
     double best_l = -1, best_q = -1;
@@ -797,8 +841,8 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   LO ne = m.nedges();
   Arr<I8> ecand(ne);
   {
-    const double* l = len.data();
-    I8* c = ecand.data();
+    auto l = cview(len);
+    auto c = view(ecand);
     double mn = o.min_length_desired;
     pfor(ne, [=] __device__(LO i) { c[i] = l[i] < mn; });
   }
@@ -806,9 +850,9 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   Arr<I8> vm = mark_down(m, EDGE, VERT, ecand);
   Arr<I8> ecodes(ne);
   {
-    const LO* ev = m.ask_verts_of(1).data();
-    const I8* v = vm.data();
-    I8* ec = ecodes.data();
+    auto ev = cview(m.ask_verts_of(1));
+    auto v = cview(vm);
+    auto ec = view(ecodes);
     pfor(ne, [=] __device__(LO e) { ec[e] = I8((v[ev[e * 2]] ? 1 : 0) | (v[ev[e * 2 + 1]] ? 2 : 0)); });
   }
   Arr<LO> c2e = collect_marked(ecodes);
@@ -831,8 +875,8 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   Arr<double> q2(nc * 2);
   coarsen_qualities(m, c2e.data(), nc, codes.data(), q2.data());
   {
-    I8* cd = codes.data();
-    const double* q = q2.data();
+    auto cd = view(codes);
+    auto q = cview(q2);
     double mqa = o.min_quality_allowed;
     pfor(nc, [=] __device__(LO i) {
       I8 code = cd[i];
@@ -858,31 +902,34 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   Arr<LO> k2onto(nkeys);
   {
     const Adj& v2e = m.ask_up(0, 1);
-    const LO* va = v2e.a2ab.data();
-    const LO* vb = v2e.ab2b.data();
-    const I8* vcd = v2e.codes.data();
-    const LO* kv = k2v.data();
-    const GO* rail = vr.data();
-    const LO* ev = m.ask_verts_of(1).data();
-    LO* re = r2e.data();
-    I8* rd = rdir.data();
-    LO* ko = k2onto.data();
+    auto va = cview(v2e.a2ab);
+    auto vb = cview(v2e.ab2b);
+    auto vcd = cview(v2e.codes);
+    auto kv = cview(k2v);
+    auto rail = cview(vr);
+    auto ev = cview(m.ask_verts_of(1));
+    auto re = view(r2e);
+    auto rd = view(rdir);
+    auto ko = view(k2onto);
     int* stw = ctx().d_status;
     pfor(nkeys, [=] __device__(LO k) {
       LO v = kv[k];
-      re[k] = -1;
+      LO fe = -1;
+      I8 fd = 0;
       for (LO x = va[v]; x < va[v + 1]; ++x)
         if (GO(vb[x]) == rail[v]) {
-          re[k] = vb[x];
-          rd[k] = I8(code_which_down(vcd[x]));
+          fe = vb[x];
+          fd = I8(code_which_down(vcd[x]));
           break;
         }
-      if (re[k] < 0) {
+      if (fe < 0) {
         raise_status(stw, ST_TOPOLOGY);
-        re[k] = 0;
-        rd[k] = 0;
+        fe = 0;
+        fd = 0;
       }
-      ko[k] = ev[LO(re[k]) * 2 + (1 - rd[k])];
+      re[k] = fe;
+      rd[k] = fd;
+      ko[k] = ev[fe * 2 + (1 - fd)];
     });
   }
   // mark_dead_ents (src/Omega_h_coarsen_topology.cpp:28-70)
@@ -891,15 +938,15 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   for (int d = 2; d <= dim; ++d) dead[d] = fill<I8>(m.nents[d], 0);
   for (int cd = dim; cd > EDGE; --cd) {
     const Adj& e2c = m.ask_up(1, cd);
-    const LO* ea = e2c.a2ab.data();
-    const LO* eb = e2c.ab2b.data();
-    const I8* ecc = e2c.codes.data();
-    const LO* cs = m.ask_down(cd, cd - 1).ab2b.data();
+    auto ea = cview(e2c.a2ab);
+    auto eb = cview(e2c.ab2b);
+    auto ecc = cview(e2c.codes);
+    auto cs = cview(m.ask_down(cd, cd - 1).ab2b);
     int nccs = simplex_degree(cd, cd - 1);
-    const LO* re = r2e.data();
-    const I8* rd = rdir.data();
-    I8* dc = dead[cd].data();
-    I8* ds = dead[cd - 1].data();
+    auto re = cview(r2e);
+    auto rd = cview(rdir);
+    auto dc = view(dead[cd]);
+    auto ds = view(dead[cd - 1]);
     pfor(nkeys, [=] __device__(LO r) {
       LO e = re[r];
       int onto = 1 - rd[r];
@@ -923,13 +970,13 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
     } else {
       // find_coarsen_domains: live d-entities around each key vertex
       const Adj& v2d = m.ask_up(0, d);
-      const LO* va = v2d.a2ab.data();
-      const LO* vb = v2d.ab2b.data();
-      const I8* vcd = v2d.codes.data();
-      const I8* dd = dead[d].data();
-      const LO* kv = k2v.data();
+      auto va = cview(v2d.a2ab);
+      auto vb = cview(v2d.ab2b);
+      auto vcd = cview(v2d.codes);
+      auto dd = cview(dead[d]);
+      auto kv = cview(k2v);
       Arr<LO> cnt(nkeys);
-      LO* ct = cnt.data();
+      auto ct = view(cnt);
       pfor(nkeys, [=] __device__(LO k) {
         LO v = kv[k], n2 = 0;
         for (LO x = va[v]; x < va[v + 1]; ++x) n2 += !dd[vb[x]];
@@ -940,12 +987,12 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
       kd2d = Arr<LO>(nprod);
       int nccv = d + 1;
       pv2v = Arr<LO>(nprod * nccv);
-      const LO* kp = k2p.data();
-      const LO* cv = m.ask_verts_of(d).data();
-      const LO* ko = k2onto.data();
-      const LO* o2n = ov2nv.data();
-      LO* kd = kd2d.data();
-      LO* pv = pv2v.data();
+      auto kp = cview(k2p);
+      auto cv = cview(m.ask_verts_of(d));
+      auto ko = cview(k2onto);
+      auto o2n = cview(ov2nv);
+      auto kd = view(kd2d);
+      auto pv = view(pv2v);
       pfor(nkeys, [=] __device__(LO k) {
         LO v = kv[k], p = kp[k];
         for (LO x = va[v]; x < va[v + 1]; ++x) {
@@ -987,8 +1034,11 @@ __constant__ SwapTables c_swap;
 static void upload_swap_tables() {
   static bool done = false;
   if (done) return;
-  SwapTables t;
-  for (int i = 0; i < 8; ++i) t.nmesh[i] = t.ntri[i] = t.nedge[i] = 0;
+  static SwapTables t;
+  for (int i = 0; i < 8; ++i) {
+    t.nmesh[i] = t.ntri[i] = t.nedge[i] = 0;
+    t.off_tri[i] = t.off_mesh[i] = t.off_uedge[i] = t.off_e2u[i] = 0;
+  }
   int p = 0;
   while (p < OHG_SWAP3D_TABLE_LEN) {
     int n = OHG_SWAP3D_TABLE[p], nm = OHG_SWAP3D_TABLE[p + 1], nt = OHG_SWAP3D_TABLE[p + 2],
@@ -1009,8 +1059,14 @@ static void upload_swap_tables() {
     p += nm * nedge;
   }
   for (int i = 0; i < OHG_SWAP3D_TABLE_LEN; ++i) t.data[i] = OHG_SWAP3D_TABLE[i];
-  OHG_CUDA(cudaMemcpyToSymbolAsync(c_swap, &t, sizeof(t), 0, cudaMemcpyHostToDevice, ctx().stream));
+  OHG_CUDA(cudaMemcpyToSymbol(c_swap, &t, sizeof(t)));
   done = true;
+}
+// table lookups, clamped to the table so a bad index cannot leave it
+__device__ __forceinline__ int swap_tab(int off, int i) {
+  int k = off + i;
+  if (k < 0 || k >= OHG_SWAP3D_TABLE_LEN) k = 0;
+  return c_swap.data[k];
 }
 
 struct Loop {
@@ -1019,12 +1075,15 @@ struct Loop {
   LO lv[7];
 };
 // swap3d::find_loop (src/Omega_h_swap3d_loop.hpp:24-78)
-__device__ __forceinline__ Loop find_loop(const LO* ea, const LO* eb, const I8* ec, const LO* ev,
-                                          const LO* tv, LO edge, int* st) {
+__device__ __forceinline__ Loop find_loop(LV ea, LV eb, View<const I8> ec, LV ev, LV tv, LO edge,
+                                          int* st) {
   Loop loop;
   LO b = ea[edge], e = ea[edge + 1];
   loop.size = e - b;
-  if (loop.size > 7) return loop;
+  if (loop.size > 7 || loop.size < 3) {
+    loop.size = 8;
+    return loop;
+  }
   loop.eev2v[0] = ev[edge * 2];
   loop.eev2v[1] = ev[edge * 2 + 1];
   LO t0[7], t1[7];
@@ -1057,16 +1116,20 @@ __device__ __forceinline__ Loop find_loop(const LO* ea, const LO* eb, const I8* 
 
 // swap3d_qualities + swap3d::choose (src/Omega_h_swap3d_qualities.cpp:10-58,
 // src/Omega_h_swap3d_choice.hpp:15-100)
-void swap3d_qualities(Mesh& m, double max_len, const LO* c2e, LO n, double* quals, I8* configs) {
+void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p,
+                      I8* configs_p) {
   upload_swap_tables();
   const Adj& e2t = m.ask_up(1, 3);
-  const LO* ea = e2t.a2ab.data();
-  const LO* eb = e2t.ab2b.data();
-  const I8* ec = e2t.codes.data();
-  const LO* ev = m.ask_verts_of(1).data();
-  const LO* tv = m.ask_verts_of(3).data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto ea = cview(e2t.a2ab);
+  auto eb = cview(e2t.ab2b);
+  auto ec = cview(e2t.codes);
+  auto ev = cview(m.ask_verts_of(1));
+  auto tv = cview(m.ask_verts_of(3));
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto quals = view(quals_p, n);
+  auto configs = view(configs_p, n);
   int* st = ctx().d_status;
   pfor(n, [=] __device__(LO cand) {
     Loop loop = find_loop(ea, eb, ec, ev, tv, c2e[cand], st);
@@ -1075,10 +1138,8 @@ void swap3d_qualities(Mesh& m, double max_len, const LO* c2e, LO n, double* qual
     if (loop.size > 7) return;
     int ls = loop.size;
     int nmeshes = c_swap.nmesh[ls], ntris = c_swap.ntri[ls], nedges = c_swap.nedge[ls];
-    const int* tri = c_swap.data + c_swap.off_tri[ls];
-    const int* msh = c_swap.data + c_swap.off_mesh[ls];
-    const int* ued = c_swap.data + c_swap.off_uedge[ls];
-    const int* e2u = c_swap.data + c_swap.off_e2u[ls];
+    int otri = c_swap.off_tri[ls], omsh = c_swap.off_mesh[ls];
+    int oued = c_swap.off_uedge[ls], oe2u = c_swap.off_e2u[ls];
     unsigned long long tcached = 0;
     unsigned ecached = 0;
     double tq[35];
@@ -1088,10 +1149,11 @@ void swap3d_qualities(Mesh& m, double max_len, const LO* c2e, LO n, double* qual
     for (int mesh = 0; mesh < nmeshes; ++mesh) {
       double mq = 1.0;
       for (int t = 0; t < ntris; ++t) {
-        int u = msh[mesh * ntris + t];
+        int u = swap_tab(omsh, mesh * ntris + t);
+        if (u < 0 || u >= 35) u = 0;
         if (!((tcached >> u) & 1ull)) {
           LO tet[4];
-          for (int k = 0; k < 3; ++k) tet[k] = loop.lv[tri[u * 3 + k]];
+          for (int k = 0; k < 3; ++k) tet[k] = loop.lv[swap_tab(otri, u * 3 + k) % 7];
           double tmq = 1.0;
           for (int tt = 0; tt < 2; ++tt) {
             tet[3] = loop.eev2v[1 - tt];
@@ -1109,10 +1171,11 @@ void swap3d_qualities(Mesh& m, double max_len, const LO* c2e, LO n, double* qual
       if (mq > bestq) {
         bool over = false;
         for (int me = 0; me < nedges; ++me) {
-          int ue = e2u[mesh * nedges + me];
+          int ue = swap_tab(oe2u, mesh * nedges + me);
+          if (ue < 0 || ue >= 26) ue = 0;
           if (!((ecached >> ue) & 1u)) {
-            LO a = loop.lv[ued[ue * 2]], b = loop.lv[ued[ue * 2 + 1]];
-            el[ue] = edge_length3(c + a * 3, c + b * 3, mt + a * 6, mt + b * 6);
+            LO a = loop.lv[swap_tab(oued, ue * 2) % 7], b = loop.lv[swap_tab(oued, ue * 2 + 1) % 7];
+            el[ue] = edge_len_v(3, c, mt, 6, a, b);
             ecached |= (1u << ue);
           }
           if (el[ue] > max_len) {
@@ -1137,19 +1200,21 @@ Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
   const Arr<double>& q = m.ask_qualities();
   LO ne = m.nelems();
   Arr<I8> a(ne), b(ne);
-  const double* qq = q.data();
-  I8* s = a.data();
-  pfor(ne, [=] __device__(LO i) { s[i] = qq[i] < ceil; });
+  {
+    auto qq = cview(q);
+    auto s = view(a);
+    pfor(ne, [=] __device__(LO i) { s[i] = qq[i] < ceil; });
+  }
   const Adj& dual = m.ask_adj(m.dim, m.dim);
-  const LO* da = dual.a2ab.data();
-  const LO* db = dual.ab2b.data();
+  auto da = cview(dual.a2ab);
+  auto db = cview(dual.ab2b);
   for (int l = 0; l < nlayers; ++l) {
-    const I8* o = a.data();
-    I8* nw = b.data();
+    auto o = cview(a);
+    auto nw = view(b);
     pfor(ne, [=] __device__(LO e) {
-      I8 r = -128;
-      for (LO x = da[e]; x < da[e + 1]; ++x) r = max(r, o[db[x]]);
-      nw[e] = r;
+      int r = -128;
+      for (LO x = da[e]; x < da[e + 1]; ++x) r = max(r, int(o[db[x]]));
+      nw[e] = I8(r);
     });
     std::swap(a, b);
   }
@@ -1158,11 +1223,12 @@ Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
 
 bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   if (m.dim != 3) return false;
+  upload_swap_tables();
   Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
   Arr<I8> edc = mark_down(m, 3, 1, ec);
   {
-    I8* e = edc.data();
-    const I8* cd = m.class_dim[1].data();
+    auto e = view(edc);
+    auto cd = cview(m.class_dim[1]);
     pfor(m.nedges(), [=] __device__(LO i) { e[i] = e[i] && cd[i] == 3; });
   }
   if (count_marked(edc) == 0) return false;
@@ -1176,13 +1242,13 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   // filter_swap_improve (src/Omega_h_swap.cpp:35-43)
   Arr<I8> keep(nc);
   {
-    const double* eq = m.ask_qualities().data();
+    auto eq = cview(m.ask_qualities());
     const Adj& e2t = m.ask_up(1, 3);
-    const LO* ea = e2t.a2ab.data();
-    const LO* eb = e2t.ab2b.data();
-    const LO* ce = c2e.data();
-    const double* q = cq.data();
-    I8* kp = keep.data();
+    auto ea = cview(e2t.a2ab);
+    auto eb = cview(e2t.ab2b);
+    auto ce = cview(c2e);
+    auto q = cview(cq);
+    auto kp = view(keep);
     pfor(nc, [=] __device__(LO i) {
       LO e = ce[i];
       double old = DBL_MAX;
@@ -1202,17 +1268,17 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   st->swap_keys = nkeys;
   // swap3d_keys_to_prods + swap3d_topology (src/Omega_h_swap3d_topology.cpp)
   const Adj& e2t = m.ask_up(1, 3);
-  const LO* ea = e2t.a2ab.data();
+  auto ea = cview(e2t.a2ab);
   Arr<LO> cnt[4], k2p[4], pv2v[4];
   for (int d = 1; d <= 3; ++d) cnt[d] = Arr<LO>(nkeys);
   {
-    const LO* ke = k2e.data();
-    LO* c1 = cnt[1].data();
-    LO* c2 = cnt[2].data();
-    LO* c3 = cnt[3].data();
+    auto ke = cview(k2e);
+    auto c1 = view(cnt[1]);
+    auto c2 = view(cnt[2]);
+    auto c3 = view(cnt[3]);
     pfor(nkeys, [=] __device__(LO k) {
       int ls = ea[ke[k] + 1] - ea[ke[k]];
-      if (ls > 7) ls = 0;
+      if (ls > 7 || ls < 0) ls = 0;
       int npt = c_swap.ntri[ls], npe = c_swap.nedge[ls];
       c1[k] = npe;
       c2[k] = npt + 2 * npe;
@@ -1224,25 +1290,25 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     pv2v[d] = Arr<LO>(last(k2p[d]) * (d + 1));
   }
   {
-    const LO* eb = e2t.ab2b.data();
-    const I8* ecd = e2t.codes.data();
-    const LO* ev = m.ask_verts_of(1).data();
-    const LO* tv = m.ask_verts_of(3).data();
-    const LO* ke = k2e.data();
-    const I8* cfg = econfig.data();
-    const LO* p1 = k2p[1].data();
-    const LO* p2 = k2p[2].data();
-    const LO* p3 = k2p[3].data();
-    LO* v1 = pv2v[1].data();
-    LO* v2 = pv2v[2].data();
-    LO* v3 = pv2v[3].data();
+    auto eb = cview(e2t.ab2b);
+    auto ecd = cview(e2t.codes);
+    auto ev = cview(m.ask_verts_of(1));
+    auto tv = cview(m.ask_verts_of(3));
+    auto ke = cview(k2e);
+    auto cfg = cview(econfig);
+    auto p1 = cview(k2p[1]);
+    auto p2 = cview(k2p[2]);
+    auto p3 = cview(k2p[3]);
+    auto v1 = view(pv2v[1]);
+    auto v2 = view(pv2v[2]);
+    auto v3 = view(pv2v[3]);
     int* stw = ctx().d_status;
     pfor(nkeys, [=] __device__(LO k) {
       Loop loop = find_loop(ea, eb, ecd, ev, tv, ke[k], stw);
       int config = cfg[ke[k]];
-      if (loop.size > 7 || loop.size < 3 || config < 0 || config >= c_swap.nmesh[loop.size]) {
-        // no valid configuration: products get the key edge's own vertices
-        // (valid indices) and the status word reports the failure
+      if (loop.size > 7 || config < 0 || config >= c_swap.nmesh[loop.size]) {
+        // no valid configuration: products get the key edge's own vertex
+        // (a valid index) and the status word reports the failure
         raise_status(stw, ST_TOPOLOGY);
         LO a = ev[ke[k] * 2];
         for (LO p = p1[k] * 2; p < p1[k + 1] * 2; ++p) v1[p] = a;
@@ -1252,13 +1318,11 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
       }
       int ls = loop.size;
       int npt = c_swap.ntri[ls], npe = c_swap.nedge[ls];
-      const int* tri = c_swap.data + c_swap.off_tri[ls];
-      const int* msh = c_swap.data + c_swap.off_mesh[ls];
-      const int* ued = c_swap.data + c_swap.off_uedge[ls];
-      const int* e2u = c_swap.data + c_swap.off_e2u[ls];
+      int otri = c_swap.off_tri[ls], omsh = c_swap.off_mesh[ls];
+      int oued = c_swap.off_uedge[ls], oe2u = c_swap.off_e2u[ls];
       for (int pe = 0; pe < npe; ++pe) {
-        int ue = e2u[config * npe + pe];
-        LO a = loop.lv[ued[ue * 2]], b = loop.lv[ued[ue * 2 + 1]];
+        int ue = swap_tab(oe2u, config * npe + pe);
+        LO a = loop.lv[swap_tab(oued, ue * 2) % 7], b = loop.lv[swap_tab(oued, ue * 2 + 1) % 7];
         LO pedge = p1[k] + pe;
         v1[pedge * 2] = a;
         v1[pedge * 2 + 1] = b;
@@ -1270,8 +1334,10 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
         }
       }
       for (int pt = 0; pt < npt; ++pt) {
-        int ut = msh[config * npt + pt];
-        LO t0 = loop.lv[tri[ut * 3]], t1 = loop.lv[tri[ut * 3 + 1]], t2 = loop.lv[tri[ut * 3 + 2]];
+        int ut = swap_tab(omsh, config * npt + pt);
+        LO t0 = loop.lv[swap_tab(otri, ut * 3) % 7];
+        LO t1 = loop.lv[swap_tab(otri, ut * 3 + 1) % 7];
+        LO t2 = loop.lv[swap_tab(otri, ut * 3 + 2) % 7];
         LO ptri = p2[k] + 2 * npe + pt;
         v2[ptri * 3] = t0;
         v2[ptri * 3 + 1] = t1;
@@ -1303,12 +1369,12 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     Arr<I8> pcd(np);
     Arr<LO> pci(np);
     {
-      const LO* ke = k2e.data();
-      const LO* kp = k2p[d].data();
-      const I8* ecd = m.class_dim[1].data();
-      const LO* eci = m.class_id[1].data();
-      I8* a = pcd.data();
-      LO* b = pci.data();
+      auto ke = cview(k2e);
+      auto kp = cview(k2p[d]);
+      auto ecd = cview(m.class_dim[1]);
+      auto eci = cview(m.class_id[1]);
+      auto a = view(pcd);
+      auto b = view(pci);
       pfor(nkeys, [=] __device__(LO k) {
         for (LO p = kp[k]; p < kp[k + 1]; ++p) {
           a[p] = ecd[ke[k]];

@@ -317,8 +317,8 @@ static bool named_array(Mesh& me, const std::string& name, const void** p, long 
     if (kind == "up_codes_") return set(a.codes.data(), a.codes.size() * 1LL);
     return false;
   }
-  if (name.rfind("star_", 0) == 0 && name.size() == 12) {
-    int d = num(11);
+  if (name.rfind("star_", 0) == 0 && name.size() == 11) {
+    int d = num(10);
     if (d < 0 || d > 1 || d >= dim) return false;
     const Adj& a = me.ask_adj(d, d);
     if (name.substr(0, 10) == "star_a2ab_") return set(a.a2ab.data(), a.a2ab.size() * 4LL);

@@ -102,6 +102,58 @@ void Arr<T>::alloc(LO count) {
   ptr = static_cast<T*>(buf->p);
 }
 
+// ------------------------------------------------------------ device views
+// A device array view.  In builds with OHG_CHECKED every subscript is bounds
+// checked: an out-of-range index is recorded (first one wins) and the access
+// is redirected to a scratch slot instead of touching memory outside the
+// array; the launch helper then reports the kernel's source line.
+struct BoundsRecord {
+  int hit;
+  long long index, size;
+};
+#ifdef OHG_CHECKED
+// one record per translation unit (no relocatable device code)
+static __device__ BoundsRecord g_bounds;
+static __device__ double g_bounds_scratch[4];
+#endif
+
+template <class T>
+struct View {
+  T* p;
+  LO n;
+  __host__ __device__ __forceinline__ T& operator[](LO i) const {
+#ifdef OHG_CHECKED
+#ifdef __CUDA_ARCH__
+    if (i < 0 || i >= n) {
+      if (atomicCAS(&g_bounds.hit, 0, 1) == 0) {
+        g_bounds.index = i;
+        g_bounds.size = n;
+      }
+      return *reinterpret_cast<T*>(g_bounds_scratch);
+    }
+#endif
+#endif
+    return p[i];
+  }
+  __host__ __device__ __forceinline__ T* ptr() const { return p; }
+};
+template <class T>
+View<T> view(const Arr<T>& a) {
+  return {a.data(), a.size()};
+}
+template <class T>
+View<T> view(T* p, LO n) {
+  return {p, n};
+}
+template <class T>
+View<const T> cview(const Arr<T>& a) {
+  return {a.data(), a.size()};
+}
+template <class T>
+View<const T> cview(const T* p, LO n) {
+  return {p, n};
+}
+
 // ------------------------------------------------------------ launches
 constexpr int kBlock = 256;
 
@@ -111,13 +163,39 @@ __global__ void k_for(LO n, F f) {
   if (i < n) f(i);
 }
 
+// checked builds: synchronise after a launch and report a bounds record or
+// launch error together with the launching source line
+#ifdef OHG_CHECKED
+static inline void checked_after_launch(const char* file, int line) {
+  Ctx& c = ctx();
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  BoundsRecord r;
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&r, g_bounds, sizeof(r));
+  if (e != cudaSuccess) cuda_fail(e, "kernel launch", file, line);
+  if (r.hit) {
+    BoundsRecord z = {0, 0, 0};
+    cudaMemcpyToSymbol(g_bounds, &z, sizeof(z));
+    throw Error(2, std::string("index ") + std::to_string(r.index) + " outside [0," +
+                       std::to_string(r.size) + ") in kernel launched at " + file + ":" +
+                       std::to_string(line));
+  }
+}
+#endif
+
 template <class F>
-inline void pfor(LO n, F f) {
+inline void pfor_at(const char* file, int line, LO n, F f) {
   if (n <= 0) return;
   Ctx& c = ctx();
   k_for<<<(n + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(n, f);
   ++c.launches;
+#ifdef OHG_CHECKED
+  checked_after_launch(file, line);
+#else
+  (void)file;
+  (void)line;
+#endif
 }
+#define pfor(n, ...) ::ohg::pfor_at(__FILE__, __LINE__, (n), __VA_ARGS__)
 
 // device status helper
 __device__ inline void raise_status(int* st, int bits) { atomicOr(st, bits); }

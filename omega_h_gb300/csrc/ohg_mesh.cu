@@ -17,8 +17,8 @@ namespace ohg {
 Adj invert_adj(const Adj& down, int k, LO nlows) {
   LO nhl = down.ab2b.size();
   Arr<LO> deg = fill<LO>(nlows, 0);
-  const LO* hl2l = down.ab2b.data();
-  LO* dg = deg.data();
+  auto hl2l = cview(down.ab2b);
+  auto dg = view(deg);
   pfor(nhl, [=] __device__(LO hl) { atomicAdd(&dg[hl2l[hl]], 1); });
   Adj up;
   up.a2ab = offset_scan(deg);
@@ -27,15 +27,16 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   up.codes = Arr<I8>(nhl);
   up.has_codes = true;
   Arr<LO> pos = fill<LO>(nlows, 0);
-  const LO* off = up.a2ab.data();
-  LO* ps = pos.data();
-  LO* lh2hl = up.ab2b.data();
+  auto off = cview(up.a2ab);
+  auto ps = view(pos);
+  auto lh2hl = view(up.ab2b);
   pfor(nhl, [=] __device__(LO hl) {
     LO l = hl2l[hl];
     lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl;
   });
-  const I8* dc = down.has_codes ? down.codes.data() : nullptr;
-  I8* codes = up.codes.data();
+  bool has_dc = down.has_codes;
+  auto dc = cview(down.codes);
+  auto codes = view(up.codes);
   pfor(nlows, [=] __device__(LO l) {
     LO b = off[l], e = off[l + 1];
     for (LO j = b + 1; j < e; ++j) {
@@ -50,7 +51,7 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
     for (LO j = b; j < e; ++j) {
       LO hl = lh2hl[j];
       int wd = hl % k;
-      if (dc) {
+      if (has_dc) {
         I8 c = dc[hl];
         codes[j] = make_code(code_is_flipped(c), code_rotation(c), wd);
       } else {
@@ -65,8 +66,8 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
 Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
   int nvh = hd + 1, nvl = ld + 1, nlh = simplex_degree(hd, ld);
   Arr<LO> uv2v(nh * nlh * nvl);
-  const LO* h = hv2v.data();
-  LO* u = uv2v.data();
+  auto h = cview(hv2v);
+  auto u = view(uv2v);
   pfor(nh * nlh, [=] __device__(LO hu) {
     LO hh = hu / nlh;
     int uu = hu % nlh;
@@ -86,13 +87,14 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
     out.codes = Arr<I8>(na);
     out.has_codes = true;
   }
-  const LO* h = hv2v.data();
-  const LO* lv = lv2v.data();
-  const LO* va = v2l.a2ab.data();
-  const LO* vb = v2l.ab2b.data();
-  const I8* vc = v2l.codes.data();
-  LO* o = out.ab2b.data();
-  I8* oc = ld > 0 ? out.codes.data() : nullptr;
+  auto h = cview(hv2v);
+  auto lv = cview(lv2v);
+  auto va = cview(v2l.a2ab);
+  auto vb = cview(v2l.ab2b);
+  auto vc = cview(v2l.codes);
+  auto o = view(out.ab2b);
+  bool with_codes = ld > 0;
+  auto oc = view(out.codes);
   int* st = ctx().d_status;
   pfor(na, [=] __device__(LO a) {
     LO hh = a / nlh;
@@ -104,19 +106,19 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
     for (LO x = va[fv]; x < va[fv + 1]; ++x) {
       LO b = vb[x];
       int wd = code_which_down(vc[x]);
-      const LO* bv = lv + LO(b) * deg;
+      LO bb = b * deg;
       I8 mc = 0;
       bool match = false;
       if (deg == 2) {
-        if (av[1] == bv[1 - wd]) {
+        if (av[1] == lv[bb + (1 - wd)]) {
           mc = make_code(false, wd, 0);
           match = true;
         }
       } else {
-        if (av[1] == bv[(wd + 1) % 3] && av[2] == bv[(wd + 2) % 3]) {
+        if (av[1] == lv[bb + (wd + 1) % 3] && av[2] == lv[bb + (wd + 2) % 3]) {
           mc = make_code(false, rotation_to_first(3, wd), 0);
           match = true;
-        } else if (av[1] == bv[(wd + 2) % 3] && av[2] == bv[(wd + 1) % 3]) {
+        } else if (av[1] == lv[bb + (wd + 2) % 3] && av[2] == lv[bb + (wd + 1) % 3]) {
           mc = make_code(true, rotation_to_first(3, wd), 0);
           match = true;
         }
@@ -124,12 +126,15 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
       if (match) {
         ++found;
         o[a] = b;
-        if (oc) oc[a] = mc;
+        if (with_codes) oc[a] = mc;
       }
     }
     if (found != 1) {
       raise_status(st, ST_NO_MATCH);
-      if (!found) o[a] = 0;
+      if (!found) {
+        o[a] = 0;
+        if (with_codes) oc[a] = 0;
+      }
     }
   });
   return out;
@@ -141,16 +146,17 @@ Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh) {
   int nmh = simplex_degree(hd, md), nlm = simplex_degree(md, ld), nlh = simplex_degree(hd, ld);
   Adj out;
   out.ab2b = Arr<LO>(nh * nlh);
-  if (ld == 1) {
+  bool with_codes = ld == 1;
+  if (with_codes) {
     out.codes = Arr<I8>(nh * nlh);
     out.has_codes = true;
   }
-  const LO* hm = h2m.ab2b.data();
-  const I8* hmc = h2m.codes.data();
-  const LO* ml = m2l.ab2b.data();
-  const I8* mlc = ld == 1 ? m2l.codes.data() : nullptr;
-  LO* o = out.ab2b.data();
-  I8* oc = ld == 1 ? out.codes.data() : nullptr;
+  auto hm = cview(h2m.ab2b);
+  auto hmc = cview(h2m.codes);
+  auto ml = cview(m2l.ab2b);
+  auto mlc = cview(m2l.codes);
+  auto o = view(out.ab2b);
+  auto oc = view(out.codes);
   pfor(nh * nlh, [=] __device__(LO x) {
     LO h = x / nlh;
     int hl = x % nlh;
@@ -159,7 +165,7 @@ Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh) {
     I8 hm2m = invert_alignment(nlm, hmc[h * nmh + ut.up]);
     int mli = align_index(nlm, ld, ut.which_down, hm2m);
     o[x] = ml[m * nlm + mli];
-    if (oc) {
+    if (with_codes) {
       bool f = code_is_flipped(hm2m) ^ (code_rotation(mlc[m * nlm + mli]) == 1) ^ ut.is_flipped;
       oc[x] = make_code(false, f, 0);
     }
@@ -173,29 +179,29 @@ static Adj verts_across_edges(const Adj& e2v, const Adj& v2e) {
   g.a2ab = v2e.a2ab;
   g.has_a2ab = true;
   g.ab2b = Arr<LO>(v2e.ab2b.size());
-  const LO* ev = e2v.ab2b.data();
-  const LO* ve = v2e.ab2b.data();
-  const I8* vc = v2e.codes.data();
-  LO* o = g.ab2b.data();
+  auto ev = cview(e2v.ab2b);
+  auto ve = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto o = view(g.ab2b);
   pfor(v2e.ab2b.size(), [=] __device__(LO x) {
-    o[x] = ev[LO(ve[x]) * 2 + (1 - code_which_down(vc[x]))];
+    o[x] = ev[ve[x] * 2 + (1 - code_which_down(vc[x]))];
   });
   return g;
 }
 static Adj edges_across_tris(const Adj& f2e, const Adj& e2f, LO ne) {
   Adj g;
   Arr<LO> deg(ne);
-  const LO* ea = e2f.a2ab.data();
-  LO* dg = deg.data();
+  auto ea = cview(e2f.a2ab);
+  auto dg = view(deg);
   pfor(ne, [=] __device__(LO e) { dg[e] = 2 * (ea[e + 1] - ea[e]); });
   g.a2ab = offset_scan(deg);
   g.has_a2ab = true;
   g.ab2b = Arr<LO>(last(g.a2ab));
-  const LO* ga = g.a2ab.data();
-  const LO* ef = e2f.ab2b.data();
-  const I8* efc = e2f.codes.data();
-  const LO* fe = f2e.ab2b.data();
-  LO* o = g.ab2b.data();
+  auto ga = cview(g.a2ab);
+  auto ef = cview(e2f.ab2b);
+  auto efc = cview(e2f.codes);
+  auto fe = cview(f2e.ab2b);
+  auto o = view(g.ab2b);
   pfor(ne, [=] __device__(LO e) {
     LO kk = ga[e];
     for (LO x = ea[e]; x < ea[e + 1]; ++x) {
@@ -212,29 +218,29 @@ static Adj edges_across_tets(const Adj& r2e, const Adj& e2r) {
   g.a2ab = e2r.a2ab;
   g.has_a2ab = true;
   g.ab2b = Arr<LO>(e2r.ab2b.size());
-  const LO* er = e2r.ab2b.data();
-  const I8* erc = e2r.codes.data();
-  const LO* re = r2e.ab2b.data();
-  LO* o = g.ab2b.data();
+  auto er = cview(e2r.ab2b);
+  auto erc = cview(e2r.codes);
+  auto re = cview(r2e.ab2b);
+  auto o = view(g.ab2b);
   pfor(e2r.ab2b.size(), [=] __device__(LO x) {
-    o[x] = re[LO(er[x]) * 6 + opposite_template(3, 1, code_which_down(erc[x]))];
+    o[x] = re[er[x] * 6 + opposite_template(3, 1, code_which_down(erc[x]))];
   });
   return g;
 }
 static Adj add_edges(const Adj& g1, const Adj& g2, LO nv) {
   Adj g;
   Arr<LO> deg(nv);
-  const LO* a1 = g1.a2ab.data();
-  const LO* a2 = g2.a2ab.data();
-  LO* dg = deg.data();
+  auto a1 = cview(g1.a2ab);
+  auto a2 = cview(g2.a2ab);
+  auto dg = view(deg);
   pfor(nv, [=] __device__(LO v) { dg[v] = (a1[v + 1] - a1[v]) + (a2[v + 1] - a2[v]); });
   g.a2ab = offset_scan(deg);
   g.has_a2ab = true;
   g.ab2b = Arr<LO>(last(g.a2ab));
-  const LO* ga = g.a2ab.data();
-  const LO* b1 = g1.ab2b.data();
-  const LO* b2 = g2.ab2b.data();
-  LO* o = g.ab2b.data();
+  auto ga = cview(g.a2ab);
+  auto b1 = cview(g1.ab2b);
+  auto b2 = cview(g2.ab2b);
+  auto o = view(g.ab2b);
   pfor(nv, [=] __device__(LO v) {
     LO kk = ga[v];
     for (LO j = a1[v]; j < a1[v + 1]; ++j) o[kk++] = b1[j];
@@ -244,11 +250,11 @@ static Adj add_edges(const Adj& g1, const Adj& g2, LO nv) {
 }
 static Adj elements_across_sides(int dim, const Adj& e2s, const Adj& s2e, LO ne) {
   int nse = dim + 1;
-  const LO* es = e2s.ab2b.data();
-  const LO* sa = s2e.a2ab.data();
-  const LO* sb = s2e.ab2b.data();
+  auto es = cview(e2s.ab2b);
+  auto sa = cview(s2e.a2ab);
+  auto sb = cview(s2e.ab2b);
   Arr<LO> deg(ne);
-  LO* dg = deg.data();
+  auto dg = view(deg);
   pfor(ne, [=] __device__(LO e) {
     int n = 0;
     for (int k = 0; k < nse; ++k) {
@@ -261,8 +267,8 @@ static Adj elements_across_sides(int dim, const Adj& e2s, const Adj& s2e, LO ne)
   g.a2ab = offset_scan(deg);
   g.has_a2ab = true;
   g.ab2b = Arr<LO>(last(g.a2ab));
-  const LO* ga = g.a2ab.data();
-  LO* o = g.ab2b.data();
+  auto ga = cview(g.a2ab);
+  auto o = view(g.ab2b);
   pfor(ne, [=] __device__(LO e) {
     LO kk = ga[e];
     for (int k = 0; k < nse; ++k) {
@@ -295,21 +301,31 @@ void Mesh::drop_cache() {
 const Adj& Mesh::ask_adj(int from, int to) {
   auto it = adj.find({from, to});
   if (it != adj.end()) return it->second;
+  if (from < 0 || to < 0 || from > dim || to > dim) throw Error(8, "bad adjacency dimensions");
   Adj d;
   if (from < to) {
-    d = invert_adj(ask_adj(to, from), simplex_degree(to, from), nents[from]);
+    const Adj& down = ask_adj(to, from);
+    d = invert_adj(down, simplex_degree(to, from), nents[from]);
   } else if (to < from) {
     const Adj& h2m = ask_adj(from, to + 1);
     const Adj& m2l = ask_adj(to + 1, to);
     d = transit(h2m, m2l, from, to, nents[from]);
   } else if (from == dim) {
-    d = elements_across_sides(dim, ask_adj(dim, dim - 1), ask_adj(dim - 1, dim), nents[dim]);
+    const Adj& e2s = ask_adj(dim, dim - 1);
+    const Adj& s2e = ask_adj(dim - 1, dim);
+    d = elements_across_sides(dim, e2s, s2e, nents[dim]);
   } else if (from == VERT) {
-    d = verts_across_edges(ask_adj(EDGE, VERT), ask_adj(VERT, EDGE));
+    const Adj& e2v = ask_adj(EDGE, VERT);
+    const Adj& v2e = ask_adj(VERT, EDGE);
+    d = verts_across_edges(e2v, v2e);
   } else {
-    d = edges_across_tris(ask_adj(FACE, EDGE), ask_adj(EDGE, FACE), nents[EDGE]);
+    const Adj& f2e = ask_adj(FACE, EDGE);
+    const Adj& e2f = ask_adj(EDGE, FACE);
+    d = edges_across_tris(f2e, e2f, nents[EDGE]);
     if (dim == 3) {
-      Adj t = edges_across_tets(ask_adj(REGION, EDGE), ask_adj(EDGE, REGION));
+      const Adj& r2e = ask_adj(REGION, EDGE);
+      const Adj& e2r = ask_adj(EDGE, REGION);
+      Adj t = edges_across_tets(r2e, e2r);
       d = add_edges(d, t, nents[EDGE]);
     }
   }
@@ -324,10 +340,11 @@ Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
   int deg = ld + 1;
   LO nu = uv2v.size() / deg;
   Arr<LO> canon(uv2v.size());
-  const LO* u = uv2v.data();
-  LO* cn = canon.data();
+  auto u = cview(uv2v);
+  auto cn = view(canon);
   pfor(nu, [=] __device__(LO x) {
-    const LO* in = u + x * deg;
+    LO in[3];
+    for (int j = 0; j < deg; ++j) in[j] = u[x * deg + j];
     int min_j = 0;
     LO min_v = in[0];
     for (int j = 1; j < deg; ++j)
@@ -347,8 +364,9 @@ Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
   });
   Arr<LO> s2u = sort_by_keys(canon, deg);
   Arr<I8> jumps(nu);
-  const LO* s = s2u.data();
-  I8* jp = jumps.data();
+  auto s = cview(s2u);
+  auto jp = view(jumps);
+  auto cnr = cview(canon);
   pfor(nu, [=] __device__(LO i) {
     if (i == nu - 1) {
       jp[i] = 1;
@@ -357,14 +375,14 @@ Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
     LO e0 = s[i], e1 = s[i + 1];
     I8 j = 0;
     for (int k = 0; k < deg; ++k)
-      if (cn[e0 * deg + k] != cn[e1 * deg + k]) j = 1;
+      if (cnr[e0 * deg + k] != cnr[e1 * deg + k]) j = 1;
     jp[i] = j;
   });
   Arr<LO> e2s = collect_marked(jumps);
   LO ne = e2s.size();
   Arr<LO> out(ne * deg);
-  const LO* es = e2s.data();
-  LO* o = out.data();
+  auto es = cview(e2s);
+  auto o = view(out);
   pfor(ne, [=] __device__(LO e) {
     LO uu = s[es[e]];
     for (int k = 0; k < deg; ++k) o[e * deg + k] = u[uu * deg + k];
@@ -381,8 +399,8 @@ __device__ __forceinline__ void hex_rot_fwd(LO* v, int n) {
   for (int i = 0; i < n - 1; ++i) v[i + 1] = v[i];
   v[0] = tmp;
 }
-__device__ int hex_case(const LO* hv, LO* hh) {
-  for (int i = 0; i < 8; ++i) hh[i] = hv[i];
+__device__ int hex_case(View<const LO> hv, LO base, LO* hh) {
+  for (int i = 0; i < 8; ++i) hh[i] = hv[base + i];
   int min_i = 0;
   for (int i = 1; i < 8; ++i)
     if (hh[i] < hh[min_i]) min_i = i;
@@ -432,7 +450,7 @@ static Arr<LO> box_elems(int dim, int n, Arr<double>* coords) {
     LO nvx = n + 1, nvxy = nvx * nvx, nv = nvxy * nvx, nxy = n * n, nh = nxy * n;
     double dx = 1.0 / n;
     *coords = Arr<double>(nv * 3);
-    double* c = coords->data();
+    auto c = view(*coords);
     pfor(nv, [=] __device__(LO v) {
       LO ij = v % nvxy, k = v / nvxy, i = ij % nvx, j = ij / nvx;
       c[v * 3 + 0] = i * dx;
@@ -440,32 +458,33 @@ static Arr<LO> box_elems(int dim, int n, Arr<double>* coords) {
       c[v * 3 + 2] = k * dx;
     });
     Arr<LO> hv(nh * 8);
-    LO* h = hv.data();
+    auto h = view(hv);
     pfor(nh, [=] __device__(LO x) {
       LO ij = x % nxy, k = x / nxy, i = ij % n, j = ij / n;
-      LO* o = h + x * 8;
-      o[0] = (k + 0) * nvxy + (j + 0) * nvx + (i + 0);
-      o[1] = (k + 0) * nvxy + (j + 0) * nvx + (i + 1);
-      o[2] = (k + 0) * nvxy + (j + 1) * nvx + (i + 1);
-      o[3] = (k + 0) * nvxy + (j + 1) * nvx + (i + 0);
-      o[4] = (k + 1) * nvxy + (j + 0) * nvx + (i + 0);
-      o[5] = (k + 1) * nvxy + (j + 0) * nvx + (i + 1);
-      o[6] = (k + 1) * nvxy + (j + 1) * nvx + (i + 1);
-      o[7] = (k + 1) * nvxy + (j + 1) * nvx + (i + 0);
+      LO b = x * 8;
+      h[b + 0] = (k + 0) * nvxy + (j + 0) * nvx + (i + 0);
+      h[b + 1] = (k + 0) * nvxy + (j + 0) * nvx + (i + 1);
+      h[b + 2] = (k + 0) * nvxy + (j + 1) * nvx + (i + 1);
+      h[b + 3] = (k + 0) * nvxy + (j + 1) * nvx + (i + 0);
+      h[b + 4] = (k + 1) * nvxy + (j + 0) * nvx + (i + 0);
+      h[b + 5] = (k + 1) * nvxy + (j + 0) * nvx + (i + 1);
+      h[b + 6] = (k + 1) * nvxy + (j + 1) * nvx + (i + 1);
+      h[b + 7] = (k + 1) * nvxy + (j + 1) * nvx + (i + 0);
     });
     Arr<LO> cnt(nh);
-    LO* ct = cnt.data();
+    auto ct = view(cnt);
+    auto hc = cview(hv);
     pfor(nh, [=] __device__(LO x) {
       LO hh[8];
-      ct[x] = hex_case(h + x * 8, hh) == 0 ? 5 : 6;
+      ct[x] = hex_case(hc, x * 8, hh) == 0 ? 5 : 6;
     });
     Arr<LO> off = offset_scan(cnt);
     Arr<LO> tv(last(off) * 4);
-    const LO* of = off.data();
-    LO* t = tv.data();
+    auto of = cview(off);
+    auto t = view(tv);
     pfor(nh, [=] __device__(LO x) {
       LO hh[8];
-      int nd = hex_case(h + x * 8, hh);
+      int nd = hex_case(hc, x * 8, hh);
       int nt = nd == 0 ? 5 : 6;
       for (int i = 0; i < nt; ++i)
         for (int j = 0; j < 4; ++j) t[(of[x] + i) * 4 + j] = hh[c_hex_tmpl[nd][i][j]];
@@ -475,13 +494,13 @@ static Arr<LO> box_elems(int dim, int n, Arr<double>* coords) {
   LO nvx = n + 1, nv = nvx * nvx, nq = n * n;
   double dx = 1.0 / n;
   *coords = Arr<double>(nv * 2);
-  double* c = coords->data();
+  auto c = view(*coords);
   pfor(nv, [=] __device__(LO v) {
     c[v * 2 + 0] = (v % nvx) * dx;
     c[v * 2 + 1] = (v / nvx) * dx;
   });
   Arr<LO> tv(nq * 6);
-  LO* t = tv.data();
+  auto t = view(tv);
   pfor(nq, [=] __device__(LO q) {
     LO i = q % n, j = q / n;
     // the minimum vertex of a box quad is already first: no rotation
@@ -549,11 +568,11 @@ __device__ void hilbert_axes_to_transpose(std::uint64_t* X, int b, int n) {
 }
 
 Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim) {
-  double mn[3], mx[3];
+  double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
   for (int j = 0; j < dim; ++j) {
     Arr<double> comp(n);
-    const double* c = coords.data();
-    double* o = comp.data();
+    auto c = cview(coords);
+    auto o = view(comp);
     pfor(n, [=] __device__(LO i) { o[i] = c[i * dim + j]; });
     mn[j] = min_f64(comp);
     mx[j] = max_f64(comp);
@@ -562,24 +581,16 @@ Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim) {
   // (src/Omega_h_bbox.hpp:65-79)
   double maxl = mx[0] - mn[0];
   for (int j = 1; j < dim; ++j) maxl = max2d(maxl, mx[j] - mn[j]);
-  double s0 = 0, s1 = 0, s2 = 0, t0 = 0, t1 = 0, t2 = 0;
-  double s[3], t[3];
+  double s[3] = {0, 0, 0}, t[3] = {0, 0, 0};
   for (int j = 0; j < dim; ++j) {
     double hi = mn[j] + maxl;
     s[j] = 1.0 / (hi - mn[j]);
     t[j] = -(s[j] * mn[j]);
   }
-  s0 = s[0];
-  s1 = s[1];
-  t0 = t[0];
-  t1 = t[1];
-  if (dim == 3) {
-    s2 = s[2];
-    t2 = t[2];
-  }
+  double s0 = s[0], s1 = s[1], s2 = s[2], t0 = t[0], t1 = t[1], t2 = t[2];
   Arr<GO> keys(n * dim);
-  const double* c = coords.data();
-  GO* k = keys.data();
+  auto c = cview(coords);
+  auto k = view(keys);
   pfor(n, [=] __device__(LO i) {
     const int nbits = 52;
     double ss[3] = {s0, s1, s2}, tt[3] = {t0, t1, t2};
@@ -613,8 +624,8 @@ void reorder_by_hilbert(Mesh& m) {
   new2old[0] = hilbert_sort(m.coords, nv, dim);
   Arr<LO> old2new_v(nv);
   {
-    const LO* p = new2old[0].data();
-    LO* o = old2new_v.data();
+    auto p = cview(new2old[0]);
+    auto o = view(old2new_v);
     pfor(nv, [=] __device__(LO i) { o[p[i]] = i; });
   }
   for (int d = 1; d <= dim; ++d) {
@@ -623,9 +634,9 @@ void reorder_by_hilbert(Mesh& m) {
     LO ne = m.nents[d];
     // key = new number of the first vertex; stable sort keeps old order
     Arr<LO> key(ne);
-    const LO* ev = ev2v.data();
-    const LO* o2n = old2new_v.data();
-    LO* kk = key.data();
+    auto ev = cview(ev2v);
+    auto o2n = cview(old2new_v);
+    auto kk = view(key);
     pfor(ne, [=] __device__(LO e) { kk[e] = o2n[ev[e * deg]]; });
     new2old[d] = sort_by_keys(key, 1);
   }
@@ -640,8 +651,8 @@ void reorder_by_hilbert(Mesh& m) {
     LO ne = m.nents[d];
     Adj nd;
     nd.ab2b = unmap(new2old[d], od.ab2b, deg);
-    LO* nb = nd.ab2b.data();
-    const LO* o2n = old2new_low.data();
+    auto nb = view(nd.ab2b);
+    auto o2n = cview(old2new_low);
     pfor(ne * deg, [=] __device__(LO x) { nb[x] = o2n[nb[x]]; });
     if (od.has_codes) {
       nd.codes = unmap(new2old[d], od.codes, deg);
@@ -649,8 +660,8 @@ void reorder_by_hilbert(Mesh& m) {
     }
     nm.set_ents(d, std::move(nd));
     Arr<LO> o2n2(ne);
-    const LO* p = new2old[d].data();
-    LO* o = o2n2.data();
+    auto p = cview(new2old[d]);
+    auto o = view(o2n2);
     pfor(ne, [=] __device__(LO i) { o[p[i]] = i; });
     old2new_low = o2n2;
   }
@@ -665,10 +676,11 @@ void classify_box(Mesh& m, int n) {
     LO ne = m.nents[d];
     m.class_id[d] = Arr<LO>(ne);
     m.class_dim[d] = Arr<I8>(ne);
-    const LO* ev = d ? m.ask_verts_of(d).data() : nullptr;
-    const double* c = m.coords.data();
-    LO* ci = m.class_id[d].data();
-    I8* cd = m.class_dim[d].data();
+    View<const LO> ev = {nullptr, 0};
+    if (d) ev = cview(m.ask_verts_of(d));
+    auto c = cview(m.coords);
+    auto ci = view(m.class_id[d]);
+    auto cd = view(m.class_dim[d]);
     int deg = d + 1;
     pfor(ne, [=] __device__(LO e) {
       int id = 0, cdim = 0;
@@ -678,7 +690,7 @@ void classify_box(Mesh& m, int n) {
           x = c[e * dim + j];
         } else {
           double comp = 0;
-          for (int k = 0; k < deg; ++k) comp += c[LO(ev[e * deg + k]) * dim + j];
+          for (int k = 0; k < deg; ++k) comp += c[ev[e * deg + k] * dim + j];
           comp /= deg;
           x = comp;
         }
@@ -720,68 +732,80 @@ void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
 // ------------------------------------------------------------ measurement
 // measure_edges_metric (src/Omega_h_shape.cpp:7-49): one thread per edge
 void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out) {
-  const LO* ev = m.ask_verts_of(1).data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto ev = cview(m.ask_verts_of(1));
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  bool all = a2e == nullptr;
+  auto ae = cview(a2e, na);
+  auto o = view(out, na);
   int dim = m.dim, mc = m.mcomp();
   pfor(na, [=] __device__(LO a) {
-    LO e = a2e ? a2e[a] : a;
+    LO e = all ? a : ae[a];
     LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
-    out[a] = dim == 3 ? edge_length3(c + v0 * 3, c + v1 * 3, mt + v0 * mc, mt + v1 * mc)
-                      : edge_length2(c + v0 * 2, c + v1 * 2, mt + v0 * mc, mt + v1 * mc);
+    o[a] = dim == 3 ? edge_length3(&c[v0 * 3], &c[v1 * 3], &mt[v0 * mc], &mt[v1 * mc])
+                    : edge_length2(&c[v0 * 2], &c[v1 * 2], &mt[v0 * mc], &mt[v1 * mc]);
   });
 }
 
-__device__ __forceinline__ double elem_quality_dev(int dim, const double* c, const double* mt,
-                                                   const LO* v) {
+__device__ __forceinline__ double elem_quality_dev(int dim, View<const double> c,
+                                                   View<const double> mt, const LO* v) {
   if (dim == 3) {
     V3 p[4];
     M3 ms[4];
     for (int i = 0; i < 4; ++i) {
-      for (int j = 0; j < 3; ++j) p[i].x[j] = c[LO(v[i]) * 3 + j];
-      ms[i] = symm3(mt + LO(v[i]) * 6);
+      for (int j = 0; j < 3; ++j) p[i].x[j] = c[v[i] * 3 + j];
+      ms[i] = symm3(&mt[v[i] * 6]);
     }
     return tet_quality(p, ms[maxdet_index3(ms, 4)]);
   }
   double p[3][2];
   int best = 0;
-  double bd = det2p(mt + LO(v[0]) * 3);
+  double bd = det2p(&mt[v[0] * 3]);
   for (int i = 0; i < 3; ++i) {
-    p[i][0] = c[LO(v[i]) * 2];
-    p[i][1] = c[LO(v[i]) * 2 + 1];
+    p[i][0] = c[v[i] * 2];
+    p[i][1] = c[v[i] * 2 + 1];
     if (i) {
-      double d = det2p(mt + LO(v[i]) * 3);
+      double d = det2p(&mt[v[i] * 3]);
       if (d > bd) {
         best = i;
         bd = d;
       }
     }
   }
-  return tri_quality(p, mt + LO(v[best]) * 3);
+  return tri_quality(p, &mt[v[best] * 3]);
 }
 
 // measure_qualities (src/Omega_h_quality.cpp:7-53): one thread per element
 void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
   int dim = m.dim;
-  const LO* ev = m.ask_verts_of(dim).data();
-  const double* c = m.coords.data();
-  const double* mt = m.metric.data();
+  auto ev = cview(m.ask_verts_of(dim));
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  bool all = a2e == nullptr;
+  auto ae = cview(a2e, na);
+  auto o = view(out, na);
   pfor(na, [=] __device__(LO a) {
-    LO e = a2e ? a2e[a] : a;
-    out[a] = elem_quality_dev(dim, c, mt, ev + e * (dim + 1));
+    LO e = all ? a : ae[a];
+    LO v[4];
+    for (int k = 0; k <= dim; ++k) v[k] = ev[e * (dim + 1) + k];
+    o[a] = elem_quality_dev(dim, c, mt, v);
   });
 }
 
 // get_mident_metrics (src/Omega_h_metric.cpp:56-104) for edges
 void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
-  const LO* ev = m.ask_verts_of(1).data();
-  const double* mt = m.metric.data();
+  auto ev = cview(m.ask_verts_of(1));
+  auto mt = cview(m.metric);
+  bool all = edges == nullptr;
+  auto ed = cview(edges, n);
+  auto o = view(out, n * 6);
   int* st = ctx().d_status;
   if (m.dim != 3) throw Error(8, "mident_metrics: 2D metrics are not supported yet");
   pfor(n, [=] __device__(LO a) {
-    LO e = edges ? edges[a] : a;
-    if (!average_metric3(mt + LO(ev[e * 2]) * 6, mt + LO(ev[e * 2 + 1]) * 6, out + a * 6))
-      raise_status(st, ST_NUMERIC);
+    LO e = all ? a : ed[a];
+    double r[6];
+    if (!average_metric3(&mt[ev[e * 2] * 6], &mt[ev[e * 2 + 1] * 6], r)) raise_status(st, ST_NUMERIC);
+    for (int k = 0; k < 6; ++k) o[a * 6 + k] = r[k];
   });
 }
 

@@ -17,7 +17,7 @@ def built():
     build.build()
 
 
-@pytest.mark.parametrize("case", sorted(SMALL_CASES))
+@pytest.mark.parametrize("case", list(SMALL_CASES))
 def test_gpu_matches_reference_per_stage(case):
     import gpu_dump
     golden = load_golden(case)
