@@ -26,6 +26,7 @@ def np_(t):
 
 
 def dump_mesh(m, prefix, out, with_length=False, with_quality=False):
+    out[prefix + "nents"] = np.array([float(m.nents(0))])
     for name in MESH_ARRAYS3:
         out[prefix + name] = np_(m.get(name))
     if with_length:
