@@ -164,6 +164,9 @@ static void scan_impl(const T* in, LO n, LO* out) {
   k_scan_sums<<<1, 1024, 0, c.stream>>>(sums.data(), nb, sums.data() + nb);
   k_tile_scan<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), out, sums.data() + nb);
   c.launches += 3;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
 }
 
 void offset_scan_into(const LO* counts, LO n, LO* out) { scan_impl(counts, n, out); }
@@ -184,14 +187,14 @@ LO last(const Arr<LO>& a) { return get_elem(a, a.size() - 1); }
 Arr<LO> collect_marked(const Arr<I8>& marks) {
   LO n = marks.size();
   Arr<I8> nz(n);
-  const I8* m = marks.data();
-  I8* z = nz.data();
+  auto m = cview(marks);
+  auto z = view(nz);
   pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
   Arr<LO> offs = offset_scan(nz);
   LO cnt = last(offs);
   Arr<LO> out(cnt);
-  const LO* o = offs.data();
-  LO* d = out.data();
+  auto o = cview(offs);
+  auto d = view(out);
   pfor(n, [=] __device__(LO i) {
     if (m[i]) d[o[i]] = i;
   });
@@ -200,8 +203,8 @@ Arr<LO> collect_marked(const Arr<I8>& marks) {
 LO count_marked(const Arr<I8>& marks) {
   LO n = marks.size();
   Arr<I8> nz(n);
-  const I8* m = marks.data();
-  I8* z = nz.data();
+  auto m = cview(marks);
+  auto z = view(nz);
   pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
   return last(offset_scan(nz));
 }
@@ -232,6 +235,9 @@ static T reduce(const Arr<T>& a, T init, Op op) {
   Arr<T> fin(1);
   k_reduce<<<1, kBlock, 0, c.stream>>>(part.data(), LO(nb), init, op, fin.data());
   c.launches += 2;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
   return get_elem(fin, 0);
 }
 struct MaxOp {
@@ -320,6 +326,9 @@ static void radix_pass_pairs(Arr<std::uint32_t>& keys, Arr<LO>& vals, int nbits)
     k_rs_scatter<<<nb, kRsThreads, 0, c.stream>>>(keys.data(), vals.data(), n, shift,
                                                    offs.data(), nb, k2.data(), v2.data());
     c.launches += 2;
+#ifdef OHG_CHECKED
+    checked_after_launch(__FILE__, __LINE__);
+#endif
     std::swap(keys, k2);
     std::swap(vals, v2);
   }

@@ -34,13 +34,13 @@ Arr<LO> sort_by_keys64(const Arr<GO>& keys, int width);
 template <class T>
 Arr<T> fill(LO n, T v) {
   Arr<T> a(n);
-  T* p = a.data();
+  auto p = view(a);
   pfor(n, [=] __device__(LO i) { p[i] = v; });
   return a;
 }
 inline Arr<LO> iota(LO n) {
   Arr<LO> a(n);
-  LO* p = a.data();
+  auto p = view(a);
   pfor(n, [=] __device__(LO i) { p[i] = i; });
   return a;
 }
@@ -48,24 +48,24 @@ inline Arr<LO> iota(LO n) {
 template <class T>
 Arr<T> unmap(const Arr<LO>& a2b, const Arr<T>& b, int w) {
   Arr<T> a(a2b.size() * w);
-  const LO* m = a2b.data();
-  const T* src = b.data();
-  T* dst = a.data();
+  auto m = cview(a2b);
+  auto src = cview(b);
+  auto dst = view(a);
   pfor(a2b.size(), [=] __device__(LO i) {
     LO k = m[i];
-    for (int j = 0; j < w; ++j) dst[i * w + j] = src[LO(k) * w + j];
+    for (int j = 0; j < w; ++j) dst[i * w + j] = src[k * w + j];
   });
   return a;
 }
 // b[a2b[i]*w+j] = a[i*w+j]  (map_into)
 template <class T>
 void map_into(const Arr<T>& a, const Arr<LO>& a2b, Arr<T>& b, int w) {
-  const LO* m = a2b.data();
-  const T* src = a.data();
-  T* dst = b.data();
+  auto m = cview(a2b);
+  auto src = cview(a);
+  auto dst = view(b);
   pfor(a2b.size(), [=] __device__(LO i) {
     LO k = m[i];
-    for (int j = 0; j < w; ++j) dst[LO(k) * w + j] = src[i * w + j];
+    for (int j = 0; j < w; ++j) dst[k * w + j] = src[i * w + j];
   });
 }
 template <class T>
@@ -76,8 +76,8 @@ Arr<T> map_onto(const Arr<T>& a, const Arr<LO>& a2b, LO nb, T init, int w) {
 }
 inline Arr<I8> mark_image(const Arr<LO>& a2b, LO nb) {
   Arr<I8> out = fill<I8>(nb, 0);
-  const LO* m = a2b.data();
-  I8* o = out.data();
+  auto m = cview(a2b);
+  auto o = view(out);
   pfor(a2b.size(), [=] __device__(LO i) { o[m[i]] = 1; });
   return out;
 }
