@@ -1025,172 +1025,197 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
 }
 
 // ------------------------------------------------------------ swap (3D)
-struct SwapTables {
-  int off_tri[8], off_mesh[8], off_uedge[8], off_e2u[8];
-  int nmesh[8], ntri[8], nedge[8];
-  int data[OHG_SWAP3D_TABLE_LEN];
-};
-__constant__ SwapTables c_swap;
-static void upload_swap_tables() {
-  static bool done = false;
-  if (done) return;
-  static SwapTables t;
-  for (int i = 0; i < 8; ++i) {
-    t.nmesh[i] = t.ntri[i] = t.nedge[i] = 0;
-    t.off_tri[i] = t.off_mesh[i] = t.off_uedge[i] = t.off_e2u[i] = 0;
-  }
-  int p = 0;
-  while (p < OHG_SWAP3D_TABLE_LEN) {
-    int n = OHG_SWAP3D_TABLE[p], nm = OHG_SWAP3D_TABLE[p + 1], nt = OHG_SWAP3D_TABLE[p + 2],
-        nu = OHG_SWAP3D_TABLE[p + 3];
-    p += 4;
-    t.nmesh[n] = nm;
-    t.ntri[n] = nt;
-    t.off_tri[n] = p;
-    p += nu * 3;
-    t.off_mesh[n] = p;
-    p += nm * nt;
-    int nedge = OHG_SWAP3D_TABLE[p], nue = OHG_SWAP3D_TABLE[p + 1];
-    p += 2;
-    t.nedge[n] = nedge;
-    t.off_uedge[n] = p;
-    p += nue * 2;
-    t.off_e2u[n] = p;
-    p += nm * nedge;
-  }
-  for (int i = 0; i < OHG_SWAP3D_TABLE_LEN; ++i) t.data[i] = OHG_SWAP3D_TABLE[i];
-  OHG_CUDA(cudaMemcpyToSymbol(c_swap, &t, sizeof(t)));
-  done = true;
-}
-// table lookups, clamped to the table so a bad index cannot leave it
-__device__ __forceinline__ int swap_tab(int off, int i) {
-  int k = off + i;
-  if (k < 0 || k >= OHG_SWAP3D_TABLE_LEN) k = 0;
-  return c_swap.data[k];
-}
+// Edge-swap triangulation tables in device memory: a header of 9 ints per
+// loop size n = 0..7 (meshes, triangles per mesh, unique triangles, edges
+// per mesh, unique edges, then the offsets of the four tables), followed by
+// the flat table of ohg_swap3d_tables.inc.
+enum { SW_NMESH, SW_NTRI, SW_NUTRI, SW_NEDGE, SW_NUEDGE, SW_OTRI, SW_OMESH, SW_OUEDGE, SW_OE2U };
+constexpr int kSwapHdr = 8 * 9;
+constexpr int kMaxUniqTris = 35, kMaxUniqEdges = 26;
 
-struct Loop {
-  int size;
-  LO eev2v[2];
-  LO lv[7];
-};
-// swap3d::find_loop (src/Omega_h_swap3d_loop.hpp:24-78)
-__device__ __forceinline__ Loop find_loop(LV ea, LV eb, View<const I8> ec, LV ev, LV tv, LO edge,
-                                          int* st) {
-  Loop loop;
-  LO b = ea[edge], e = ea[edge + 1];
-  loop.size = e - b;
-  if (loop.size > 7 || loop.size < 3) {
-    loop.size = 8;
-    return loop;
-  }
-  loop.eev2v[0] = ev[edge * 2];
-  loop.eev2v[1] = ev[edge * 2 + 1];
-  LO t0[7], t1[7];
-  for (int le = 0; le < loop.size; ++le) {
-    LO tet = eb[b + le];
-    I8 code = ec[b + le];
-    int opp = opposite_template(3, 1, code_which_down(code));
-    int rot = code_rotation(code);
-    t0[le] = tv[tet * 4 + down_template(3, 1, opp, rot ^ 0)];
-    t1[le] = tv[tet * 4 + down_template(3, 1, opp, rot ^ 1)];
-  }
-  for (int i = 0; i < loop.size - 1; ++i) {
-    int j;
-    for (j = i + 1; j < loop.size; ++j)
-      if (t0[j] == t1[i]) break;
-    if (j >= loop.size) {
-      raise_status(st, ST_TOPOLOGY);
-      loop.size = 8;
-      return loop;
+static View<const int> swap_tables() {
+  Ctx& c = ctx();
+  if (!c.d_swap_tables) {
+    std::vector<int> h(kSwapHdr + OHG_SWAP3D_TABLE_LEN, 0);
+    int p = 0;
+    while (p < OHG_SWAP3D_TABLE_LEN) {
+      int n = OHG_SWAP3D_TABLE[p], nm = OHG_SWAP3D_TABLE[p + 1], nt = OHG_SWAP3D_TABLE[p + 2],
+          nu = OHG_SWAP3D_TABLE[p + 3];
+      int* hd = &h[n * 9];
+      p += 4;
+      hd[SW_NMESH] = nm;
+      hd[SW_NTRI] = nt;
+      hd[SW_NUTRI] = nu;
+      hd[SW_OTRI] = kSwapHdr + p;
+      p += nu * 3;
+      hd[SW_OMESH] = kSwapHdr + p;
+      p += nm * nt;
+      int ne = OHG_SWAP3D_TABLE[p], nue = OHG_SWAP3D_TABLE[p + 1];
+      p += 2;
+      hd[SW_NEDGE] = ne;
+      hd[SW_NUEDGE] = nue;
+      hd[SW_OUEDGE] = kSwapHdr + p;
+      p += nue * 2;
+      hd[SW_OE2U] = kSwapHdr + p;
+      p += nm * ne;
     }
-    LO a0 = t0[i + 1], a1 = t1[i + 1];
-    t0[i + 1] = t0[j];
-    t1[i + 1] = t1[j];
-    t0[j] = a0;
-    t1[j] = a1;
+    for (int i = 0; i < OHG_SWAP3D_TABLE_LEN; ++i) h[kSwapHdr + i] = OHG_SWAP3D_TABLE[i];
+    OHG_CUDA(cudaMalloc(&c.d_swap_tables, h.size() * sizeof(int)));
+    OHG_CUDA(cudaMemcpy(c.d_swap_tables, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    c.swap_tables_len = int(h.size());
   }
-  for (int i = 0; i < loop.size; ++i) loop.lv[i] = t0[i];
-  return loop;
+  return {c.d_swap_tables, c.swap_tables_len};
 }
 
-// swap3d_qualities + swap3d::choose (src/Omega_h_swap3d_qualities.cpp:10-58,
-// src/Omega_h_swap3d_choice.hpp:15-100)
-void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p,
-                      I8* configs_p) {
-  upload_swap_tables();
+// swap3d::find_loop (src/Omega_h_swap3d_loop.hpp:24-78): the ring of tets
+// around each edge, loop vertices ordered to curl around it.  One thread per
+// edge; ring sizes outside 3..7 are reported as size 0.
+static void swap_loops(Mesh& m, const LO* edges_p, LO n, Arr<int>& lsize, Arr<LO>& lverts,
+                       Arr<LO>& leev) {
   const Adj& e2t = m.ask_up(1, 3);
   auto ea = cview(e2t.a2ab);
   auto eb = cview(e2t.ab2b);
   auto ec = cview(e2t.codes);
   auto ev = cview(m.ask_verts_of(1));
   auto tv = cview(m.ask_verts_of(3));
+  auto edges = cview(edges_p, n);
+  lsize = Arr<int>(n);
+  lverts = Arr<LO>(n * 7);
+  leev = Arr<LO>(n * 2);
+  auto ls = view(lsize);
+  auto lv = view(lverts);
+  auto le = view(leev);
+  int* st = ctx().d_status;
+  pfor(n, [=] __device__(LO i) {
+    LO edge = edges[i];
+    LO b = ea[edge];
+    int size = ea[edge + 1] - b;
+    le[i * 2] = ev[edge * 2];
+    le[i * 2 + 1] = ev[edge * 2 + 1];
+    for (int k = 0; k < 7; ++k) lv[i * 7 + k] = 0;
+    if (size < 3 || size > 7) {
+      ls[i] = 0;
+      return;
+    }
+    LO t0[7], t1[7];
+    for (int k = 0; k < size; ++k) {
+      LO tet = eb[b + k];
+      I8 code = ec[b + k];
+      int opp = opposite_template(3, 1, code_which_down(code) & 7);
+      int rot = code_rotation(code);
+      t0[k] = tv[tet * 4 + down_template(3, 1, opp, rot ^ 0)];
+      t1[k] = tv[tet * 4 + down_template(3, 1, opp, rot ^ 1)];
+    }
+    for (int a = 0; a < size - 1; ++a) {
+      int j = a + 1;
+      while (j < size && t0[j] != t1[a]) ++j;
+      if (j >= size) {
+        raise_status(st, ST_TOPOLOGY);
+        ls[i] = 0;
+        return;
+      }
+      LO x0 = t0[a + 1], x1 = t1[a + 1];
+      t0[a + 1] = t0[j];
+      t1[a + 1] = t1[j];
+      t0[j] = x0;
+      t1[j] = x1;
+    }
+    for (int k = 0; k < size; ++k) lv[i * 7 + k] = t0[k];
+    ls[i] = size;
+  });
+}
+
+// swap3d_qualities + swap3d::choose (src/Omega_h_swap3d_qualities.cpp:10-58,
+// src/Omega_h_swap3d_choice.hpp:15-100).  The reference evaluates unique
+// triangles and edges lazily per candidate; here every unique triangle's two
+// tets and every unique edge length are evaluated by their own threads into
+// global memory, then one thread per candidate walks the triangulations in
+// table order with the reference's comparisons (first best wins, a negative
+// triangle ends a triangulation, an edge longer than max_length_allowed
+// rejects it).  The values are pure functions of the loop, so the choice is
+// the same.
+void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p,
+                      I8* configs_p) {
+  auto tab = swap_tables();
+  Arr<int> lsize;
+  Arr<LO> lverts, leev;
+  swap_loops(m, c2e_p, n, lsize, lverts, leev);
+  auto ls = cview(lsize);
+  auto lv = cview(lverts);
+  auto le = cview(leev);
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
-  auto c2e = cview(c2e_p, n);
+  Arr<double> tq(n * kMaxUniqTris), el(n * kMaxUniqEdges);
+  {
+    auto q = view(tq);
+    pfor(n * kMaxUniqTris, [=] __device__(LO idx) {
+      LO i = idx / kMaxUniqTris;
+      int u = idx % kMaxUniqTris;
+      int size = ls[i];
+      if (size < 3 || u >= tab[size * 9 + SW_NUTRI]) return;
+      int otri = tab[size * 9 + SW_OTRI];
+      LO tet[4];
+      for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+      double tmq = 1.0;
+      for (int tt = 0; tt < 2; ++tt) {
+        tet[3] = le[i * 2 + (1 - tt)];
+        tmq = min2d(tmq, elem_quality_v(3, c, mt, tet));
+        LO s = tet[1];
+        tet[1] = tet[2];
+        tet[2] = s;
+      }
+      q[idx] = tmq;
+    });
+  }
+  {
+    auto l = view(el);
+    pfor(n * kMaxUniqEdges, [=] __device__(LO idx) {
+      LO i = idx / kMaxUniqEdges;
+      int u = idx % kMaxUniqEdges;
+      int size = ls[i];
+      if (size < 3 || u >= tab[size * 9 + SW_NUEDGE]) return;
+      int oued = tab[size * 9 + SW_OUEDGE];
+      LO a = lv[i * 7 + tab[oued + u * 2]], b = lv[i * 7 + tab[oued + u * 2 + 1]];
+      l[idx] = edge_len_v(3, c, mt, 6, a, b);
+    });
+  }
+  auto q = cview(tq);
+  auto l = cview(el);
   auto quals = view(quals_p, n);
   auto configs = view(configs_p, n);
-  int* st = ctx().d_status;
-  pfor(n, [=] __device__(LO cand) {
-    Loop loop = find_loop(ea, eb, ec, ev, tv, c2e[cand], st);
-    quals[cand] = -1.0;
-    configs[cand] = -1;
-    if (loop.size > 7) return;
-    int ls = loop.size;
-    int nmeshes = c_swap.nmesh[ls], ntris = c_swap.ntri[ls], nedges = c_swap.nedge[ls];
-    int otri = c_swap.off_tri[ls], omsh = c_swap.off_mesh[ls];
-    int oued = c_swap.off_uedge[ls], oe2u = c_swap.off_e2u[ls];
-    unsigned long long tcached = 0;
-    unsigned ecached = 0;
-    double tq[35];
-    double el[26];
+  pfor(n, [=] __device__(LO i) {
+    int size = ls[i];
+    if (size < 3) {
+      quals[i] = -1.0;
+      configs[i] = -1;
+      return;
+    }
+    const int* h = &tab[size * 9];
+    int nmeshes = h[SW_NMESH], ntris = h[SW_NTRI], nedges = h[SW_NEDGE];
+    int omsh = h[SW_OMESH], oe2u = h[SW_OE2U];
     int best = -1;
     double bestq = 0.0;
     for (int mesh = 0; mesh < nmeshes; ++mesh) {
       double mq = 1.0;
       for (int t = 0; t < ntris; ++t) {
-        int u = swap_tab(omsh, mesh * ntris + t);
-        if (u < 0 || u >= 35) u = 0;
-        if (!((tcached >> u) & 1ull)) {
-          LO tet[4];
-          for (int k = 0; k < 3; ++k) tet[k] = loop.lv[swap_tab(otri, u * 3 + k) % 7];
-          double tmq = 1.0;
-          for (int tt = 0; tt < 2; ++tt) {
-            tet[3] = loop.eev2v[1 - tt];
-            tmq = min2d(tmq, elem_quality_v(3, c, mt, tet));
-            LO s = tet[1];
-            tet[1] = tet[2];
-            tet[2] = s;
-          }
-          tcached |= (1ull << u);
-          tq[u] = tmq;
-        }
-        mq = min2d(mq, tq[u]);
+        mq = min2d(mq, q[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]]);
         if (mq < 0.0) break;
       }
       if (mq > bestq) {
         bool over = false;
-        for (int me = 0; me < nedges; ++me) {
-          int ue = swap_tab(oe2u, mesh * nedges + me);
-          if (ue < 0 || ue >= 26) ue = 0;
-          if (!((ecached >> ue) & 1u)) {
-            LO a = loop.lv[swap_tab(oued, ue * 2) % 7], b = loop.lv[swap_tab(oued, ue * 2 + 1) % 7];
-            el[ue] = edge_len_v(3, c, mt, 6, a, b);
-            ecached |= (1u << ue);
-          }
-          if (el[ue] > max_len) {
+        for (int e = 0; e < nedges; ++e)
+          if (l[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]] > max_len) {
             over = true;
             break;
           }
-        }
         if (!over) {
           best = mesh;
           bestq = mq;
         }
       }
     }
-    configs[cand] = I8(best);
-    quals[cand] = bestq;
+    configs[i] = I8(best);
+    quals[i] = bestq;
   });
 }
 
@@ -1223,7 +1248,6 @@ Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
 
 bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   if (m.dim != 3) return false;
-  upload_swap_tables();
   Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
   Arr<I8> edc = mark_down(m, 3, 1, ec);
   {
@@ -1267,19 +1291,20 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   LO nkeys = k2e.size();
   st->swap_keys = nkeys;
   // swap3d_keys_to_prods + swap3d_topology (src/Omega_h_swap3d_topology.cpp)
-  const Adj& e2t = m.ask_up(1, 3);
-  auto ea = cview(e2t.a2ab);
+  auto tab = swap_tables();
+  Arr<int> lsize;
+  Arr<LO> lverts, leev;
+  swap_loops(m, k2e.data(), nkeys, lsize, lverts, leev);
   Arr<LO> cnt[4], k2p[4], pv2v[4];
   for (int d = 1; d <= 3; ++d) cnt[d] = Arr<LO>(nkeys);
   {
-    auto ke = cview(k2e);
+    auto ls = cview(lsize);
     auto c1 = view(cnt[1]);
     auto c2 = view(cnt[2]);
     auto c3 = view(cnt[3]);
     pfor(nkeys, [=] __device__(LO k) {
-      int ls = ea[ke[k] + 1] - ea[ke[k]];
-      if (ls > 7 || ls < 0) ls = 0;
-      int npt = c_swap.ntri[ls], npe = c_swap.nedge[ls];
+      int size = ls[k];
+      int npt = tab[size * 9 + SW_NTRI], npe = tab[size * 9 + SW_NEDGE];
       c1[k] = npe;
       c2[k] = npt + 2 * npe;
       c3[k] = 2 * npt;
@@ -1290,10 +1315,9 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     pv2v[d] = Arr<LO>(last(k2p[d]) * (d + 1));
   }
   {
-    auto eb = cview(e2t.ab2b);
-    auto ecd = cview(e2t.codes);
-    auto ev = cview(m.ask_verts_of(1));
-    auto tv = cview(m.ask_verts_of(3));
+    auto ls = cview(lsize);
+    auto lv = cview(lverts);
+    auto le = cview(leev);
     auto ke = cview(k2e);
     auto cfg = cview(econfig);
     auto p1 = cview(k2p[1]);
@@ -1304,25 +1328,24 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     auto v3 = view(pv2v[3]);
     int* stw = ctx().d_status;
     pfor(nkeys, [=] __device__(LO k) {
-      Loop loop = find_loop(ea, eb, ecd, ev, tv, ke[k], stw);
+      int size = ls[k];
       int config = cfg[ke[k]];
-      if (loop.size > 7 || config < 0 || config >= c_swap.nmesh[loop.size]) {
-        // no valid configuration: products get the key edge's own vertex
-        // (a valid index) and the status word reports the failure
+      if (size < 3 || config < 0 || config >= tab[size * 9 + SW_NMESH]) {
+        // no valid configuration: the key's products get one of its loop
+        // vertices (a valid index) and the status word reports the failure
         raise_status(stw, ST_TOPOLOGY);
-        LO a = ev[ke[k] * 2];
+        LO a = le[k * 2];
         for (LO p = p1[k] * 2; p < p1[k + 1] * 2; ++p) v1[p] = a;
         for (LO p = p2[k] * 3; p < p2[k + 1] * 3; ++p) v2[p] = a;
         for (LO p = p3[k] * 4; p < p3[k + 1] * 4; ++p) v3[p] = a;
         return;
       }
-      int ls = loop.size;
-      int npt = c_swap.ntri[ls], npe = c_swap.nedge[ls];
-      int otri = c_swap.off_tri[ls], omsh = c_swap.off_mesh[ls];
-      int oued = c_swap.off_uedge[ls], oe2u = c_swap.off_e2u[ls];
+      const int* h = &tab[size * 9];
+      int npt = h[SW_NTRI], npe = h[SW_NEDGE];
+      int otri = h[SW_OTRI], omsh = h[SW_OMESH], oued = h[SW_OUEDGE], oe2u = h[SW_OE2U];
       for (int pe = 0; pe < npe; ++pe) {
-        int ue = swap_tab(oe2u, config * npe + pe);
-        LO a = loop.lv[swap_tab(oued, ue * 2) % 7], b = loop.lv[swap_tab(oued, ue * 2 + 1) % 7];
+        int ue = tab[oe2u + config * npe + pe];
+        LO a = lv[k * 7 + tab[oued + ue * 2]], b = lv[k * 7 + tab[oued + ue * 2 + 1]];
         LO pedge = p1[k] + pe;
         v1[pedge * 2] = a;
         v1[pedge * 2 + 1] = b;
@@ -1330,14 +1353,14 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
           LO ptri = p2[k] + 2 * pe + eev;
           v2[ptri * 3] = a;
           v2[ptri * 3 + 1] = b;
-          v2[ptri * 3 + 2] = loop.eev2v[eev];
+          v2[ptri * 3 + 2] = le[k * 2 + eev];
         }
       }
       for (int pt = 0; pt < npt; ++pt) {
-        int ut = swap_tab(omsh, config * npt + pt);
-        LO t0 = loop.lv[swap_tab(otri, ut * 3) % 7];
-        LO t1 = loop.lv[swap_tab(otri, ut * 3 + 1) % 7];
-        LO t2 = loop.lv[swap_tab(otri, ut * 3 + 2) % 7];
+        int ut = tab[omsh + config * npt + pt];
+        LO t0 = lv[k * 7 + tab[otri + ut * 3]];
+        LO t1 = lv[k * 7 + tab[otri + ut * 3 + 1]];
+        LO t2 = lv[k * 7 + tab[otri + ut * 3 + 2]];
         LO ptri = p2[k] + 2 * npe + pt;
         v2[ptri * 3] = t0;
         v2[ptri * 3 + 1] = t1;
@@ -1347,7 +1370,7 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
           v3[ptet * 4] = t0;
           v3[ptet * 4 + 1] = eev == 0 ? t2 : t1;
           v3[ptet * 4 + 2] = eev == 0 ? t1 : t2;
-          v3[ptet * 4 + 3] = loop.eev2v[eev];
+          v3[ptet * 4 + 3] = le[k * 2 + eev];
         }
       }
     });

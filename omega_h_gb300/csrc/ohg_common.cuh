@@ -48,6 +48,8 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   int* d_status = nullptr;  // device status word
   int* h_pinned = nullptr;  // pinned host scratch for small reads
+  int* d_swap_tables = nullptr;  // edge-swap triangulation tables (device copy)
+  int swap_tables_len = 0;
   std::uint64_t launches = 0;
   explicit Ctx(int dev);
   ~Ctx();

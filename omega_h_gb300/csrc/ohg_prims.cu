@@ -34,6 +34,7 @@ Ctx::Ctx(int dev) : device(dev) {
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
   cudaFree(d_status);
+  if (d_swap_tables) cudaFree(d_swap_tables);
   cudaFreeHost(h_pinned);
   cudaStreamDestroy(stream);
 }
