@@ -67,10 +67,33 @@ def run_oracle(driver, spec, mode=""):
         return load_dump_dir(d)
 
 
-def compare_arrays(expected, got, keys=None, rtol=1e-12):
-    """Bit-exact for integer arrays, relative error <= rtol for reals.
-    Returns (list of failures, max real relative error, count of real
-    values that are not bitwise equal)."""
+# Real-valued tolerances.  Every real computed before the first metric
+# interpolation (lengths, qualities, cavity qualities of the input mesh) must
+# agree within STRICT_RTOL.  The log-Euclidean metric average (one closed-form
+# 3x3 eigensolve per logarithm and exponential) is ill-conditioned where two
+# eigenvalues (nearly) coincide, e.g. the two tangential sizes of the shock
+# metric: there a one-ulp difference between CUDA's and glibc's cbrt/acos/cos
+# in the cubic root solve moves a double root by O(sqrt(ulp)) before the two
+# roots are merged.  Interpolated metric tensors are therefore compared
+# relative to their largest component (INTERP_TENSOR_RTOL), and every real
+# computed from them afterwards within INTERP_RTOL.  Integers stay bit-exact.
+STRICT_RTOL = 1e-12
+INTERP_TENSOR_RTOL = 1e-6
+INTERP_RTOL = 1e-7
+
+
+def interp_dependent(key):
+    """Arrays whose values can depend on an interpolated metric: the midpoint
+    metrics themselves and everything produced after the refine rebuild."""
+    return key in ("r_midmetrics",) or key.startswith("r_out_") or \
+        not key.startswith(("in_", "r_"))
+
+
+def compare_arrays(expected, got, keys=None, rtol=STRICT_RTOL):
+    """Bit-exact for integer arrays, relative error <= rtol for reals (with
+    the interpolation tolerances above for interpolation-dependent arrays).
+    Returns (list of failures, max real relative error, count of real values
+    that are not bitwise equal)."""
     fails = []
     maxerr = 0.0
     nreal_diff = 0
@@ -86,11 +109,19 @@ def compare_arrays(expected, got, keys=None, rtol=1e-12):
             continue
         if a.dtype.kind == "f":
             if a.size:
-                err = float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-300)))
-                maxerr = max(maxerr, err)
                 nreal_diff += int(np.sum(a != b))
-                if not err <= rtol:
-                    fails.append(f"{k}: max rel err {err:.3e}")
+                interp = interp_dependent(k) and rtol == STRICT_RTOL
+                if interp and (k.endswith("metric") or k.endswith("metrics")) and a.size % 6 == 0:
+                    A, B = a.reshape(-1, 6), b.reshape(-1, 6)
+                    nrm = np.maximum(np.max(np.abs(A), axis=1), 1e-300)
+                    err = float(np.max(np.max(np.abs(A - B), axis=1) / nrm))
+                    tol = INTERP_TENSOR_RTOL
+                else:
+                    err = float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-300)))
+                    tol = INTERP_RTOL if interp else rtol
+                maxerr = max(maxerr, err)
+                if not err <= tol:
+                    fails.append(f"{k}: max rel err {err:.3e} > {tol:.0e}")
         else:
             nd = int(np.sum(a != b.astype(a.dtype)))
             if nd:
