@@ -185,6 +185,19 @@ int ohg_sort_by_keys(ohg_context* ctx, const void* keys_dev, int n, int width, i
 int ohg_hilbert_sort(ohg_context* ctx, const double* coords_dev, int n, int dim, int* perm_dev);
 /* offset_scan (src/Omega_h_int_scan.cpp:10-20): n+1 outputs */
 int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
+/* offset_scan without any device allocation: no counterpart in the
+ * reference.  For hosts that cannot let the library allocate at that moment
+ * (their own arena owns the device memory, or they are recovering from an
+ * out-of-memory failure and need offsets to compact before freeing).  The
+ * scan's tile sums live in one fixed device array per device, sized for at
+ * most ohg_offset_scan_noalloc_limit() counts (4,194,304); larger n fails
+ * with OHG_ERR_INVALID before any launch.  The first call on a device looks
+ * up the array's address (make it before capturing the stream into a graph).
+ * Nothing has to be zeroed beforehand.  Calls in flight on one device at the
+ * same time (other streams, contexts or threads) race on the shared array:
+ * order them. */
+int ohg_offset_scan_noalloc(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
+int ohg_offset_scan_noalloc_limit(int* max_counts);
 
 #ifdef __cplusplus
 }

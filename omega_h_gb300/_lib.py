@@ -83,6 +83,8 @@ SIGNATURES = {
     "ohg_sort_by_keys": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p],
     "ohg_hilbert_sort": [c_void_p, c_void_p, c_int, c_int, c_void_p],
     "ohg_offset_scan": [c_void_p, c_void_p, c_int, c_void_p],
+    "ohg_offset_scan_noalloc": [c_void_p, c_void_p, c_int, c_void_p],
+    "ohg_offset_scan_noalloc_limit": [P(c_int)],
 }
 _RESTYPE = {"ohg_last_error": c_char_p}
 

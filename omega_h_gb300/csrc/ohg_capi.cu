@@ -665,5 +665,16 @@ int ohg_hilbert_sort(ohg_context* c, const double* coords, int n, int dim, int* 
 int ohg_offset_scan(ohg_context* c, const int* counts, int n, int* out) {
   return guarded(c, [&] { offset_scan_into(counts, n, out); });
 }
+int ohg_offset_scan_noalloc(ohg_context* c, const int* counts, int n, int* out) {
+  return guarded(c, [&] { offset_scan_fixed_scratch(counts, n, out); });
+}
+int ohg_offset_scan_noalloc_limit(int* out) {
+  if (!out) {
+    g_err = "null output";
+    return OHG_ERR_INVALID;
+  }
+  *out = offset_scan_fixed_limit();
+  return OHG_OK;
+}
 
 }  // extern "C"

@@ -1,5 +1,6 @@
 // Scan, compaction, reduction and radix-sort kernels.
 #include <cfloat>
+#include <mutex>
 
 #include "ohg_prims.cuh"
 
@@ -181,6 +182,69 @@ Arr<LO> offset_scan(const Arr<I8>& counts) {
   Arr<LO> out(counts.size() + 1);
   scan_impl(counts.data(), counts.size(), out.data());
   return out;
+}
+
+// ------------------------------------------------------------ fixed-scratch scan
+// The same three-phase scan with its tile sums in a statically sized device
+// array instead of pool memory.  It serves hosts that cannot let a library
+// allocate device memory at the moment they need offsets: a host whose
+// arena already owns the device memory it may use (the library's pool would
+// then grow behind its back), or one recovering from an out-of-memory failure
+// that needs offsets to compact its arrays before anything can be freed.
+// Limit: kFixedScanMaxTiles tiles of kScanTile counts, 4,194,304 counts.
+// Nothing in the scratch has to start at zero: every slot a call reads was
+// written earlier in the same call.  There is one scratch per device, so two
+// calls in flight on one device at once (other streams, contexts or threads)
+// race on it; callers order such calls themselves.
+constexpr LO kFixedScanMaxTiles = 1024;
+constexpr LO kFixedScanMaxCounts = kFixedScanMaxTiles * kScanTile;
+static __device__ __align__(256) LO g_fixed_scan_scratch[kFixedScanMaxTiles + 1];
+
+// Looks up (once per device, with that device current) the device address of
+// the scratch array; later calls return the cached address.
+static LO* fixed_scan_scratch(int dev) {
+  static std::mutex mu;
+  static std::map<int, LO*> addrs;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = addrs.find(dev);
+  if (it != addrs.end()) return it->second;
+  int cur = -1;
+  OHG_CUDA(cudaGetDevice(&cur));
+  if (cur != dev) OHG_CUDA(cudaSetDevice(dev));
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_fixed_scan_scratch);
+  if (cur != dev) cudaSetDevice(cur);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    throw Error(1, std::string("cudaGetSymbolAddress of the fixed scan scratch failed: ") +
+                       cudaGetErrorString(e));
+  }
+  addrs[dev] = static_cast<LO*>(p);
+  return static_cast<LO*>(p);
+}
+
+LO offset_scan_fixed_limit() { return kFixedScanMaxCounts; }
+
+void offset_scan_fixed_scratch(const LO* counts, LO n, LO* out) {
+  if (n < 0) throw Error(8, "offset scan without allocation: negative count " + std::to_string(n));
+  if (n > kFixedScanMaxCounts)
+    throw Error(8, "offset scan without allocation: " + std::to_string(n) +
+                       " counts exceed the fixed scratch limit of " +
+                       std::to_string(kFixedScanMaxCounts));
+  Ctx& c = ctx();
+  LO* sums = fixed_scan_scratch(c.device);
+  if (n == 0) {
+    OHG_CUDA(cudaMemsetAsync(out, 0, sizeof(LO), c.stream));
+    return;
+  }
+  LO nb = (n + kScanTile - 1) / kScanTile;
+  k_tile_sums<LO><<<nb, kScanThreads, 0, c.stream>>>(counts, n, sums);
+  k_scan_sums<<<1, 1024, 0, c.stream>>>(sums, nb, sums + nb);
+  k_tile_scan<LO><<<nb, kScanThreads, 0, c.stream>>>(counts, n, sums, out, sums + nb);
+  c.launches += 3;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
 }
 
 LO last(const Arr<LO>& a) { return get_elem(a, a.size() - 1); }

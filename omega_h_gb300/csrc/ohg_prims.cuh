@@ -13,6 +13,11 @@ Arr<LO> offset_scan(const Arr<I8>& counts);
 // same, into caller memory of n+1 entries
 void offset_scan_into(const LO* counts, LO n, LO* out);
 void offset_scan_into(const I8* counts, LO n, LO* out);
+// same, with the scan's scratch in a fixed device array instead of pool
+// memory: allocates nothing, at most offset_scan_fixed_limit() counts, and
+// calls in flight on one device at once race on the shared scratch
+void offset_scan_fixed_scratch(const LO* counts, LO n, LO* out);
+LO offset_scan_fixed_limit();
 
 // indices of nonzero marks (collect_marked, src/Omega_h_map.cpp:174-185)
 Arr<LO> collect_marked(const Arr<I8>& marks);
