@@ -64,6 +64,17 @@ int ohg_context_destroy(ohg_context* ctx);
 int ohg_context_launches(ohg_context* ctx, unsigned long long* out);
 /* the context's cudaStream_t, for callers that order their own work on it */
 int ohg_context_stream(ohg_context* ctx, void** stream_out);
+/* Precision mode of the cavity-quality and overshoot stages (no counterpart
+ * in the reference, which computes in FP64 throughout).  on = 1 (default):
+ * FP32 enclosures of the FP64 lengths and qualities decide wherever they
+ * settle a comparison, and the rest is recomputed in FP64 with the
+ * reference's arithmetic, so decisions and output reals equal FP64's.
+ * on = 0: FP64 throughout. */
+int ohg_context_set_screening(ohg_context* ctx, int on);
+/* screening counters since the last reset: [0] cavity tets screened,
+ * [1] tets recomputed in FP64, [2] edge lengths screened, [3] edge lengths
+ * recomputed in FP64 */
+int ohg_context_screen_counts(ohg_context* ctx, unsigned long long* counts4, int reset);
 
 /* ---- meshes ---- */
 /* build_box on the unit square/cube with n subdivisions per axis, Hilbert
@@ -122,6 +133,16 @@ int ohg_swap_edges(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
 int ohg_measure_edges_metric(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
 /* measure_qualities (src/Omega_h_quality.cpp:25-44); a2e_dev NULL = all */
 int ohg_measure_qualities(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
+/* FP32 enclosures [lo, hi] of the FP64 quality (tet_quality,
+ * src/Omega_h_quality.hpp:8-52) of n vertex 4-tuples of the mesh, with the
+ * FP64 value itself; the screening step of the precision mode, exposed for
+ * checking it (no counterpart in the reference) */
+int ohg_screen_tet_qualities(ohg_mesh* mesh, const int* tv2v_dev, int n, float* lo_dev,
+                             float* hi_dev, double* exact_dev);
+/* the same for the metric length (edge_length, src/Omega_h_shape.hpp:112-157)
+ * of n vertex pairs */
+int ohg_screen_edge_lengths(ohg_mesh* mesh, const int* ev2v_dev, int n, float* lo_dev,
+                            float* hi_dev, double* exact_dev);
 /* get_mident_metrics for edges (src/Omega_h_metric.cpp:73-101): 6 per edge */
 int ohg_get_mident_metrics(ohg_mesh* mesh, const int* edges_dev, int n, double* out_dev);
 /* refine_qualities (src/Omega_h_refine_qualities.cpp:88-107) */

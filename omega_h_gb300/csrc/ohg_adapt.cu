@@ -1,9 +1,11 @@
 // Refine, coarsen and 3D edge-swap operators of one adapt pass, the
 // topology rebuild (modify) and field transfer, all on device arrays.
 #include <cfloat>
+#include <cmath>
 
 #include "ohg_adapt.cuh"
 #include "ohg_math.cuh"
+#include "ohg_screen.cuh"
 
 namespace ohg {
 
@@ -52,6 +54,106 @@ __device__ __forceinline__ double elem_quality_v(int dim, RV c, RV mt, const LO*
 __device__ __forceinline__ double edge_len_v(int dim, RV c, RV mt, int mc, LO a, LO b) {
   return dim == 3 ? edge_length3(&c[a * 3], &c[b * 3], &mt[a * mc], &mt[b * mc])
                   : edge_length2(&c[a * 2], &c[b * 2], &mt[a * mc], &mt[b * mc]);
+}
+
+// ------------------------------------------------------------ screening
+VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nv) {
+  VertScreen s;
+  s.xh = Arr<float4>(nv);
+  s.xl = Arr<float4>(nv);
+  s.ma = Arr<float4>(nv);
+  s.mb = Arr<float4>(nv);
+  s.dkey = Arr<long long>(nv);
+  s.sdet = Arr<double>(nv);
+  auto c = cview(coords);
+  auto mt = cview(metric);
+  auto xh = view(s.xh);
+  auto xl = view(s.xl);
+  auto ma = view(s.ma);
+  auto mb = view(s.mb);
+  auto dk = view(s.dkey);
+  auto sd = view(s.sdet);
+  pfor(nv, [=] __device__(LO v) {
+    float h[3], l[3];
+    for (int j = 0; j < 3; ++j) {
+      double x = c[v * 3 + j];
+      h[j] = __double2float_rn(x);
+      l[j] = __double2float_rn(x - double(h[j]));  // x - h is exact in double
+    }
+    float mxh = fmaxf(fabsf(h[0]), fmaxf(fabsf(h[1]), fabsf(h[2])));
+    xh[v] = make_float4(h[0], h[1], h[2], mxh);
+    xl[v] = make_float4(l[0], l[1], l[2], 0.0f);
+    const double* m = &mt[v * 6];
+    float f[6];
+    for (int j = 0; j < 6; ++j) f[j] = __double2float_rn(m[j]);
+    float s0 = fabsf(f[0]) + fabsf(f[1]) + fabsf(f[2]) +
+               2.0f * (fabsf(f[3]) + fabsf(f[4]) + fabsf(f[5]));
+    s0 = __fmul_ru(s0, 1.0f + 0x1p-20f);
+    double det = det3(symm3(m));
+    double sdet = sqrt(det);
+    ma[v] = make_float4(f[0], f[1], f[2], f[3]);
+    mb[v] = make_float4(f[4], f[5], s0, __double2float_rn(sdet));
+    dk[v] = order_key(det);
+    sd[v] = sdet;
+  });
+  return s;
+}
+
+void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
+  if (m.dim != 3) throw Error(8, "screen_tets: 3D meshes only");
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto tv = cview(tv2v_p, n * 4);
+  auto lo = view(lo_p, n);
+  auto hi = view(hi_p, n);
+  auto ex = view(ex_p, n);
+  pfor(n, [=] __device__(LO i) {
+    LO vv[4] = {tv[i * 4], tv[i * 4 + 1], tv[i * 4 + 2], tv[i * 4 + 3]};
+    FIv b = tet_quality_bounds(sv, vv);
+    lo[i] = b.lo;
+    hi[i] = b.hi;
+    ex[i] = tet_quality_exact(sv, c, mt, vv);
+  });
+}
+
+void screen_edges(Mesh& m, const LO* ev2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
+  if (m.dim != 3) throw Error(8, "screen_edges: 3D meshes only");
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto ev = cview(ev2v_p, n * 2);
+  auto lo = view(lo_p, n);
+  auto hi = view(hi_p, n);
+  auto ex = view(ex_p, n);
+  pfor(n, [=] __device__(LO i) {
+    FIv b = edge_len_bounds(sv, ev[i * 2], ev[i * 2 + 1]);
+    lo[i] = b.lo;
+    hi[i] = b.hi;
+    ex[i] = edge_len_v(3, c, mt, 6, ev[i * 2], ev[i * 2 + 1]);
+  });
+}
+
+// adds v over the calling warp's active lanes to *p with one atomic
+__device__ __forceinline__ void warp_count(unsigned long long* p, unsigned v) {
+  unsigned mask = __activemask();
+  unsigned tot = __reduce_add_sync(mask, v);
+  if (int(threadIdx.x & 31) == __ffs(mask) - 1 && tot) atomicAdd(p, (unsigned long long)tot);
+}
+
+// smallest float >= x, for comparing floats against a double threshold
+static float float_at_or_above(double x) {
+  float f = float(x);
+  if (double(f) < x) f = std::nextafter(f, INFINITY);
+  return f;
+}
+// largest float <= x
+static float float_at_or_below(double x) {
+  float f = float(x);
+  if (double(f) > x) f = std::nextafter(f, -INFINITY);
+  return f;
 }
 
 // ------------------------------------------------------------ indset
@@ -707,9 +809,69 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
   }
 }
 
+// prevent_coarsen_overshoot with FP32 screening of the new edge lengths:
+// an enclosure of each FP64 length settles "length >= max_length" unless the
+// threshold lies inside it; those lengths are computed in FP64.
+static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
+                                               LO n, const I8* ci_p, I8* co_p) {
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto ev = cview(m.ask_verts_of(1));
+  const Adj& v2e = m.ask_up(0, 1);
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto ci = cview(ci_p, n);
+  auto co = view(co_p, n);
+  float thr = float_at_or_above(max_length);  // for float x: x >= max_length <=> x >= thr
+  unsigned long long* cnt = ctx().d_screen_counts;
+  pfor(n, [=] __device__(LO cand) {
+    LO e = c2e[cand];
+    I8 code = ci[cand];
+    unsigned nscreen = 0, nexact = 0;
+    for (int col = 0; col < 2; ++col) {
+      if (!collapses(code, col)) continue;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
+        LO e2 = vb[x];
+        if (e2 == e) continue;
+        int ein = code_which_down(vc[x]), eout = 1 - ein;
+        LO nv[2];
+        nv[ein] = v_onto;
+        nv[eout] = ev[e2 * 2 + eout];
+        FIv L = edge_len_bounds(sv, nv[0], nv[1]);
+        ++nscreen;
+        bool over;
+        if (L.lo >= thr) {
+          over = true;
+        } else if (L.hi < thr) {
+          over = false;
+        } else {
+          over = edge_len_v(3, c, mt, 6, nv[0], nv[1]) >= max_length;
+          ++nexact;
+        }
+        if (over) {
+          code = dont_collapse(code, col);
+          break;
+        }
+      }
+    }
+    co[cand] = code;
+    warp_count(&cnt[2], nscreen);
+    warp_count(&cnt[3], nexact);
+  });
+}
+
 // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
 void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n,
                                const I8* ci_p, I8* co_p) {
+  if (m.dim == 3 && ctx().screening) {
+    prevent_coarsen_overshoot_screened(m, max_length, c2e_p, n, ci_p, co_p);
+    return;
+  }
   auto ev = cview(m.ask_verts_of(1));
   const Adj& v2e = m.ask_up(0, 1);
   auto va = cview(v2e.a2ab);
@@ -744,9 +906,88 @@ void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n
   });
 }
 
+// The cavity of collapsing v_col onto v_onto: the elements around v_col that
+// do not contain v_onto, with v_col replaced by v_onto.  Returns false for an
+// element that dies in the collapse.
+__device__ __forceinline__ bool collapse_elem(LV cv, int dim, LO el, int ccv_col, LO v_onto,
+                                              LO vv[4]) {
+  for (int k = 0; k <= dim; ++k) vv[k] = cv[el * (dim + 1) + k];
+  for (int k = 0; k <= dim; ++k)
+    if (k != ccv_col && vv[k] == v_onto) return false;
+  vv[ccv_col & 3] = v_onto;
+  return true;
+}
+
+constexpr int kMaxScreenCavity = 64;
+
+// coarsen_qualities_tmpl (src/Omega_h_coarsen_qualities.cpp:15-63) with FP32
+// screening: every cavity tet gets an enclosure [lo, hi] of its FP64 quality;
+// only tets with lo <= min(1, min hi) can hold the cavity minimum, and only
+// those are evaluated in FP64 (the same operations as the reference's), so
+// the minimum is the reference's minimum.
+static void coarsen_qualities_screened(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
+                                       double* q2_p) {
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto ev = cview(m.ask_verts_of(1));
+  auto cv = cview(m.ask_verts_of(3));
+  const Adj& v2c = m.ask_up(0, 3);
+  auto va = cview(v2c.a2ab);
+  auto vb = cview(v2c.ab2b);
+  auto vc = cview(v2c.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto codes = cview(codes_p, n);
+  auto q2 = view(q2_p, n * 2);
+  unsigned long long* cnt = ctx().d_screen_counts;
+  pfor(n, [=] __device__(LO cand) {
+    LO e = c2e[cand];
+    I8 code = codes[cand];
+    unsigned nscreen = 0, nexact = 0;
+    for (int col = 0; col < 2; ++col) {
+      q2[cand * 2 + col] = -1.0;
+      if (!collapses(code, col)) continue;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      LO x0 = va[v_col], x1 = va[v_col + 1];
+      float lo[kMaxScreenCavity];
+      float min_hi = 1.0f;
+      int k = 0;
+      for (LO x = x0; x < x1; ++x) {
+        LO vv[4];
+        if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+        FIv b = tet_quality_bounds(sv, vv);
+        if (k < kMaxScreenCavity) lo[k] = b.lo;
+        ++k;
+        min_hi = fminf(min_hi, b.hi);
+      }
+      bool all = k > kMaxScreenCavity;
+      double minq = 1.0;
+      int j = 0;
+      for (LO x = x0; x < x1; ++x) {
+        LO vv[4];
+        if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+        if (all || lo[j] <= min_hi) {
+          minq = min2d(minq, tet_quality_exact(sv, c, mt, vv));
+          ++nexact;
+        }
+        ++j;
+      }
+      nscreen += k;
+      q2[cand * 2 + col] = minq;
+    }
+    warp_count(&cnt[0], nscreen);
+    warp_count(&cnt[1], nexact);
+  });
+}
+
 // coarsen_qualities_tmpl (src/Omega_h_coarsen_qualities.cpp:15-63)
 void coarsen_qualities(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, double* q2_p) {
   int dim = m.dim;
+  if (dim == 3 && ctx().screening) {
+    coarsen_qualities_screened(m, c2e_p, n, codes_p, q2_p);
+    return;
+  }
   auto ev = cview(m.ask_verts_of(1));
   auto cv = cview(m.ask_verts_of(dim));
   const Adj& v2c = m.ask_up(0, dim);
@@ -1134,8 +1375,211 @@ static void swap_loops(Mesh& m, const LO* edges_p, LO n, Arr<int>& lsize, Arr<LO
 // triangle ends a triangulation, an edge longer than max_length_allowed
 // rejects it).  The values are pure functions of the loop, so the choice is
 // the same.
+// swap3d_qualities with FP32 screening.  The reference picks, in table
+// order, the first triangulation with the largest min quality among those
+// whose new edges are all within max_len, provided that quality is > 0.  That
+// is order independent apart from ties, so it is computed from enclosures:
+//  1. every unique triangle gets an enclosure of its FP64 quality (min of 1
+//     and its two tets), every unique edge an exact "longer than max_len"
+//     flag (screened, FP64 where the threshold is inside the enclosure);
+//  2. L* = the largest lower bound of a valid triangulation; only valid
+//     triangulations with upper bound >= L* and > 0 can hold the maximum,
+//     and in each only triangles with lower bound <= its upper bound can
+//     hold its minimum: those triangles are evaluated in FP64;
+//  3. the FP64 minima of those triangulations give the reference's choice
+//     and quality, the first one winning ties.
+static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, LO n,
+                                      double* quals_p, I8* configs_p) {
+  auto tab = swap_tables();
+  Arr<int> lsize;
+  Arr<LO> lverts, leev;
+  swap_loops(m, c2e_p, n, lsize, lverts, leev);
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto ls = cview(lsize);
+  auto lv = cview(lverts);
+  auto le = cview(leev);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  unsigned long long* cnt = ctx().d_screen_counts;
+  Arr<float2> tbnd(n * kMaxUniqTris);
+  Arr<I8> over(n * kMaxUniqEdges);
+  Arr<unsigned long long> need(n);
+  Arr<float> lstar(n);
+  Arr<double> tq(n * kMaxUniqTris);
+  {
+    auto tb = view(tbnd);
+    pfor(n * kMaxUniqTris, [=] __device__(LO idx) {
+      LO i = idx / kMaxUniqTris;
+      int u = idx % kMaxUniqTris;
+      int size = ls[i];
+      unsigned ns = 0;
+      if (size >= 3 && u < tab[size * 9 + SW_NUTRI]) {
+        int otri = tab[size * 9 + SW_OTRI];
+        LO tet[4];
+        for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+        float lo = 1.0f, hi = 1.0f;
+        for (int tt = 0; tt < 2; ++tt) {
+          tet[3] = le[i * 2 + (1 - tt)];
+          FIv b = tet_quality_bounds(sv, tet);
+          lo = fminf(lo, b.lo);
+          hi = fminf(hi, b.hi);
+          LO sw = tet[1];
+          tet[1] = tet[2];
+          tet[2] = sw;
+        }
+        tb[idx] = make_float2(lo, hi);
+        ns = 2;
+      }
+      warp_count(&cnt[0], ns);
+    });
+  }
+  {
+    auto ov = view(over);
+    float thr = float_at_or_below(max_len);  // for float x: x > max_len <=> x > thr
+    pfor(n * kMaxUniqEdges, [=] __device__(LO idx) {
+      LO i = idx / kMaxUniqEdges;
+      int u = idx % kMaxUniqEdges;
+      int size = ls[i];
+      unsigned ns = 0, nx = 0;
+      if (size >= 3 && u < tab[size * 9 + SW_NUEDGE]) {
+        int oued = tab[size * 9 + SW_OUEDGE];
+        LO a = lv[i * 7 + tab[oued + u * 2]], b = lv[i * 7 + tab[oued + u * 2 + 1]];
+        FIv L = edge_len_bounds(sv, a, b);
+        bool o;
+        if (L.lo > thr) {
+          o = true;
+        } else if (L.hi <= thr) {
+          o = false;
+        } else {
+          o = edge_len_v(3, c, mt, 6, a, b) > max_len;
+          nx = 1;
+        }
+        ov[idx] = o;
+        ns = 1;
+      }
+      warp_count(&cnt[2], ns);
+      warp_count(&cnt[3], nx);
+    });
+  }
+  auto tb = cview(tbnd);
+  auto ov = cview(over);
+  {
+    auto nd = view(need);
+    auto lst = view(lstar);
+    pfor(n, [=] __device__(LO i) {
+      int size = ls[i];
+      if (size < 3) {
+        nd[i] = 0;
+        lst[i] = INFINITY;
+        return;
+      }
+      const int* h = &tab[size * 9];
+      int nmeshes = h[SW_NMESH], ntris = h[SW_NTRI], nedges = h[SW_NEDGE];
+      int omsh = h[SW_OMESH], oe2u = h[SW_OE2U];
+      float L = -INFINITY;
+      for (int mesh = 0; mesh < nmeshes; ++mesh) {
+        bool valid = true;
+        for (int e = 0; e < nedges; ++e)
+          if (ov[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]]) valid = false;
+        if (!valid) continue;
+        float mlo = 1.0f;
+        for (int t = 0; t < ntris; ++t)
+          mlo = fminf(mlo, tb[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]].x);
+        L = fmaxf(L, mlo);
+      }
+      unsigned long long mask = 0;
+      for (int mesh = 0; mesh < nmeshes; ++mesh) {
+        bool valid = true;
+        for (int e = 0; e < nedges; ++e)
+          if (ov[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]]) valid = false;
+        if (!valid) continue;
+        float mhi = 1.0f;
+        for (int t = 0; t < ntris; ++t)
+          mhi = fminf(mhi, tb[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]].y);
+        if (!(mhi >= L && mhi > 0.0f)) continue;
+        for (int t = 0; t < ntris; ++t) {
+          int u = tab[omsh + mesh * ntris + t];
+          if (tb[i * kMaxUniqTris + u].x <= mhi) mask |= 1ull << u;
+        }
+      }
+      nd[i] = mask;
+      lst[i] = L;
+    });
+  }
+  auto nd = cview(need);
+  {
+    auto q = view(tq);
+    pfor(n * kMaxUniqTris, [=] __device__(LO idx) {
+      LO i = idx / kMaxUniqTris;
+      int u = idx % kMaxUniqTris;
+      unsigned nx = 0;
+      if ((nd[i] >> u) & 1ull) {
+        int size = ls[i];
+        int otri = tab[size * 9 + SW_OTRI];
+        LO tet[4];
+        for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+        double tmq = 1.0;
+        for (int tt = 0; tt < 2; ++tt) {
+          tet[3] = le[i * 2 + (1 - tt)];
+          tmq = min2d(tmq, tet_quality_exact(sv, c, mt, tet));
+          LO sw = tet[1];
+          tet[1] = tet[2];
+          tet[2] = sw;
+        }
+        q[idx] = tmq;
+        nx = 2;
+      }
+      warp_count(&cnt[1], nx);
+    });
+  }
+  auto q = cview(tq);
+  auto lst = cview(lstar);
+  auto quals = view(quals_p, n);
+  auto configs = view(configs_p, n);
+  pfor(n, [=] __device__(LO i) {
+    int size = ls[i];
+    int best = -1;
+    double bestq = 0.0;
+    if (size < 3) {
+      quals[i] = -1.0;
+      configs[i] = -1;
+      return;
+    }
+    const int* h = &tab[size * 9];
+    int nmeshes = h[SW_NMESH], ntris = h[SW_NTRI], nedges = h[SW_NEDGE];
+    int omsh = h[SW_OMESH], oe2u = h[SW_OE2U];
+    float L = lst[i];
+    for (int mesh = 0; mesh < nmeshes; ++mesh) {
+      bool valid = true;
+      for (int e = 0; e < nedges; ++e)
+        if (ov[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]]) valid = false;
+      if (!valid) continue;
+      float mhi = 1.0f;
+      for (int t = 0; t < ntris; ++t)
+        mhi = fminf(mhi, tb[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]].y);
+      if (!(mhi >= L && mhi > 0.0f)) continue;
+      double mq = 1.0;
+      for (int t = 0; t < ntris; ++t) {
+        int u = tab[omsh + mesh * ntris + t];
+        if (tb[i * kMaxUniqTris + u].x <= mhi) mq = min2d(mq, q[i * kMaxUniqTris + u]);
+      }
+      if (mq > bestq) {
+        best = mesh;
+        bestq = mq;
+      }
+    }
+    configs[i] = I8(best);
+    quals[i] = bestq;
+  });
+}
+
 void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p,
                       I8* configs_p) {
+  if (ctx().screening) {
+    swap3d_qualities_screened(m, max_len, c2e_p, n, quals_p, configs_p);
+    return;
+  }
   auto tab = swap_tables();
   Arr<int> lsize;
   Arr<LO> lverts, leev;

@@ -36,6 +36,10 @@ void check_collapse_exposure(Mesh& m, const LO* c2e, LO n, const I8* codes_in, I
 void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e, LO n,
                                const I8* codes_in, I8* codes_out);
 void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* out2);
+// FP32 enclosures of the FP64 quality of arbitrary vertex 4-tuples and of
+// the FP64 metric length of vertex pairs, with the FP64 values (3D)
+void screen_tets(Mesh& m, const LO* tv2v, LO n, float* lo, float* hi, double* exact);
+void screen_edges(Mesh& m, const LO* ev2v, LO n, float* lo, float* hi, double* exact);
 void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,
                   I8* vert_cands, double* vert_quals, GO* vert_rails);
 Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers);

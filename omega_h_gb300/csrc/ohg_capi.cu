@@ -86,6 +86,28 @@ int ohg_context_launches(ohg_context* c, unsigned long long* out) {
   return OHG_OK;
 }
 
+int ohg_context_set_screening(ohg_context* c, int on) {
+  if (!c) {
+    g_err = "null context";
+    return OHG_ERR_INVALID;
+  }
+  c->ctx.screening = on ? 1 : 0;
+  return OHG_OK;
+}
+int ohg_context_screen_counts(ohg_context* c, unsigned long long* out4, int reset) {
+  if (!out4) {
+    g_err = "null output";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    Ctx& x = ctx();
+    OHG_CUDA(cudaMemcpyAsync(out4, x.d_screen_counts, 4 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, x.stream));
+    if (reset)
+      OHG_CUDA(cudaMemsetAsync(x.d_screen_counts, 0, 4 * sizeof(unsigned long long), x.stream));
+    x.sync();
+  });
+}
 int ohg_context_stream(ohg_context* c, void** out) {
   if (!c) return OHG_ERR_INVALID;
   *out = reinterpret_cast<void*>(c->ctx.stream);
@@ -469,6 +491,16 @@ int ohg_measure_edges_metric(ohg_mesh* m, const int* a2e, int n, double* out) {
 int ohg_measure_qualities(ohg_mesh* m, const int* a2e, int n, double* out) {
   MESH_GUARD(m);
   return guarded(m->owner, [&] { measure_qualities(m->mesh, a2e, n, out); });
+}
+int ohg_screen_tet_qualities(ohg_mesh* m, const int* tv2v, int n, float* lo, float* hi,
+                             double* exact) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] { screen_tets(m->mesh, tv2v, n, lo, hi, exact); });
+}
+int ohg_screen_edge_lengths(ohg_mesh* m, const int* ev2v, int n, float* lo, float* hi,
+                            double* exact) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] { screen_edges(m->mesh, ev2v, n, lo, hi, exact); });
 }
 int ohg_get_mident_metrics(ohg_mesh* m, const int* e, int n, double* out) {
   MESH_GUARD(m);

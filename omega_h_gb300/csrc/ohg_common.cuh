@@ -51,6 +51,11 @@ struct Ctx {
   int* d_swap_tables = nullptr;  // edge-swap triangulation tables (device copy)
   int swap_tables_len = 0;
   std::uint64_t launches = 0;
+  // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
+  int screening = 1;
+  // screening counters: cavity tets screened, tets recomputed in FP64,
+  // edge lengths screened, edge lengths recomputed in FP64
+  unsigned long long* d_screen_counts = nullptr;
   explicit Ctx(int dev);
   ~Ctx();
   Ctx(const Ctx&) = delete;

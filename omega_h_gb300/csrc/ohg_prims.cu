@@ -27,6 +27,8 @@ Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaMalloc(&d_status, sizeof(int)));
   OHG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
   OHG_CUDA(cudaMallocHost(&h_pinned, 64));
+  OHG_CUDA(cudaMalloc(&d_screen_counts, 4 * sizeof(unsigned long long)));
+  OHG_CUDA(cudaMemset(d_screen_counts, 0, 4 * sizeof(unsigned long long)));
   cudaMemPool_t pool;
   OHG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
   std::uint64_t thr = ~std::uint64_t(0);
@@ -35,6 +37,7 @@ Ctx::Ctx(int dev) : device(dev) {
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
   cudaFree(d_status);
+  cudaFree(d_screen_counts);
   if (d_swap_tables) cudaFree(d_swap_tables);
   cudaFreeHost(h_pinned);
   cudaStreamDestroy(stream);

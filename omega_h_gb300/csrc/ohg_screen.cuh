@@ -1,0 +1,300 @@
+// FP32 screening of metric edge lengths and tet mean-ratio qualities with
+// rigorous enclosures of the FP64 values.
+//
+// Every function here returns an interval [lo, hi] of floats that provably
+// contains the value the FP64 kernels (ohg_math.cuh, the reference's
+// arithmetic) compute for the same inputs.  Callers decide in FP32 where the
+// interval settles a comparison and recompute in FP64 only where it does
+// not, so every decision, and every real that is output, equals the FP64 one.
+//
+// How the enclosure is argued:
+//  * inputs are FP64 values; each is carried as a float with an absolute
+//    error bound (coordinates as hi + lo float pairs, so coordinate
+//    differences are accurate to the edge length, not the coordinate size);
+//  * sums of products (triple product, v^T M v) get the classical bound
+//    gamma_k * (the same expression on absolute values) for the rounding of
+//    both the float and the double evaluation, plus a first-order-exact
+//    perturbation term for the input errors;
+//  * monotone steps (sqrt, cbrt, the final division, the logarithmic mean)
+//    map interval endpoints with directed rounding: a correctly rounded or
+//    1-ulp double operation of a value inside [lo, hi] lands inside the same
+//    float interval because rounding is monotone and float endpoints are
+//    doubles;
+//  * bound arithmetic itself is done in round-to-nearest on non-negative
+//    terms and inflated by (1 + 2^-15), which covers the relative error of
+//    the at most ~200 roundings along any chain;
+//  * cbrtf, logf (CUDA: at most 1 ulp) and the double cbrt/log (at most 1
+//    ulp) are covered by widening their results by 2^-20 / 2^-15 relative;
+//  * anything non-finite widens the interval to [-inf, +inf].
+#pragma once
+#include <cfloat>
+#include <cstring>
+
+#include "ohg_common.cuh"
+#include "ohg_math.cuh"
+
+namespace ohg {
+
+constexpr float kU = 0x1p-24f;          // float unit roundoff
+constexpr float kInflate = 1.0f + 0x1p-15f;
+constexpr float kTiny = 1e-35f;         // covers subnormal rounding
+
+// Per-vertex screening data (built by build_vert_screen).
+//  xh = (x_hi, y_hi, z_hi, max |hi|), xl = (x_lo, y_lo, z_lo, 0) with
+//  x = x_hi + x_lo to about 2^-48 |x|;
+//  ma = (xx, yy, zz, yx), mb = (zy, zx, S0 = sum |M_ij|, sqrt(det M) as float);
+//  dkey = order-preserving integer key of det M (maxdet choice, exact);
+//  sdet = sqrt(det M) in double, identical to what the reference computes
+//  per element from the same metric.
+struct VertScreen {
+  Arr<float4> xh, xl, ma, mb;
+  Arr<long long> dkey;
+  Arr<double> sdet;
+};
+
+struct ScreenView {
+  View<const float4> xh, xl, ma, mb;
+  View<const long long> dkey;
+  View<const double> sdet;
+};
+inline ScreenView screen_view(const VertScreen& s) {
+  return {cview(s.xh), cview(s.xl), cview(s.ma), cview(s.mb), cview(s.dkey), cview(s.sdet)};
+}
+
+// order-preserving map of a double to a signed 64-bit key (+0 and -0 equal)
+__host__ __device__ __forceinline__ long long order_key(double d) {
+  if (d == 0.0) return 0;
+#ifdef __CUDA_ARCH__
+  long long b = __double_as_longlong(d);
+#else
+  long long b;
+  std::memcpy(&b, &d, sizeof(b));
+#endif
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+struct FIv {
+  float lo, hi;
+};
+
+__device__ __forceinline__ FIv widen_all() { return {-INFINITY, INFINITY}; }
+__device__ __forceinline__ bool finite_iv(FIv a) { return a.lo >= -FLT_MAX && a.hi <= FLT_MAX && a.lo <= a.hi; }
+
+// coordinate difference p1 - p0 (3 floats) and its infinity-norm error bound
+// against fl64(p1 - p0)
+__device__ __forceinline__ float sdiff3(float4 h1, float4 l1, float4 h0, float4 l0, float v[3]) {
+  v[0] = __fadd_rn(__fsub_rn(h1.x, h0.x), __fsub_rn(l1.x, l0.x));
+  v[1] = __fadd_rn(__fsub_rn(h1.y, h0.y), __fsub_rn(l1.y, l0.y));
+  v[2] = __fadd_rn(__fsub_rn(h1.z, h0.z), __fsub_rn(l1.z, l0.z));
+  float n = fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2])));
+  // 2u|v| from the float roundings, ~6u^2 |x| from the lo parts and the
+  // hi/lo split, u_double |v| from the double subtraction
+  return __fmaf_rn(n, 0x1p-22f, __fmaf_rn(__fadd_rn(h1.w, h0.w), 0x1p-44f, kTiny));
+}
+
+// q = v^T M v in float with the absolute-value sums the bound needs:
+// A = |v|^T |M| |v|, S1 = 1^T |M| |v|
+__device__ __forceinline__ float mprod(float4 ma, float4 mb, const float v[3], float& A, float& S1) {
+  float xx = ma.x, yy = ma.y, zz = ma.z, yx = ma.w, zy = mb.x, zx = mb.y;
+  float y0 = __fmaf_rn(zx, v[2], __fmaf_rn(yx, v[1], __fmul_rn(xx, v[0])));
+  float y1 = __fmaf_rn(zy, v[2], __fmaf_rn(yy, v[1], __fmul_rn(yx, v[0])));
+  float y2 = __fmaf_rn(zz, v[2], __fmaf_rn(zy, v[1], __fmul_rn(zx, v[0])));
+  float q = __fmaf_rn(v[2], y2, __fmaf_rn(v[1], y1, __fmul_rn(v[0], y0)));
+  float a0 = fabsf(v[0]), a1 = fabsf(v[1]), a2 = fabsf(v[2]);
+  float axx = fabsf(xx), ayy = fabsf(yy), azz = fabsf(zz), ayx = fabsf(yx), azy = fabsf(zy),
+        azx = fabsf(zx);
+  float w0 = __fmaf_rn(azx, a2, __fmaf_rn(ayx, a1, __fmul_rn(axx, a0)));
+  float w1 = __fmaf_rn(azy, a2, __fmaf_rn(ayy, a1, __fmul_rn(ayx, a0)));
+  float w2 = __fmaf_rn(azz, a2, __fmaf_rn(azy, a1, __fmul_rn(azx, a0)));
+  S1 = __fadd_rn(__fadd_rn(w0, w1), w2);
+  A = __fmaf_rn(a2, w2, __fmaf_rn(a1, w1, __fmul_rn(a0, w0)));
+  return q;
+}
+
+// error bound of one v^T M v against the double evaluation of the same
+// product from the double inputs, given the infinity-norm error e of v:
+// rounding of both evaluations (6 roundings per term, float and double) and
+// of the metric's conversion to float (u A), plus the input perturbation
+// 2 e S1 + e^2 S0 (exact to first and second order for a symmetric M)
+__device__ __forceinline__ float mprod_err(float A, float S1, float S0, float e) {
+  float pert = __fmaf_rn(e, __fmaf_rn(2.0f, S1, __fmul_rn(e, S0)), 0.0f);
+  return __fmaf_rn(7.1f * kU, A, __fmaf_rn(pert, 1.0f + kU, kTiny));
+}
+
+// Interval of the double metric edge length (edge_length3: the logarithmic
+// mean of sqrt(v^T M0 v) and sqrt(v^T M1 v)) between vertices a and b.
+__device__ __forceinline__ FIv edge_len_bounds(const ScreenView& s, LO a, LO b) {
+  float4 ha = s.xh[a], la = s.xl[a], hb = s.xh[b], lb = s.xl[b];
+  float v[3];
+  float e = sdiff3(hb, lb, ha, la, v);  // p1 - p0 with p0 = a
+  float qv[2], qe[2];
+  LO vs[2] = {a, b};
+  for (int k = 0; k < 2; ++k) {
+    float4 ma = s.ma[vs[k]], mb = s.mb[vs[k]];
+    float A, S1;
+    qv[k] = mprod(ma, mb, v, A, S1);
+    qe[k] = __fmul_rn(mprod_err(A, S1, mb.z, e), kInflate);
+  }
+  float l_lo[2], l_hi[2];
+  for (int k = 0; k < 2; ++k) {
+    float lo = __fsub_rd(qv[k], qe[k]);
+    float hi = __fadd_ru(qv[k], qe[k]);
+    if (!(lo > 0.0f) || !(hi <= FLT_MAX)) return widen_all();
+    l_lo[k] = __fsqrt_rd(lo);
+    l_hi[k] = __fsqrt_ru(hi);
+  }
+  // logarithmic mean, increasing in both arguments: evaluate it at the low
+  // and the high corners
+  float m[2];
+  for (int c = 0; c < 2; ++c) {
+    float x = c ? l_hi[0] : l_lo[0], y = c ? l_hi[1] : l_lo[1];
+    float r = __fdiv_rn(x, y);
+    float lm;
+    if (r > 1.01f || r < 0.99f) {
+      // |log r| >= 0.00995: float relative error below 110 u
+      lm = __fdiv_rn(__fsub_rn(x, y), logf(r));
+      lm = c ? __fmul_ru(lm, 1.0f + 0x1p-15f) : __fmul_rd(lm, 1.0f - 0x1p-15f);
+    } else {
+      // between the geometric and the arithmetic mean
+      lm = c ? __fmul_ru(__fmul_ru(__fadd_ru(x, y), 0.5f), 1.0f + 0x1p-20f)
+             : __fmul_rd(__fsqrt_rd(__fmul_rd(x, y)), 1.0f - 0x1p-20f);
+    }
+    m[c] = lm;
+  }
+  // the double evaluation's own error: relative 2^-50 (1 + 300 max(la, lb))
+  // on the log branch (|la - lb| > 1e-3 bounds the cancellation), 2^-53 on
+  // the mean branch
+  float mx = fmaxf(l_hi[0], l_hi[1]);
+  float d = __fmaf_ru(mx, 300.0f * 0x1p-50f, 0x1p-50f);
+  FIv r = {__fmul_rd(m[0], 1.0f - d), __fmul_ru(m[1], 1.0f + d)};
+  if (!finite_iv(r) || !(r.lo > 0.0f)) return widen_all();
+  return r;
+}
+
+// index (0..3) of the vertex whose metric has the largest determinant, the
+// first one on ties (maxdet_metric, src/Omega_h_metric.hpp:170-182)
+__device__ __forceinline__ int maxdet_vertex(const ScreenView& s, const LO vv[4]) {
+  int best = 0;
+  long long bk = s.dkey[vv[0]];
+  for (int i = 1; i < 4; ++i) {
+    long long k = s.dkey[vv[i]];
+    if (k > bk) {
+      best = i;
+      bk = k;
+    }
+  }
+  return best;
+}
+
+// Interval of the double tet quality (tet_quality on the maxdet metric).
+__device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {
+  int mi = maxdet_vertex(s, vv);
+  float4 ma = s.ma[vv[mi]], mb = s.mb[vv[mi]];
+  float4 h[4], l[4];
+  for (int i = 0; i < 4; ++i) {
+    h[i] = s.xh[vv[i]];
+    l[i] = s.xl[vv[i]];
+  }
+  // the six edges in the reference's order; the third, -b1, has the same
+  // v^T M v as b1
+  float ev[6][3], ee[6];
+  ee[0] = sdiff3(h[1], l[1], h[0], l[0], ev[0]);
+  ee[1] = sdiff3(h[2], l[2], h[1], l[1], ev[1]);
+  ee[2] = sdiff3(h[2], l[2], h[0], l[0], ev[2]);
+  ee[3] = sdiff3(h[3], l[3], h[0], l[0], ev[3]);
+  ee[4] = sdiff3(h[3], l[3], h[1], l[1], ev[4]);
+  ee[5] = sdiff3(h[3], l[3], h[2], l[2], ev[5]);
+  const float* b0 = ev[0];
+  const float* b1 = ev[2];
+  const float* b2 = ev[3];
+  float e0 = ee[0], e1 = ee[2], e2 = ee[3];
+  // triple product T = (b0 x b1) . b2
+  float c0 = __fmaf_rn(b0[1], b1[2], -__fmul_rn(b0[2], b1[1]));
+  float c1 = __fmaf_rn(b0[2], b1[0], -__fmul_rn(b0[0], b1[2]));
+  float c2 = __fmaf_rn(b0[0], b1[1], -__fmul_rn(b0[1], b1[0]));
+  float T = __fmaf_rn(c2, b2[2], __fmaf_rn(c1, b2[1], __fmul_rn(c0, b2[0])));
+  float P = __fmaf_rn(
+      fabsf(b2[2]), __fmaf_rn(fabsf(b0[0]), fabsf(b1[1]), __fmul_rn(fabsf(b0[1]), fabsf(b1[0]))),
+      __fmaf_rn(fabsf(b2[1]),
+                __fmaf_rn(fabsf(b0[2]), fabsf(b1[0]), __fmul_rn(fabsf(b0[0]), fabsf(b1[2]))),
+                __fmul_rn(fabsf(b2[0]), __fmaf_rn(fabsf(b0[1]), fabsf(b1[2]),
+                                                  __fmul_rn(fabsf(b0[2]), fabsf(b1[1]))))));
+  float n0 = fmaxf(fabsf(b0[0]), fmaxf(fabsf(b0[1]), fabsf(b0[2])));
+  float n1 = fmaxf(fabsf(b1[0]), fmaxf(fabsf(b1[1]), fabsf(b1[2])));
+  float n2 = fmaxf(fabsf(b2[0]), fmaxf(fabsf(b2[1]), fabsf(b2[2])));
+  float n1e = __fadd_rn(n1, e1), n2e = __fadd_rn(n2, e2);
+  float pertT = __fmul_rn(
+      6.0f, __fmaf_rn(e0, __fmul_rn(n1e, n2e), __fmaf_rn(n0, __fmul_rn(e1, n2e), __fmul_rn(n0, __fmul_rn(n1, e2)))));
+  float eT = __fmaf_rn(5.1f * kU, P, __fadd_rn(pertT, kTiny));
+  // rs = T / 6, s = rs * sqrt(det M)
+  float rs = __fdiv_rn(T, 6.0f);
+  float ers = __fmaf_rn(fabsf(rs), 0x1p-22f, __fdiv_rn(eT, 6.0f));
+  float sd = mb.w;
+  float sv = __fmul_rn(rs, sd);
+  float es = __fmaf_rn(fabsf(sv), 0x1p-22f, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
+  es = __fmul_rn(es, kInflate);
+  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
+  if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
+  float s_lo = __fsub_rd(sv, es);
+  // mean squared metric length
+  float msum = 0.0f, emsum = 0.0f, asum = 0.0f;
+  for (int i = 0; i < 6; ++i) {
+    float A, S1;
+    float q = mprod(ma, mb, ev[i], A, S1);
+    msum = __fadd_rn(msum, q);
+    asum = __fadd_rn(asum, A);
+    emsum = __fadd_rn(emsum, mprod_err(A, S1, mb.z, ee[i]));
+  }
+  float msl = __fdiv_rn(msum, 6.0f);
+  float emsl = __fmaf_rn(fabsf(msl), 0x1p-22f, __fdiv_rn(__fmaf_rn(5.1f * kU, asum, emsum), 6.0f));
+  emsl = __fmul_rn(emsl, kInflate);
+  float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
+  if (!(msl_lo > 0.0f) || !(msl_hi <= FLT_MAX)) return widen_all();
+  if (s_lo < 0.0f) {
+    // sign of the size not settled: the value is either s (>= s_lo) or a
+    // non-negative quality
+    return {s_lo, INFINITY};
+  }
+  // x = s / 0.1178511301977579, y = x * x
+  float x = __fmul_rn(sv, 8.485281374238571f);
+  float ex = __fmaf_rn(fabsf(x), 0x1p-22f, __fmul_rn(es, 8.4853f));
+  float y = __fmul_rn(x, x);
+  float ey = __fmaf_rn(fabsf(y), 0x1p-22f, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
+  ey = __fmul_rn(ey, kInflate);
+  float y_lo = fmaxf(__fsub_rd(y, ey), 0.0f), y_hi = __fadd_ru(y, ey);
+  float r_lo = __fmul_rd(cbrtf(y_lo), 1.0f - 0x1p-20f);
+  float r_hi = __fmul_ru(cbrtf(y_hi), 1.0f + 0x1p-20f);
+  FIv q = {__fdiv_rd(r_lo, msl_hi), __fdiv_ru(r_hi, msl_lo)};
+  if (!finite_iv(q)) return widen_all();
+  return q;
+}
+
+// The double tet quality with sqrt(det M) and the maxdet choice taken from
+// the per-vertex screening data: the same operations, in the same order, as
+// tet_quality(p, metric of the maxdet vertex), since sqrt(det3(M)) of a
+// vertex metric is the same double wherever it is computed.
+__device__ __forceinline__ double tet_quality_exact(const ScreenView& s, View<const double> c,
+                                                    View<const double> mt, const LO vv[4]) {
+  int mi = maxdet_vertex(s, vv);
+  V3 p[4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 3; ++j) p[i].x[j] = c[vv[i] * 3 + j];
+  M3 m = symm3(&mt[vv[mi] * 6]);
+  double sdet = s.sdet[vv[mi]];
+  V3 b0 = sub3(p[1], p[0]), b1 = sub3(p[2], p[0]), b2 = sub3(p[3], p[0]);
+  double rs = dot3(cross3(b0, b1), b2) / 6.0;
+  double sz = rs * sdet;
+  if (sz < 0) return sz;
+  V3 nb1 = {{-b1.x[0], -b1.x[1], -b1.x[2]}};
+  V3 ev[6] = {b0, sub3(p[2], p[1]), nb1, b2, sub3(p[3], p[1]), sub3(p[3], p[2])};
+  double msl = 0;
+  for (int i = 0; i < 6; ++i) msl += metric_product3(m, ev[i]);
+  msl = msl / 6;
+  double x = sz / kEquilateralTet;
+  return cbrt(x * x) / msl;
+}
+
+// builds the per-vertex screening data of a 3D mesh
+VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nverts);
+
+}  // namespace ohg

@@ -40,6 +40,18 @@ class Context:
         _lib.call("ohg_context_launches", self.handle, ctypes.byref(v))
         return v.value
 
+    def set_screening(self, on):
+        """FP32 screening with exact FP64 recheck (True, default) or FP64
+        throughout (False)."""
+        _lib.call("ohg_context_set_screening", self.handle, 1 if on else 0)
+
+    def screen_counts(self, reset=False):
+        """(tets screened, tets recomputed in FP64, lengths screened, lengths
+        recomputed in FP64) since the last reset."""
+        v = (ctypes.c_ulonglong * 4)()
+        _lib.call("ohg_context_screen_counts", self.handle, v, 1 if reset else 0)
+        return tuple(int(x) for x in v)
+
     def close(self):
         if self.handle:
             _lib.call("ohg_context_destroy", self.handle)
