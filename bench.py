@@ -13,6 +13,7 @@ Between timed steps L2 is flushed by writing a 256 MiB buffer.  With N > 1
 (torchrun) every rank adapts its own replica: the pass does not shard.
 """
 import argparse
+import hashlib
 import ctypes
 import json
 import os
@@ -219,6 +220,35 @@ def run_ours(args):
     torch.cuda.synchronize()
     gpu_launches = ctx.launches() - launches0
     total_ms = sum(ms)
+
+    # ---- precision mode: FP32 enclosures + FP64 recheck against FP64 throughout
+    def pass_digest(screening):
+        ctx.set_screening(screening)
+        ctx.screen_counts(reset=True)
+        mm = clone(base)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        mm.adapt_pass(opts)
+        e1.record(lib_stream)
+        torch.cuda.synchronize()
+        counts = ctx.screen_counts(reset=True)
+        h = hashlib.sha256()
+        for k in ("ev2v_3", "coords", "metric", "length", "quality", "class_id_3"):
+            h.update(mm.get(k).cpu().numpy().tobytes())
+        mm.close()
+        ctx.set_screening(True)
+        return e0.elapsed_time(e1), counts, h.hexdigest()
+
+    fp64_ms, _, fp64_digest = pass_digest(False)
+    scr_ms, counts, scr_digest = pass_digest(True)
+    precision = {"fp64_pass_ms": fp64_ms, "screened_pass_ms": scr_ms,
+                 "tets_screened": counts[0], "tets_fp64": counts[1],
+                 "lengths_screened": counts[2], "lengths_fp64": counts[3],
+                 "tet_recheck_fraction": counts[1] / max(counts[0], 1),
+                 "length_recheck_fraction": counts[3] / max(counts[2], 1),
+                 "outputs_bitwise_equal_to_fp64": fp64_digest == scr_digest}
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -304,6 +334,7 @@ def run_ours(args):
                              "frac": achieved / peak, "peak_kind": peak_kind,
                              "traffic": None, "algorithmic_bytes": kernels[dom]["alg_bytes"],
                              "stages": kernels},
+                "precision": precision,
                 "cpu_baseline": cpu, "gpu_launches": gpu_launches, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -1,5 +1,7 @@
 // Refine, coarsen and 3D edge-swap operators of one adapt pass, the
 // topology rebuild (modify) and field transfer, all on device arrays.
+#include <math_constants.h>
+
 #include <cfloat>
 #include <cmath>
 
@@ -1069,6 +1071,298 @@ void choose_rails(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, const doubl
   });
 }
 
+// Exact FP64 minimum quality of the cavity of collapsing v_col onto v_onto,
+// min(1, tet qualities): enclosures first, then FP64 only for the tets whose
+// lower bound does not exceed the smallest upper bound.
+__device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, LV va, LV vb,
+                                     View<const I8> vc, LO v_col, LO v_onto, unsigned* nexact) {
+  LO x0 = va[v_col], x1 = va[v_col + 1];
+  float min_hi = 1.0f;
+  for (LO x = x0; x < x1; ++x) {
+    LO vv[4];
+    if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+    min_hi = fminf(min_hi, tet_quality_bounds(sv, vv).hi);
+  }
+  double minq = 1.0;
+  for (LO x = x0; x < x1; ++x) {
+    LO vv[4];
+    if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+    if (tet_quality_bounds(sv, vv).lo <= min_hi) {
+      minq = min2d(minq, tet_quality_exact(sv, c, mt, vv));
+      ++*nexact;
+    }
+  }
+  return minq;
+}
+
+// The quality filter of coarsen_by_size (src/Omega_h_coarsen.cpp:29-58 with
+// coarsen_qualities and filter_coarsen_min_qual) from enclosures: a
+// direction whose enclosure of min(1, cavity qualities) lies on one side of
+// min_quality_allowed is decided without FP64; the others get their FP64
+// minimum.  q2 holds the FP64 minimum where it was computed and NaN where the
+// direction passed on its enclosure (its value is computed later only if
+// choose_rails_lazy needs it).
+static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa, double* q2_p) {
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  auto sv = screen_view(vs);
+  auto ev = cview(m.ask_verts_of(1));
+  auto cv = cview(m.ask_verts_of(3));
+  const Adj& v2c = m.ask_up(0, 3);
+  auto va = cview(v2c.a2ab);
+  auto vb = cview(v2c.ab2b);
+  auto vc = cview(v2c.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto codes = view(codes_p, n);
+  auto q2 = view(q2_p, n * 2);
+  unsigned long long* cnt = ctx().d_screen_counts;
+  pfor(n, [=] __device__(LO cand) {
+    LO e = c2e[cand];
+    I8 code = codes[cand];
+    unsigned nscreen = 0, nexact = 0;
+    for (int col = 0; col < 2; ++col) {
+      q2[cand * 2 + col] = -1.0;
+      if (!collapses(code, col)) continue;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      float lo = 1.0f, hi = 1.0f;
+      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
+        LO vv[4];
+        if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+        FIv b = tet_quality_bounds(sv, vv);
+        lo = fminf(lo, b.lo);
+        hi = fminf(hi, b.hi);
+        ++nscreen;
+      }
+      bool pass;
+      if (double(lo) >= mqa) {
+        pass = true;
+        q2[cand * 2 + col] = CUDART_NAN;
+      } else if (double(hi) < mqa) {
+        pass = false;
+      } else {
+        double q = collapse_min_exact(sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
+        q2[cand * 2 + col] = q;
+        pass = q >= mqa;
+      }
+      if (!pass) code = dont_collapse(code, col);
+    }
+    codes[cand] = code;
+    warp_count(&cnt[0], nscreen);
+    warp_count(&cnt[1], nexact);
+  });
+}
+
+// FP64 minima min(1, cavity qualities) of K collapse cavities (v_col[k] onto
+// v_onto[k]; every v_col distinct), written to out[k].  Enclosures select the
+// tets that can hold each minimum; those are gathered into one dense list so
+// that the FP64 evaluations run in full warps (GB300's FP64 pipe is narrow,
+// and a divergent warp occupies it as long as a full one).
+static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& vcol,
+                                  const Arr<LO>& vonto, double* out_p) {
+  LO K = vcol.size();
+  if (K == 0) return;
+  auto cv = cview(m.ask_verts_of(3));
+  const Adj& v2t = m.ask_up(0, 3);
+  auto ta = cview(v2t.a2ab);
+  auto tb = cview(v2t.ab2b);
+  auto tc = cview(v2t.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto vcv = cview(vcol);
+  auto vov = cview(vonto);
+  Arr<float> lo_at(v2t.ab2b.size());
+  Arr<float> mhi(K);
+  Arr<LO> cnt(K);
+  {
+    auto lo = view(lo_at);
+    auto mh = view(mhi);
+    auto ct = view(cnt);
+    pfor(K, [=] __device__(LO k) {
+      LO v = vcv[k], onto = vov[k];
+      float min_hi = 1.0f;
+      for (LO x = ta[v]; x < ta[v + 1]; ++x) {
+        LO vv[4];
+        if (!collapse_elem(cv, 3, tb[x], code_which_down(tc[x]), onto, vv)) {
+          lo[x] = INFINITY;
+          continue;
+        }
+        FIv b = tet_quality_bounds(sv, vv);
+        lo[x] = b.lo;
+        min_hi = fminf(min_hi, b.hi);
+      }
+      LO n = 0;
+      for (LO x = ta[v]; x < ta[v + 1]; ++x) n += lo[x] <= min_hi;
+      mh[k] = min_hi;
+      ct[k] = n;
+    });
+  }
+  Arr<LO> offs = offset_scan(cnt);
+  LO ntot = last(offs);
+  Arr<LO> tets(ntot * 4);
+  {
+    auto lo = cview(lo_at);
+    auto mh = cview(mhi);
+    auto of = cview(offs);
+    auto tt = view(tets);
+    pfor(K, [=] __device__(LO k) {
+      LO v = vcv[k], onto = vov[k];
+      LO j = of[k];
+      for (LO x = ta[v]; x < ta[v + 1]; ++x) {
+        if (!(lo[x] <= mh[k])) continue;
+        LO vv[4];
+        collapse_elem(cv, 3, tb[x], code_which_down(tc[x]), onto, vv);
+        for (int q = 0; q < 4; ++q) tt[j * 4 + q] = vv[q];
+        ++j;
+      }
+    });
+  }
+  Arr<double> eq(ntot);
+  {
+    auto tt = cview(tets);
+    auto q = view(eq);
+    pfor(ntot, [=] __device__(LO j) {
+      LO vv[4] = {tt[j * 4], tt[j * 4 + 1], tt[j * 4 + 2], tt[j * 4 + 3]};
+      q[j] = tet_quality_exact(sv, c, mt, vv);
+    });
+  }
+  unsigned long long* counts = ctx().d_screen_counts;
+  {
+    auto of = cview(offs);
+    auto q = cview(eq);
+    auto out = view(out_p, K);
+    pfor(K, [=] __device__(LO k) {
+      double minq = 1.0;
+      for (LO j = of[k]; j < of[k + 1]; ++j) minq = min2d(minq, q[j]);
+      out[k] = minq;
+      warp_count(&counts[1], unsigned(of[k + 1] - of[k]));
+    });
+  }
+}
+
+// choose_rails (src/Omega_h_collapse_rail.cpp:15-67) on lazily known
+// qualities.  The reference keeps, per vertex, the shortest candidate edge
+// that collapses the vertex, the higher quality on equal lengths and the
+// earlier edge on equal both: that is the first edge of minimal length, or,
+// when several share the minimal length, the first of those with the largest
+// quality.  Qualities are computed in FP64 only for the chosen edges (in one
+// compacted pass) and for edges tied on length.
+static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
+                              const double* quals2_p, I8* vcand_p, double* vqual_p, GO* vrail_p) {
+  LO nv = m.nverts();
+  VertScreen vs = build_vert_screen(m.coords, m.metric, nv);
+  auto sv = screen_view(vs);
+  Arr<LO> e2c = fill<LO>(m.nedges(), -1);
+  auto c2e = cview(c2e_p, n);
+  {
+    auto ec = view(e2c);
+    pfor(n, [=] __device__(LO i) { ec[c2e[i]] = i; });
+  }
+  const Adj& v2e = m.ask_up(0, 1);
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto ev = cview(m.ask_verts_of(1));
+  auto cv = cview(m.ask_verts_of(3));
+  const Adj& v2t = m.ask_up(0, 3);
+  auto ta = cview(v2t.a2ab);
+  auto tb = cview(v2t.ab2b);
+  auto tc = cview(v2t.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto len = cview(m.ask_lengths());
+  auto ec = cview(e2c);
+  auto codes = cview(codes_p, n);
+  auto quals2 = cview(quals2_p, n * 2);
+  auto vcand = view(vcand_p, nv);
+  auto vqual = view(vqual_p, nv);
+  auto vrail = view(vrail_p, nv);
+  Arr<LO> vonto(nv);
+  Arr<I8> needm(nv);
+  auto von = view(vonto);
+  auto nm = view(needm);
+  unsigned long long* cnt = ctx().d_screen_counts;
+  pfor(nv, [=] __device__(LO v) {
+    unsigned nexact = 0;
+    // the shortest length and how many eligible edges have it
+    double best_l = 0;
+    int ntie = 0;
+    LO first = -1;
+    for (LO x = va[v]; x < va[v + 1]; ++x) {
+      LO e = vb[x];
+      LO cand = ec[e];
+      if (cand == -1) continue;
+      if (!collapses(codes[cand], code_which_down(vc[x]))) continue;
+      double l = len[e];
+      if (first == -1 || l < best_l) {
+        first = x;
+        best_l = l;
+        ntie = 1;
+      } else if (l == best_l) {
+        ++ntie;
+      }
+    }
+    von[v] = -1;
+    nm[v] = 0;
+    if (first == -1) {
+      vcand[v] = 0;
+      vqual[v] = -1.0;
+      vrail[v] = -1;
+      return;
+    }
+    LO chosen = -1;
+    double best_q = -1;
+    if (ntie == 1) {
+      LO e = vb[first];
+      int eev = code_which_down(vc[first]);
+      chosen = e;
+      best_q = quals2[ec[e] * 2 + eev];
+      if (best_q != best_q) {  // computed below
+        von[v] = ev[e * 2 + (1 - eev)];
+        nm[v] = 1;
+      }
+    } else {
+      for (LO x = first; x < va[v + 1]; ++x) {
+        LO e = vb[x];
+        LO cand = ec[e];
+        if (cand == -1) continue;
+        int eev = code_which_down(vc[x]);
+        if (!collapses(codes[cand], eev)) continue;
+        if (!(len[e] == best_l)) continue;
+        double q = quals2[cand * 2 + eev];
+        if (q != q) q = collapse_min_exact(sv, c, mt, cv, ta, tb, tc, v, ev[e * 2 + (1 - eev)], &nexact);
+        if (chosen == -1 || q > best_q) {
+          chosen = e;
+          best_q = q;
+        }
+      }
+    }
+    vcand[v] = 1;
+    vqual[v] = best_q;
+    vrail[v] = chosen;
+    warp_count(&cnt[1], nexact);
+  });
+  // the FP64 quality of each chosen rail not known yet
+  Arr<LO> need = collect_marked(needm);
+  LO K = need.size();
+  if (K == 0) return;
+  Arr<LO> kv = need;
+  Arr<LO> ko(K);
+  {
+    auto nd = cview(need);
+    auto o = view(ko);
+    auto vo = cview(vonto);
+    pfor(K, [=] __device__(LO k) { o[k] = vo[nd[k]]; });
+  }
+  Arr<double> kq(K);
+  collapse_minima_exact(m, sv, kv, ko, kq.data());
+  {
+    auto nd = cview(need);
+    auto q = cview(kq);
+    pfor(K, [=] __device__(LO k) { vqual[nd[k]] = q[k]; });
+  }
+}
+
 static void filter_cands(Arr<LO>& c2e, Arr<I8>& codes, Arr<double>* q2) {
   Arr<LO> keep = collect_marked(codes);
   c2e = unmap(keep, c2e, 1);
@@ -1114,8 +1408,11 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
-  coarsen_qualities(m, c2e.data(), nc, codes.data(), q2.data());
-  {
+  bool lazy = dim == 3 && ctx().screening;
+  if (lazy) {
+    coarsen_filter_lazy(m, c2e.data(), nc, codes.data(), o.min_quality_allowed, q2.data());
+  } else {
+    coarsen_qualities(m, c2e.data(), nc, codes.data(), q2.data());
     auto cd = view(codes);
     auto q = cview(q2);
     double mqa = o.min_quality_allowed;
@@ -1132,7 +1429,12 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   Arr<I8> vc(nv);
   Arr<double> vq(nv);
   Arr<GO> vr(nv);
-  choose_rails(m, c2e.data(), c2e.size(), codes.data(), q2.data(), vc.data(), vq.data(), vr.data());
+  if (lazy)
+    choose_rails_lazy(m, c2e.data(), c2e.size(), codes.data(), q2.data(), vc.data(), vq.data(),
+                      vr.data());
+  else
+    choose_rails(m, c2e.data(), c2e.size(), codes.data(), q2.data(), vc.data(), vq.data(),
+                 vr.data());
   Arr<I8> vkeys = find_indset(m, VERT, vq, vc, &st->indset_rounds);
   Arr<LO> k2v = collect_marked(vkeys);
   LO nkeys = k2v.size();
@@ -1509,28 +1811,45 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   }
   auto nd = cview(need);
   {
+    // the triangles that need FP64, as one dense list (full warps on the
+    // narrow FP64 pipe)
+    Arr<LO> tcnt(n);
+    auto tc = view(tcnt);
+    pfor(n, [=] __device__(LO i) { tc[i] = __popcll(nd[i]); });
+    Arr<LO> toff = offset_scan(tcnt);
+    LO ntot = last(toff);
+    Arr<LO> ent(ntot);
+    auto of = cview(toff);
+    auto en = view(ent);
+    pfor(n, [=] __device__(LO i) {
+      unsigned long long mbits = nd[i];
+      LO j = of[i];
+      while (mbits) {
+        int u = __ffsll((long long)mbits) - 1;
+        mbits &= mbits - 1;
+        en[j++] = i * kMaxUniqTris + u;
+      }
+    });
     auto q = view(tq);
-    pfor(n * kMaxUniqTris, [=] __device__(LO idx) {
+    auto enc = cview(ent);
+    pfor(ntot, [=] __device__(LO j) {
+      LO idx = enc[j];
       LO i = idx / kMaxUniqTris;
       int u = idx % kMaxUniqTris;
-      unsigned nx = 0;
-      if ((nd[i] >> u) & 1ull) {
-        int size = ls[i];
-        int otri = tab[size * 9 + SW_OTRI];
-        LO tet[4];
-        for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
-        double tmq = 1.0;
-        for (int tt = 0; tt < 2; ++tt) {
-          tet[3] = le[i * 2 + (1 - tt)];
-          tmq = min2d(tmq, tet_quality_exact(sv, c, mt, tet));
-          LO sw = tet[1];
-          tet[1] = tet[2];
-          tet[2] = sw;
-        }
-        q[idx] = tmq;
-        nx = 2;
+      int size = ls[i];
+      int otri = tab[size * 9 + SW_OTRI];
+      LO tet[4];
+      for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+      double tmq = 1.0;
+      for (int tt = 0; tt < 2; ++tt) {
+        tet[3] = le[i * 2 + (1 - tt)];
+        tmq = min2d(tmq, tet_quality_exact(sv, c, mt, tet));
+        LO sw = tet[1];
+        tet[1] = tet[2];
+        tet[2] = sw;
       }
-      warp_count(&cnt[1], nx);
+      q[idx] = tmq;
+      warp_count(&cnt[1], 2u);
     });
   }
   auto q = cview(tq);

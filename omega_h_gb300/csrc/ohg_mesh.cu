@@ -9,11 +9,119 @@
 namespace ohg {
 
 // ------------------------------------------------------------ invert_adj
+// Bitonic sort of each CSR row in registers: a group of G lanes per row with
+// E entries per lane (element i = r * G + lane), G * E >= the row length.
+// Sorted entries hl = high * k + which_down become the high entity and the
+// alignment code.  Rows longer than G * E are sorted by the group's first lane
+// in memory (only reached for rows beyond 128 entries).
+template <int E>
+__global__ void k_row_sort(LO nlows, int G, const LO* off, LO* lh2hl, I8* codes, const I8* dc,
+                           bool has_dc, int k) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  LO l = LO(t / G);
+  int lane = int(t % G);
+  bool live = l < nlows;
+  LO b = live ? off[l] : 0, n = live ? off[l + 1] - b : 0;
+  LO v[E];
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    int i = r * G + lane;
+    v[r] = (i < n) ? lh2hl[b + i] : 0x7fffffff;
+  }
+  int N = G * E;
+  for (int kk = 2; kk <= N; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      if (j >= G) {
+        int jr = j / G;
+#pragma unroll
+        for (int jc = 1; jc < E; jc <<= 1) {
+          if (jr != jc) continue;
+#pragma unroll
+          for (int r = 0; r < E; ++r) {
+            const int p = r ^ jc;  // known at compile time: v stays in registers
+            if (p > r && p < E) {
+              int i = r * G + lane;
+              bool up = (i & kk) == 0;
+              LO a = v[r], c = v[p];
+              v[r] = up ? min(a, c) : max(a, c);
+              v[p] = up ? max(a, c) : min(a, c);
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          LO o = __shfl_xor_sync(0xffffffffu, v[r], j, G);
+          int i = r * G + lane;
+          bool up = (i & kk) == 0;
+          bool lower = (lane & j) == 0;
+          v[r] = (lower == up) ? min(v[r], o) : max(v[r], o);
+        }
+      }
+    }
+  }
+  if (n > N) {
+    if (lane == 0) {
+      for (LO j = b + 1; j < b + n; ++j) {
+        LO x = lh2hl[j];
+        LO i = j - 1;
+        while (i >= b && lh2hl[i] > x) {
+          lh2hl[i + 1] = lh2hl[i];
+          --i;
+        }
+        lh2hl[i + 1] = x;
+      }
+      for (LO j = b; j < b + n; ++j) {
+        LO hl = lh2hl[j];
+        I8 c = has_dc ? dc[hl] : I8(0);
+        codes[j] = make_code(has_dc && code_is_flipped(c), has_dc ? code_rotation(c) : 0, hl % k);
+        lh2hl[j] = hl / k;
+      }
+    }
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    int i = r * G + lane;
+    if (i < n) {
+      LO hl = v[r];
+      I8 c = has_dc ? dc[hl] : I8(0);
+      codes[b + i] = make_code(has_dc && code_is_flipped(c), has_dc ? code_rotation(c) : 0, hl % k);
+      lh2hl[b + i] = hl / k;
+    }
+  }
+}
+
+static void sort_rows_by_high(LO nlows, LO maxdeg, const Arr<LO>& off, Arr<LO>& lh2hl,
+                              Arr<I8>& codes, const Adj& down, int k) {
+  if (nlows <= 0) return;
+  int G = 1;
+  while (G < maxdeg && G < 32) G <<= 1;
+  int E = 1;
+  while (G * E < maxdeg && E < 4) E <<= 1;
+  long long nthreads = ((long long)nlows * G + 31) / 32 * 32;
+  Ctx& c = ctx();
+  unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
+  const I8* dc = down.has_codes ? down.codes.data() : nullptr;
+  if (E == 1)
+    k_row_sort<1><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
+                                                    codes.data(), dc, down.has_codes, k);
+  else if (E == 2)
+    k_row_sort<2><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
+                                                    codes.data(), dc, down.has_codes, k);
+  else
+    k_row_sort<4><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
+                                                    codes.data(), dc, down.has_codes, k);
+  ++c.launches;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
+}
+
 // Upward adjacency from a downward one (src/Omega_h_adj.cpp:231-263).
 // Degrees by atomics, offsets by scan, slots by atomics, then each row is
-// insertion-sorted by the high entity's use index so rows list high entities
-// in increasing order, the order the reference obtains with
-// sort_by_high_index.
+// sorted by the high entity's use index so rows list high entities in
+// increasing order, the order the reference obtains with sort_by_high_index.
 Adj invert_adj(const Adj& down, int k, LO nlows) {
   LO nhl = down.ab2b.size();
   Arr<LO> deg = fill<LO>(nlows, 0);
@@ -34,32 +142,9 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
     LO l = hl2l[hl];
     lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl;
   });
-  bool has_dc = down.has_codes;
-  auto dc = cview(down.codes);
-  auto codes = view(up.codes);
-  pfor(nlows, [=] __device__(LO l) {
-    LO b = off[l], e = off[l + 1];
-    for (LO j = b + 1; j < e; ++j) {
-      LO x = lh2hl[j];
-      LO i = j - 1;
-      while (i >= b && lh2hl[i] > x) {
-        lh2hl[i + 1] = lh2hl[i];
-        --i;
-      }
-      lh2hl[i + 1] = x;
-    }
-    for (LO j = b; j < e; ++j) {
-      LO hl = lh2hl[j];
-      int wd = hl % k;
-      if (has_dc) {
-        I8 c = dc[hl];
-        codes[j] = make_code(code_is_flipped(c), code_rotation(c), wd);
-      } else {
-        codes[j] = make_code(false, 0, wd);
-      }
-      lh2hl[j] = hl / k;
-    }
-  });
+  // rows sorted by high entity (sort_by_high_index)
+  LO maxdeg = nlows ? max_lo(deg) : 0;
+  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, down, k);
   return up;
 }
 

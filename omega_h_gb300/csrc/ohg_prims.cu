@@ -88,33 +88,70 @@ __global__ void k_tile_sums(const T* in, LO n, LO* sums) {
   }
 }
 
-// single block: exclusive scan of nb tile sums in place, total into *total
+// exclusive scan of one value per thread across a block of 1024 threads
+// (warp shuffles, then a scan of the 32 warp totals); *block_total gets the sum
+__device__ __forceinline__ LO block_exclusive_scan_1024(LO v, LO* block_total) {
+  __shared__ LO wsum[32];
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  LO incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    LO y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    LO w = wsum[lane];
+    LO wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      LO y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    wsum[lane] = wi - w;
+    if (lane == 31) *block_total = wi;
+  }
+  __syncthreads();
+  return wsum[warp] + incl - v;
+}
+
+// single block of 1024 threads: exclusive scan of nb tile sums in place,
+// total into *total
 __global__ void k_scan_sums(LO* sums, LO nb, LO* total) {
-  __shared__ LO tsum[1024];
+  __shared__ LO tot;
   LO per = (nb + blockDim.x - 1) / blockDim.x;
   LO b0 = LO(threadIdx.x) * per;
   LO s = 0;
   for (LO k = 0; k < per; ++k)
     if (b0 + k < nb) s += sums[b0 + k];
-  tsum[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    LO run = 0;
-    for (unsigned t = 0; t < blockDim.x; ++t) {
-      LO v = tsum[t];
-      tsum[t] = run;
-      run += v;
-    }
-    *total = run;
-  }
-  __syncthreads();
-  LO run = tsum[threadIdx.x];
+  LO run = block_exclusive_scan_1024(s, &tot);
+  if (threadIdx.x == 0) *total = tot;
   for (LO k = 0; k < per; ++k)
     if (b0 + k < nb) {
       LO v = sums[b0 + k];
       sums[b0 + k] = run;
       run += v;
     }
+}
+
+// one block of 1024 threads scans n <= kSmallScan counts directly
+constexpr int kSmallScanItems = 4;
+constexpr int kSmallScan = 1024 * kSmallScanItems;
+template <class T>
+__global__ void k_small_scan(const T* in, LO n, LO* out) {
+  __shared__ LO tot;
+  LO base = LO(threadIdx.x) * kSmallScanItems;
+  LO v[kSmallScanItems];
+  LO s = 0;
+  for (int k = 0; k < kSmallScanItems; ++k) {
+    v[k] = base + k < n ? LO(in[base + k]) : 0;
+    s += v[k];
+  }
+  LO run = block_exclusive_scan_1024(s, &tot);
+  for (int k = 0; k < kSmallScanItems; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) out[n] = tot;
 }
 
 template <class T>
@@ -161,6 +198,14 @@ static void scan_impl(const T* in, LO n, LO* out) {
   Ctx& c = ctx();
   if (n == 0) {
     OHG_CUDA(cudaMemsetAsync(out, 0, sizeof(LO), c.stream));
+    return;
+  }
+  if (n <= kSmallScan) {
+    k_small_scan<T><<<1, 1024, 0, c.stream>>>(in, n, out);
+    c.launches += 1;
+#ifdef OHG_CHECKED
+    checked_after_launch(__FILE__, __LINE__);
+#endif
     return;
   }
   LO nb = (n + kScanTile - 1) / kScanTile;

@@ -38,6 +38,12 @@ namespace ohg {
 constexpr float kU = 0x1p-24f;          // float unit roundoff
 constexpr float kInflate = 1.0f + 0x1p-15f;
 constexpr float kTiny = 1e-35f;         // covers subnormal rounding
+// relative rounding of one float and one double operation, with margin:
+// kC1 >= (u + u_double)(1 + u), kC2 >= 2 kC1
+constexpr float kC1 = 0x1.004p-24f;
+constexpr float kC2 = 0x1.004p-23f;
+constexpr float kSixth = 1.0f / 6.0f;    // float(1/6), within u of 1/6
+constexpr float kSixthUp = 0.16666669f;  // above 1/6
 
 // Per-vertex screening data (built by build_vert_screen).
 //  xh = (x_hi, y_hi, z_hi, max |hi|), xl = (x_lo, y_lo, z_lo, 0) with
@@ -89,7 +95,7 @@ __device__ __forceinline__ float sdiff3(float4 h1, float4 l1, float4 h0, float4 
   float n = fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2])));
   // 2u|v| from the float roundings, ~6u^2 |x| from the lo parts and the
   // hi/lo split, u_double |v| from the double subtraction
-  return __fmaf_rn(n, 0x1p-22f, __fmaf_rn(__fadd_rn(h1.w, h0.w), 0x1p-44f, kTiny));
+  return __fmaf_rn(n, kC2, __fmaf_rn(__fadd_rn(h1.w, h0.w), 0x1p-44f, kTiny));
 }
 
 // q = v^T M v in float with the absolute-value sums the bound needs:
@@ -222,16 +228,30 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
   float n0 = fmaxf(fabsf(b0[0]), fmaxf(fabsf(b0[1]), fabsf(b0[2])));
   float n1 = fmaxf(fabsf(b1[0]), fmaxf(fabsf(b1[1]), fabsf(b1[2])));
   float n2 = fmaxf(fabsf(b2[0]), fmaxf(fabsf(b2[1]), fabsf(b2[2])));
-  float n1e = __fadd_rn(n1, e1), n2e = __fadd_rn(n2, e2);
-  float pertT = __fmul_rn(
-      6.0f, __fmaf_rn(e0, __fmul_rn(n1e, n2e), __fmaf_rn(n0, __fmul_rn(e1, n2e), __fmul_rn(n0, __fmul_rn(n1, e2)))));
-  float eT = __fmaf_rn(5.1f * kU, P, __fadd_rn(pertT, kTiny));
-  // rs = T / 6, s = rs * sqrt(det M)
-  float rs = __fdiv_rn(T, 6.0f);
-  float ers = __fmaf_rn(fabsf(rs), 0x1p-22f, __fdiv_rn(eT, 6.0f));
+  // input perturbation of the trilinear T: first order |d0 . (b1 x b2)| <=
+  // e0 * sum |b1 x b2| (absolute-value form) and cyclically; every term of
+  // second and third order is below 6 e e n
+  float a0[3] = {fabsf(b0[0]), fabsf(b0[1]), fabsf(b0[2])};
+  float a1[3] = {fabsf(b1[0]), fabsf(b1[1]), fabsf(b1[2])};
+  float a2[3] = {fabsf(b2[0]), fabsf(b2[1]), fabsf(b2[2])};
+  float c12 = 0.0f, c20 = 0.0f, c01 = 0.0f;
+  for (int i = 0; i < 3; ++i) {
+    int j = (i + 1) % 3, k = (i + 2) % 3;
+    c12 = __fadd_rn(c12, __fmaf_rn(a1[j], a2[k], __fmul_rn(a1[k], a2[j])));
+    c20 = __fadd_rn(c20, __fmaf_rn(a2[j], a0[k], __fmul_rn(a2[k], a0[j])));
+    c01 = __fadd_rn(c01, __fmaf_rn(a0[j], a1[k], __fmul_rn(a0[k], a1[j])));
+  }
+  float first = __fmaf_rn(e0, c12, __fmaf_rn(e1, c20, __fmul_rn(e2, c01)));
+  float second = __fmul_rn(
+      6.0f, __fmaf_rn(__fmul_rn(e0, e1), __fadd_rn(n2, e2),
+                      __fmaf_rn(__fmul_rn(e0, e2), n1, __fmul_rn(__fmul_rn(e1, e2), n0))));
+  float eT = __fmaf_rn(5.1f * kU, P, __fadd_rn(__fadd_rn(first, second), kTiny));
+  // rs = T / 6 (here T times float(1/6): one more rounding, so kC2), s = rs * sqrt(det M)
+  float rs = __fmul_rn(T, kSixth);
+  float ers = __fmaf_rn(fabsf(rs), kC2, __fmul_rn(eT, kSixthUp));
   float sd = mb.w;
   float sv = __fmul_rn(rs, sd);
-  float es = __fmaf_rn(fabsf(sv), 0x1p-22f, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
+  float es = __fmaf_rn(fabsf(sv), kC2, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
   es = __fmul_rn(es, kInflate);
   if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
   if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
@@ -245,11 +265,12 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
     asum = __fadd_rn(asum, A);
     emsum = __fadd_rn(emsum, mprod_err(A, S1, mb.z, ee[i]));
   }
-  float msl = __fdiv_rn(msum, 6.0f);
-  float emsl = __fmaf_rn(fabsf(msl), 0x1p-22f, __fdiv_rn(__fmaf_rn(5.1f * kU, asum, emsum), 6.0f));
+  float msl = __fmul_rn(msum, kSixth);
+  float emsl = __fmaf_rn(fabsf(msl), kC2, __fmul_rn(__fmaf_rn(5.1f * kU, asum, emsum), kSixthUp));
   emsl = __fmul_rn(emsl, kInflate);
   float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
-  if (!(msl_lo > 0.0f) || !(msl_hi <= FLT_MAX)) return widen_all();
+  // the range keeps __fdividef within its documented 2-ulp error
+  if (!(msl_lo > 1e-30f) || !(msl_hi < 1e30f)) return widen_all();
   if (s_lo < 0.0f) {
     // sign of the size not settled: the value is either s (>= s_lo) or a
     // non-negative quality
@@ -257,14 +278,32 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
   }
   // x = s / 0.1178511301977579, y = x * x
   float x = __fmul_rn(sv, 8.485281374238571f);
-  float ex = __fmaf_rn(fabsf(x), 0x1p-22f, __fmul_rn(es, 8.4853f));
+  float ex = __fmaf_rn(fabsf(x), kC2, __fmul_rn(es, 8.4853f));
   float y = __fmul_rn(x, x);
-  float ey = __fmaf_rn(fabsf(y), 0x1p-22f, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
+  float ey = __fmaf_rn(fabsf(y), kC1, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
   ey = __fmul_rn(ey, kInflate);
-  float y_lo = fmaxf(__fsub_rd(y, ey), 0.0f), y_hi = __fadd_ru(y, ey);
-  float r_lo = __fmul_rd(cbrtf(y_lo), 1.0f - 0x1p-20f);
-  float r_hi = __fmul_ru(cbrtf(y_hi), 1.0f + 0x1p-20f);
-  FIv q = {__fdiv_rd(r_lo, msl_hi), __fdiv_ru(r_hi, msl_lo)};
+  // cbrt over [y - ey, y + ey] from one cbrtf (at most 1 ulp; the double
+  // cbrt at most 1 ulp too): with d = ey / y,
+  //   (1 + d)^(1/3) <= 1 + d/3 and (1 - d)^(1/3) >= 1 - d/3 - d^2 (d <= 1/2)
+  float r_lo, r_hi;
+  if (!(y < 1e30f) || !(ey < 1e30f)) return widen_all();  // keeps __fdividef in range
+  if (!(y > 1e-30f)) {
+    r_lo = 0.0f;
+    r_hi = __fmul_ru(cbrtf(__fadd_ru(fmaxf(y, 0.0f), ey)), 1.0f + 0x1p-20f);
+  } else {
+    float cy = cbrtf(y);
+    float d = __fmul_ru(__fdividef(ey, y), 1.0f + 0x1p-21f);
+    r_hi = __fmul_ru(__fmul_ru(cy, 1.0f + 0x1p-21f), __fmaf_ru(d, 0.33333334f, 1.0f));
+    if (d <= 0.5f) {
+      float f = __fsub_rd(__fmaf_rd(-d, 0.33333334f, 1.0f), __fmul_ru(d, d));
+      r_lo = __fmul_rd(__fmul_rd(cy, 1.0f - 0x1p-21f), f);
+    } else {
+      r_lo = 0.0f;
+    }
+  }
+  // q = r / msl; __fdividef is within 2 ulp for divisors in [2^-126, 2^126]
+  FIv q = {__fmul_rd(__fdividef(r_lo, msl_hi), 1.0f - 0x1p-21f),
+           __fmul_ru(__fdividef(r_hi, msl_lo), 1.0f + 0x1p-21f)};
   if (!finite_iv(q)) return widen_all();
   return q;
 }
