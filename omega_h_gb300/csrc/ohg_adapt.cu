@@ -171,49 +171,64 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
     auto s0 = view(a);
     pfor(n, [=] __device__(LO i) { s0[i] = cd[i] ? UNKNOWN : NOT_IN; });
   }
-  Arr<int> flag(1);
-  auto fl = view(flag);
+  // Rounds are launched in batches of kIndsetBatch with one flag per round
+  // and one host read per batch: a round after the one that left no vertex
+  // UNKNOWN changes nothing, so the state is the converged one and the
+  // count is taken from the first round whose flag stayed clear.
+  constexpr int kIndsetBatch = 8;
+  Arr<int> flags(kIndsetBatch);
   auto xa = cview(g.a2ab);
   auto xb = cview(g.ab2b);
   auto q = cview(quality);
   int rounds = 0;
-  int any = count_marked(cands) > 0;
+  bool any = count_marked(cands) > 0;
   while (any) {
     if (rounds >= kMaxIndsetRounds) throw Error(5, "independent set did not converge");
-    OHG_CUDA(cudaMemsetAsync(flag.data(), 0, sizeof(int), c.stream));
-    auto old = cview(a);
-    auto nw = view(b);
-    pfor(n, [=] __device__(LO v) {
-      I8 sv = old[v];
-      if (sv != UNKNOWN) {
-        nw[v] = sv;
-        return;
-      }
-      LO beg = xa[v], end = xa[v + 1];
-      for (LO j = beg; j < end; ++j)
-        if (old[xb[j]] == IN) {
-          nw[v] = NOT_IN;
+    OHG_CUDA(cudaMemsetAsync(flags.data(), 0, kIndsetBatch * sizeof(int), c.stream));
+    for (int r = 0; r < kIndsetBatch; ++r) {
+      int* fl = flags.data() + r;
+      auto old = cview(a);
+      auto nw = view(b);
+      pfor(n, [=] __device__(LO v) {
+        I8 sv = old[v];
+        if (sv != UNKNOWN) {
+          nw[v] = sv;
           return;
         }
-      double qv = q[v];
-      for (LO j = beg; j < end; ++j) {
-        LO u = xb[j];
-        if (old[u] == NOT_IN) continue;
-        double qu = q[u];
-        bool less = (qu != qv) ? (qu < qv) : (u < v);
-        if (!less) {
-          nw[v] = UNKNOWN;
-          fl[0] = 1;
-          return;
+        LO beg = xa[v], end = xa[v + 1];
+        for (LO j = beg; j < end; ++j)
+          if (old[xb[j]] == IN) {
+            nw[v] = NOT_IN;
+            return;
+          }
+        double qv = q[v];
+        for (LO j = beg; j < end; ++j) {
+          LO u = xb[j];
+          if (old[u] == NOT_IN) continue;
+          double qu = q[u];
+          bool less = (qu != qv) ? (qu < qv) : (u < v);
+          if (!less) {
+            nw[v] = UNKNOWN;
+            fl[0] = 1;
+            return;
+          }
         }
-      }
-      nw[v] = IN;
-    });
-    std::swap(a, b);
-    ++rounds;
-    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flag.data(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        nw[v] = IN;
+      });
+      std::swap(a, b);
+    }
+    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flags.data(), kIndsetBatch * sizeof(int),
+                             cudaMemcpyDeviceToHost, c.stream));
     c.sync();
-    any = c.h_pinned[0];
+    int done = -1;
+    for (int r = 0; r < kIndsetBatch && done < 0; ++r)
+      if (!c.h_pinned[r]) done = r;
+    if (done >= 0) {
+      rounds += done + 1;
+      any = false;
+    } else {
+      rounds += kIndsetBatch;
+    }
   }
   if (rounds_out) *rounds_out += rounds;
   return a;
@@ -1117,6 +1132,7 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
   auto codes = view(codes_p, n);
   auto q2 = view(q2_p, n * 2);
   unsigned long long* cnt = ctx().d_screen_counts;
+  float mqa_f = float_at_or_above(mqa);  // for float x: x >= mqa <=> x >= mqa_f
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     I8 code = codes[cand];
@@ -1125,8 +1141,10 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
       q2[cand * 2 + col] = -1.0;
       if (!collapses(code, col)) continue;
       LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      // the minimum only falls as tets are added: once an upper bound is
+      // below the threshold the direction fails, whatever the other tets are
       float lo = 1.0f, hi = 1.0f;
-      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
+      for (LO x = va[v_col]; x < va[v_col + 1] && hi >= mqa_f; ++x) {
         LO vv[4];
         if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
         FIv b = tet_quality_bounds(sv, vv);
@@ -1135,10 +1153,10 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
         ++nscreen;
       }
       bool pass;
-      if (double(lo) >= mqa) {
+      if (lo >= mqa_f) {
         pass = true;
         q2[cand * 2 + col] = CUDART_NAN;
-      } else if (double(hi) < mqa) {
+      } else if (hi < mqa_f) {
         pass = false;
       } else {
         double q = collapse_min_exact(sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);

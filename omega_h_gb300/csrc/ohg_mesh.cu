@@ -4,6 +4,7 @@
 
 #include "ohg_math.cuh"
 #include "ohg_mesh.cuh"
+#include "ohg_screen.cuh"
 #include "ohg_workload.hpp"
 
 namespace ohg {
@@ -15,13 +16,25 @@ namespace ohg {
 // alignment code.  Rows longer than G * E are sorted by the group's first lane
 // in memory (only reached for rows beyond 128 entries).
 template <int E>
-__global__ void k_row_sort(LO nlows, int G, const LO* off, LO* lh2hl, I8* codes, const I8* dc,
-                           bool has_dc, int k) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  LO l = LO(t / G);
-  int lane = int(t % G);
+__device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, LO j) {
+  LO hl = key >> 3;
+  int c = key & 7;
+  codes[j] = make_code(c & 1, (c >> 1) & 3, hl % k);
+  lh2hl[j] = hl / k;
+}
+
+// rows with lo_len < n <= hi_len are sorted here; the others are left alone
+template <int E>
+__global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off, LO* lh2hl,
+                           I8* codes, int k) {
+  const int G = 1 << lg;
+  unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  LO l = LO(t >> lg);
+  int lane = int(t & unsigned(G - 1));
   bool live = l < nlows;
   LO b = live ? off[l] : 0, n = live ? off[l + 1] - b : 0;
+  if (n <= lo_len || n > hi_len) n = 0;  // not this launch's row (all lanes of the row agree)
+  if (G == 32 && n == 0) return;         // a warp is one row here: the whole warp leaves
   LO v[E];
 #pragma unroll
   for (int r = 0; r < E; ++r) {
@@ -71,51 +84,48 @@ __global__ void k_row_sort(LO nlows, int G, const LO* off, LO* lh2hl, I8* codes,
         }
         lh2hl[i + 1] = x;
       }
-      for (LO j = b; j < b + n; ++j) {
-        LO hl = lh2hl[j];
-        I8 c = has_dc ? dc[hl] : I8(0);
-        codes[j] = make_code(has_dc && code_is_flipped(c), has_dc ? code_rotation(c) : 0, hl % k);
-        lh2hl[j] = hl / k;
-      }
+      for (LO j = b; j < b + n; ++j) unpack_use<E>(lh2hl[j], k, lh2hl, codes, j);
     }
     return;
   }
 #pragma unroll
   for (int r = 0; r < E; ++r) {
     int i = r * G + lane;
-    if (i < n) {
-      LO hl = v[r];
-      I8 c = has_dc ? dc[hl] : I8(0);
-      codes[b + i] = make_code(has_dc && code_is_flipped(c), has_dc ? code_rotation(c) : 0, hl % k);
-      lh2hl[b + i] = hl / k;
-    }
+    if (i < n) unpack_use<E>(v[r], k, lh2hl, codes, b + i);
   }
 }
 
+// Rows of up to 32 entries are sorted by groups of G lanes (G the smallest
+// power of two >= min(longest row, 32)), one entry per lane; when longer rows
+// exist, a second launch sorts them by whole warps with up to 4 entries per
+// lane (rows beyond 128 by one lane in memory).
 static void sort_rows_by_high(LO nlows, LO maxdeg, const Arr<LO>& off, Arr<LO>& lh2hl,
-                              Arr<I8>& codes, const Adj& down, int k) {
+                              Arr<I8>& codes, int k) {
   if (nlows <= 0) return;
-  int G = 1;
-  while (G < maxdeg && G < 32) G <<= 1;
-  int E = 1;
-  while (G * E < maxdeg && E < 4) E <<= 1;
-  long long nthreads = ((long long)nlows * G + 31) / 32 * 32;
   Ctx& c = ctx();
-  unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
-  const I8* dc = down.has_codes ? down.codes.data() : nullptr;
-  if (E == 1)
-    k_row_sort<1><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
-                                                    codes.data(), dc, down.has_codes, k);
-  else if (E == 2)
-    k_row_sort<2><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
-                                                    codes.data(), dc, down.has_codes, k);
-  else
-    k_row_sort<4><<<nblocks, kBlock, 0, c.stream>>>(nlows, G, off.data(), lh2hl.data(),
-                                                    codes.data(), dc, down.has_codes, k);
-  ++c.launches;
+  auto launch = [&](int lg, int E, LO lo_len, LO hi_len) {
+    long long nthreads = (((long long)nlows << lg) + 31) / 32 * 32;
+    if (nthreads + kBlock > 0xffffffffLL) throw Error(8, "invert_adj: too many rows for one launch");
+    unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
+    if (E == 1)
+      k_row_sort<1><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
+                                                      lh2hl.data(), codes.data(), k);
+    else if (E == 2)
+      k_row_sort<2><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
+                                                      lh2hl.data(), codes.data(), k);
+    else
+      k_row_sort<4><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
+                                                      lh2hl.data(), codes.data(), k);
+    ++c.launches;
 #ifdef OHG_CHECKED
-  checked_after_launch(__FILE__, __LINE__);
+    checked_after_launch(__FILE__, __LINE__);
 #endif
+  };
+  int lg = 0;
+  while ((1 << lg) < maxdeg && lg < 5) ++lg;
+  // rows of 0..32 entries (a row of one entry still needs unpacking)
+  launch(lg, 1, -1, 32);
+  if (maxdeg > 32) launch(5, maxdeg > 64 ? 4 : 2, 32, 0x7fffffff);
 }
 
 // Upward adjacency from a downward one (src/Omega_h_adj.cpp:231-263).
@@ -134,17 +144,24 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   up.ab2b = Arr<LO>(nhl);
   up.codes = Arr<I8>(nhl);
   up.has_codes = true;
+  // slots by atomics; each slot holds the use index hl and the use's down
+  // code (flip, rotation) packed as hl * 8 + code, read here where the
+  // reads of the down arrays are coalesced
+  if (nhl >= (1 << 28)) throw Error(8, "invert_adj: more than 2^28 uses");
   Arr<LO> pos = fill<LO>(nlows, 0);
   auto off = cview(up.a2ab);
   auto ps = view(pos);
   auto lh2hl = view(up.ab2b);
+  bool has_dc = down.has_codes;
+  auto dc = cview(down.codes);
   pfor(nhl, [=] __device__(LO hl) {
     LO l = hl2l[hl];
-    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl;
+    LO c = has_dc ? LO(dc[hl] & 7) : 0;
+    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl * 8 + c;
   });
   // rows sorted by high entity (sort_by_high_index)
   LO maxdeg = nlows ? max_lo(deg) : 0;
-  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, down, k);
+  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, k);
   return up;
 }
 
@@ -186,26 +203,47 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
     int uu = a % nlh;
     LO av[3];
     for (int j = 0; j < deg; ++j) av[j] = h[hh * nvh + down_template(hd, ld, uu, j)];
-    LO fv = av[0];
+    // The matching low entity contains every vertex of the use, so any of
+    // their upward lists finds it; the shortest is scanned.  The alignment
+    // code depends only on where av[0] sits in the match.
+    int js = 0;
+    LO dmin = va[av[0] + 1] - va[av[0]];
+    for (int j = 1; j < deg; ++j) {
+      LO dj = va[av[j] + 1] - va[av[j]];
+      if (dj < dmin) {
+        dmin = dj;
+        js = j;
+      }
+    }
+    LO fv = av[js];
     int found = 0;
     for (LO x = va[fv]; x < va[fv + 1]; ++x) {
       LO b = vb[x];
-      int wd = code_which_down(vc[x]);
+      int wj = code_which_down(vc[x]);  // position of av[js] in b
       LO bb = b * deg;
       I8 mc = 0;
       bool match = false;
       if (deg == 2) {
-        if (av[1] == lv[bb + (1 - wd)]) {
-          mc = make_code(false, wd, 0);
+        if (av[1 - js] == lv[bb + (1 - wj)]) {
+          mc = make_code(false, js == 0 ? wj : 1 - wj, 0);
           match = true;
         }
       } else {
-        if (av[1] == lv[bb + (wd + 1) % 3] && av[2] == lv[bb + (wd + 2) % 3]) {
+        // rotate so that av[0] leads: av[0] is at position (wj - js) mod 3
+        int wd = (wj - js + 3) % 3;
+        if (av[1] == lv[bb + (wd + 1) % 3] && av[2] == lv[bb + (wd + 2) % 3] &&
+            av[0] == lv[bb + wd]) {
           mc = make_code(false, rotation_to_first(3, wd), 0);
           match = true;
-        } else if (av[1] == lv[bb + (wd + 2) % 3] && av[2] == lv[bb + (wd + 1) % 3]) {
-          mc = make_code(true, rotation_to_first(3, wd), 0);
-          match = true;
+        } else {
+          // flipped: av = (b[w], b[w-1], b[w-2]) with av[0] at position w;
+          // av[js] at wj gives w = wj + js
+          int wf = (wj + js) % 3;
+          if (av[0] == lv[bb + wf] && av[1] == lv[bb + (wf + 2) % 3] &&
+              av[2] == lv[bb + (wf + 1) % 3]) {
+            mc = make_code(true, rotation_to_first(3, wf), 0);
+            match = true;
+          }
         }
       }
       if (match) {
@@ -869,6 +907,18 @@ void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
   bool all = a2e == nullptr;
   auto ae = cview(a2e, na);
   auto o = view(out, na);
+  if (dim == 3 && na > 0) {
+    // per-vertex det M (maxdet choice) and sqrt(det M), computed once per
+    // vertex instead of four and one times per element: the same doubles
+    VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+    auto sv = screen_view(vs);
+    pfor(na, [=] __device__(LO a) {
+      LO e = all ? a : ae[a];
+      LO v[4] = {ev[e * 4], ev[e * 4 + 1], ev[e * 4 + 2], ev[e * 4 + 3]};
+      o[a] = tet_quality_exact(sv, c, mt, v);
+    });
+    return;
+  }
   pfor(na, [=] __device__(LO a) {
     LO e = all ? a : ae[a];
     LO v[4];
