@@ -166,6 +166,9 @@ int ohg_choose_rails(ohg_mesh* mesh, const int* cands2edges_dev, int n,
                      long long* vert_rails_dev);
 /* mark_sliver_layers (src/Omega_h_mark.hpp:23) */
 int ohg_mark_sliver_layers(ohg_mesh* mesh, double qual_ceil, int nlayers, signed char* out_dev);
+/* swap2d_qualities (src/Omega_h_swap2d_qualities.cpp:70-81): 2D meshes */
+int ohg_swap2d_qualities(ohg_mesh* mesh, double max_length_allowed, const int* cands2edges_dev,
+                         int n, double* quals_dev);
 /* swap3d_qualities (src/Omega_h_swap3d.hpp:9-10) */
 int ohg_swap3d_qualities(ohg_mesh* mesh, double max_length_allowed, const int* cands2edges_dev,
                          int n, double* quals_dev, signed char* configs_dev);

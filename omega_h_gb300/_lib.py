@@ -73,6 +73,7 @@ SIGNATURES = {
     "ohg_coarsen_qualities": [c_void_p, c_void_p, c_int, c_void_p, c_void_p],
     "ohg_choose_rails": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "ohg_mark_sliver_layers": [c_void_p, c_double, c_int, c_void_p],
+    "ohg_swap2d_qualities": [c_void_p, c_double, c_void_p, c_int, c_void_p],
     "ohg_swap3d_qualities": [c_void_p, c_double, c_void_p, c_int, c_void_p, c_void_p],
     "ohg_find_indset": [c_void_p, c_int, c_void_p, c_void_p, c_void_p, P(c_int)],
     "ohg_time_stage": [c_void_p, c_char_p, c_int, P(ctypes.c_float), P(c_double)],

@@ -2027,28 +2027,67 @@ Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
   return a;
 }
 
-bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
-  if (m.dim != 3) return false;
-  Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
-  Arr<I8> edc = mark_down(m, 3, 1, ec);
-  {
-    auto e = view(edc);
-    auto cd = cview(m.class_dim[1]);
-    pfor(m.nedges(), [=] __device__(LO i) { e[i] = e[i] && cd[i] == 3; });
+// swap2d cavity (src/Omega_h_swap2d_qualities.cpp:35-46): the vertices
+// opposite an interior edge in its two triangles, ordered by the triangles'
+// rotation codes
+__device__ __forceinline__ bool swap2d_opposite(LV ea, LV eb, View<const I8> ec, LV tv, LO edge,
+                                                LO ov[2]) {
+  if (ea[edge + 1] - ea[edge] != 2) return false;
+  for (int i = 0; i < 2; ++i) {
+    LO x = ea[edge] + i;
+    I8 code = ec[x];
+    int rot = code_rotation(code) & 1;
+    ov[rot] = tv[eb[x] * 3 + opposite_template(2, 1, code_which_down(code))];
   }
-  if (count_marked(edc) == 0) return false;
-  Arr<LO> c2e = collect_marked(edc);
+  return true;
+}
+
+// swap2d_qualities_tmpl (src/Omega_h_swap2d_qualities.cpp:15-67): -1 where the
+// new diagonal (ov[0], ov[1]) is longer than max_len, else the min of 1 and
+// the two new triangles' qualities
+void swap2d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p) {
+  const Adj& e2t = m.ask_up(1, 2);
+  auto ea = cview(e2t.a2ab);
+  auto eb = cview(e2t.ab2b);
+  auto ec = cview(e2t.codes);
+  auto tv = cview(m.ask_verts_of(2));
+  auto ev = cview(m.ask_verts_of(1));
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto q = view(quals_p, n);
+  int* st = ctx().d_status;
+  pfor(n, [=] __device__(LO cand) {
+    LO edge = c2e[cand];
+    LO ov[2];
+    if (!swap2d_opposite(ea, eb, ec, tv, edge, ov)) {
+      raise_status(st, ST_TOPOLOGY);
+      q[cand] = -1.0;
+      return;
+    }
+    if (edge_len_v(2, c, mt, 3, ov[0], ov[1]) > max_len) {
+      q[cand] = -1.0;
+      return;
+    }
+    LO e0 = ev[edge * 2], e1 = ev[edge * 2 + 1];
+    double minq = 1.0;
+    for (int i = 0; i < 2; ++i) {
+      LO ntv[3] = {i == 0 ? e1 : e0, ov[i], ov[1 - i]};
+      minq = min2d(minq, elem_quality_v(2, c, mt, ntv));
+    }
+    q[cand] = minq;
+  });
+}
+
+// filter_swap_improve (src/Omega_h_swap.cpp:35-43) and find_indset over the
+// kept candidates: the key edges
+static Arr<LO> swap_keys(Mesh& m, Arr<LO> c2e, Arr<double> cq, PassStats* st) {
   LO nc = c2e.size();
-  Arr<double> cq(nc);
-  Arr<I8> cc(nc);
-  swap3d_qualities(m, o.max_length_allowed, c2e.data(), nc, cq.data(), cc.data());
   LO ne = m.nedges();
-  Arr<I8> econfig = map_onto(cc, c2e, ne, I8(-1), 1);
-  // filter_swap_improve (src/Omega_h_swap.cpp:35-43)
   Arr<I8> keep(nc);
   {
     auto eq = cview(m.ask_qualities());
-    const Adj& e2t = m.ask_up(1, 3);
+    const Adj& e2t = m.ask_up(1, m.dim);
     auto ea = cview(e2t.a2ab);
     auto eb = cview(e2t.ab2b);
     auto ce = cview(c2e);
@@ -2062,15 +2101,116 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     });
   }
   Arr<LO> kept = collect_marked(keep);
-  if (kept.size() == 0) return false;
+  if (kept.size() == 0) return Arr<LO>(0);
   c2e = unmap(kept, c2e, 1);
   cq = unmap(kept, cq, 1);
   Arr<I8> is_cand = mark_image(c2e, ne);
   Arr<double> edge_q = map_onto(cq, c2e, ne, -1.0, 1);
   Arr<I8> keys = find_indset(m, EDGE, edge_q, is_cand, &st->indset_rounds);
   Arr<LO> k2e = collect_marked(keys);
+  st->swap_keys = k2e.size();
+  return k2e;
+}
+
+// modify + transfer_swap: every product inherits the key edge's
+// classification; lengths and qualities of products are re-measured
+static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2v) {
+  int dim = m.dim;
   LO nkeys = k2e.size();
-  st->swap_keys = nkeys;
+  Mesh nm;
+  nm.dim = dim;
+  nm.nents[0] = m.nverts();
+  nm.coords = m.coords;
+  nm.metric = m.metric;
+  nm.class_dim[0] = m.class_dim[0];
+  nm.class_id[0] = m.class_id[0];
+  Arr<LO> old_lows2new = iota(m.nverts());
+  for (int d = 1; d <= dim; ++d) {
+    ModifyOut mo = modify_ents_adapt(m, nm, d, EDGE, k2e, k2p[d], pv2v[d], old_lows2new);
+    LO nnew = nm.nents[d];
+    LO np = mo.prods2new.size();
+    Arr<I8> pcd(np);
+    Arr<LO> pci(np);
+    {
+      auto ke = cview(k2e);
+      auto kp = cview(k2p[d]);
+      auto ecd = cview(m.class_dim[1]);
+      auto eci = cview(m.class_id[1]);
+      auto a = view(pcd);
+      auto b = view(pci);
+      pfor(nkeys, [=] __device__(LO k) {
+        for (LO p = kp[k]; p < kp[k + 1]; ++p) {
+          a[p] = ecd[ke[k]];
+          b[p] = eci[ke[k]];
+        }
+      });
+    }
+    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
+    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
+    xfer_lengths_qualities(m, nm, d, mo);
+    old_lows2new = mo.old2new;
+  }
+  m = std::move(nm);
+}
+
+// swap_edges_2d (src/Omega_h_swap2d.cpp:14-80) with swap2d_topology
+// (src/Omega_h_swap2d_topology.cpp:37-95): per key one new edge
+// (ov[0], ov[1]) and two new triangles (ev[1-i], ov[i], ov[1-i])
+static bool swap_edges_2d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2e) {
+  LO nc = c2e.size();
+  Arr<double> cq(nc);
+  swap2d_qualities(m, o.max_length_allowed, c2e.data(), nc, cq.data());
+  if (ctx().take_status() & ST_TOPOLOGY) throw Error(10, "2D edge swap: an interior edge without two triangles");
+  Arr<LO> k2e = swap_keys(m, c2e, cq, st);
+  LO nkeys = k2e.size();
+  if (nkeys == 0) return false;
+  Arr<LO> k2p[4], pv2v[4];
+  k2p[1] = iota(nkeys + 1);
+  k2p[2] = Arr<LO>(nkeys + 1);
+  pv2v[1] = Arr<LO>(nkeys * 2);
+  pv2v[2] = Arr<LO>(nkeys * 6);
+  {
+    const Adj& e2t = m.ask_up(1, 2);
+    auto ea = cview(e2t.a2ab);
+    auto eb = cview(e2t.ab2b);
+    auto ec = cview(e2t.codes);
+    auto tv = cview(m.ask_verts_of(2));
+    auto ev = cview(m.ask_verts_of(1));
+    auto ke = cview(k2e);
+    auto p2 = view(k2p[2]);
+    auto v1 = view(pv2v[1]);
+    auto v2 = view(pv2v[2]);
+    pfor(nkeys + 1, [=] __device__(LO k) { p2[k] = 2 * k; });
+    pfor(nkeys, [=] __device__(LO k) {
+      LO e = ke[k];
+      LO ov[2];
+      swap2d_opposite(ea, eb, ec, tv, e, ov);
+      v1[k * 2] = ov[0];
+      v1[k * 2 + 1] = ov[1];
+      LO e0 = ev[e * 2], e1 = ev[e * 2 + 1];
+      for (int i = 0; i < 2; ++i) {
+        LO t = k * 2 + i;
+        v2[t * 3] = i == 0 ? e1 : e0;
+        v2[t * 3 + 1] = ov[i];
+        v2[t * 3 + 2] = ov[1 - i];
+      }
+    });
+  }
+  swap_rebuild(m, k2e, k2p, pv2v);
+  return true;
+}
+
+// swap_edges_3d (src/Omega_h_swap3d.cpp:14-84)
+static bool swap_edges_3d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2e) {
+  LO nc = c2e.size();
+  Arr<double> cq(nc);
+  Arr<I8> cc(nc);
+  swap3d_qualities(m, o.max_length_allowed, c2e.data(), nc, cq.data(), cc.data());
+  LO ne = m.nedges();
+  Arr<I8> econfig = map_onto(cc, c2e, ne, I8(-1), 1);
+  Arr<LO> k2e = swap_keys(m, c2e, cq, st);
+  LO nkeys = k2e.size();
+  if (nkeys == 0) return false;
   // swap3d_keys_to_prods + swap3d_topology (src/Omega_h_swap3d_topology.cpp)
   auto tab = swap_tables();
   Arr<int> lsize;
@@ -2157,42 +2297,24 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     });
   }
   if (ctx().take_status() & ST_TOPOLOGY) throw Error(10, "edge swap found an invalid edge ring");
-  Mesh nm;
-  nm.dim = 3;
-  nm.nents[0] = m.nverts();
-  nm.coords = m.coords;
-  nm.metric = m.metric;
-  nm.class_dim[0] = m.class_dim[0];
-  nm.class_id[0] = m.class_id[0];
-  Arr<LO> old_lows2new = iota(m.nverts());
-  for (int d = 1; d <= 3; ++d) {
-    ModifyOut mo = modify_ents_adapt(m, nm, d, EDGE, k2e, k2p[d], pv2v[d], old_lows2new);
-    LO nnew = nm.nents[d];
-    // transfer_inherit_swap: every product inherits the key edge's class
-    LO np = mo.prods2new.size();
-    Arr<I8> pcd(np);
-    Arr<LO> pci(np);
-    {
-      auto ke = cview(k2e);
-      auto kp = cview(k2p[d]);
-      auto ecd = cview(m.class_dim[1]);
-      auto eci = cview(m.class_id[1]);
-      auto a = view(pcd);
-      auto b = view(pci);
-      pfor(nkeys, [=] __device__(LO k) {
-        for (LO p = kp[k]; p < kp[k + 1]; ++p) {
-          a[p] = ecd[ke[k]];
-          b[p] = eci[ke[k]];
-        }
-      });
-    }
-    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
-    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
-    xfer_lengths_qualities(m, nm, d, mo);
-    old_lows2new = mo.old2new;
-  }
-  m = std::move(nm);
+  swap_rebuild(m, k2e, k2p, pv2v);
   return true;
+}
+
+// swap_edges (src/Omega_h_swap.cpp:45-53) after swap_part1
+// (src/Omega_h_swap.cpp:14-27): interior edges of the sliver layers
+bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
+  int dim = m.dim;
+  Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
+  Arr<I8> edc = mark_down(m, dim, 1, ec);
+  {
+    auto e = view(edc);
+    auto cd = cview(m.class_dim[1]);
+    pfor(m.nedges(), [=] __device__(LO i) { e[i] = e[i] && cd[i] == dim; });
+  }
+  if (count_marked(edc) == 0) return false;
+  Arr<LO> c2e = collect_marked(edc);
+  return dim == 3 ? swap_edges_3d(m, o, st, c2e) : swap_edges_2d(m, o, st, c2e);
 }
 
 // ------------------------------------------------------------ the pass
@@ -2211,7 +2333,7 @@ PassStats adapt_pass(Mesh& m, const AdaptOpts& o) {
   st.did_coarsen = coarsen_by_size(m, o, &st);
   OHG_CUDA(cudaEventRecord(e2, c.stream));
   st.min_quality = min_f64(m.ask_qualities());
-  if (st.min_quality < o.min_quality_desired && m.dim == 3) st.did_swap = swap_edges(m, o, &st);
+  if (st.min_quality < o.min_quality_desired) st.did_swap = swap_edges(m, o, &st);
   OHG_CUDA(cudaEventRecord(e3, c.stream));
   c.sync();
   OHG_CUDA(cudaEventElapsedTime(&st.ms_refine, e0, e1));

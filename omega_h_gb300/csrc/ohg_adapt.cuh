@@ -43,6 +43,8 @@ void screen_edges(Mesh& m, const LO* ev2v, LO n, float* lo, float* hi, double* e
 void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,
                   I8* vert_cands, double* vert_quals, GO* vert_rails);
 Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers);
+// swap2d_qualities (src/Omega_h_swap2d_qualities.cpp:15-81)
+void swap2d_qualities(Mesh& m, double max_length_allowed, const LO* c2e, LO n, double* quals);
 void swap3d_qualities(Mesh& m, double max_length_allowed, const LO* c2e, LO n, double* quals,
                       I8* configs);
 

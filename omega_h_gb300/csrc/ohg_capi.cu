@@ -548,6 +548,11 @@ int ohg_mark_sliver_layers(ohg_mesh* m, double ceil, int nlayers, signed char* o
     OHG_CUDA(cudaMemcpyAsync(out, a.data(), size_t(a.size()), cudaMemcpyDeviceToDevice, ctx().stream));
   });
 }
+int ohg_swap2d_qualities(ohg_mesh* m, double ml, const int* c2e, int n, double* q) {
+  MESH_GUARD(m);
+  if (m->mesh.dim != 2) return OHG_ERR_INVALID;
+  return guarded(m->owner, [&] { swap2d_qualities(m->mesh, ml, c2e, n, q); });
+}
 int ohg_swap3d_qualities(ohg_mesh* m, double ml, const int* c2e, int n, double* q, signed char* cf) {
   MESH_GUARD(m);
   if (m->mesh.dim != 3) return OHG_ERR_INVALID;

@@ -409,4 +409,136 @@ OHG_HD bool average_metric3(const double* m0, const double* m1, double* out) {
   return ok;
 }
 
+// ------------------------------------------------------------ eigen (2x2)
+// The 2x2 symmetric eigendecomposition of src/Omega_h_eigen.hpp (quadratic
+// roots, a double root below 5e-5 taken as isotropic) and the 2D
+// log-Euclidean metric average, in the reference's operation order.
+struct V2 {
+  double x[2];
+};
+struct M2 {
+  V2 c[2];  // columns
+};
+OHG_HD V2 mv2(const M2& a, V2 b) {
+  V2 c;
+  for (int i = 0; i < 2; ++i) c.x[i] = a.c[0].x[i] * b.x[0];
+  for (int i = 0; i < 2; ++i) c.x[i] = c.x[i] + a.c[1].x[i] * b.x[1];
+  return c;
+}
+OHG_HD M2 mm2(const M2& a, const M2& b) {
+  M2 c;
+  for (int j = 0; j < 2; ++j) c.c[j] = mv2(a, b.c[j]);
+  return c;
+}
+OHG_HD M2 tr2(const M2& a) {
+  M2 b;
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) b.c[i].x[j] = a.c[j].x[i];
+  return b;
+}
+OHG_HD M2 ident2() {
+  M2 a;
+  a.c[0].x[0] = 1;
+  a.c[0].x[1] = 0;
+  a.c[1].x[0] = 0;
+  a.c[1].x[1] = 1;
+  return a;
+}
+OHG_HD double det2m(const M2& m) {
+  double a = m.c[0].x[0], b = m.c[1].x[0], c = m.c[0].x[1], d = m.c[1].x[1];
+  return a * d - b * c;
+}
+// packed (xx, yy, yx)
+OHG_HD M2 symm2(const double* v) {
+  M2 s;
+  s.c[0].x[0] = v[0];
+  s.c[1].x[1] = v[1];
+  s.c[1].x[0] = v[2];
+  s.c[0].x[1] = s.c[1].x[0];
+  return s;
+}
+struct Eig2 {
+  M2 q;
+  V2 l;
+  bool ok;
+};
+OHG_HD Eig2 eigen2(M2 m) {
+  Eig2 r;
+  r.ok = true;
+  double nm = 0.0;
+  for (int j = 0; j < 2; ++j)
+    for (int i = 0; i < 2; ++i) nm = max2d(nm, fabs(m.c[j].x[i]));
+  if (nm <= 1e-10) {
+    r.q = ident2();
+    r.l.x[0] = r.l.x[1] = 0;
+    return r;
+  }
+  for (int j = 0; j < 2; ++j)
+    for (int i = 0; i < 2; ++i) m.c[j].x[i] = m.c[j].x[i] / nm;
+  double tr = m.c[0].x[0];
+  tr += m.c[1].x[1];
+  double a = -tr;
+  double b = det2m(m);
+  double disc = sq(a) - 4. * b;
+  if (fabs(disc) < 5e-5) {
+    double rt = -a / 2.;
+    r.l.x[0] = r.l.x[1] = rt;
+    r.q = ident2();
+  } else {
+    if (!(disc > 0.0)) r.ok = false;
+    double roots[2] = {(-a + sqrt(disc)) / 2., (-a - sqrt(disc)) / 2.};
+    for (int i = 0; i < 2; ++i) {
+      M2 s = m;
+      for (int k = 0; k < 2; ++k) s.c[k].x[k] = s.c[k].x[k] - roots[i];
+      M2 ts = tr2(s);
+      int best = 0;
+      double bn = sqrt(ts.c[0].x[0] * ts.c[0].x[0] + ts.c[0].x[1] * ts.c[0].x[1]);
+      double n1 = sqrt(ts.c[1].x[0] * ts.c[1].x[0] + ts.c[1].x[1] * ts.c[1].x[1]);
+      if (n1 > bn) {
+        best = 1;
+        bn = n1;
+      }
+      if (!(bn > 1e-10)) r.ok = false;
+      double r0 = ts.c[best].x[0] / bn, r1 = ts.c[best].x[1] / bn;
+      r.q.c[i].x[0] = -r1;
+      r.q.c[i].x[1] = r0;
+      r.l.x[i] = roots[i];
+    }
+  }
+  r.l.x[0] = r.l.x[0] * nm;
+  r.l.x[1] = r.l.x[1] * nm;
+  return r;
+}
+OHG_HD M2 compose_ortho2(const M2& q, V2 l) {
+  M2 d;
+  d.c[0].x[1] = d.c[1].x[0] = 0.0;
+  d.c[0].x[0] = l.x[0];
+  d.c[1].x[1] = l.x[1];
+  return mm2(mm2(q, d), tr2(q));
+}
+// exp(mean(log M0, log M1)) for two packed 2D metrics
+OHG_HD bool average_metric2(const double* m0, const double* m1, double* out) {
+  M2 am;
+  am.c[0].x[0] = am.c[0].x[1] = am.c[1].x[0] = am.c[1].x[1] = 0.0;
+  bool ok = true;
+  for (int k = 0; k < 2; ++k) {
+    Eig2 e = eigen2(symm2(k == 0 ? m0 : m1));
+    ok = ok && e.ok;
+    for (int i = 0; i < 2; ++i) e.l.x[i] = log(e.l.x[i]);
+    M2 L = compose_ortho2(e.q, e.l);
+    for (int j = 0; j < 2; ++j)
+      for (int i = 0; i < 2; ++i) am.c[j].x[i] = am.c[j].x[i] + L.c[j].x[i];
+  }
+  for (int j = 0; j < 2; ++j)
+    for (int i = 0; i < 2; ++i) am.c[j].x[i] = am.c[j].x[i] / 2;
+  Eig2 e = eigen2(am);
+  ok = ok && e.ok;
+  for (int i = 0; i < 2; ++i) e.l.x[i] = exp(e.l.x[i]);
+  M2 r = compose_ortho2(e.q, e.l);
+  out[0] = r.c[0].x[0];
+  out[1] = r.c[1].x[1];
+  out[2] = r.c[1].x[0];
+  return ok;
+}
+
 }  // namespace ohg

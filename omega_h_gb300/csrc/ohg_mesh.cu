@@ -933,15 +933,24 @@ void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
   auto mt = cview(m.metric);
   bool all = edges == nullptr;
   auto ed = cview(edges, n);
-  auto o = view(out, n * 6);
+  int mc = m.mcomp();
+  auto o = view(out, n * mc);
   int* st = ctx().d_status;
-  if (m.dim != 3) throw Error(8, "mident_metrics: 2D metrics are not supported yet");
-  pfor(n, [=] __device__(LO a) {
-    LO e = all ? a : ed[a];
-    double r[6];
-    if (!average_metric3(&mt[ev[e * 2] * 6], &mt[ev[e * 2 + 1] * 6], r)) raise_status(st, ST_NUMERIC);
-    for (int k = 0; k < 6; ++k) o[a * 6 + k] = r[k];
-  });
+  if (m.dim == 3) {
+    pfor(n, [=] __device__(LO a) {
+      LO e = all ? a : ed[a];
+      double r[6];
+      if (!average_metric3(&mt[ev[e * 2] * 6], &mt[ev[e * 2 + 1] * 6], r)) raise_status(st, ST_NUMERIC);
+      for (int k = 0; k < 6; ++k) o[a * 6 + k] = r[k];
+    });
+  } else {
+    pfor(n, [=] __device__(LO a) {
+      LO e = all ? a : ed[a];
+      double r[3];
+      if (!average_metric2(&mt[ev[e * 2] * 3], &mt[ev[e * 2 + 1] * 3], r)) raise_status(st, ST_NUMERIC);
+      for (int k = 0; k < 3; ++k) o[a * 3 + k] = r[k];
+    });
+  }
 }
 
 const Arr<double>& Mesh::ask_lengths() {

@@ -165,7 +165,8 @@ class Mesh:
         return out
 
     def mident_metrics(self, edges):
-        out = torch.empty(edges.numel() * 6, dtype=torch.float64, device=self._dev())
+        mc = 6 if self.dim == 3 else 3
+        out = torch.empty(edges.numel() * mc, dtype=torch.float64, device=self._dev())
         _lib.call("ohg_get_mident_metrics", self.handle, _ptr(edges), edges.numel(), _ptr(out))
         return out
 
@@ -209,6 +210,12 @@ class Mesh:
         out = torch.empty(self.nelems(), dtype=torch.int8, device=self._dev())
         _lib.call("ohg_mark_sliver_layers", self.handle, qual_ceil, nlayers, _ptr(out))
         return out
+
+    def swap2d_qualities(self, max_length_allowed, c2e):
+        q = torch.empty(c2e.numel(), dtype=torch.float64, device=self._dev())
+        _lib.call("ohg_swap2d_qualities", self.handle, max_length_allowed, _ptr(c2e), c2e.numel(),
+                  _ptr(q))
+        return q
 
     def swap3d_qualities(self, max_length_allowed, c2e):
         q = torch.empty(c2e.numel(), dtype=torch.float64, device=self._dev())

@@ -439,6 +439,7 @@ V<I8> mark_sliver_layers(Mesh& m, double qual_ceil, int nlayers);
 void swap3d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e,
                       V<double>* quals, V<I8>* configs);
 V<I8> filter_swap_improve(Mesh& m, const V<LO>& c2e, const V<double>& quals);
+V<double> swap2d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e);
 
 // the whole pass: refine -> coarsen -> swap (if min quality < desired)
 struct PassResult {

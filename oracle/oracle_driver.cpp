@@ -201,24 +201,28 @@ static void dump_coarsen_stage(Mesh& m, const AdaptOpts& o) {
 static void dump_swap_stage(Mesh& m, const AdaptOpts& o) {
   V<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
   dump("s_elem_cands", ec);
-  const Adj& e2t = m.ask_up(1, 3);
+  const Adj& e2t = m.ask_up(1, m.dim);
   V<I8> edc((size_t)(m.nedges()), 0);
   bool any = false;
   for (LO e = 0; e < m.nedges(); ++e) {
     for (LO j = e2t.a2ab[e]; j < e2t.a2ab[e + 1]; ++j)
       if (ec[e2t.ab2b[j]]) edc[e] = 1;
-    edc[e] = edc[e] && m.class_dim[1][e] == 3;
+    edc[e] = edc[e] && m.class_dim[1][e] == m.dim;
     any |= bool(edc[e]);
   }
   dump("s_edge_cands", edc);
   if (!any) return;
   V<LO> c2e = collect_marked(edc);
   V<double> cq;
-  V<I8> cc;
-  swap3d_qualities(m, o, c2e, &cq, &cc);
+  if (m.dim == 3) {
+    V<I8> cc;
+    swap3d_qualities(m, o, c2e, &cq, &cc);
+    dump("s_cand_configs", cc);
+  } else {
+    cq = swap2d_qualities(m, o, c2e);
+  }
   dump("s_cands2edges", c2e);
   dump("s_cand_quals", cq);
-  dump("s_cand_configs", cc);
   V<I8> keep = filter_swap_improve(m, c2e, cq);
   dump("s_keep", keep);
   V<LO> kept;
@@ -285,7 +289,7 @@ int main(int argc, char** argv) {
     const V<double>& q = m.ask_qualities();
     double minq = q[0];
     for (double x : q) minq = std::min(minq, x);
-    if (minq < o.min_quality_desired && dim == 3) {
+    if (minq < o.min_quality_desired) {
       if (stages) dump_swap_stage(m, o);
       r.did_swap = swap_edges(m, o);
     }

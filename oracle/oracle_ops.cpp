@@ -963,10 +963,51 @@ void swap3d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e, V<double>* 
   }
 }
 
+// swap2d_qualities_tmpl (src/Omega_h_swap2d_qualities.cpp:15-67): the two
+// triangles of an interior edge, replaced by the two across the other
+// diagonal (ov[0], ov[1]); -1 where that diagonal is longer than
+// max_length_allowed, else the min of 1 and the two new qualities.
+static void swap2d_cavity(Mesh& m, LO edge, LO ov[2]) {
+  const Adj& e2t = m.ask_up(1, 2);
+  const V<LO>& tv2v = m.ask_verts_of(2);
+  OCHECK(e2t.a2ab[edge + 1] == 2 + e2t.a2ab[edge]);
+  for (int i = 0; i < 2; ++i) {
+    LO et = e2t.a2ab[edge] + i;
+    I8 code = e2t.codes[et];
+    int tte = code_which_down(code), rot = code_rotation(code);
+    LO t = e2t.ab2b[et];
+    ov[rot] = tv2v[(size_t)(t) * 3 + opposite_template(2, 1, tte)];
+  }
+}
+V<double> swap2d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e) {
+  const V<LO>& ev2v = m.ask_verts_of(1);
+  V<double> out(c2e.size());
+  for (size_t cand = 0; cand < c2e.size(); ++cand) {
+    LO edge = c2e[cand];
+    LO ov[2];
+    swap2d_cavity(m, edge, ov);
+    const double* p0 = &m.coords[(size_t)(ov[0]) * 2];
+    const double* p1 = &m.coords[(size_t)(ov[1]) * 2];
+    double l = edge_length2(p0, p1, &m.metric[(size_t)(ov[0]) * 3], &m.metric[(size_t)(ov[1]) * 3]);
+    if (l > o.max_length_allowed) {
+      out[cand] = -1.0;
+      continue;
+    }
+    LO ev[2] = {ev2v[(size_t)(edge) * 2], ev2v[(size_t)(edge) * 2 + 1]};
+    double minq = 1.0;
+    for (int i = 0; i < 2; ++i) {
+      LO ntv[3] = {ev[1 - i], ov[i], ov[1 - i]};
+      minq = min2(minq, elem_quality(m, ntv));
+    }
+    out[cand] = minq;
+  }
+  return out;
+}
+
 // filter_swap_improve (src/Omega_h_swap.cpp:35-43)
 V<I8> filter_swap_improve(Mesh& m, const V<LO>& c2e, const V<double>& cq) {
   const V<double>& eq = m.ask_qualities();
-  const Adj& e2t = m.ask_up(1, 3);
+  const Adj& e2t = m.ask_up(1, m.dim);
   V<I8> keep(c2e.size());
   for (size_t i = 0; i < c2e.size(); ++i) {
     LO e = c2e[i];
@@ -977,18 +1018,97 @@ V<I8> filter_swap_improve(Mesh& m, const V<LO>& c2e, const V<double>& cq) {
   return keep;
 }
 
-// swap_edges_3d (src/Omega_h_swap3d.cpp:14-84, src/Omega_h_swap.cpp:14-43)
+// products inherit the key edge's classification; lengths and qualities
+// are re-measured for products (transfer_swap, src/Omega_h_transfer.cpp)
+static void swap_rebuild(Mesh& m, const V<LO>& k2e, V<LO>* k2p, V<LO>* pv2v) {
+  int dim = m.dim;
+  LO nkeys = LO(k2e.size());
+  Mesh nm;
+  nm.dim = dim;
+  nm.nents[0] = m.nverts();
+  nm.coords = m.coords;
+  nm.metric = m.metric;
+  nm.class_dim[0] = m.class_dim[0];
+  nm.class_id[0] = m.class_id[0];
+  V<LO> old_lows2new = iota_lo(m.nverts());
+  for (int d = 1; d <= dim; ++d) {
+    ModifyOut mo = modify_ents_adapt(m, nm, d, EDGE, k2e, k2p[d], pv2v[d], old_lows2new);
+    LO nnew = nm.nents[d];
+    V<I8> pcd((size_t)(k2p[d][nkeys]));
+    V<LO> pci((size_t)(k2p[d][nkeys]));
+    for (LO k = 0; k < nkeys; ++k)
+      for (LO p = k2p[d][k]; p < k2p[d][k + 1]; ++p) {
+        pcd[p] = m.class_dim[1][k2e[k]];
+        pci[p] = m.class_id[1][k2e[k]];
+      }
+    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
+    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
+    xfer_lengths_qualities(m, nm, d, mo);
+    old_lows2new = mo.old2new;
+  }
+  m = std::move(nm);
+}
+
+// swap_edges_2d (src/Omega_h_swap2d.cpp:14-80) with swap2d_topology
+// (src/Omega_h_swap2d_topology.cpp:37-95): one new edge (ov[0], ov[1]) and
+// two new triangles (ev[1-i], ov[i], ov[1-i]) per key
+static bool swap_edges_2d(Mesh& m, const AdaptOpts& o, const V<LO>& c2e_in) {
+  V<LO> c2e = c2e_in;
+  V<double> cq = swap2d_qualities(m, o, c2e);
+  V<I8> keepm = filter_swap_improve(m, c2e, cq);
+  V<LO> keep = collect_marked(keepm);
+  c2e = unmap(keep, c2e, 1);
+  cq = unmap(keep, cq, 1);
+  if (c2e.empty()) return false;
+  LO ne = m.nedges();
+  V<I8> is_cand = mark_image(c2e, ne);
+  V<double> edge_q((size_t)(ne), -1.0);
+  map_into(cq, c2e, edge_q, 1);
+  V<I8> keys = find_indset(m, EDGE, edge_q, is_cand);
+  V<LO> k2e = collect_marked(keys);
+  LO nkeys = LO(k2e.size());
+  const V<LO>& ev2v = m.ask_verts_of(1);
+  V<LO> k2p[4], pv2v[4];
+  k2p[1].resize((size_t)(nkeys) + 1);
+  k2p[2].resize((size_t)(nkeys) + 1);
+  for (LO k = 0; k <= nkeys; ++k) {
+    k2p[1][k] = k;
+    k2p[2][k] = 2 * k;
+  }
+  pv2v[1].resize((size_t)(nkeys) * 2);
+  pv2v[2].resize((size_t)(nkeys) * 6);
+  for (LO k = 0; k < nkeys; ++k) {
+    LO e = k2e[k];
+    LO ov[2];
+    swap2d_cavity(m, e, ov);
+    pv2v[1][(size_t)(k) * 2] = ov[0];
+    pv2v[1][(size_t)(k) * 2 + 1] = ov[1];
+    LO ev[2] = {ev2v[(size_t)(e) * 2], ev2v[(size_t)(e) * 2 + 1]};
+    for (int i = 0; i < 2; ++i) {
+      size_t t = (size_t)(k) * 2 + i;
+      pv2v[2][t * 3] = ev[1 - i];
+      pv2v[2][t * 3 + 1] = ov[i];
+      pv2v[2][t * 3 + 2] = ov[1 - i];
+    }
+  }
+  swap_rebuild(m, k2e, k2p, pv2v);
+  return true;
+}
+
+// swap_edges (src/Omega_h_swap.cpp:45-53): swap_part1 (src/Omega_h_swap.cpp:
+// 14-27), then swap_edges_3d (src/Omega_h_swap3d.cpp:14-84) or swap_edges_2d
 bool swap_edges(Mesh& m, const AdaptOpts& o) {
-  OCHECK(m.dim == 3);
+  int dim = m.dim;
   V<I8> ecands = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
-  V<I8> edc = mark_down(m, 3, 1, ecands);
+  V<I8> edc = mark_down(m, dim, 1, ecands);
   bool any = false;
   for (size_t e = 0; e < edc.size(); ++e) {
-    edc[e] = edc[e] && (m.class_dim[1][e] == 3);
+    edc[e] = edc[e] && (m.class_dim[1][e] == dim);
     any |= bool(edc[e]);
   }
   if (!any) return false;
   V<LO> c2e = collect_marked(edc);
+  if (dim == 2) return swap_edges_2d(m, o, c2e);
   V<double> cq;
   V<I8> cc;
   swap3d_qualities(m, o, c2e, &cq, &cc);
@@ -1050,31 +1170,7 @@ bool swap_edges(Mesh& m, const AdaptOpts& o) {
       }
     }
   }
-  Mesh nm;
-  nm.dim = 3;
-  nm.nents[0] = m.nverts();
-  nm.coords = m.coords;
-  nm.metric = m.metric;
-  nm.class_dim[0] = m.class_dim[0];
-  nm.class_id[0] = m.class_id[0];
-  V<LO> old_lows2new = iota_lo(m.nverts());
-  for (int d = 1; d <= 3; ++d) {
-    ModifyOut mo = modify_ents_adapt(m, nm, d, EDGE, k2e, k2p[d], pv2v[d], old_lows2new);
-    LO nnew = nm.nents[d];
-    // transfer_swap: products inherit the key edge's classification
-    V<I8> pcd((size_t)(k2p[d][nkeys]));
-    V<LO> pci((size_t)(k2p[d][nkeys]));
-    for (LO k = 0; k < nkeys; ++k)
-      for (LO p = k2p[d][k]; p < k2p[d][k + 1]; ++p) {
-        pcd[p] = m.class_dim[1][k2e[k]];
-        pci[p] = m.class_id[1][k2e[k]];
-      }
-    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
-    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
-    xfer_lengths_qualities(m, nm, d, mo);
-    old_lows2new = mo.old2new;
-  }
-  m = std::move(nm);
+  swap_rebuild(m, k2e, k2p, pv2v);
   return true;
 }
 
@@ -1086,7 +1182,7 @@ PassResult adapt_pass(Mesh& m, const AdaptOpts& o) {
   const V<double>& q = m.ask_qualities();
   double minq = 1.79769313486231570815e+308;
   for (double x : q) minq = min2(minq, x);
-  if (minq < o.min_quality_desired && m.dim == 3) r.did_swap = swap_edges(m, o);
+  if (minq < o.min_quality_desired) r.did_swap = swap_edges(m, o);
   return r;
 }
 

@@ -29,6 +29,7 @@
 #include <Omega_h_refine_qualities.hpp>
 #include <Omega_h_shape.hpp>
 #include <Omega_h_swap.hpp>
+#include <Omega_h_swap2d.hpp>
 #include <Omega_h_swap3d.hpp>
 #include <Omega_h_swap3d_loop.hpp>
 #include <Omega_h_swap3d_tables.hpp>
@@ -241,11 +242,15 @@ static void dump_swap_stage(Mesh* mesh, AdaptOpts const& opts) {
   if (get_max(edges_are_cands) <= 0) return;
   auto cands2edges = collect_marked(edges_are_cands);
   Reals cand_quals;
-  Read<I8> cand_configs;
-  swap3d_qualities(mesh, opts, cands2edges, &cand_quals, &cand_configs);
+  if (mesh->dim() == 3) {
+    Read<I8> cand_configs;
+    swap3d_qualities(mesh, opts, cands2edges, &cand_quals, &cand_configs);
+    dump("s_cand_configs", cand_configs);
+  } else {
+    cand_quals = swap2d_qualities(mesh, opts, cands2edges);
+  }
   dump("s_cands2edges", cands2edges);
   dump("s_cand_quals", cand_quals);
-  dump("s_cand_configs", cand_configs);
   auto keep = filter_swap_improve(mesh, cands2edges, cand_quals);
   dump("s_keep", keep);
   filter_swap(keep, &cands2edges, &cand_quals);
@@ -365,7 +370,7 @@ int main(int argc, char** argv) {
   mesh.set_parting(OMEGA_H_GHOSTED);
   double minq = get_min(mesh.ask_qualities());
   bool did_swap = false;
-  if (minq < opts.min_quality_desired && dim == 3) {
+  if (minq < opts.min_quality_desired) {
     if (stages) dump_swap_stage(&mesh, opts);
     t1 = std::chrono::steady_clock::now();
     did_swap = swap_edges(&mesh, opts);

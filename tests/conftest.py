@@ -18,6 +18,12 @@ SMALL_CASES = {
     "box12_shock": (3, 12, 1, 7, 0.2),
     "box12_blayer": (3, 12, 2, 3, 0.2),
 }
+# 2D squares, 2048 triangles each (2D defaults: min_quality_allowed 0.3)
+SMALL_CASES_2D = {
+    "sq32_iso": (2, 32, 0, 5, 0.3),
+    "sq32_shock": (2, 32, 1, 5, 0.3),
+    "sq32_blayer": (2, 32, 2, 5, 0.3),
+}
 BIG_CASE = ("box64_shock", (3, 64, 1, 2024, 0.2))
 # arrays that are metadata, not per-stage outputs
 SKIP_KEYS = ("meta_json", "swap3d_tables", "opts", "opts_values", "r_rep2md")

@@ -40,6 +40,11 @@ CASES = {
     "box12_blayer": (3, 12, 2, 3, 0.2, True),
     # 64^3 shock metric (1,572,864 tets, 274,625 verts): digests only
     "box64_shock": (3, 64, 1, 2024, 0.2, False),
+    # 2D 32^2 boxes (2048 triangles), 2D defaults (min_quality_allowed 0.3):
+    # isotropic (coarsen, swap), shock (refine, coarsen, swap), boundary layer
+    "sq32_iso": (2, 32, 0, 5, 0.3, True),
+    "sq32_shock": (2, 32, 1, 5, 0.3, True),
+    "sq32_blayer": (2, 32, 2, 5, 0.3, True),
 }
 
 

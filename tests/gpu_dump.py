@@ -12,13 +12,21 @@ import torch
 from omega_h_gb300 import _lib
 from omega_h_gb300.mesh import Context, Mesh, adapt_opts
 
-MESH_ARRAYS3 = ["coords", "metric", "down_1", "ev2v_2", "down_2", "downcodes_2", "ev2v_3",
-                "down_3", "downcodes_3"] + [f"class_dim_{d}" for d in range(4)] + \
-               [f"class_id_{d}" for d in range(4)]
-ADJ_ARRAYS3 = [f"up_{k}_{lo}{hi}" for lo in range(3) for hi in range(lo + 1, 4)
-               for k in ("a2ab", "ab2b", "codes")] + \
-              ["down31", "downcodes31", "star_a2ab_0", "star_ab2b_0", "star_a2ab_1",
-               "star_ab2b_1", "dual_a2ab", "dual_ab2b"]
+def mesh_arrays(dim):
+    names = ["coords", "metric", "down_1", "ev2v_2", "down_2", "downcodes_2"]
+    if dim == 3:
+        names += ["ev2v_3", "down_3", "downcodes_3"]
+    return names + [f"class_dim_{d}" for d in range(dim + 1)] + \
+        [f"class_id_{d}" for d in range(dim + 1)]
+
+
+def adj_arrays(dim):
+    names = [f"up_{k}_{lo}{hi}" for lo in range(dim) for hi in range(lo + 1, dim + 1)
+             for k in ("a2ab", "ab2b", "codes")]
+    if dim == 3:
+        names += ["down31", "downcodes31"]
+    return names + ["star_a2ab_0", "star_ab2b_0", "star_a2ab_1", "star_ab2b_1", "dual_a2ab",
+                    "dual_ab2b"]
 
 
 def np_(t):
@@ -27,7 +35,7 @@ def np_(t):
 
 def dump_mesh(m, prefix, out, with_length=False, with_quality=False):
     out[prefix + "nents"] = np.array([float(m.nents(0))])
-    for name in MESH_ARRAYS3:
+    for name in mesh_arrays(m.dim):
         out[prefix + name] = np_(m.get(name))
     if with_length:
         out[prefix + "length"] = np_(m.get("length"))
@@ -123,21 +131,25 @@ def coarsen_stage(m, o, out):
 def swap_stage(m, o, out):
     ec = m.mark_sliver_layers(o.min_quality_desired, o.nsliver_layers)
     out["s_elem_cands"] = np_(ec)
-    a2ab = m.get("up_a2ab_13").long()
-    ab2b = m.get("up_ab2b_13").long()
+    dim = m.dim
+    a2ab = m.get(f"up_a2ab_1{dim}").long()
+    ab2b = m.get(f"up_ab2b_1{dim}").long()
     deg = a2ab[1:] - a2ab[:-1]
     owner = torch.repeat_interleave(torch.arange(deg.numel(), device=deg.device), deg)
     edc = torch.zeros(m.nents(1), dtype=torch.int32, device=deg.device)
     edc.index_reduce_(0, owner, ec[ab2b].to(torch.int32), "amax", include_self=True)
-    edc = ((edc > 0) & (m.get("class_dim_1") == 3)).to(torch.int8)
+    edc = ((edc > 0) & (m.get("class_dim_1") == dim)).to(torch.int8)
     out["s_edge_cands"] = np_(edc)
     if not bool(edc.any()):
         return
     c2e = torch.nonzero(edc).flatten().to(torch.int32)
-    q, cf = m.swap3d_qualities(o.max_length_allowed, c2e)
+    if dim == 3:
+        q, cf = m.swap3d_qualities(o.max_length_allowed, c2e)
+        out["s_cand_configs"] = np_(cf)
+    else:
+        q = m.swap2d_qualities(o.max_length_allowed, c2e)
     out["s_cands2edges"] = np_(c2e)
     out["s_cand_quals"] = np_(q)
-    out["s_cand_configs"] = np_(cf)
 
 
 def run(dim, n, kind, seed, mqa, stages=True, device=0):
@@ -149,7 +161,7 @@ def run(dim, n, kind, seed, mqa, stages=True, device=0):
     o = adapt_opts(dim, min_quality_allowed=mqa)
     if stages:
         dump_mesh(m, "in_", out)
-        for name in ADJ_ARRAYS3:
+        for name in adj_arrays(dim):
             out["in_" + name] = np_(m.get(name))
         out["in_length_fresh"] = np_(m.measure_edges_metric())
         out["in_quality_fresh"] = np_(m.measure_qualities())
@@ -164,7 +176,7 @@ def run(dim, n, kind, seed, mqa, stages=True, device=0):
         dump_mesh(m, "c_out_", out, with_length=True)
     minq = float(m.get("quality").min())
     did_s = False
-    if minq < o.min_quality_desired and dim == 3:
+    if minq < o.min_quality_desired:
         if stages:
             swap_stage(m, o, out)
         did_s = m.swap_edges(o)

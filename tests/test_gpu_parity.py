@@ -5,8 +5,10 @@ of every integer array and sampled reals) and against the oracle on seeds
 without fixtures.  Integers bit-exact; reals within 1e-12 relative."""
 import pytest
 
-from conftest import (BIG_CASE, SMALL_CASES, compare_arrays, compare_digest, load_digest,
-                      load_golden, run_oracle)
+from conftest import (BIG_CASE, SMALL_CASES, SMALL_CASES_2D, compare_arrays, compare_digest,
+                      load_digest, load_golden, run_oracle)
+
+ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D}
 
 pytestmark = pytest.mark.gpu
 
@@ -21,11 +23,11 @@ def built():
     build.build()
 
 
-@pytest.mark.parametrize("case", list(SMALL_CASES))
+@pytest.mark.parametrize("case", list(ALL_SMALL))
 def test_gpu_matches_reference_per_stage(case):
     import gpu_dump
     golden = load_golden(case)
-    got = gpu_dump.run(*SMALL_CASES[case])
+    got = gpu_dump.run(*ALL_SMALL[case])
     keys = [k for k in golden if k in got or not k.startswith(NOT_DUMPED)]
     fails, maxerr, ndiff = compare_arrays(golden, got, keys=keys, rtol=1e-12)
     print(f"{case}: max real rel err {maxerr:.3e}, {ndiff} reals not bitwise equal")
@@ -43,7 +45,8 @@ def test_gpu_full_size_pass_matches_reference_digest():
     assert list(got["pass_flags"]) == [0, 1, 1]
 
 
-@pytest.mark.parametrize("spec", [(3, 10, 3, 5, 0.2), (3, 9, 1, 99, 0.25), (3, 14, 2, 11, 0.2)])
+@pytest.mark.parametrize("spec", [(3, 10, 3, 5, 0.2), (3, 9, 1, 99, 0.25), (3, 14, 2, 11, 0.2),
+                                  (2, 40, 1, 9, 0.3), (2, 28, 2, 4, 0.3), (2, 36, 3, 2, 0.3)])
 def test_gpu_matches_oracle_other_seeds(oracle_driver, spec):
     import gpu_dump
     want = run_oracle(oracle_driver, spec)

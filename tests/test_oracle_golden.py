@@ -3,14 +3,16 @@ fixtures generated by tests/golden/make_golden.py from the reference built
 from source).  CPU only."""
 import pytest
 
-from conftest import (BIG_CASE, SMALL_CASES, compare_arrays, compare_digest, load_digest,
-                      load_golden, run_oracle)
+from conftest import (BIG_CASE, SMALL_CASES, SMALL_CASES_2D, compare_arrays, compare_digest,
+                      load_digest, load_golden, run_oracle)
+
+ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D}
 
 
-@pytest.mark.parametrize("case", sorted(SMALL_CASES))
+@pytest.mark.parametrize("case", sorted(ALL_SMALL))
 def test_oracle_matches_reference_per_stage(oracle_driver, case):
     golden = load_golden(case)
-    got = run_oracle(oracle_driver, SMALL_CASES[case])
+    got = run_oracle(oracle_driver, ALL_SMALL[case])
     fails, maxerr, ndiff = compare_arrays(golden, got)
     assert not fails, fails[:10]
     # the restatement keeps the reference's operation order: reals are
