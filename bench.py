@@ -30,6 +30,20 @@ sys.path.insert(0, ROOT)
 WORKLOAD = {"workload": "box64_shock_pass", "dim": 3, "n": 64, "metric": "shock", "metric_kind": 1,
             "seed": 2024, "min_quality_allowed": 0.2, "elements": 1572864, "verts": 274625}
 METRIC = "elements/s per adapt pass"
+# Batched workload: 1024 independent 3D boxes, subdivisions per axis
+# log-uniform integers in [4, 40] (seeded), isotropic sine metric with seeded
+# h0, amplitude and wave vector per mesh
+BATCH = {"workload": "batch1024_sine", "meshes": 1024, "n_min": 4, "n_max": 40, "seed": 7,
+         "metric_kind": 3, "plain_sample": 64}
+
+
+def batch_specs(b=BATCH):
+    import numpy as np
+    rng = np.random.default_rng(b["seed"])
+    u = rng.uniform(np.log(b["n_min"]), np.log(b["n_max"] + 1), b["meshes"])
+    ns = np.clip(np.floor(np.exp(u)).astype(int), b["n_min"], b["n_max"])
+    seeds = rng.integers(1, 2 ** 31, b["meshes"])
+    return [(int(n), int(s)) for n, s in zip(ns, seeds)]
 
 
 def _args():
@@ -39,6 +53,7 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload leg")
     ap.add_argument("--profile-pass", action="store_true",
                     help="build the workload, run one warm-up and one timed pass, exit "
                          "(for kernel launch lists under a profiler)")
@@ -157,6 +172,70 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(ctx, lib_stream, flush, args):
+    """The batched workload as one union pass (timed over the pass only,
+    inputs resident) against plain per-mesh passes on a sample of the same
+    meshes; elements are those of the input meshes."""
+    import torch
+    from omega_h_gb300.mesh import Mesh, adapt_opts, adapt_pass_batch
+    specs = batch_specs()
+    opts = adapt_opts(3)
+    base = []
+    for n, seed in specs:
+        m = Mesh.build_box(ctx, 3, n)
+        m.apply_workload(n, seed, BATCH["metric_kind"])
+        base.append(m)
+    nel = sum(m.nelems() for m in base)
+
+    def clones(ms):
+        out = []
+        for m in ms:
+            h = ctypes.c_void_p()
+            _lib_call("ohg_mesh_clone", m.handle, ctypes.byref(h))
+            out.append(Mesh(ctx, h))
+        return out
+
+    def timed(fn):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        fn()
+        e1.record(lib_stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    ms_batch = []
+    for step in range(max(1, args.warmup) + 2):
+        work = clones(base)
+        t = timed(lambda: adapt_pass_batch(ctx, work, opts))
+        if step >= max(1, args.warmup):
+            ms_batch.append(t)
+        for m in work:
+            m.close()
+    stride = max(1, len(base) // BATCH["plain_sample"])
+    sample = base[::stride]
+    nel_sample = sum(m.nelems() for m in sample)
+    work = clones(sample)
+    adapt_pass_batch(ctx, clones(sample[:2]), opts)  # warm
+    ms_plain = timed(lambda: [m.adapt_pass(opts) for m in work])
+    for m in work + base:
+        m.close()
+    batched = nel / (statistics.median(ms_batch) / 1e3)
+    plain = nel_sample / (ms_plain / 1e3)
+    return {"workload": BATCH["workload"], "meshes": len(base), "elements": nel,
+            "metric_kind": "iso_sine", "batched_ms_per_pass": statistics.median(ms_batch),
+            "batched_elements_per_s": batched,
+            "plain_elements_per_s": plain,
+            "plain_sample": {"meshes": len(sample), "elements": nel_sample, "ms": ms_plain},
+            "batched_over_plain": batched / plain}
+
+
+def _lib_call(name, *a):
+    from omega_h_gb300 import _lib
+    return _lib.call(name, *a)
+
+
 def run_ours(args):
     import torch
     rank, world, local = _dist()
@@ -240,6 +319,8 @@ def run_ours(args):
         mm.close()
         ctx.set_screening(True)
         return e0.elapsed_time(e1), counts, h.hexdigest()
+
+    batched = run_batch(ctx, lib_stream, flush, args) if rank == 0 and not args.no_batch else None
 
     fp64_ms, _, fp64_digest = pass_digest(False)
     scr_ms, counts, scr_digest = pass_digest(True)
@@ -335,6 +416,7 @@ def run_ours(args):
                              "traffic": None, "algorithmic_bytes": kernels[dom]["alg_bytes"],
                              "stages": kernels},
                 "precision": precision,
+                "batched": batched,
                 "cpu_baseline": cpu, "gpu_launches": gpu_launches, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -122,6 +122,21 @@ int ohg_adapt_opts_default(int dim, ohg_adapt_opts* out);
 /* refine_by_size -> coarsen_by_size -> swap_edges when the minimum element
  * quality is below min_quality_desired (src/Omega_h_adapt.cpp:173-210) */
 int ohg_adapt_pass(ohg_mesh* mesh, const ohg_adapt_opts* opts, ohg_pass_stats* stats);
+/* ---- batches of meshes (no counterpart in the reference) ----
+ * The disjoint union of n meshes of one dimension is one mesh; one adapt
+ * pass over it gives, mesh by mesh, bit for bit the result of n separate
+ * passes (every decision is local to a mesh and numbering order within a
+ * mesh is kept), in the launches of a single pass.  Class ids must lie in
+ * [0, 2^20) and n <= 2047. */
+int ohg_mesh_concat(ohg_context* ctx, ohg_mesh* const* meshes, int n, ohg_mesh** union_out);
+/* the n parts of a union after any number of passes, as new mesh handles
+ * sharing the union's device memory; the union handle is consumed in the
+ * sense that its arrays are rewritten (destroy it after splitting) */
+int ohg_mesh_split(ohg_mesh* union_mesh, int n, ohg_mesh** parts_out);
+/* concat, one adapt pass, split: each meshes[i] is replaced by its result;
+ * stats are those of the union pass */
+int ohg_adapt_pass_batch(ohg_context* ctx, ohg_mesh* const* meshes, int n,
+                         const ohg_adapt_opts* opts, ohg_pass_stats* stats);
 /* one operator each; *did = whether the mesh changed
  * (src/Omega_h_refine.hpp:8, src/Omega_h_coarsen.hpp:44, src/Omega_h_swap.hpp:14) */
 int ohg_refine_by_size(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);

@@ -60,6 +60,9 @@ SIGNATURES = {
     "ohg_mesh_set_array": [c_void_p, c_char_p, c_void_p, c_ll],
     "ohg_adapt_opts_default": [c_int, P(AdaptOpts)],
     "ohg_adapt_pass": [c_void_p, P(AdaptOpts), P(PassStats)],
+    "ohg_mesh_concat": [c_void_p, P(c_void_p), c_int, P(c_void_p)],
+    "ohg_mesh_split": [c_void_p, c_int, P(c_void_p)],
+    "ohg_adapt_pass_batch": [c_void_p, P(c_void_p), c_int, P(AdaptOpts), P(PassStats)],
     "ohg_refine_by_size": [c_void_p, P(AdaptOpts), P(c_int)],
     "ohg_coarsen_by_size": [c_void_p, P(AdaptOpts), P(c_int)],
     "ohg_swap_edges": [c_void_p, P(AdaptOpts), P(c_int)],

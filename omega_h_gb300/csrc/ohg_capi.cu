@@ -5,6 +5,7 @@
 
 #include "../../include/ohg.h"
 #include "ohg_adapt.cuh"
+#include "ohg_batch.cuh"
 
 using namespace ohg;
 
@@ -441,25 +442,74 @@ int ohg_adapt_opts_default(int dim, ohg_adapt_opts* out) {
   return OHG_OK;
 }
 
+static void to_stats(const PassStats& s, ohg_pass_stats* out) {
+  if (!out) return;
+  out->did_refine = s.did_refine;
+  out->did_coarsen = s.did_coarsen;
+  out->did_swap = s.did_swap;
+  out->nelems_in = s.nelems_in;
+  out->nelems_out = s.nelems_out;
+  out->refine_keys = s.refine_keys;
+  out->coarsen_keys = s.coarsen_keys;
+  out->swap_keys = s.swap_keys;
+  out->indset_rounds = s.indset_rounds;
+  out->min_quality = s.min_quality;
+  out->ms_refine = s.ms_refine;
+  out->ms_coarsen = s.ms_coarsen;
+  out->ms_swap = s.ms_swap;
+}
 int ohg_adapt_pass(ohg_mesh* m, const ohg_adapt_opts* o, ohg_pass_stats* out) {
   MESH_GUARD(m);
-  return guarded(m->owner, [&] {
-    PassStats s = adapt_pass(m->mesh, to_opts(m->mesh.dim, o));
-    if (out) {
-      out->did_refine = s.did_refine;
-      out->did_coarsen = s.did_coarsen;
-      out->did_swap = s.did_swap;
-      out->nelems_in = s.nelems_in;
-      out->nelems_out = s.nelems_out;
-      out->refine_keys = s.refine_keys;
-      out->coarsen_keys = s.coarsen_keys;
-      out->swap_keys = s.swap_keys;
-      out->indset_rounds = s.indset_rounds;
-      out->min_quality = s.min_quality;
-      out->ms_refine = s.ms_refine;
-      out->ms_coarsen = s.ms_coarsen;
-      out->ms_swap = s.ms_swap;
+  return guarded(m->owner, [&] { to_stats(adapt_pass(m->mesh, to_opts(m->mesh.dim, o)), out); });
+}
+static int batch_args(ohg_context* c, ohg_mesh* const* ms, int n) {
+  if (!c || !ms || n <= 0) {
+    g_err = "batch: null context or no meshes";
+    return OHG_ERR_INVALID;
+  }
+  for (int i = 0; i < n; ++i)
+    if (!ms[i] || ms[i]->owner != c) {
+      g_err = "batch: a null mesh or a mesh of another context";
+      return OHG_ERR_INVALID;
     }
+  return OHG_OK;
+}
+int ohg_mesh_concat(ohg_context* c, ohg_mesh* const* ms, int n, ohg_mesh** out) {
+  int rc = batch_args(c, ms, n);
+  if (rc) return rc;
+  ohg_mesh* u = new ohg_mesh{c, Mesh()};
+  rc = guarded(c, [&] {
+    std::vector<Mesh*> v;
+    for (int i = 0; i < n; ++i) v.push_back(&ms[i]->mesh);
+    u->mesh = concat_meshes(v);
+  });
+  if (rc != OHG_OK) {
+    delete u;
+    return rc;
+  }
+  *out = u;
+  return OHG_OK;
+}
+int ohg_mesh_split(ohg_mesh* u, int n, ohg_mesh** outs) {
+  MESH_GUARD(u);
+  if (n <= 0 || !outs) return OHG_ERR_INVALID;
+  std::vector<Mesh> parts;
+  int rc = guarded(u->owner, [&] { parts = split_mesh(u->mesh, n); });
+  if (rc != OHG_OK) return rc;
+  for (int i = 0; i < n; ++i) outs[i] = new ohg_mesh{u->owner, std::move(parts[i])};
+  return OHG_OK;
+}
+int ohg_adapt_pass_batch(ohg_context* c, ohg_mesh* const* ms, int n, const ohg_adapt_opts* o,
+                         ohg_pass_stats* out) {
+  int rc = batch_args(c, ms, n);
+  if (rc) return rc;
+  return guarded(c, [&] {
+    std::vector<Mesh*> v;
+    for (int i = 0; i < n; ++i) v.push_back(&ms[i]->mesh);
+    Mesh u = concat_meshes(v);
+    to_stats(adapt_pass(u, to_opts(u.dim, o)), out);
+    std::vector<Mesh> parts = split_mesh(u, n);
+    for (int i = 0; i < n; ++i) ms[i]->mesh = std::move(parts[i]);
   });
 }
 int ohg_refine_by_size(ohg_mesh* m, const ohg_adapt_opts* o, int* did) {

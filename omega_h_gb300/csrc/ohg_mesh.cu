@@ -15,10 +15,11 @@ namespace ohg {
 // Sorted entries hl = high * k + which_down become the high entity and the
 // alignment code.  Rows longer than G * E are sorted by the group's first lane
 // in memory (only reached for rows beyond 128 entries).
-template <int E>
-__device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, LO j) {
-  LO hl = key >> 3;
-  int c = key & 7;
+// key = hl * 8 + down code (packed) or hl with the code read from dc
+__device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, LO j,
+                                           const I8* dc, bool packed) {
+  LO hl = packed ? key >> 3 : key;
+  int c = packed ? (key & 7) : (dc ? int(dc[hl] & 7) : 0);
   codes[j] = make_code(c & 1, (c >> 1) & 3, hl % k);
   lh2hl[j] = hl / k;
 }
@@ -26,7 +27,7 @@ __device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, 
 // rows with lo_len < n <= hi_len are sorted here; the others are left alone
 template <int E>
 __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off, LO* lh2hl,
-                           I8* codes, int k) {
+                           I8* codes, int k, const I8* dc, bool packed) {
   const int G = 1 << lg;
   unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   LO l = LO(t >> lg);
@@ -84,14 +85,14 @@ __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off
         }
         lh2hl[i + 1] = x;
       }
-      for (LO j = b; j < b + n; ++j) unpack_use<E>(lh2hl[j], k, lh2hl, codes, j);
+      for (LO j = b; j < b + n; ++j) unpack_use(lh2hl[j], k, lh2hl, codes, j, dc, packed);
     }
     return;
   }
 #pragma unroll
   for (int r = 0; r < E; ++r) {
     int i = r * G + lane;
-    if (i < n) unpack_use<E>(v[r], k, lh2hl, codes, b + i);
+    if (i < n) unpack_use(v[r], k, lh2hl, codes, b + i, dc, packed);
   }
 }
 
@@ -100,7 +101,7 @@ __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off
 // exist, a second launch sorts them by whole warps with up to 4 entries per
 // lane (rows beyond 128 by one lane in memory).
 static void sort_rows_by_high(LO nlows, LO maxdeg, const Arr<LO>& off, Arr<LO>& lh2hl,
-                              Arr<I8>& codes, int k) {
+                              Arr<I8>& codes, int k, const I8* dc, bool packed) {
   if (nlows <= 0) return;
   Ctx& c = ctx();
   auto launch = [&](int lg, int E, LO lo_len, LO hi_len) {
@@ -109,13 +110,13 @@ static void sort_rows_by_high(LO nlows, LO maxdeg, const Arr<LO>& off, Arr<LO>& 
     unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
     if (E == 1)
       k_row_sort<1><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k);
+                                                      lh2hl.data(), codes.data(), k, dc, packed);
     else if (E == 2)
       k_row_sort<2><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k);
+                                                      lh2hl.data(), codes.data(), k, dc, packed);
     else
       k_row_sort<4><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k);
+                                                      lh2hl.data(), codes.data(), k, dc, packed);
     ++c.launches;
 #ifdef OHG_CHECKED
     checked_after_launch(__FILE__, __LINE__);
@@ -147,7 +148,8 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   // slots by atomics; each slot holds the use index hl and the use's down
   // code (flip, rotation) packed as hl * 8 + code, read here where the
   // reads of the down arrays are coalesced
-  if (nhl >= (1 << 28)) throw Error(8, "invert_adj: more than 2^28 uses");
+  // (beyond 2^28 uses the key is hl alone and the code is read afterwards)
+  bool packed = nhl < (1 << 28);
   Arr<LO> pos = fill<LO>(nlows, 0);
   auto off = cview(up.a2ab);
   auto ps = view(pos);
@@ -157,11 +159,12 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   pfor(nhl, [=] __device__(LO hl) {
     LO l = hl2l[hl];
     LO c = has_dc ? LO(dc[hl] & 7) : 0;
-    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = hl * 8 + c;
+    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = packed ? hl * 8 + c : hl;
   });
   // rows sorted by high entity (sort_by_high_index)
   LO maxdeg = nlows ? max_lo(deg) : 0;
-  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, k);
+  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, k,
+                    packed ? nullptr : (has_dc ? down.codes.data() : nullptr), packed);
   return up;
 }
 
@@ -842,9 +845,7 @@ void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
     if (cd[v] != dim) continue;
     for (int j = 0; j < dim; ++j) c[size_t(v) * dim + j] += workload::jitter(seed, v, j, dim, n);
   }
-  workload::MetricParams mp;
-  mp.kind = kind;
-  if (kind == workload::METRIC_SHOCK) workload::shock_normal(seed, mp.normal);
+  workload::MetricParams mp = workload::make_params(kind, seed);
   std::vector<double> met(size_t(nv) * mc);
   for (LO v = 0; v < nv; ++v) workload::metric_at(mp, dim, &c[size_t(v) * dim], &met[size_t(v) * mc]);
   m.coords = to_device(c);

@@ -77,6 +77,21 @@ inline void shock_normal(std::uint64_t seed, double out[3]) {
   for (int i = 0; i < 3; ++i) out[i] *= inv;
 }
 
+// Parameters of a metric family from a seed: the shock normal, and for the
+// isotropic sine field h0 uniform in [0.02, 0.2], a uniform in [0, 0.5] and
+// k with integer components uniform in 1..4.
+inline MetricParams make_params(int kind, std::uint64_t seed) {
+  MetricParams p;
+  p.kind = kind;
+  if (kind == METRIC_SHOCK) shock_normal(seed, p.normal);
+  if (kind == METRIC_ISO_SINE) {
+    p.h0 = 0.02 + 0.18 * uniform01(seed, 3, 0);
+    p.amp = 0.5 * uniform01(seed, 3, 1);
+    for (int i = 0; i < 3; ++i) p.k[i] = 1.0 + std::floor(4.0 * uniform01(seed, 3, 2 + i));
+  }
+  return p;
+}
+
 // Writes the packed metric of one vertex at point x (dim components).
 inline void metric_at(const MetricParams& p, int dim, const double* x,
                       double* m) {

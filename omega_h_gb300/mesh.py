@@ -241,3 +241,32 @@ class Mesh:
             self.close()
         except Exception:
             pass
+
+
+def _handles(meshes):
+    return (ctypes.c_void_p * len(meshes))(*[m.handle.value for m in meshes])
+
+
+def concat(ctx, meshes):
+    """The disjoint union of meshes of one dimension (ohg_mesh_concat)."""
+    h = ctypes.c_void_p()
+    _lib.call("ohg_mesh_concat", ctx.handle, _handles(meshes), len(meshes), ctypes.byref(h))
+    return Mesh(ctx, h)
+
+
+def split(union, n):
+    """The n parts of a union (ohg_mesh_split); the union's arrays are
+    rewritten, so close it afterwards."""
+    outs = (ctypes.c_void_p * n)()
+    _lib.call("ohg_mesh_split", union.handle, n, outs)
+    return [Mesh(union.ctx, ctypes.c_void_p(outs[i])) for i in range(n)]
+
+
+def adapt_pass_batch(ctx, meshes, opts=None):
+    """One adapt pass over the union of meshes (ohg_adapt_pass_batch); each
+    mesh is replaced by its result.  Returns the union's pass stats."""
+    o = opts or adapt_opts(meshes[0].dim)
+    s = _lib.PassStats()
+    _lib.call("ohg_adapt_pass_batch", ctx.handle, _handles(meshes), len(meshes), ctypes.byref(o),
+              ctypes.byref(s))
+    return s.as_dict()

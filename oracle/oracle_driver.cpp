@@ -258,9 +258,7 @@ int main(int argc, char** argv) {
       for (int j = 0; j < dim; ++j)
         m.coords[(size_t)(v) * dim + j] += ohg::workload::jitter(seed, v, j, dim, n);
     }
-    ohg::workload::MetricParams mp;
-    mp.kind = kind;
-    if (kind == ohg::workload::METRIC_SHOCK) ohg::workload::shock_normal(seed, mp.normal);
+    ohg::workload::MetricParams mp = ohg::workload::make_params(kind, seed);
     int mc = m.mcomp();
     m.metric.resize((size_t)(m.nverts()) * mc);
     for (LO v = 0; v < m.nverts(); ++v)

@@ -326,10 +326,7 @@ int main(int argc, char** argv) {
       hc[v * dim + j] += ohg::workload::jitter(seed, v, j, dim, n);
   }
   mesh.set_coords(Reals(hc.write()));
-  ohg::workload::MetricParams mp;
-  mp.kind = metric_kind;
-  if (metric_kind == ohg::workload::METRIC_SHOCK)
-    ohg::workload::shock_normal(seed, mp.normal);
+  ohg::workload::MetricParams mp = ohg::workload::make_params(metric_kind, seed);
   int ncomp = dim == 3 ? 6 : 3;
   HostWrite<Real> hm(mesh.nverts() * ncomp);
   HostRead<Real> hc2(mesh.coords());

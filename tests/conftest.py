@@ -17,12 +17,14 @@ SMALL_CASES = {
     "box8_iso": (3, 8, 0, 12345, 0.3),
     "box12_shock": (3, 12, 1, 7, 0.2),
     "box12_blayer": (3, 12, 2, 3, 0.2),
+    "box10_sine": (3, 10, 3, 5, 0.2),
 }
 # 2D squares, 2048 triangles each (2D defaults: min_quality_allowed 0.3)
 SMALL_CASES_2D = {
     "sq32_iso": (2, 32, 0, 5, 0.3),
     "sq32_shock": (2, 32, 1, 5, 0.3),
     "sq32_blayer": (2, 32, 2, 5, 0.3),
+    "sq40_sine": (2, 40, 3, 2, 0.3),
 }
 BIG_CASE = ("box64_shock", (3, 64, 1, 2024, 0.2))
 # arrays that are metadata, not per-stage outputs

@@ -45,6 +45,9 @@ CASES = {
     "sq32_iso": (2, 32, 0, 5, 0.3, True),
     "sq32_shock": (2, 32, 1, 5, 0.3, True),
     "sq32_blayer": (2, 32, 2, 5, 0.3, True),
+    # isotropic sine field of the batched workload (seeded h0, a, k)
+    "box10_sine": (3, 10, 3, 5, 0.2, True),
+    "sq40_sine": (2, 40, 3, 2, 0.3, True),
 }
 
 
