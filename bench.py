@@ -37,6 +37,29 @@ BATCH = {"workload": "batch1024_sine", "meshes": 1024, "n_min": 4, "n_max": 40, 
          "metric_kind": 3, "plain_sample": 64}
 
 
+# Serving workload: Poisson arrivals; half 2D squares (n log-uniform in
+# [16, 1024]), half 3D boxes (n log-uniform in [4, 64]); metric family
+# uniform over isotropic sine, shock and boundary layer; 1 to 3 passes per
+# request; 150 GB admission budget.  A bounded sample of the stream is served
+# at each rate so the run stays within minutes.
+SERVE = {"workload": "serve_mix", "requests": 160, "rates_per_s": [50.0, 200.0, 800.0],
+         "budget_gb": 150.0, "seed": 11}
+
+
+def serve_specs(sv=SERVE):
+    import numpy as np
+    rng = np.random.default_rng(sv["seed"])
+    out = []
+    for _ in range(sv["requests"]):
+        dim = 2 if rng.uniform() < 0.5 else 3
+        lo, hi = (16, 1024) if dim == 2 else (4, 64)
+        n = int(np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1)))), lo, hi))
+        kind = int(rng.choice([3, 1, 2]))
+        out.append((dim, n, kind, int(rng.integers(1, 2 ** 31)), int(rng.integers(1, 4))))
+    gaps = rng.exponential(1.0, sv["requests"])
+    return out, gaps
+
+
 def batch_specs(b=BATCH):
     import numpy as np
     rng = np.random.default_rng(b["seed"])
@@ -54,6 +77,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
     ap.add_argument("--profile-pass", action="store_true",
                     help="build the workload, run one warm-up and one timed pass, exit "
                          "(for kernel launch lists under a profiler)")
@@ -231,6 +255,56 @@ def run_batch(ctx, lib_stream, flush, args):
             "batched_over_plain": batched / plain}
 
 
+def run_serve(ctx, args):
+    """The serving workload at each arrival rate: continuous batching against
+    one request at a time, the same requests (resident meshes cloned from the
+    same bases) and the same arrival times."""
+    import numpy as np
+    from omega_h_gb300.mesh import Mesh
+    from omega_h_gb300.serve import Request, serve, serve_one_at_a_time, summary
+    specs, gaps = serve_specs()
+    bases = []
+    for dim, n, kind, seed, _ in specs:
+        m = Mesh.build_box(ctx, dim, n)
+        m.apply_workload(n, seed, kind)
+        bases.append(m)
+    elements = sum(m.nelems() for m in bases)
+
+    def stream(rate):
+        arr = np.cumsum(gaps) / rate
+        arr -= arr[0]
+        reqs = []
+        for i, (b, sp) in enumerate(zip(bases, specs)):
+            h = ctypes.c_void_p()
+            _lib_call("ohg_mesh_clone", b.handle, ctypes.byref(h))
+            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(ctx, h), passes=sp[4]))
+        return reqs
+
+    # warm both paths once on a few requests
+    for fn in (lambda r: serve(ctx, r), lambda r: serve_one_at_a_time(ctx, r)):
+        w = stream(1e9)[:6]
+        fn(w)
+        for r in w:
+            r.mesh.close()
+    rates = []
+    for rate in SERVE["rates_per_s"]:
+        res = {}
+        for name, fn in (("served", lambda r: serve(ctx, r, budget_bytes=SERVE["budget_gb"] * 1e9)),
+                         ("plain", lambda r: serve_one_at_a_time(ctx, r))):
+            reqs = stream(rate)
+            out = fn(reqs)
+            res[name] = summary(out)
+            for r in out:
+                r.mesh.close()
+        res["rate_per_s"] = rate
+        res["served_over_plain"] = res["served"]["elements_per_s"] / max(res["plain"]["elements_per_s"], 1e-9)
+        rates.append(res)
+    for m in bases:
+        m.close()
+    return {"workload": SERVE["workload"], "requests": len(specs), "elements": elements,
+            "budget_gb": SERVE["budget_gb"], "rates": rates}
+
+
 def _lib_call(name, *a):
     from omega_h_gb300 import _lib
     return _lib.call(name, *a)
@@ -321,6 +395,7 @@ def run_ours(args):
         return e0.elapsed_time(e1), counts, h.hexdigest()
 
     batched = run_batch(ctx, lib_stream, flush, args) if rank == 0 and not args.no_batch else None
+    served = run_serve(ctx, args) if rank == 0 and not args.no_serve else None
 
     fp64_ms, _, fp64_digest = pass_digest(False)
     scr_ms, counts, scr_digest = pass_digest(True)
@@ -417,6 +492,7 @@ def run_ours(args):
                              "stages": kernels},
                 "precision": precision,
                 "batched": batched,
+                "served": served,
                 "cpu_baseline": cpu, "gpu_launches": gpu_launches, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:

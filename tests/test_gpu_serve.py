@@ -1,0 +1,67 @@
+"""Serving with continuous batching: every request's result is bit for bit
+its result alone, whatever it was batched with, and the admission budget
+holds requests back without losing any."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from omega_h_gb300 import build
+    build.build()
+    from omega_h_gb300.mesh import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+# (dim, n, metric kind, seed, passes, arrival s)
+STREAM = [(3, 6, 1, 11, 2, 0.0), (2, 30, 3, 12, 1, 0.0), (3, 9, 2, 13, 3, 0.001),
+          (2, 50, 1, 14, 2, 0.002), (3, 5, 3, 15, 1, 0.003), (2, 20, 2, 16, 3, 0.004),
+          (3, 11, 3, 17, 2, 0.02), (2, 64, 3, 18, 1, 0.03)]
+
+
+def _mesh(ctx, dim, n, kind, seed):
+    from omega_h_gb300.mesh import Mesh
+    m = Mesh.build_box(ctx, dim, n)
+    m.apply_workload(n, seed, kind)
+    return m
+
+
+def _arrays(m):
+    names = ["coords", "metric", "ev2v_1", "ev2v_2", "down_1", "down_2", "downcodes_2",
+             "length", "quality"]
+    if m.dim == 3:
+        names += ["ev2v_3", "down_3", "downcodes_3"]
+    names += [f"class_id_{d}" for d in range(m.dim + 1)]
+    return {k: m.get(k).cpu().numpy() for k in names}
+
+
+@pytest.mark.parametrize("budget", [150e9, 3e7], ids=["roomy", "tight"])
+def test_served_results_equal_results_alone(ctx, budget):
+    from omega_h_gb300.serve import Request, serve, summary
+    alone = []
+    for dim, n, kind, seed, passes, _ in STREAM:
+        m = _mesh(ctx, dim, n, kind, seed)
+        for _ in range(passes):
+            m.adapt_pass()
+        alone.append(_arrays(m))
+        m.close()
+    reqs = [Request(rid=i, arrival=a, mesh=_mesh(ctx, d, n, k, s), passes=p)
+            for i, (d, n, k, s, p, a) in enumerate(STREAM)]
+    out = serve(ctx, reqs, budget_bytes=budget)
+    assert all(r.done >= r.admitted >= r.arrival - 1e-9 and r.passes_done == r.passes for r in out)
+    for r in out:
+        got = _arrays(r.mesh)
+        want = alone[r.rid]
+        for k in want:
+            assert np.array_equal(want[k].view(np.uint8), got[k].view(np.uint8)), \
+                f"request {r.rid}: {k} differs from its result alone"
+        r.mesh.close()
+    s = summary(out)
+    assert s["requests"] == len(STREAM) and s["p99_ms"] >= s["p50_ms"] > 0
