@@ -262,10 +262,12 @@ def run_serve(ctx, args):
     import numpy as np
     from omega_h_gb300.mesh import Mesh
     from omega_h_gb300.serve import Request, serve, serve_one_at_a_time, summary
+    from omega_h_gb300.mesh import Context
     specs, gaps = serve_specs()
+    ctxs = {3: ctx, 2: Context(ctx.device)}  # 2D and 3D union passes overlap
     bases = []
     for dim, n, kind, seed, _ in specs:
-        m = Mesh.build_box(ctx, dim, n)
+        m = Mesh.build_box(ctxs[dim], dim, n)
         m.apply_workload(n, seed, kind)
         bases.append(m)
     elements = sum(m.nelems() for m in bases)
@@ -277,11 +279,12 @@ def run_serve(ctx, args):
         for i, (b, sp) in enumerate(zip(bases, specs)):
             h = ctypes.c_void_p()
             _lib_call("ohg_mesh_clone", b.handle, ctypes.byref(h))
-            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(ctx, h), passes=sp[4]))
+            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(ctxs[sp[0]], h),
+                                passes=sp[4]))
         return reqs
 
     # warm both paths once on a few requests
-    for fn in (lambda r: serve(ctx, r), lambda r: serve_one_at_a_time(ctx, r)):
+    for fn in (lambda r: serve(ctxs, r), lambda r: serve_one_at_a_time(ctx, r)):
         w = stream(1e9)[:6]
         fn(w)
         for r in w:
@@ -289,7 +292,7 @@ def run_serve(ctx, args):
     rates = []
     for rate in SERVE["rates_per_s"]:
         res = {}
-        for name, fn in (("served", lambda r: serve(ctx, r, budget_bytes=SERVE["budget_gb"] * 1e9)),
+        for name, fn in (("served", lambda r: serve(ctxs, r, budget_bytes=SERVE["budget_gb"] * 1e9)),
                          ("plain", lambda r: serve_one_at_a_time(ctx, r))):
             reqs = stream(rate)
             out = fn(reqs)
@@ -301,6 +304,7 @@ def run_serve(ctx, args):
         rates.append(res)
     for m in bases:
         m.close()
+    ctxs[2].close()
     return {"workload": SERVE["workload"], "requests": len(specs), "elements": elements,
             "budget_gb": SERVE["budget_gb"], "rates": rates}
 

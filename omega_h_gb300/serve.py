@@ -9,9 +9,14 @@ step, finished requests leave and free their memory.  Because a union pass is
 bit for bit the separate passes, a request's result does not depend on what
 it was batched with.
 
+With one context per dimension (``ctx`` a dict {2: ctx2, 3: ctx3}, each
+request's mesh built on the context of its dimension), the 2D and 3D union
+passes of a step run concurrently on the two contexts' streams.
+
 ``serve_one_at_a_time`` runs the same stream with one request on the device
 at a time and no batching, the baseline the batched loop is measured against.
 """
+import concurrent.futures
 import time
 from dataclasses import dataclass, field
 
@@ -53,6 +58,19 @@ def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter)
     """Continuous batching.  Returns the requests with admitted/done times
     (seconds from the stream start) and per-pass union stats."""
     reqs = _prepare(requests)
+    ctxs = ctx if isinstance(ctx, dict) else {2: ctx, 3: ctx}
+    parallel = ctxs[2] is not ctxs[3]
+    pool = concurrent.futures.ThreadPoolExecutor(2) if parallel else None
+
+    def run_group(dim, group):
+        o = opts[dim] if opts else adapt_opts(dim)
+        n_before = [r.mesh.nelems() for r in group]
+        st = adapt_pass_batch(ctxs[dim], [r.mesh for r in group], o)
+        for r, nb in zip(group, n_before):
+            r.passes_done += 1
+            r.element_passes += nb
+            r.stats.append(st)
+
     t0 = clock()
     pending = list(reqs)
     active = []
@@ -72,17 +90,14 @@ def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter)
         if not active:
             time.sleep(max(0.0, pending[0].arrival - now))
             continue
-        for dim in (2, 3):
-            group = [r for r in active if r.dim == dim]
-            if not group:
-                continue
-            o = opts[dim] if opts else adapt_opts(dim)
-            n_before = [r.mesh.nelems() for r in group]
-            st = adapt_pass_batch(ctx, [r.mesh for r in group], o)
-            for r, nb in zip(group, n_before):
-                r.passes_done += 1
-                r.element_passes += nb
-                r.stats.append(st)
+        groups = [(d, [r for r in active if r.dim == d]) for d in (2, 3)]
+        groups = [(d, g) for d, g in groups if g]
+        if pool and len(groups) == 2:
+            for f in [pool.submit(run_group, d, g) for d, g in groups]:
+                f.result()
+        else:
+            for d, g in groups:
+                run_group(d, g)
         now = clock() - t0
         still = []
         for r in active:
@@ -92,6 +107,8 @@ def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter)
             else:
                 still.append(r)
         active = still
+    if pool:
+        pool.shutdown()
     return reqs
 
 

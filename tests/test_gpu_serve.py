@@ -26,6 +26,14 @@ STREAM = [(3, 6, 1, 11, 2, 0.0), (2, 30, 3, 12, 1, 0.0), (3, 9, 2, 13, 3, 0.001)
           (3, 11, 3, 17, 2, 0.02), (2, 64, 3, 18, 1, 0.03)]
 
 
+@pytest.fixture(scope="module")
+def ctx2(ctx):
+    from omega_h_gb300.mesh import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
 def _mesh(ctx, dim, n, kind, seed):
     from omega_h_gb300.mesh import Mesh
     m = Mesh.build_box(ctx, dim, n)
@@ -42,8 +50,9 @@ def _arrays(m):
     return {k: m.get(k).cpu().numpy() for k in names}
 
 
+@pytest.mark.parametrize("two_contexts", [False, True], ids=["one_ctx", "two_ctx"])
 @pytest.mark.parametrize("budget", [150e9, 3e7], ids=["roomy", "tight"])
-def test_served_results_equal_results_alone(ctx, budget):
+def test_served_results_equal_results_alone(ctx, ctx2, budget, two_contexts):
     from omega_h_gb300.serve import Request, serve, summary
     alone = []
     for dim, n, kind, seed, passes, _ in STREAM:
@@ -52,9 +61,10 @@ def test_served_results_equal_results_alone(ctx, budget):
             m.adapt_pass()
         alone.append(_arrays(m))
         m.close()
-    reqs = [Request(rid=i, arrival=a, mesh=_mesh(ctx, d, n, k, s), passes=p)
+    ctxs = {2: ctx2 if two_contexts else ctx, 3: ctx}
+    reqs = [Request(rid=i, arrival=a, mesh=_mesh(ctxs[d], d, n, k, s), passes=p)
             for i, (d, n, k, s, p, a) in enumerate(STREAM)]
-    out = serve(ctx, reqs, budget_bytes=budget)
+    out = serve(ctxs, reqs, budget_bytes=budget)
     assert all(r.done >= r.admitted >= r.arrival - 1e-9 and r.passes_done == r.passes for r in out)
     for r in out:
         got = _arrays(r.mesh)
