@@ -78,6 +78,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the boundary-layer precision workloads")
     ap.add_argument("--profile-pass", action="store_true",
                     help="build the workload, run one warm-up and one timed pass, exit "
                          "(for kernel launch lists under a profiler)")
@@ -194,6 +196,66 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# Precision workloads: boundary-layer metric (aspect up to 1000:1) on a 2D
+# 1024^2 square (2,097,152 triangles) and a 3D 48^3 box (663,552 tets)
+PRECISION = [{"workload": "sq1024_blayer", "dim": 2, "n": 1024, "metric_kind": 2, "seed": 3},
+             {"workload": "box48_blayer", "dim": 3, "n": 48, "metric_kind": 2, "seed": 3}]
+
+
+def precision_report(ctx, lib_stream, flush, m_base, opts):
+    """One pass in FP64 throughout and one screened, from clones of m_base:
+    pass times, screening counters and whether every output array is
+    bitwise the same."""
+    import torch
+    from omega_h_gb300.mesh import Mesh
+
+    def one(screening):
+        ctx.set_screening(screening)
+        ctx.screen_counts(reset=True)
+        h = ctypes.c_void_p()
+        _lib_call("ohg_mesh_clone", m_base.handle, ctypes.byref(h))
+        mm = Mesh(ctx, h)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        mm.adapt_pass(opts)
+        e1.record(lib_stream)
+        torch.cuda.synchronize()
+        counts = ctx.screen_counts(reset=True)
+        dg = hashlib.sha256()
+        d = mm.dim
+        for k in (f"ev2v_{d}", "coords", "metric", "length", "quality", f"class_id_{d}"):
+            dg.update(mm.get(k).cpu().numpy().tobytes())
+        mm.close()
+        ctx.set_screening(True)
+        return e0.elapsed_time(e1), counts, dg.hexdigest()
+
+    one(True)  # warm
+    fp64_ms, _, fp64_digest = one(False)
+    scr_ms, counts, scr_digest = one(True)
+    return {"fp64_pass_ms": fp64_ms, "screened_pass_ms": scr_ms,
+            "elements_screened": counts[0], "elements_fp64": counts[1],
+            "lengths_screened": counts[2], "lengths_fp64": counts[3],
+            "element_recheck_fraction": counts[1] / max(counts[0], 1),
+            "length_recheck_fraction": counts[3] / max(counts[2], 1),
+            "max_error_vs_fp64": 0.0 if fp64_digest == scr_digest else None,
+            "outputs_bitwise_equal_to_fp64": fp64_digest == scr_digest}
+
+
+def run_precision(ctx, lib_stream, flush):
+    from omega_h_gb300.mesh import Mesh, adapt_opts
+    out = []
+    for w in PRECISION:
+        m = Mesh.build_box(ctx, w["dim"], w["n"])
+        m.apply_workload(w["n"], w["seed"], w["metric_kind"])
+        r = precision_report(ctx, lib_stream, flush, m, adapt_opts(w["dim"]))
+        r.update({"workload": w["workload"], "elements": m.nelems()})
+        m.close()
+        out.append(r)
+    return out
 
 
 def run_batch(ctx, lib_stream, flush, args):
@@ -378,37 +440,15 @@ def run_ours(args):
     gpu_launches = ctx.launches() - launches0
     total_ms = sum(ms)
 
-    # ---- precision mode: FP32 enclosures + FP64 recheck against FP64 throughout
-    def pass_digest(screening):
-        ctx.set_screening(screening)
-        ctx.screen_counts(reset=True)
-        mm = clone(base)
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(lib_stream)
-        mm.adapt_pass(opts)
-        e1.record(lib_stream)
-        torch.cuda.synchronize()
-        counts = ctx.screen_counts(reset=True)
-        h = hashlib.sha256()
-        for k in ("ev2v_3", "coords", "metric", "length", "quality", "class_id_3"):
-            h.update(mm.get(k).cpu().numpy().tobytes())
-        mm.close()
-        ctx.set_screening(True)
-        return e0.elapsed_time(e1), counts, h.hexdigest()
-
+    # ---- batched and served workloads
     batched = run_batch(ctx, lib_stream, flush, args) if rank == 0 and not args.no_batch else None
     served = run_serve(ctx, args) if rank == 0 and not args.no_serve else None
 
-    fp64_ms, _, fp64_digest = pass_digest(False)
-    scr_ms, counts, scr_digest = pass_digest(True)
-    precision = {"fp64_pass_ms": fp64_ms, "screened_pass_ms": scr_ms,
-                 "tets_screened": counts[0], "tets_fp64": counts[1],
-                 "lengths_screened": counts[2], "lengths_fp64": counts[3],
-                 "tet_recheck_fraction": counts[1] / max(counts[0], 1),
-                 "length_recheck_fraction": counts[3] / max(counts[2], 1),
-                 "outputs_bitwise_equal_to_fp64": fp64_digest == scr_digest}
+    # ---- precision mode: FP32 enclosures + FP64 recheck against FP64 throughout
+    precision = precision_report(ctx, lib_stream, flush, base, opts)
+    precision["workload"] = w["workload"]
+    if rank == 0 and not args.no_precision:
+        precision = [precision] + run_precision(ctx, lib_stream, flush)
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)

@@ -148,9 +148,9 @@ int ohg_swap_edges(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
 int ohg_measure_edges_metric(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
 /* measure_qualities (src/Omega_h_quality.cpp:25-44); a2e_dev NULL = all */
 int ohg_measure_qualities(ohg_mesh* mesh, const int* a2e_dev, int n, double* out_dev);
-/* FP32 enclosures [lo, hi] of the FP64 quality (tet_quality,
- * src/Omega_h_quality.hpp:8-52) of n vertex 4-tuples of the mesh, with the
- * FP64 value itself; the screening step of the precision mode, exposed for
+/* FP32 enclosures [lo, hi] of the FP64 quality (src/Omega_h_quality.hpp:8-52)
+ * of n simplices given as vertex (dim+1)-tuples of the mesh, with the FP64
+ * value itself; the screening step of the precision mode, exposed for
  * checking it (no counterpart in the reference) */
 int ohg_screen_tet_qualities(ohg_mesh* mesh, const int* tv2v_dev, int n, float* lo_dev,
                              float* hi_dev, double* exact_dev);

@@ -59,7 +59,8 @@ __device__ __forceinline__ double edge_len_v(int dim, RV c, RV mt, int mc, LO a,
 }
 
 // ------------------------------------------------------------ screening
-VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nv) {
+VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nv,
+                             int dim) {
   VertScreen s;
   s.xh = Arr<float4>(nv);
   s.xl = Arr<float4>(nv);
@@ -75,6 +76,29 @@ VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metri
   auto mb = view(s.mb);
   auto dk = view(s.dkey);
   auto sd = view(s.sdet);
+  if (dim == 2) {
+    pfor(nv, [=] __device__(LO v) {
+      float h[2], l[2];
+      for (int j = 0; j < 2; ++j) {
+        double x = c[v * 2 + j];
+        h[j] = __double2float_rn(x);
+        l[j] = __double2float_rn(x - double(h[j]));
+      }
+      xh[v] = make_float4(h[0], h[1], 0.0f, fmaxf(fabsf(h[0]), fabsf(h[1])));
+      xl[v] = make_float4(l[0], l[1], 0.0f, 0.0f);
+      const double* m = &mt[v * 3];
+      float f[3];
+      for (int j = 0; j < 3; ++j) f[j] = __double2float_rn(m[j]);
+      float s0 = __fmul_ru(fabsf(f[0]) + fabsf(f[1]) + 2.0f * fabsf(f[2]), 1.0f + 0x1p-20f);
+      double det = det2p(m);
+      double sdet = sqrt(det);
+      ma[v] = make_float4(f[0], f[1], f[2], s0);
+      mb[v] = make_float4(0.0f, 0.0f, 0.0f, __double2float_rn(sdet));
+      dk[v] = order_key(det);
+      sd[v] = sdet;
+    });
+    return s;
+  }
   pfor(nv, [=] __device__(LO v) {
     float h[3], l[3];
     for (int j = 0; j < 3; ++j) {
@@ -102,27 +126,28 @@ VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metri
 }
 
 void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
-  if (m.dim != 3) throw Error(8, "screen_tets: 3D meshes only");
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  int dim = m.dim, nvv = dim + 1;
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
-  auto tv = cview(tv2v_p, n * 4);
+  auto tv = cview(tv2v_p, n * nvv);
   auto lo = view(lo_p, n);
   auto hi = view(hi_p, n);
   auto ex = view(ex_p, n);
   pfor(n, [=] __device__(LO i) {
-    LO vv[4] = {tv[i * 4], tv[i * 4 + 1], tv[i * 4 + 2], tv[i * 4 + 3]};
-    FIv b = tet_quality_bounds(sv, vv);
+    LO vv[4] = {0, 0, 0, 0};
+    for (int k = 0; k < nvv; ++k) vv[k] = tv[i * nvv + k];
+    FIv b = elem_quality_bounds(dim, sv, vv);
     lo[i] = b.lo;
     hi[i] = b.hi;
-    ex[i] = tet_quality_exact(sv, c, mt, vv);
+    ex[i] = elem_quality_exact(dim, sv, c, mt, vv);
   });
 }
 
 void screen_edges(Mesh& m, const LO* ev2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
-  if (m.dim != 3) throw Error(8, "screen_edges: 3D meshes only");
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  int dim = m.dim, mc = m.mcomp();
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
@@ -131,10 +156,10 @@ void screen_edges(Mesh& m, const LO* ev2v_p, LO n, float* lo_p, float* hi_p, dou
   auto hi = view(hi_p, n);
   auto ex = view(ex_p, n);
   pfor(n, [=] __device__(LO i) {
-    FIv b = edge_len_bounds(sv, ev[i * 2], ev[i * 2 + 1]);
+    FIv b = edge_len_bounds_d(dim, sv, ev[i * 2], ev[i * 2 + 1]);
     lo[i] = b.lo;
     hi[i] = b.hi;
-    ex[i] = edge_len_v(3, c, mt, 6, ev[i * 2], ev[i * 2 + 1]);
+    ex[i] = edge_len_v(dim, c, mt, mc, ev[i * 2], ev[i * 2 + 1]);
   });
 }
 
@@ -831,7 +856,8 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
 // threshold lies inside it; those lengths are computed in FP64.
 static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
                                                LO n, const I8* ci_p, I8* co_p) {
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  int dim = m.dim, mc = m.mcomp();
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
   const Adj& v2e = m.ask_up(0, 1);
@@ -859,7 +885,7 @@ static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const
         LO nv[2];
         nv[ein] = v_onto;
         nv[eout] = ev[e2 * 2 + eout];
-        FIv L = edge_len_bounds(sv, nv[0], nv[1]);
+        FIv L = edge_len_bounds_d(dim, sv, nv[0], nv[1]);
         ++nscreen;
         bool over;
         if (L.lo >= thr) {
@@ -867,7 +893,7 @@ static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const
         } else if (L.hi < thr) {
           over = false;
         } else {
-          over = edge_len_v(3, c, mt, 6, nv[0], nv[1]) >= max_length;
+          over = edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length;
           ++nexact;
         }
         if (over) {
@@ -885,7 +911,7 @@ static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const
 // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
 void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n,
                                const I8* ci_p, I8* co_p) {
-  if (m.dim == 3 && ctx().screening) {
+  if (ctx().screening) {
     prevent_coarsen_overshoot_screened(m, max_length, c2e_p, n, ci_p, co_p);
     return;
   }
@@ -1089,21 +1115,22 @@ void choose_rails(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, const doubl
 // Exact FP64 minimum quality of the cavity of collapsing v_col onto v_onto,
 // min(1, tet qualities): enclosures first, then FP64 only for the tets whose
 // lower bound does not exceed the smallest upper bound.
-__device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, LV va, LV vb,
-                                     View<const I8> vc, LO v_col, LO v_onto, unsigned* nexact) {
+__device__ double collapse_min_exact(int dim, const ScreenView& sv, RV c, RV mt, LV cv, LV va,
+                                     LV vb, View<const I8> vc, LO v_col, LO v_onto,
+                                     unsigned* nexact) {
   LO x0 = va[v_col], x1 = va[v_col + 1];
   float min_hi = 1.0f;
   for (LO x = x0; x < x1; ++x) {
     LO vv[4];
-    if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
-    min_hi = fminf(min_hi, tet_quality_bounds(sv, vv).hi);
+    if (!collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+    min_hi = fminf(min_hi, elem_quality_bounds(dim, sv, vv).hi);
   }
   double minq = 1.0;
   for (LO x = x0; x < x1; ++x) {
     LO vv[4];
-    if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
-    if (tet_quality_bounds(sv, vv).lo <= min_hi) {
-      minq = min2d(minq, tet_quality_exact(sv, c, mt, vv));
+    if (!collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+    if (elem_quality_bounds(dim, sv, vv).lo <= min_hi) {
+      minq = min2d(minq, elem_quality_exact(dim, sv, c, mt, vv));
       ++*nexact;
     }
   }
@@ -1118,11 +1145,12 @@ __device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, L
 // direction passed on its enclosure (its value is computed later only if
 // choose_rails_lazy needs it).
 static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa, double* q2_p) {
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  int dim = m.dim;
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
-  auto cv = cview(m.ask_verts_of(3));
-  const Adj& v2c = m.ask_up(0, 3);
+  auto cv = cview(m.ask_verts_of(dim));
+  const Adj& v2c = m.ask_up(0, dim);
   auto va = cview(v2c.a2ab);
   auto vb = cview(v2c.ab2b);
   auto vc = cview(v2c.codes);
@@ -1146,8 +1174,8 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
       float lo = 1.0f, hi = 1.0f;
       for (LO x = va[v_col]; x < va[v_col + 1] && hi >= mqa_f; ++x) {
         LO vv[4];
-        if (!collapse_elem(cv, 3, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
-        FIv b = tet_quality_bounds(sv, vv);
+        if (!collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
+        FIv b = elem_quality_bounds(dim, sv, vv);
         lo = fminf(lo, b.lo);
         hi = fminf(hi, b.hi);
         ++nscreen;
@@ -1159,7 +1187,7 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
       } else if (hi < mqa_f) {
         pass = false;
       } else {
-        double q = collapse_min_exact(sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
+        double q = collapse_min_exact(dim, sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
         q2[cand * 2 + col] = q;
         pass = q >= mqa;
       }
@@ -1180,8 +1208,9 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
                                   const Arr<LO>& vonto, double* out_p) {
   LO K = vcol.size();
   if (K == 0) return;
-  auto cv = cview(m.ask_verts_of(3));
-  const Adj& v2t = m.ask_up(0, 3);
+  int dim = m.dim;
+  auto cv = cview(m.ask_verts_of(dim));
+  const Adj& v2t = m.ask_up(0, dim);
   auto ta = cview(v2t.a2ab);
   auto tb = cview(v2t.ab2b);
   auto tc = cview(v2t.codes);
@@ -1201,11 +1230,11 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
       float min_hi = 1.0f;
       for (LO x = ta[v]; x < ta[v + 1]; ++x) {
         LO vv[4];
-        if (!collapse_elem(cv, 3, tb[x], code_which_down(tc[x]), onto, vv)) {
+        if (!collapse_elem(cv, dim, tb[x], code_which_down(tc[x]), onto, vv)) {
           lo[x] = INFINITY;
           continue;
         }
-        FIv b = tet_quality_bounds(sv, vv);
+        FIv b = elem_quality_bounds(dim, sv, vv);
         lo[x] = b.lo;
         min_hi = fminf(min_hi, b.hi);
       }
@@ -1217,7 +1246,7 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
   }
   Arr<LO> offs = offset_scan(cnt);
   LO ntot = last(offs);
-  Arr<LO> tets(ntot * 4);
+  Arr<LO> tets(ntot * 4);  // dim + 1 vertices per entry, stride 4
   {
     auto lo = cview(lo_at);
     auto mh = cview(mhi);
@@ -1228,8 +1257,8 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
       LO j = of[k];
       for (LO x = ta[v]; x < ta[v + 1]; ++x) {
         if (!(lo[x] <= mh[k])) continue;
-        LO vv[4];
-        collapse_elem(cv, 3, tb[x], code_which_down(tc[x]), onto, vv);
+        LO vv[4] = {0, 0, 0, 0};
+        collapse_elem(cv, dim, tb[x], code_which_down(tc[x]), onto, vv);
         for (int q = 0; q < 4; ++q) tt[j * 4 + q] = vv[q];
         ++j;
       }
@@ -1241,7 +1270,7 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
     auto q = view(eq);
     pfor(ntot, [=] __device__(LO j) {
       LO vv[4] = {tt[j * 4], tt[j * 4 + 1], tt[j * 4 + 2], tt[j * 4 + 3]};
-      q[j] = tet_quality_exact(sv, c, mt, vv);
+      q[j] = elem_quality_exact(dim, sv, c, mt, vv);
     });
   }
   unsigned long long* counts = ctx().d_screen_counts;
@@ -1268,7 +1297,8 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
 static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
                               const double* quals2_p, I8* vcand_p, double* vqual_p, GO* vrail_p) {
   LO nv = m.nverts();
-  VertScreen vs = build_vert_screen(m.coords, m.metric, nv);
+  int dim = m.dim;
+  VertScreen vs = build_vert_screen(m.coords, m.metric, nv, dim);
   auto sv = screen_view(vs);
   Arr<LO> e2c = fill<LO>(m.nedges(), -1);
   auto c2e = cview(c2e_p, n);
@@ -1281,8 +1311,8 @@ static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
   auto vb = cview(v2e.ab2b);
   auto vc = cview(v2e.codes);
   auto ev = cview(m.ask_verts_of(1));
-  auto cv = cview(m.ask_verts_of(3));
-  const Adj& v2t = m.ask_up(0, 3);
+  auto cv = cview(m.ask_verts_of(dim));
+  const Adj& v2t = m.ask_up(0, dim);
   auto ta = cview(v2t.a2ab);
   auto tb = cview(v2t.ab2b);
   auto tc = cview(v2t.codes);
@@ -1348,7 +1378,7 @@ static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
         if (!collapses(codes[cand], eev)) continue;
         if (!(len[e] == best_l)) continue;
         double q = quals2[cand * 2 + eev];
-        if (q != q) q = collapse_min_exact(sv, c, mt, cv, ta, tb, tc, v, ev[e * 2 + (1 - eev)], &nexact);
+        if (q != q) q = collapse_min_exact(dim, sv, c, mt, cv, ta, tb, tc, v, ev[e * 2 + (1 - eev)], &nexact);
         if (chosen == -1 || q > best_q) {
           chosen = e;
           best_q = q;
@@ -1426,7 +1456,7 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
-  bool lazy = dim == 3 && ctx().screening;
+  bool lazy = ctx().screening;
   if (lazy) {
     coarsen_filter_lazy(m, c2e.data(), nc, codes.data(), o.min_quality_allowed, q2.data());
   } else {

@@ -333,7 +333,203 @@ __device__ __forceinline__ double tet_quality_exact(const ScreenView& s, View<co
   return cbrt(x * x) / msl;
 }
 
-// builds the per-vertex screening data of a 3D mesh
-VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nverts);
+// ------------------------------------------------------------ 2D
+// Per-vertex data of a 2D mesh: xh = (x_hi, y_hi, 0, max |hi|),
+// xl = (x_lo, y_lo, 0, 0), ma = (xx, yy, yx, S0), mb = (0, 0, 0, sqrt(det M)).
+
+// q = v^T M v for a 2D metric with A = |v|^T |M| |v| and S1 = 1^T |M| |v|
+__device__ __forceinline__ float mprod2(float4 ma, const float v[2], float& A, float& S1) {
+  float xx = ma.x, yy = ma.y, yx = ma.z;
+  float y0 = __fmaf_rn(yx, v[1], __fmul_rn(xx, v[0]));
+  float y1 = __fmaf_rn(yy, v[1], __fmul_rn(yx, v[0]));
+  float q = __fmaf_rn(v[1], y1, __fmul_rn(v[0], y0));
+  float a0 = fabsf(v[0]), a1 = fabsf(v[1]);
+  float w0 = __fmaf_rn(fabsf(yx), a1, __fmul_rn(fabsf(xx), a0));
+  float w1 = __fmaf_rn(fabsf(yy), a1, __fmul_rn(fabsf(yx), a0));
+  S1 = __fadd_rn(w0, w1);
+  A = __fmaf_rn(a1, w1, __fmul_rn(a0, w0));
+  return q;
+}
+// error of a 2D v^T M v: at most 4 roundings per term in either evaluation
+// plus the metric's conversion, and the input perturbation
+__device__ __forceinline__ float mprod2_err(float A, float S1, float S0, float e) {
+  float pert = __fmaf_rn(e, __fmaf_rn(2.0f, S1, __fmul_rn(e, S0)), 0.0f);
+  return __fmaf_rn(5.1f * kU, A, __fmaf_rn(pert, 1.0f + kU, kTiny));
+}
+__device__ __forceinline__ float sdiff2(float4 h1, float4 l1, float4 h0, float4 l0, float v[2]) {
+  v[0] = __fadd_rn(__fsub_rn(h1.x, h0.x), __fsub_rn(l1.x, l0.x));
+  v[1] = __fadd_rn(__fsub_rn(h1.y, h0.y), __fsub_rn(l1.y, l0.y));
+  float n = fmaxf(fabsf(v[0]), fabsf(v[1]));
+  return __fmaf_rn(n, kC2, __fmaf_rn(__fadd_rn(h1.w, h0.w), 0x1p-44f, kTiny));
+}
+
+// the logarithmic-mean enclosure shared by both dimensions (see
+// edge_len_bounds)
+__device__ __forceinline__ FIv log_mean_bounds(const float l_lo[2], const float l_hi[2]) {
+  float m[2];
+  for (int c = 0; c < 2; ++c) {
+    float x = c ? l_hi[0] : l_lo[0], y = c ? l_hi[1] : l_lo[1];
+    float r = __fdiv_rn(x, y);
+    float lm;
+    if (r > 1.01f || r < 0.99f) {
+      lm = __fdiv_rn(__fsub_rn(x, y), logf(r));
+      lm = c ? __fmul_ru(lm, 1.0f + 0x1p-15f) : __fmul_rd(lm, 1.0f - 0x1p-15f);
+    } else {
+      lm = c ? __fmul_ru(__fmul_ru(__fadd_ru(x, y), 0.5f), 1.0f + 0x1p-20f)
+             : __fmul_rd(__fsqrt_rd(__fmul_rd(x, y)), 1.0f - 0x1p-20f);
+    }
+    m[c] = lm;
+  }
+  float mx = fmaxf(l_hi[0], l_hi[1]);
+  float d = __fmaf_ru(mx, 300.0f * 0x1p-50f, 0x1p-50f);
+  FIv r = {__fmul_rd(m[0], 1.0f - d), __fmul_ru(m[1], 1.0f + d)};
+  if (!finite_iv(r) || !(r.lo > 0.0f)) return widen_all();
+  return r;
+}
+
+// Interval of the double 2D metric edge length (edge_length2)
+__device__ __forceinline__ FIv edge_len_bounds2(const ScreenView& s, LO a, LO b) {
+  float v[2];
+  float e = sdiff2(s.xh[b], s.xl[b], s.xh[a], s.xl[a], v);
+  float l_lo[2], l_hi[2];
+  LO vs[2] = {a, b};
+  for (int k = 0; k < 2; ++k) {
+    float4 ma = s.ma[vs[k]];
+    float A, S1;
+    float q = mprod2(ma, v, A, S1);
+    float qe = __fmul_rn(mprod2_err(A, S1, ma.w, e), kInflate);
+    float lo = __fsub_rd(q, qe), hi = __fadd_ru(q, qe);
+    if (!(lo > 0.0f) || !(hi <= FLT_MAX)) return widen_all();
+    l_lo[k] = __fsqrt_rd(lo);
+    l_hi[k] = __fsqrt_ru(hi);
+  }
+  return log_mean_bounds(l_lo, l_hi);
+}
+
+__device__ __forceinline__ int maxdet_vertex3(const ScreenView& s, const LO vv[3]) {
+  int best = 0;
+  long long bk = s.dkey[vv[0]];
+  for (int i = 1; i < 3; ++i) {
+    long long k = s.dkey[vv[i]];
+    if (k > bk) {
+      best = i;
+      bk = k;
+    }
+  }
+  return best;
+}
+
+constexpr float kInvEqTri = 2.3094010767585030f;  // float(1 / 0.4330127018922193)
+constexpr float kInvEqTriUp = 2.3094013f;         // above 1 / 0.4330127018922193
+constexpr float kThird = 1.0f / 3.0f;
+constexpr float kThirdUp = 0.33333337f;
+
+// Interval of the double triangle quality (tri_quality on the maxdet metric):
+// x / msl with x = area * sqrt(det M) / s_eq, msl the mean v^T M v of the
+// three edges; a negative size is returned as the size.
+__device__ __forceinline__ FIv tri_quality_bounds(const ScreenView& s, const LO vv[3]) {
+  int mi = maxdet_vertex3(s, vv);
+  float4 ma = s.ma[vv[mi]];
+  float sd = s.mb[vv[mi]].w;
+  float4 h[3], l[3];
+  for (int i = 0; i < 3; ++i) {
+    h[i] = s.xh[vv[i]];
+    l[i] = s.xl[vv[i]];
+  }
+  float ev[3][2], ee[3];
+  ee[0] = sdiff2(h[1], l[1], h[0], l[0], ev[0]);  // b0
+  ee[1] = sdiff2(h[2], l[2], h[1], l[1], ev[1]);
+  ee[2] = sdiff2(h[2], l[2], h[0], l[0], ev[2]);  // b1 (the third edge is -b1)
+  const float* b0 = ev[0];
+  const float* b1 = ev[2];
+  float e0 = ee[0], e1 = ee[2];
+  // T = b0 x b1 (rs = T / 2 is exact in both evaluations)
+  float T = __fmaf_rn(b0[0], b1[1], -__fmul_rn(b0[1], b1[0]));
+  float P = __fmaf_rn(fabsf(b0[0]), fabsf(b1[1]), __fmul_rn(fabsf(b0[1]), fabsf(b1[0])));
+  float pert = __fmaf_rn(e0, __fadd_rn(fabsf(b1[0]), fabsf(b1[1])),
+                         __fmaf_rn(e1, __fadd_rn(fabsf(b0[0]), fabsf(b0[1])),
+                                   __fmul_rn(2.0f, __fmul_rn(e0, e1))));
+  float eT = __fmaf_rn(3.1f * kU, P, __fadd_rn(pert, kTiny));
+  float rs = __fmul_rn(T, 0.5f);
+  float ers = __fmul_rn(eT, 0.5f);
+  float sv = __fmul_rn(rs, sd);
+  float es = __fmaf_rn(fabsf(sv), kC2, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
+  es = __fmul_rn(es, kInflate);
+  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
+  if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};
+  float s_lo = __fsub_rd(sv, es);
+  float msum = 0.0f, emsum = 0.0f, asum = 0.0f;
+  for (int i = 0; i < 3; ++i) {
+    float A, S1;
+    float q = mprod2(ma, ev[i], A, S1);
+    msum = __fadd_rn(msum, q);
+    asum = __fadd_rn(asum, A);
+    emsum = __fadd_rn(emsum, mprod2_err(A, S1, ma.w, ee[i]));
+  }
+  float msl = __fmul_rn(msum, kThird);
+  float emsl = __fmaf_rn(fabsf(msl), kC2, __fmul_rn(__fmaf_rn(2.1f * kU, asum, emsum), kThirdUp));
+  emsl = __fmul_rn(emsl, kInflate);
+  float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
+  if (!(msl_lo > 1e-30f) || !(msl_hi < 1e30f)) return widen_all();
+  if (s_lo < 0.0f) return {s_lo, INFINITY};
+  float x = __fmul_rn(sv, kInvEqTri);
+  float ex = __fmaf_rn(fabsf(x), kC2, __fmul_rn(es, kInvEqTriUp));
+  ex = __fmul_rn(ex, kInflate);
+  float x_lo = fmaxf(__fsub_rd(x, ex), 0.0f), x_hi = __fadd_ru(x, ex);
+  if (!(x_hi < 1e30f)) return widen_all();
+  FIv q = {__fmul_rd(__fdividef(x_lo, msl_hi), 1.0f - 0x1p-21f),
+           __fmul_ru(__fdividef(x_hi, msl_lo), 1.0f + 0x1p-21f)};
+  if (!finite_iv(q)) return widen_all();
+  return q;
+}
+
+// The double triangle quality with sqrt(det M) and the maxdet choice taken
+// from the per-vertex data: the operations of tri_quality on the maxdet
+// vertex metric.
+__device__ __forceinline__ double tri_quality_exact(const ScreenView& s, View<const double> c,
+                                                    View<const double> mt, const LO vv[3]) {
+  int mi = maxdet_vertex3(s, vv);
+  double p[3][2];
+  for (int i = 0; i < 3; ++i) {
+    p[i][0] = c[vv[i] * 2];
+    p[i][1] = c[vv[i] * 2 + 1];
+  }
+  const double* m = &mt[vv[mi] * 3];
+  double b00 = p[1][0] - p[0][0], b01 = p[1][1] - p[0][1];
+  double b10 = p[2][0] - p[0][0], b11 = p[2][1] - p[0][1];
+  double rs = (b00 * b11 - b01 * b10) / 2.0;
+  double sz = rs * s.sdet[vv[mi]];
+  if (sz < 0) return sz;
+  double ev[3][2] = {{b00, b01}, {p[2][0] - p[1][0], p[2][1] - p[1][1]}, {-b10, -b11}};
+  double msl = 0;
+  for (int i = 0; i < 3; ++i) {
+    double a0 = m[0] * ev[i][0], a1 = m[2] * ev[i][0];
+    a0 = a0 + m[2] * ev[i][1];
+    a1 = a1 + m[1] * ev[i][1];
+    double d = ev[i][0] * a0;
+    d = d + ev[i][1] * a1;
+    msl += d;
+  }
+  msl = msl / 3;
+  double x = sz / kEquilateralTri;
+  return x / msl;
+}
+
+// dimension dispatch
+__device__ __forceinline__ FIv elem_quality_bounds(int dim, const ScreenView& s, const LO* vv) {
+  return dim == 3 ? tet_quality_bounds(s, vv) : tri_quality_bounds(s, vv);
+}
+__device__ __forceinline__ double elem_quality_exact(int dim, const ScreenView& s,
+                                                     View<const double> c, View<const double> mt,
+                                                     const LO* vv) {
+  return dim == 3 ? tet_quality_exact(s, c, mt, vv) : tri_quality_exact(s, c, mt, vv);
+}
+__device__ __forceinline__ FIv edge_len_bounds_d(int dim, const ScreenView& s, LO a, LO b) {
+  return dim == 3 ? edge_len_bounds(s, a, b) : edge_len_bounds2(s, a, b);
+}
+
+// builds the per-vertex screening data of a mesh of dimension dim
+VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nverts,
+                             int dim = 3);
 
 }  // namespace ohg

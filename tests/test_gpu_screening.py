@@ -22,9 +22,9 @@ def ctx():
     c.close()
 
 
-def _mesh(ctx, n, kind, seed):
+def _mesh(ctx, n, kind, seed, dim=3):
     from omega_h_gb300.mesh import Mesh
-    m = Mesh.build_box(ctx, 3, n)
+    m = Mesh.build_box(ctx, dim, n)
     m.apply_workload(n, seed, kind)
     return m
 
@@ -87,37 +87,66 @@ def test_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     m.close()
 
 
+@pytest.mark.parametrize("n,kind,seed", [(32, 0, 1), (48, 1, 7), (40, 2, 3), (64, 3, 5)])
+def test_2d_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
+    import torch
+    m = _mesh(ctx, n, kind, seed, dim=2)
+    tv = m.get("ev2v_2").view(-1, 3)
+    nt = tv.shape[0]
+    mirrored = tv[:, [1, 0, 2]]
+    mixed = tv.clone()
+    g = torch.Generator().manual_seed(seed)
+    col = torch.randint(0, 3, (nt,), generator=g).cuda()
+    rows = torch.arange(nt, device=tv.device)
+    mixed[rows, col] = tv[(rows + 1) % nt, col]
+    tris = torch.cat([tv, mirrored, mixed]).contiguous()
+    lo, hi, ex = _screen(m, "ohg_screen_tet_qualities", tris, 3)
+    assert np.array_equal(ex[:nt], m.get("quality").cpu().numpy())
+    _check_enclosure(lo, hi, ex, "2D triangle qualities")
+    ev = m.get("ev2v_1").view(-1, 2)
+    nv = m.nents(0)
+    far = torch.stack([ev[:, 0], (ev[:, 1] + 17) % nv], 1)
+    edges = torch.cat([ev, far]).contiguous()
+    lo, hi, ex = _screen(m, "ohg_screen_edge_lengths", edges, 2)
+    assert np.array_equal(ex[:ev.shape[0]], m.get("length").cpu().numpy())
+    _check_enclosure(lo, hi, ex, "2D edge lengths")
+    m.close()
+
+
 PASS_ARRAYS = ["coords", "metric", "length", "quality"] + \
     [f"ev2v_{d}" for d in (1, 2, 3)] + [f"down_{d}" for d in (1, 2, 3)] + \
     [f"downcodes_{d}" for d in (2, 3)] + [f"class_dim_{d}" for d in range(4)] + \
     [f"class_id_{d}" for d in range(4)]
 
 
-def _pass_arrays(ctx, n, kind, seed, mqa, screening):
+def _pass_arrays(ctx, n, kind, seed, mqa, screening, dim=3):
     from omega_h_gb300.mesh import adapt_opts
     ctx.set_screening(screening)
     try:
-        m = _mesh(ctx, n, kind, seed)
-        st = m.adapt_pass(adapt_opts(3, min_quality_allowed=mqa))
-        out = {k: m.get(k).cpu().numpy() for k in PASS_ARRAYS}
+        m = _mesh(ctx, n, kind, seed, dim=dim)
+        st = m.adapt_pass(adapt_opts(dim, min_quality_allowed=mqa))
+        names = PASS_ARRAYS if dim == 3 else [k for k in PASS_ARRAYS if not k.endswith("_3")]
+        out = {k: m.get(k).cpu().numpy() for k in names}
         m.close()
     finally:
         ctx.set_screening(True)
     return st, out
 
 
-@pytest.mark.parametrize("n,kind,seed,mqa", [(8, 0, 12345, 0.3), (12, 1, 7, 0.2),
-                                             (12, 2, 3, 0.2), (20, 1, 11, 0.2),
-                                             (16, 0, 5, 0.3), (32, 1, 2024, 0.2)])
-def test_screened_pass_equals_fp64_pass_bit_for_bit(ctx, n, kind, seed, mqa):
+@pytest.mark.parametrize("dim,n,kind,seed,mqa", [(3, 8, 0, 12345, 0.3), (3, 12, 1, 7, 0.2),
+                                                 (3, 12, 2, 3, 0.2), (3, 20, 1, 11, 0.2),
+                                                 (3, 16, 0, 5, 0.3), (3, 32, 1, 2024, 0.2),
+                                                 (3, 10, 3, 5, 0.2), (2, 64, 1, 3, 0.3),
+                                                 (2, 96, 2, 4, 0.3), (2, 80, 3, 5, 0.3)])
+def test_screened_pass_equals_fp64_pass_bit_for_bit(ctx, dim, n, kind, seed, mqa):
     ctx.screen_counts(reset=True)
-    st1, a1 = _pass_arrays(ctx, n, kind, seed, mqa, True)
+    st1, a1 = _pass_arrays(ctx, n, kind, seed, mqa, True, dim)
     counts = ctx.screen_counts(reset=True)
-    st0, a0 = _pass_arrays(ctx, n, kind, seed, mqa, False)
+    st0, a0 = _pass_arrays(ctx, n, kind, seed, mqa, False, dim)
     for k in ("did_refine", "did_coarsen", "did_swap", "nelems_out", "refine_keys",
               "coarsen_keys", "swap_keys", "indset_rounds"):
         assert st1[k] == st0[k], k
-    for k in PASS_ARRAYS:
+    for k in a0:
         assert a1[k].shape == a0[k].shape, k
         assert np.array_equal(a1[k].view(np.uint8), a0[k].view(np.uint8)), f"{k} differs"
     tets, tets_fp64, lens, lens_fp64 = counts
