@@ -17,6 +17,16 @@
 #include <utility>
 #include <vector>
 
+// Independent per-entity loops run on all host threads when built with
+// OpenMP, as the reference's parallel_for does in its OpenMP build; every
+// iteration writes only its own outputs, so results do not depend on the
+// thread count.  Lazily derived adjacencies are asked for before each loop.
+#ifdef _OPENMP
+#define ORC_PARALLEL_FOR _Pragma("omp parallel for schedule(dynamic, 512)")
+#else
+#define ORC_PARALLEL_FOR
+#endif
+
 namespace orc {
 
 typedef std::int32_t LO;

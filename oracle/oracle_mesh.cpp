@@ -358,6 +358,7 @@ Adj reflect_down(const V<LO>& hv2v, const V<LO>& lv2v, const Adj& v2l, int hd,
   Adj out;
   out.ab2b.resize((size_t)(na));
   out.codes.resize((size_t)(na));
+  ORC_PARALLEL_FOR
   for (LO a = 0; a < na; ++a) {
     const LO* av = &uv2v[(size_t)(a) * deg];
     LO fv = av[0];
@@ -404,6 +405,7 @@ Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld) {
   Adj out;
   out.ab2b.resize((size_t)(nh) * nlh);
   if (ld == 1) out.codes.resize((size_t)(nh) * nlh);
+  ORC_PARALLEL_FOR
   for (LO h = 0; h < nh; ++h) {
     for (int hl = 0; hl < nlh; ++hl) {
       UpT ut = up_template(hd, ld, hl, 0);
@@ -936,6 +938,7 @@ V<double> measure_edges_metric(Mesh& m, const V<LO>& a2e) {
   const V<LO>& ev2v = m.ask_verts_of(1);
   int dim = m.dim, mc = m.mcomp();
   V<double> out(a2e.size());
+  ORC_PARALLEL_FOR
   for (size_t a = 0; a < a2e.size(); ++a) {
     LO e = a2e[a];
     LO v0 = ev2v[(size_t)(e) * 2], v1 = ev2v[(size_t)(e) * 2 + 1];
@@ -971,6 +974,7 @@ V<double> measure_qualities(Mesh& m, const V<LO>& a2e) {
   const V<LO>& ev2v = m.ask_verts_of(m.dim);
   int deg = m.dim + 1;
   V<double> out(a2e.size());
+  ORC_PARALLEL_FOR
   for (size_t a = 0; a < a2e.size(); ++a) out[a] = elem_quality(m, &ev2v[(size_t)(a2e[a]) * deg]);
   return out;
 }
@@ -979,6 +983,7 @@ V<double> get_mident_metrics(Mesh& m, const V<LO>& edges) {
   const V<LO>& ev2v = m.ask_verts_of(1);
   int mc = m.mcomp();
   V<double> out(edges.size() * (size_t)(mc));
+  ORC_PARALLEL_FOR
   for (size_t a = 0; a < edges.size(); ++a) {
     LO e = edges[a];
     const double* m0 = &m.metric[(size_t)(ev2v[(size_t)(e) * 2]) * mc];

@@ -90,6 +90,7 @@ V<I8> find_indset(const Adj& g, const V<double>& q, const V<I8>& cands, int* nro
   };
   while (std::find(state.begin(), state.end(), I8(UNKNOWN)) != state.end()) {
     V<I8> ns = state;
+    ORC_PARALLEL_FOR
     for (LO v = 0; v < n; ++v) {
       if (state[v] != UNKNOWN) continue;
       bool rejected = false;
@@ -291,6 +292,7 @@ V<double> refine_qualities(Mesh& m, const V<LO>& c2e) {
   const Adj& e2c = m.ask_up(1, dim);
   V<double> mid = get_mident_metrics(m, c2e);
   V<double> out(c2e.size());
+  ORC_PARALLEL_FOR
   for (size_t cand = 0; cand < c2e.size(); ++cand) {
     LO e = c2e[cand];
     LO ev[2] = {ev2v[(size_t)(e) * 2], ev2v[(size_t)(e) * 2 + 1]};
@@ -584,6 +586,7 @@ V<I8> prevent_coarsen_overshoot(Mesh& m, double max_length, const V<LO>& c2e,
   const Adj& v2e = m.ask_up(0, 1);
   int dim = m.dim, mc = m.mcomp();
   V<I8> out(codes.size());
+  ORC_PARALLEL_FOR
   for (size_t cand = 0; cand < c2e.size(); ++cand) {
     LO e = c2e[cand];
     I8 code = codes[cand];
@@ -620,6 +623,7 @@ V<double> coarsen_qualities(Mesh& m, const V<LO>& c2e, const V<I8>& codes) {
   const V<LO>& cv2v = m.ask_verts_of(dim);
   const Adj& v2c = m.ask_up(0, dim);
   V<double> q(c2e.size() * 2, -1.0);
+  ORC_PARALLEL_FOR
   for (size_t cand = 0; cand < c2e.size(); ++cand) {
     LO e = c2e[cand];
     I8 code = codes[cand];
@@ -659,6 +663,7 @@ void choose_rails(Mesh& m, const V<LO>& c2e, const V<I8>& codes, const V<double>
   vc->assign((size_t)(nv), 0);
   vq->assign((size_t)(nv), 0.0);
   vr->assign((size_t)(nv), 0);
+  ORC_PARALLEL_FOR
   for (LO v = 0; v < nv; ++v) {
     bool is_cand = false;
     GO best_global = -1;
@@ -905,6 +910,10 @@ void swap3d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e, V<double>* 
                       V<I8>* configs) {
   quals->assign(c2e.size(), -1.0);
   configs->assign(c2e.size(), -1);
+  m.ask_up(1, 3);  // caches used inside the parallel loop
+  m.ask_verts_of(1);
+  m.ask_verts_of(3);
+  ORC_PARALLEL_FOR
   for (size_t cand = 0; cand < c2e.size(); ++cand) {
     Loop loop = find_loop(m, c2e[cand]);
     if (loop.size > 7) continue;
@@ -982,6 +991,9 @@ static void swap2d_cavity(Mesh& m, LO edge, LO ov[2]) {
 V<double> swap2d_qualities(Mesh& m, const AdaptOpts& o, const V<LO>& c2e) {
   const V<LO>& ev2v = m.ask_verts_of(1);
   V<double> out(c2e.size());
+  m.ask_up(1, 2);  // caches used inside the parallel loop
+  m.ask_verts_of(2);
+  ORC_PARALLEL_FOR
   for (size_t cand = 0; cand < c2e.size(); ++cand) {
     LO edge = c2e[cand];
     LO ov[2];
