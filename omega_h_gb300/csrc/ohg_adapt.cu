@@ -854,9 +854,10 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
 // prevent_coarsen_overshoot with FP32 screening of the new edge lengths:
 // an enclosure of each FP64 length settles "length >= max_length" unless the
 // threshold lies inside it; those lengths are computed in FP64.
-static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
-                                               LO n, const I8* ci_p, I8* co_p) {
-  int dim = m.dim, mc = m.mcomp();
+template <int D>
+static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, const LO* c2e_p,
+                                                 LO n, const I8* ci_p, I8* co_p) {
+  constexpr int dim = D, mc = D == 3 ? 6 : 3;
   VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
@@ -906,6 +907,13 @@ static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const
     warp_count(&cnt[2], nscreen);
     warp_count(&cnt[3], nexact);
   });
+}
+static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
+                                               LO n, const I8* ci_p, I8* co_p) {
+  if (m.dim == 3)
+    prevent_coarsen_overshoot_screened_d<3>(m, max_length, c2e_p, n, ci_p, co_p);
+  else
+    prevent_coarsen_overshoot_screened_d<2>(m, max_length, c2e_p, n, ci_p, co_p);
 }
 
 // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
@@ -1115,9 +1123,9 @@ void choose_rails(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, const doubl
 // Exact FP64 minimum quality of the cavity of collapsing v_col onto v_onto,
 // min(1, tet qualities): enclosures first, then FP64 only for the tets whose
 // lower bound does not exceed the smallest upper bound.
-__device__ double collapse_min_exact(int dim, const ScreenView& sv, RV c, RV mt, LV cv, LV va,
-                                     LV vb, View<const I8> vc, LO v_col, LO v_onto,
-                                     unsigned* nexact) {
+template <int dim>
+__device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, LV va, LV vb,
+                                     View<const I8> vc, LO v_col, LO v_onto, unsigned* nexact) {
   LO x0 = va[v_col], x1 = va[v_col + 1];
   float min_hi = 1.0f;
   for (LO x = x0; x < x1; ++x) {
@@ -1144,8 +1152,10 @@ __device__ double collapse_min_exact(int dim, const ScreenView& sv, RV c, RV mt,
 // minimum.  q2 holds the FP64 minimum where it was computed and NaN where the
 // direction passed on its enclosure (its value is computed later only if
 // choose_rails_lazy needs it).
-static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa, double* q2_p) {
-  int dim = m.dim;
+template <int D>
+static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,
+                                  double* q2_p) {
+  constexpr int dim = D;
   VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
@@ -1187,7 +1197,7 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
       } else if (hi < mqa_f) {
         pass = false;
       } else {
-        double q = collapse_min_exact(dim, sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
+        double q = collapse_min_exact<dim>(sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
         q2[cand * 2 + col] = q;
         pass = q >= mqa;
       }
@@ -1198,17 +1208,25 @@ static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, dou
     warp_count(&cnt[1], nexact);
   });
 }
+static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,
+                                double* q2_p) {
+  if (m.dim == 3)
+    coarsen_filter_lazy_d<3>(m, c2e_p, n, codes_p, mqa, q2_p);
+  else
+    coarsen_filter_lazy_d<2>(m, c2e_p, n, codes_p, mqa, q2_p);
+}
 
 // FP64 minima min(1, cavity qualities) of K collapse cavities (v_col[k] onto
 // v_onto[k]; every v_col distinct), written to out[k].  Enclosures select the
 // tets that can hold each minimum; those are gathered into one dense list so
 // that the FP64 evaluations run in full warps (GB300's FP64 pipe is narrow,
 // and a divergent warp occupies it as long as a full one).
-static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& vcol,
-                                  const Arr<LO>& vonto, double* out_p) {
+template <int D>
+static void collapse_minima_exact_d(Mesh& m, const ScreenView& sv, const Arr<LO>& vcol,
+                                    const Arr<LO>& vonto, double* out_p) {
   LO K = vcol.size();
   if (K == 0) return;
-  int dim = m.dim;
+  constexpr int dim = D;
   auto cv = cview(m.ask_verts_of(dim));
   const Adj& v2t = m.ask_up(0, dim);
   auto ta = cview(v2t.a2ab);
@@ -1286,6 +1304,13 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
     });
   }
 }
+static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& vcol,
+                                  const Arr<LO>& vonto, double* out_p) {
+  if (m.dim == 3)
+    collapse_minima_exact_d<3>(m, sv, vcol, vonto, out_p);
+  else
+    collapse_minima_exact_d<2>(m, sv, vcol, vonto, out_p);
+}
 
 // choose_rails (src/Omega_h_collapse_rail.cpp:15-67) on lazily known
 // qualities.  The reference keeps, per vertex, the shortest candidate edge
@@ -1294,10 +1319,12 @@ static void collapse_minima_exact(Mesh& m, const ScreenView& sv, const Arr<LO>& 
 // when several share the minimal length, the first of those with the largest
 // quality.  Qualities are computed in FP64 only for the chosen edges (in one
 // compacted pass) and for edges tied on length.
-static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
-                              const double* quals2_p, I8* vcand_p, double* vqual_p, GO* vrail_p) {
+template <int D>
+static void choose_rails_lazy_d(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
+                                const double* quals2_p, I8* vcand_p, double* vqual_p,
+                                GO* vrail_p) {
   LO nv = m.nverts();
-  int dim = m.dim;
+  constexpr int dim = D;
   VertScreen vs = build_vert_screen(m.coords, m.metric, nv, dim);
   auto sv = screen_view(vs);
   Arr<LO> e2c = fill<LO>(m.nedges(), -1);
@@ -1378,7 +1405,7 @@ static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
         if (!collapses(codes[cand], eev)) continue;
         if (!(len[e] == best_l)) continue;
         double q = quals2[cand * 2 + eev];
-        if (q != q) q = collapse_min_exact(dim, sv, c, mt, cv, ta, tb, tc, v, ev[e * 2 + (1 - eev)], &nexact);
+        if (q != q) q = collapse_min_exact<dim>(sv, c, mt, cv, ta, tb, tc, v, ev[e * 2 + (1 - eev)], &nexact);
         if (chosen == -1 || q > best_q) {
           chosen = e;
           best_q = q;
@@ -1409,6 +1436,13 @@ static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
     auto q = cview(kq);
     pfor(K, [=] __device__(LO k) { vqual[nd[k]] = q[k]; });
   }
+}
+static void choose_rails_lazy(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
+                              const double* quals2_p, I8* vcand_p, double* vqual_p, GO* vrail_p) {
+  if (m.dim == 3)
+    choose_rails_lazy_d<3>(m, c2e_p, n, codes_p, quals2_p, vcand_p, vqual_p, vrail_p);
+  else
+    choose_rails_lazy_d<2>(m, c2e_p, n, codes_p, quals2_p, vcand_p, vqual_p, vrail_p);
 }
 
 static void filter_cands(Arr<LO>& c2e, Arr<I8>& codes, Arr<double>* q2) {
