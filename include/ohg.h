@@ -64,6 +64,13 @@ int ohg_context_destroy(ohg_context* ctx);
 int ohg_context_launches(ohg_context* ctx, unsigned long long* out);
 /* the context's cudaStream_t, for callers that order their own work on it */
 int ohg_context_stream(ohg_context* ctx, void** stream_out);
+/* Measurement hooks (no counterpart in the reference): when on, named hot
+ * kernels ("coarsen_filter") record CUDA events around each launch on the
+ * context's stream; ohg_context_kernel_time sums their durations and
+ * algorithmic bytes since the last reset. */
+int ohg_context_time_kernels(ohg_context* ctx, int on);
+int ohg_context_kernel_time(ohg_context* ctx, const char* name, double* total_ms,
+                            double* total_bytes, int* launches, int reset);
 /* Precision mode of the cavity-quality and overshoot stages (no counterpart
  * in the reference, which computes in FP64 throughout).  on = 1 (default):
  * FP32 enclosures of the FP64 lengths and qualities decide wherever they

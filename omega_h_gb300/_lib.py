@@ -90,6 +90,8 @@ SIGNATURES = {
     "ohg_screen_tet_qualities": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_screen_edge_lengths": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_context_set_screening": [c_void_p, c_int],
+    "ohg_context_time_kernels": [c_void_p, c_int],
+    "ohg_context_kernel_time": [c_void_p, c_char_p, P(c_double), P(c_double), P(c_int), c_int],
     "ohg_context_screen_counts": [c_void_p, P(ctypes.c_ulonglong), c_int],
     "ohg_offset_scan_noalloc": [c_void_p, c_void_p, c_int, c_void_p],
     "ohg_offset_scan_noalloc_limit": [P(c_int)],

@@ -1171,6 +1171,13 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   auto q2 = view(q2_p, n * 2);
   unsigned long long* cnt = ctx().d_screen_counts;
   float mqa_f = float_at_or_above(mqa);  // for float x: x >= mqa <=> x >= mqa_f
+  // algorithmic bytes: candidates in and codes and q2 out, the candidate
+  // edges' vertices, vertex-to-element rows, element vertices and the
+  // per-vertex screening data, each read once
+  LO nV = m.nverts(), nT = m.nelems();
+  double bytes = double(n) * (4 + 1 + 8 + 1 + 16) + double(nV + 1) * 4 +
+                 double(v2c.ab2b.size()) * 5 + double(nT) * 4 * (dim + 1) + double(nV) * 80;
+  KernelTimer timer("coarsen_filter", bytes);
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     I8 code = codes[cand];

@@ -109,6 +109,45 @@ int ohg_context_screen_counts(ohg_context* c, unsigned long long* out4, int rese
     x.sync();
   });
 }
+int ohg_context_time_kernels(ohg_context* c, int on) {
+  if (!c) {
+    g_err = "null context";
+    return OHG_ERR_INVALID;
+  }
+  c->ctx.time_kernels = on != 0;
+  return OHG_OK;
+}
+int ohg_context_kernel_time(ohg_context* c, const char* name, double* total_ms,
+                            double* total_bytes, int* launches, int reset) {
+  if (!name || !total_ms || !total_bytes || !launches) {
+    g_err = "null argument";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    Ctx& x = ctx();
+    x.sync();
+    double ms = 0, by = 0;
+    int n = 0;
+    for (auto& k : x.kernel_launches) {
+      if (k.name != name) continue;
+      float t = 0;
+      OHG_CUDA(cudaEventElapsedTime(&t, k.start, k.stop));
+      ms += t;
+      by += k.bytes;
+      ++n;
+    }
+    *total_ms = ms;
+    *total_bytes = by;
+    *launches = n;
+    if (reset) {
+      for (auto& k : x.kernel_launches) {
+        cudaEventDestroy(k.start);
+        cudaEventDestroy(k.stop);
+      }
+      x.kernel_launches.clear();
+    }
+  });
+}
 int ohg_context_stream(ohg_context* c, void** out) {
   if (!c) return OHG_ERR_INVALID;
   *out = reinterpret_cast<void*>(c->ctx.stream);

@@ -56,6 +56,15 @@ struct Ctx {
   // screening counters: cavity tets screened, tets recomputed in FP64,
   // edge lengths screened, edge lengths recomputed in FP64
   unsigned long long* d_screen_counts = nullptr;
+  // opt-in timing of named kernels: CUDA events on the context's stream
+  // around each launch, resolved when read (no synchronisation in between)
+  bool time_kernels = false;
+  struct KernelLaunch {
+    std::string name;
+    cudaEvent_t start, stop;
+    double bytes;
+  };
+  std::vector<KernelLaunch> kernel_launches;
   explicit Ctx(int dev);
   ~Ctx();
   Ctx(const Ctx&) = delete;
@@ -203,6 +212,29 @@ inline void pfor_at(const char* file, int line, LO n, F f) {
 #endif
 }
 #define pfor(n, ...) ::ohg::pfor_at(__FILE__, __LINE__, (n), __VA_ARGS__)
+
+// Records a named kernel's launch duration (when the context times
+// kernels) with its algorithmic bytes; construct before the launch, destroy
+// after it.
+struct KernelTimer {
+  Ctx* c = nullptr;
+  Ctx::KernelLaunch k;
+  KernelTimer(const char* name, double bytes) {
+    Ctx& x = ctx();
+    if (!x.time_kernels) return;
+    c = &x;
+    k.name = name;
+    k.bytes = bytes;
+    OHG_CUDA(cudaEventCreate(&k.start));
+    OHG_CUDA(cudaEventCreate(&k.stop));
+    OHG_CUDA(cudaEventRecord(k.start, x.stream));
+  }
+  ~KernelTimer() {
+    if (!c) return;
+    cudaEventRecord(k.stop, c->stream);
+    c->kernel_launches.push_back(k);
+  }
+};
 
 // device status helper
 __device__ inline void raise_status(int* st, int bits) { atomicOr(st, bits); }

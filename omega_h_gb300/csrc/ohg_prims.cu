@@ -36,6 +36,10 @@ Ctx::Ctx(int dev) : device(dev) {
 }
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
+  for (auto& k : kernel_launches) {
+    cudaEventDestroy(k.start);
+    cudaEventDestroy(k.stop);
+  }
   cudaFree(d_status);
   cudaFree(d_screen_counts);
   if (d_swap_tables) cudaFree(d_swap_tables);

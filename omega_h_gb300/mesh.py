@@ -52,6 +52,16 @@ class Context:
         _lib.call("ohg_context_screen_counts", self.handle, v, 1 if reset else 0)
         return tuple(int(x) for x in v)
 
+    def time_kernels(self, on):
+        _lib.call("ohg_context_time_kernels", self.handle, 1 if on else 0)
+
+    def kernel_time(self, name, reset=False):
+        """(total ms, total algorithmic bytes, launches) of a named kernel."""
+        ms, by, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        _lib.call("ohg_context_kernel_time", self.handle, name.encode(), ctypes.byref(ms),
+                  ctypes.byref(by), ctypes.byref(n), 1 if reset else 0)
+        return ms.value, by.value, n.value
+
     def close(self):
         if self.handle:
             _lib.call("ohg_context_destroy", self.handle)
