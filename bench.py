@@ -447,6 +447,7 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = ctx.launches()
+    syncs0 = ctx.syncs()
     ms, stats = [], None
     ctx.kernel_time(DOMINANT, reset=True)
     ctx.time_kernels(True)  # events around the dominant kernel's launches
@@ -458,6 +459,7 @@ def run_ours(args):
     ctx.time_kernels(False)
     dom_ms, dom_bytes, dom_n = ctx.kernel_time(DOMINANT, reset=True)
     gpu_launches = ctx.launches() - launches0
+    host_syncs = ctx.syncs() - syncs0
     total_ms = sum(ms)
 
     # ---- batched and served workloads
@@ -566,7 +568,8 @@ def run_ours(args):
                 "precision": precision,
                 "batched": batched,
                 "served": served,
-                "cpu_baseline": cpu, "gpu_launches": gpu_launches, "clocks": clk.summary()}
+                "cpu_baseline": cpu, "gpu_launches": gpu_launches,
+                "host_syncs_per_step": host_syncs / args.steps, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

@@ -55,6 +55,13 @@ typedef struct ohg_pass_stats {
   float ms_refine, ms_coarsen, ms_swap;
 } ohg_pass_stats;
 
+/* Outcome of ohg_adapt: whether the mesh needed work, how many times each
+ * operator changed it, and whether min_quality_desired was reached. */
+typedef struct ohg_adapt_result {
+  int did, quality_satisfied;
+  int refines, coarsens, swaps, sliver_coarsens, length_rounds;
+} ohg_adapt_result;
+
 const char* ohg_last_error(void);
 
 /* ---- context: one device, one stream, one stream-ordered memory pool ---- */
@@ -62,6 +69,8 @@ int ohg_context_create(int device, ohg_context** out);
 int ohg_context_destroy(ohg_context* ctx);
 /* number of kernels this library has launched on the context */
 int ohg_context_launches(ohg_context* ctx, unsigned long long* out);
+/* number of times the host has waited on the context's stream */
+int ohg_context_syncs(ohg_context* ctx, unsigned long long* out);
 /* the context's cudaStream_t, for callers that order their own work on it */
 int ohg_context_stream(ohg_context* ctx, void** stream_out);
 /* Measurement hooks (no counterpart in the reference): when on, named hot
@@ -129,6 +138,14 @@ int ohg_adapt_opts_default(int dim, ohg_adapt_opts* out);
 /* refine_by_size -> coarsen_by_size -> swap_edges when the minimum element
  * quality is below min_quality_desired (src/Omega_h_adapt.cpp:173-210) */
 int ohg_adapt_pass(ohg_mesh* mesh, const ohg_adapt_opts* opts, ohg_pass_stats* stats);
+/* Omega_h::adapt (src/Omega_h_adapt.cpp:272-288) for meshes without
+ * conservation tags or geometry: refine/coarsen by size until lengths
+ * settle, then edge swaps and sliver collapses (coarsen_slivers,
+ * src/Omega_h_coarsen.cpp:210-220) until the worst quality reaches
+ * min_quality_desired or nothing helps */
+int ohg_adapt(ohg_mesh* mesh, const ohg_adapt_opts* opts, ohg_adapt_result* result);
+/* coarsen_slivers (src/Omega_h_coarsen.cpp:210-220) */
+int ohg_coarsen_slivers(ohg_mesh* mesh, const ohg_adapt_opts* opts, int* did);
 /* ---- batches of meshes (no counterpart in the reference) ----
  * The disjoint union of n meshes of one dimension is one mesh; one adapt
  * pass over it gives, mesh by mesh, bit for bit the result of n separate

@@ -28,6 +28,15 @@ class AdaptOpts(ctypes.Structure):
                 ("min_quality_desired", c_double), ("nsliver_layers", c_int)]
 
 
+class AdaptResult(ctypes.Structure):
+    _fields_ = [("did", c_int), ("quality_satisfied", c_int), ("refines", c_int),
+                ("coarsens", c_int), ("swaps", c_int), ("sliver_coarsens", c_int),
+                ("length_rounds", c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class PassStats(ctypes.Structure):
     _fields_ = [("did_refine", c_int), ("did_coarsen", c_int), ("did_swap", c_int),
                 ("nelems_in", c_int), ("nelems_out", c_int), ("refine_keys", c_int),
@@ -45,6 +54,7 @@ SIGNATURES = {
     "ohg_context_create": [c_int, P(c_void_p)],
     "ohg_context_destroy": [c_void_p],
     "ohg_context_launches": [c_void_p, P(c_ull)],
+    "ohg_context_syncs": [c_void_p, P(c_ull)],
     "ohg_context_stream": [c_void_p, P(c_void_p)],
     "ohg_build_box": [c_void_p, c_int, c_int, P(c_void_p)],
     "ohg_mesh_from_arrays": [c_void_p, c_int, P(c_int), P(c_void_p), P(c_void_p), P(c_void_p),
@@ -60,6 +70,8 @@ SIGNATURES = {
     "ohg_mesh_set_array": [c_void_p, c_char_p, c_void_p, c_ll],
     "ohg_adapt_opts_default": [c_int, P(AdaptOpts)],
     "ohg_adapt_pass": [c_void_p, P(AdaptOpts), P(PassStats)],
+    "ohg_adapt": [c_void_p, P(AdaptOpts), P(AdaptResult)],
+    "ohg_coarsen_slivers": [c_void_p, P(AdaptOpts), P(c_int)],
     "ohg_mesh_concat": [c_void_p, P(c_void_p), c_int, P(c_void_p)],
     "ohg_mesh_split": [c_void_p, c_int, P(c_void_p)],
     "ohg_adapt_pass_batch": [c_void_p, P(c_void_p), c_int, P(AdaptOpts), P(PassStats)],

@@ -1459,19 +1459,16 @@ static void filter_cands(Arr<LO>& c2e, Arr<I8>& codes, Arr<double>* q2) {
   if (q2) *q2 = unmap(keep, *q2, 2);
 }
 
-bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
+// coarsen_verts + coarsen (src/Omega_h_coarsen.cpp:29-176): collapse the
+// marked vertices along their edges.  allowed: overshoot limit
+// max_length_allowed instead of max_length_desired; improve: keep only
+// directions whose cavity quality beats the worst element now at the
+// collapsing vertex (filter_coarsen_improve,
+// src/Omega_h_coarsen_qualities.cpp:111-122).
+static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool allowed,
+                          bool improve, PassStats* st) {
   int dim = m.dim;
-  const Arr<double>& len = m.ask_lengths();
   LO ne = m.nedges();
-  Arr<I8> ecand(ne);
-  {
-    auto l = cview(len);
-    auto c = view(ecand);
-    double mn = o.min_length_desired;
-    pfor(ne, [=] __device__(LO i) { c[i] = l[i] < mn; });
-  }
-  if (count_marked(ecand) == 0) return false;
-  Arr<I8> vm = mark_down(m, EDGE, VERT, ecand);
   Arr<I8> ecodes(ne);
   {
     auto ev = cview(m.ask_verts_of(1));
@@ -1490,25 +1487,45 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   codes = codes2;
   filter_cands(c2e, codes, nullptr);
   codes2 = Arr<I8>(c2e.size());
-  prevent_coarsen_overshoot(m, o.max_length_desired, c2e.data(), c2e.size(), codes.data(),
-                            codes2.data());
+  prevent_coarsen_overshoot(m, allowed ? o.max_length_allowed : o.max_length_desired, c2e.data(),
+                            c2e.size(), codes.data(), codes2.data());
   codes = codes2;
   filter_cands(c2e, codes, nullptr);
   if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
-  bool lazy = ctx().screening;
+  bool lazy = ctx().screening && !improve;
   if (lazy) {
     coarsen_filter_lazy(m, c2e.data(), nc, codes.data(), o.min_quality_allowed, q2.data());
   } else {
     coarsen_qualities(m, c2e.data(), nc, codes.data(), q2.data());
+    // the worst element quality at each vertex now (graph_reduce MIN)
+    Arr<double> vold;
+    if (improve) {
+      const Adj& v2c = m.ask_up(0, dim);
+      auto va = cview(v2c.a2ab);
+      auto vb = cview(v2c.ab2b);
+      auto eq = cview(m.ask_qualities());
+      vold = Arr<double>(m.nverts());
+      auto vo = view(vold);
+      pfor(m.nverts(), [=] __device__(LO v) {
+        double mq = DBL_MAX;
+        for (LO x = va[v]; x < va[v + 1]; ++x) mq = min2d(mq, eq[vb[x]]);
+        vo[v] = mq;
+      });
+    }
     auto cd = view(codes);
     auto q = cview(q2);
+    auto ce = cview(c2e);
+    auto ev = cview(m.ask_verts_of(1));
+    auto vo = cview(vold);
     double mqa = o.min_quality_allowed;
     pfor(nc, [=] __device__(LO i) {
       I8 code = cd[i];
-      for (int d = 0; d < 2; ++d)
+      for (int d = 0; d < 2; ++d) {
         if (!(q[i * 2 + d] >= mqa)) code = dont_collapse(code, d);
+        if (improve && !(q[i * 2 + d] > vo[ev[ce[i] * 2 + d]])) code = dont_collapse(code, d);
+      }
       cd[i] = code;
     });
   }
@@ -1654,6 +1671,30 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   }
   m = std::move(nm);
   return true;
+}
+
+// coarsen_by_size (src/Omega_h_coarsen.cpp:198-208): vertices of edges
+// shorter than min_length_desired
+bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
+  const Arr<double>& len = m.ask_lengths();
+  LO ne = m.nedges();
+  Arr<I8> ecand(ne);
+  {
+    auto l = cview(len);
+    auto c = view(ecand);
+    double mn = o.min_length_desired;
+    pfor(ne, [=] __device__(LO i) { c[i] = l[i] < mn; });
+  }
+  if (count_marked(ecand) == 0) return false;
+  return coarsen_verts(m, o, mark_down(m, EDGE, VERT, ecand), false, false, st);
+}
+
+// coarsen_slivers (src/Omega_h_coarsen.cpp:210-220): vertices of the sliver
+// layers, overshoot up to max_length_allowed, local improvement required
+bool coarsen_slivers(Mesh& m, const AdaptOpts& o, PassStats* st) {
+  Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
+  if (count_marked(ec) == 0) return false;
+  return coarsen_verts(m, o, mark_down(m, m.dim, VERT, ec), true, true, st);
 }
 
 // ------------------------------------------------------------ swap (3D)
@@ -2386,6 +2427,58 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
   if (count_marked(edc) == 0) return false;
   Arr<LO> c2e = collect_marked(edc);
   return dim == 3 ? swap_edges_3d(m, o, st, c2e) : swap_edges_2d(m, o, st, c2e);
+}
+
+// ------------------------------------------------------------ adapt()
+// Omega_h::adapt (src/Omega_h_adapt.cpp:153-212, 272-288) for meshes without
+// conservation tags or a geometry model: nothing to do when qualities and
+// lengths already meet the goals; satisfy_lengths (refine and coarsen by
+// size until neither changes the mesh); satisfy_quality (edge swaps, else
+// sliver collapses, until the worst quality reaches min_quality_desired or
+// neither helps).
+AdaptResult adapt(Mesh& m, const AdaptOpts& o) {
+  AdaptResult r;
+  PassStats st;
+  auto meets_goals = [&] {
+    const Arr<double>& len = m.ask_lengths();
+    return min_f64(m.ask_qualities()) >= o.min_quality_desired &&
+           min_f64(len) >= o.min_length_desired && max_f64(len) <= o.max_length_desired;
+  };
+  if (meets_goals()) return r;
+  r.did = true;
+  constexpr int kMaxRounds = 1000;  // a guard; the reference's loops are unbounded
+  bool any;
+  do {
+    any = false;
+    if (refine_by_size(m, o, &st)) {
+      ++r.refines;
+      any = true;
+    }
+    if (coarsen_by_size(m, o, &st)) {
+      ++r.coarsens;
+      any = true;
+    }
+    if (++r.length_rounds > kMaxRounds) throw Error(5, "adapt: lengths did not settle");
+  } while (any);
+  if (min_f64(m.ask_qualities()) >= o.min_quality_desired) {
+    r.quality_satisfied = true;
+    return r;
+  }
+  int rounds = 0;
+  do {
+    if (++rounds > kMaxRounds) throw Error(5, "adapt: qualities did not settle");
+    if (swap_edges(m, o, &st)) {
+      ++r.swaps;
+      continue;
+    }
+    if (coarsen_slivers(m, o, &st)) {
+      ++r.sliver_coarsens;
+      continue;
+    }
+    return r;  // could not satisfy quality
+  } while (min_f64(m.ask_qualities()) < o.min_quality_desired);
+  r.quality_satisfied = true;
+  return r;
 }
 
 // ------------------------------------------------------------ the pass

@@ -50,6 +50,16 @@ void swap3d_qualities(Mesh& m, double max_length_allowed, const LO* c2e, LO n, d
 
 bool refine_by_size(Mesh& m, const AdaptOpts& o, PassStats* st);
 bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st);
+bool coarsen_slivers(Mesh& m, const AdaptOpts& o, PassStats* st);
+
+// outcome of a full adapt(): whether the mesh needed work, how many times
+// each operator changed it, and whether the quality goal was reached
+struct AdaptResult {
+  bool did = false;
+  bool quality_satisfied = false;
+  int refines = 0, coarsens = 0, swaps = 0, sliver_coarsens = 0, length_rounds = 0;
+};
+AdaptResult adapt(Mesh& m, const AdaptOpts& o);
 bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st);
 // refine -> coarsen -> swap when min quality < min_quality_desired
 PassStats adapt_pass(Mesh& m, const AdaptOpts& o);

@@ -86,6 +86,11 @@ int ohg_context_launches(ohg_context* c, unsigned long long* out) {
   *out = c->ctx.launches;
   return OHG_OK;
 }
+int ohg_context_syncs(ohg_context* c, unsigned long long* out) {
+  if (!c || !out) return OHG_ERR_INVALID;
+  *out = c->ctx.syncs;
+  return OHG_OK;
+}
 
 int ohg_context_set_screening(ohg_context* c, int on) {
   if (!c) {
@@ -500,6 +505,29 @@ static void to_stats(const PassStats& s, ohg_pass_stats* out) {
 int ohg_adapt_pass(ohg_mesh* m, const ohg_adapt_opts* o, ohg_pass_stats* out) {
   MESH_GUARD(m);
   return guarded(m->owner, [&] { to_stats(adapt_pass(m->mesh, to_opts(m->mesh.dim, o)), out); });
+}
+int ohg_adapt(ohg_mesh* m, const ohg_adapt_opts* o, ohg_adapt_result* out) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] {
+    AdaptResult r = adapt(m->mesh, to_opts(m->mesh.dim, o));
+    if (out) {
+      out->did = r.did;
+      out->quality_satisfied = r.quality_satisfied;
+      out->refines = r.refines;
+      out->coarsens = r.coarsens;
+      out->swaps = r.swaps;
+      out->sliver_coarsens = r.sliver_coarsens;
+      out->length_rounds = r.length_rounds;
+    }
+  });
+}
+int ohg_coarsen_slivers(ohg_mesh* m, const ohg_adapt_opts* o, int* did) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] {
+    PassStats s;
+    bool d = coarsen_slivers(m->mesh, to_opts(m->mesh.dim, o), &s);
+    if (did) *did = d;
+  });
 }
 static int batch_args(ohg_context* c, ohg_mesh* const* ms, int n) {
   if (!c || !ms || n <= 0) {

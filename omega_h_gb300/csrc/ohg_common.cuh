@@ -51,6 +51,7 @@ struct Ctx {
   int* d_swap_tables = nullptr;  // edge-swap triangulation tables (device copy)
   int swap_tables_len = 0;
   std::uint64_t launches = 0;
+  std::uint64_t syncs = 0;  // host waits on the stream (sizes and flags read back)
   // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
   int screening = 1;
   // screening counters: cavity tets screened, tets recomputed in FP64,

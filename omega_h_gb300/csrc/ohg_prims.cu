@@ -46,7 +46,10 @@ Ctx::~Ctx() {
   cudaFreeHost(h_pinned);
   cudaStreamDestroy(stream);
 }
-void Ctx::sync() { OHG_CUDA(cudaStreamSynchronize(stream)); }
+void Ctx::sync() {
+  ++syncs;
+  OHG_CUDA(cudaStreamSynchronize(stream));
+}
 int Ctx::take_status() {
   OHG_CUDA(cudaMemcpyAsync(h_pinned, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
   OHG_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int), stream));

@@ -40,6 +40,11 @@ class Context:
         _lib.call("ohg_context_launches", self.handle, ctypes.byref(v))
         return v.value
 
+    def syncs(self):
+        v = ctypes.c_ulonglong()
+        _lib.call("ohg_context_syncs", self.handle, ctypes.byref(v))
+        return v.value
+
     def set_screening(self, on):
         """FP32 screening with exact FP64 recheck (True, default) or FP64
         throughout (False)."""
@@ -142,6 +147,17 @@ class Mesh:
         s = _lib.PassStats()
         _lib.call("ohg_adapt_pass", self.handle, ctypes.byref(o), ctypes.byref(s))
         return s.as_dict()
+
+    def adapt(self, opts=None):
+        """Omega_h::adapt: passes until lengths settle, then swaps and sliver
+        collapses until the quality goal is met or nothing helps."""
+        o = opts or adapt_opts(self.dim)
+        r = _lib.AdaptResult()
+        _lib.call("ohg_adapt", self.handle, ctypes.byref(o), ctypes.byref(r))
+        return r.as_dict()
+
+    def coarsen_slivers(self, opts=None):
+        return self._op("ohg_coarsen_slivers", opts)
 
     def _op(self, fname, opts):
         o = opts or adapt_opts(self.dim)

@@ -457,6 +457,14 @@ struct PassResult {
 };
 PassResult adapt_pass(Mesh& m, const AdaptOpts& o);
 
+// coarsen_slivers and the full adapt() loop
+bool coarsen_slivers(Mesh& m, const AdaptOpts& o);
+struct AdaptResult {
+  bool did = false, quality_satisfied = false;
+  int refines = 0, coarsens = 0, swaps = 0, sliver_coarsens = 0, length_rounds = 0;
+};
+AdaptResult adapt(Mesh& m, const AdaptOpts& o);
+
 // swap3d tables (same content as src/Omega_h_swap3d_tables.hpp, own layout)
 namespace swap3d {
 int mesh_count(int loop);

@@ -3,7 +3,7 @@
 // oracle/ref_driver.cpp writes for the reference, so tests can compare the two
 // (and the GPU product) array by array.
 //
-//   oracle_driver DIM N METRIC SEED MIN_QUAL_ALLOWED OUTDIR [nostages|time]
+//   oracle_driver DIM N METRIC SEED MIN_QUAL_ALLOWED OUTDIR [nostages|time|adapt]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -240,7 +240,7 @@ static void dump_swap_stage(Mesh& m, const AdaptOpts& o) {
 
 int main(int argc, char** argv) {
   if (argc < 7) {
-    std::fprintf(stderr, "usage: %s DIM N METRIC SEED MQA OUTDIR [nostages|time]\n", argv[0]);
+    std::fprintf(stderr, "usage: %s DIM N METRIC SEED MQA OUTDIR [nostages|time|adapt]\n", argv[0]);
     return 2;
   }
   int dim = std::atoi(argv[1]), n = std::atoi(argv[2]), kind = std::atoi(argv[3]);
@@ -275,6 +275,18 @@ int main(int argc, char** argv) {
       dump("in_length_fresh", measure_edges_metric(m, all_e));
       dump("in_quality_fresh", measure_qualities(m, all_t));
       dump("in_hilbert_perm", hilbert_sort(m.coords, dim));
+    }
+    if (mode == "adapt") {
+      // the full adapt() loop instead of one pass
+      auto ta = std::chrono::steady_clock::now();
+      AdaptResult ar = adapt(m, o);
+      double t_ad = std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
+      dump("adapt_result", V<LO>{ar.did, ar.quality_satisfied, ar.refines, ar.coarsens, ar.swaps,
+                                 ar.sliver_coarsens, ar.length_rounds});
+      dump_mesh(m, "out_");
+      if (g_manifest) std::fclose(g_manifest);
+      std::printf("build %.4f adapt %.4f elems_out %d\n", t_build, t_ad, int(m.nelems()));
+      return 0;
     }
     auto t1 = std::chrono::steady_clock::now();
     if (stages) dump_refine_stage(m, o);

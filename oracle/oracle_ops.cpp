@@ -734,17 +734,13 @@ void mark_dead_ents(Mesh& m, const V<LO>& r2e, const V<I8>& rdir, V<I8>* dead) {
 }
 
 // coarsen_by_size .. coarsen_element_based2 (src/Omega_h_coarsen.cpp:29-208)
-bool coarsen_by_size(Mesh& m, const AdaptOpts& o) {
+// coarsen_verts + coarsen (src/Omega_h_coarsen.cpp:29-176, 178-196):
+// collapse the marked vertices; allowed selects max_length_allowed as the
+// overshoot limit, improve the filter_coarsen_improve step
+// (src/Omega_h_coarsen_qualities.cpp:111-122)
+static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const V<I8>& vmarks, bool allowed,
+                          bool improve) {
   int dim = m.dim;
-  const V<double>& len = m.ask_lengths();
-  V<I8> ecand(len.size());
-  bool any = false;
-  for (size_t i = 0; i < len.size(); ++i) {
-    ecand[i] = len[i] < o.min_length_desired;
-    any |= bool(ecand[i]);
-  }
-  if (!any) return false;
-  V<I8> vmarks = mark_down(m, EDGE, VERT, ecand);
   const V<LO>& ev2v = m.ask_verts_of(1);
   LO ne = m.nedges();
   V<I8> ecodes((size_t)(ne));
@@ -774,13 +770,29 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o) {
     if (q) *q = unmap(keep, *q, 2);
   };
   filt(nullptr);
-  codes = prevent_coarsen_overshoot(m, o.max_length_desired, c2e, codes);
+  codes = prevent_coarsen_overshoot(m, allowed ? o.max_length_allowed : o.max_length_desired,
+                                    c2e, codes);
   filt(nullptr);
   if (c2e.empty()) return false;
   V<double> quals = coarsen_qualities(m, c2e, codes);
   for (size_t c = 0; c < codes.size(); ++c)
     for (int d = 0; d < 2; ++d)
       if (!(quals[c * 2 + d] >= o.min_quality_allowed)) codes[c] = dont_collapse(codes[c], d);
+  if (improve) {
+    // the worst element quality at each vertex (graph_reduce MIN over v2e)
+    const V<double>& eq = m.ask_qualities();
+    const Adj& v2c = m.ask_up(0, dim);
+    V<double> vold((size_t)(m.nverts()));
+    for (LO v = 0; v < m.nverts(); ++v) {
+      double mq = 1.79769313486231570815e+308;
+      for (LO x = v2c.a2ab[v]; x < v2c.a2ab[v + 1]; ++x) mq = min2(mq, eq[v2c.ab2b[x]]);
+      vold[v] = mq;
+    }
+    for (size_t c = 0; c < codes.size(); ++c)
+      for (int d = 0; d < 2; ++d)
+        if (!(quals[c * 2 + d] > vold[ev2v[(size_t)(c2e[c]) * 2 + d]]))
+          codes[c] = dont_collapse(codes[c], d);
+  }
   filt(&quals);
   if (c2e.empty()) return false;
   V<I8> vc;
@@ -847,6 +859,28 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o) {
   }
   m = std::move(nm);
   return true;
+}
+
+// coarsen_by_size (src/Omega_h_coarsen.cpp:198-208)
+bool coarsen_by_size(Mesh& m, const AdaptOpts& o) {
+  const V<double>& len = m.ask_lengths();
+  V<I8> ecand(len.size());
+  bool any = false;
+  for (size_t i = 0; i < len.size(); ++i) {
+    ecand[i] = len[i] < o.min_length_desired;
+    any |= bool(ecand[i]);
+  }
+  if (!any) return false;
+  return coarsen_verts(m, o, mark_down(m, EDGE, VERT, ecand), false, false);
+}
+
+// coarsen_slivers (src/Omega_h_coarsen.cpp:210-220)
+bool coarsen_slivers(Mesh& m, const AdaptOpts& o) {
+  V<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
+  bool any = false;
+  for (I8 x : ec) any |= bool(x);
+  if (!any) return false;
+  return coarsen_verts(m, o, mark_down(m, m.dim, VERT, ec), true, true);
 }
 
 // ------------------------------------------------------------ swap (3D)
@@ -1184,6 +1218,63 @@ bool swap_edges(Mesh& m, const AdaptOpts& o) {
   }
   swap_rebuild(m, k2e, k2p, pv2v);
   return true;
+}
+
+// ------------------------------------------------------------ adapt()
+// Omega_h::adapt (src/Omega_h_adapt.cpp:153-212, 272-288) without
+// conservation tags or geometry
+AdaptResult adapt(Mesh& m, const AdaptOpts& o) {
+  AdaptResult r;
+  auto minv = [](const V<double>& a) {
+    double x = 1.79769313486231570815e+308;
+    for (double y : a) x = min2(x, y);
+    return x;
+  };
+  auto maxv = [](const V<double>& a) {
+    double x = -1.79769313486231570815e+308;
+    for (double y : a) x = std::max(x, y);
+    return x;
+  };
+  {
+    const V<double>& len = m.ask_lengths();
+    if (minv(m.ask_qualities()) >= o.min_quality_desired && minv(len) >= o.min_length_desired &&
+        maxv(len) <= o.max_length_desired)
+      return r;
+  }
+  r.did = true;
+  bool any;
+  do {
+    any = false;
+    if (refine_by_size(m, o)) {
+      ++r.refines;
+      any = true;
+    }
+    if (coarsen_by_size(m, o)) {
+      ++r.coarsens;
+      any = true;
+    }
+    ++r.length_rounds;
+    OCHECK(r.length_rounds <= 1000);
+  } while (any);
+  if (minv(m.ask_qualities()) >= o.min_quality_desired) {
+    r.quality_satisfied = true;
+    return r;
+  }
+  int rounds = 0;
+  do {
+    OCHECK(++rounds <= 1000);
+    if (swap_edges(m, o)) {
+      ++r.swaps;
+      continue;
+    }
+    if (coarsen_slivers(m, o)) {
+      ++r.sliver_coarsens;
+      continue;
+    }
+    return r;
+  } while (minv(m.ask_qualities()) < o.min_quality_desired);
+  r.quality_satisfied = true;
+  return r;
 }
 
 // ------------------------------------------------------------ the pass

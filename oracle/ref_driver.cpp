@@ -308,7 +308,8 @@ int main(int argc, char** argv) {
   unsigned long long seed = std::strtoull(argv[4], nullptr, 10);
   double mqa = std::atof(argv[5]);
   g_out = argv[6];
-  bool stages = argc < 8 || std::string(argv[7]) != "nostages";
+  std::string mode = argc < 8 ? "" : argv[7];
+  bool stages = mode.empty();
   g_manifest = std::fopen((g_out + "/manifest.txt").c_str(), "w");
   auto lib = Library(&argc, &argv);
   auto t0 = std::chrono::steady_clock::now();
@@ -349,6 +350,19 @@ int main(int argc, char** argv) {
     dump("in_quality_fresh", measure_qualities(&mesh));
     dump("in_hilbert_perm", hilbert::sort_coords(mesh.coords(), dim));
     if (dim == 3) dump_swap_tables();
+  }
+  if (mode == "adapt") {
+    // the full Omega_h::adapt() instead of one pass; the counts of operator
+    // calls are not observable from outside adapt(), so only the outcome and
+    // the mesh are dumped
+    auto ta = std::chrono::steady_clock::now();
+    bool did = adapt(&mesh, opts);
+    double t_ad = seconds_since(ta);
+    dump("adapt_did", LOs({int(did)}));
+    dump_mesh(&mesh, "out_");
+    std::fclose(g_manifest);
+    std::printf("build %.4f adapt %.4f elems_out %d\n", t_build, t_ad, int(mesh.nelems()));
+    return 0;
   }
   // one adapt pass
   double t_ref = 0, t_coa = 0, t_swp = 0;

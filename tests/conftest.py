@@ -26,6 +26,13 @@ SMALL_CASES_2D = {
     "sq32_blayer": (2, 32, 2, 5, 0.3),
     "sq40_sine": (2, 40, 3, 2, 0.3),
 }
+# the full adapt() loop: golden name -> spec (final mesh only)
+ADAPT_CASES = {
+    "box8_iso_adapt": (3, 8, 0, 12345, 0.3),
+    "box10_sine_adapt": (3, 10, 3, 5, 0.2),
+    "sq32_shock_adapt": (2, 32, 1, 5, 0.3),
+    "sq32_blayer_adapt": (2, 32, 2, 5, 0.3),
+}
 BIG_CASE = ("box64_shock", (3, 64, 1, 2024, 0.2))
 # arrays that are metadata, not per-stage outputs
 SKIP_KEYS = ("meta_json", "swap3d_tables", "opts", "opts_values", "r_rep2md")

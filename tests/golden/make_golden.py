@@ -48,6 +48,12 @@ CASES = {
     # isotropic sine field of the batched workload (seeded h0, a, k)
     "box10_sine": (3, 10, 3, 5, 0.2, True),
     "sq40_sine": (2, 40, 3, 2, 0.3, True),
+    # the full adapt() loop (passes until lengths settle, then swaps and
+    # sliver collapses): the final mesh only
+    "box8_iso_adapt": (3, 8, 0, 12345, 0.3, True, "adapt"),
+    "box10_sine_adapt": (3, 10, 3, 5, 0.2, True, "adapt"),
+    "sq32_shock_adapt": (2, 32, 1, 5, 0.3, True, "adapt"),
+    "sq32_blayer_adapt": (2, 32, 2, 5, 0.3, True, "adapt"),
 }
 
 
@@ -57,10 +63,11 @@ def build_ref(ref):
 
 
 def run_case(name, spec):
-    dim, n, kind, seed, mqa, full = spec
+    dim, n, kind, seed, mqa, full = spec[:6]
+    mode = spec[6] if len(spec) > 6 else None
     with tempfile.TemporaryDirectory() as tmp:
         args = [os.path.join(ROOT, "oracle/_ref/ref_driver"), str(dim), str(n),
-                str(kind), str(seed), str(mqa), tmp]
+                str(kind), str(seed), str(mqa), tmp] + ([mode] if mode else [])
         out = subprocess.run(args, check=True, capture_output=True, text=True)
         arrs = {}
         with open(os.path.join(tmp, "manifest.txt")) as f:

@@ -1,0 +1,86 @@
+"""The full adapt() loop on the GPU (passes until lengths settle, then edge
+swaps and sliver collapses) against the reference's final mesh, its operator
+counts against the oracle's, and the precision mode against FP64
+throughout."""
+import numpy as np
+import pytest
+
+from conftest import ADAPT_CASES, compare_arrays, load_golden, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from omega_h_gb300 import build
+    build.build()
+    from omega_h_gb300.mesh import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _adapt(ctx, dim, n, kind, seed, mqa):
+    import gpu_dump
+    from omega_h_gb300.mesh import Mesh, adapt_opts
+    m = Mesh.build_box(ctx, dim, n)
+    m.apply_workload(n, seed, kind)
+    r = m.adapt(adapt_opts(dim, min_quality_allowed=mqa))
+    out = {}
+    gpu_dump.dump_mesh(m, "out_", out, with_length=True, with_quality=True)
+    m.close()
+    return r, out
+
+
+# Over many rounds, every refine interpolates metrics through log and exp,
+# where CUDA's and glibc's results differ by an ulp in about 0.1 % of
+# arguments.  On a symmetric box, edges of exactly equal length are common,
+# and choose_rails breaks such ties by quality: a one-ulp difference can send
+# a collapse along the other edge of a tie.  These cases are therefore held
+# to the fraction of connectivity entries that may differ (measured: 16 of
+# 84,580 edges for box8_iso_adapt, after 11 refines and 12 coarsens); array
+# sizes, reals and operator counts stay checked.  The other cases are
+# bit-exact in every integer.
+LIBM_TIE_SENSITIVE = {"box8_iso_adapt": 1e-3}
+
+
+@pytest.mark.parametrize("case", sorted(ADAPT_CASES))
+def test_full_adapt_matches_reference(ctx, oracle_driver, case):
+    golden = load_golden(case)
+    r, got = _adapt(ctx, *ADAPT_CASES[case])
+    keys = [k for k in golden if k.startswith("out_") and k in got]
+    frac = LIBM_TIE_SENSITIVE.get(case)
+    if frac is not None:
+        for k in keys:
+            a, b = np.asarray(golden[k]), np.asarray(got[k])
+            assert a.shape == b.shape, f"{k}: shape {a.shape} vs {b.shape}"
+            if a.dtype.kind != "f":
+                nd = int(np.sum(a != b.astype(a.dtype)))
+                print(f"  {k}: {nd}/{a.size} differ")
+                assert nd <= frac * a.size, f"{k}: {nd}/{a.size} integers differ"
+        keys = [k for k in keys if np.asarray(golden[k]).dtype.kind == "f"]
+    fails, maxerr, ndiff = compare_arrays(golden, got, keys=keys)
+    print(f"{case}: {r}, max real rel err {maxerr:.2e}, {ndiff} reals not bitwise equal")
+    assert not fails, fails[:10]
+    assert int(golden["adapt_did"][0]) == r["did"]
+    want = run_oracle(oracle_driver, ADAPT_CASES[case], mode="adapt")["adapt_result"]
+    names = ["did", "quality_satisfied", "refines", "coarsens", "swaps", "sliver_coarsens",
+             "length_rounds"]
+    assert [r[k] for k in names] == [int(x) for x in want]
+
+
+def test_full_adapt_screened_equals_fp64(ctx):
+    outs = []
+    for screening in (True, False):
+        ctx.set_screening(screening)
+        try:
+            outs.append(_adapt(ctx, 3, 12, 1, 7, 0.2))
+        finally:
+            ctx.set_screening(True)
+    (r1, a1), (r0, a0) = outs
+    assert r1 == r0
+    for k in a0:
+        assert np.array_equal(np.asarray(a1[k]).view(np.uint8), np.asarray(a0[k]).view(np.uint8)), k
