@@ -192,24 +192,31 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
   Ctx& c = ctx();
   Arr<I8> a(n), b(n);
   auto cd = cview(cands);
+  // flags[0..kIndsetBatch): a vertex is still UNKNOWN after that round of
+  // the batch; flags[kIndsetBatch]: there was a candidate at all
+  constexpr int kIndsetBatch = 8;
+  Arr<int> flags(kIndsetBatch + 1);
+  OHG_CUDA(cudaMemsetAsync(flags.data(), 0, (kIndsetBatch + 1) * sizeof(int), c.stream));
   {
     auto s0 = view(a);
-    pfor(n, [=] __device__(LO i) { s0[i] = cd[i] ? UNKNOWN : NOT_IN; });
+    int* anyc = flags.data() + kIndsetBatch;
+    pfor(n, [=] __device__(LO i) {
+      s0[i] = cd[i] ? UNKNOWN : NOT_IN;
+      if (cd[i]) *anyc = 1;
+    });
   }
   // Rounds are launched in batches of kIndsetBatch with one flag per round
   // and one host read per batch: a round after the one that left no vertex
   // UNKNOWN changes nothing, so the state is the converged one and the
   // count is taken from the first round whose flag stayed clear.
-  constexpr int kIndsetBatch = 8;
-  Arr<int> flags(kIndsetBatch);
   auto xa = cview(g.a2ab);
   auto xb = cview(g.ab2b);
   auto q = cview(quality);
   int rounds = 0;
-  bool any = count_marked(cands) > 0;
+  bool any = true, first = true;
   while (any) {
     if (rounds >= kMaxIndsetRounds) throw Error(5, "independent set did not converge");
-    OHG_CUDA(cudaMemsetAsync(flags.data(), 0, kIndsetBatch * sizeof(int), c.stream));
+    if (!first) OHG_CUDA(cudaMemsetAsync(flags.data(), 0, kIndsetBatch * sizeof(int), c.stream));
     for (int r = 0; r < kIndsetBatch; ++r) {
       int* fl = flags.data() + r;
       auto old = cview(a);
@@ -242,9 +249,11 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
       });
       std::swap(a, b);
     }
-    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flags.data(), kIndsetBatch * sizeof(int),
+    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flags.data(), (kIndsetBatch + 1) * sizeof(int),
                              cudaMemcpyDeviceToHost, c.stream));
     c.sync();
+    if (first && !c.h_pinned[kIndsetBatch]) break;  // no candidate: zero rounds
+    first = false;
     int done = -1;
     for (int r = 0; r < kIndsetBatch && done < 0; ++r)
       if (!c.h_pinned[r]) done = r;
@@ -697,9 +706,8 @@ static void inherit_refine(Mesh& m, int d, const Arr<LO>& k2e, const Arr<LO>& k2
   });
 }
 
-static bool refine(Mesh& m, const AdaptOpts& o, const Arr<I8>& cands, PassStats* st) {
+static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* st) {
   int dim = m.dim, mc = m.mcomp();
-  Arr<LO> c2e = collect_marked(cands);
   LO nc = c2e.size();
   Arr<double> mid(nc * mc);
   mident_metrics(m, c2e.data(), nc, mid.data());
@@ -786,8 +794,9 @@ bool refine_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
   auto c = view(cands);
   double mx = o.max_length_desired;
   pfor(len.size(), [=] __device__(LO i) { c[i] = l[i] > mx; });
-  if (count_marked(cands) == 0) return false;
-  return refine(m, o, cands, st);
+  Arr<LO> c2e = collect_marked(cands);
+  if (c2e.size() == 0) return false;
+  return refine(m, o, c2e, st);
 }
 
 // ------------------------------------------------------------ coarsen
@@ -1480,8 +1489,8 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Arr<I8> codes0 = unmap(c2e, ecodes, 1);
   Arr<I8> codes(c2e.size());
   check_collapse_class(m, c2e.data(), c2e.size(), codes0.data(), codes.data());
-  if (max_i8(codes) <= 0) return false;
   filter_cands(c2e, codes, nullptr);
+  if (c2e.size() == 0) return false;
   Arr<I8> codes2(c2e.size());
   check_collapse_exposure(m, c2e.data(), c2e.size(), codes.data(), codes2.data());
   codes = codes2;
@@ -1685,7 +1694,7 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
     double mn = o.min_length_desired;
     pfor(ne, [=] __device__(LO i) { c[i] = l[i] < mn; });
   }
-  if (count_marked(ecand) == 0) return false;
+  // no separate count: without candidates the candidate list below is empty
   return coarsen_verts(m, o, mark_down(m, EDGE, VERT, ecand), false, false, st);
 }
 
@@ -1693,7 +1702,6 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
 // layers, overshoot up to max_length_allowed, local improvement required
 bool coarsen_slivers(Mesh& m, const AdaptOpts& o, PassStats* st) {
   Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
-  if (count_marked(ec) == 0) return false;
   return coarsen_verts(m, o, mark_down(m, m.dim, VERT, ec), true, true, st);
 }
 
@@ -2424,8 +2432,8 @@ bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
     auto cd = cview(m.class_dim[1]);
     pfor(m.nedges(), [=] __device__(LO i) { e[i] = e[i] && cd[i] == dim; });
   }
-  if (count_marked(edc) == 0) return false;
   Arr<LO> c2e = collect_marked(edc);
+  if (c2e.size() == 0) return false;
   return dim == 3 ? swap_edges_3d(m, o, st, c2e) : swap_edges_2d(m, o, st, c2e);
 }
 
