@@ -318,16 +318,19 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   LO nkeys = keys2kds.size();
   ModifyOut out;
   LO nold = om.nents[ent_dim];
-  if (ent_dim >= key_dim) {
+  // entities kept as they are (0/1 marks and their offsets); the three sizes
+  // this function needs (kept, new, products) are read back together below
+  bool some_mod = ent_dim >= key_dim;
+  Arr<I8> same;
+  Arr<LO> same_offs;
+  if (some_mod) {
     Arr<I8> km = mark_image(keys2kds, om.nents[key_dim]);
     Arr<I8> mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
-    Arr<I8> same(nold);
+    same = Arr<I8>(nold);
     auto me = cview(mods_ent);
     auto sm = view(same);
     pfor(nold, [=] __device__(LO e) { sm[e] = !me[e]; });
-    out.same2old = collect_marked(same);
-  } else {
-    out.same2old = iota(nold);
+    same_offs = offset_scan(same);
   }
   // representatives (get_mods2reps, src/Omega_h_modify.cpp:163-195)
   Arr<LO> reps;
@@ -359,17 +362,24 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   }
   // get_rep_counts (src/Omega_h_modify.cpp:210-243): integer sums, so the
   // atomics give a deterministic result
-  Arr<LO> counts = fill<LO>(nold, 0);
+  Arr<LO> counts(nold);
   {
     auto ct = view(counts);
-    auto s2o = cview(out.same2old);
-    pfor(out.same2old.size(), [=] __device__(LO i) { ct[s2o[i]] = 1; });
+    auto sm = cview(same);
+    pfor(nold, [=] __device__(LO e) { ct[e] = some_mod ? LO(sm[e]) : 1; });
     auto r = cview(reps);
     auto kp = cview(keys2prods);
     pfor(nkeys, [=] __device__(LO k) { atomicAdd(&ct[r[k]], kp[k + 1] - kp[k]); });
   }
   Arr<LO> offs = offset_scan(counts);
-  LO nnew = last(offs);
+  LO sizes[3] = {nold, 0, 0};  // kept, new, products
+  if (some_mod) {
+    read_lasts({&same_offs, &offs, &keys2prods}, sizes);
+  } else {
+    read_lasts({&offs, &keys2prods}, sizes + 1);
+  }
+  LO nnew = sizes[1];
+  out.same2old = some_mod ? collect_marked_offs(same, same_offs, sizes[0]) : iota(nold);
   bool has_order = key_dim > ent_dim;
   Arr<LO> order;
   if (has_order) {
@@ -399,7 +409,7 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     });
   }
   out.same2new = unmap(out.same2old, offs, 1);
-  out.prods2new = Arr<LO>(last(keys2prods));
+  out.prods2new = Arr<LO>(sizes[2]);
   {
     auto of = cview(offs);
     auto r = cview(reps);

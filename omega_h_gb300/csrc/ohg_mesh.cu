@@ -10,11 +10,6 @@
 namespace ohg {
 
 // ------------------------------------------------------------ invert_adj
-// Bitonic sort of each CSR row in registers: a group of G lanes per row with
-// E entries per lane (element i = r * G + lane), G * E >= the row length.
-// Sorted entries hl = high * k + which_down become the high entity and the
-// alignment code.  Rows longer than G * E are sorted by the group's first lane
-// in memory (only reached for rows beyond 128 entries).
 // key = hl * 8 + down code (packed) or hl with the code read from dc
 __device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, LO j,
                                            const I8* dc, bool packed) {
@@ -24,26 +19,24 @@ __device__ __forceinline__ void unpack_use(LO key, int k, LO* lh2hl, I8* codes, 
   lh2hl[j] = hl / k;
 }
 
-// rows with lo_len < n <= hi_len are sorted here; the others are left alone
+// One launch for every row length, with no host read of the longest row:
+// each warp takes four consecutive rows.  When all four have at most 8
+// entries (a warp vote), 8-lane groups sort them at once; when all have at
+// most 16, half warps sort them two at a time; otherwise the whole warp sorts
+// them one after the other with 1, 2 or 4 entries per lane (rows beyond 128
+// entries by one lane in memory).  Every branch is uniform across
+// the warp, so the shuffles always run on full warps.
 template <int E>
-__global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off, LO* lh2hl,
-                           I8* codes, int k, const I8* dc, bool packed) {
-  const int G = 1 << lg;
-  unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-  LO l = LO(t >> lg);
-  int lane = int(t & unsigned(G - 1));
-  bool live = l < nlows;
-  LO b = live ? off[l] : 0, n = live ? off[l + 1] - b : 0;
-  if (n <= lo_len || n > hi_len) n = 0;  // not this launch's row (all lanes of the row agree)
-  if (G == 32 && n == 0) return;         // a warp is one row here: the whole warp leaves
+__device__ __forceinline__ void warp_sort_row(LO b, LO n, int lane, LO* lh2hl, I8* codes, int k,
+                                              const I8* dc, bool packed) {
+  constexpr int G = 32;
   LO v[E];
 #pragma unroll
   for (int r = 0; r < E; ++r) {
     int i = r * G + lane;
     v[r] = (i < n) ? lh2hl[b + i] : 0x7fffffff;
   }
-  int N = G * E;
-  for (int kk = 2; kk <= N; kk <<= 1) {
+  for (int kk = 2; kk <= G * E; kk <<= 1) {
     for (int j = kk >> 1; j > 0; j >>= 1) {
       if (j >= G) {
         int jr = j / G;
@@ -52,20 +45,20 @@ __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off
           if (jr != jc) continue;
 #pragma unroll
           for (int r = 0; r < E; ++r) {
-            const int p = r ^ jc;  // known at compile time: v stays in registers
+            const int p = r ^ jc;
             if (p > r && p < E) {
               int i = r * G + lane;
               bool up = (i & kk) == 0;
-              LO a = v[r], c = v[p];
-              v[r] = up ? min(a, c) : max(a, c);
-              v[p] = up ? max(a, c) : min(a, c);
+              LO x = v[r], y = v[p];
+              v[r] = up ? min(x, y) : max(x, y);
+              v[p] = up ? max(x, y) : min(x, y);
             }
           }
         }
       } else {
 #pragma unroll
         for (int r = 0; r < E; ++r) {
-          LO o = __shfl_xor_sync(0xffffffffu, v[r], j, G);
+          LO o = __shfl_xor_sync(0xffffffffu, v[r], j);
           int i = r * G + lane;
           bool up = (i & kk) == 0;
           bool lower = (lane & j) == 0;
@@ -74,21 +67,6 @@ __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off
       }
     }
   }
-  if (n > N) {
-    if (lane == 0) {
-      for (LO j = b + 1; j < b + n; ++j) {
-        LO x = lh2hl[j];
-        LO i = j - 1;
-        while (i >= b && lh2hl[i] > x) {
-          lh2hl[i + 1] = lh2hl[i];
-          --i;
-        }
-        lh2hl[i + 1] = x;
-      }
-      for (LO j = b; j < b + n; ++j) unpack_use(lh2hl[j], k, lh2hl, codes, j, dc, packed);
-    }
-    return;
-  }
 #pragma unroll
   for (int r = 0; r < E; ++r) {
     int i = r * G + lane;
@@ -96,37 +74,86 @@ __global__ void k_row_sort(LO nlows, int lg, LO lo_len, LO hi_len, const LO* off
   }
 }
 
-// Rows of up to 32 entries are sorted by groups of G lanes (G the smallest
-// power of two >= min(longest row, 32)), one entry per lane; when longer rows
-// exist, a second launch sorts them by whole warps with up to 4 entries per
-// lane (rows beyond 128 by one lane in memory).
-static void sort_rows_by_high(LO nlows, LO maxdeg, const Arr<LO>& off, Arr<LO>& lh2hl,
-                              Arr<I8>& codes, int k, const I8* dc, bool packed) {
+// a row of at most G entries sorted by a group of G lanes (sl = lane in group)
+template <int G>
+__device__ __forceinline__ void group_sort_row(LO b, LO n, int sl, LO* lh2hl, I8* codes, int k,
+                                               const I8* dc, bool packed) {
+  LO v = sl < n ? lh2hl[b + sl] : 0x7fffffff;
+#pragma unroll
+  for (int kk = 2; kk <= G; kk <<= 1) {
+#pragma unroll
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      LO o = __shfl_xor_sync(0xffffffffu, v, j, G);
+      bool up = (sl & kk) == 0;
+      bool lower = (sl & j) == 0;
+      v = (lower == up) ? min(v, o) : max(v, o);
+    }
+  }
+  if (sl < n) unpack_use(v, k, lh2hl, codes, b + sl, dc, packed);
+}
+
+__global__ void k_row_sort_adaptive(LO nlows, const LO* off, LO* lh2hl, I8* codes, int k,
+                                    const I8* dc, bool packed) {
+  unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  int lane = int(t & 31u);
+  LO row0 = LO(t >> 5) * 4;
+  LO l = row0 + (lane >> 3);
+  LO b = l < nlows ? off[l] : 0, n = l < nlows ? off[l + 1] - b : 0;
+  if (!__any_sync(0xffffffffu, n > 8)) {
+    // four rows of at most 8 entries, one per 8-lane group
+    group_sort_row<8>(b, n, lane & 7, lh2hl, codes, k, dc, packed);
+    return;
+  }
+  if (!__any_sync(0xffffffffu, n > 16)) {
+    // two rows at a time of at most 16 entries, one per half warp
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      LO l2 = row0 + 2 * h + (lane >> 4);
+      LO b2 = l2 < nlows ? off[l2] : 0, n2 = l2 < nlows ? off[l2 + 1] - b2 : 0;
+      group_sort_row<16>(b2, n2, lane & 15, lh2hl, codes, k, dc, packed);
+    }
+    return;
+  }
+  for (int r = 0; r < 4; ++r) {
+    LO row = row0 + r;
+    if (row >= nlows) break;  // same for every lane
+    LO rb = off[row], rn = off[row + 1] - rb;
+    if (rn <= 32) {
+      warp_sort_row<1>(rb, rn, lane, lh2hl, codes, k, dc, packed);
+    } else if (rn <= 64) {
+      warp_sort_row<2>(rb, rn, lane, lh2hl, codes, k, dc, packed);
+    } else if (rn <= 128) {
+      warp_sort_row<4>(rb, rn, lane, lh2hl, codes, k, dc, packed);
+    } else if (lane == 0) {
+      for (LO j = rb + 1; j < rb + rn; ++j) {
+        LO x = lh2hl[j];
+        LO i = j - 1;
+        while (i >= rb && lh2hl[i] > x) {
+          lh2hl[i + 1] = lh2hl[i];
+          --i;
+        }
+        lh2hl[i + 1] = x;
+      }
+      for (LO j = rb; j < rb + rn; ++j) unpack_use(lh2hl[j], k, lh2hl, codes, j, dc, packed);
+    }
+    __syncwarp();
+  }
+}
+
+static void sort_rows_by_high(LO nlows, const Arr<LO>& off, Arr<LO>& lh2hl, Arr<I8>& codes, int k,
+                              const I8* dc, bool packed) {
   if (nlows <= 0) return;
   Ctx& c = ctx();
-  auto launch = [&](int lg, int E, LO lo_len, LO hi_len) {
-    long long nthreads = (((long long)nlows << lg) + 31) / 32 * 32;
-    if (nthreads + kBlock > 0xffffffffLL) throw Error(8, "invert_adj: too many rows for one launch");
-    unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
-    if (E == 1)
-      k_row_sort<1><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k, dc, packed);
-    else if (E == 2)
-      k_row_sort<2><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k, dc, packed);
-    else
-      k_row_sort<4><<<nblocks, kBlock, 0, c.stream>>>(nlows, lg, lo_len, hi_len, off.data(),
-                                                      lh2hl.data(), codes.data(), k, dc, packed);
-    ++c.launches;
+  long long nwarps = (nlows + 3) / 4;
+  long long nthreads = nwarps * 32;
+  if (nthreads + kBlock > 0xffffffffLL) throw Error(8, "invert_adj: too many rows for one launch");
+  unsigned nblocks = unsigned((nthreads + kBlock - 1) / kBlock);
+  k_row_sort_adaptive<<<nblocks, kBlock, 0, c.stream>>>(nlows, off.data(), lh2hl.data(),
+                                                        codes.data(), k, dc, packed);
+  ++c.launches;
 #ifdef OHG_CHECKED
-    checked_after_launch(__FILE__, __LINE__);
+  checked_after_launch(__FILE__, __LINE__);
 #endif
-  };
-  int lg = 0;
-  while ((1 << lg) < maxdeg && lg < 5) ++lg;
-  // rows of 0..32 entries (a row of one entry still needs unpacking)
-  launch(lg, 1, -1, 32);
-  if (maxdeg > 32) launch(5, maxdeg > 64 ? 4 : 2, 32, 0x7fffffff);
 }
 
 // Upward adjacency from a downward one (src/Omega_h_adj.cpp:231-263).
@@ -162,8 +189,7 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
     lh2hl[off[l] + atomicAdd(&ps[l], 1)] = packed ? hl * 8 + c : hl;
   });
   // rows sorted by high entity (sort_by_high_index)
-  LO maxdeg = nlows ? max_lo(deg) : 0;
-  sort_rows_by_high(nlows, maxdeg, up.a2ab, up.ab2b, up.codes, k,
+  sort_rows_by_high(nlows, up.a2ab, up.ab2b, up.codes, k,
                     packed ? nullptr : (has_dc ? down.codes.data() : nullptr), packed);
   return up;
 }

@@ -304,6 +304,29 @@ void offset_scan_fixed_scratch(const LO* counts, LO n, LO* out) {
 
 LO last(const Arr<LO>& a) { return get_elem(a, a.size() - 1); }
 
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out) {
+  Ctx& c = ctx();
+  int n = int(arrs.size());
+  if (n > 16) throw Error(8, "read_lasts: at most 16 arrays");
+  for (int i = 0; i < n; ++i)
+    OHG_CUDA(cudaMemcpyAsync(c.h_pinned + i, arrs[i]->data() + arrs[i]->size() - 1, sizeof(LO),
+                             cudaMemcpyDeviceToHost, c.stream));
+  c.sync();
+  for (int i = 0; i < n; ++i) out[i] = c.h_pinned[i];
+}
+
+Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt) {
+  LO n = marks.size();
+  Arr<LO> out(cnt);
+  auto m = cview(marks);
+  auto o = cview(offs);
+  auto d = view(out);
+  pfor(n, [=] __device__(LO i) {
+    if (m[i]) d[o[i]] = i;
+  });
+  return out;
+}
+
 Arr<LO> collect_marked(const Arr<I8>& marks) {
   LO n = marks.size();
   Arr<I8> nz(n);

@@ -24,6 +24,10 @@ Arr<LO> collect_marked(const Arr<I8>& marks);
 LO count_marked(const Arr<I8>& marks);
 
 LO last(const Arr<LO>& a);
+// the last element of each array (at most 16) with one host wait
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out);
+// indices of nonzero marks given offset_scan of the 0/1 marks and its total
+Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt);
 
 // reductions (synchronise the stream)
 I8 max_i8(const Arr<I8>& a);
