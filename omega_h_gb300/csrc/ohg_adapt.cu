@@ -170,6 +170,17 @@ __device__ __forceinline__ void warp_count(unsigned long long* p, unsigned v) {
   if (int(threadIdx.x & 31) == __ffs(mask) - 1 && tot) atomicAdd(p, (unsigned long long)tot);
 }
 
+// warp_count for code that every lane of the warp reaches
+__device__ __forceinline__ void warp_count_full(unsigned long long* p, unsigned v) {
+  unsigned tot = __reduce_add_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31u) == 0u && tot) atomicAdd(p, (unsigned long long)tot);
+}
+
+// lanes per collapse direction in the cavity screens (both directions of a
+// candidate must fit in one warp: at most 16)
+constexpr int kCavityLanes = 8;
+static_assert(kCavityLanes <= 16, "two directions per warp");
+
 // smallest float >= x, for comparing floats against a double threshold
 static float float_at_or_above(double x) {
   float f = float(x);
@@ -870,112 +881,6 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
   }
 }
 
-// prevent_coarsen_overshoot with FP32 screening of the new edge lengths:
-// an enclosure of each FP64 length settles "length >= max_length" unless the
-// threshold lies inside it; those lengths are computed in FP64.
-template <int D>
-static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, const LO* c2e_p,
-                                                 LO n, const I8* ci_p, I8* co_p) {
-  constexpr int dim = D, mc = D == 3 ? 6 : 3;
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
-  auto sv = screen_view(vs);
-  auto ev = cview(m.ask_verts_of(1));
-  const Adj& v2e = m.ask_up(0, 1);
-  auto va = cview(v2e.a2ab);
-  auto vb = cview(v2e.ab2b);
-  auto vc = cview(v2e.codes);
-  auto c = cview(m.coords);
-  auto mt = cview(m.metric);
-  auto c2e = cview(c2e_p, n);
-  auto ci = cview(ci_p, n);
-  auto co = view(co_p, n);
-  float thr = float_at_or_above(max_length);  // for float x: x >= max_length <=> x >= thr
-  unsigned long long* cnt = ctx().d_screen_counts;
-  pfor(n, [=] __device__(LO cand) {
-    LO e = c2e[cand];
-    I8 code = ci[cand];
-    unsigned nscreen = 0, nexact = 0;
-    for (int col = 0; col < 2; ++col) {
-      if (!collapses(code, col)) continue;
-      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
-      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
-        LO e2 = vb[x];
-        if (e2 == e) continue;
-        int ein = code_which_down(vc[x]), eout = 1 - ein;
-        LO nv[2];
-        nv[ein] = v_onto;
-        nv[eout] = ev[e2 * 2 + eout];
-        FIv L = edge_len_bounds_d(dim, sv, nv[0], nv[1]);
-        ++nscreen;
-        bool over;
-        if (L.lo >= thr) {
-          over = true;
-        } else if (L.hi < thr) {
-          over = false;
-        } else {
-          over = edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length;
-          ++nexact;
-        }
-        if (over) {
-          code = dont_collapse(code, col);
-          break;
-        }
-      }
-    }
-    co[cand] = code;
-    warp_count(&cnt[2], nscreen);
-    warp_count(&cnt[3], nexact);
-  });
-}
-static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
-                                               LO n, const I8* ci_p, I8* co_p) {
-  if (m.dim == 3)
-    prevent_coarsen_overshoot_screened_d<3>(m, max_length, c2e_p, n, ci_p, co_p);
-  else
-    prevent_coarsen_overshoot_screened_d<2>(m, max_length, c2e_p, n, ci_p, co_p);
-}
-
-// prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
-void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n,
-                               const I8* ci_p, I8* co_p) {
-  if (ctx().screening) {
-    prevent_coarsen_overshoot_screened(m, max_length, c2e_p, n, ci_p, co_p);
-    return;
-  }
-  auto ev = cview(m.ask_verts_of(1));
-  const Adj& v2e = m.ask_up(0, 1);
-  auto va = cview(v2e.a2ab);
-  auto vb = cview(v2e.ab2b);
-  auto vc = cview(v2e.codes);
-  auto c = cview(m.coords);
-  auto mt = cview(m.metric);
-  int dim = m.dim, mc = m.mcomp();
-  auto c2e = cview(c2e_p, n);
-  auto ci = cview(ci_p, n);
-  auto co = view(co_p, n);
-  pfor(n, [=] __device__(LO cand) {
-    LO e = c2e[cand];
-    I8 code = ci[cand];
-    for (int col = 0; col < 2; ++col) {
-      if (!collapses(code, col)) continue;
-      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
-      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
-        LO e2 = vb[x];
-        if (e2 == e) continue;
-        int ein = code_which_down(vc[x]), eout = 1 - ein;
-        LO nv[2];
-        nv[ein] = v_onto;
-        nv[eout] = ev[e2 * 2 + eout];
-        if (edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length) {
-          code = dont_collapse(code, col);
-          break;
-        }
-      }
-    }
-    co[cand] = code;
-  });
-}
-
 // The cavity of collapsing v_col onto v_onto: the elements around v_col that
 // do not contain v_onto, with v_col replaced by v_onto.  Returns false for an
 // element that dies in the collapse.
@@ -1164,6 +1069,243 @@ __device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, L
   return minq;
 }
 
+// Persistent screening of collapse directions.  Each warp takes chunks of
+// kQueueChunk directions from a global counter, and each lane takes the next
+// direction of its warp's chunk as soon as its current one is settled, so
+// the lanes stay busy whatever the cavity sizes and early exits (the
+// while-while loop of persistent ray traversal).  A direction whose
+// enclosure of min(1, cavity qualities) straddles the threshold goes to a
+// list for the FP64 stage, with the smallest upper bound of its cavity.
+constexpr int kQueueChunk = 64;
+
+// The refill step of a persistent warp: lanes with st == 0 take the next
+// items of the warp's chunk, calling start(item), which returns the lane's
+// new state (1: working on the item, 0: the item was settled at once);
+// lanes find st == 2 once the queue is exhausted.  Every lane of the warp
+// calls this.
+struct WarpQueue {
+  long long next = 0, end = 0;
+  template <class Start>
+  __device__ __forceinline__ void refill(int& st, LO nitems, unsigned long long* counter,
+                                         Start start) {
+    const unsigned full = 0xffffffffu;
+    const int lane = int(threadIdx.x & 31u);
+    const unsigned below = (1u << lane) - 1u;
+    unsigned needm = __ballot_sync(full, st == 0);
+    while (needm) {
+      if (next >= end) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)kQueueChunk);
+        base = __shfl_sync(full, base, 0);
+        if (base >= (unsigned long long)nitems) {
+          if (st == 0) st = 2;
+          return;
+        }
+        next = (long long)base;
+        end = next + kQueueChunk < nitems ? next + kQueueChunk : nitems;
+      }
+      int avail = int(end - next);
+      int rank = __popc(needm & below);
+      if (st == 0 && rank < avail) st = start(LO(next + rank));
+      int took = __popc(needm);
+      next += took < avail ? took : avail;
+      needm = __ballot_sync(full, st == 0);
+    }
+  }
+};
+
+struct CoarsenScreenArgs {
+  LO ndirs;
+  ScreenView sv;
+  LV ev, cv, va, vb;
+  View<const I8> vc;
+  View<const LO> c2e;
+  View<const I8> codes;
+  View<double> q2;
+  float mqa_f;
+  unsigned long long* queue;  // [0] next direction, [1] directions in the list
+  LO* amb_dir;
+  float* amb_mhi;
+  unsigned long long* cnt;
+};
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) {
+  constexpr int dim = D;
+  WarpQueue q;
+  int st = 0;  // 0: needs a direction, 1: screening one, 2: done
+  LO d = 0, x = 0, x1 = 0, v_onto = 0;
+  float lo = 1.0f, hi = 1.0f;
+  unsigned nscreen = 0;
+  for (;;) {
+    q.refill(st, a.ndirs, &a.queue[0], [&](LO item) {
+      d = item;
+      LO cand = d >> 1;
+      int col = d & 1;
+      if (!collapses(a.codes[cand], col)) {
+        a.q2[d] = -1.0;
+        return 0;
+      }
+      LO e = a.c2e[cand];
+      LO v_col = a.ev[e * 2 + col];
+      v_onto = a.ev[e * 2 + (1 - col)];
+      x = a.va[v_col];
+      x1 = a.va[v_col + 1];
+      lo = hi = 1.0f;
+      if (x < x1) return 1;
+      a.q2[d] = CUDART_NAN;  // empty cavity: min(1) passes
+      return 0;
+    });
+    if (__all_sync(0xffffffffu, st == 2)) break;
+    if (st == 1) {
+      LO vv[4];
+      if (collapse_elem(a.cv, dim, a.vb[x], code_which_down(a.vc[x]), v_onto, vv)) {
+        FIv b = elem_quality_bounds(dim, a.sv, vv);
+        lo = fminf(lo, b.lo);
+        hi = fminf(hi, b.hi);
+        ++nscreen;
+      }
+      ++x;
+      if (hi < a.mqa_f) {
+        a.q2[d] = -1.0;  // fails: the minimum only falls as elements are added
+        st = 0;
+      } else if (x >= x1) {
+        if (lo >= a.mqa_f) {
+          a.q2[d] = CUDART_NAN;  // passes on its enclosure
+        } else {
+          LO k = LO(atomicAdd(&a.queue[1], 1ULL));
+          a.amb_dir[k] = d;
+          a.amb_mhi[k] = hi;
+          a.q2[d] = -1.0;  // replaced by the FP64 minimum
+        }
+        st = 0;
+      }
+    }
+  }
+  warp_count_full(a.cnt, nscreen);
+}
+
+// grid of a persistent kernel: as many blocks as stay resident on the device,
+// and no more than the work needs
+template <class K>
+static unsigned persistent_blocks(K kernel, long long work_warps) {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0));
+    if (per_sm < 1) per_sm = 1;
+  }
+  long long full = (long long)per_sm * ctx().num_sms;
+  long long need = (work_warps * 32 + kBlock - 1) / kBlock;
+  long long b = need < full ? need : full;
+  return unsigned(b < 1 ? 1 : b);
+}
+
+// prevent_coarsen_overshoot with FP32 screening of the new edge lengths:
+// an enclosure of each FP64 length settles "length >= max_length" unless the
+// threshold lies inside it; those lengths are computed in FP64.
+template <int D>
+static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, const LO* c2e_p,
+                                                 LO n, const I8* ci_p, I8* co_p) {
+  constexpr int dim = D, mc = D == 3 ? 6 : 3;
+  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
+  auto sv = screen_view(vs);
+  auto ev = cview(m.ask_verts_of(1));
+  const Adj& v2e = m.ask_up(0, 1);
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto c2e = cview(c2e_p, n);
+  auto ci = cview(ci_p, n);
+  auto co = view(co_p, n);
+  float thr = float_at_or_above(max_length);  // for float x: x >= max_length <=> x >= thr
+  unsigned long long* cnt = ctx().d_screen_counts;
+  pfor(n, [=] __device__(LO cand) {
+    LO e = c2e[cand];
+    I8 code = ci[cand];
+    unsigned nscreen = 0, nexact = 0;
+    for (int col = 0; col < 2; ++col) {
+      if (!collapses(code, col)) continue;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
+        LO e2 = vb[x];
+        if (e2 == e) continue;
+        int ein = code_which_down(vc[x]), eout = 1 - ein;
+        LO nv[2];
+        nv[ein] = v_onto;
+        nv[eout] = ev[e2 * 2 + eout];
+        FIv L = edge_len_bounds_d(dim, sv, nv[0], nv[1]);
+        ++nscreen;
+        bool over;
+        if (L.lo >= thr) {
+          over = true;
+        } else if (L.hi < thr) {
+          over = false;
+        } else {
+          over = edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length;
+          ++nexact;
+        }
+        if (over) {
+          code = dont_collapse(code, col);
+          break;
+        }
+      }
+    }
+    co[cand] = code;
+    warp_count(&cnt[2], nscreen);
+    warp_count(&cnt[3], nexact);
+  });
+}
+static void prevent_coarsen_overshoot_screened(Mesh& m, double max_length, const LO* c2e_p,
+                                               LO n, const I8* ci_p, I8* co_p) {
+  if (m.dim == 3)
+    prevent_coarsen_overshoot_screened_d<3>(m, max_length, c2e_p, n, ci_p, co_p);
+  else
+    prevent_coarsen_overshoot_screened_d<2>(m, max_length, c2e_p, n, ci_p, co_p);
+}
+
+// prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
+void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n,
+                               const I8* ci_p, I8* co_p) {
+  if (ctx().screening) {
+    prevent_coarsen_overshoot_screened(m, max_length, c2e_p, n, ci_p, co_p);
+    return;
+  }
+  auto ev = cview(m.ask_verts_of(1));
+  const Adj& v2e = m.ask_up(0, 1);
+  auto va = cview(v2e.a2ab);
+  auto vb = cview(v2e.ab2b);
+  auto vc = cview(v2e.codes);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  int dim = m.dim, mc = m.mcomp();
+  auto c2e = cview(c2e_p, n);
+  auto ci = cview(ci_p, n);
+  auto co = view(co_p, n);
+  pfor(n, [=] __device__(LO cand) {
+    LO e = c2e[cand];
+    I8 code = ci[cand];
+    for (int col = 0; col < 2; ++col) {
+      if (!collapses(code, col)) continue;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      for (LO x = va[v_col]; x < va[v_col + 1]; ++x) {
+        LO e2 = vb[x];
+        if (e2 == e) continue;
+        int ein = code_which_down(vc[x]), eout = 1 - ein;
+        LO nv[2];
+        nv[ein] = v_onto;
+        nv[eout] = ev[e2 * 2 + eout];
+        if (edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length) {
+          code = dont_collapse(code, col);
+          break;
+        }
+      }
+    }
+    co[cand] = code;
+  });
+}
+
 // The quality filter of coarsen_by_size (src/Omega_h_coarsen.cpp:29-58 with
 // coarsen_qualities and filter_coarsen_min_qual) from enclosures: a
 // direction whose enclosure of min(1, cavity qualities) lies on one side of
@@ -1196,42 +1338,119 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   LO nV = m.nverts(), nT = m.nelems();
   double bytes = double(n) * (4 + 1 + 8 + 1 + 16) + double(nV + 1) * 4 +
                  double(v2c.ab2b.size()) * 5 + double(nT) * 4 * (dim + 1) + double(nV) * 80;
-  KernelTimer timer("coarsen_filter", bytes);
-  pfor(n, [=] __device__(LO cand) {
-    LO e = c2e[cand];
-    I8 code = codes[cand];
-    unsigned nscreen = 0, nexact = 0;
-    for (int col = 0; col < 2; ++col) {
-      q2[cand * 2 + col] = -1.0;
-      if (!collapses(code, col)) continue;
+  LO ndirs = LO(2LL * n);
+  if (2LL * n + (long long)kQueueChunk * 32 * 65536 > 0x7fffffffffffLL || 2LL * n > 0x7fffffffLL)
+    throw Error(8, "coarsen filter: too many candidates");
+  Arr<unsigned long long> queue = fill<unsigned long long>(2, 0ULL);
+  Arr<LO> amb_dir(ndirs);
+  Arr<float> amb_mhi(ndirs);
+  CoarsenScreenArgs args{ndirs, sv, ev, cv, va, vb, vc, c2e, cview(codes_p, n), q2, mqa_f,
+                         queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
+  {
+    KernelTimer timer("coarsen_filter", bytes);
+    unsigned nb = persistent_blocks(k_coarsen_screen<D>, (ndirs + kQueueChunk - 1) / kQueueChunk);
+    k_coarsen_screen<D><<<nb, kBlock, 0, ctx().stream>>>(args);
+    ++ctx().launches;
+#ifdef OHG_CHECKED
+    checked_after_launch(__FILE__, __LINE__);
+#endif
+  }
+  // FP64 minima of the straddling directions: the elements whose lower bound
+  // does not exceed the smallest upper bound become (direction, element)
+  // pairs in one dense list, evaluated in full warps, reduced by an atomic
+  // minimum on order keys (the minimum of a set of doubles does not depend
+  // on the order of evaluation)
+  unsigned long long hq[2];
+  {
+    Ctx& cx = ctx();
+    OHG_CUDA(cudaMemcpyAsync(cx.h_pinned, queue.data() + 1, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, cx.stream));
+    cx.sync();
+    std::memcpy(&hq[1], cx.h_pinned, sizeof(unsigned long long));
+  }
+  LO K = LO(hq[1]);
+  if (K > 0) {
+    auto ad = cview(amb_dir);
+    auto am = cview(amb_mhi);
+    constexpr int G = kCavityLanes;
+    // elements of each cavity that need FP64
+    Arr<LO> pcount(K);
+    auto pc = view(pcount);
+    group_for(G, K, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+      if (k < 0) return;
+      LO d = ad[k], e = c2e[d >> 1];
+      int col = d & 1;
       LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
-      // the minimum only falls as tets are added: once an upper bound is
-      // below the threshold the direction fails, whatever the other tets are
-      float lo = 1.0f, hi = 1.0f;
-      for (LO x = va[v_col]; x < va[v_col + 1] && hi >= mqa_f; ++x) {
+      float mh = am[k];
+      LO x1 = va[v_col + 1], np = 0;
+      for (LO xb = va[v_col]; xb < x1; xb += G) {
+        LO x = xb + gl;
         LO vv[4];
-        if (!collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv)) continue;
-        FIv b = elem_quality_bounds(dim, sv, vv);
-        lo = fminf(lo, b.lo);
-        hi = fminf(hi, b.hi);
-        ++nscreen;
+        if (x < x1 && collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv) &&
+            elem_quality_bounds(dim, sv, vv).lo <= mh)
+          ++np;
       }
-      bool pass;
-      if (lo >= mqa_f) {
-        pass = true;
-        q2[cand * 2 + col] = CUDART_NAN;
-      } else if (hi < mqa_f) {
-        pass = false;
-      } else {
-        double q = collapse_min_exact<dim>(sv, c, mt, cv, va, vb, vc, v_col, v_onto, &nexact);
-        q2[cand * 2 + col] = q;
-        pass = q >= mqa;
+#pragma unroll
+      for (int j = G / 2; j > 0; j >>= 1) np += __shfl_xor_sync(gm, np, j, G);
+      if (gl == 0) pc[k] = np;
+    });
+    Arr<LO> poff = offset_scan(pcount);
+    LO P = last(poff);
+    Arr<LO> pk(P), px(P);
+    auto po = cview(poff);
+    auto pkv = view(pk);
+    auto pxv = view(px);
+    group_for(G, K, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+      if (k < 0) return;
+      LO d = ad[k], e = c2e[d >> 1];
+      int col = d & 1;
+      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+      float mh = am[k];
+      LO x1 = va[v_col + 1], at = po[k];
+      unsigned glt = gm & ((1u << (threadIdx.x & 31u)) - 1u);
+      for (LO xb = va[v_col]; xb < x1; xb += G) {
+        LO x = xb + gl;
+        LO vv[4];
+        bool need = x < x1 && collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv) &&
+                    elem_quality_bounds(dim, sv, vv).lo <= mh;
+        unsigned bits = __ballot_sync(gm, need) & gm;
+        if (need) {
+          LO slot = at + __popc(bits & glt);
+          pkv[slot] = k;
+          pxv[slot] = x;
+        }
+        at += __popc(bits);
       }
-      if (!pass) code = dont_collapse(code, col);
+    });
+    Arr<long long> kmin = fill<long long>(K, order_key(1.0));
+    auto km = view(kmin);
+    auto pkc = cview(pk);
+    auto pxc = cview(px);
+    pfor(P, [=] __device__(LO i) {
+      LO k = pkc[i], x = pxc[i];
+      LO d = ad[k], e = c2e[d >> 1];
+      int col = d & 1;
+      LO v_onto = ev[e * 2 + (1 - col)];
+      LO vv[4];
+      collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv);
+      atomicMin(&km[k], order_key(elem_quality_exact(dim, sv, c, mt, vv)));
+    });
+    auto kmc = cview(kmin);
+    unsigned long long nfp64 = (unsigned long long)P;
+    pfor(K, [=] __device__(LO k) {
+      q2[ad[k]] = key_to_double(kmc[k]);
+      if (k == 0) cnt[1] += nfp64;
+    });
+  }
+  // the decisions: a direction passes on its enclosure (NaN) or on its FP64
+  // minimum; -1 marks a failed or non-collapsing direction
+  pfor(n, [=] __device__(LO cand) {
+    I8 code = codes[cand];
+    for (int col = 0; col < 2; ++col) {
+      double q = q2[cand * 2 + col];
+      if (collapses(code, col) && !(q != q || q >= mqa)) code = dont_collapse(code, col);
     }
     codes[cand] = code;
-    warp_count(&cnt[0], nscreen);
-    warp_count(&cnt[1], nexact);
   });
 }
 static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,

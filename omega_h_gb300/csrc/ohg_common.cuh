@@ -50,6 +50,7 @@ struct Ctx {
   int* h_pinned = nullptr;  // pinned host scratch for small reads
   int* d_swap_tables = nullptr;  // edge-swap triangulation tables (device copy)
   int swap_tables_len = 0;
+  int num_sms = 0;  // streaming multiprocessors of the device
   std::uint64_t launches = 0;
   std::uint64_t syncs = 0;  // host waits on the stream (sizes and flags read back)
   // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
@@ -213,6 +214,62 @@ inline void pfor_at(const char* file, int line, LO n, F f) {
 #endif
 }
 #define pfor(n, ...) ::ohg::pfor_at(__FILE__, __LINE__, (n), __VA_ARGS__)
+
+// Lane groups: G consecutive lanes of a warp (G a power of two, at most 32)
+// share one work item, item = global thread / G, with gl the lane in the
+// group.  Every thread of the grid calls f, threads past the last item with
+// item = -1, so code after the item's work may use full-warp collectives.
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+  unsigned lane = threadIdx.x & 31u;
+  return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~unsigned(G - 1)));
+}
+template <int G>
+__device__ __forceinline__ float group_min(float v, unsigned gm) {
+#pragma unroll
+  for (int j = G / 2; j > 0; j >>= 1) v = fminf(v, __shfl_xor_sync(gm, v, j, G));
+  return v;
+}
+template <int G>
+__device__ __forceinline__ double group_min(double v, unsigned gm) {
+#pragma unroll
+  for (int j = G / 2; j > 0; j >>= 1) {
+    double o = __shfl_xor_sync(gm, v, j, G);
+    v = (o < v) ? o : v;
+  }
+  return v;
+}
+template <int G>
+__device__ __forceinline__ bool group_any(bool p, unsigned gm) {
+  return (__ballot_sync(gm, p) & gm) != 0u;
+}
+
+template <int G, class F>
+__global__ void k_group_for(LO n, F f) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long item = t / G;
+  f(item < n ? LO(item) : LO(-1), int(t % G), group_mask<G>());
+}
+
+template <int G, class F>
+inline void group_for_at(const char* file, int line, LO n, int block, F f) {
+  static_assert(G >= 1 && G <= 32 && (G & (G - 1)) == 0, "G: a power of two up to 32");
+  if (n <= 0) return;
+  if (block % 32 != 0 || block > 1024) throw Error(8, "group_for: block not a multiple of 32");
+  Ctx& c = ctx();
+  long long threads = (long long)n * G;
+  long long blocks = (threads + block - 1) / block;
+  if (blocks > 0x7fffffffLL) throw Error(8, "group_for: too many items for one launch");
+  k_group_for<G><<<unsigned(blocks), block, 0, c.stream>>>(n, f);
+  ++c.launches;
+#ifdef OHG_CHECKED
+  checked_after_launch(file, line);
+#else
+  (void)file;
+  (void)line;
+#endif
+}
+#define group_for(G, n, block, ...) ::ohg::group_for_at<G>(__FILE__, __LINE__, (n), (block), __VA_ARGS__)
 
 // Records a named kernel's launch duration (when the context times
 // kernels) with its algorithmic bytes; construct before the launch, destroy

@@ -24,6 +24,7 @@ void set_ctx(Ctx* c) { g_ctx = c; }
 Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaSetDevice(dev));
   OHG_CUDA(cudaStreamCreate(&stream));  // blocking: ordered with the legacy default stream
+  OHG_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   OHG_CUDA(cudaMalloc(&d_status, sizeof(int)));
   OHG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
   OHG_CUDA(cudaMallocHost(&h_pinned, 64));

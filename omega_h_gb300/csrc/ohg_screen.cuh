@@ -79,6 +79,18 @@ __host__ __device__ __forceinline__ long long order_key(double d) {
   return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+// inverse of order_key (zero comes back as +0)
+__host__ __device__ __forceinline__ double key_to_double(long long k) {
+  long long b = k >= 0 ? k : (k ^ 0x7fffffffffffffffLL);
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double d;
+  std::memcpy(&d, &b, sizeof(d));
+  return d;
+#endif
+}
+
 struct FIv {
   float lo, hi;
 };
@@ -256,17 +268,54 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
   if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
   if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
   float s_lo = __fsub_rd(sv, es);
-  // mean squared metric length
-  float msum = 0.0f, emsum = 0.0f, asum = 0.0f;
+  // mean squared metric length: the sum over the six edges of v^T M v is
+  // the contraction M : G with G = sum v v^T.  Its float evaluation differs
+  // from the exact value for the float edges and float metric by at most
+  // (gamma_6 for G, gamma_4 for the contraction) times
+  // asum = sum |v|^T |M| |v| = |M| : (sum |v| |v|^T); the metric's
+  // conversion to float adds u asum and the double evaluation far less
+  // (12.2 u asum in all).  The edge errors e_i perturb the sum by at most
+  // sum 2 e_i 1^T |M| |v_i| + e_i^2 S0 = 2 c . w + S0 sum e_i^2, with c the
+  // column sums of |M| and w = sum e_i |v_i|.
+  float gxx = 0.0f, gyy = 0.0f, gzz = 0.0f, gxy = 0.0f, gyz = 0.0f, gzx = 0.0f;
+  float hxy = 0.0f, hyz = 0.0f, hzx = 0.0f;
+  float wx = 0.0f, wy = 0.0f, wz = 0.0f, esq = 0.0f;
+#pragma unroll
   for (int i = 0; i < 6; ++i) {
-    float A, S1;
-    float q = mprod(ma, mb, ev[i], A, S1);
-    msum = __fadd_rn(msum, q);
-    asum = __fadd_rn(asum, A);
-    emsum = __fadd_rn(emsum, mprod_err(A, S1, mb.z, ee[i]));
+    const float* v = ev[i];
+    float ax = fabsf(v[0]), ay = fabsf(v[1]), az = fabsf(v[2]), e = ee[i];
+    gxx = __fmaf_rn(v[0], v[0], gxx);
+    gyy = __fmaf_rn(v[1], v[1], gyy);
+    gzz = __fmaf_rn(v[2], v[2], gzz);
+    gxy = __fmaf_rn(v[0], v[1], gxy);
+    gyz = __fmaf_rn(v[1], v[2], gyz);
+    gzx = __fmaf_rn(v[2], v[0], gzx);
+    hxy = __fmaf_rn(ax, ay, hxy);
+    hyz = __fmaf_rn(ay, az, hyz);
+    hzx = __fmaf_rn(az, ax, hzx);
+    wx = __fmaf_rn(e, ax, wx);
+    wy = __fmaf_rn(e, ay, wy);
+    wz = __fmaf_rn(e, az, wz);
+    esq = __fmaf_rn(e, e, esq);
   }
+  float mxx = ma.x, myy = ma.y, mzz = ma.z, myx = ma.w, mzy = mb.x, mzx = mb.y;
+  float dg = __fmaf_rn(mzz, gzz, __fmaf_rn(myy, gyy, __fmul_rn(mxx, gxx)));
+  float od = __fmaf_rn(mzx, gzx, __fmaf_rn(mzy, gyz, __fmul_rn(myx, gxy)));
+  float msum = __fmaf_rn(2.0f, od, dg);
+  float axx = fabsf(mxx), ayy = fabsf(myy), azz = fabsf(mzz), ayx = fabsf(myx), azy = fabsf(mzy),
+        azx = fabsf(mzx);
+  float adg = __fmaf_rn(azz, gzz, __fmaf_rn(ayy, gyy, __fmul_rn(axx, gxx)));
+  float aod = __fmaf_rn(azx, hzx, __fmaf_rn(azy, hyz, __fmul_rn(ayx, hxy)));
+  float asum = __fmaf_rn(2.0f, aod, adg);
+  float cx = __fadd_rn(__fadd_rn(axx, ayx), azx);
+  float cy = __fadd_rn(__fadd_rn(ayx, ayy), azy);
+  float cz = __fadd_rn(__fadd_rn(azx, azy), azz);
+  float cw = __fmaf_rn(cz, wz, __fmaf_rn(cy, wy, __fmul_rn(cx, wx)));
+  float pert = __fmul_rn(__fmaf_rn(2.0f, cw, __fmul_rn(mb.z, esq)), 1.0f + kU);
   float msl = __fmul_rn(msum, kSixth);
-  float emsl = __fmaf_rn(fabsf(msl), kC2, __fmul_rn(__fmaf_rn(5.1f * kU, asum, emsum), kSixthUp));
+  float emsl = __fmaf_rn(fabsf(msl), kC2,
+                         __fmul_rn(__fmaf_rn(12.2f * kU, asum, __fadd_rn(pert, 16.0f * kTiny)),
+                                   kSixthUp));
   emsl = __fmul_rn(emsl, kInflate);
   float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
   // the range keeps __fdividef within its documented 2-ulp error
