@@ -34,6 +34,8 @@ METRIC = "elements/s per adapt pass"
 # list): the screened coarsen quality filter; its DRAM traffic per launch
 # (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture
 DOMINANT = "coarsen_filter"
+# untimed passes in which the launch-shape autotuner explores its variants
+AUTOTUNE_PASSES = 4
 DOMINANT_TRAFFIC = 121394432  # bytes per launch on the 64^3 shock pass
 # Batched workload: 1024 independent 3D boxes, subdivisions per axis
 # log-uniform integers in [4, 40] (seeded), isotropic sine metric with seeded
@@ -85,6 +87,8 @@ def _args():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the boundary-layer precision workloads")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="launch shapes at their defaults (no exploration passes)")
     ap.add_argument("--profile-pass", action="store_true",
                     help="build the workload, run one warm-up and one timed pass, exit "
                          "(for kernel launch lists under a profiler)")
@@ -309,6 +313,9 @@ def run_batch(ctx, lib_stream, flush, args):
 
     ms_batch = []
     for step in range(max(1, args.warmup) + 2):
+        # the warm-up passes explore launch shapes for the union's sizes
+        if not args.no_autotune:
+            ctx.autotune("explore" if step < max(1, args.warmup) else "frozen")
         work = clones(base)
         t = timed(lambda: adapt_pass_batch(ctx, work, opts))
         if step >= max(1, args.warmup):
@@ -435,6 +442,16 @@ def run_ours(args):
         torch.cuda.synchronize()
         m.close()
         return e0.elapsed_time(e1), st
+
+    # ---- launch-shape autotuning: untimed passes in explore mode, then the
+    # choices are frozen for everything that follows
+    tune_passes = 0 if args.no_autotune else AUTOTUNE_PASSES
+    if tune_passes:
+        ctx.autotune("explore")
+        for _ in range(tune_passes):
+            one_pass(False)
+        ctx.autotune("frozen")
+    tuning = ctx.tuning()
 
     if args.profile_pass:
         one_pass(False)
@@ -569,7 +586,9 @@ def run_ours(args):
                 "batched": batched,
                 "served": served,
                 "cpu_baseline": cpu, "gpu_launches": gpu_launches,
-                "host_syncs_per_step": host_syncs / args.steps, "clocks": clk.summary()}
+                "host_syncs_per_step": host_syncs / args.steps, "clocks": clk.summary(),
+                "autotune": {"passes": tune_passes, "sites": tuning[0], "chosen": tuning[1],
+                             "non_default": tuning[2]}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

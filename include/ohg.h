@@ -92,6 +92,22 @@ int ohg_context_set_screening(ohg_context* ctx, int on);
  * recomputed in FP64 */
 int ohg_context_screen_counts(ohg_context* ctx, unsigned long long* counts4, int reset);
 
+/* Launch-shape autotuner (no counterpart in the reference, whose launches
+ * use Kokkos' fixed policies).  Tuned sites are the element-wise launches of
+ * at least 65,536 items (block 128, 256 or 512 threads) and the persistent
+ * coarsen screen (block 256 or 512, queue chunk 64 or 32), each per size
+ * class (log2 of the item count).  Every variant computes the same results.
+ * mode 0: defaults; 1: explore (each site's first launch runs the default
+ * untimed, the next ones each variant once, timed by CUDA events read at the
+ * next host wait; the site then keeps the fastest); 2 (default): frozen, the
+ * choices made so far and the defaults elsewhere.  force >= 0 makes every
+ * tuned site run variant (force mod its variant count); -1 ends that. */
+int ohg_context_autotune(ohg_context* ctx, int mode);
+int ohg_context_force_variant(ohg_context* ctx, int force);
+/* tuned sites so far: [0] sites seen, [1] sites with a choice, [2] sites
+ * whose choice is not the default variant */
+int ohg_context_tuning(ohg_context* ctx, int* counts3);
+
 /* ---- meshes ---- */
 /* build_box on the unit square/cube with n subdivisions per axis, Hilbert
  * renumbered and classified (build_box, src/Omega_h_build.cpp:136-149) */

@@ -1070,7 +1070,7 @@ __device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, L
 }
 
 // Persistent screening of collapse directions.  Each warp takes chunks of
-// kQueueChunk directions from a global counter, and each lane takes the next
+// directions (kQueueChunk by default) from a global counter, and each lane takes the next
 // direction of its warp's chunk as soon as its current one is settled, so
 // the lanes stay busy whatever the cavity sizes and early exits (the
 // while-while loop of persistent ray traversal).  A direction whose
@@ -1086,7 +1086,7 @@ constexpr int kQueueChunk = 64;
 struct WarpQueue {
   long long next = 0, end = 0;
   template <class Start>
-  __device__ __forceinline__ void refill(int& st, LO nitems, unsigned long long* counter,
+  __device__ __forceinline__ void refill(int& st, LO nitems, int chunk, unsigned long long* counter,
                                          Start start) {
     const unsigned full = 0xffffffffu;
     const int lane = int(threadIdx.x & 31u);
@@ -1095,14 +1095,14 @@ struct WarpQueue {
     while (needm) {
       if (next >= end) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(counter, (unsigned long long)kQueueChunk);
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
         base = __shfl_sync(full, base, 0);
         if (base >= (unsigned long long)nitems) {
           if (st == 0) st = 2;
           return;
         }
         next = (long long)base;
-        end = next + kQueueChunk < nitems ? next + kQueueChunk : nitems;
+        end = next + chunk < nitems ? next + chunk : nitems;
       }
       int avail = int(end - next);
       int rank = __popc(needm & below);
@@ -1116,6 +1116,7 @@ struct WarpQueue {
 
 struct CoarsenScreenArgs {
   LO ndirs;
+  int chunk;
   ScreenView sv;
   LV ev, cv, va, vb;
   View<const I8> vc;
@@ -1130,7 +1131,7 @@ struct CoarsenScreenArgs {
 };
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) {
+__global__ void __launch_bounds__(512) k_coarsen_screen(CoarsenScreenArgs a) {
   constexpr int dim = D;
   WarpQueue q;
   int st = 0;  // 0: needs a direction, 1: screening one, 2: done
@@ -1138,7 +1139,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) 
   float lo = 1.0f, hi = 1.0f;
   unsigned nscreen = 0;
   for (;;) {
-    q.refill(st, a.ndirs, &a.queue[0], [&](LO item) {
+    q.refill(st, a.ndirs, a.chunk, &a.queue[0], [&](LO item) {
       d = item;
       LO cand = d >> 1;
       int col = d & 1;
@@ -1185,17 +1186,18 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) 
   warp_count_full(a.cnt, nscreen);
 }
 
-// grid of a persistent kernel: as many blocks as stay resident on the device,
-// and no more than the work needs
+// grid of a persistent kernel: as many blocks of the given size as stay
+// resident on the device, and no more than the work needs
 template <class K>
-static unsigned persistent_blocks(K kernel, long long work_warps) {
-  static int per_sm = 0;
+static unsigned persistent_blocks(K kernel, int block, long long work_warps) {
+  static std::map<int, int> per_sm_of;
+  int& per_sm = per_sm_of[block];
   if (per_sm == 0) {
-    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0));
+    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0));
     if (per_sm < 1) per_sm = 1;
   }
   long long full = (long long)per_sm * ctx().num_sms;
-  long long need = (work_warps * 32 + kBlock - 1) / kBlock;
+  long long need = (work_warps * 32 + block - 1) / block;
   long long b = need < full ? need : full;
   return unsigned(b < 1 ? 1 : b);
 }
@@ -1339,18 +1341,24 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   double bytes = double(n) * (4 + 1 + 8 + 1 + 16) + double(nV + 1) * 4 +
                  double(v2c.ab2b.size()) * 5 + double(nT) * 4 * (dim + 1) + double(nV) * 80;
   LO ndirs = LO(2LL * n);
-  if (2LL * n + (long long)kQueueChunk * 32 * 65536 > 0x7fffffffffffLL || 2LL * n > 0x7fffffffLL)
-    throw Error(8, "coarsen filter: too many candidates");
+  if (2LL * n > 0x7fffffffLL) throw Error(8, "coarsen filter: too many candidates");
   Arr<unsigned long long> queue = fill<unsigned long long>(2, 0ULL);
   Arr<LO> amb_dir(ndirs);
   Arr<float> amb_mhi(ndirs);
-  CoarsenScreenArgs args{ndirs, sv, ev, cv, va, vb, vc, c2e, cview(codes_p, n), q2, mqa_f,
+  // tuned launch shape: block 256 or 512 threads, queue chunk 64 or 32
+  // directions (the results do not depend on either)
+  Ctx& cx = ctx();
+  int var = cx.tuner.select("coarsen_screen", D, ndirs, 4, 0, cx.stream);
+  bool timed = cx.tuner.open >= 0;
+  int block = (var & 1) ? 512 : 256, chunk = (var & 2) ? 32 : kQueueChunk;
+  CoarsenScreenArgs args{ndirs, chunk, sv, ev, cv, va, vb, vc, c2e, cview(codes_p, n), q2, mqa_f,
                          queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
   {
     KernelTimer timer("coarsen_filter", bytes);
-    unsigned nb = persistent_blocks(k_coarsen_screen<D>, (ndirs + kQueueChunk - 1) / kQueueChunk);
-    k_coarsen_screen<D><<<nb, kBlock, 0, ctx().stream>>>(args);
-    ++ctx().launches;
+    unsigned nb = persistent_blocks(k_coarsen_screen<D>, block, (ndirs + chunk - 1) / chunk);
+    k_coarsen_screen<D><<<nb, block, 0, cx.stream>>>(args);
+    if (timed) cx.tuner.stop(cx.stream);
+    ++cx.launches;
 #ifdef OHG_CHECKED
     checked_after_launch(__FILE__, __LINE__);
 #endif
@@ -1362,7 +1370,6 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   // on the order of evaluation)
   unsigned long long hq[2];
   {
-    Ctx& cx = ctx();
     OHG_CUDA(cudaMemcpyAsync(cx.h_pinned, queue.data() + 1, sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, cx.stream));
     cx.sync();

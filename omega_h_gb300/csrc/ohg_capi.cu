@@ -92,6 +92,47 @@ int ohg_context_syncs(ohg_context* c, unsigned long long* out) {
   return OHG_OK;
 }
 
+int ohg_context_autotune(ohg_context* c, int mode) {
+  if (!c || mode < 0 || mode > 2) {
+    g_err = "ohg_context_autotune: null context or mode not 0, 1 or 2";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    Ctx& x = ctx();
+    x.sync();  // reads the exploration launches still in flight
+    x.tuner.mode = mode;
+  });
+}
+int ohg_context_force_variant(ohg_context* c, int force) {
+  if (!c) {
+    g_err = "null context";
+    return OHG_ERR_INVALID;
+  }
+  c->ctx.tuner.forced = force < 0 ? -1 : force;
+  return OHG_OK;
+}
+int ohg_context_tuning(ohg_context* c, int* counts3) {
+  if (!counts3) {
+    g_err = "null argument";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    Ctx& x = ctx();
+    x.sync();
+    int seen = 0, chosen = 0, moved = 0;
+    for (auto& kv : x.tuner.sites) {
+      ++seen;
+      if (kv.second.chosen >= 0) {
+        ++chosen;
+        if (kv.second.chosen != kv.second.dflt) ++moved;
+      }
+    }
+    counts3[0] = seen;
+    counts3[1] = chosen;
+    counts3[2] = moved;
+  });
+}
+
 int ohg_context_set_screening(ohg_context* c, int on) {
   if (!c) {
     g_err = "null context";

@@ -11,6 +11,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -43,6 +44,46 @@ void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (ohg_e_ != cudaSuccess) ::ohg::cuda_fail(ohg_e_, #call, __FILE__, __LINE__); \
   } while (0)
 
+// Online launch-shape autotuner.  A tuned launch site (a kernel and the
+// size class of its launch, log2 of the item count) has a few variants (block
+// sizes, queue chunks) that all compute the same results; in explore mode
+// the first launches of a site run each variant once, timed by CUDA events
+// on the context's stream, and the site then keeps the fastest.  Events are
+// read at the next host wait, so tuning adds no synchronisation.  Frozen
+// mode uses the choices made so far (the default variant elsewhere); off
+// mode uses the defaults.
+struct Tuner {
+  enum Mode { OFF = 0, EXPLORE = 1, FROZEN = 2 };
+  struct Site {
+    const char* name = nullptr;
+    int line = 0, bucket = 0;
+    int nvar = 0, dflt = 0;
+    int seen = 0;                // launches of the site
+    std::vector<float> best;     // fastest timed launch per variant (ms), < 0 untimed
+    std::vector<char> launched;  // variant timed (in flight or read)
+    int chosen = -1;
+  };
+  struct Pending {
+    Site* site;
+    int var;
+    cudaEvent_t a, b;
+  };
+  int mode = FROZEN;
+  int forced = -1;  // every tuned site runs variant (forced mod its count)
+  std::unordered_map<std::uint64_t, Site> sites;
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> spare;
+  int open = -1;  // pending entry of the launch being issued
+  // variant for a launch of n items at site (name, line); brackets it with
+  // events when it is an exploration launch (open >= 0: the caller then
+  // calls stop after the launch)
+  int select(const char* name, int line, long long n, int nvar, int dflt, cudaStream_t s);
+  void stop(cudaStream_t s);
+  // reads finished events (call after the stream is idle)
+  void resolve();
+  void release();
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -67,6 +108,7 @@ struct Ctx {
     double bytes;
   };
   std::vector<KernelLaunch> kernel_launches;
+  Tuner tuner;
   explicit Ctx(int dev);
   ~Ctx();
   Ctx(const Ctx&) = delete;
@@ -200,11 +242,35 @@ static inline void checked_after_launch(const char* file, int line) {
 }
 #endif
 
+// launches of at least this many items have their block size tuned
+constexpr LO kTuneMinItems = 1 << 16;
+
+// block-size variants of a k_for instance: 128, 256 (default), 512, as far
+// as the kernel's register use allows
+template <class F>
+inline int k_for_variants() {
+  static int nvar = 0;
+  if (nvar == 0) {
+    cudaFuncAttributes fa;
+    OHG_CUDA(cudaFuncGetAttributes(&fa, k_for<F>));
+    nvar = fa.maxThreadsPerBlock >= 512 ? 3 : 2;
+  }
+  return nvar;
+}
+
 template <class F>
 inline void pfor_at(const char* file, int line, LO n, F f) {
   if (n <= 0) return;
   Ctx& c = ctx();
-  k_for<<<(n + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(n, f);
+  int block = kBlock;
+  bool timed = false;
+  if (n >= kTuneMinItems && c.tuner.mode != Tuner::OFF) {
+    int v = c.tuner.select(file, line, n, k_for_variants<F>(), 1, c.stream);
+    timed = c.tuner.open >= 0;
+    block = 128 << v;
+  }
+  k_for<<<(n + block - 1) / block, block, 0, c.stream>>>(n, f);
+  if (timed) c.tuner.stop(c.stream);
   ++c.launches;
 #ifdef OHG_CHECKED
   checked_after_launch(file, line);

@@ -37,6 +37,7 @@ Ctx::Ctx(int dev) : device(dev) {
 }
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
+  tuner.release();
   for (auto& k : kernel_launches) {
     cudaEventDestroy(k.start);
     cudaEventDestroy(k.stop);
@@ -50,6 +51,101 @@ Ctx::~Ctx() {
 void Ctx::sync() {
   ++syncs;
   OHG_CUDA(cudaStreamSynchronize(stream));
+  if (!tuner.pending.empty()) tuner.resolve();
+}
+
+// ------------------------------------------------------------ autotuner
+int Tuner::select(const char* name, int line, long long n, int nvar, int dflt, cudaStream_t s) {
+  open = -1;
+  if (nvar <= 1) return 0;
+  if (forced >= 0) return forced % nvar;
+  if (mode == OFF) return dflt;
+  int bucket = 0;
+  while ((2LL << bucket) <= n) ++bucket;
+  std::uint64_t key = std::uint64_t(reinterpret_cast<std::uintptr_t>(name)) * 0x9E3779B97F4A7C15ULL ^
+                      (std::uint64_t(line) << 8) ^ std::uint64_t(bucket);
+  Site& st = sites[key];
+  if (st.nvar == 0) {
+    st.name = name;
+    st.line = line;
+    st.bucket = bucket;
+    st.nvar = nvar;
+    st.dflt = dflt;
+    st.best.assign(nvar, -1.0f);
+    st.launched.assign(nvar, 0);
+  }
+  int seen = st.seen++;
+  if (st.chosen >= 0) return st.chosen;
+  if (mode != EXPLORE) {
+    // frozen: the fastest variant timed so far, else the default
+    int b = -1;
+    for (int v = 0; v < nvar; ++v)
+      if (st.best[v] >= 0.0f && (b < 0 || st.best[v] < st.best[b])) b = v;
+    return b >= 0 ? b : dflt;
+  }
+  // the site's first launch is not timed (it may load the kernel); then
+  // each variant once
+  if (seen == 0) return dflt;
+  int v = -1;
+  for (int k = 0; k < nvar; ++k) {
+    int c = (dflt + k) % nvar;
+    if (!st.launched[c]) {
+      v = c;
+      break;
+    }
+  }
+  if (v < 0) return dflt;  // all timed, waiting for the events
+  st.launched[v] = 1;
+  Pending p{&st, v, nullptr, nullptr};
+  for (cudaEvent_t* e : {&p.a, &p.b}) {
+    if (!spare.empty()) {
+      *e = spare.back();
+      spare.pop_back();
+    } else {
+      OHG_CUDA(cudaEventCreate(e));
+    }
+  }
+  OHG_CUDA(cudaEventRecord(p.a, s));
+  pending.push_back(p);
+  open = int(pending.size()) - 1;
+  return v;
+}
+
+void Tuner::stop(cudaStream_t s) {
+  if (open >= 0) OHG_CUDA(cudaEventRecord(pending[open].b, s));
+  open = -1;
+}
+
+void Tuner::resolve() {
+  for (Pending& p : pending) {
+    float ms = -1.0f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) != cudaSuccess) {
+      cudaGetLastError();
+      ms = -1.0f;
+    }
+    Site& st = *p.site;
+    if (ms >= 0.0f && (st.best[p.var] < 0.0f || ms < st.best[p.var])) st.best[p.var] = ms;
+    spare.push_back(p.a);
+    spare.push_back(p.b);
+    bool all = true;
+    int b = 0;
+    for (int v = 0; v < st.nvar; ++v) {
+      if (st.best[v] < 0.0f) all = false;
+      else if (st.best[v] < st.best[b] || st.best[b] < 0.0f) b = v;
+    }
+    if (all) st.chosen = b;
+  }
+  pending.clear();
+}
+
+void Tuner::release() {
+  for (Pending& p : pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  pending.clear();
+  for (cudaEvent_t e : spare) cudaEventDestroy(e);
+  spare.clear();
 }
 int Ctx::take_status() {
   OHG_CUDA(cudaMemcpyAsync(h_pinned, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));

@@ -45,6 +45,20 @@ class Context:
         _lib.call("ohg_context_syncs", self.handle, ctypes.byref(v))
         return v.value
 
+    def autotune(self, mode):
+        """Launch-shape autotuner: "off", "explore" or "frozen" (default)."""
+        _lib.call("ohg_context_autotune", self.handle, {"off": 0, "explore": 1, "frozen": 2}[mode])
+
+    def force_variant(self, v):
+        """Run every tuned launch site with variant v (None: the tuner's)."""
+        _lib.call("ohg_context_force_variant", self.handle, -1 if v is None else int(v))
+
+    def tuning(self):
+        """(sites seen, sites with a choice, choices other than the default)."""
+        v = (ctypes.c_int * 3)()
+        _lib.call("ohg_context_tuning", self.handle, v)
+        return tuple(int(x) for x in v)
+
     def set_screening(self, on):
         """FP32 screening with exact FP64 recheck (True, default) or FP64
         throughout (False)."""
