@@ -50,7 +50,7 @@ BATCH = {"workload": "batch1024_sine", "meshes": 1024, "n_min": 4, "n_max": 40, 
 # request; 150 GB admission budget.  A bounded sample of the stream is served
 # at each rate so the run stays within minutes.
 SERVE = {"workload": "serve_mix", "requests": 160, "rates_per_s": [50.0, 200.0, 800.0],
-         "budget_gb": 150.0, "seed": 11}
+         "budget_gb": 150.0, "seed": 11, "slots_per_dim": 2}
 
 
 def serve_specs(sv=SERVE):
@@ -340,46 +340,56 @@ def run_batch(ctx, lib_stream, flush, args):
             "batched_over_plain": batched / plain}
 
 
-def run_serve(ctx, args):
+def run_serve(ctx, args, slots_per_dim=None):
     """The serving workload at each arrival rate: continuous batching against
     one request at a time, the same requests (resident meshes cloned from the
-    same bases) and the same arrival times."""
+    same bases) and the same arrival times.  Batching routes each request to
+    one of slots_per_dim contexts of its dimension; their union passes
+    overlap on the device."""
     import numpy as np
     from omega_h_gb300.mesh import Mesh
-    from omega_h_gb300.serve import Request, serve, serve_one_at_a_time, summary
+    from omega_h_gb300.serve import Request, route, serve, serve_one_at_a_time, summary
     from omega_h_gb300.mesh import Context
+    k = slots_per_dim or SERVE["slots_per_dim"]
     specs, gaps = serve_specs()
-    ctxs = {3: ctx, 2: Context(ctx.device)}  # 2D and 3D union passes overlap
+    extra = [Context(ctx.device) for _ in range(2 * k - 1)]
+    slots = {3: [ctx] + extra[:k - 1], 2: extra[k - 1:]}
+    ctxs = {3: ctx, 2: slots[2][0]}
     bases = []
     for dim, n, kind, seed, _ in specs:
         m = Mesh.build_box(ctxs[dim], dim, n)
         m.apply_workload(n, seed, kind)
         bases.append(m)
     elements = sum(m.nelems() for m in bases)
+    dims = [sp[0] for sp in specs]
+    where = route(dims, [b.nelems() * sp[4] for b, sp in zip(bases, specs)],
+                  {d: len(c) for d, c in slots.items()})
 
-    def stream(rate):
+    def stream(rate, routed):
         arr = np.cumsum(gaps) / rate
         arr -= arr[0]
         reqs = []
         for i, (b, sp) in enumerate(zip(bases, specs)):
             h = ctypes.c_void_p()
-            _lib_call("ohg_mesh_clone", b.handle, ctypes.byref(h))
-            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(ctxs[sp[0]], h),
+            target = slots[sp[0]][where[i]] if routed else ctxs[sp[0]]
+            _lib_call("ohg_mesh_clone_to", b.handle, target.handle, ctypes.byref(h))
+            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(target, h),
                                 passes=sp[4]))
         return reqs
 
     # warm both paths once on a few requests
-    for fn in (lambda r: serve(ctxs, r), lambda r: serve_one_at_a_time(ctx, r)):
-        w = stream(1e9)[:6]
+    for fn, routed in ((lambda r: serve(ctx, r), True), (lambda r: serve_one_at_a_time(ctx, r), False)):
+        w = stream(1e9, routed)[:6]
         fn(w)
         for r in w:
             r.mesh.close()
     rates = []
     for rate in SERVE["rates_per_s"]:
         res = {}
-        for name, fn in (("served", lambda r: serve(ctxs, r, budget_bytes=SERVE["budget_gb"] * 1e9)),
-                         ("plain", lambda r: serve_one_at_a_time(ctx, r))):
-            reqs = stream(rate)
+        for name, fn, routed in (
+                ("served", lambda r: serve(ctx, r, budget_bytes=SERVE["budget_gb"] * 1e9), True),
+                ("plain", lambda r: serve_one_at_a_time(ctx, r), False)):
+            reqs = stream(rate, routed)
             out = fn(reqs)
             res[name] = summary(out)
             for r in out:
@@ -389,9 +399,10 @@ def run_serve(ctx, args):
         rates.append(res)
     for m in bases:
         m.close()
-    ctxs[2].close()
+    for c in extra:
+        c.close()
     return {"workload": SERVE["workload"], "requests": len(specs), "elements": elements,
-            "budget_gb": SERVE["budget_gb"], "rates": rates}
+            "budget_gb": SERVE["budget_gb"], "slots_per_dim": k, "rates": rates}
 
 
 def _lib_call(name, *a):

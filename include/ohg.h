@@ -134,6 +134,10 @@ int ohg_mesh_from_arrays(ohg_context* ctx, int dim, const int* nents,
                          const double* metric_dev, ohg_mesh** out);
 /* a device copy of a mesh's stored arrays (derived adjacencies are not copied) */
 int ohg_mesh_clone(ohg_mesh* mesh, ohg_mesh** out);
+/* a copy of a mesh owned by another context (no counterpart in the
+ * reference): the source context's stream is waited on, then the copies run
+ * on the target context's stream */
+int ohg_mesh_clone_to(ohg_mesh* src, ohg_context* ctx, ohg_mesh** out);
 int ohg_mesh_destroy(ohg_mesh* mesh);
 int ohg_mesh_dim(ohg_mesh* mesh, int* out);
 int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);

@@ -63,6 +63,7 @@ SIGNATURES = {
     "ohg_mesh_from_arrays": [c_void_p, c_int, P(c_int), P(c_void_p), P(c_void_p), P(c_void_p),
                              P(c_void_p), c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_clone": [c_void_p, P(c_void_p)],
+    "ohg_mesh_clone_to": [c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_apply_workload": [c_void_p, c_int, c_ull, c_int],
     "ohg_mesh_from_elems": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_destroy": [c_void_p],

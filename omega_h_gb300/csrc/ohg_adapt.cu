@@ -1190,7 +1190,7 @@ __global__ void __launch_bounds__(512) k_coarsen_screen(CoarsenScreenArgs a) {
 // resident on the device, and no more than the work needs
 template <class K>
 static unsigned persistent_blocks(K kernel, int block, long long work_warps) {
-  static std::map<int, int> per_sm_of;
+  thread_local std::map<int, int> per_sm_of;  // per host thread: no locking
   int& per_sm = per_sm_of[block];
   if (per_sm == 0) {
     OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0));

@@ -252,31 +252,51 @@ int ohg_mesh_from_arrays(ohg_context* c, int dim, const int* nents, const int* c
   return OHG_OK;
 }
 
+static void clone_mesh(const Mesh& a, Mesh& b) {
+  b.dim = a.dim;
+  for (int d = 0; d < 4; ++d) b.nents[d] = a.nents[d];
+  for (int d = 1; d <= a.dim; ++d) {
+    const Adj& x = a.adj.at({d, d - 1});
+    Adj y;
+    y.ab2b = copy_arr(x.ab2b);
+    if (x.has_codes) {
+      y.codes = copy_arr(x.codes);
+      y.has_codes = true;
+    }
+    b.adj[{d, d - 1}] = std::move(y);
+  }
+  for (int d = 0; d <= a.dim; ++d) {
+    b.class_dim[d] = copy_arr(a.class_dim[d]);
+    b.class_id[d] = copy_arr(a.class_id[d]);
+  }
+  b.coords = copy_arr(a.coords);
+  b.metric = copy_arr(a.metric);
+}
+
 int ohg_mesh_clone(ohg_mesh* src, ohg_mesh** out) {
   MESH_GUARD(src);
   ohg_mesh* m = new ohg_mesh{src->owner, Mesh()};
-  int rc = guarded(src->owner, [&] {
-    const Mesh& a = src->mesh;
-    Mesh& b = m->mesh;
-    b.dim = a.dim;
-    for (int d = 0; d < 4; ++d) b.nents[d] = a.nents[d];
-    for (int d = 1; d <= a.dim; ++d) {
-      const Adj& x = a.adj.at({d, d - 1});
-      Adj y;
-      y.ab2b = copy_arr(x.ab2b);
-      if (x.has_codes) {
-        y.codes = copy_arr(x.codes);
-        y.has_codes = true;
-      }
-      b.adj[{d, d - 1}] = std::move(y);
-    }
-    for (int d = 0; d <= a.dim; ++d) {
-      b.class_dim[d] = copy_arr(a.class_dim[d]);
-      b.class_id[d] = copy_arr(a.class_id[d]);
-    }
-    b.coords = copy_arr(a.coords);
-    b.metric = copy_arr(a.metric);
-  });
+  int rc = guarded(src->owner, [&] { clone_mesh(src->mesh, m->mesh); });
+  if (rc != OHG_OK) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return OHG_OK;
+}
+
+int ohg_mesh_clone_to(ohg_mesh* src, ohg_context* c, ohg_mesh** out) {
+  MESH_GUARD(src);
+  if (!c || !out) {
+    g_err = "ohg_mesh_clone_to: null context or output";
+    return OHG_ERR_INVALID;
+  }
+  // the source's arrays are complete once its context's stream is idle;
+  // the copies then run on the target context's stream
+  int rc = guarded(src->owner, [&] { ctx().sync(); });
+  if (rc != OHG_OK) return rc;
+  ohg_mesh* m = new ohg_mesh{c, Mesh()};
+  rc = guarded(c, [&] { clone_mesh(src->mesh, m->mesh); });
   if (rc != OHG_OK) {
     delete m;
     return rc;

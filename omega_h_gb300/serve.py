@@ -9,9 +9,12 @@ step, finished requests leave and free their memory.  Because a union pass is
 bit for bit the separate passes, a request's result does not depend on what
 it was batched with.
 
-With one context per dimension (``ctx`` a dict {2: ctx2, 3: ctx3}, each
-request's mesh built on the context of its dimension), the 2D and 3D union
-passes of a step run concurrently on the two contexts' streams.
+Each request's mesh lives on a context (a slot: one stream and its memory
+pool on the device), chosen when the request is routed; ``route`` spreads a
+stream of requests over the slots of each dimension by the work already sent
+to each.  A step runs one union pass per slot that holds admitted requests,
+all slots at once from a pool of host threads (the library's calls release
+the interpreter lock), so the slots' passes overlap on the device.
 
 ``serve_one_at_a_time`` runs the same stream with one request on the device
 at a time and no batching, the baseline the batched loop is measured against.
@@ -54,18 +57,35 @@ def _prepare(reqs):
     return sorted(reqs, key=lambda r: (r.arrival, r.rid))
 
 
+def route(dims, work, slots):
+    """Slot index for each request (in arrival order): the slot of the
+    request's dimension with the least work routed to it so far.  ``slots``
+    maps a dimension to its number of slots."""
+    load = {d: [0.0] * k for d, k in slots.items()}
+    out = []
+    for d, w in zip(dims, work):
+        i = min(range(slots[d]), key=lambda j: load[d][j])
+        load[d][i] += w
+        out.append(i)
+    return out
+
+
 def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter):
     """Continuous batching.  Returns the requests with admitted/done times
-    (seconds from the stream start) and per-pass union stats."""
+    (seconds from the stream start) and per-pass union stats.  The slots are
+    the contexts of the requests' meshes (``ctx`` is kept for callers that
+    pass one; the meshes decide)."""
     reqs = _prepare(requests)
-    ctxs = ctx if isinstance(ctx, dict) else {2: ctx, 3: ctx}
-    parallel = ctxs[2] is not ctxs[3]
-    pool = concurrent.futures.ThreadPoolExecutor(2) if parallel else None
+    slots = []
+    for r in reqs:
+        if not any(r.mesh.ctx is c for c in slots):
+            slots.append(r.mesh.ctx)
+    pool = concurrent.futures.ThreadPoolExecutor(len(slots)) if len(slots) > 1 else None
 
     def run_group(dim, group):
         o = opts[dim] if opts else adapt_opts(dim)
         n_before = [r.mesh.nelems() for r in group]
-        st = adapt_pass_batch(ctxs[dim], [r.mesh for r in group], o)
+        st = adapt_pass_batch(group[0].mesh.ctx, [r.mesh for r in group], o)
         for r, nb in zip(group, n_before):
             r.passes_done += 1
             r.element_passes += nb
@@ -90,9 +110,13 @@ def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter)
         if not active:
             time.sleep(max(0.0, pending[0].arrival - now))
             continue
-        groups = [(d, [r for r in active if r.dim == d]) for d in (2, 3)]
-        groups = [(d, g) for d, g in groups if g]
-        if pool and len(groups) == 2:
+        groups = []
+        for c in slots:
+            for d in (2, 3):
+                g = [r for r in active if r.mesh.ctx is c and r.dim == d]
+                if g:
+                    groups.append((d, g))
+        if pool and len(groups) > 1:
             for f in [pool.submit(run_group, d, g) for d, g in groups]:
                 f.result()
         else:

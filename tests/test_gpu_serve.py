@@ -34,6 +34,15 @@ def ctx2(ctx):
     c.close()
 
 
+@pytest.fixture(scope="module")
+def more(ctx):
+    from omega_h_gb300.mesh import Context
+    cs = [Context(0), Context(0)]
+    yield cs
+    for c in cs:
+        c.close()
+
+
 def _mesh(ctx, dim, n, kind, seed):
     from omega_h_gb300.mesh import Mesh
     m = Mesh.build_box(ctx, dim, n)
@@ -50,10 +59,10 @@ def _arrays(m):
     return {k: m.get(k).cpu().numpy() for k in names}
 
 
-@pytest.mark.parametrize("two_contexts", [False, True], ids=["one_ctx", "two_ctx"])
+@pytest.mark.parametrize("slots", [1, 2, 4], ids=["one_ctx", "two_ctx", "four_ctx"])
 @pytest.mark.parametrize("budget", [150e9, 3e7], ids=["roomy", "tight"])
-def test_served_results_equal_results_alone(ctx, ctx2, budget, two_contexts):
-    from omega_h_gb300.serve import Request, serve, summary
+def test_served_results_equal_results_alone(ctx, ctx2, more, budget, slots):
+    from omega_h_gb300.serve import Request, route, serve, summary
     alone = []
     for dim, n, kind, seed, passes, _ in STREAM:
         m = _mesh(ctx, dim, n, kind, seed)
@@ -61,9 +70,15 @@ def test_served_results_equal_results_alone(ctx, ctx2, budget, two_contexts):
             m.adapt_pass()
         alone.append(_arrays(m))
         m.close()
-    ctxs = {2: ctx2 if two_contexts else ctx, 3: ctx}
-    reqs = [Request(rid=i, arrival=a, mesh=_mesh(ctxs[d], d, n, k, s), passes=p)
+    # slots per dimension: one context for both, one each, or two each
+    per_dim = {1: {2: [ctx], 3: [ctx]}, 2: {2: [ctx2], 3: [ctx]},
+               4: {2: [ctx2, more[0]], 3: [ctx, more[1]]}}[slots]
+    dims = [d for d, *_ in STREAM]
+    work = [(2 * n * n if d == 2 else 6 * n ** 3) * p for d, n, _, _, p, _ in STREAM]
+    where = route(dims, work, {d: len(c) for d, c in per_dim.items()})
+    reqs = [Request(rid=i, arrival=a, mesh=_mesh(per_dim[d][where[i]], d, n, k, s), passes=p)
             for i, (d, n, k, s, p, a) in enumerate(STREAM)]
+    ctxs = {d: c[0] for d, c in per_dim.items()}
     out = serve(ctxs, reqs, budget_bytes=budget)
     assert all(r.done >= r.admitted >= r.arrival - 1e-9 and r.passes_done == r.passes for r in out)
     for r in out:
