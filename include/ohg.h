@@ -138,6 +138,20 @@ int ohg_mesh_clone(ohg_mesh* mesh, ohg_mesh** out);
  * reference): the source context's stream is waited on, then the copies run
  * on the target context's stream */
 int ohg_mesh_clone_to(ohg_mesh* src, ohg_context* ctx, ohg_mesh** out);
+/* .osh files, the reference's binary mesh format, one part (binary::write
+ * and binary::read, src/Omega_h_file.cpp:355-450 and :488-505): path is the
+ * directory holding 0.osh, nparts and version.  The writer gives the bytes
+ * the reference writes for the same mesh state: tags in the reference's
+ * order, its partitioning flag, the box's class sets; compress = 1 writes
+ * zlib streams (the system's libz, loaded at run time; ohg_osh_zlib tells
+ * whether it was found).  The reader takes versions 1-9; tags other than
+ * coordinates, metric, class_id, class_dim, global, length and quality are
+ * kept as they are and written back, until an operator rebuilds the mesh.
+ * Meshes of several parts, non-simplex families and parent links are
+ * refused with OHG_ERR_INVALID. */
+int ohg_mesh_write_osh(ohg_mesh* mesh, const char* path, int compress);
+int ohg_mesh_read_osh(ohg_context* ctx, const char* path, ohg_mesh** out);
+int ohg_osh_zlib(int* available);
 int ohg_mesh_destroy(ohg_mesh* mesh);
 int ohg_mesh_dim(ohg_mesh* mesh, int* out);
 int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);

@@ -64,6 +64,9 @@ SIGNATURES = {
                              P(c_void_p), c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_clone": [c_void_p, P(c_void_p)],
     "ohg_mesh_clone_to": [c_void_p, c_void_p, P(c_void_p)],
+    "ohg_mesh_write_osh": [c_void_p, c_char_p, c_int],
+    "ohg_mesh_read_osh": [c_void_p, c_char_p, P(c_void_p)],
+    "ohg_osh_zlib": [P(c_int)],
     "ohg_mesh_apply_workload": [c_void_p, c_int, c_ull, c_int],
     "ohg_mesh_from_elems": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_destroy": [c_void_p],

@@ -16,7 +16,8 @@ LIB = os.path.join(HERE, "libohg.so")
 # bounds-checked variant: every device array subscript is checked and each
 # launch is followed by a synchronising check that names its source line
 LIB_CHECKED = os.path.join(HERE, "libohg_checked.so")
-SOURCES = ["ohg_prims.cu", "ohg_mesh.cu", "ohg_adapt.cu", "ohg_batch.cu", "ohg_capi.cu"]
+SOURCES = ["ohg_prims.cu", "ohg_mesh.cu", "ohg_adapt.cu", "ohg_batch.cu", "ohg_osh.cu",
+           "ohg_capi.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "--extended-lambda", "-fmad=false", "-lineinfo",
@@ -52,7 +53,7 @@ def build(force=False, verbose=False, checked=False):
     with concurrent.futures.ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, checked), SOURCES))
     tmp = lib + ".tmp"
-    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

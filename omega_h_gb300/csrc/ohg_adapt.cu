@@ -728,6 +728,7 @@ static void inherit_refine(Mesh& m, int d, const Arr<LO>& k2e, const Arr<LO>& k2
 }
 
 static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* st) {
+  m.parting = 1;  // ghosted (src/Omega_h_refine.cpp:85)
   int dim = m.dim, mc = m.mcomp();
   LO nc = c2e.size();
   Arr<double> mid(nc * mc);
@@ -759,6 +760,8 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* s
   st->refine_keys = nkeys;
   Mesh nm;
   nm.dim = dim;
+  nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.class_sets = m.class_sets;
   Arr<LO> k2mid, ov2nv, old_lows2new;
   for (int d = 0; d <= dim; ++d) {
     Arr<LO> k2p, pv2v;
@@ -1727,6 +1730,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   check_collapse_class(m, c2e.data(), c2e.size(), codes0.data(), codes.data());
   filter_cands(c2e, codes, nullptr);
   if (c2e.size() == 0) return false;
+  m.parting = 1;  // ghosted once candidates pass the class check (src/Omega_h_coarsen.cpp:159-164)
   Arr<I8> codes2(c2e.size());
   check_collapse_exposure(m, c2e.data(), c2e.size(), codes.data(), codes2.data());
   codes = codes2;
@@ -1856,6 +1860,8 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   // coarsen_element_based2 (src/Omega_h_coarsen.cpp:106-156)
   Mesh nm;
   nm.dim = dim;
+  nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.class_sets = m.class_sets;
   Arr<LO> ov2nv, old_lows2new;
   for (int d = 0; d <= dim; ++d) {
     Arr<LO> k2p, pv2v, kd2d;
@@ -1937,6 +1943,7 @@ bool coarsen_by_size(Mesh& m, const AdaptOpts& o, PassStats* st) {
 // coarsen_slivers (src/Omega_h_coarsen.cpp:210-220): vertices of the sliver
 // layers, overshoot up to max_length_allowed, local improvement required
 bool coarsen_slivers(Mesh& m, const AdaptOpts& o, PassStats* st) {
+  m.parting = 1;  // src/Omega_h_coarsen.cpp:212
   Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
   return coarsen_verts(m, o, mark_down(m, m.dim, VERT, ec), true, true, st);
 }
@@ -2475,6 +2482,8 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
   LO nkeys = k2e.size();
   Mesh nm;
   nm.dim = dim;
+  nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.class_sets = m.class_sets;
   nm.nents[0] = m.nverts();
   nm.coords = m.coords;
   nm.metric = m.metric;
@@ -2660,6 +2669,7 @@ static bool swap_edges_3d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2
 // swap_edges (src/Omega_h_swap.cpp:45-53) after swap_part1
 // (src/Omega_h_swap.cpp:14-27): interior edges of the sliver layers
 bool swap_edges(Mesh& m, const AdaptOpts& o, PassStats* st) {
+  m.parting = 1;  // swap_part1 (src/Omega_h_swap.cpp:15)
   int dim = m.dim;
   Arr<I8> ec = mark_sliver_layers(m, o.min_quality_desired, o.nsliver_layers);
   Arr<I8> edc = mark_down(m, dim, 1, ec);
@@ -2690,6 +2700,11 @@ AdaptResult adapt(Mesh& m, const AdaptOpts& o) {
   };
   if (meets_goals()) return r;
   r.did = true;
+  // element-based partitioning when adapt() returns (src/Omega_h_adapt.cpp:285)
+  struct ElemBasedOnExit {
+    Mesh& m;
+    ~ElemBasedOnExit() { m.parting = 0; }
+  } on_exit{m};
   constexpr int kMaxRounds = 1000;  // a guard; the reference's loops are unbounded
   bool any;
   do {
@@ -2735,11 +2750,16 @@ PassStats adapt_pass(Mesh& m, const AdaptOpts& o) {
   OHG_CUDA(cudaEventCreate(&e1));
   OHG_CUDA(cudaEventCreate(&e2));
   OHG_CUDA(cudaEventCreate(&e3));
+  // each operator of the pass runs on a ghosted mesh (partitioning state
+  // only: one part has no ghosts to exchange)
   OHG_CUDA(cudaEventRecord(e0, c.stream));
+  m.parting = 1;
   st.did_refine = refine_by_size(m, o, &st);
   OHG_CUDA(cudaEventRecord(e1, c.stream));
+  m.parting = 1;
   st.did_coarsen = coarsen_by_size(m, o, &st);
   OHG_CUDA(cudaEventRecord(e2, c.stream));
+  m.parting = 1;
   st.min_quality = min_f64(m.ask_qualities());
   if (st.min_quality < o.min_quality_desired) st.did_swap = swap_edges(m, o, &st);
   OHG_CUDA(cudaEventRecord(e3, c.stream));

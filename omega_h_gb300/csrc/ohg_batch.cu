@@ -137,6 +137,9 @@ Mesh concat_meshes(const std::vector<Mesh*>& ms) {
     u.quality = concat_arrays(qs, 1, nullptr);
     u.has_quality = true;
   }
+  u.parting = ms[0]->parting;
+  u.rebuilt = ms[0]->rebuilt;
+  u.class_sets = ms[0]->class_sets;
   return u;
 }
 
@@ -208,6 +211,9 @@ std::vector<Mesh> split_mesh(Mesh& u, int K) {
   std::vector<Mesh> out(K);
   for (int k = 0; k < K; ++k) {
     Mesh& m = out[k];
+    m.parting = u.parting;
+    m.rebuilt = u.rebuilt;
+    m.class_sets = u.class_sets;
     m.dim = dim;
     LO v0 = start[0][k], nv = start[0][k + 1] - v0;
     m.coords = slice(u.coords, v0 * dim, nv * dim);

@@ -271,6 +271,13 @@ static void clone_mesh(const Mesh& a, Mesh& b) {
   }
   b.coords = copy_arr(a.coords);
   b.metric = copy_arr(a.metric);
+  // the state written to .osh files (lengths and qualities are not copied:
+  // a clone measures them afresh)
+  b.parting = a.parting;
+  b.rebuilt = a.rebuilt;
+  b.class_sets = a.class_sets;
+  for (const Mesh::Tag& t : a.extra_tags) b.extra_tags.push_back({t.dim, t.ncomps, t.type, t.name, copy_arr(t.bytes)});
+  for (int d = 0; d < 4; ++d) b.tag_order[d] = a.tag_order[d];
 }
 
 int ohg_mesh_clone(ohg_mesh* src, ohg_mesh** out) {
@@ -302,6 +309,36 @@ int ohg_mesh_clone_to(ohg_mesh* src, ohg_context* c, ohg_mesh** out) {
     return rc;
   }
   *out = m;
+  return OHG_OK;
+}
+
+int ohg_mesh_write_osh(ohg_mesh* m, const char* path, int compress) {
+  MESH_GUARD(m);
+  if (!path) {
+    g_err = "ohg_mesh_write_osh: null path";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(m->owner, [&] { write_osh(m->mesh, path, compress != 0); });
+}
+
+int ohg_mesh_read_osh(ohg_context* c, const char* path, ohg_mesh** out) {
+  if (!c || !path || !out) {
+    g_err = "ohg_mesh_read_osh: null argument";
+    return OHG_ERR_INVALID;
+  }
+  ohg_mesh* m = new ohg_mesh{c, Mesh()};
+  int rc = guarded(c, [&] { m->mesh = read_osh(path); });
+  if (rc != OHG_OK) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return OHG_OK;
+}
+
+int ohg_osh_zlib(int* available) {
+  if (!available) return OHG_ERR_INVALID;
+  *available = zlib_available() ? 1 : 0;
   return OHG_OK;
 }
 

@@ -692,6 +692,16 @@ Mesh build_box(int dim, int n) {
   m.coords = coords;
   reorder_by_hilbert(m);
   classify_box(m, n);
+  // named sets of the box's model entities (get_box_class_sets,
+  // src/Omega_h_box.cpp:162-185): the faces (3D) or sides (2D) and the body,
+  // by model dimension and id
+  if (dim == 3) {
+    m.class_sets = {{"z-", {{2, 4}}},  {"y-", {{2, 10}}}, {"x-", {{2, 12}}}, {"body", {{3, 13}}},
+                    {"x+", {{2, 14}}}, {"y+", {{2, 16}}}, {"z+", {{2, 22}}}};
+  } else {
+    m.class_sets = {{"y-", {{1, 1}}}, {"x-", {{1, 3}}}, {"body", {{2, 4}}}, {"x+", {{1, 5}}},
+                    {"y+", {{1, 7}}}};
+  }
   return m;
 }
 

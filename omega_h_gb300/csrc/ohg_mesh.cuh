@@ -28,6 +28,21 @@ struct Mesh {
   bool has_length = false, has_quality = false;
   Arr<double> length, quality;
   std::map<std::pair<int, int>, Adj> adj;
+  // state the reference writes to .osh files: its partitioning mode (0
+  // element-based, 1 ghosted: set by the operators as the reference's are),
+  // whether the tags are in the order a rebuild leaves them, the named sets
+  // of geometric model entities, tags this library does not model (kept
+  // until the next rebuild), and the tag order of a file that was read
+  int parting = 0;
+  bool rebuilt = false;
+  std::map<std::string, std::vector<std::pair<int, int>>> class_sets;
+  struct Tag {
+    int dim, ncomps, type;
+    std::string name;
+    Arr<I8> bytes;
+  };
+  std::vector<Tag> extra_tags;
+  std::vector<std::string> tag_order[4];
 
   int mcomp() const { return dim == 3 ? 6 : 3; }
   LO nverts() const { return nents[0]; }
@@ -57,6 +72,12 @@ Arr<LO> hilbert_sort(const Arr<double>& coords, LO n, int dim);
 void reorder_by_hilbert(Mesh& m);
 void classify_box(Mesh& m, int n);
 void apply_workload(Mesh& m, int n, std::uint64_t seed, int metric_kind);
+
+// .osh files (src/Omega_h_file.cpp): the mesh to/from one part of the
+// reference's binary format
+void write_osh(Mesh& m, const std::string& dir, bool compress);
+Mesh read_osh(const std::string& dir);
+bool zlib_available();
 
 // measurement kernels
 void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out);

@@ -124,6 +124,17 @@ class Mesh:
                   _ptr(ev2v), _ptr(coords), _ptr(metric), ctypes.byref(h))
         return cls(ctx, h)
 
+    @classmethod
+    def read_osh(cls, ctx, path):
+        """A mesh from an .osh directory (the reference's binary format)."""
+        h = ctypes.c_void_p()
+        _lib.call("ohg_mesh_read_osh", ctx.handle, str(path).encode(), ctypes.byref(h))
+        return cls(ctx, h)
+
+    def write_osh(self, path, compress=False):
+        """Write the mesh as an .osh directory, as the reference would."""
+        _lib.call("ohg_mesh_write_osh", self.handle, str(path).encode(), 1 if compress else 0)
+
     def apply_workload(self, n, seed, metric_kind):
         _lib.call("ohg_mesh_apply_workload", self.handle, n, seed, metric_kind)
 

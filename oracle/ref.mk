@@ -28,7 +28,7 @@ SRC_NAMES := adapt adj align amr amr_topology amr_transfer any approach array \
   regex regress remotes reorder scatterplot shape shared_alloc simplify sort \
   stacktrace surface swap swap2d swap2d_qualities swap2d_topology swap3d \
   swap3d_qualities swap3d_topology tag timer transfer unmap_mesh vector vtk \
-  xml xml_lite yaml random coarsen_flip overlay
+  xml xml_lite yaml random coarsen_flip overlay gmsh
 
 OBJS := $(patsubst %,$(OUT)/obj/Omega_h_%.o,$(SRC_NAMES))
 

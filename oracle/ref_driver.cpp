@@ -351,6 +351,11 @@ int main(int argc, char** argv) {
     dump("in_hilbert_perm", hilbert::sort_coords(mesh.coords(), dim));
     if (dim == 3) dump_swap_tables();
   }
+  // "osh": the mesh before and after one pass in the reference's own binary
+  // format (binary::write, src/Omega_h_file.cpp:355-396), for the .osh
+  // reader/writer parity tests
+  bool osh = mode == "osh";
+  if (osh) binary::write(filesystem::path(g_out + "/in.osh"), &mesh);
   if (mode == "adapt") {
     // the full Omega_h::adapt() instead of one pass; the counts of operator
     // calls are not observable from outside adapt(), so only the outcome and
@@ -360,6 +365,8 @@ int main(int argc, char** argv) {
     double t_ad = seconds_since(ta);
     dump("adapt_did", LOs({int(did)}));
     dump_mesh(&mesh, "out_");
+    if (argc > 8 && std::string(argv[8]) == "osh")
+      binary::write(filesystem::path(g_out + "/out.osh"), &mesh);
     std::fclose(g_manifest);
     std::printf("build %.4f adapt %.4f elems_out %d\n", t_build, t_ad, int(mesh.nelems()));
     return 0;
@@ -389,6 +396,7 @@ int main(int argc, char** argv) {
   }
   dump("pass_flags", LOs({did_refine, did_coarsen, did_swap}));
   dump_mesh(&mesh, "out_");
+  if (osh) binary::write(filesystem::path(g_out + "/out.osh"), &mesh);
   std::fclose(g_manifest);
   std::printf(
       "build %.4f refine %.4f coarsen %.4f swap %.4f pass %.4f "

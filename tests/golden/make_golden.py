@@ -7,7 +7,10 @@ its own sources by ``oracle/ref.mk``) on seeded box workloads and stores
   after each operator of one adapt pass (small cases);
 * ``<case>_digest.json``: sha256 digests of every integer array and
   sum/min/max/strided samples of every real array (full-size cases, whose raw
-  arrays are too large to commit).
+  arrays are too large to commit);
+* ``osh/<case>/{in,out}.osh/``: the mesh before and after one pass, written
+  by the reference's own binary::write (its .osh format), with the mesh
+  arrays after the pass in ``osh/<case>/out_arrays.npz``.
 
 On one rank the reference's global numbers are always 0..n-1 (checked here),
 so ``global_*`` arrays are dropped from the fixtures.
@@ -55,6 +58,40 @@ CASES = {
     "sq32_shock_adapt": (2, 32, 1, 5, 0.3, True, "adapt"),
     "sq32_blayer_adapt": (2, 32, 2, 5, 0.3, True, "adapt"),
 }
+
+
+# .osh fixtures: (dim, n, metric kind, seed, min_quality_allowed)
+OSH_CASES = {
+    "box4_shock": (3, 4, 1, 7, 0.2),     # refine only: ghosted parting
+    "box4_blayer": (3, 4, 2, 1, 0.2),    # refine and swap: element-based parting
+    "sq8_blayer": (2, 8, 2, 3, 0.2),     # 2D refine and swap
+}
+
+
+def run_osh_case(name, spec):
+    import shutil
+    dim, n, kind, seed, mqa = spec
+    dst = os.path.join(HERE, "osh", name)
+    if os.path.isdir(dst):
+        shutil.rmtree(dst)
+    os.makedirs(dst)
+    with tempfile.TemporaryDirectory() as tmp:
+        args = [os.path.join(ROOT, "oracle/_ref/ref_driver"), str(dim), str(n),
+                str(kind), str(seed), str(mqa), tmp, "osh"]
+        out = subprocess.run(args, check=True, capture_output=True, text=True)
+        for part in ("in.osh", "out.osh"):
+            shutil.copytree(os.path.join(tmp, part), os.path.join(dst, part))
+        arrs = {}
+        with open(os.path.join(tmp, "manifest.txt")) as f:
+            for line in f:
+                key, dt, count = line.split()
+                if key.startswith("out_"):
+                    arrs[key] = np.fromfile(os.path.join(tmp, key + ".bin"), dtype=np.dtype(dt))
+    np.savez_compressed(os.path.join(dst, "out_arrays.npz"), **arrs)
+    with open(os.path.join(dst, "case.json"), "w") as f:
+        json.dump({"case": name, "dim": dim, "n": n, "metric": kind, "seed": seed,
+                   "min_quality_allowed": mqa, "driver_stdout": out.stdout.strip()}, f)
+    print(name, out.stdout.strip())
 
 
 def build_ref(ref):
@@ -118,8 +155,11 @@ def main():
     if not os.path.isdir(a.ref):
         sys.exit(f"reference sources not found at {a.ref}")
     build_ref(a.ref)
-    for name in a.cases or CASES:
-        run_case(name, CASES[name])
+    for name in a.cases or list(CASES) + list(OSH_CASES):
+        if name in OSH_CASES:
+            run_osh_case(name, OSH_CASES[name])
+        else:
+            run_case(name, CASES[name])
 
 
 if __name__ == "__main__":
