@@ -296,6 +296,64 @@ int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev
 int ohg_offset_scan_noalloc(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
 int ohg_offset_scan_noalloc_limit(int* max_counts);
 
+/* ---- metric tools (src/Omega_h_metric.cpp, src/Omega_h_metric_input.cpp)
+ * Metrics are packed symmetric tensors per vertex: (xx, yy, zz, yx, zy, zx)
+ * in 3D, (xx, yy, yx) in 2D; all pointers are device pointers.  Every
+ * function computes in FP64 with the reference's operation order.  A
+ * metric intersection whose less degenerate operand has an eigenvalue below
+ * 1e-10 (Barral's degenerate cases) and a failed eigendecomposition set the
+ * device status, returned as OHG_ERR_NUMERIC. */
+/* intersect_metrics (src/Omega_h_metric.cpp:536-557) */
+int ohg_intersect_metrics(ohg_context* ctx, int dim, int n, const double* a, const double* b,
+                          double* out);
+/* clamp_metrics (src/Omega_h_metric.cpp:36-56): eigenvalues into
+ * [1/h_max^2, 1/h_min^2] */
+int ohg_clamp_metrics(ohg_context* ctx, int dim, int n, const double* metrics, double h_min,
+                      double h_max, double* out);
+/* get_hessian_metrics (src/Omega_h_metric.cpp:332-368) */
+int ohg_hessian_metrics(ohg_context* ctx, int dim, int n, const double* hessians, double eps,
+                        double* out);
+/* get_implied_metrics (src/Omega_h_metric.cpp:304-309): out holds nverts
+ * metrics */
+int ohg_mesh_implied_metrics(ohg_mesh* mesh, double* out);
+/* limit_metric_gradation (src/Omega_h_metric.cpp:199-220); steps (may be
+ * null) receives the number of sweeps */
+int ohg_mesh_limit_metric_gradation(ohg_mesh* mesh, const double* metrics, double max_rate,
+                                    double tol, double* out, int* steps);
+/* get_expected_nelems (src/Omega_h_metric.cpp:516-519), summed exactly */
+int ohg_mesh_expected_nelems(ohg_mesh* mesh, const double* metrics, double* out);
+
+/* MetricSource / MetricInput (src/Omega_h_metric_input.cpp:13-35).  type:
+ * 0 constant (knob = length), 3 given (the metrics in `given`, scaled by
+ * 1/knob^2), 4 implied (scaled by 1/knob^2); variation (1), derivative (2)
+ * and curvature (5) are refused.  isotropy: 0 anisotropic, 2 iso-size
+ * (1, iso-length, is refused).  scales: 0 absolute, 1 scaled by the
+ * element-count iteration.  At least one source must stay anisotropic. */
+typedef struct ohg_metric_source {
+  int type;
+  double knob;
+  int isotropy;
+  int scales;
+  const double* given;
+} ohg_metric_source;
+typedef struct ohg_metric_input {
+  int nsources;
+  ohg_metric_source sources[8];
+  int should_limit_lengths;
+  double min_length, max_length;
+  int should_limit_gradation;
+  double max_gradation_rate, gradation_convergence_tolerance;
+  int should_limit_element_count;
+  double max_element_count, min_element_count, element_count_over_relaxation;
+  int nsmoothing_steps;
+} ohg_metric_input;
+/* MetricInput() defaults (src/Omega_h_metric_input.cpp:23-35), no sources */
+int ohg_metric_input_default(ohg_metric_input* out);
+/* generate_metrics (src/Omega_h_metric_input.cpp:140-275): out holds
+ * nverts metrics; niters (may be null) the element-count iterations */
+int ohg_mesh_generate_metrics(ohg_mesh* mesh, const ohg_metric_input* in, double* out,
+                              int* niters);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,23 @@ class AdaptResult(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MetricSource(ctypes.Structure):
+    """ohg_metric_source (MetricSource, src/Omega_h_metric_input.cpp:13-20)."""
+    _fields_ = [("type", c_int), ("knob", c_double), ("isotropy", c_int), ("scales", c_int),
+                ("given", c_void_p)]
+
+
+class MetricInput(ctypes.Structure):
+    """ohg_metric_input (MetricInput, src/Omega_h_metric_input.cpp:23-35)."""
+    _fields_ = [("nsources", c_int), ("sources", MetricSource * 8),
+                ("should_limit_lengths", c_int), ("min_length", c_double),
+                ("max_length", c_double), ("should_limit_gradation", c_int),
+                ("max_gradation_rate", c_double), ("gradation_convergence_tolerance", c_double),
+                ("should_limit_element_count", c_int), ("max_element_count", c_double),
+                ("min_element_count", c_double), ("element_count_over_relaxation", c_double),
+                ("nsmoothing_steps", c_int)]
+
+
 class PassStats(ctypes.Structure):
     _fields_ = [("did_refine", c_int), ("did_coarsen", c_int), ("did_swap", c_int),
                 ("nelems_in", c_int), ("nelems_out", c_int), ("refine_keys", c_int),
@@ -67,6 +84,14 @@ SIGNATURES = {
     "ohg_mesh_write_osh": [c_void_p, c_char_p, c_int],
     "ohg_mesh_read_osh": [c_void_p, c_char_p, P(c_void_p)],
     "ohg_osh_zlib": [P(c_int)],
+    "ohg_intersect_metrics": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p],
+    "ohg_clamp_metrics": [c_void_p, c_int, c_int, c_void_p, c_double, c_double, c_void_p],
+    "ohg_hessian_metrics": [c_void_p, c_int, c_int, c_void_p, c_double, c_void_p],
+    "ohg_mesh_implied_metrics": [c_void_p, c_void_p],
+    "ohg_mesh_limit_metric_gradation": [c_void_p, c_void_p, c_double, c_double, c_void_p, P(c_int)],
+    "ohg_mesh_expected_nelems": [c_void_p, c_void_p, P(c_double)],
+    "ohg_metric_input_default": [P(MetricInput)],
+    "ohg_mesh_generate_metrics": [c_void_p, P(MetricInput), c_void_p, P(c_int)],
     "ohg_mesh_apply_workload": [c_void_p, c_int, c_ull, c_int],
     "ohg_mesh_from_elems": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, P(c_void_p)],
     "ohg_mesh_destroy": [c_void_p],

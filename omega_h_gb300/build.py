@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libohg.so")
 # launch is followed by a synchronising check that names its source line
 LIB_CHECKED = os.path.join(HERE, "libohg_checked.so")
 SOURCES = ["ohg_prims.cu", "ohg_mesh.cu", "ohg_adapt.cu", "ohg_batch.cu", "ohg_osh.cu",
-           "ohg_capi.cu"]
+           "ohg_metric.cu", "ohg_capi.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "--extended-lambda", "-fmad=false", "-lineinfo",

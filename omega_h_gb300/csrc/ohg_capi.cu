@@ -4,6 +4,7 @@
 #include <string>
 
 #include "../../include/ohg.h"
+#include "ohg_metric.cuh"
 #include "ohg_adapt.cuh"
 #include "ohg_batch.cuh"
 
@@ -927,6 +928,110 @@ int ohg_offset_scan_noalloc_limit(int* out) {
   }
   *out = offset_scan_fixed_limit();
   return OHG_OK;
+}
+
+
+// ------------------------------------------------------------ metric tools
+static bool metric_args(int dim, int n) {
+  if ((dim != 2 && dim != 3) || n < 0) {
+    g_err = "metric tools: dim must be 2 or 3 and n >= 0";
+    return false;
+  }
+  return true;
+}
+int ohg_intersect_metrics(ohg_context* c, int dim, int n, const double* a, const double* b,
+                          double* out) {
+  if (!metric_args(dim, n)) return OHG_ERR_INVALID;
+  return guarded(c, [&] { intersect_metrics(dim, n, a, b, out); });
+}
+int ohg_clamp_metrics(ohg_context* c, int dim, int n, const double* m, double h_min, double h_max,
+                      double* out) {
+  if (!metric_args(dim, n)) return OHG_ERR_INVALID;
+  if (!(h_min > 0.0) || !(h_min <= h_max)) {
+    g_err = "ohg_clamp_metrics: need 0 < h_min <= h_max";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] { clamp_metrics(dim, n, m, h_min, h_max, out); });
+}
+int ohg_hessian_metrics(ohg_context* c, int dim, int n, const double* h, double eps, double* out) {
+  if (!metric_args(dim, n) || !(eps > 0.0)) {
+    g_err = "ohg_hessian_metrics: dim 2 or 3 and eps > 0";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] { hessian_metrics(dim, n, h, eps, out); });
+}
+int ohg_mesh_implied_metrics(ohg_mesh* m, double* out) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] {
+    Arr<double> r = implied_metrics(m->mesh);
+    OHG_CUDA(cudaMemcpyAsync(out, r.data(), sizeof(double) * size_t(r.size()),
+                             cudaMemcpyDeviceToDevice, ctx().stream));
+  });
+}
+int ohg_mesh_limit_metric_gradation(ohg_mesh* m, const double* metrics, double max_rate, double tol,
+                                    double* out, int* steps) {
+  MESH_GUARD(m);
+  return guarded(m->owner, [&] {
+    Mesh& me = m->mesh;
+    LO n = me.nverts() * me.mcomp();
+    Arr<double> in(n);
+    OHG_CUDA(cudaMemcpyAsync(in.data(), metrics, sizeof(double) * size_t(n),
+                             cudaMemcpyDeviceToDevice, ctx().stream));
+    Arr<double> r = limit_metric_gradation(me, in, max_rate, tol, steps);
+    OHG_CUDA(cudaMemcpyAsync(out, r.data(), sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice,
+                             ctx().stream));
+  });
+}
+int ohg_mesh_expected_nelems(ohg_mesh* m, const double* metrics, double* out) {
+  MESH_GUARD(m);
+  if (!out) return OHG_ERR_INVALID;
+  return guarded(m->owner, [&] { *out = expected_nelems(m->mesh, metrics); });
+}
+int ohg_metric_input_default(ohg_metric_input* o) {
+  if (!o) return OHG_ERR_INVALID;
+  MetricInput d;
+  *o = ohg_metric_input{};
+  o->nsources = 0;
+  o->should_limit_lengths = d.limit_lengths;
+  o->min_length = d.min_length;
+  o->max_length = d.max_length;
+  o->should_limit_gradation = d.limit_gradation;
+  o->max_gradation_rate = d.max_gradation_rate;
+  o->gradation_convergence_tolerance = d.gradation_tol;
+  o->should_limit_element_count = d.limit_element_count;
+  o->max_element_count = d.max_element_count;
+  o->min_element_count = d.min_element_count;
+  o->element_count_over_relaxation = d.element_count_over_relaxation;
+  o->nsmoothing_steps = d.nsmoothing_steps;
+  return OHG_OK;
+}
+int ohg_mesh_generate_metrics(ohg_mesh* m, const ohg_metric_input* in, double* out, int* niters) {
+  MESH_GUARD(m);
+  if (!in || !out || in->nsources < 0 || in->nsources > 8) {
+    g_err = "ohg_mesh_generate_metrics: null input or output, or more than 8 sources";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(m->owner, [&] {
+    MetricInput mi;
+    for (int i = 0; i < in->nsources; ++i) {
+      const ohg_metric_source& s = in->sources[i];
+      mi.sources.push_back({s.type, s.knob, s.isotropy, s.scales, s.given});
+    }
+    mi.limit_lengths = in->should_limit_lengths != 0;
+    mi.min_length = in->min_length;
+    mi.max_length = in->max_length;
+    mi.limit_gradation = in->should_limit_gradation != 0;
+    mi.max_gradation_rate = in->max_gradation_rate;
+    mi.gradation_tol = in->gradation_convergence_tolerance;
+    mi.limit_element_count = in->should_limit_element_count != 0;
+    mi.max_element_count = in->max_element_count;
+    mi.min_element_count = in->min_element_count;
+    mi.element_count_over_relaxation = in->element_count_over_relaxation;
+    mi.nsmoothing_steps = in->nsmoothing_steps;
+    Arr<double> r = generate_metrics(m->mesh, mi, niters);
+    OHG_CUDA(cudaMemcpyAsync(out, r.data(), sizeof(double) * size_t(r.size()),
+                             cudaMemcpyDeviceToDevice, ctx().stream));
+  });
 }
 
 }  // extern "C"

@@ -282,6 +282,60 @@ class Mesh:
                   ctypes.byref(r))
         return out, r.value
 
+    # ---- metric tools ---------------------------------------------------
+    def _metric_out(self):
+        return torch.empty(self.nents(0) * (6 if self.dim == 3 else 3), dtype=torch.float64,
+                           device=self._dev())
+
+    def implied_metrics(self):
+        """get_implied_metrics: the metric the current elements imply."""
+        out = self._metric_out()
+        _lib.call("ohg_mesh_implied_metrics", self.handle, _ptr(out))
+        return out
+
+    def limit_metric_gradation(self, metrics, max_rate=1.0, tol=1e-3):
+        """limit_metric_gradation; returns (metrics, sweeps)."""
+        out = self._metric_out()
+        steps = ctypes.c_int()
+        _lib.call("ohg_mesh_limit_metric_gradation", self.handle, _ptr(metrics.contiguous()),
+                  max_rate, tol, _ptr(out), ctypes.byref(steps))
+        return out, steps.value
+
+    def expected_nelems(self, metrics):
+        v = ctypes.c_double()
+        _lib.call("ohg_mesh_expected_nelems", self.handle, _ptr(metrics.contiguous()),
+                  ctypes.byref(v))
+        return v.value
+
+    def generate_metrics(self, sources, **opts):
+        """generate_metrics.  sources: dicts with type ("constant", "given",
+        "implied"), knob, isotropy ("anisotropic", "iso_size"), scales
+        (bool) and, for "given", metrics (a device tensor).  opts: the
+        MetricInput fields.  Returns (metrics, element-count iterations)."""
+        types = {"constant": 0, "given": 3, "implied": 4}
+        isos = {"anisotropic": 0, "iso_length": 1, "iso_size": 2}
+        mi = _lib.MetricInput()
+        _lib.call("ohg_metric_input_default", ctypes.byref(mi))
+        keep = []
+        for i, s in enumerate(sources):
+            src = mi.sources[i]
+            src.type = types[s["type"]]
+            src.knob = s.get("knob", 1.0)
+            src.isotropy = isos[s.get("isotropy", "anisotropic")]
+            src.scales = 1 if s.get("scales", True) else 0
+            if "metrics" in s:
+                t = s["metrics"].contiguous()
+                keep.append(t)
+                src.given = t.data_ptr()
+        mi.nsources = len(sources)
+        for k, v in opts.items():
+            setattr(mi, k, v)
+        out = self._metric_out()
+        nit = ctypes.c_int()
+        _lib.call("ohg_mesh_generate_metrics", self.handle, ctypes.byref(mi), _ptr(out),
+                  ctypes.byref(nit))
+        return out, nit.value
+
     def close(self):
         if self.handle:
             _lib.call("ohg_mesh_destroy", self.handle)
@@ -311,6 +365,28 @@ def split(union, n):
     outs = (ctypes.c_void_p * n)()
     _lib.call("ohg_mesh_split", union.handle, n, outs)
     return [Mesh(union.ctx, ctypes.c_void_p(outs[i])) for i in range(n)]
+
+
+def intersect_metrics(ctx, dim, a, b):
+    """intersect_metrics over packed metric tensors (device tensors)."""
+    out = torch.empty_like(a)
+    _lib.call("ohg_intersect_metrics", ctx.handle, dim, a.numel() // (6 if dim == 3 else 3),
+              _ptr(a.contiguous()), _ptr(b.contiguous()), _ptr(out))
+    return out
+
+
+def clamp_metrics(ctx, dim, m, h_min, h_max):
+    out = torch.empty_like(m)
+    _lib.call("ohg_clamp_metrics", ctx.handle, dim, m.numel() // (6 if dim == 3 else 3),
+              _ptr(m.contiguous()), h_min, h_max, _ptr(out))
+    return out
+
+
+def hessian_metrics(ctx, dim, hessians, eps):
+    out = torch.empty_like(hessians)
+    _lib.call("ohg_hessian_metrics", ctx.handle, dim, hessians.numel() // (6 if dim == 3 else 3),
+              _ptr(hessians.contiguous()), eps, _ptr(out))
+    return out
 
 
 def adapt_pass_batch(ctx, meshes, opts=None):

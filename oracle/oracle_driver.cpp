@@ -91,7 +91,7 @@ static void dump_refine_stage(Mesh& m, const AdaptOpts& o) {
   const V<double>& len = m.ask_lengths();
   V<I8> cands(len.size());
   bool any = false;
-  for (size_t i = 0; i < len.size(); ++i) any |= bool(cands[i] = len[i] > o.max_length_desired);
+  for (size_t i = 0; i < len.size(); ++i) any |= bool((cands[i] = len[i] > o.max_length_desired));
   dump("r_cands", cands);
   if (!any) return;
   V<LO> c2e = collect_marked(cands);
@@ -118,7 +118,7 @@ static void dump_coarsen_stage(Mesh& m, const AdaptOpts& o) {
   const V<double>& len = m.ask_lengths();
   V<I8> ec(len.size());
   bool any = false;
-  for (size_t i = 0; i < len.size(); ++i) any |= bool(ec[i] = len[i] < o.min_length_desired);
+  for (size_t i = 0; i < len.size(); ++i) any |= bool((ec[i] = len[i] < o.min_length_desired));
   dump("c_edge_is_cand", ec);
   if (!any) return;
   // mark_down(EDGE -> VERT)

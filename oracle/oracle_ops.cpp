@@ -286,7 +286,7 @@ static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& m
 // ------------------------------------------------------------ refine
 // refine_qualities_tmpl (src/Omega_h_refine_qualities.cpp:34-86)
 V<double> refine_qualities(Mesh& m, const V<LO>& c2e) {
-  int dim = m.dim, mc = m.mcomp();
+  int dim = m.dim;
   const V<LO>& ev2v = m.ask_verts_of(1);
   const V<LO>& cv2v = m.ask_verts_of(dim);
   const Adj& e2c = m.ask_up(1, dim);

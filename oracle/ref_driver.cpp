@@ -36,6 +36,7 @@
 #include <Omega_h_timer.hpp>
 
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -295,6 +296,60 @@ static void dump_swap_tables() {
   dump("swap3d_tables", Read<I32>(h.write()));
 }
 
+// A smooth scalar field's Hessian at each vertex, packed like a metric:
+// f = sin(4x) cos(3y) (+ z^2 in 3D).  The same numbers feed the GPU side
+// through the dump.
+static Reals analytic_hessians(Mesh* mesh) {
+  int dim = mesh->dim();
+  int nc = dim == 3 ? 6 : 3;
+  HostRead<Real> c(mesh->coords());
+  HostWrite<Real> h(mesh->nverts() * nc);
+  for (LO v = 0; v < mesh->nverts(); ++v) {
+    double x = c[v * dim], y = c[v * dim + 1];
+    double sx = std::sin(4 * x), cx = std::cos(4 * x), sy = std::sin(3 * y), cy = std::cos(3 * y);
+    double fxx = -16 * sx * cy, fyy = -9 * sx * cy, fxy = -12 * cx * sy;
+    if (dim == 3) {
+      double r[6] = {fxx, fyy, 2.0, fxy, 0.0, 0.0};
+      for (int k = 0; k < 6; ++k) h[v * 6 + k] = r[k];
+    } else {
+      double r[3] = {fxx, fyy, fxy};
+      for (int k = 0; k < 3; ++k) h[v * 3 + k] = r[k];
+    }
+  }
+  return Reals(h.write());
+}
+
+// "metric": the metric tools on the box after the workload
+static void dump_metric_tools(Mesh* mesh) {
+  auto n = mesh->nverts();
+  auto given = mesh->get_array<Real>(VERT, "metric");
+  dump("mt_given", given);
+  auto implied = get_implied_metrics(mesh);
+  dump("mt_implied", implied);
+  dump("mt_intersect", intersect_metrics(n, given, implied));
+  dump("mt_clamp", clamp_metrics(n, given, 0.02, 0.2));
+  auto hess = analytic_hessians(mesh);
+  dump("mt_hessians", hess);
+  dump("mt_hessian_metrics", get_hessian_metrics(mesh->dim(), hess, 0.01));
+  dump("mt_gradation", limit_metric_gradation(mesh, given, 1.0, 1e-3, false));
+  dump("mt_expected_nelems", Reals({get_expected_nelems(mesh, given)}));
+  MetricInput in;
+  in.verbose = false;
+  in.add_source(MetricSource(OMEGA_H_GIVEN, 1.0, "metric", OMEGA_H_ANISOTROPIC, OMEGA_H_SCALES));
+  in.add_source(MetricSource(OMEGA_H_IMPLIED, 2.0, "", OMEGA_H_ISO_SIZE, OMEGA_H_ABSOLUTE));
+  in.add_source(MetricSource(OMEGA_H_CONSTANT, 0.3, "", OMEGA_H_ANISOTROPIC, OMEGA_H_ABSOLUTE));
+  in.should_limit_lengths = true;
+  in.min_length = 0.05;
+  in.max_length = 0.5;
+  in.should_limit_gradation = true;
+  in.max_gradation_rate = 1.0;
+  in.nsmoothing_steps = 1;
+  in.should_limit_element_count = true;
+  in.max_element_count = 4.0 * mesh->nelems();
+  in.min_element_count = 1.0 * mesh->nelems();
+  dump("mt_generated", generate_metrics(mesh, in));
+}
+
 int main(int argc, char** argv) {
   if (argc < 7) {
     std::fprintf(stderr,
@@ -354,6 +409,12 @@ int main(int argc, char** argv) {
   // "osh": the mesh before and after one pass in the reference's own binary
   // format (binary::write, src/Omega_h_file.cpp:355-396), for the .osh
   // reader/writer parity tests
+  if (mode == "metric") {
+    dump_metric_tools(&mesh);
+    std::fclose(g_manifest);
+    std::printf("metric tools on %d verts\n", int(mesh.nverts()));
+    return 0;
+  }
   bool osh = mode == "osh";
   if (osh) binary::write(filesystem::path(g_out + "/in.osh"), &mesh);
   if (mode == "adapt") {

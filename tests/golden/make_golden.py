@@ -10,7 +10,10 @@ its own sources by ``oracle/ref.mk``) on seeded box workloads and stores
   arrays are too large to commit);
 * ``osh/<case>/{in,out}.osh/``: the mesh before and after one pass, written
   by the reference's own binary::write (its .osh format), with the mesh
-  arrays after the pass in ``osh/<case>/out_arrays.npz``.
+  arrays after the pass in ``osh/<case>/out_arrays.npz``;
+* ``metric/<case>.npz``: the metric tools' outputs on the box after the
+  workload (intersection, clamp, Hessian metrics, implied metrics,
+  gradation, expected element count, generate_metrics).
 
 On one rank the reference's global numbers are always 0..n-1 (checked here),
 so ``global_*`` arrays are dropped from the fixtures.
@@ -18,6 +21,8 @@ so ``global_*`` arrays are dropped from the fixtures.
 Usage (needs the reference sources, i.e. only in the build container)::
 
     python tests/golden/make_golden.py [--ref /path/to/omega_h] [case ...]
+
+(metric tool cases are named ``metric:<case>``)
 """
 import argparse
 import hashlib
@@ -66,6 +71,37 @@ OSH_CASES = {
     "box4_blayer": (3, 4, 2, 1, 0.2),    # refine and swap: element-based parting
     "sq8_blayer": (2, 8, 2, 3, 0.2),     # 2D refine and swap
 }
+
+
+# metric tool fixtures: (dim, n, metric kind, seed); the reference's
+# intersect, clamp, Hessian, implied, gradation, expected element count and
+# generate_metrics outputs on the box after the workload
+METRIC_CASES = {
+    "box4_shock": (3, 4, 1, 7),
+    "box6_iso": (3, 6, 0, 5),
+    "sq8_blayer": (2, 8, 2, 3),
+    "sq12_sine": (2, 12, 3, 4),
+}
+
+
+def run_metric_case(name, spec):
+    dim, n, kind, seed = spec
+    with tempfile.TemporaryDirectory() as tmp:
+        args = [os.path.join(ROOT, "oracle/_ref/ref_driver"), str(dim), str(n), str(kind),
+                str(seed), "0.2", tmp, "metric"]
+        out = subprocess.run(args, check=True, capture_output=True, text=True, timeout=600)
+        arrs = {}
+        with open(os.path.join(tmp, "manifest.txt")) as f:
+            for line in f:
+                key, dt, count = line.split()
+                if key.startswith("mt_"):
+                    arrs[key] = np.fromfile(os.path.join(tmp, key + ".bin"), dtype=np.dtype(dt))
+    meta = {"case": name, "dim": dim, "n": n, "metric": kind, "seed": seed,
+            "driver_stdout": out.stdout.strip()}
+    arrs["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    os.makedirs(os.path.join(HERE, "metric"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "metric", name + ".npz"), **arrs)
+    print(name, out.stdout.strip())
 
 
 def run_osh_case(name, spec):
@@ -155,8 +191,10 @@ def main():
     if not os.path.isdir(a.ref):
         sys.exit(f"reference sources not found at {a.ref}")
     build_ref(a.ref)
-    for name in a.cases or list(CASES) + list(OSH_CASES):
-        if name in OSH_CASES:
+    for name in a.cases or list(CASES) + list(OSH_CASES) + ["metric:" + k for k in METRIC_CASES]:
+        if name.startswith("metric:"):
+            run_metric_case(name[7:], METRIC_CASES[name[7:]])
+        elif name in OSH_CASES:
             run_osh_case(name, OSH_CASES[name])
         else:
             run_case(name, CASES[name])
