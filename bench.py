@@ -87,6 +87,7 @@ def _args():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the boundary-layer precision workloads")
+    ap.add_argument("--no-tools", action="store_true", help="skip the .osh and metric tools")
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch shapes at their defaults (no exploration passes)")
     ap.add_argument("--profile-pass", action="store_true",
@@ -263,6 +264,88 @@ def precision_report(ctx, lib_stream, flush, m_base, opts):
             "length_recheck_fraction": counts[3] / max(counts[2], 1),
             "max_error_vs_fp64": 0.0 if fp64_digest == scr_digest else None,
             "outputs_bitwise_equal_to_fp64": fp64_digest == scr_digest}
+
+
+def run_tools(ctx, lib_stream, flush, base):
+    """The tools beside the pass on the 64^3 shock mesh: one part of the
+    reference's .osh format written and read back (the device arrays to and
+    from the file), and the metric tools (implied metrics, an intersection,
+    gradation limiting of the implied metrics, the expected element count,
+    generate_metrics).  Each is timed once after one untimed run, with L2
+    flushed before it."""
+    import shutil
+    import tempfile
+    import torch
+    out = {}
+
+    def timed(fn):
+        fn()
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, r
+
+    from omega_h_gb300.mesh import Mesh, intersect_metrics
+
+    def osh_timing():
+        tmp = tempfile.mkdtemp(prefix="ohg_osh_")
+        holder = []
+        try:
+            path = os.path.join(tmp, "box64.osh")
+            ms_w, _ = timed(lambda: base.write_osh(path))
+            nbytes = os.path.getsize(os.path.join(path, "0.osh"))
+
+            def read():
+                if holder:
+                    holder.pop().close()
+                holder.append(Mesh.read_osh(ctx, path))
+            ms_r, _ = timed(read)
+            return {"file_bytes": nbytes, "write_ms": ms_w, "read_ms": ms_r,
+                    "write_gb_s": nbytes / ms_w / 1e6, "read_gb_s": nbytes / ms_r / 1e6,
+                    "note": "uncompressed, to the box's local disk; includes the device<->host "
+                            "copies of every array"}
+        except Exception as e:  # reported, not fatal to the bench line
+            return {"error": str(e)}
+        finally:
+            for h in holder:
+                h.close()
+            shutil.rmtree(tmp, ignore_errors=True)
+    out["osh"] = osh_timing()
+    # metric tools on a 64^3 box with the isotropic sine field: gradation's
+    # stopping test (every tensor entry within 1e-3 relative, floor 1e-10)
+    # settles on it, whereas on anisotropic metrics whose off-diagonal
+    # entries sit just above the floor it can keep seeing rounding noise
+    # (in the reference as here)
+    m = Mesh.build_box(ctx, 3, 64)
+    m.apply_workload(64, 5, 3)
+    try:
+        nv = m.nents(0)
+        metric = m.get("metric")
+        mt = {"workload": "box64_sine: 64^3 box, isotropic sine metric (seed 5)",
+              "vertices": nv, "elements": m.nelems()}
+        try:
+            ms_i, implied = timed(lambda: m.implied_metrics())
+            ms_x, _ = timed(lambda: intersect_metrics(ctx, 3, metric, implied))
+            mt.update({"implied_ms": ms_i, "intersect_ms": ms_x,
+                       "intersect_verts_per_s": nv / ms_x * 1e3})
+            ms_g, (_, sweeps) = timed(lambda: m.limit_metric_gradation(metric, 1.0, 1e-3))
+            mt.update({"gradation_ms": ms_g, "gradation_sweeps": sweeps,
+                       "gradation_vert_sweeps_per_s": nv * sweeps / ms_g * 1e3})
+            ms_n, ne = timed(lambda: m.expected_nelems(metric))
+            mt.update({"expected_nelems_ms": ms_n, "expected_nelems": ne})
+            ms_gen, (_, nit) = timed(lambda: m.generate_metrics(
+                [{"type": "given", "metrics": metric},
+                 {"type": "implied", "knob": 2.0, "isotropy": "iso_size", "scales": False}],
+                should_limit_gradation=1, max_gradation_rate=1.0))
+            mt.update({"generate_metrics_ms": ms_gen, "generate_metrics_iterations": nit})
+        except Exception as e:  # reported, not fatal to the bench line
+            mt["error"] = str(e)
+        out["metric_tools"] = mt
+    finally:
+        m.close()
+    return out
 
 
 def run_precision(ctx, lib_stream, flush):
@@ -494,6 +577,9 @@ def run_ours(args):
     batched = run_batch(ctx, lib_stream, flush, args) if rank == 0 and not args.no_batch else None
     served = run_serve(ctx, args) if rank == 0 and not args.no_serve else None
 
+    # ---- .osh and metric tools
+    tools = run_tools(ctx, lib_stream, flush, base) if rank == 0 and not args.no_tools else None
+
     # ---- precision mode: FP32 enclosures + FP64 recheck against FP64 throughout
     precision = precision_report(ctx, lib_stream, flush, base, opts)
     precision["workload"] = w["workload"]
@@ -596,6 +682,7 @@ def run_ours(args):
                 "precision": precision,
                 "batched": batched,
                 "served": served,
+                "tools": tools,
                 "cpu_baseline": cpu, "gpu_launches": gpu_launches,
                 "host_syncs_per_step": host_syncs / args.steps, "clocks": clk.summary(),
                 "autotune": {"passes": tune_passes, "sites": tuning[0], "chosen": tuning[1],

@@ -1134,7 +1134,7 @@ struct CoarsenScreenArgs {
 };
 
 template <int D>
-__global__ void __launch_bounds__(512) k_coarsen_screen(CoarsenScreenArgs a) {
+__global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) {
   constexpr int dim = D;
   WarpQueue q;
   int st = 0;  // 0: needs a direction, 1: screening one, 2: done
@@ -1348,12 +1348,12 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   Arr<unsigned long long> queue = fill<unsigned long long>(2, 0ULL);
   Arr<LO> amb_dir(ndirs);
   Arr<float> amb_mhi(ndirs);
-  // tuned launch shape: block 256 or 512 threads, queue chunk 64 or 32
-  // directions (the results do not depend on either)
+  // tuned launch shape: queue chunk 64 or 32 directions (the results do not
+  // depend on it); blocks of 256 threads
   Ctx& cx = ctx();
-  int var = cx.tuner.select("coarsen_screen", D, ndirs, 4, 0, cx.stream);
+  int var = cx.tuner.select("coarsen_screen", D, ndirs, 2, 0, cx.stream);
   bool timed = cx.tuner.open >= 0;
-  int block = (var & 1) ? 512 : 256, chunk = (var & 2) ? 32 : kQueueChunk;
+  int block = kBlock, chunk = (var & 1) ? 32 : kQueueChunk;
   CoarsenScreenArgs args{ndirs, chunk, sv, ev, cv, va, vb, vc, c2e, cview(codes_p, n), q2, mqa_f,
                          queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
   {

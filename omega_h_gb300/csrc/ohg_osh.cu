@@ -130,30 +130,31 @@ class In {
     p_ += size_t(n);
     return s;
   }
-  // one array's bytes (decompressed) and its item count
-  std::vector<char> array(int esize, bool compressed, LO* n_out) {
+  // one array's bytes and item count: a view into the file buffer, or the
+  // decompressed bytes (held in *owned)
+  const char* array(int esize, bool compressed, LO* n_out, std::vector<char>* owned) {
     LO n = val<LO>();
     if (n < 0) throw Error(1, ".osh: negative array size");
     size_t nb = size_t(n) * size_t(esize);
-    std::vector<char> out(nb);
-    if (compressed) {
-      std::int64_t cb = val<std::int64_t>();
-      if (cb < 0) throw Error(1, ".osh: negative compressed size");
-      need(size_t(cb));
-      const Zlib& z = zlib();
-      if (!z.ok()) throw Error(1, ".osh: compressed file and no zlib on this system");
-      unsigned long got = nb;
-      int rc = z.uncompress(reinterpret_cast<unsigned char*>(out.data()), &got,
-                            reinterpret_cast<const unsigned char*>(b_.data() + p_), size_t(cb));
-      if (rc != 0 || got != nb) throw Error(1, ".osh: zlib stream does not match its array");
-      p_ += size_t(cb);
-    } else {
-      need(nb);
-      if (nb) std::memcpy(out.data(), b_.data() + p_, nb);
-      p_ += nb;
-    }
     *n_out = n;
-    return out;
+    if (!compressed) {
+      need(nb);
+      const char* p = b_.data() + p_;
+      p_ += nb;
+      return p;
+    }
+    std::int64_t cb = val<std::int64_t>();
+    if (cb < 0) throw Error(1, ".osh: negative compressed size");
+    need(size_t(cb));
+    const Zlib& z = zlib();
+    if (!z.ok()) throw Error(1, ".osh: compressed file and no zlib on this system");
+    owned->resize(nb);
+    unsigned long got = nb;
+    int rc = z.uncompress(reinterpret_cast<unsigned char*>(owned->data()), &got,
+                          reinterpret_cast<const unsigned char*>(b_.data() + p_), size_t(cb));
+    if (rc != 0 || got != nb) throw Error(1, ".osh: zlib stream does not match its array");
+    p_ += size_t(cb);
+    return owned->data();
   }
   bool done() const { return p_ == b_.size(); }
 
@@ -165,11 +166,14 @@ class In {
   size_t p_ = 0;
 };
 
+// one array from host bytes to the device, in one copy
 template <class T>
-Arr<T> upload(const std::vector<char>& bytes, LO n) {
-  std::vector<T> h(static_cast<size_t>(n));
-  if (n) std::memcpy(h.data(), bytes.data(), size_t(n) * sizeof(T));
-  return to_device(h);
+Arr<T> upload(const char* bytes, LO n) {
+  Arr<T> a(n);
+  if (n)
+    OHG_CUDA(cudaMemcpyAsync(a.data(), bytes, size_t(n) * sizeof(T), cudaMemcpyHostToDevice,
+                             ctx().stream));
+  return a;
 }
 
 void write_text(const std::string& path, int v) {
@@ -327,9 +331,12 @@ Mesh read_osh(const std::string& dir) {
   int version = read_int_file(dir + "/version");
   if (version < 1 || version > kLatestVersion)
     throw Error(1, ".osh: unsupported version " + std::to_string(version));
-  std::ifstream f(dir + "/0.osh", std::ios::binary);
+  std::ifstream f(dir + "/0.osh", std::ios::binary | std::ios::ate);
   if (!f) throw Error(1, "cannot read " + dir + "/0.osh");
-  std::vector<char> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  std::streamsize fsize = f.tellg();
+  f.seekg(0);
+  std::vector<char> b(static_cast<size_t>(fsize > 0 ? fsize : 0));
+  if (fsize > 0 && !f.read(b.data(), fsize)) throw Error(1, "cannot read " + dir + "/0.osh");
   In in(std::move(b));
   unsigned char mg0 = (unsigned char)in.val<char>(), mg1 = (unsigned char)in.val<char>();
   if (mg0 != kMagic[0] || mg1 != kMagic[1]) throw Error(1, ".osh: bad magic number");
@@ -351,10 +358,11 @@ Mesh read_osh(const std::string& dir) {
   for (int d = 1; d <= m.dim; ++d) {
     Adj a;
     LO n;
-    std::vector<char> ab = in.array(4, comp, &n);
+    std::vector<char> owned;
+    const char* ab = in.array(4, comp, &n, &owned);
     a.ab2b = upload<LO>(ab, n);
     if (d > 1) {
-      std::vector<char> cb = in.array(1, comp, &n);
+      const char* cb = in.array(1, comp, &n, &owned);
       a.codes = upload<I8>(cb, n);
       a.has_codes = true;
     }
@@ -370,7 +378,9 @@ Mesh read_osh(const std::string& dir) {
         if (version >= 2) in.val<I8>();
       }
       LO n;
-      std::vector<char> bytes = in.array(type_size(type), comp, &n);
+      std::vector<char> owned;
+      const char* bytes = in.array(type_size(type), comp, &n, &owned);
+      size_t nbytes = size_t(n) * size_t(type_size(type));
       if (n != LO(std::int64_t(m.nents[d]) * ncomps))
         throw Error(1, ".osh: tag " + name + " has the wrong size");
       m.tag_order[d].push_back(name);
@@ -391,13 +401,13 @@ Mesh read_osh(const std::string& dir) {
         m.has_quality = true;
       } else if (name == "global" && type == T_I64 && ncomps == 1) {
         std::vector<std::int64_t> g(static_cast<size_t>(n));
-        if (n) std::memcpy(g.data(), bytes.data(), bytes.size());
+        if (n) std::memcpy(g.data(), bytes, nbytes);
         known = is_iota(g);  // one rank numbers 0..n-1; anything else is kept as is
       } else {
         known = false;
       }
       if (!known) {
-        Mesh::Tag t{d, ncomps, type, name, upload<I8>(bytes, LO(bytes.size()))};
+        Mesh::Tag t{d, ncomps, type, name, upload<I8>(bytes, LO(nbytes))};
         m.extra_tags.push_back(std::move(t));
       }
     }
