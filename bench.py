@@ -36,7 +36,7 @@ METRIC = "elements/s per adapt pass"
 DOMINANT = "coarsen_filter"
 # untimed passes in which the launch-shape autotuner explores its variants
 AUTOTUNE_PASSES = 4
-DOMINANT_TRAFFIC = 121394432  # bytes per launch on the 64^3 shock pass
+DOMINANT_TRAFFIC = 118974208  # bytes per launch on the 64^3 shock pass (ncu dram read + write)
 # Batched workload: 1024 independent 3D boxes, subdivisions per axis
 # log-uniform integers in [4, 40] (seeded), isotropic sine metric with seeded
 # h0, amplitude and wave vector per mesh
