@@ -585,11 +585,9 @@ def run_ours(args):
     precision["workload"] = w["workload"]
     if rank == 0 and not args.no_precision:
         precision = [precision] + run_precision(ctx, lib_stream, flush)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * nelems * args.steps / (total_ms / 1e3)
+    from omega_h_gb300.replicas import replica_throughput
+    value, total_s = replica_throughput(nelems * args.steps, total_ms / 1e3, dev)
+    total_ms = total_s * 1e3
 
     # ---- e2e through the C ABI from pinned host buffers
     names = ["down_1", "down_2", "downcodes_2", "down_3", "downcodes_3", "coords", "metric"] + \
@@ -625,8 +623,7 @@ def run_ours(args):
         flush.fill_(1)
         d2h = e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = world * nelems * args.steps / e2e_s
+    e2e_value, e2e_s = replica_throughput(nelems * args.steps, time.perf_counter() - t0, dev)
 
     # ---- roofline: the pass's dominant kernel timed in the timed steps above
     # (CUDA events on the library stream around each launch), plus the
