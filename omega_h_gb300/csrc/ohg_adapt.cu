@@ -125,9 +125,16 @@ VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metri
   return s;
 }
 
+// the mesh's screening data, built once per coords and metric
+const VertScreen& mesh_screen(Mesh& m) {
+  if (!m.screen)
+    m.screen = std::make_shared<VertScreen>(build_vert_screen(m.coords, m.metric, m.nverts(), m.dim));
+  return *m.screen;
+}
+
 void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
   int dim = m.dim, nvv = dim + 1;
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
@@ -147,7 +154,7 @@ void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, doub
 
 void screen_edges(Mesh& m, const LO* ev2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
   int dim = m.dim, mc = m.mcomp();
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
@@ -905,7 +912,7 @@ constexpr int kMaxScreenCavity = 64;
 // the minimum is the reference's minimum.
 static void coarsen_qualities_screened(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p,
                                        double* q2_p) {
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
   auto cv = cview(m.ask_verts_of(3));
@@ -1212,7 +1219,7 @@ template <int D>
 static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, const LO* c2e_p,
                                                  LO n, const I8* ci_p, I8* co_p) {
   constexpr int dim = D, mc = D == 3 ? 6 : 3;
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
   const Adj& v2e = m.ask_up(0, 1);
@@ -1322,7 +1329,7 @@ template <int D>
 static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,
                                   double* q2_p) {
   constexpr int dim = D;
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts(), dim);
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto ev = cview(m.ask_verts_of(1));
   auto cv = cview(m.ask_verts_of(dim));
@@ -1580,7 +1587,7 @@ static void choose_rails_lazy_d(Mesh& m, const LO* c2e_p, LO n, const I8* codes_
                                 GO* vrail_p) {
   LO nv = m.nverts();
   constexpr int dim = D;
-  VertScreen vs = build_vert_screen(m.coords, m.metric, nv, dim);
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   Arr<LO> e2c = fill<LO>(m.nedges(), -1);
   auto c2e = cview(c2e_p, n);
@@ -2077,7 +2084,7 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   Arr<int> lsize;
   Arr<LO> lverts, leev;
   swap_loops(m, c2e_p, n, lsize, lverts, leev);
-  VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+  const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
   auto ls = cview(lsize);
   auto lv = cview(lverts);
@@ -2487,6 +2494,7 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
   nm.nents[0] = m.nverts();
   nm.coords = m.coords;
   nm.metric = m.metric;
+  nm.screen = m.screen;  // same vertices, same screening data
   nm.class_dim[0] = m.class_dim[0];
   nm.class_id[0] = m.class_id[0];
   Arr<LO> old_lows2new = iota(m.nverts());

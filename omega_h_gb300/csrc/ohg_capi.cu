@@ -557,6 +557,7 @@ int ohg_mesh_set_array(ohg_mesh* m, const char* name, const void* src, long long
     OHG_CUDA(cudaMemcpyAsync(a.data(), src, size_t(nbytes), cudaMemcpyDeviceToDevice, ctx().stream));
     *dst = a;
     me.has_length = me.has_quality = false;
+    me.screen.reset();
   });
 }
 

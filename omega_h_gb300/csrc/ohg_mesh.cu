@@ -887,6 +887,7 @@ void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
   m.coords = to_device(c);
   m.metric = to_device(met);
   m.has_length = m.has_quality = false;
+  m.screen.reset();
 }
 
 // ------------------------------------------------------------ measurement
@@ -947,7 +948,7 @@ void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
   if (dim == 3 && na > 0) {
     // per-vertex det M (maxdet choice) and sqrt(det M), computed once per
     // vertex instead of four and one times per element: the same doubles
-    VertScreen vs = build_vert_screen(m.coords, m.metric, m.nverts());
+    const VertScreen& vs = mesh_screen(m);
     auto sv = screen_view(vs);
     pfor(na, [=] __device__(LO a) {
       LO e = all ? a : ae[a];

@@ -18,6 +18,8 @@ inline int simplex_degree(int from, int to) {
   return t[from][to];
 }
 
+struct VertScreen;
+
 struct Mesh {
   int dim = 3;
   LO nents[4] = {0, 0, 0, 0};
@@ -43,6 +45,9 @@ struct Mesh {
   };
   std::vector<Tag> extra_tags;
   std::vector<std::string> tag_order[4];
+  // the precision mode's per-vertex screening data, built on first use from
+  // coords and metric; reset wherever those arrays are replaced
+  std::shared_ptr<VertScreen> screen;
 
   int mcomp() const { return dim == 3 ? 6 : 3; }
   LO nverts() const { return nents[0]; }

@@ -2,6 +2,7 @@
 // radix sorts and gathers/scatters (the roles of src/Omega_h_int_scan.cpp,
 // src/Omega_h_map.cpp, src/Omega_h_sort.cpp and src/Omega_h_reduce.hpp).
 #pragma once
+#include <cstring>
 #include "ohg_common.cuh"
 
 namespace ohg {
@@ -43,6 +44,16 @@ Arr<LO> sort_by_keys64(const Arr<GO>& keys, int width);
 template <class T>
 Arr<T> fill(LO n, T v) {
   Arr<T> a(n);
+  if (n <= 0) return a;
+  // a value whose bytes are all equal (0, -1, 0.0) is a memset
+  unsigned char b[sizeof(T)];
+  std::memcpy(b, &v, sizeof(T));
+  bool same = true;
+  for (size_t k = 1; k < sizeof(T); ++k) same = same && b[k] == b[0];
+  if (same) {
+    OHG_CUDA(cudaMemsetAsync(a.data(), b[0], sizeof(T) * size_t(n), ctx().stream));
+    return a;
+  }
   auto p = view(a);
   pfor(n, [=] __device__(LO i) { p[i] = v; });
   return a;

@@ -580,5 +580,8 @@ __device__ __forceinline__ FIv edge_len_bounds_d(int dim, const ScreenView& s, L
 // builds the per-vertex screening data of a mesh of dimension dim
 VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nverts,
                              int dim = 3);
+// the mesh's screening data, built on first use and kept with the mesh
+struct Mesh;
+const VertScreen& mesh_screen(Mesh& m);
 
 }  // namespace ohg
