@@ -596,6 +596,8 @@ def run_ours(args):
     nents = (ctypes.c_int * 4)(*[base.nents(d) for d in range(4)])
     h2d = sum(t.numel() * t.element_size() for t in host.values())
 
+    out_host = {}
+
     def e2e_step():
         devs = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
         torch.cuda.synchronize()
@@ -609,8 +611,18 @@ def run_ours(args):
                   P(devs["coords"]), P(devs["metric"]), ctypes.byref(h))
         m = Mesh(ctx, h)
         m.adapt_pass(opts)
-        outs = [m.get(k).cpu() for k in names]
-        d2h = sum(t.numel() * t.element_size() for t in outs)
+        # the result's arrays straight into pinned host buffers (allocated in
+        # the warm-up steps, whose output sizes are the same)
+        d2h = 0
+        for k in names:
+            nb = ctypes.c_longlong()
+            _lib.call("ohg_mesh_array_bytes", m.handle, k.encode(), ctypes.byref(nb))
+            buf = out_host.get(k)
+            if buf is None or buf.numel() < nb.value:
+                buf = torch.empty(nb.value, dtype=torch.uint8).pin_memory()
+                out_host[k] = buf
+            _lib.call("ohg_mesh_get_array", m.handle, k.encode(), P(buf), nb.value)
+            d2h += nb.value
         m.close()
         return d2h
 

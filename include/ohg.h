@@ -162,7 +162,9 @@ int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);
  * star_a2ab_<d>, star_ab2b_<d>, dual_a2ab, dual_ab2b (Mesh::ask_adj,
  * src/Omega_h_mesh.cpp:347-357; tags, src/Omega_h_mesh.hpp:62-78) */
 int ohg_mesh_array_bytes(ohg_mesh* mesh, const char* name, long long* nbytes);
-int ohg_mesh_get_array(ohg_mesh* mesh, const char* name, void* dst_dev, long long capacity_bytes);
+/* copies a named array to dst, device memory or host memory (pinned host
+ * memory is copied to by DMA); returns after the copy completed */
+int ohg_mesh_get_array(ohg_mesh* mesh, const char* name, void* dst, long long capacity_bytes);
 /* replaces vertex coordinates or metric ("coords" | "metric") */
 int ohg_mesh_set_array(ohg_mesh* mesh, const char* name, const void* src_dev, long long nbytes);
 

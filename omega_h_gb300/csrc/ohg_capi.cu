@@ -526,7 +526,9 @@ int ohg_mesh_get_array(ohg_mesh* m, const char* name, void* dst, long long cap) 
       fits = false;
       return;
     }
-    if (b) OHG_CUDA(cudaMemcpyAsync(dst, p, size_t(b), cudaMemcpyDeviceToDevice, ctx().stream));
+    // dst may be device memory or host memory (pinned host memory is copied
+    // to by DMA); the kind is inferred from the address
+    if (b) OHG_CUDA(cudaMemcpyAsync(dst, p, size_t(b), cudaMemcpyDefault, ctx().stream));
     ctx().sync();
   });
   if (rc == OHG_OK && !ok) {
