@@ -297,6 +297,62 @@ __global__ void k_tile_scan(const T* in, LO n, const LO* sums, LO* out, const LO
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
 }
 
+// The tile scan for up to kFoldTiles tiles: each block first adds up the
+// raw sums of the tiles before it (at most a few KB, read from L2), so the
+// separate scan of the tile sums is not launched; the last block also writes
+// the total.  Integer sums, so the result is the three-phase scan's.
+constexpr LO kFoldTiles = 2048;
+template <class T>
+__global__ void k_tile_scan_fold(const T* in, LO n, const LO* sums, LO nb, LO* out) {
+  __shared__ LO warp_tot[kScanThreads / 32];
+  __shared__ LO prefix;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  LO p = 0;
+  for (LO b = LO(threadIdx.x); b < LO(blockIdx.x); b += kScanThreads) p += sums[b];
+  for (int o = 16; o > 0; o >>= 1) p += __shfl_down_sync(0xffffffffu, p, o);
+  if (lane == 0) warp_tot[warp] = p;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    LO t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += warp_tot[w];
+    prefix = t;
+    if (LO(blockIdx.x) == nb - 1) out[n] = t + sums[blockIdx.x];
+  }
+  __syncthreads();
+  LO base = LO(blockIdx.x) * kScanTile + LO(threadIdx.x) * kScanItems;
+  LO v[kScanItems];
+  LO s = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    LO i = base + k;
+    v[k] = i < n ? LO(in[i]) : 0;
+    s += v[k];
+  }
+  LO incl = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    LO y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  __syncthreads();  // warp_tot is reused
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    LO w = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
+    LO wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      LO y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+  }
+  __syncthreads();
+  LO run = prefix + warp_tot[warp] + incl - s;
+  for (int k = 0; k < kScanItems; ++k) {
+    LO i = base + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+}
+
 template <class T>
 static void scan_impl(const T* in, LO n, LO* out) {
   Ctx& c = ctx();
@@ -315,6 +371,14 @@ static void scan_impl(const T* in, LO n, LO* out) {
   LO nb = (n + kScanTile - 1) / kScanTile;
   Arr<LO> sums(nb + 1);
   k_tile_sums<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data());
+  if (nb <= kFoldTiles) {
+    k_tile_scan_fold<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), nb, out);
+    c.launches += 2;
+#ifdef OHG_CHECKED
+    checked_after_launch(__FILE__, __LINE__);
+#endif
+    return;
+  }
   k_scan_sums<<<1, 1024, 0, c.stream>>>(sums.data(), nb, sums.data() + nb);
   k_tile_scan<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), out, sums.data() + nb);
   c.launches += 3;
