@@ -114,7 +114,8 @@ int ohg_context_tuning(ohg_context* ctx, int* counts3);
 int ohg_build_box(ohg_context* ctx, int dim, int n, ohg_mesh** out);
 /* seeded jitter of interior vertices (uniform +-0.15/n per axis) and an
  * analytic metric: 0 isotropic h=0.05+0.1|x0-0.5|, 1 shock, 2 boundary
- * layer, 3 isotropic sine */
+ * layer, 3 isotropic sine, as packed tensors; 10 and 13: kinds 0 and 3 as
+ * one scalar per vertex (an isotropic metric) */
 int ohg_mesh_apply_workload(ohg_mesh* mesh, int n, unsigned long long seed, int metric_kind);
 /* build_from_elems_and_coords (src/Omega_h_build.cpp:100-105): elements to
  * vertices plus coordinates and metric, all device arrays copied in */
@@ -165,7 +166,10 @@ int ohg_mesh_array_bytes(ohg_mesh* mesh, const char* name, long long* nbytes);
 /* copies a named array to dst, device memory or host memory (pinned host
  * memory is copied to by DMA); returns after the copy completed */
 int ohg_mesh_get_array(ohg_mesh* mesh, const char* name, void* dst, long long capacity_bytes);
-/* replaces vertex coordinates or metric ("coords" | "metric") */
+/* replaces vertex coordinates or metric ("coords" | "metric").  A metric of
+ * nverts values is isotropic (the reference's one-component metric tag: its
+ * scalar lengths, sizes, maxdet and log-Euclidean means are used), one of
+ * nverts * 6 (3D) or * 3 (2D) values is a packed tensor. */
 int ohg_mesh_set_array(ohg_mesh* mesh, const char* name, const void* src_dev, long long nbytes);
 
 /* ---- the pass ---- */

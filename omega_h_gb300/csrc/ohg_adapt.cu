@@ -26,34 +26,22 @@ AdaptOpts::AdaptOpts(int dim) {
 typedef View<const double> RV;
 typedef View<const LO> LV;
 
-__device__ __forceinline__ double elem_quality_v(int dim, RV c, RV mt, const LO* v) {
-  if (dim == 3) {
-    V3 p[4];
-    M3 ms[4];
-    for (int i = 0; i < 4; ++i) {
-      for (int j = 0; j < 3; ++j) p[i].x[j] = c[v[i] * 3 + j];
-      ms[i] = symm3(&mt[v[i] * 6]);
-    }
-    return tet_quality(p, ms[maxdet_index3(ms, 4)]);
+// FP64 element quality of vertices v with the maxdet metric (mc metric
+// components per vertex; 1: isotropic)
+__device__ __forceinline__ double elem_quality_v(int dim, RV c, RV mt, int mc, const LO* v) {
+  double pts[12];
+  const double* ms[4];
+  for (int i = 0; i <= dim; ++i) {
+    for (int j = 0; j < dim; ++j) pts[i * dim + j] = c[v[i] * dim + j];
+    ms[i] = &mt[v[i] * mc];
   }
-  double p[3][2];
-  int best = 0;
-  double bd = det2p(&mt[v[0] * 3]);
-  for (int i = 0; i < 3; ++i) {
-    p[i][0] = c[v[i] * 2];
-    p[i][1] = c[v[i] * 2 + 1];
-    if (i) {
-      double d = det2p(&mt[v[i] * 3]);
-      if (d > bd) {
-        best = i;
-        bd = d;
-      }
-    }
-  }
-  return tri_quality(p, &mt[v[best] * 3]);
+  return elem_quality_ms(dim, mc, pts, ms);
 }
 
 __device__ __forceinline__ double edge_len_v(int dim, RV c, RV mt, int mc, LO a, LO b) {
+  if (mc == 1)
+    return dim == 3 ? edge_length_iso3(&c[a * 3], &c[b * 3], mt[a], mt[b])
+                    : edge_length_iso2(&c[a * 2], &c[b * 2], mt[a], mt[b]);
   return dim == 3 ? edge_length3(&c[a * 3], &c[b * 3], &mt[a * mc], &mt[b * mc])
                   : edge_length2(&c[a * 2], &c[b * 2], &mt[a * mc], &mt[b * mc]);
 }
@@ -62,6 +50,8 @@ __device__ __forceinline__ double edge_len_v(int dim, RV c, RV mt, int mc, LO a,
 VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nv,
                              int dim) {
   VertScreen s;
+  int mc = nv > 0 ? LO(metric.size() / nv) : (dim == 3 ? 6 : 3);
+  s.mc = mc;
   s.xh = Arr<float4>(nv);
   s.xl = Arr<float4>(nv);
   s.ma = Arr<float4>(nv);
@@ -86,6 +76,15 @@ VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metri
       }
       xh[v] = make_float4(h[0], h[1], 0.0f, fmaxf(fabsf(h[0]), fabsf(h[1])));
       xl[v] = make_float4(l[0], l[1], 0.0f, 0.0f);
+      if (mc == 1) {  // isotropic: diag(m), size factor m
+        double m = mt[v];
+        float f = __double2float_rn(m);
+        ma[v] = make_float4(f, f, 0.0f, __fmul_ru(2.0f * fabsf(f), 1.0f + 0x1p-20f));
+        mb[v] = make_float4(0.0f, 0.0f, 0.0f, __double2float_rn(m));
+        dk[v] = order_key(m);
+        sd[v] = m;
+        return;
+      }
       const double* m = &mt[v * 3];
       float f[3];
       for (int j = 0; j < 3; ++j) f[j] = __double2float_rn(m[j]);
@@ -109,6 +108,17 @@ VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metri
     float mxh = fmaxf(fabsf(h[0]), fmaxf(fabsf(h[1]), fabsf(h[2])));
     xh[v] = make_float4(h[0], h[1], h[2], mxh);
     xl[v] = make_float4(l[0], l[1], l[2], 0.0f);
+    if (mc == 1) {  // isotropic: diag(m), size factor sqrt(m (m m))
+      double m = mt[v];
+      float f = __double2float_rn(m);
+      double sf = iso_size_factor(3, m);
+      ma[v] = make_float4(f, f, f, 0.0f);
+      mb[v] = make_float4(0.0f, 0.0f, __fmul_ru(3.0f * fabsf(f), 1.0f + 0x1p-20f),
+                          __double2float_rn(sf));
+      dk[v] = order_key(m);
+      sd[v] = sf;
+      return;
+    }
     const double* m = &mt[v * 6];
     float f[6];
     for (int j = 0; j < 6; ++j) f[j] = __double2float_rn(m[j]);
@@ -555,42 +565,22 @@ void refine_qualities(Mesh& m, const LO* c2e_p, LO n, const double* mid_p, doubl
         int ccs = opposite_template(dim, 0, ccv);
         LO sv[3];
         for (int k = 0; k < dim; ++k) sv[k] = cv[el * (dim + 1) + down_template(dim, dim - 1, ccs, k)];
-        double q;
+        // the child: the face opposite the endpoint plus the midpoint (in
+        // 3D with the face's last two vertices swapped, flip_new_elem)
         if (dim == 3) {
           LO t = sv[1];
           sv[1] = sv[2];
           sv[2] = t;
-          V3 p[4];
-          M3 ms[4];
-          for (int i = 0; i < 3; ++i) {
-            for (int j = 0; j < 3; ++j) p[i].x[j] = c[sv[i] * 3 + j];
-            ms[i] = symm3(&mt[sv[i] * 6]);
-          }
-          for (int j = 0; j < 3; ++j) p[3].x[j] = midp[j];
-          ms[3] = symm3(&mid[cand * 6]);
-          q = tet_quality(p, ms[maxdet_index3(ms, 4)]);
-        } else {
-          double p[3][2];
-          const double* mm[3];
-          for (int i = 0; i < 2; ++i) {
-            p[i][0] = c[sv[i] * 2];
-            p[i][1] = c[sv[i] * 2 + 1];
-            mm[i] = &mt[sv[i] * 3];
-          }
-          p[2][0] = midp[0];
-          p[2][1] = midp[1];
-          mm[2] = &mid[cand * 3];
-          int best = 0;
-          double bd = det2p(mm[0]);
-          for (int i = 1; i < 3; ++i) {
-            double d = det2p(mm[i]);
-            if (d > bd) {
-              best = i;
-              bd = d;
-            }
-          }
-          q = tri_quality(p, mm[best]);
         }
+        double pts[12];
+        const double* ms[4];
+        for (int i = 0; i < dim; ++i) {
+          for (int j = 0; j < dim; ++j) pts[i * dim + j] = c[sv[i] * dim + j];
+          ms[i] = &mt[sv[i] * mc];
+        }
+        for (int j = 0; j < dim; ++j) pts[dim * dim + j] = midp[j];
+        ms[dim] = &mid[cand * mc];
+        double q = elem_quality_ms(dim, mc, pts, ms);
         minq = min2d(minq, q);
       }
     }
@@ -768,6 +758,7 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* s
   Mesh nm;
   nm.dim = dim;
   nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.metric_comps = m.metric_comps;
   nm.class_sets = m.class_sets;
   Arr<LO> k2mid, ov2nv, old_lows2new;
   for (int d = 0; d <= dim; ++d) {
@@ -968,6 +959,7 @@ static void coarsen_qualities_screened(Mesh& m, const LO* c2e_p, LO n, const I8*
 
 // coarsen_qualities_tmpl (src/Omega_h_coarsen_qualities.cpp:15-63)
 void coarsen_qualities(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, double* q2_p) {
+  int mc = m.mcomp();  // metric components per vertex (1: isotropic)
   int dim = m.dim;
   if (dim == 3 && ctx().screening) {
     coarsen_qualities_screened(m, c2e_p, n, codes_p, q2_p);
@@ -1002,7 +994,7 @@ void coarsen_qualities(Mesh& m, const LO* c2e_p, LO n, const I8* codes_p, double
           if (k != ccv_col && vv[k] == v_onto) dies = true;
         if (dies) continue;
         vv[ccv_col & 3] = v_onto;
-        minq = min2d(minq, elem_quality_v(dim, c, mt, vv));
+        minq = min2d(minq, elem_quality_v(dim, c, mt, mc, vv));
       }
       q2[cand * 2 + col] = minq;
     }
@@ -1868,6 +1860,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Mesh nm;
   nm.dim = dim;
   nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.metric_comps = m.metric_comps;
   nm.class_sets = m.class_sets;
   Arr<LO> ov2nv, old_lows2new;
   for (int d = 0; d <= dim; ++d) {
@@ -2080,6 +2073,7 @@ static void swap_loops(Mesh& m, const LO* edges_p, LO n, Arr<int>& lsize, Arr<LO
 //     and quality, the first one winning ties.
 static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, LO n,
                                       double* quals_p, I8* configs_p) {
+  int mc = m.mcomp();  // metric components per vertex (1: isotropic)
   auto tab = swap_tables();
   Arr<int> lsize;
   Arr<LO> lverts, leev;
@@ -2142,7 +2136,7 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
         } else if (L.hi <= thr) {
           o = false;
         } else {
-          o = edge_len_v(3, c, mt, 6, a, b) > max_len;
+          o = edge_len_v(3, c, mt, mc, a, b) > max_len;
           nx = 1;
         }
         ov[idx] = o;
@@ -2283,6 +2277,7 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
 
 void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p,
                       I8* configs_p) {
+  int mc = m.mcomp();  // metric components per vertex (1: isotropic)
   if (ctx().screening) {
     swap3d_qualities_screened(m, max_len, c2e_p, n, quals_p, configs_p);
     return;
@@ -2310,7 +2305,7 @@ void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* qu
       double tmq = 1.0;
       for (int tt = 0; tt < 2; ++tt) {
         tet[3] = le[i * 2 + (1 - tt)];
-        tmq = min2d(tmq, elem_quality_v(3, c, mt, tet));
+        tmq = min2d(tmq, elem_quality_v(3, c, mt, mc, tet));
         LO s = tet[1];
         tet[1] = tet[2];
         tet[2] = s;
@@ -2327,7 +2322,7 @@ void swap3d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* qu
       if (size < 3 || u >= tab[size * 9 + SW_NUEDGE]) return;
       int oued = tab[size * 9 + SW_OUEDGE];
       LO a = lv[i * 7 + tab[oued + u * 2]], b = lv[i * 7 + tab[oued + u * 2 + 1]];
-      l[idx] = edge_len_v(3, c, mt, 6, a, b);
+      l[idx] = edge_len_v(3, c, mt, mc, a, b);
     });
   }
   auto q = cview(tq);
@@ -2416,6 +2411,7 @@ __device__ __forceinline__ bool swap2d_opposite(LV ea, LV eb, View<const I8> ec,
 // new diagonal (ov[0], ov[1]) is longer than max_len, else the min of 1 and
 // the two new triangles' qualities
 void swap2d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* quals_p) {
+  int mc = m.mcomp();  // metric components per vertex (1: isotropic)
   const Adj& e2t = m.ask_up(1, 2);
   auto ea = cview(e2t.a2ab);
   auto eb = cview(e2t.ab2b);
@@ -2435,7 +2431,7 @@ void swap2d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* qu
       q[cand] = -1.0;
       return;
     }
-    if (edge_len_v(2, c, mt, 3, ov[0], ov[1]) > max_len) {
+    if (edge_len_v(2, c, mt, mc, ov[0], ov[1]) > max_len) {
       q[cand] = -1.0;
       return;
     }
@@ -2443,7 +2439,7 @@ void swap2d_qualities(Mesh& m, double max_len, const LO* c2e_p, LO n, double* qu
     double minq = 1.0;
     for (int i = 0; i < 2; ++i) {
       LO ntv[3] = {i == 0 ? e1 : e0, ov[i], ov[1 - i]};
-      minq = min2d(minq, elem_quality_v(2, c, mt, ntv));
+      minq = min2d(minq, elem_quality_v(2, c, mt, mc, ntv));
     }
     q[cand] = minq;
   });
@@ -2490,6 +2486,7 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
   Mesh nm;
   nm.dim = dim;
   nm.rebuilt = true;  // element-based partitioning after a rebuild
+  nm.metric_comps = m.metric_comps;
   nm.class_sets = m.class_sets;
   nm.nents[0] = m.nverts();
   nm.coords = m.coords;

@@ -69,10 +69,14 @@ Mesh concat_meshes(const std::vector<Mesh*>& ms) {
   if (K == 0) throw Error(8, "concat of no meshes");
   if (K > kMaxParts) throw Error(8, "concat of more than " + std::to_string(kMaxParts) + " meshes");
   int dim = ms[0]->dim;
-  for (Mesh* m : ms)
+  for (Mesh* m : ms) {
     if (m->dim != dim) throw Error(8, "concat of meshes of different dimensions");
+    if (m->mcomp() != ms[0]->mcomp())
+      throw Error(8, "concat of meshes with isotropic and anisotropic metrics");
+  }
   Mesh u;
   u.dim = dim;
+  u.metric_comps = ms[0]->metric_comps;
   std::vector<std::vector<LO>> off(dim + 1, std::vector<LO>(K, 0));
   for (int d = 0; d <= dim; ++d) {
     LO run = 0;
@@ -211,6 +215,7 @@ std::vector<Mesh> split_mesh(Mesh& u, int K) {
   std::vector<Mesh> out(K);
   for (int k = 0; k < K; ++k) {
     Mesh& m = out[k];
+    m.metric_comps = u.metric_comps;
     m.parting = u.parting;
     m.rebuilt = u.rebuilt;
     m.class_sets = u.class_sets;

@@ -274,6 +274,7 @@ static void clone_mesh(const Mesh& a, Mesh& b) {
   b.metric = copy_arr(a.metric);
   // the state written to .osh files (lengths and qualities are not copied:
   // a clone measures them afresh)
+  b.metric_comps = a.metric_comps;
   b.parting = a.parting;
   b.rebuilt = a.rebuilt;
   b.class_sets = a.class_sets;
@@ -550,12 +551,18 @@ int ohg_mesh_set_array(ohg_mesh* m, const char* name, const void* src, long long
     g_err = "only coords and metric can be set";
     return OHG_ERR_INVALID;
   }
-  if (nbytes != dst->size() * 8LL) {
+  // a metric of one value per vertex is isotropic; of the packed tensor's
+  // size, anisotropic
+  long long full = (long long)me.nverts() * (me.dim == 3 ? 6 : 3) * 8LL;
+  long long iso = (long long)me.nverts() * 8LL;
+  bool ok = n == "metric" ? (nbytes == full || nbytes == iso) : nbytes == dst->size() * 8LL;
+  if (!ok) {
     g_err = "size mismatch for " + n;
     return OHG_ERR_BOUNDS;
   }
   return guarded(m->owner, [&] {
-    Arr<double> a(dst->size());
+    if (n == "metric") me.metric_comps = (nbytes == iso && nbytes != full) ? 1 : 0;
+    Arr<double> a(LO(nbytes / 8));
     OHG_CUDA(cudaMemcpyAsync(a.data(), src, size_t(nbytes), cudaMemcpyDeviceToDevice, ctx().stream));
     *dst = a;
     me.has_length = me.has_quality = false;

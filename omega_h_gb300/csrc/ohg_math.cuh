@@ -232,6 +232,98 @@ OHG_HD double tri_quality(const double p[3][2], const double* m) {
   return x / msl;
 }
 
+// ------------------------------------------------------------ isotropic metrics
+// A metric of one component m per vertex (the reference's Tensor<1>): the
+// product v^T (m v) scales each component first and sums left to right, the
+// size factor is power<dim, 2>(m) (sqrt(m (m m)) in 3D, m in 2D), maxdet
+// compares m itself, and the log-Euclidean mean of 1x1 tensors is
+// exp(mean of logs), with the eigensolver's zero path (|x| <= 1e-10) kept
+// (src/Omega_h_metric.hpp:10-23,126-150, src/Omega_h_shape.hpp:400-403,
+// src/Omega_h_eigen.hpp:288-321).
+OHG_HD double iso_product3(double m, V3 v) {
+  double o = v.x[0] * (v.x[0] * m);
+  o = o + v.x[1] * (v.x[1] * m);
+  o = o + v.x[2] * (v.x[2] * m);
+  return o;
+}
+OHG_HD double iso_product2(double m, double v0, double v1) {
+  double o = v0 * (v0 * m);
+  o = o + v1 * (v1 * m);
+  return o;
+}
+OHG_HD double edge_length_iso3(const double* p0, const double* p1, double m0, double m1) {
+  V3 v = {{p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]}};
+  return aniso_length(sqrt(iso_product3(m0, v)), sqrt(iso_product3(m1, v)));
+}
+OHG_HD double edge_length_iso2(const double* p0, const double* p1, double m0, double m1) {
+  double v0 = p1[0] - p0[0], v1 = p1[1] - p0[1];
+  return aniso_length(sqrt(iso_product2(m0, v0, v1)), sqrt(iso_product2(m1, v0, v1)));
+}
+OHG_HD double iso_size_factor(int dim, double m) { return dim == 3 ? sqrt(m * (m * m)) : m; }
+OHG_HD double tet_quality_iso(const V3 p[4], double m) {
+  V3 b0 = sub3(p[1], p[0]), b1 = sub3(p[2], p[0]), b2 = sub3(p[3], p[0]);
+  double rs = dot3(cross3(b0, b1), b2) / 6.0;
+  double s = rs * iso_size_factor(3, m);
+  if (s < 0) return s;
+  V3 nb1 = {{-b1.x[0], -b1.x[1], -b1.x[2]}};
+  V3 ev[6] = {b0, sub3(p[2], p[1]), nb1, b2, sub3(p[3], p[1]), sub3(p[3], p[2])};
+  double msl = 0;
+  for (int i = 0; i < 6; ++i) msl += iso_product3(m, ev[i]);
+  msl = msl / 6;
+  double x = s / kEquilateralTet;
+  return cbrt(x * x) / msl;
+}
+OHG_HD double tri_quality_iso(const double p[3][2], double m) {
+  double b00 = p[1][0] - p[0][0], b01 = p[1][1] - p[0][1];
+  double b10 = p[2][0] - p[0][0], b11 = p[2][1] - p[0][1];
+  double rs = (b00 * b11 - b01 * b10) / 2.0;
+  double s = rs * m;
+  if (s < 0) return s;
+  double ev[3][2] = {{b00, b01}, {p[2][0] - p[1][0], p[2][1] - p[1][1]}, {-b10, -b11}};
+  double msl = 0;
+  for (int i = 0; i < 3; ++i) msl += iso_product2(m, ev[i][0], ev[i][1]);
+  msl = msl / 3;
+  double x = s / kEquilateralTri;
+  return x / msl;
+}
+OHG_HD double iso_log(double m) { return fabs(m) <= 1e-10 ? log(0.0) : log(m); }
+OHG_HD double average_metric_iso(double a, double b) {
+  double am = 0.0 + iso_log(a);
+  am = am + iso_log(b);
+  am = am / 2;
+  return fabs(am) <= 1e-10 ? exp(0.0) : exp(am);
+}
+
+// the determinant the maxdet choice compares: the tensor's, or the scalar
+OHG_HD double metric_det(int dim, int mc, const double* m) {
+  return mc == 1 ? m[0] : dim == 3 ? det3(symm3(m)) : det2p(m);
+}
+// FP64 element quality with the maxdet metric among per-vertex metrics
+// ms[0..dim] (mc components each; 1: isotropic); pts holds dim + 1 points
+OHG_HD double elem_quality_ms(int dim, int mc, const double* pts, const double* const* ms) {
+  int best = 0;
+  double bd = metric_det(dim, mc, ms[0]);
+  for (int i = 1; i <= dim; ++i) {
+    double d = metric_det(dim, mc, ms[i]);
+    if (d > bd) {
+      best = i;
+      bd = d;
+    }
+  }
+  if (dim == 3) {
+    V3 p[4];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 3; ++j) p[i].x[j] = pts[i * 3 + j];
+    return mc == 1 ? tet_quality_iso(p, ms[best][0]) : tet_quality(p, symm3(ms[best]));
+  }
+  double p[3][2];
+  for (int i = 0; i < 3; ++i) {
+    p[i][0] = pts[i * 2];
+    p[i][1] = pts[i * 2 + 1];
+  }
+  return mc == 1 ? tri_quality_iso(p, ms[best][0]) : tri_quality(p, ms[best]);
+}
+
 // ------------------------------------------------------------ eigen (3x3)
 OHG_HD double sq(double x) { return x * x; }
 OHG_HD double cube(double x) { return x * (x * x); }

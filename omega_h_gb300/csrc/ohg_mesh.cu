@@ -873,7 +873,11 @@ void classify_box(Mesh& m, int n) {
 // seeded jitter of interior vertices and the analytic metric field (host
 // side: input construction only)
 void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
-  int dim = m.dim, mc = m.mcomp();
+  bool scalar = workload::scalar_kind(kind);
+  int base = workload::base_kind(kind);
+  if (scalar && base != workload::METRIC_ISO_LINEAR && base != workload::METRIC_ISO_SINE)
+    throw Error(1, "apply_workload: a scalar metric needs an isotropic kind (0 or 3)");
+  int dim = m.dim, mc = dim == 3 ? 6 : 3;
   std::vector<double> c = to_host(m.coords);
   std::vector<I8> cd = to_host(m.class_dim[0]);
   LO nv = m.nverts();
@@ -881,9 +885,14 @@ void apply_workload(Mesh& m, int n, std::uint64_t seed, int kind) {
     if (cd[v] != dim) continue;
     for (int j = 0; j < dim; ++j) c[size_t(v) * dim + j] += workload::jitter(seed, v, j, dim, n);
   }
-  workload::MetricParams mp = workload::make_params(kind, seed);
+  workload::MetricParams mp = workload::make_params(base, seed);
   std::vector<double> met(size_t(nv) * mc);
   for (LO v = 0; v < nv; ++v) workload::metric_at(mp, dim, &c[size_t(v) * dim], &met[size_t(v) * mc]);
+  if (scalar) {  // the isotropic tensor's eigenvalue, one per vertex
+    for (LO v = 0; v < nv; ++v) met[size_t(v)] = met[size_t(v) * mc];
+    met.resize(size_t(nv));
+  }
+  m.metric_comps = scalar ? 1 : 0;
   m.coords = to_device(c);
   m.metric = to_device(met);
   m.has_length = m.has_quality = false;
@@ -903,42 +912,29 @@ void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out) {
   pfor(na, [=] __device__(LO a) {
     LO e = all ? a : ae[a];
     LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
-    o[a] = dim == 3 ? edge_length3(&c[v0 * 3], &c[v1 * 3], &mt[v0 * mc], &mt[v1 * mc])
-                    : edge_length2(&c[v0 * 2], &c[v1 * 2], &mt[v0 * mc], &mt[v1 * mc]);
+    if (mc == 1)
+      o[a] = dim == 3 ? edge_length_iso3(&c[v0 * 3], &c[v1 * 3], mt[v0], mt[v1])
+                      : edge_length_iso2(&c[v0 * 2], &c[v1 * 2], mt[v0], mt[v1]);
+    else
+      o[a] = dim == 3 ? edge_length3(&c[v0 * 3], &c[v1 * 3], &mt[v0 * mc], &mt[v1 * mc])
+                      : edge_length2(&c[v0 * 2], &c[v1 * 2], &mt[v0 * mc], &mt[v1 * mc]);
   });
 }
 
-__device__ __forceinline__ double elem_quality_dev(int dim, View<const double> c,
+__device__ __forceinline__ double elem_quality_dev(int dim, int mc, View<const double> c,
                                                    View<const double> mt, const LO* v) {
-  if (dim == 3) {
-    V3 p[4];
-    M3 ms[4];
-    for (int i = 0; i < 4; ++i) {
-      for (int j = 0; j < 3; ++j) p[i].x[j] = c[v[i] * 3 + j];
-      ms[i] = symm3(&mt[v[i] * 6]);
-    }
-    return tet_quality(p, ms[maxdet_index3(ms, 4)]);
+  double pts[12];
+  const double* ms[4];
+  for (int i = 0; i <= dim; ++i) {
+    for (int j = 0; j < dim; ++j) pts[i * dim + j] = c[v[i] * dim + j];
+    ms[i] = &mt[v[i] * mc];
   }
-  double p[3][2];
-  int best = 0;
-  double bd = det2p(&mt[v[0] * 3]);
-  for (int i = 0; i < 3; ++i) {
-    p[i][0] = c[v[i] * 2];
-    p[i][1] = c[v[i] * 2 + 1];
-    if (i) {
-      double d = det2p(&mt[v[i] * 3]);
-      if (d > bd) {
-        best = i;
-        bd = d;
-      }
-    }
-  }
-  return tri_quality(p, &mt[v[best] * 3]);
+  return elem_quality_ms(dim, mc, pts, ms);
 }
 
 // measure_qualities (src/Omega_h_quality.cpp:7-53): one thread per element
 void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
-  int dim = m.dim;
+  int dim = m.dim, mc = m.mcomp();
   auto ev = cview(m.ask_verts_of(dim));
   auto c = cview(m.coords);
   auto mt = cview(m.metric);
@@ -961,7 +957,7 @@ void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
     LO e = all ? a : ae[a];
     LO v[4];
     for (int k = 0; k <= dim; ++k) v[k] = ev[e * (dim + 1) + k];
-    o[a] = elem_quality_dev(dim, c, mt, v);
+    o[a] = elem_quality_dev(dim, mc, c, mt, v);
   });
 }
 
@@ -974,7 +970,12 @@ void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
   int mc = m.mcomp();
   auto o = view(out, n * mc);
   int* st = ctx().d_status;
-  if (m.dim == 3) {
+  if (mc == 1) {
+    pfor(n, [=] __device__(LO a) {
+      LO e = all ? a : ed[a];
+      o[a] = average_metric_iso(mt[ev[e * 2]], mt[ev[e * 2 + 1]]);
+    });
+  } else if (m.dim == 3) {
     pfor(n, [=] __device__(LO a) {
       LO e = all ? a : ed[a];
       double r[6];

@@ -49,7 +49,10 @@ struct Mesh {
   // coords and metric; reset wherever those arrays are replaced
   std::shared_ptr<VertScreen> screen;
 
-  int mcomp() const { return dim == 3 ? 6 : 3; }
+  // components of the vertex metric: the packed tensor (6 in 3D, 3 in 2D),
+  // or 1 for an isotropic metric (metric_comps = 1)
+  int metric_comps = 0;
+  int mcomp() const { return metric_comps ? metric_comps : (dim == 3 ? 6 : 3); }
   LO nverts() const { return nents[0]; }
   LO nedges() const { return nents[1]; }
   LO nelems() const { return nents[dim]; }

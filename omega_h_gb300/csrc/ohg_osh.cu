@@ -387,8 +387,10 @@ Mesh read_osh(const std::string& dir) {
       bool known = true;
       if (name == "coordinates" && d == 0 && type == T_F64 && ncomps == m.dim) {
         m.coords = upload<double>(bytes, n);
-      } else if (name == "metric" && d == 0 && type == T_F64 && ncomps == m.mcomp()) {
+      } else if (name == "metric" && d == 0 && type == T_F64 &&
+                 (ncomps == m.mcomp() || ncomps == 1)) {
         m.metric = upload<double>(bytes, n);
+        m.metric_comps = ncomps == 1 ? 1 : 0;
       } else if (name == "class_id" && type == T_I32 && ncomps == 1) {
         m.class_id[d] = upload<LO>(bytes, n);
       } else if (name == "class_dim" && type == T_I8 && ncomps == 1) {

@@ -52,19 +52,26 @@ constexpr float kSixthUp = 0.16666669f;  // above 1/6
 //  dkey = order-preserving integer key of det M (maxdet choice, exact);
 //  sdet = sqrt(det M) in double, identical to what the reference computes
 //  per element from the same metric.
+//  An isotropic metric m (one component) is held as the tensor diag(m):
+//  its float products and sums bound the reference's scalar evaluation as
+//  they bound the tensor one; dkey orders m itself and sdet is the
+//  reference's size factor power<dim, 2>(m).  mc is the number of metric
+//  components of the mesh (1: isotropic).
 struct VertScreen {
   Arr<float4> xh, xl, ma, mb;
   Arr<long long> dkey;
   Arr<double> sdet;
+  int mc = 0;
 };
 
 struct ScreenView {
   View<const float4> xh, xl, ma, mb;
   View<const long long> dkey;
   View<const double> sdet;
+  int mc;
 };
 inline ScreenView screen_view(const VertScreen& s) {
-  return {cview(s.xh), cview(s.xl), cview(s.ma), cview(s.mb), cview(s.dkey), cview(s.sdet)};
+  return {cview(s.xh), cview(s.xl), cview(s.ma), cview(s.mb), cview(s.dkey), cview(s.sdet), s.mc};
 }
 
 // order-preserving map of a double to a signed 64-bit key (+0 and -0 equal)
@@ -367,7 +374,6 @@ __device__ __forceinline__ double tet_quality_exact(const ScreenView& s, View<co
   V3 p[4];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 3; ++j) p[i].x[j] = c[vv[i] * 3 + j];
-  M3 m = symm3(&mt[vv[mi] * 6]);
   double sdet = s.sdet[vv[mi]];
   V3 b0 = sub3(p[1], p[0]), b1 = sub3(p[2], p[0]), b2 = sub3(p[3], p[0]);
   double rs = dot3(cross3(b0, b1), b2) / 6.0;
@@ -376,7 +382,13 @@ __device__ __forceinline__ double tet_quality_exact(const ScreenView& s, View<co
   V3 nb1 = {{-b1.x[0], -b1.x[1], -b1.x[2]}};
   V3 ev[6] = {b0, sub3(p[2], p[1]), nb1, b2, sub3(p[3], p[1]), sub3(p[3], p[2])};
   double msl = 0;
-  for (int i = 0; i < 6; ++i) msl += metric_product3(m, ev[i]);
+  if (s.mc == 1) {
+    double m = mt[vv[mi]];
+    for (int i = 0; i < 6; ++i) msl += iso_product3(m, ev[i]);
+  } else {
+    M3 m = symm3(&mt[vv[mi] * 6]);
+    for (int i = 0; i < 6; ++i) msl += metric_product3(m, ev[i]);
+  }
   msl = msl / 6;
   double x = sz / kEquilateralTet;
   return cbrt(x * x) / msl;
@@ -543,7 +555,6 @@ __device__ __forceinline__ double tri_quality_exact(const ScreenView& s, View<co
     p[i][0] = c[vv[i] * 2];
     p[i][1] = c[vv[i] * 2 + 1];
   }
-  const double* m = &mt[vv[mi] * 3];
   double b00 = p[1][0] - p[0][0], b01 = p[1][1] - p[0][1];
   double b10 = p[2][0] - p[0][0], b11 = p[2][1] - p[0][1];
   double rs = (b00 * b11 - b01 * b10) / 2.0;
@@ -551,6 +562,14 @@ __device__ __forceinline__ double tri_quality_exact(const ScreenView& s, View<co
   if (sz < 0) return sz;
   double ev[3][2] = {{b00, b01}, {p[2][0] - p[1][0], p[2][1] - p[1][1]}, {-b10, -b11}};
   double msl = 0;
+  if (s.mc == 1) {
+    double mi_ = mt[vv[mi]];
+    for (int i = 0; i < 3; ++i) msl += iso_product2(mi_, ev[i][0], ev[i][1]);
+    msl = msl / 3;
+    double x = sz / kEquilateralTri;
+    return x / msl;
+  }
+  const double* m = &mt[vv[mi] * 3];
   for (int i = 0; i < 3; ++i) {
     double a0 = m[0] * ev[i][0], a1 = m[2] * ev[i][0];
     a0 = a0 + m[2] * ev[i][1];

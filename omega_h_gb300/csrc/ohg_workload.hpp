@@ -20,6 +20,13 @@ enum MetricKind : int {
   METRIC_ISO_SINE = 3,    // h = h0*(1 + a*sin(2*pi*k.x)), M = I/h^2
 };
 
+// kind + kScalarKind: an isotropic field stored as one scalar per vertex,
+// as the reference stores an isotropic metric (a tag of one component);
+// only for the isotropic kinds
+constexpr int kScalarKind = 10;
+inline bool scalar_kind(int kind) { return kind >= kScalarKind; }
+inline int base_kind(int kind) { return kind >= kScalarKind ? kind - kScalarKind : kind; }
+
 struct MetricParams {
   int kind = METRIC_ISO_LINEAR;
   // shock: unit normal of the rotated plane through (0.5,0.5,0.5)

@@ -215,8 +215,14 @@ class Mesh:
         _lib.call("ohg_measure_qualities", self.handle, _ptr(a2e), n, _ptr(out))
         return out
 
+    def metric_components(self):
+        """6 (3D) or 3 (2D) for a packed tensor metric, 1 for an isotropic one."""
+        nb = ctypes.c_longlong()
+        _lib.call("ohg_mesh_array_bytes", self.handle, b"metric", ctypes.byref(nb))
+        return nb.value // 8 // max(1, self.nents(0))
+
     def mident_metrics(self, edges):
-        mc = 6 if self.dim == 3 else 3
+        mc = self.metric_components()
         out = torch.empty(edges.numel() * mc, dtype=torch.float64, device=self._dev())
         _lib.call("ohg_get_mident_metrics", self.handle, _ptr(edges), edges.numel(), _ptr(out))
         return out

@@ -382,13 +382,21 @@ int main(int argc, char** argv) {
       hc[v * dim + j] += ohg::workload::jitter(seed, v, j, dim, n);
   }
   mesh.set_coords(Reals(hc.write()));
-  ohg::workload::MetricParams mp = ohg::workload::make_params(metric_kind, seed);
+  ohg::workload::MetricParams mp =
+      ohg::workload::make_params(ohg::workload::base_kind(metric_kind), seed);
   int ncomp = dim == 3 ? 6 : 3;
   HostWrite<Real> hm(mesh.nverts() * ncomp);
   HostRead<Real> hc2(mesh.coords());
   for (LO v = 0; v < mesh.nverts(); ++v)
     ohg::workload::metric_at(mp, dim, &hc2[v * dim], &hm[v * ncomp]);
-  mesh.add_tag(VERT, "metric", ncomp, Reals(hm.write()));
+  if (ohg::workload::scalar_kind(metric_kind)) {
+    // an isotropic metric tag of one component per vertex
+    HostWrite<Real> hs(mesh.nverts());
+    for (LO v = 0; v < mesh.nverts(); ++v) hs[v] = hm[v * ncomp];
+    mesh.add_tag(VERT, "metric", 1, Reals(hs.write()));
+  } else {
+    mesh.add_tag(VERT, "metric", ncomp, Reals(hm.write()));
+  }
 
   AdaptOpts opts(&mesh);
   opts.min_quality_allowed = mqa;

@@ -26,6 +26,14 @@ SMALL_CASES_2D = {
     "sq32_blayer": (2, 32, 2, 5, 0.3),
     "sq40_sine": (2, 40, 3, 2, 0.3),
 }
+# isotropic metrics stored as one scalar per vertex (the reference's
+# one-component metric tag; kind + 10); checked on the GPU against the
+# reference (the oracle restatement carries packed tensors only)
+SCALAR_CASES = {
+    "box8_iso_scalar": (3, 8, 10, 12345, 0.3),
+    "box10_sine_scalar": (3, 10, 13, 5, 0.2),
+    "sq32_sine_scalar": (2, 32, 13, 5, 0.3),
+}
 # the full adapt() loop: golden name -> spec (final mesh only)
 ADAPT_CASES = {
     "box8_iso_adapt": (3, 8, 0, 12345, 0.3),

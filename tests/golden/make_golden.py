@@ -56,6 +56,11 @@ CASES = {
     # isotropic sine field of the batched workload (seeded h0, a, k)
     "box10_sine": (3, 10, 3, 5, 0.2, True),
     "sq40_sine": (2, 40, 3, 2, 0.3, True),
+    # isotropic metrics stored as one scalar per vertex (kind + 10), the
+    # reference's isotropic metric tag
+    "box8_iso_scalar": (3, 8, 10, 12345, 0.3, True),
+    "box10_sine_scalar": (3, 10, 13, 5, 0.2, True),
+    "sq32_sine_scalar": (2, 32, 13, 5, 0.3, True),
     # the full adapt() loop (passes until lengths settle, then swaps and
     # sliver collapses): the final mesh only
     "box8_iso_adapt": (3, 8, 0, 12345, 0.3, True, "adapt"),

@@ -122,3 +122,23 @@ def test_tags_it_does_not_model_survive(ctx, tmp_path):
     m.write_osh(tmp_path / "y.osh")
     m.close()
     _same_files(str(tmp_path / "x.osh"), str(tmp_path / "y.osh"))
+
+
+def test_scalar_metric_round_trip(ctx, tmp_path):
+    """A mesh with an isotropic metric (one component per vertex) is written
+    with a one-component metric tag, as the reference writes it, and reads
+    back to the same bytes."""
+    from omega_h_gb300.mesh import Mesh, adapt_opts
+    m = Mesh.build_box(ctx, 3, 6)
+    m.apply_workload(6, 4, 13)
+    m.adapt_pass(adapt_opts(3, min_quality_allowed=0.2))
+    m.write_osh(tmp_path / "a.osh")
+    m.close()
+    f = osh.read(str(tmp_path / "a.osh"))
+    name, ncomps, ty, arr = [t for t in f["tags"][0] if t[0] == "metric"][0]
+    assert ncomps == 1 and ty == 5 and arr.size == f["nverts"]
+    r = Mesh.read_osh(ctx, tmp_path / "a.osh")
+    assert r.metric_components() == 1
+    r.write_osh(tmp_path / "b.osh")
+    r.close()
+    _same_files(str(tmp_path / "a.osh"), str(tmp_path / "b.osh"))

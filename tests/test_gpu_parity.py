@@ -5,10 +5,11 @@ of every integer array and sampled reals) and against the oracle on seeds
 without fixtures.  Integers bit-exact; reals within 1e-12 relative."""
 import pytest
 
-from conftest import (BIG_CASE, SMALL_CASES, SMALL_CASES_2D, compare_arrays, compare_digest,
+from conftest import (BIG_CASE, SCALAR_CASES, SMALL_CASES, SMALL_CASES_2D, compare_arrays,
+                      compare_digest,
                       load_digest, load_golden, run_oracle)
 
-ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D}
+ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D, **SCALAR_CASES}
 
 pytestmark = pytest.mark.gpu
 

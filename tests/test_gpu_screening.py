@@ -53,7 +53,9 @@ def _check_enclosure(lo, hi, ex, what):
           f"median {np.median(w):.2e} max {w.max():.2e}")
 
 
-@pytest.mark.parametrize("n,kind,seed", [(12, 0, 1), (16, 1, 7), (16, 2, 3), (24, 1, 2024)])
+# kinds 10 and 13: isotropic metrics stored as one scalar per vertex
+@pytest.mark.parametrize("n,kind,seed", [(12, 0, 1), (16, 1, 7), (16, 2, 3), (24, 1, 2024),
+                                         (16, 10, 3), (16, 13, 4)])
 def test_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     import torch
     m = _mesh(ctx, n, kind, seed)
@@ -87,7 +89,8 @@ def test_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     m.close()
 
 
-@pytest.mark.parametrize("n,kind,seed", [(32, 0, 1), (48, 1, 7), (40, 2, 3), (64, 3, 5)])
+@pytest.mark.parametrize("n,kind,seed", [(32, 0, 1), (48, 1, 7), (40, 2, 3), (64, 3, 5),
+                                         (48, 13, 6)])
 def test_2d_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     import torch
     m = _mesh(ctx, n, kind, seed, dim=2)
@@ -137,7 +140,9 @@ def _pass_arrays(ctx, n, kind, seed, mqa, screening, dim=3):
                                                  (3, 12, 2, 3, 0.2), (3, 20, 1, 11, 0.2),
                                                  (3, 16, 0, 5, 0.3), (3, 32, 1, 2024, 0.2),
                                                  (3, 10, 3, 5, 0.2), (2, 64, 1, 3, 0.3),
-                                                 (2, 96, 2, 4, 0.3), (2, 80, 3, 5, 0.3)])
+                                                 (2, 96, 2, 4, 0.3), (2, 80, 3, 5, 0.3),
+                                                 (3, 16, 13, 8, 0.2), (3, 12, 10, 2, 0.3),
+                                                 (2, 80, 13, 9, 0.3)])
 def test_screened_pass_equals_fp64_pass_bit_for_bit(ctx, dim, n, kind, seed, mqa):
     ctx.screen_counts(reset=True)
     st1, a1 = _pass_arrays(ctx, n, kind, seed, mqa, True, dim)
