@@ -67,6 +67,7 @@ CASES = {
     "box10_sine_adapt": (3, 10, 3, 5, 0.2, True, "adapt"),
     "sq32_shock_adapt": (2, 32, 1, 5, 0.3, True, "adapt"),
     "sq32_blayer_adapt": (2, 32, 2, 5, 0.3, True, "adapt"),
+    "box8_sine_scalar_adapt": (3, 8, 13, 5, 0.2, True, "adapt"),
 }
 
 

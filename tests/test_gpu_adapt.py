@@ -5,7 +5,7 @@ throughout."""
 import numpy as np
 import pytest
 
-from conftest import ADAPT_CASES, compare_arrays, load_golden, run_oracle
+from conftest import ADAPT_CASES, INTERP_RTOL, compare_arrays, load_golden, run_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -84,3 +84,38 @@ def test_full_adapt_screened_equals_fp64(ctx):
     assert r1 == r0
     for k in a0:
         assert np.array_equal(np.asarray(a1[k]).view(np.uint8), np.asarray(a0[k]).view(np.uint8)), k
+
+
+def test_full_adapt_with_a_scalar_metric_matches_reference(ctx):
+    """The full loop with an isotropic metric stored as one scalar per vertex
+    (box8_sine_scalar_adapt, written by the reference with a one-component
+    metric tag): the final mesh against the reference's.  A single pass with
+    scalar metrics is bit-exact in every integer (test_gpu_parity); over the
+    loop's many rounds the scalar midpoint metric exp(mean of logs) meets the
+    same one-ulp libm differences as the tensor case above, so the same
+    fraction of differing connectivity entries is allowed (measured: 2 of
+    14,252 edges)."""
+    golden = load_golden("box8_sine_scalar_adapt")
+    r, got = _adapt(ctx, 3, 8, 13, 5, 0.2)
+    keys = [k for k in golden if k.startswith("out_") and k in got]
+    for k in keys:
+        a, b = np.asarray(golden[k]), np.asarray(got[k])
+        assert a.shape == b.shape, f"{k}: shape {a.shape} vs {b.shape}"
+        if a.dtype.kind != "f":
+            nd = int(np.sum(a != b.astype(a.dtype)))
+            print(f"  {k}: {nd}/{a.size} differ")
+            assert nd <= 1e-3 * a.size, f"{k}: {nd}/{a.size} integers differ"
+    # vertex arrays do not depend on the connectivity: held to the strict
+    # tolerances; edge lengths and element qualities only where the entity's
+    # vertices agree with the reference's
+    fails, maxerr, _ = compare_arrays(golden, got, keys=["out_nents", "out_coords", "out_metric"])
+    assert not fails, fails[:10]
+    for real, conn, width in (("out_length", "out_down_1", 2), ("out_quality", "out_ev2v_3", 4)):
+        same = np.all((np.asarray(golden[conn]).reshape(-1, width)
+                       == np.asarray(got[conn]).reshape(-1, width)), axis=1)
+        a, b = np.asarray(golden[real])[same], np.asarray(got[real])[same]
+        err = float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-300)))
+        maxerr = max(maxerr, err)
+        assert err <= INTERP_RTOL, f"{real}: max rel err {err:.3e} on {same.sum()} matching entities"
+    print(f"box8_sine_scalar_adapt: {r}, max real rel err {maxerr:.2e}")
+    assert int(golden["adapt_did"][0]) == r["did"]
