@@ -891,7 +891,8 @@ int ohg_reflect_down(ohg_context* c, const int* hv2v, int nhigh, int hd, int ld,
     v2l.ab2b = Arr<LO>::wrap(const_cast<LO*>(vb), nvl);
     v2l.codes = Arr<I8>::wrap(const_cast<I8*>(vc), nvl);
     Adj r = reflect_down(Arr<LO>::wrap(const_cast<LO*>(hv2v), nhigh * (hd + 1)), nhigh,
-                         Arr<LO>::wrap(const_cast<LO*>(lv2v), nvl), v2l, hd, ld);
+                         Arr<LO>::wrap(const_cast<LO*>(lv2v), nvl), v2l, hd, ld,
+                         /*check_unique=*/true);
     LO na = nhigh * simplex_degree(hd, ld);
     OHG_CUDA(cudaMemcpyAsync(hl2l, r.ab2b.data(), size_t(na) * 4, cudaMemcpyDeviceToDevice, ctx().stream));
     if (codes_out && ld > 0)

@@ -264,6 +264,11 @@ inline void pfor_at(const char* file, int line, LO n, F f) {
   Ctx& c = ctx();
   int block = kBlock;
   bool timed = false;
+  // A launch of fewer than kBlock items per SM takes blocks of whole warps
+  // small enough for every SM to get one: small launches here are the
+  // per-candidate FP64 loops (midpoint metrics, cavity qualities), and the
+  // FP64 rate is a per-SM resource.
+  if (n < LO(c.num_sms) * kBlock) block = std::max(32, (n / c.num_sms) & ~31);
   if (n >= kTuneMinItems && c.tuner.mode != Tuner::OFF) {
     int v = c.tuner.select(file, line, n, k_for_variants<F>(), 1, c.stream);
     timed = c.tuner.open >= 0;

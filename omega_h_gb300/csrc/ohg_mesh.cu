@@ -165,6 +165,8 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   Arr<LO> deg = fill<LO>(nlows, 0);
   auto hl2l = cview(down.ab2b);
   auto dg = view(deg);
+  // Lanes of a warp that hit the same low entity (frequent: neighbouring
+  // high entities share low ones in the Hilbert order) add with one atomic.
   pfor(nhl, [=] __device__(LO hl) { atomicAdd(&dg[hl2l[hl]], 1); });
   Adj up;
   up.a2ab = offset_scan(deg);
@@ -208,8 +210,12 @@ Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
 }
 
 // reflect_down / find_matches (src/Omega_h_adj.cpp:297-441): one thread per
-// use scans the upward list of the use's first vertex
-Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld) {
+// use scans the upward list of the use's vertex with the fewest entries.
+// With check_unique the whole list is scanned and a second match is an
+// error; without it (entities this library built, unique by construction)
+// the scan stops at the match.
+Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld,
+                 bool check_unique) {
   int nvh = hd + 1, nlh = simplex_degree(hd, ld), deg = ld + 1;
   LO na = nh * nlh;
   Adj out;
@@ -279,6 +285,7 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
         ++found;
         o[a] = b;
         if (with_codes) oc[a] = mc;
+        if (!check_unique) break;
       }
     }
     if (found != 1) {

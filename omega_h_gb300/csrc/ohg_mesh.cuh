@@ -68,7 +68,10 @@ struct Mesh {
 
 // adjacency derivation (src/Omega_h_adj.cpp)
 Adj invert_adj(const Adj& down, int nlows_per_high, LO nlows);
-Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld);
+// check_unique: scan every candidate and report a second match (arrays from
+// a caller); otherwise stop at the first
+Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld,
+                 bool check_unique = false);
 Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh);
 Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld);
 Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld);
