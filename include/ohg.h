@@ -288,6 +288,11 @@ int ohg_sort_by_keys(ohg_context* ctx, const void* keys_dev, int n, int width, i
 int ohg_hilbert_sort(ohg_context* ctx, const double* coords_dev, int n, int dim, int* perm_dev);
 /* offset_scan (src/Omega_h_int_scan.cpp:10-20): n+1 outputs */
 int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
+/* collect_marked (src/Omega_h_map.cpp:174-185): the indices i < n with
+ * marks_dev[i] != 0, in increasing order, into out_dev (room for n ints);
+ * their number into *count (host) */
+int ohg_collect_marked(ohg_context* ctx, const signed char* marks_dev, int n, int* out_dev,
+                       int* count);
 /* offset_scan without any device allocation: no counterpart in the
  * reference.  For hosts that cannot let the library allocate at that moment
  * (their own arena owns the device memory, or they are recovering from an

@@ -27,6 +27,7 @@ static int status_to_code(int st) {
   if (st & ST_BOUNDS) return OHG_ERR_BOUNDS;
   if (st & ST_TOPOLOGY) return OHG_ERR_TOPOLOGY;
   if (st & ST_NUMERIC) return OHG_ERR_NUMERIC;
+  if (st & ST_STALL) return OHG_ERR_TIMEOUT;
   return OHG_OK;
 }
 
@@ -928,6 +929,19 @@ int ohg_hilbert_sort(ohg_context* c, const double* coords, int n, int dim, int* 
 }
 int ohg_offset_scan(ohg_context* c, const int* counts, int n, int* out) {
   return guarded(c, [&] { offset_scan_into(counts, n, out); });
+}
+int ohg_collect_marked(ohg_context* c, const signed char* marks, int n, int* out, int* count) {
+  if (n < 0 || !count || (n > 0 && (!marks || !out))) {
+    g_err = "ohg_collect_marked: bad arguments";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    Arr<LO> r = collect_marked(Arr<I8>::wrap(const_cast<I8*>(marks), n));
+    if (r.size())
+      OHG_CUDA(cudaMemcpyAsync(out, r.data(), size_t(r.size()) * sizeof(LO),
+                               cudaMemcpyDeviceToDevice, ctx().stream));
+    *count = r.size();
+  });
 }
 int ohg_offset_scan_noalloc(ohg_context* c, const int* counts, int n, int* out) {
   return guarded(c, [&] { offset_scan_fixed_scratch(counts, n, out); });

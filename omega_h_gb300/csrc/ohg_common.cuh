@@ -30,6 +30,7 @@ enum StatusBits : int {
   ST_BOUNDS = 4,        // an index fell outside its array
   ST_NUMERIC = 8,       // a degenerate eigen solve or non-finite value
   ST_TOPOLOGY = 16,     // an edge ring that does not close
+  ST_STALL = 32,        // a scan tile waited past its limit for a predecessor
 };
 
 struct Error : std::runtime_error {

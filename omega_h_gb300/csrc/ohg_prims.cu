@@ -297,60 +297,187 @@ __global__ void k_tile_scan(const T* in, LO n, const LO* sums, LO* out, const LO
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
 }
 
-// The tile scan for up to kFoldTiles tiles: each block first adds up the
-// raw sums of the tiles before it (at most a few KB, read from L2), so the
-// separate scan of the tile sums is not launched; the last block also writes
-// the total.  Integer sums, so the result is the three-phase scan's.
-constexpr LO kFoldTiles = 2048;
-template <class T>
-__global__ void k_tile_scan_fold(const T* in, LO n, const LO* sums, LO nb, LO* out) {
-  __shared__ LO warp_tot[kScanThreads / 32];
-  __shared__ LO prefix;
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  LO p = 0;
-  for (LO b = LO(threadIdx.x); b < LO(blockIdx.x); b += kScanThreads) p += sums[b];
-  for (int o = 16; o > 0; o >>= 1) p += __shfl_down_sync(0xffffffffu, p, o);
-  if (lane == 0) warp_tot[warp] = p;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    LO t = 0;
-    for (int w = 0; w < kScanThreads / 32; ++w) t += warp_tot[w];
-    prefix = t;
-    if (LO(blockIdx.x) == nb - 1) out[n] = t + sums[blockIdx.x];
+// ------------------------------------------------------------ single-pass scan
+// Exclusive scan in one launch by decoupled look-back (D. Merrill and
+// M. Garland, "Single-pass Parallel Prefix Scan with Decoupled Look-back",
+// NVIDIA technical report NVR-2016-002).  Each block takes the next tile
+// number from a ticket counter, so every tile before it belongs to a block
+// that is already running; it publishes its tile's sum (flag A), adds the
+// published values of the tiles before it back to the first one that holds
+// an inclusive prefix (flag P), then publishes its own inclusive prefix.  A
+// status word packs the flag (bits 32-33) with the 32-bit value, so one
+// 64-bit store publishes both.  Each item is read once and each offset
+// written once: half the traffic of the tile-sums-then-scan form.
+constexpr unsigned long long kTileAgg = 1ull << 32, kTilePre = 2ull << 32;
+// polls of one predecessor's status word before the wait is given up
+constexpr int kLookbackPolls = 1 << 20;
+
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
+  return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+// Exclusive prefix of tile t > 0, by the 32 lanes of one warp, each reading
+// one predecessor's status word per step.  A predecessor that has published
+// nothing after kLookbackPolls polls raises ST_STALL and counts as an
+// inclusive prefix of 0, so the wait always ends (the host then reports the
+// status as an error).
+__device__ LO tile_lookback(const unsigned long long* st, LO t, int* status) {
+  int lane = int(threadIdx.x & 31u);
+  LO prefix = 0;
+  for (LO top = t - 1;; top -= 32) {
+    LO j = top - lane;
+    unsigned long long w = kTilePre;  // before tile 0: an inclusive prefix of 0
+    if (j >= 0) {
+      w = ld_status(&st[j]);
+      for (int poll = 0; (w >> 32) == 0; ++poll) {
+        if (poll == kLookbackPolls) {
+          raise_status(status, ST_STALL);
+          w = kTilePre;
+          break;
+        }
+        __nanosleep(32);
+        w = ld_status(&st[j]);
+      }
+    }
+    unsigned pre = __ballot_sync(0xffffffffu, (w >> 32) == 2);
+    int stop = pre ? __ffs(pre) - 1 : 31;
+    LO v = lane <= stop ? LO(unsigned(w)) : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    prefix += v;
+    if (pre) return prefix;
   }
+}
+
+// One tile of kScanTile items per block.  kCompact = false: out[i] is the
+// exclusive prefix of in[i] and out[n] the total.  kCompact = true: in holds
+// marks; out (if not null) receives the indices of the nonzero ones in
+// increasing order and *count their number.  st holds nb zeroed status
+// words followed by the zeroed ticket counter.  vec: in (and out, for
+// offsets) are 16-byte aligned, so whole tiles move as 16-byte vectors.
+template <class T, bool kCompact>
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_lookback(const T* in, LO n, LO* out, unsigned long long* st, LO nb, int* status,
+                    bool vec, LO* count) {
+  static_assert(kScanItems == 16, "16 items per thread: 4 int4 of LO or one int4 of I8");
+  __shared__ LO s_tile, s_prefix;
+  __shared__ LO s_warp[kScanThreads / 32];
+  if (threadIdx.x == 0) s_tile = LO(atomicAdd(&st[nb], 1ull));
   __syncthreads();
-  LO base = LO(blockIdx.x) * kScanTile + LO(threadIdx.x) * kScanItems;
+  LO t = s_tile;
+  LO base = t * kScanTile + LO(threadIdx.x) * kScanItems;
   LO v[kScanItems];
-  LO s = 0;
-  for (int k = 0; k < kScanItems; ++k) {
-    LO i = base + k;
-    v[k] = i < n ? LO(in[i]) : 0;
-    s += v[k];
+  if (vec && base + kScanItems <= n) {
+    if (sizeof(T) == 1) {
+      int4 q = *reinterpret_cast<const int4*>(in + base);
+      const T* b = reinterpret_cast<const T*>(&q);
+#pragma unroll
+      for (int k = 0; k < kScanItems; ++k) v[k] = kCompact ? LO(b[k] != 0) : LO(b[k]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < kScanItems / 4; ++q) {
+        int4 w = reinterpret_cast<const int4*>(in + base)[q];
+        v[q * 4] = w.x;
+        v[q * 4 + 1] = w.y;
+        v[q * 4 + 2] = w.z;
+        v[q * 4 + 3] = w.w;
+      }
+      if (kCompact)
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = LO(v[k] != 0);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      LO i = base + k;
+      v[k] = i < n ? (kCompact ? LO(in[i] != 0) : LO(in[i])) : 0;
+    }
   }
+  LO s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) s += v[k];
+  int lane = int(threadIdx.x & 31u), warp = int(threadIdx.x >> 5);
   LO incl = s;
   for (int o = 1; o < 32; o <<= 1) {
     LO y = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += y;
   }
-  __syncthreads();  // warp_tot is reused
-  if (lane == 31) warp_tot[warp] = incl;
+  if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
+  LO wex = 0, agg = 0;
+#pragma unroll
+  for (int w = 0; w < kScanThreads / 32; ++w) {
+    LO x = s_warp[w];
+    if (w < warp) wex += x;
+    agg += x;
+  }
   if (warp == 0) {
-    LO w = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
-    LO wi = w;
-    for (int o = 1; o < 32; o <<= 1) {
-      LO y = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += y;
+    LO prefix = 0;
+    if (t == 0) {
+      if (lane == 0) atomicExch(&st[0], kTilePre | unsigned(agg));
+    } else {
+      if (lane == 0) atomicExch(&st[t], kTileAgg | unsigned(agg));
+      prefix = tile_lookback(st, t, status);
+      if (lane == 0) atomicExch(&st[t], kTilePre | unsigned(prefix + agg));
     }
-    if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+    if (lane == 0) {
+      s_prefix = prefix;
+      if (t == nb - 1) {
+        if (kCompact) *count = prefix + agg;
+        else out[n] = prefix + agg;
+      }
+    }
   }
   __syncthreads();
-  LO run = prefix + warp_tot[warp] + incl - s;
-  for (int k = 0; k < kScanItems; ++k) {
-    LO i = base + k;
-    if (i < n) out[i] = run;
-    run += v[k];
+  LO run = s_prefix + wex + incl - s;
+  if (kCompact) {
+    if (out) {
+#pragma unroll
+      for (int k = 0; k < kScanItems; ++k)
+        if (v[k]) out[run++] = base + k;
+    }
+  } else if (vec && base + kScanItems <= n) {
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      int4 w;
+      w.x = run;
+      run += v[q * 4];
+      w.y = run;
+      run += v[q * 4 + 1];
+      w.z = run;
+      run += v[q * 4 + 2];
+      w.w = run;
+      run += v[q * 4 + 3];
+      reinterpret_cast<int4*>(out + base)[q] = w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      LO i = base + k;
+      if (i < n) out[i] = run;
+      run += v[k];
+    }
   }
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<std::uintptr_t>(p) & 15u) == 0; }
+
+// launches k_scan_lookback over n > 0 items with fresh status words; count
+// (compaction) is written into the status array's last slot when null
+template <class T, bool kCompact>
+static void launch_lookback(const T* in, LO n, LO* out, Arr<unsigned long long>& st, LO** count) {
+  Ctx& c = ctx();
+  LO nb = (n + kScanTile - 1) / kScanTile;
+  st = Arr<unsigned long long>(nb + 2);
+  OHG_CUDA(cudaMemsetAsync(st.data(), 0, size_t(nb + 2) * sizeof(unsigned long long), c.stream));
+  bool vec = aligned16(in) && (kCompact || aligned16(out));
+  LO* cnt = reinterpret_cast<LO*>(st.data() + nb + 1);
+  if (count) *count = cnt;
+  k_scan_lookback<T, kCompact>
+      <<<nb, kScanThreads, 0, c.stream>>>(in, n, out, st.data(), nb, c.d_status, vec, cnt);
+  c.launches += 1;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
 }
 
 template <class T>
@@ -368,23 +495,8 @@ static void scan_impl(const T* in, LO n, LO* out) {
 #endif
     return;
   }
-  LO nb = (n + kScanTile - 1) / kScanTile;
-  Arr<LO> sums(nb + 1);
-  k_tile_sums<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data());
-  if (nb <= kFoldTiles) {
-    k_tile_scan_fold<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), nb, out);
-    c.launches += 2;
-#ifdef OHG_CHECKED
-    checked_after_launch(__FILE__, __LINE__);
-#endif
-    return;
-  }
-  k_scan_sums<<<1, 1024, 0, c.stream>>>(sums.data(), nb, sums.data() + nb);
-  k_tile_scan<T><<<nb, kScanThreads, 0, c.stream>>>(in, n, sums.data(), out, sums.data() + nb);
-  c.launches += 3;
-#ifdef OHG_CHECKED
-  checked_after_launch(__FILE__, __LINE__);
-#endif
+  Arr<unsigned long long> st;
+  launch_lookback<T, false>(in, n, out, st, nullptr);
 }
 
 void offset_scan_into(const LO* counts, LO n, LO* out) { scan_impl(counts, n, out); }
@@ -488,29 +600,31 @@ Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt) {
   return out;
 }
 
+// indices of the nonzero marks in increasing order: one compaction launch
+// and one read of the count; the result keeps its n-slot buffer
 Arr<LO> collect_marked(const Arr<I8>& marks) {
   LO n = marks.size();
-  Arr<I8> nz(n);
-  auto m = cview(marks);
-  auto z = view(nz);
-  pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
-  Arr<LO> offs = offset_scan(nz);
-  LO cnt = last(offs);
-  Arr<LO> out(cnt);
-  auto o = cview(offs);
-  auto d = view(out);
-  pfor(n, [=] __device__(LO i) {
-    if (m[i]) d[o[i]] = i;
-  });
+  if (n == 0) return Arr<LO>(0);
+  Ctx& c = ctx();
+  Arr<LO> out(n);
+  Arr<unsigned long long> st;
+  LO* cnt = nullptr;
+  launch_lookback<I8, true>(marks.data(), n, out.data(), st, &cnt);
+  OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
+  c.sync();
+  out.n = c.h_pinned[0];
   return out;
 }
 LO count_marked(const Arr<I8>& marks) {
   LO n = marks.size();
-  Arr<I8> nz(n);
-  auto m = cview(marks);
-  auto z = view(nz);
-  pfor(n, [=] __device__(LO i) { z[i] = m[i] != 0; });
-  return last(offset_scan(nz));
+  if (n == 0) return 0;
+  Ctx& c = ctx();
+  Arr<unsigned long long> st;
+  LO* cnt = nullptr;
+  launch_lookback<I8, true>(marks.data(), n, nullptr, st, &cnt);
+  OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
+  c.sync();
+  return c.h_pinned[0];
 }
 
 // ------------------------------------------------------------ reductions
