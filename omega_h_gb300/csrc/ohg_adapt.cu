@@ -1224,11 +1224,13 @@ static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, con
   auto ci = cview(ci_p, n);
   auto co = view(co_p, n);
   float thr = float_at_or_above(max_length);  // for float x: x >= max_length <=> x >= thr
+  float tdn = float_at_or_below(max_length);
   unsigned long long* cnt = ctx().d_screen_counts;
   pfor(n, [=] __device__(LO cand) {
     LO e = c2e[cand];
     I8 code = ci[cand];
     unsigned nscreen = 0, nexact = 0;
+    LenCut cut = len_cut(tdn, thr);
     for (int col = 0; col < 2; ++col) {
       if (!collapses(code, col)) continue;
       LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
@@ -1239,16 +1241,23 @@ static void prevent_coarsen_overshoot_screened_d(Mesh& m, double max_length, con
         LO nv[2];
         nv[ein] = v_onto;
         nv[eout] = ev[e2 * 2 + eout];
-        FIv L = edge_len_bounds_d(dim, sv, nv[0], nv[1]);
+        float qlo[2], qhi[2];
+        bool qok = edge_q_bounds_d(dim, sv, nv[0], nv[1], qlo, qhi);
+        int side = len_cut_side(qlo, qhi, qok, cut);
         ++nscreen;
         bool over;
-        if (L.lo >= thr) {
-          over = true;
-        } else if (L.hi < thr) {
-          over = false;
+        if (side != 0) {
+          over = side > 0;
         } else {
-          over = edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length;
-          ++nexact;
+          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+          if (L.lo >= thr) {
+            over = true;
+          } else if (L.hi < thr) {
+            over = false;
+          } else {
+            over = edge_len_v(dim, c, mt, mc, nv[0], nv[1]) >= max_length;
+            ++nexact;
+          }
         }
         if (over) {
           code = dont_collapse(code, col);
@@ -2121,6 +2130,9 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   {
     auto ov = view(over);
     float thr = float_at_or_below(max_len);  // for float x: x > max_len <=> x > thr
+    // floats t_dn <= max_len < t_up for the end-length cut (strict above)
+    float tup = float_at_or_above(max_len);
+    if (double(tup) == max_len) tup = std::nextafter(tup, INFINITY);
     pfor(n * kMaxUniqEdges, [=] __device__(LO idx) {
       LO i = idx / kMaxUniqEdges;
       int u = idx % kMaxUniqEdges;
@@ -2129,15 +2141,22 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
       if (size >= 3 && u < tab[size * 9 + SW_NUEDGE]) {
         int oued = tab[size * 9 + SW_OUEDGE];
         LO a = lv[i * 7 + tab[oued + u * 2]], b = lv[i * 7 + tab[oued + u * 2 + 1]];
-        FIv L = edge_len_bounds(sv, a, b);
+        float qlo[2], qhi[2];
+        bool qok = edge_q_bounds3(sv, a, b, qlo, qhi);
+        int side = len_cut_side(qlo, qhi, qok, len_cut(thr, tup));
         bool o;
-        if (L.lo > thr) {
-          o = true;
-        } else if (L.hi <= thr) {
-          o = false;
+        if (side != 0) {
+          o = side > 0;
         } else {
-          o = edge_len_v(3, c, mt, mc, a, b) > max_len;
-          nx = 1;
+          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+          if (L.lo > thr) {
+            o = true;
+          } else if (L.hi <= thr) {
+            o = false;
+          } else {
+            o = edge_len_v(3, c, mt, mc, a, b) > max_len;
+            nx = 1;
+          }
         }
         ov[idx] = o;
         ns = 1;

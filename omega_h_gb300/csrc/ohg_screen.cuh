@@ -148,53 +148,79 @@ __device__ __forceinline__ float mprod_err(float A, float S1, float S0, float e)
 
 // Interval of the double metric edge length (edge_length3: the logarithmic
 // mean of sqrt(v^T M0 v) and sqrt(v^T M1 v)) between vertices a and b.
-__device__ __forceinline__ FIv edge_len_bounds(const ScreenView& s, LO a, LO b) {
+// Enclosures [lo[k], hi[k]] of the double v^T M_k v at the two ends (k = 0:
+// vertex a) of the edge a-b; false when an enclosure is not positive and
+// finite (the length enclosure is then unbounded).
+__device__ __forceinline__ bool edge_q_bounds3(const ScreenView& s, LO a, LO b, float lo[2],
+                                               float hi[2]) {
   float4 ha = s.xh[a], la = s.xl[a], hb = s.xh[b], lb = s.xl[b];
   float v[3];
   float e = sdiff3(hb, lb, ha, la, v);  // p1 - p0 with p0 = a
-  float qv[2], qe[2];
   LO vs[2] = {a, b};
+  bool ok = true;
   for (int k = 0; k < 2; ++k) {
     float4 ma = s.ma[vs[k]], mb = s.mb[vs[k]];
     float A, S1;
-    qv[k] = mprod(ma, mb, v, A, S1);
-    qe[k] = __fmul_rn(mprod_err(A, S1, mb.z, e), kInflate);
+    float q = mprod(ma, mb, v, A, S1);
+    float qe = __fmul_rn(mprod_err(A, S1, mb.z, e), kInflate);
+    lo[k] = __fsub_rd(q, qe);
+    hi[k] = __fadd_ru(q, qe);
+    ok = ok && lo[k] > 0.0f && hi[k] <= FLT_MAX;
   }
+  return ok;
+}
+
+__device__ __forceinline__ FIv log_mean_bounds(const float l_lo[2], const float l_hi[2]);
+
+// the length enclosure from positive, finite end enclosures
+__device__ __forceinline__ FIv len_from_q(const float lo[2], const float hi[2]) {
   float l_lo[2], l_hi[2];
   for (int k = 0; k < 2; ++k) {
-    float lo = __fsub_rd(qv[k], qe[k]);
-    float hi = __fadd_ru(qv[k], qe[k]);
-    if (!(lo > 0.0f) || !(hi <= FLT_MAX)) return widen_all();
-    l_lo[k] = __fsqrt_rd(lo);
-    l_hi[k] = __fsqrt_ru(hi);
+    l_lo[k] = __fsqrt_rd(lo[k]);
+    l_hi[k] = __fsqrt_ru(hi[k]);
   }
-  // logarithmic mean, increasing in both arguments: evaluate it at the low
-  // and the high corners
-  float m[2];
-  for (int c = 0; c < 2; ++c) {
-    float x = c ? l_hi[0] : l_lo[0], y = c ? l_hi[1] : l_lo[1];
-    float r = __fdiv_rn(x, y);
-    float lm;
-    if (r > 1.01f || r < 0.99f) {
-      // |log r| >= 0.00995: float relative error below 110 u
-      lm = __fdiv_rn(__fsub_rn(x, y), logf(r));
-      lm = c ? __fmul_ru(lm, 1.0f + 0x1p-15f) : __fmul_rd(lm, 1.0f - 0x1p-15f);
-    } else {
-      // between the geometric and the arithmetic mean
-      lm = c ? __fmul_ru(__fmul_ru(__fadd_ru(x, y), 0.5f), 1.0f + 0x1p-20f)
-             : __fmul_rd(__fsqrt_rd(__fmul_rd(x, y)), 1.0f - 0x1p-20f);
-    }
-    m[c] = lm;
-  }
-  // the double evaluation's own error: relative 2^-50 (1 + 300 max(la, lb))
-  // on the log branch (|la - lb| > 1e-3 bounds the cancellation), 2^-53 on
-  // the mean branch
-  float mx = fmaxf(l_hi[0], l_hi[1]);
-  float d = __fmaf_ru(mx, 300.0f * 0x1p-50f, 0x1p-50f);
-  FIv r = {__fmul_rd(m[0], 1.0f - d), __fmul_ru(m[1], 1.0f + d)};
-  if (!finite_iv(r) || !(r.lo > 0.0f)) return widen_all();
-  return r;
+  return log_mean_bounds(l_lo, l_hi);
 }
+
+__device__ __forceinline__ FIv edge_len_bounds(const ScreenView& s, LO a, LO b) {
+  float lo[2], hi[2];
+  if (!edge_q_bounds3(s, a, b, lo, hi)) return widen_all();
+  return len_from_q(lo, hi);
+}
+
+// A threshold test of the double edge length from the end enclosures alone.
+// The logarithmic mean lies between the two end lengths, so when both end
+// lengths are below (at or above) a threshold, so is the exact mean; the
+// double evaluation then adds a relative error d <= 2^-50 (1 + 300 l) for
+// end lengths l (the bound log_mean_bounds applies), at most
+// 2^-50 (1 + 300 * 1025) = 307501 * 2^-50 while the squared enclosures stay
+// below kLenCutQCap = 2^20.  For floats t_dn <= T <= t_up, below_q and
+// above_q are squared end lengths under which the double length is < t_dn,
+// and over which it is >= t_up: below_q <= (t_dn / (1 + d))^2 and
+// above_q >= (t_up / (1 - d))^2, rounded outward.
+constexpr float kLenCutQCap = 0x1p20f;
+constexpr float kLenCutD = 307501.0f * 0x1p-50f;
+struct LenCut {
+  float below_q, above_q;
+};
+__device__ __forceinline__ LenCut len_cut(float t_dn, float t_up) {
+  if (!(t_dn > 0.0f) || !(t_up <= FLT_MAX)) return {-1.0f, INFINITY};
+  float sb = __fdiv_rd(t_dn, __fadd_ru(1.0f, kLenCutD));
+  float sa = __fdiv_ru(t_up, __fsub_rd(1.0f, kLenCutD));
+  return {__fmul_rd(sb, sb), __fmul_ru(sa, sa)};
+}
+// -1: the double length is < t_dn; +1: it is >= t_up; 0: not settled (also
+// when the enclosures are not positive and finite)
+__device__ __forceinline__ int len_cut_side(const float lo[2], const float hi[2], bool ok,
+                                            const LenCut& c) {
+  if (!ok) return 0;
+  float hmax = fmaxf(hi[0], hi[1]), lmin = fminf(lo[0], lo[1]);
+  if (!(hmax <= kLenCutQCap)) return 0;
+  if (hmax < c.below_q) return -1;
+  if (lmin >= c.above_q) return 1;
+  return 0;
+}
+
 
 // index (0..3) of the vertex whose metric has the largest determinant, the
 // first one on ties (maxdet_metric, src/Omega_h_metric.hpp:170-182)
@@ -449,22 +475,27 @@ __device__ __forceinline__ FIv log_mean_bounds(const float l_lo[2], const float 
 }
 
 // Interval of the double 2D metric edge length (edge_length2)
-__device__ __forceinline__ FIv edge_len_bounds2(const ScreenView& s, LO a, LO b) {
+__device__ __forceinline__ bool edge_q_bounds2(const ScreenView& s, LO a, LO b, float lo[2],
+                                               float hi[2]) {
   float v[2];
   float e = sdiff2(s.xh[b], s.xl[b], s.xh[a], s.xl[a], v);
-  float l_lo[2], l_hi[2];
   LO vs[2] = {a, b};
+  bool ok = true;
   for (int k = 0; k < 2; ++k) {
     float4 ma = s.ma[vs[k]];
     float A, S1;
     float q = mprod2(ma, v, A, S1);
     float qe = __fmul_rn(mprod2_err(A, S1, ma.w, e), kInflate);
-    float lo = __fsub_rd(q, qe), hi = __fadd_ru(q, qe);
-    if (!(lo > 0.0f) || !(hi <= FLT_MAX)) return widen_all();
-    l_lo[k] = __fsqrt_rd(lo);
-    l_hi[k] = __fsqrt_ru(hi);
+    lo[k] = __fsub_rd(q, qe);
+    hi[k] = __fadd_ru(q, qe);
+    ok = ok && lo[k] > 0.0f && hi[k] <= FLT_MAX;
   }
-  return log_mean_bounds(l_lo, l_hi);
+  return ok;
+}
+__device__ __forceinline__ FIv edge_len_bounds2(const ScreenView& s, LO a, LO b) {
+  float lo[2], hi[2];
+  if (!edge_q_bounds2(s, a, b, lo, hi)) return widen_all();
+  return len_from_q(lo, hi);
 }
 
 __device__ __forceinline__ int maxdet_vertex3(const ScreenView& s, const LO vv[3]) {
@@ -594,6 +625,10 @@ __device__ __forceinline__ double elem_quality_exact(int dim, const ScreenView& 
 }
 __device__ __forceinline__ FIv edge_len_bounds_d(int dim, const ScreenView& s, LO a, LO b) {
   return dim == 3 ? edge_len_bounds(s, a, b) : edge_len_bounds2(s, a, b);
+}
+__device__ __forceinline__ bool edge_q_bounds_d(int dim, const ScreenView& s, LO a, LO b,
+                                                float lo[2], float hi[2]) {
+  return dim == 3 ? edge_q_bounds3(s, a, b, lo, hi) : edge_q_bounds2(s, a, b, lo, hi);
 }
 
 // builds the per-vertex screening data of a mesh of dimension dim
