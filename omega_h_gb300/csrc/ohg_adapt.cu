@@ -2100,14 +2100,46 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   Arr<unsigned long long> need(n);
   Arr<float> lstar(n);
   Arr<double> tq(n * kMaxUniqTris);
+  // The (candidate, unique triangle) and (candidate, unique edge) items of
+  // all loops, numbered consecutively: loops of 4 to 6 edges use 4 to 20 of
+  // the 35 triangle slots, so a grid over the slots would leave most lanes
+  // idle.  titem/eitem map an item back to its candidate; the slots past
+  // the last item (the grid still spans n times the table maximum) return.
+  Arr<LO> tioff, eioff, titem(n * kMaxUniqTris), eitem(n * kMaxUniqEdges);
+  {
+    Arr<LO> tcnt(n), ecnt(n);
+    auto tc = view(tcnt);
+    auto ec = view(ecnt);
+    pfor(n, [=] __device__(LO i) {
+      int size = ls[i];
+      tc[i] = size >= 3 ? tab[size * 9 + SW_NUTRI] : 0;
+      ec[i] = size >= 3 ? tab[size * 9 + SW_NUEDGE] : 0;
+    });
+    tioff = offset_scan(tcnt);
+    eioff = offset_scan(ecnt);
+    auto to = cview(tioff);
+    auto eo = cview(eioff);
+    auto ti = view(titem);
+    auto ei = view(eitem);
+    pfor(n, [=] __device__(LO i) {
+      for (LO k = to[i]; k < to[i + 1]; ++k) ti[k] = i;
+      for (LO k = eo[i]; k < eo[i + 1]; ++k) ei[k] = i;
+    });
+  }
+  auto to = cview(tioff);
+  auto eo = cview(eioff);
+  auto ti = cview(titem);
+  auto ei = cview(eitem);
   {
     auto tb = view(tbnd);
-    pfor(n * kMaxUniqTris, [=] __device__(LO idx) {
-      LO i = idx / kMaxUniqTris;
-      int u = idx % kMaxUniqTris;
+    pfor(n * kMaxUniqTris, [=] __device__(LO item) {
+      if (item >= to[n]) return;
+      LO i = ti[item];
+      int u = int(item - to[i]);
+      LO idx = i * kMaxUniqTris + u;
       int size = ls[i];
       unsigned ns = 0;
-      if (size >= 3 && u < tab[size * 9 + SW_NUTRI]) {
+      {
         int otri = tab[size * 9 + SW_OTRI];
         LO tet[4];
         for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
@@ -2133,12 +2165,14 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     // floats t_dn <= max_len < t_up for the end-length cut (strict above)
     float tup = float_at_or_above(max_len);
     if (double(tup) == max_len) tup = std::nextafter(tup, INFINITY);
-    pfor(n * kMaxUniqEdges, [=] __device__(LO idx) {
-      LO i = idx / kMaxUniqEdges;
-      int u = idx % kMaxUniqEdges;
+    pfor(n * kMaxUniqEdges, [=] __device__(LO item) {
+      if (item >= eo[n]) return;
+      LO i = ei[item];
+      int u = int(item - eo[i]);
+      LO idx = i * kMaxUniqEdges + u;
       int size = ls[i];
       unsigned ns = 0, nx = 0;
-      if (size >= 3 && u < tab[size * 9 + SW_NUEDGE]) {
+      {
         int oued = tab[size * 9 + SW_OUEDGE];
         LO a = lv[i * 7 + tab[oued + u * 2]], b = lv[i * 7 + tab[oued + u * 2 + 1]];
         float qlo[2], qhi[2];
