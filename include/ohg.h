@@ -276,7 +276,9 @@ int ohg_reflect_down(ohg_context* ctx, const int* hv2v_dev, int nhigh, int high_
                      const int* v2l_ab2b_dev, const signed char* v2l_codes_dev, int nverts,
                      int* hl2l_dev, signed char* codes_out_dev);
 /* find_indset on an explicit graph (src/Omega_h_indset.cpp:17-34), entity
- * numbers as global numbers */
+ * numbers as global numbers.  *rounds: the rounds run; the rounds update
+ * their states in place, so the count (never the set) depends on the launch
+ * schedule */
 int ohg_find_indset_graph(ohg_context* ctx, int n, const int* xadj_dev, const int* adj_dev,
                           const double* quality_dev, const signed char* candidates_dev,
                           signed char* out_dev, int* rounds);

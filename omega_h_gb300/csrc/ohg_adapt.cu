@@ -215,10 +215,23 @@ static float float_at_or_below(double x) {
 enum { NOT_IN = 0, IN = 1, UNKNOWN = 2 };
 constexpr int kMaxIndsetRounds = 4096;
 
+// find_indset (src/Omega_h_indset.cpp:5-34; its rounds, local_iteration,
+// src/Omega_h_indset_inline.hpp:14-43, and their driver, lines 53-76):
+// a candidate joins when no neighbour has joined and every neighbour not yet
+// excluded ranks below it by (quality, index); it is excluded once a
+// neighbour has joined.  The set these rules settle on is unique: the greedy
+// set by decreasing rank.  The rounds here update one state array in place:
+// a state only ever moves from UNKNOWN to IN or NOT_IN, so a read that
+// misses a neighbour's decision of the same round sees UNKNOWN and can only
+// postpone a decision, never change one (a lower-ranked neighbour cannot
+// join while a higher-ranked one is UNKNOWN).  Decisions then spread within
+// a round along the launch order, and the set is the same as with rounds
+// that read only the previous round's states; the round count depends on
+// the schedule.
 Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands,
                     int* rounds_out) {
   Ctx& c = ctx();
-  Arr<I8> a(n), b(n);
+  Arr<I8> a(n);
   auto cd = cview(cands);
   // flags[0..kIndsetBatch): a vertex is still UNKNOWN after that round of
   // the batch; flags[kIndsetBatch]: there was a candidate at all
@@ -240,6 +253,7 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
   auto xa = cview(g.a2ab);
   auto xb = cview(g.ab2b);
   auto q = cview(quality);
+  I8* stp = a.data();
   int rounds = 0;
   bool any = true, first = true;
   while (any) {
@@ -247,35 +261,28 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
     if (!first) OHG_CUDA(cudaMemsetAsync(flags.data(), 0, kIndsetBatch * sizeof(int), c.stream));
     for (int r = 0; r < kIndsetBatch; ++r) {
       int* fl = flags.data() + r;
-      auto old = cview(a);
-      auto nw = view(b);
       pfor(n, [=] __device__(LO v) {
-        I8 sv = old[v];
-        if (sv != UNKNOWN) {
-          nw[v] = sv;
-          return;
-        }
+        volatile I8* s = stp;
+        if (s[v] != UNKNOWN) return;
         LO beg = xa[v], end = xa[v + 1];
         for (LO j = beg; j < end; ++j)
-          if (old[xb[j]] == IN) {
-            nw[v] = NOT_IN;
+          if (s[xb[j]] == IN) {
+            s[v] = NOT_IN;
             return;
           }
         double qv = q[v];
         for (LO j = beg; j < end; ++j) {
           LO u = xb[j];
-          if (old[u] == NOT_IN) continue;
+          if (s[u] == NOT_IN) continue;
           double qu = q[u];
           bool less = (qu != qv) ? (qu < qv) : (u < v);
           if (!less) {
-            nw[v] = UNKNOWN;
-            fl[0] = 1;
+            *fl = 1;
             return;
           }
         }
-        nw[v] = IN;
+        s[v] = IN;
       });
-      std::swap(a, b);
     }
     OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flags.data(), (kIndsetBatch + 1) * sizeof(int),
                              cudaMemcpyDeviceToHost, c.stream));
