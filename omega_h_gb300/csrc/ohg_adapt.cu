@@ -309,11 +309,25 @@ Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& q, const Arr<I8>& cands, 
 
 // ------------------------------------------------------------ marks
 static Arr<I8> mark_up(Mesh& m, int ld, int hd, const Arr<I8>& lm) {
-  auto hl = cview(m.ask_down(hd, ld).ab2b);
-  int deg = simplex_degree(hd, ld);
   Arr<I8> out(m.nents[hd]);
   auto l = cview(lm);
   auto o = view(out);
+  if (ld == VERT && hd == FACE && !m.adj.count({FACE, VERT})) {
+    // through the face's edges: the face-vertex list is not derived for it
+    auto fe = cview(m.ask_down(FACE, EDGE).ab2b);
+    auto ev = cview(m.ask_verts_of(EDGE));
+    pfor(m.nents[FACE], [=] __device__(LO f) {
+      I8 r = 0;
+      for (int k = 0; k < 3; ++k) {
+        LO e = fe[f * 3 + k];
+        if (l[ev[e * 2]] || l[ev[e * 2 + 1]]) r = 1;
+      }
+      o[f] = r;
+    });
+    return out;
+  }
+  auto hl = cview(m.ask_down(hd, ld).ab2b);
+  int deg = simplex_degree(hd, ld);
   pfor(m.nents[hd], [=] __device__(LO h) {
     I8 r = 0;
     for (int k = 0; k < deg; ++k)
@@ -356,10 +370,10 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   // entities kept as they are (0/1 marks and their offsets); the three sizes
   // this function needs (kept, new, products) are read back together below
   bool some_mod = ent_dim >= key_dim;
-  Arr<I8> same;
+  Arr<I8> same, km;
   Arr<LO> same_offs;
   if (some_mod) {
-    Arr<I8> km = mark_image(keys2kds, om.nents[key_dim]);
+    km = mark_image(keys2kds, om.nents[key_dim]);
     Arr<I8> mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
     same = Arr<I8>(nold);
     auto me = cview(mods_ent);
@@ -375,7 +389,50 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     reps = Arr<LO>(nkeys);
     auto kd = cview(keys2kds);
     auto r = view(reps);
-    if (ent_dim > key_dim) {
+    if (ent_dim > key_dim && key_dim == VERT && !om.adj.count({VERT, ent_dim})) {
+      // The representative is the first entry of the key vertex's upward
+      // row, which lists entities in increasing order: the smallest entity
+      // index containing the vertex.  Without the rows at hand that is an
+      // atomic minimum over the entities' vertices (faces through their
+      // edges, so no face-vertex list is derived either).
+      LO nv = om.nverts(), nent = om.nents[ent_dim];
+      Arr<unsigned> vmin(nv);
+      OHG_CUDA(cudaMemsetAsync(vmin.data(), 0xff, size_t(nv) * sizeof(unsigned), ctx().stream));
+      auto vm = view(vmin);
+      auto kmv = cview(km);
+      if (ent_dim == FACE && !om.adj.count({FACE, VERT})) {
+        auto fe = cview(om.ask_down(FACE, EDGE).ab2b);
+        auto ev = cview(om.ask_verts_of(EDGE));
+        pfor(nent, [=] __device__(LO f) {
+          for (int k = 0; k < 3; ++k) {
+            LO e = fe[f * 3 + k];
+            for (int j = 0; j < 2; ++j) {
+              LO v = ev[e * 2 + j];
+              if (kmv[v]) atomicMin(&vm[v], unsigned(f));
+            }
+          }
+        });
+      } else {
+        auto hv = cview(om.ask_verts_of(ent_dim));
+        int nvh = ent_dim + 1;
+        pfor(nent, [=] __device__(LO h) {
+          for (int k = 0; k < nvh; ++k) {
+            LO v = hv[h * nvh + k];
+            if (kmv[v]) atomicMin(&vm[v], unsigned(h));
+          }
+        });
+      }
+      int* stw = ctx().d_status;
+      pfor(nkeys, [=] __device__(LO k) {
+        unsigned b = vm[kd[k]];
+        if (b == 0xffffffffu) {
+          raise_status(stw, ST_TOPOLOGY);
+          r[k] = 0;
+        } else {
+          r[k] = LO(b);
+        }
+      });
+    } else if (ent_dim > key_dim) {
       const Adj& up = om.ask_up(key_dim, ent_dim);
       auto ua = cview(up.a2ab);
       auto ub = cview(up.ab2b);
@@ -475,9 +532,16 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   LO nprods = out.prods2new.size();
   Adj pd;
   if (ld > VERT) {
-    const Arr<LO>& lv2v = nm.ask_verts_of(ld);
-    const Adj& v2l = nm.ask_up(VERT, ld);
-    pd = reflect_down(prod_verts2verts, nprods, lv2v, v2l, ent_dim, ld);
+    // the products' sides among the new mesh's entities of dimension ld:
+    // by a hash of their vertex tuples, so the new mesh's vertex-to-ld
+    // upward lists (otherwise built for this alone) are not derived
+    if (nm.nents[ld] < (LO(1) << 29)) {
+      pd = reflect_down_hashed(prod_verts2verts, nprods, nm.ask_verts_of(ld), nm.nents[ld],
+                               ent_dim, ld);
+    } else {  // the table size would pass the index range: upward lists
+      pd = reflect_down(prod_verts2verts, nprods, nm.ask_verts_of(ld), nm.ask_up(VERT, ld),
+                        ent_dim, ld);
+    }
   } else {
     pd.ab2b = prod_verts2verts;
   }

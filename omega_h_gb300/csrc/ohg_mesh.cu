@@ -209,6 +209,108 @@ Arr<LO> form_uses(const Arr<LO>& hv2v, LO nh, int hd, int ld) {
   return uv2v;
 }
 
+// ------------------------------------------------------------ hashed reflect_down
+// The same matches as reflect_down (src/Omega_h_adj.cpp:297-441) without the
+// low entities' upward lists: the low entities go into an open-addressing
+// table keyed by their sorted vertex tuple (the table holds entity numbers;
+// a probe compares the stored entity's vertices), and each use looks up its
+// own tuple.  Low entities are unique, so each tuple is stored once.  The
+// table has a power-of-two size of at least twice the entity count, so a
+// probe sequence meets a free slot within its length; both loops are also
+// bounded by the table size.
+__device__ __forceinline__ unsigned tuple_hash(const LO* sv, int deg) {
+  unsigned h = 0x9e3779b9u;
+  for (int j = 0; j < deg; ++j) {
+    h ^= unsigned(sv[j]) + 0x7f4a7c15u + (h << 6) + (h >> 2);
+    h *= 0x85ebca6bu;
+    h ^= h >> 15;
+  }
+  h ^= h >> 16;
+  h *= 0x7feb352du;
+  h ^= h >> 15;
+  return h;
+}
+__device__ __forceinline__ void sort_tuple(LO* v, int deg) {
+  if (v[0] > v[1]) { LO t = v[0]; v[0] = v[1]; v[1] = t; }
+  if (deg == 3) {
+    if (v[1] > v[2]) { LO t = v[1]; v[1] = v[2]; v[2] = t; }
+    if (v[0] > v[1]) { LO t = v[0]; v[0] = v[1]; v[1] = t; }
+  }
+}
+
+Adj reflect_down_hashed(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, LO nl, int hd, int ld) {
+  Ctx& c = ctx();
+  int nvh = hd + 1, nlh = simplex_degree(hd, ld), deg = ld + 1;
+  LO na = nh * nlh;
+  Adj out;
+  out.ab2b = Arr<LO>(na);
+  if (ld > 0) {
+    out.codes = Arr<I8>(na);
+    out.has_codes = true;
+  }
+  if (na == 0) return out;
+  LO tsize = 1;
+  while (tsize < 2 * nl || tsize < 64) tsize *= 2;
+  Arr<LO> table(tsize);
+  OHG_CUDA(cudaMemsetAsync(table.data(), 0xff, size_t(tsize) * sizeof(LO), c.stream));
+  unsigned tmask = unsigned(tsize - 1);
+  auto tab = view(table);
+  auto lv = cview(lv2v);
+  int* st = c.d_status;
+  pfor(nl, [=] __device__(LO l) {
+    LO sv[3];
+    for (int j = 0; j < deg; ++j) sv[j] = lv[l * deg + j];
+    sort_tuple(sv, deg);
+    unsigned slot = tuple_hash(sv, deg) & tmask;
+    for (LO probe = 0; probe <= LO(tmask); ++probe) {
+      if (atomicCAS(&tab[LO(slot)], -1, l) == -1) return;
+      slot = (slot + 1) & tmask;
+    }
+    raise_status(st, ST_NO_MATCH);  // unreachable with the table at most half full
+  });
+  auto h = cview(hv2v);
+  auto o = view(out.ab2b);
+  auto oc = view(out.codes);
+  bool with_codes = ld > 0;
+  pfor(na, [=] __device__(LO a) {
+    LO hh = a / nlh;
+    int uu = a % nlh;
+    LO av[3], sv[3];
+    for (int j = 0; j < deg; ++j) sv[j] = av[j] = h[hh * nvh + down_template(hd, ld, uu, j)];
+    sort_tuple(sv, deg);
+    unsigned slot = tuple_hash(sv, deg) & tmask;
+    for (LO probe = 0; probe <= LO(tmask); ++probe) {
+      LO l = tab[LO(slot)];
+      if (l < 0) break;
+      LO lw[3], ls[3];
+      for (int j = 0; j < deg; ++j) ls[j] = lw[j] = lv[l * deg + j];
+      sort_tuple(ls, deg);
+      bool same = ls[0] == sv[0] && ls[1] == sv[1] && (deg == 2 || ls[2] == sv[2]);
+      if (same) {
+        o[a] = l;
+        if (with_codes) {
+          // positions of av[0] and av[1] in the match give the alignment
+          int p0 = lw[0] == av[0] ? 0 : lw[1] == av[0] ? 1 : 2;
+          I8 code;
+          if (deg == 2) {
+            code = make_code(false, p0, 0);
+          } else {
+            int p1 = lw[0] == av[1] ? 0 : lw[1] == av[1] ? 1 : 2;
+            code = make_code(p1 != (p0 + 1) % 3, rotation_to_first(3, p0), 0);
+          }
+          oc[a] = code;
+        }
+        return;
+      }
+      slot = (slot + 1) & tmask;
+    }
+    raise_status(st, ST_NO_MATCH);
+    o[a] = 0;
+    if (with_codes) oc[a] = 0;
+  });
+  return out;
+}
+
 // reflect_down / find_matches (src/Omega_h_adj.cpp:297-441): one thread per
 // use scans the upward list of the use's vertex with the fewest entries.
 // With check_unique the whole list is scanned and a second match is an

@@ -68,6 +68,9 @@ struct Mesh {
 
 // adjacency derivation (src/Omega_h_adj.cpp)
 Adj invert_adj(const Adj& down, int nlows_per_high, LO nlows);
+// reflect_down by a hash table of the low entities' vertex tuples (entities
+// this library built: unique by construction); needs no upward adjacency
+Adj reflect_down_hashed(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, LO nl, int hd, int ld);
 // check_unique: scan every candidate and report a second match (arrays from
 // a caller); otherwise stop at the first
 Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l, int hd, int ld,
