@@ -127,7 +127,9 @@ int ohg_mesh_from_elems(ohg_context* ctx, int dim, int nverts, int nelems,
  * alignment codes codes_dev[d] for d >= 2), classification per dimension,
  * vertex coordinates and metric (Mesh::set_ents, src/Omega_h_mesh.cpp:87-95;
  * tags "class_dim", "class_id", "coordinates", "metric").  nents[d] entities
- * of each dimension; arrays are copied in. */
+ * of each dimension; arrays are copied in, from device or host memory (the
+ * kind is inferred from each address: pinned host memory is read by DMA),
+ * and the call returns after the copies completed. */
 int ohg_mesh_from_arrays(ohg_context* ctx, int dim, const int* nents,
                          const int* const* down_dev, const signed char* const* codes_dev,
                          const signed char* const* class_dim_dev,
@@ -166,6 +168,11 @@ int ohg_mesh_array_bytes(ohg_mesh* mesh, const char* name, long long* nbytes);
 /* copies a named array to dst, device memory or host memory (pinned host
  * memory is copied to by DMA); returns after the copy completed */
 int ohg_mesh_get_array(ohg_mesh* mesh, const char* name, void* dst, long long capacity_bytes);
+/* ohg_mesh_get_array for n arrays at once: names[i] into dsts[i] (capacity
+ * caps[i] bytes), all copies queued before one wait.  Every name and
+ * capacity is checked before any copy starts. */
+int ohg_mesh_get_arrays(ohg_mesh* mesh, int n, const char* const* names, void* const* dsts,
+                        const long long* caps);
 /* replaces vertex coordinates or metric ("coords" | "metric").  A metric of
  * nverts values is isotropic (the reference's one-component metric tag: its
  * scalar lengths, sizes, maxdet and log-Euclidean means are used), one of

@@ -99,6 +99,7 @@ SIGNATURES = {
     "ohg_mesh_nents": [c_void_p, c_int, P(c_int)],
     "ohg_mesh_array_bytes": [c_void_p, c_char_p, P(c_ll)],
     "ohg_mesh_get_array": [c_void_p, c_char_p, c_void_p, c_ll],
+    "ohg_mesh_get_arrays": [c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_mesh_set_array": [c_void_p, c_char_p, c_void_p, c_ll],
     "ohg_adapt_opts_default": [c_int, P(AdaptOpts)],
     "ohg_adapt_pass": [c_void_p, P(AdaptOpts), P(PassStats)],

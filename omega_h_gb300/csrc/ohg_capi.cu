@@ -211,6 +211,8 @@ int ohg_mesh_from_arrays(ohg_context* c, int dim, const int* nents, const int* c
     return OHG_ERR_INVALID;
   }
   ohg_mesh* m = new ohg_mesh{c, Mesh()};
+  // the arrays may be device or host memory (the copy kind is inferred from
+  // each address); the call returns after every copy completed
   int rc = guarded(c, [&] {
     Mesh& me = m->mesh;
     me.dim = dim;
@@ -221,13 +223,13 @@ int ohg_mesh_from_arrays(ohg_context* c, int dim, const int* nents, const int* c
       Adj a;
       a.ab2b = Arr<LO>(nents[d] * deg);
       OHG_CUDA(cudaMemcpyAsync(a.ab2b.data(), down[d], size_t(nents[d]) * deg * 4,
-                               cudaMemcpyDeviceToDevice, s));
+                               cudaMemcpyDefault, s));
       if (d >= 2) {
         if (!codes || !codes[d]) throw Error(OHG_ERR_INVALID, "missing alignment codes");
         a.codes = Arr<I8>(nents[d] * deg);
         a.has_codes = true;
         OHG_CUDA(cudaMemcpyAsync(a.codes.data(), codes[d], size_t(nents[d]) * deg,
-                                 cudaMemcpyDeviceToDevice, s));
+                                 cudaMemcpyDefault, s));
       }
       me.set_ents(d, std::move(a));
     }
@@ -235,16 +237,16 @@ int ohg_mesh_from_arrays(ohg_context* c, int dim, const int* nents, const int* c
       me.class_dim[d] = Arr<I8>(nents[d]);
       me.class_id[d] = Arr<LO>(nents[d]);
       OHG_CUDA(cudaMemcpyAsync(me.class_dim[d].data(), cdim[d], size_t(nents[d]),
-                               cudaMemcpyDeviceToDevice, s));
+                               cudaMemcpyDefault, s));
       OHG_CUDA(cudaMemcpyAsync(me.class_id[d].data(), cid[d], size_t(nents[d]) * 4,
-                               cudaMemcpyDeviceToDevice, s));
+                               cudaMemcpyDefault, s));
     }
     me.coords = Arr<double>(nents[0] * dim);
     me.metric = Arr<double>(nents[0] * me.mcomp());
     OHG_CUDA(cudaMemcpyAsync(me.coords.data(), coords, size_t(nents[0]) * dim * 8,
-                             cudaMemcpyDeviceToDevice, s));
+                             cudaMemcpyDefault, s));
     OHG_CUDA(cudaMemcpyAsync(me.metric.data(), metric, size_t(nents[0]) * me.mcomp() * 8,
-                             cudaMemcpyDeviceToDevice, s));
+                             cudaMemcpyDefault, s));
   });
   if (rc != OHG_OK) {
     delete m;
@@ -540,6 +542,41 @@ int ohg_mesh_get_array(ohg_mesh* m, const char* name, void* dst, long long cap) 
   if (rc == OHG_OK && !fits) {
     g_err = std::string("destination too small for ") + name;
     return OHG_ERR_BOUNDS;
+  }
+  return rc;
+}
+int ohg_mesh_get_arrays(ohg_mesh* m, int n, const char* const* names, void* const* dsts,
+                        const long long* caps) {
+  MESH_GUARD(m);
+  if (n < 0 || (n > 0 && (!names || !dsts || !caps))) {
+    g_err = "ohg_mesh_get_arrays: bad arguments";
+    return OHG_ERR_INVALID;
+  }
+  std::string bad;
+  int bad_rc = OHG_OK;
+  int rc = guarded(m->owner, [&] {
+    std::vector<Arr<GO>> tmps(static_cast<size_t>(n));
+    std::vector<const void*> ps(static_cast<size_t>(n));
+    std::vector<long long> bs(static_cast<size_t>(n));
+    for (int i = 0; i < n && bad_rc == OHG_OK; ++i) {
+      if (!names[i] || !named_array(m->mesh, names[i], &ps[i], &bs[i], &tmps[i])) {
+        bad = std::string("unknown mesh array ") + (names[i] ? names[i] : "(null)");
+        bad_rc = OHG_ERR_INVALID;
+      } else if (bs[i] > caps[i]) {
+        bad = std::string("destination too small for ") + names[i];
+        bad_rc = OHG_ERR_BOUNDS;
+      }
+    }
+    if (bad_rc != OHG_OK) return;
+    // every copy queued on the context's stream, one wait for all of them
+    for (int i = 0; i < n; ++i)
+      if (bs[i])
+        OHG_CUDA(cudaMemcpyAsync(dsts[i], ps[i], size_t(bs[i]), cudaMemcpyDefault, ctx().stream));
+    ctx().sync();
+  });
+  if (rc == OHG_OK && bad_rc != OHG_OK) {
+    g_err = bad;
+    return bad_rc;
   }
   return rc;
 }
