@@ -1955,12 +1955,16 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       auto vcd = cview(v2d.codes);
       auto dd = cview(dead[d]);
       auto kv = cview(k2v);
+      // one warp per key: the lanes stride the key vertex's row (rows of
+      // tens of entries, which one thread would walk alone)
       Arr<LO> cnt(nkeys);
       auto ct = view(cnt);
-      pfor(nkeys, [=] __device__(LO k) {
+      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+        if (k < 0) return;
         LO v = kv[k], n2 = 0;
-        for (LO x = va[v]; x < va[v + 1]; ++x) n2 += !dd[vb[x]];
-        ct[k] = n2;
+        for (LO x = va[v] + gl; x < va[v + 1]; x += 32) n2 += !dd[vb[x]];
+        n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
+        if (gl == 0) ct[k] = n2;
       });
       k2p = offset_scan(cnt);
       LO nprod = last(k2p);
@@ -1973,18 +1977,30 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       auto o2n = cview(ov2nv);
       auto kd = view(kd2d);
       auto pv = view(pv2v);
-      pfor(nkeys, [=] __device__(LO k) {
-        LO v = kv[k], p = kp[k];
-        for (LO x = va[v]; x < va[v + 1]; ++x) {
-          LO el = vb[x];
-          if (dd[el]) continue;
-          int ccv_col = code_which_down(vcd[x]);
-          kd[p] = el;
-          for (int ccv = 0; ccv < nccv; ++ccv) {
-            LO ov = ccv == ccv_col ? ko[k] : cv[el * nccv + ccv];
-            pv[p * nccv + ccv] = o2n[ov];
+      // the live entries in row order, ranked within each 32-entry step
+      // by a ballot: the positions a walk of the row would give them
+      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+        if (k < 0) return;
+        LO v = kv[k], p = kp[k], beg = va[v], end = va[v + 1];
+        for (LO x0 = beg; x0 < end; x0 += 32) {
+          LO x = x0 + gl;
+          LO el = 0;
+          bool live = false;
+          if (x < end) {
+            el = vb[x];
+            live = !dd[el];
           }
-          ++p;
+          unsigned lm = __ballot_sync(gm, live);
+          if (live) {
+            LO q = p + LO(__popc(lm & ((1u << gl) - 1u)));
+            int ccv_col = code_which_down(vcd[x]);
+            kd[q] = el;
+            for (int ccv = 0; ccv < nccv; ++ccv) {
+              LO ov = ccv == ccv_col ? ko[k] : cv[el * nccv + ccv];
+              pv[q * nccv + ccv] = o2n[ov];
+            }
+          }
+          p += LO(__popc(lm));
         }
       });
     }
