@@ -402,7 +402,64 @@ Adj reflect_down(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, const Adj& v2l
 }
 
 // transit (src/Omega_h_adj.cpp:443-510)
+// transit for a fixed (high, low) pair: one thread per high entity reads
+// its middle-dimension row once and writes all its low entities, with the
+// templates unrolled (the pairs are (2,0), (3,0) and (3,1))
+// entities of dimension t on a simplex of dimension f: C(f+1, t+1)
+constexpr int simplex_degree_c(int f, int t) {
+  return f == 3 ? (t == 0 ? 4 : t == 1 ? 6 : t == 2 ? 4 : 1)
+                : f == 2 ? (t == 2 ? 1 : 3) : f == 1 ? (t == 0 ? 2 : 1) : 1;
+}
+template <int HD, int LD>
+static void transit_fixed(const Adj& h2m, const Adj& m2l, LO nh, Adj& out) {
+  constexpr int MD = LD + 1;
+  constexpr int NMH = simplex_degree_c(HD, MD);
+  constexpr int NLM = simplex_degree_c(MD, LD);
+  constexpr int NLH = simplex_degree_c(HD, LD);
+  static_assert(HD - LD >= 2, "a transit skips at least one dimension");
+  auto hm = cview(h2m.ab2b);
+  auto hmc = cview(h2m.codes);
+  auto ml = cview(m2l.ab2b);
+  auto mlc = cview(m2l.codes);
+  auto o = view(out.ab2b);
+  auto oc = view(out.codes);
+  pfor(nh, [=] __device__(LO h) {
+    LO mrow[NMH];
+    I8 crow[NMH];
+#pragma unroll
+    for (int i = 0; i < NMH; ++i) {
+      mrow[i] = hm[h * NMH + i];
+      crow[i] = hmc[h * NMH + i];
+    }
+#pragma unroll
+    for (int hl = 0; hl < NLH; ++hl) {
+      UpTemplate ut = up_template0(HD, LD, hl);
+      LO m = mrow[ut.up];
+      I8 hm2m = invert_alignment(NLM, crow[ut.up]);
+      int mli = align_index(NLM, LD, ut.which_down, hm2m);
+      o[h * NLH + hl] = ml[m * NLM + mli];
+      if (LD == 1) {
+        bool f = code_is_flipped(hm2m) ^ (code_rotation(mlc[m * NLM + mli]) == 1) ^ ut.is_flipped;
+        oc[h * NLH + hl] = make_code(false, f, 0);
+      }
+    }
+  });
+}
+
 Adj transit(const Adj& h2m, const Adj& m2l, int hd, int ld, LO nh) {
+  if ((hd == 2 && ld == 0) || (hd == 3 && ld <= 1)) {
+    Adj out;
+    int nlh = simplex_degree(hd, ld);
+    out.ab2b = Arr<LO>(nh * nlh);
+    if (ld == 1) {
+      out.codes = Arr<I8>(nh * nlh);
+      out.has_codes = true;
+    }
+    if (hd == 2) transit_fixed<2, 0>(h2m, m2l, nh, out);
+    else if (ld == 0) transit_fixed<3, 0>(h2m, m2l, nh, out);
+    else transit_fixed<3, 1>(h2m, m2l, nh, out);
+    return out;
+  }
   int md = ld + 1;
   int nmh = simplex_degree(hd, md), nlm = simplex_degree(md, ld), nlh = simplex_degree(hd, ld);
   Adj out;
