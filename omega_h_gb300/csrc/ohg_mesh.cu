@@ -160,13 +160,11 @@ static void sort_rows_by_high(LO nlows, const Arr<LO>& off, Arr<LO>& lh2hl, Arr<
 // Degrees by atomics, offsets by scan, slots by atomics, then each row is
 // sorted by the high entity's use index so rows list high entities in
 // increasing order, the order the reference obtains with sort_by_high_index.
-Adj invert_adj(const Adj& down, int k, LO nlows) {
+Adj invert_adj(const Adj& down, int k, LO nlows, bool sorted) {
   LO nhl = down.ab2b.size();
   Arr<LO> deg = fill<LO>(nlows, 0);
   auto hl2l = cview(down.ab2b);
   auto dg = view(deg);
-  // Lanes of a warp that hit the same low entity (frequent: neighbouring
-  // high entities share low ones in the Hilbert order) add with one atomic.
   pfor(nhl, [=] __device__(LO hl) { atomicAdd(&dg[hl2l[hl]], 1); });
   Adj up;
   up.a2ab = offset_scan(deg);
@@ -185,6 +183,18 @@ Adj invert_adj(const Adj& down, int k, LO nlows) {
   auto lh2hl = view(up.ab2b);
   bool has_dc = down.has_codes;
   auto dc = cview(down.codes);
+  if (!sorted) {
+    // rows in atomic order: each slot gets its final entry and code here
+    auto uc = view(up.codes);
+    pfor(nhl, [=] __device__(LO hl) {
+      LO l = hl2l[hl];
+      int c = has_dc ? int(dc[hl] & 7) : 0;
+      LO j = off[l] + atomicAdd(&ps[l], 1);
+      lh2hl[j] = hl / k;
+      uc[j] = make_code(c & 1, (c >> 1) & 3, hl % k);
+    });
+    return up;
+  }
   pfor(nhl, [=] __device__(LO hl) {
     LO l = hl2l[hl];
     LO c = has_dc ? LO(dc[hl] & 7) : 0;
@@ -604,9 +614,22 @@ static Adj elements_across_sides(int dim, const Adj& e2s, const Adj& s2e, LO ne)
 void Mesh::set_ents(int d, Adj down) {
   nents[d] = down.ab2b.size() / simplex_degree(d, d - 1);
   adj[{d, d - 1}] = std::move(down);
+  adj_any_order.clear();
+}
+
+const Adj& Mesh::ask_up_any_order(int from, int to) {
+  auto it = adj.find({from, to});
+  if (it != adj.end()) return it->second;
+  auto jt = adj_any_order.find({from, to});
+  if (jt != adj_any_order.end()) return jt->second;
+  if (from < 0 || from >= to || to > dim) throw Error(8, "bad upward adjacency dimensions");
+  const Adj& down = ask_adj(to, from);
+  return adj_any_order[{from, to}] =
+             invert_adj(down, simplex_degree(to, from), nents[from], /*sorted=*/false);
 }
 
 void Mesh::drop_cache() {
+  adj_any_order.clear();
   for (auto it = adj.begin(); it != adj.end();) {
     if (it->first.second == it->first.first - 1)
       ++it;
@@ -629,8 +652,9 @@ const Adj& Mesh::ask_adj(int from, int to) {
     const Adj& m2l = ask_adj(to + 1, to);
     d = transit(h2m, m2l, from, to, nents[from]);
   } else if (from == dim) {
+    // a side's other element does not depend on the order of its row
     const Adj& e2s = ask_adj(dim, dim - 1);
-    const Adj& s2e = ask_adj(dim - 1, dim);
+    const Adj& s2e = ask_up_any_order(dim - 1, dim);
     d = elements_across_sides(dim, e2s, s2e, nents[dim]);
   } else if (from == VERT) {
     const Adj& e2v = ask_adj(EDGE, VERT);

@@ -30,6 +30,9 @@ struct Mesh {
   bool has_length = false, has_quality = false;
   Arr<double> length, quality;
   std::map<std::pair<int, int>, Adj> adj;
+  // upward adjacencies whose rows are in no particular order, for the
+  // consumers that do not depend on it (never returned by ask_adj)
+  std::map<std::pair<int, int>, Adj> adj_any_order;
   // state the reference writes to .osh files: its partitioning mode (0
   // element-based, 1 ghosted: set by the operators as the reference's are),
   // whether the tags are in the order a rebuild leaves them, the named sets
@@ -61,13 +64,17 @@ struct Mesh {
   const Adj& ask_down(int from, int to) { return ask_adj(from, to); }
   const Adj& ask_up(int from, int to) { return ask_adj(from, to); }
   const Arr<LO>& ask_verts_of(int d) { return ask_adj(d, 0).ab2b; }
+  // the sorted upward adjacency if it is at hand, else one with its rows in
+  // atomic order (no row sort)
+  const Adj& ask_up_any_order(int from, int to);
   const Arr<double>& ask_lengths();
   const Arr<double>& ask_qualities();
   void drop_cache();  // forget derived adjacencies (keeps stored down ones)
 };
 
 // adjacency derivation (src/Omega_h_adj.cpp)
-Adj invert_adj(const Adj& down, int nlows_per_high, LO nlows);
+// sorted = false leaves each row in the order its atomics gave it
+Adj invert_adj(const Adj& down, int nlows_per_high, LO nlows, bool sorted = true);
 // reflect_down by a hash table of the low entities' vertex tuples (entities
 // this library built: unique by construction); needs no upward adjacency
 Adj reflect_down_hashed(const Arr<LO>& hv2v, LO nh, const Arr<LO>& lv2v, LO nl, int hd, int ld);
