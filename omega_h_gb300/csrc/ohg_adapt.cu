@@ -612,7 +612,7 @@ void refine_qualities(Mesh& m, const LO* c2e_p, LO n, const double* mid_p, doubl
   int dim = m.dim, mc = m.mcomp();
   auto ev = cview(m.ask_verts_of(1));
   auto cv = cview(m.ask_verts_of(dim));
-  const Adj& e2c = m.ask_up(1, dim);
+  const Adj& e2c = m.ask_up_any_order(1, dim);  // a minimum over the row
   auto ea = cview(e2c.a2ab);
   auto eb = cview(e2c.ab2b);
   auto ec = cview(e2c.codes);
@@ -925,7 +925,7 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
   View<const I8> in = cview(ci_p, n);
   for (int cd = 2; cd <= m.dim; ++cd) {
     View<I8> out = cd == m.dim ? view(co_p, n) : view(tmp);
-    const Adj& e2c = m.ask_up(1, cd);
+    const Adj& e2c = m.ask_up_any_order(1, cd);  // flags only: row order is free
     auto ea = cview(e2c.a2ab);
     auto eb = cview(e2c.ab2b);
     auto ecc = cview(e2c.codes);
@@ -1914,7 +1914,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   dead[1] = mark_image(r2e, ne);
   for (int d = 2; d <= dim; ++d) dead[d] = fill<I8>(m.nents[d], 0);
   for (int cd = dim; cd > EDGE; --cd) {
-    const Adj& e2c = m.ask_up(1, cd);
+    const Adj& e2c = m.ask_up_any_order(1, cd);  // marks only: row order is free
     auto ea = cview(e2c.a2ab);
     auto eb = cview(e2c.ab2b);
     auto ecc = cview(e2c.codes);

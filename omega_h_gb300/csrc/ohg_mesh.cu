@@ -638,12 +638,38 @@ void Mesh::drop_cache() {
   }
 }
 
+// An upward adjacency built with its rows in atomic order, put into the
+// sorted order: each entry goes back to the key the sorted path sorts (the
+// use index hl = high * k + side, packed with the code) and the rows go
+// through the same row sort, so the result is the sorted inversion's.
+static void sort_any_order_rows(Adj& up, int k, LO nlows, const Adj& down) {
+  LO nhl = up.ab2b.size();
+  bool packed = nhl < (1 << 28);
+  auto ab = view(up.ab2b);
+  auto uc = cview(up.codes);
+  pfor(nhl, [=] __device__(LO j) {
+    I8 c = uc[j];
+    LO hl = ab[j] * k + code_which_down(c);
+    ab[j] = packed ? hl * 8 + LO(c & 7) : hl;
+  });
+  sort_rows_by_high(nlows, up.a2ab, up.ab2b, up.codes, k,
+                    packed ? nullptr : (down.has_codes ? down.codes.data() : nullptr), packed);
+}
+
 // Mesh::derive_adj (src/Omega_h_mesh.cpp:307-345)
 const Adj& Mesh::ask_adj(int from, int to) {
   auto it = adj.find({from, to});
   if (it != adj.end()) return it->second;
   if (from < 0 || to < 0 || from > dim || to > dim) throw Error(8, "bad adjacency dimensions");
   Adj d;
+  auto jt = from < to ? adj_any_order.find({from, to}) : adj_any_order.end();
+  if (jt != adj_any_order.end()) {
+    // already inverted for a consumer that ignores row order: sort it
+    d = std::move(jt->second);
+    adj_any_order.erase(jt);
+    sort_any_order_rows(d, simplex_degree(to, from), nents[from], ask_adj(to, from));
+    return adj[{from, to}] = std::move(d);
+  }
   if (from < to) {
     const Adj& down = ask_adj(to, from);
     d = invert_adj(down, simplex_degree(to, from), nents[from]);
