@@ -589,6 +589,45 @@ static Arr<T> xfer(const Arr<T>& old, const ModifyOut& mo, LO nnew, const Arr<T>
   return nd;
 }
 
+// class_dim and class_id of dimension d together, as xfer does for each:
+// products take their values (pcd/pci, or those of the old entities kd2d),
+// kept entities their old ones; two launches for both arrays
+static void xfer_class(Mesh& om, Mesh& nm, int d, const ModifyOut& mo, LO nnew, const I8* pcd,
+                       const LO* pci, const LO* kd2d) {
+  Arr<I8> cd(nnew);
+  Arr<LO> ci(nnew);
+  auto ocd = cview(om.class_dim[d]);
+  auto oci = cview(om.class_id[d]);
+  auto ncd = view(cd);
+  auto nci = view(ci);
+  LO np = mo.prods2new.size();
+  if (np) {
+    auto p2n = cview(mo.prods2new);
+    auto kd = cview(kd2d, kd2d ? np : 0);
+    auto pd = cview(pcd, pcd ? np : 0);
+    auto pi = cview(pci, pci ? np : 0);
+    bool gather = kd2d != nullptr;
+    pfor(np, [=] __device__(LO p) {
+      LO q = p2n[p];
+      if (gather) {
+        ncd[q] = ocd[kd[p]];
+        nci[q] = oci[kd[p]];
+      } else {
+        ncd[q] = pd[p];
+        nci[q] = pi[p];
+      }
+    });
+  }
+  auto s2o = cview(mo.same2old);
+  auto s2n = cview(mo.same2new);
+  pfor(mo.same2old.size(), [=] __device__(LO i) {
+    ncd[s2n[i]] = ocd[s2o[i]];
+    nci[s2n[i]] = oci[s2o[i]];
+  });
+  nm.class_dim[d] = cd;
+  nm.class_id[d] = ci;
+}
+
 static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& mo) {
   LO np = mo.prods2new.size();
   if (d == EDGE && om.has_length) {
@@ -850,8 +889,7 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* s
     Arr<LO> pci(np);
     inherit_refine(m, d, k2e, k2p, m.class_dim, pcd);
     inherit_refine(m, d, k2e, k2p, m.class_id, pci);
-    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
-    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
+    xfer_class(m, nm, d, mo, nnew, pcd.data(), pci.data(), nullptr);
     if (d == VERT) {
       Arr<double> pc(nkeys * dim);
       auto ev = cview(m.ask_verts_of(1));
@@ -2007,8 +2045,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
     ModifyOut mo = modify_ents_adapt(m, nm, d, VERT, k2v, k2p, pv2v, old_lows2new);
     LO nnew = nm.nents[d];
     if (d == VERT) ov2nv = mo.old2new;
-    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, unmap(kd2d, m.class_dim[d], 1), 1);
-    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, unmap(kd2d, m.class_id[d], 1), 1);
+    xfer_class(m, nm, d, mo, nnew, nullptr, nullptr, kd2d.data());
     if (d == VERT) {
       nm.coords = xfer(m.coords, mo, nnew, Arr<double>(), dim);
       nm.metric = xfer(m.metric, mo, nnew, Arr<double>(), m.mcomp());
@@ -2655,8 +2692,7 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
         }
       });
     }
-    nm.class_dim[d] = xfer(m.class_dim[d], mo, nnew, pcd, 1);
-    nm.class_id[d] = xfer(m.class_id[d], mo, nnew, pci, 1);
+    xfer_class(m, nm, d, mo, nnew, pcd.data(), pci.data(), nullptr);
     xfer_lengths_qualities(m, nm, d, mo);
     old_lows2new = mo.old2new;
   }

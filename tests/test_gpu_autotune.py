@@ -32,6 +32,13 @@ def _pass(ctx, n=24, kind=1, seed=5):
     return st, out
 
 
+def _counts(st):
+    """the pass statistics that do not depend on timing or on the launch
+    schedule (the independent-set rounds update their states in place, so
+    their count may vary; the set does not)"""
+    return {k: v for k, v in st.items() if not k.startswith("ms_") and k != "indset_rounds"}
+
+
 def _same(a, b):
     assert a.keys() == b.keys()
     for k in a:
@@ -47,8 +54,7 @@ def test_every_variant_gives_the_same_pass(ctx):
         for v in range(4):
             ctx.force_variant(v)
             st, out = _pass(ctx)
-            assert {k: v for k, v in st.items() if not k.startswith("ms_")} == \
-                {k: v for k, v in st0.items() if not k.startswith("ms_")}
+            assert _counts(st) == _counts(st0)
             _same(ref, out)
     finally:
         ctx.force_variant(None)

@@ -78,7 +78,9 @@ def test_mesh_from_host_arrays_equals_mesh_from_device_arrays(ctx):
         m.close()
     base.close()
     (s0, a0) = results[0]
-    counts = lambda st: {k: v for k, v in st.items() if not k.startswith("ms_")}  # noqa: E731
+    # timings and the schedule-dependent independent-set round count aside
+    counts = lambda st: {k: v for k, v in st.items()  # noqa: E731
+                         if not k.startswith("ms_") and k != "indset_rounds"}
     for st, a in results[1:]:
         assert counts(st) == counts(s0)
         for k in NAMES:
