@@ -302,6 +302,12 @@ int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev
  * their number into *count (host) */
 int ohg_collect_marked(ohg_context* ctx, const signed char* marks_dev, int n, int* out_dev,
                        int* count);
+/* Self-test of failure detection, no counterpart in the reference: runs the
+ * single-pass scan of n counts (n > 4096, device memory) with its first tile
+ * withheld, so the other tiles' bounded waits on it run out (under a second).
+ * Returns OHG_ERR_TIMEOUT when the limit works; the context stays usable.
+ * out_dev (n+1 ints) is scratch. */
+int ohg_selftest_scan_wait_limit(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
 /* offset_scan without any device allocation: no counterpart in the
  * reference.  For hosts that cannot let the library allocate at that moment
  * (their own arena owns the device memory, or they are recovering from an

@@ -133,6 +133,7 @@ SIGNATURES = {
     "ohg_hilbert_sort": [c_void_p, c_void_p, c_int, c_int, c_void_p],
     "ohg_offset_scan": [c_void_p, c_void_p, c_int, c_void_p],
     "ohg_collect_marked": [c_void_p, c_void_p, c_int, c_void_p, c_void_p],
+    "ohg_selftest_scan_wait_limit": [c_void_p, c_void_p, c_int, c_void_p],
     "ohg_screen_tet_qualities": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_screen_edge_lengths": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_context_set_screening": [c_void_p, c_int],

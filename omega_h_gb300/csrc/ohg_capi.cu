@@ -980,6 +980,9 @@ int ohg_collect_marked(ohg_context* c, const signed char* marks, int n, int* out
     *count = r.size();
   });
 }
+int ohg_selftest_scan_wait_limit(ohg_context* c, const int* counts, int n, int* out) {
+  return guarded(c, [&] { scan_wait_limit_selftest(counts, n, out); });
+}
 int ohg_offset_scan_noalloc(ohg_context* c, const int* counts, int n, int* out) {
   return guarded(c, [&] { offset_scan_fixed_scratch(counts, n, out); });
 }

@@ -480,6 +480,26 @@ static void launch_lookback(const T* in, LO n, LO* out, Arr<unsigned long long>&
 #endif
 }
 
+// Self-test of the look-back's wait limit: the scan of n counts (more than
+// one tile) with the first tile's ticket withheld, so no block ever
+// publishes tile 0 and the other tiles' waits on it run out.  The status
+// word then holds ST_STALL; out[i] for i in the first tile is not written.
+void scan_wait_limit_selftest(const LO* counts, LO n, LO* out) {
+  Ctx& c = ctx();
+  LO nb = (n + kScanTile - 1) / kScanTile;
+  if (nb < 2) throw Error(8, "scan wait-limit self-test: needs at least two tiles");
+  Arr<unsigned long long> st(nb + 2);
+  OHG_CUDA(cudaMemsetAsync(st.data(), 0, size_t(nb + 2) * sizeof(unsigned long long), c.stream));
+  unsigned long long first = 1;  // tickets start at tile 1
+  OHG_CUDA(cudaMemcpyAsync(st.data() + nb, &first, sizeof(first), cudaMemcpyHostToDevice,
+                           c.stream));
+  bool vec = aligned16(counts) && aligned16(out);
+  k_scan_lookback<LO, false><<<nb - 1, kScanThreads, 0, c.stream>>>(
+      counts, n, out, st.data(), nb, c.d_status, vec, reinterpret_cast<LO*>(st.data() + nb + 1));
+  c.launches += 1;
+  c.sync();
+}
+
 template <class T>
 static void scan_impl(const T* in, LO n, LO* out) {
   Ctx& c = ctx();

@@ -20,6 +20,10 @@ void offset_scan_into(const I8* counts, LO n, LO* out);
 void offset_scan_fixed_scratch(const LO* counts, LO n, LO* out);
 LO offset_scan_fixed_limit();
 
+// the single-pass scan with its first tile withheld, so that the other
+// tiles' bounded waits run out and raise ST_STALL (a test of the limit)
+void scan_wait_limit_selftest(const LO* counts, LO n, LO* out);
+
 // indices of nonzero marks (collect_marked, src/Omega_h_map.cpp:174-185)
 Arr<LO> collect_marked(const Arr<I8>& marks);
 LO count_marked(const Arr<I8>& marks);

@@ -90,3 +90,19 @@ def test_collect_marked_from_an_unaligned_start(ctx):
         got, cnt = _collect(ctx, marks)
         want = torch.nonzero(marks, as_tuple=False).flatten().to(torch.int32)
         assert cnt == want.numel() and torch.equal(got, want)
+
+
+def test_scan_wait_limit_reports_a_timeout_and_the_context_stays_usable(ctx):
+    """The look-back's waits are bounded: with the first tile withheld (a
+    status word nothing will set) the other tiles give up after their poll
+    limit, the call returns OHG_ERR_TIMEOUT, and the next scan is correct."""
+    import torch
+    from omega_h_gb300 import _lib
+    n = 3 * 4096
+    counts = torch.ones(n, dtype=torch.int32, device="cuda")
+    out = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    with pytest.raises(_lib.OhgError) as e:
+        _lib.call("ohg_selftest_scan_wait_limit", ctx.handle, _P(counts), n, _P(out))
+    assert e.value.code == 5  # OHG_ERR_TIMEOUT
+    _scan(ctx, counts, out)
+    assert torch.equal(out.cpu(), torch.arange(n + 1, dtype=torch.int32))
