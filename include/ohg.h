@@ -71,6 +71,9 @@ int ohg_context_destroy(ohg_context* ctx);
 int ohg_context_launches(ohg_context* ctx, unsigned long long* out);
 /* number of times the host has waited on the context's stream */
 int ohg_context_syncs(ohg_context* ctx, unsigned long long* out);
+/* number of device allocations the library has made on the context (no
+ * counterpart in the reference: the reference allocates through Read<T>) */
+int ohg_context_allocations(ohg_context* ctx, unsigned long long* out);
 /* the context's cudaStream_t, for callers that order their own work on it */
 int ohg_context_stream(ohg_context* ctx, void** stream_out);
 /* Measurement hooks (no counterpart in the reference): when on, named hot
@@ -315,8 +318,10 @@ int ohg_selftest_scan_wait_limit(ohg_context* ctx, const int* counts_dev, int n,
  * scan's tile sums live in one fixed device array per device, sized for at
  * most ohg_offset_scan_noalloc_limit() counts (4,194,304); larger n fails
  * with OHG_ERR_INVALID before any launch.  The first call on a device looks
- * up the array's address (make it before capturing the stream into a graph).
- * Nothing has to be zeroed beforehand.  Calls in flight on one device at the
+ * up the array's address; make that first call before any stream capture.
+ * Like every entry point here, the call waits for the context's stream
+ * before it returns (it reads the status word).  Nothing has to be zeroed
+ * beforehand.  Calls in flight on one device at the
  * same time (other streams, contexts or threads) race on the shared array:
  * order them. */
 int ohg_offset_scan_noalloc(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);

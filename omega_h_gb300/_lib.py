@@ -72,6 +72,7 @@ SIGNATURES = {
     "ohg_context_destroy": [c_void_p],
     "ohg_context_launches": [c_void_p, P(c_ull)],
     "ohg_context_syncs": [c_void_p, P(c_ull)],
+    "ohg_context_allocations": [c_void_p, P(c_ull)],
     "ohg_context_autotune": [c_void_p, c_int],
     "ohg_context_force_variant": [c_void_p, c_int],
     "ohg_context_tuning": [c_void_p, P(c_int)],

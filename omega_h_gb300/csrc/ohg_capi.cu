@@ -31,6 +31,16 @@ static int status_to_code(int st) {
   return OHG_OK;
 }
 
+// After a failed call the status bits it raised are cleared, so that they
+// are not reported again by the next call on the context.
+static void clear_status_after_error(ohg_context* c) {
+  try {
+    c->ctx.take_status();
+  } catch (Error&) {
+    cudaGetLastError();
+  }
+}
+
 // runs f with the context current; converts exceptions and device status
 template <class F>
 static int guarded(ohg_context* c, F f) {
@@ -40,6 +50,11 @@ static int guarded(ohg_context* c, F f) {
   }
   set_ctx(&c->ctx);
   try {
+    // every entry point runs with its context's device current, so that
+    // launches on the context's stream and device symbol lookups agree
+    int cur = -1;
+    OHG_CUDA(cudaGetDevice(&cur));
+    if (cur != c->ctx.device) OHG_CUDA(cudaSetDevice(c->ctx.device));
     f();
     int st = c->ctx.take_status();
     int code = status_to_code(st);
@@ -51,9 +66,11 @@ static int guarded(ohg_context* c, F f) {
   } catch (Error& e) {
     g_err = e.what();
     cudaGetLastError();
+    clear_status_after_error(c);
     return e.code;
   } catch (std::exception& e) {
     g_err = e.what();
+    clear_status_after_error(c);
     return OHG_ERR_INVALID;
   }
 }
@@ -91,6 +108,11 @@ int ohg_context_launches(ohg_context* c, unsigned long long* out) {
 int ohg_context_syncs(ohg_context* c, unsigned long long* out) {
   if (!c || !out) return OHG_ERR_INVALID;
   *out = c->ctx.syncs;
+  return OHG_OK;
+}
+int ohg_context_allocations(ohg_context* c, unsigned long long* out) {
+  if (!c || !out) return OHG_ERR_INVALID;
+  *out = c->ctx.allocs;
   return OHG_OK;
 }
 

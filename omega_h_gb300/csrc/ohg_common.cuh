@@ -85,6 +85,11 @@ struct Tuner {
   void release();
 };
 
+// pinned host scratch: small reads, with one slot kept for the status word
+// read beside scan totals
+constexpr int kPinnedInts = 32;
+constexpr int kPinnedStatusSlot = kPinnedInts - 1;
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -95,6 +100,7 @@ struct Ctx {
   int num_sms = 0;  // streaming multiprocessors of the device
   std::uint64_t launches = 0;
   std::uint64_t syncs = 0;  // host waits on the stream (sizes and flags read back)
+  std::uint64_t allocs = 0;  // device allocations made through dev_alloc
   // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
   int screening = 1;
   // screening counters: cavity tets screened, tets recomputed in FP64,

@@ -27,7 +27,7 @@ Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   OHG_CUDA(cudaMalloc(&d_status, sizeof(int)));
   OHG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
-  OHG_CUDA(cudaMallocHost(&h_pinned, 64));
+  OHG_CUDA(cudaMallocHost(&h_pinned, kPinnedInts * sizeof(int)));
   OHG_CUDA(cudaMalloc(&d_screen_counts, 4 * sizeof(unsigned long long)));
   OHG_CUDA(cudaMemset(d_screen_counts, 0, 4 * sizeof(unsigned long long)));
   cudaMemPool_t pool;
@@ -156,7 +156,9 @@ int Ctx::take_status() {
 
 void* dev_alloc(size_t bytes) {
   void* p = nullptr;
-  cudaError_t e = cudaMallocAsync(&p, bytes, ctx().stream);
+  Ctx& c = ctx();
+  ++c.allocs;
+  cudaError_t e = cudaMallocAsync(&p, bytes, c.stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     throw Error(6, "device allocation of " + std::to_string(bytes) + " bytes failed");
@@ -484,6 +486,8 @@ static void launch_lookback(const T* in, LO n, LO* out, Arr<unsigned long long>&
 // one tile) with the first tile's ticket withheld, so no block ever
 // publishes tile 0 and the other tiles' waits on it run out.  The status
 // word then holds ST_STALL; out[i] for i in the first tile is not written.
+// The total is then read the way every size is read back from a scan, so
+// the read itself must refuse it (Error 5, OHG_ERR_TIMEOUT).
 void scan_wait_limit_selftest(const LO* counts, LO n, LO* out) {
   Ctx& c = ctx();
   LO nb = (n + kScanTile - 1) / kScanTile;
@@ -497,7 +501,7 @@ void scan_wait_limit_selftest(const LO* counts, LO n, LO* out) {
   k_scan_lookback<LO, false><<<nb - 1, kScanThreads, 0, c.stream>>>(
       counts, n, out, st.data(), nb, c.d_status, vec, reinterpret_cast<LO*>(st.data() + nb + 1));
   c.launches += 1;
-  c.sync();
+  last(Arr<LO>::wrap(out, n + 1));
 }
 
 template <class T>
@@ -595,16 +599,40 @@ void offset_scan_fixed_scratch(const LO* counts, LO n, LO* out) {
 #endif
 }
 
-LO last(const Arr<LO>& a) { return get_elem(a, a.size() - 1); }
+// Sizes read back from scans come with the status word, copied in the same
+// wait.  A scan tile whose look-back gave up (ST_STALL) wrote offsets from an
+// incomplete prefix, so its offsets and the scan's total need not agree; no
+// array may then be sized from that total or filled through those offsets.
+static void queue_status_read(Ctx& c) {
+  OHG_CUDA(cudaMemcpyAsync(c.h_pinned + kPinnedStatusSlot, c.d_status, sizeof(int),
+                           cudaMemcpyDeviceToHost, c.stream));
+}
+static void check_no_stall(const Ctx& c) {
+  if (c.h_pinned[kPinnedStatusSlot] & ST_STALL)
+    throw Error(5, "a scan tile gave up waiting for its predecessor; its offsets and total "
+                   "are not used");
+}
+
+LO last(const Arr<LO>& a) {
+  Ctx& c = ctx();
+  OHG_CUDA(cudaMemcpyAsync(c.h_pinned, a.data() + a.size() - 1, sizeof(LO),
+                           cudaMemcpyDeviceToHost, c.stream));
+  queue_status_read(c);
+  c.sync();
+  check_no_stall(c);
+  return c.h_pinned[0];
+}
 
 void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out) {
   Ctx& c = ctx();
   int n = int(arrs.size());
-  if (n > 16) throw Error(8, "read_lasts: at most 16 arrays");
+  if (n > kPinnedStatusSlot) throw Error(8, "read_lasts: too many arrays");
   for (int i = 0; i < n; ++i)
     OHG_CUDA(cudaMemcpyAsync(c.h_pinned + i, arrs[i]->data() + arrs[i]->size() - 1, sizeof(LO),
                              cudaMemcpyDeviceToHost, c.stream));
+  queue_status_read(c);
   c.sync();
+  check_no_stall(c);
   for (int i = 0; i < n; ++i) out[i] = c.h_pinned[i];
 }
 
@@ -631,7 +659,9 @@ Arr<LO> collect_marked(const Arr<I8>& marks) {
   LO* cnt = nullptr;
   launch_lookback<I8, true>(marks.data(), n, out.data(), st, &cnt);
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
+  queue_status_read(c);
   c.sync();
+  check_no_stall(c);
   out.n = c.h_pinned[0];
   return out;
 }
@@ -643,7 +673,9 @@ LO count_marked(const Arr<I8>& marks) {
   LO* cnt = nullptr;
   launch_lookback<I8, true>(marks.data(), n, nullptr, st, &cnt);
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
+  queue_status_read(c);
   c.sync();
+  check_no_stall(c);
   return c.h_pinned[0];
 }
 

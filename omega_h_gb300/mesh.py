@@ -45,6 +45,12 @@ class Context:
         _lib.call("ohg_context_syncs", self.handle, ctypes.byref(v))
         return v.value
 
+    def allocations(self):
+        """Device allocations the library has made on this context."""
+        v = ctypes.c_ulonglong()
+        _lib.call("ohg_context_allocations", self.handle, ctypes.byref(v))
+        return v.value
+
     def autotune(self, mode):
         """Launch-shape autotuner: "off", "explore" or "frozen" (default)."""
         _lib.call("ohg_context_autotune", self.handle, {"off": 0, "explore": 1, "frozen": 2}[mode])

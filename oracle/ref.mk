@@ -4,11 +4,13 @@
 # CMake would generate, an options header of #define lines, is written here
 # with every optional backend (MPI, OpenMP, Kokkos, CUDA, zlib) switched off.
 #
-#   make -f oracle/ref.mk REF=/root/reference -j8
+#   make -f oracle/ref.mk REF=<reference source checkout> -j8
 #
 # Outputs (git-ignored): oracle/_ref/libomega_h_ref.a, oracle/_ref/ref_driver
 
-REF ?= /root/reference
+ifndef REF
+$(error REF must name the reference's source checkout)
+endif
 OUT := oracle/_ref
 CXX ?= g++
 CXXFLAGS := -O2 -std=c++17 -ffp-contract=off -fno-fast-math -w \

@@ -191,11 +191,12 @@ def run_case(name, spec):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("OMEGA_H_REFERENCE_SRC"),
+                    help="the reference's source checkout (or set OMEGA_H_REFERENCE_SRC)")
     ap.add_argument("cases", nargs="*")
     a = ap.parse_args()
-    if not os.path.isdir(a.ref):
-        sys.exit(f"reference sources not found at {a.ref}")
+    if not a.ref or not os.path.isdir(a.ref):
+        sys.exit(f"reference sources not found: pass --ref or set OMEGA_H_REFERENCE_SRC")
     build_ref(a.ref)
     for name in a.cases or list(CASES) + list(OSH_CASES) + ["metric:" + k for k in METRIC_CASES]:
         if name.startswith("metric:"):

@@ -64,6 +64,20 @@ def test_noalloc_scan_matches_allocating_scan_twice_in_a_row(ctx, n):
             assert torch.equal(got[1:].to(torch.int64), torch.cumsum(c64, 0))
 
 
+def test_noalloc_scan_allocates_nothing(ctx):
+    """The property the entry point exists for: after its first call on the
+    device (which looks up the scratch address), further calls make no
+    device allocation through the library, while the allocating scan does."""
+    counts = _counts(1_000_003, 11)
+    _scan(ctx, "ohg_offset_scan_noalloc", counts)
+    before = ctx.allocations()
+    for _ in range(3):
+        _scan(ctx, "ohg_offset_scan_noalloc", counts)
+    assert ctx.allocations() == before
+    _scan(ctx, "ohg_offset_scan", counts)
+    assert ctx.allocations() > before
+
+
 def test_noalloc_scan_rejects_sizes_beyond_its_scratch(ctx):
     from omega_h_gb300 import _lib
     lim = _limit()
