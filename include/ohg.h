@@ -261,6 +261,12 @@ int ohg_swap2d_qualities(ohg_mesh* mesh, double max_length_allowed, const int* c
 /* swap3d_qualities (src/Omega_h_swap3d.hpp:9-10) */
 int ohg_swap3d_qualities(ohg_mesh* mesh, double max_length_allowed, const int* cands2edges_dev,
                          int n, double* quals_dev, signed char* configs_dev);
+/* swap3d::find_loop (src/Omega_h_swap3d_loop.hpp:24-78) for n edges: the
+ * number of tets around each edge (0 when outside 3..7), the edge's two
+ * vertices (2 ints per edge) and the loop vertices ordered to curl around
+ * it (7 ints per edge, unused slots 0); device arrays */
+int ohg_swap3d_find_loops(ohg_mesh* mesh, const int* edges_dev, int n, int* sizes_dev,
+                          int* eev2v_dev, int* loop_verts_dev);
 /* find_indset over the mesh's star graph (src/Omega_h_indset.hpp:11-14) */
 int ohg_find_indset(ohg_mesh* mesh, int ent_dim, const double* quality_dev,
                     const signed char* candidates_dev, signed char* out_dev, int* rounds);
@@ -298,6 +304,14 @@ int ohg_sort_by_keys(ohg_context* ctx, const void* keys_dev, int n, int width, i
                      int* perm_dev);
 /* hilbert::sort_coords (src/Omega_h_hilbert.cpp:52-55) */
 int ohg_hilbert_sort(ohg_context* ctx, const double* coords_dev, int n, int dim, int* perm_dev);
+/* hilbert::AxestoTranspose then hilbert::untranspose
+ * (src/Omega_h_hilbert.hpp:65-117), Skilling's transform, for n points of
+ * dim (1..3) integer coordinates of bits (1..64) bits each: the Hilbert
+ * index as dim words of bits bits, most significant word first; device
+ * arrays of dim words per point.  A coordinate of more than bits bits sets
+ * OHG_ERR_BOUNDS. */
+int ohg_hilbert_transpose(ohg_context* ctx, const unsigned long long* axes_dev, int n, int dim,
+                          int bits, unsigned long long* keys_dev);
 /* offset_scan (src/Omega_h_int_scan.cpp:10-20): n+1 outputs */
 int ohg_offset_scan(ohg_context* ctx, const int* counts_dev, int n, int* out_dev);
 /* collect_marked (src/Omega_h_map.cpp:174-185): the indices i < n with
@@ -331,10 +345,23 @@ int ohg_offset_scan_noalloc_limit(int* max_counts);
  * Metrics are packed symmetric tensors per vertex: (xx, yy, zz, yx, zy, zx)
  * in 3D, (xx, yy, yx) in 2D; all pointers are device pointers.  Every
  * function computes in FP64 with the reference's operation order.  A
- * metric intersection whose less degenerate operand has an eigenvalue below
- * 1e-10 (Barral's degenerate cases) and a failed eigendecomposition set the
- * device status, returned as OHG_ERR_NUMERIC. */
-/* intersect_metrics (src/Omega_h_metric.cpp:536-557) */
+ * failed eigendecomposition sets the device status, returned as
+ * OHG_ERR_NUMERIC. */
+/* find_polynomial_roots (src/Omega_h_eigen.hpp:21-85) of n monic cubics
+ * x^3 + a_2 x^2 + a_1 x + a_0, coefficients (a_0, a_1, a_2) per cubic:
+ * the number of distinct roots, 3 roots and 3 multiplicities per cubic;
+ * roots closer than eps are merged (the reference's default is 1e-6, its
+ * eigensolver uses 5e-5) */
+int ohg_cubic_roots(ohg_context* ctx, int n, const double* coeffs_dev, double eps,
+                    int* nroots_dev, double* roots_dev, int* mults_dev);
+/* decompose_eigen (src/Omega_h_eigen.hpp:278-293) of n dim x dim matrices
+ * (dim 2 or 3) stored by columns: q (by columns) holds the eigenvectors, l
+ * the eigenvalues; a failed decomposition returns OHG_ERR_NUMERIC */
+int ohg_decompose_eigen(ohg_context* ctx, int dim, int n, const double* m_dev, double* q_dev,
+                        double* l_dev);
+/* intersect_metrics (src/Omega_h_metric.cpp:536-557), including Barral's
+ * degenerate cases where eigenvalues are below 1e-10
+ * (src/Omega_h_metric_intersect.hpp:25-212) */
 int ohg_intersect_metrics(ohg_context* ctx, int dim, int n, const double* a, const double* b,
                           double* out);
 /* clamp_metrics (src/Omega_h_metric.cpp:36-56): eigenvalues into

@@ -86,6 +86,8 @@ SIGNATURES = {
     "ohg_mesh_read_osh": [c_void_p, c_char_p, P(c_void_p)],
     "ohg_osh_zlib": [P(c_int)],
     "ohg_intersect_metrics": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p],
+    "ohg_cubic_roots": [c_void_p, c_int, c_void_p, c_double, c_void_p, c_void_p, c_void_p],
+    "ohg_decompose_eigen": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_clamp_metrics": [c_void_p, c_int, c_int, c_void_p, c_double, c_double, c_void_p],
     "ohg_hessian_metrics": [c_void_p, c_int, c_int, c_void_p, c_double, c_void_p],
     "ohg_mesh_implied_metrics": [c_void_p, c_void_p],
@@ -124,6 +126,7 @@ SIGNATURES = {
     "ohg_mark_sliver_layers": [c_void_p, c_double, c_int, c_void_p],
     "ohg_swap2d_qualities": [c_void_p, c_double, c_void_p, c_int, c_void_p],
     "ohg_swap3d_qualities": [c_void_p, c_double, c_void_p, c_int, c_void_p, c_void_p],
+    "ohg_swap3d_find_loops": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_find_indset": [c_void_p, c_int, c_void_p, c_void_p, c_void_p, P(c_int)],
     "ohg_time_stage": [c_void_p, c_char_p, c_int, P(ctypes.c_float), P(c_double)],
     "ohg_invert_adj": [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p],
@@ -132,6 +135,7 @@ SIGNATURES = {
     "ohg_find_indset_graph": [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P(c_int)],
     "ohg_sort_by_keys": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p],
     "ohg_hilbert_sort": [c_void_p, c_void_p, c_int, c_int, c_void_p],
+    "ohg_hilbert_transpose": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p],
     "ohg_offset_scan": [c_void_p, c_void_p, c_int, c_void_p],
     "ohg_collect_marked": [c_void_p, c_void_p, c_int, c_void_p, c_void_p],
     "ohg_selftest_scan_wait_limit": [c_void_p, c_void_p, c_int, c_void_p],

@@ -2182,6 +2182,21 @@ static void swap_loops(Mesh& m, const LO* edges_p, LO n, Arr<int>& lsize, Arr<LO
   });
 }
 
+void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO* loop_verts) {
+  if (m.dim != 3) throw Error(8, "swap3d loops: the mesh is not 3D");
+  if (n == 0) return;
+  Arr<int> lsize;
+  Arr<LO> lverts, leev;
+  swap_loops(m, edges, n, lsize, lverts, leev);
+  Ctx& c = ctx();
+  OHG_CUDA(cudaMemcpyAsync(sizes, lsize.data(), size_t(n) * sizeof(int), cudaMemcpyDeviceToDevice,
+                           c.stream));
+  OHG_CUDA(cudaMemcpyAsync(eev2v, leev.data(), size_t(n) * 2 * sizeof(LO),
+                           cudaMemcpyDeviceToDevice, c.stream));
+  OHG_CUDA(cudaMemcpyAsync(loop_verts, lverts.data(), size_t(n) * 7 * sizeof(LO),
+                           cudaMemcpyDeviceToDevice, c.stream));
+}
+
 // swap3d_qualities + swap3d::choose (src/Omega_h_swap3d_qualities.cpp:10-58,
 // src/Omega_h_swap3d_choice.hpp:15-100).  The reference evaluates unique
 // triangles and edges lazily per candidate; here every unique triangle's two

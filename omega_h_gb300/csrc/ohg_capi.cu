@@ -844,6 +844,15 @@ int ohg_swap3d_qualities(ohg_mesh* m, double ml, const int* c2e, int n, double* 
   if (m->mesh.dim != 3) return OHG_ERR_INVALID;
   return guarded(m->owner, [&] { swap3d_qualities(m->mesh, ml, c2e, n, q, cf); });
 }
+int ohg_swap3d_find_loops(ohg_mesh* m, const int* edges, int n, int* sizes, int* eev2v,
+                          int* loop_verts) {
+  MESH_GUARD(m);
+  if (m->mesh.dim != 3 || n < 0 || (n > 0 && (!edges || !sizes || !eev2v || !loop_verts))) {
+    g_err = "ohg_swap3d_find_loops: needs a 3D mesh, n >= 0 and non-null arrays";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(m->owner, [&] { swap3d_find_loops(m->mesh, edges, n, sizes, eev2v, loop_verts); });
+}
 int ohg_find_indset(ohg_mesh* m, int d, const double* q, const signed char* cands,
                     signed char* out, int* rounds) {
   MESH_GUARD(m);
@@ -986,6 +995,17 @@ int ohg_hilbert_sort(ohg_context* c, const double* coords, int n, int dim, int* 
     OHG_CUDA(cudaMemcpyAsync(perm, p.data(), size_t(n) * 4, cudaMemcpyDeviceToDevice, ctx().stream));
   });
 }
+int ohg_hilbert_transpose(ohg_context* c, const unsigned long long* axes, int n, int dim, int bits,
+                          unsigned long long* keys) {
+  if (n < 0 || dim < 1 || dim > 3 || bits < 1 || bits > 64 || (n > 0 && (!axes || !keys))) {
+    g_err = "ohg_hilbert_transpose: bad arguments";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] {
+    hilbert_transpose_keys(reinterpret_cast<const std::uint64_t*>(axes), n, dim, bits,
+                           reinterpret_cast<std::uint64_t*>(keys));
+  });
+}
 int ohg_offset_scan(ohg_context* c, const int* counts, int n, int* out) {
   return guarded(c, [&] { offset_scan_into(counts, n, out); });
 }
@@ -1025,6 +1045,21 @@ static bool metric_args(int dim, int n) {
     return false;
   }
   return true;
+}
+int ohg_cubic_roots(ohg_context* c, int n, const double* coeffs, double eps, int* nroots,
+                    double* roots, int* mults) {
+  if (n < 0 || (n > 0 && (!coeffs || !nroots || !roots || !mults)) || !(eps >= 0.0)) {
+    g_err = "ohg_cubic_roots: bad arguments";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] { cubic_roots_batch(n, coeffs, eps, nroots, roots, mults); });
+}
+int ohg_decompose_eigen(ohg_context* c, int dim, int n, const double* m, double* q, double* l) {
+  if ((dim != 2 && dim != 3) || n < 0 || (n > 0 && (!m || !q || !l))) {
+    g_err = "ohg_decompose_eigen: dim must be 2 or 3, with n >= 0 and non-null arrays";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] { decompose_eigen_batch(dim, n, m, q, l); });
 }
 int ohg_intersect_metrics(ohg_context* c, int dim, int n, const double* a, const double* b,
                           double* out) {

@@ -363,8 +363,56 @@ OHG_HD V3 single_eigvec3(const M3& m, double l, bool* ok) {
   if (!(vn > 1e-10)) *ok = false;
   return {{v.x[0] / vn, v.x[1] / vn, v.x[2] / vn}};
 }
-OHG_HD Eig3 eigen3(M3 m) {
+// find_polynomial_roots of x^3 + a_2 x^2 + a_1 x + a_0 with real roots
+// (src/Omega_h_eigen.hpp:21-85): Cardano's formula when the discriminant D
+// is >= 0, else the trigonometric form; roots closer than eps are merged,
+// a pair first (into slots 1 and 2, averaged), then all three.  Returns the
+// number of distinct roots; mult[] holds the multiplicities.
+OHG_HD int cubic_roots(double a_0, double a_1, double a_2, double eps, double rt[3], int mult[3]) {
   const double PI = 3.14159265358979323;
+  double p = (3. * a_1 - sq(a_2)) / 3.;
+  double q = (9. * a_1 * a_2 - 27. * a_0 - 2. * cube(a_2)) / 27.;
+  double Q = p / 3.;
+  double R = q / 2.;
+  double D = cube(Q) + sq(R);
+  double shift = -a_2 / 3.;
+  if (D >= 0.0) {
+    double S = cbrt(R + sqrt(D));
+    double T = cbrt(R - sqrt(D));
+    double B = S + T;
+    rt[0] = shift + B;
+    rt[1] = rt[2] = shift - (1. / 2.) * B;
+  } else {
+    double ct = R / sqrt(-cube(Q));
+    double theta = acos(min2d(max2d(ct, -1.0), 1.0));
+    double radius = 2. * sqrt(-Q);
+    rt[0] = radius * cos((theta) / 3.) + shift;
+    rt[1] = radius * cos((theta + 2. * PI) / 3.) + shift;
+    rt[2] = radius * cos((theta - 2. * PI) / 3.) + shift;
+  }
+  mult[0] = mult[1] = mult[2] = 1;
+  if (fabs(rt[0] - rt[1]) < eps) {
+    double t = rt[0];
+    rt[0] = rt[2];
+    rt[2] = t;
+  } else if (fabs(rt[0] - rt[2]) < eps) {
+    double t = rt[0];
+    rt[0] = rt[1];
+    rt[1] = t;
+  } else if (!(fabs(rt[1] - rt[2]) < eps)) {
+    return 3;
+  }
+  rt[1] = (rt[1] + rt[2]) / 2;
+  mult[1] = 2;
+  if (fabs(rt[0] - rt[1]) < eps) {
+    rt[0] = (1. / 3.) * rt[0] + (2. / 3.) * rt[1];
+    mult[0] = 3;
+    return 1;
+  }
+  return 2;
+}
+
+OHG_HD Eig3 eigen3(M3 m) {
   Eig3 r;
   r.ok = true;
   double nm = 0.0;
@@ -387,53 +435,9 @@ OHG_HD Eig3 eigen3(M3 m) {
   double a_2 = -tA;
   double a_1 = (1. / 2.) * ((tA * tA) - t2);
   double a_0 = -det3(m);
-  double p = (3. * a_1 - sq(a_2)) / 3.;
-  double q = (9. * a_1 * a_2 - 27. * a_0 - 2. * cube(a_2)) / 27.;
-  double Q = p / 3.;
-  double R = q / 2.;
-  double D = cube(Q) + sq(R);
-  double shift = -a_2 / 3.;
   double rt[3];
-  if (D >= 0.0) {
-    double S = cbrt(R + sqrt(D));
-    double T = cbrt(R - sqrt(D));
-    double B = S + T;
-    rt[0] = shift + B;
-    rt[1] = rt[2] = shift - (1. / 2.) * B;
-  } else {
-    double ct = R / sqrt(-cube(Q));
-    double theta = acos(min2d(max2d(ct, -1.0), 1.0));
-    double radius = 2. * sqrt(-Q);
-    rt[0] = radius * cos((theta) / 3.) + shift;
-    rt[1] = radius * cos((theta + 2. * PI) / 3.) + shift;
-    rt[2] = radius * cos((theta - 2. * PI) / 3.) + shift;
-  }
-  const double eps = 5e-5;
-  int nroots;
-  if (fabs(rt[0] - rt[1]) < eps) {
-    double t = rt[0];
-    rt[0] = rt[2];
-    rt[2] = t;
-    nroots = 0;
-  } else if (fabs(rt[0] - rt[2]) < eps) {
-    double t = rt[0];
-    rt[0] = rt[1];
-    rt[1] = t;
-    nroots = 0;
-  } else if (fabs(rt[1] - rt[2]) < eps) {
-    nroots = 0;
-  } else {
-    nroots = 3;
-  }
-  if (nroots == 0) {
-    rt[1] = (rt[1] + rt[2]) / 2;
-    if (fabs(rt[0] - rt[1]) < eps) {
-      rt[0] = (1. / 3.) * rt[0] + (2. / 3.) * rt[1];
-      nroots = 1;
-    } else {
-      nroots = 2;
-    }
-  }
+  int mult[3];
+  int nroots = cubic_roots(a_0, a_1, a_2, 5e-5, rt, mult);
   if (nroots == 3) {
     for (int i = 0; i < 3; ++i) {
       r.q.c[i] = single_eigvec3(m, rt[i], &r.ok);

@@ -945,6 +945,32 @@ __device__ void hilbert_axes_to_transpose(std::uint64_t* X, int b, int n) {
   for (int i = 0; i < n; i++) X[i] ^= t;
 }
 
+// untranspose (src/Omega_h_hilbert.hpp:112-117): the transposed form's bits,
+// most significant first and interleaved across the axes, as dim words of
+// b bits each
+__device__ void hilbert_untranspose(const std::uint64_t* X, std::uint64_t* Y, int b, int n) {
+  for (int j = 0; j < n; ++j) Y[j] = 0;
+  for (int i = 0; i < b * n; ++i)
+    Y[i / b] |= (((X[i % n] >> (b - 1 - (i / n))) & 1) << (b - 1 - (i % b)));
+}
+
+void hilbert_transpose_keys(const std::uint64_t* axes_p, LO n, int dim, int bits,
+                            std::uint64_t* keys_p) {
+  auto ax = cview(axes_p, n * dim);
+  auto k = view(keys_p, n * dim);
+  int* st = ctx().d_status;
+  pfor(n, [=] __device__(LO i) {
+    std::uint64_t X[3], Y[3];
+    for (int j = 0; j < dim; ++j) {
+      X[j] = ax[i * dim + j];
+      if (bits < 64 && (X[j] >> bits) != 0) raise_status(st, ST_BOUNDS);
+    }
+    hilbert_axes_to_transpose(X, bits, dim);
+    hilbert_untranspose(X, Y, bits, dim);
+    for (int j = 0; j < dim; ++j) k[i * dim + j] = Y[j];
+  });
+}
+
 Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim) {
   double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
   for (int j = 0; j < dim; ++j) {
@@ -981,9 +1007,7 @@ Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim) {
       if (X[j] >= (std::uint64_t(1) << nbits)) X[j] = (std::uint64_t(1) << nbits) - 1;
     }
     hilbert_axes_to_transpose(X, nbits, dim);
-    for (int j = 0; j < dim; ++j) Y[j] = 0;
-    for (int b = 0; b < nbits * dim; ++b)
-      Y[b / nbits] |= (((X[b % dim] >> (nbits - 1 - (b / dim))) & 1) << (nbits - 1 - (b % nbits)));
+    hilbert_untranspose(X, Y, nbits, dim);
     for (int j = 0; j < dim; ++j) k[i * dim + j] = GO(Y[j]);
   });
   return keys;

@@ -89,6 +89,8 @@ Arr<LO> find_unique(const Arr<LO>& hv2v, LO nh, int hd, int ld);
 // construction: box mesh, Hilbert renumbering, box classification
 Mesh build_box(int dim, int n);
 Arr<GO> hilbert_keys(const Arr<double>& coords, LO n, int dim);
+void hilbert_transpose_keys(const std::uint64_t* axes, LO n, int dim, int bits,
+                            std::uint64_t* keys);
 Arr<LO> hilbert_sort(const Arr<double>& coords, LO n, int dim);
 void reorder_by_hilbert(Mesh& m);
 void classify_box(Mesh& m, int n);

@@ -4,7 +4,7 @@
 // (eigendecomposition, inverse, Householder QR, log/exp of an SPD tensor)
 // in the reference's operation order, so that the discrete decisions inside
 // them (the eigen solver's root merging, the clamps) come out the same:
-//   intersect_metrics   Barral's simultaneous reduction, non-degenerate path
+//   intersect_metrics   Barral's simultaneous reduction and degenerate cases
 //   clamp_metrics       eigenvalues clamped to [1/h_max^2, 1/h_min^2]
 //   hessian_metrics     Alauzet-Frey: |eigenvalues| d^2 / (2 (d+1)^2 eps)
 //   implied_metrics     each element's unit-edge metric, log-averaged to
@@ -129,17 +129,194 @@ OHG_HD void unsymm2(const M2& s, double* v) {
   v[2] = s.c[1].x[0];
 }
 
-// metric intersection (src/Omega_h_metric_intersect.hpp:215-262), the path
-// where the less degenerate metric has no eigenvalue below 1e-10 (edges
-// shorter than about 1e5); *degen is set for the degenerate cases, which
-// are not computed here
-OHG_HD M3 intersect3(M3 m1, M3 m2, bool* degen, bool* ok) {
+// ------------------------------------------------------------ intersection
+// Metric intersection (src/Omega_h_metric_intersect.hpp:215-262): Barral's
+// simultaneous reduction when the less degenerate metric has no eigenvalue
+// below 1e-10, else the degenerate cases of Barral's dissertation, appendix
+// A (src/Omega_h_metric_intersect.hpp:25-212): 2D case 5; 3D cases 2
+// (both metrics rank 1), 3 (ranks 2 and 1) and 4 (both rank 2).  Products
+// are taken in the reference's order, so the discrete choices (orthogonality
+// tests, which eigenvector is which) fall the same way.
+OHG_HD double dot2(V2 a, V2 b) {
+  double o = a.x[0] * b.x[0];
+  o = o + (a.x[1] * b.x[1]);
+  return o;
+}
+OHG_HD M2 outer2(V2 a, V2 b) {
+  M2 c;
+  for (int j = 0; j < 2; ++j)
+    for (int i = 0; i < 2; ++i) c.c[j].x[i] = a.x[i] * b.x[j];
+  return c;
+}
+OHG_HD M3 outer3(V3 a, V3 b) {
+  M3 c;
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) c.c[j].x[i] = a.x[i] * b.x[j];
+  return c;
+}
+OHG_HD V3 normalize3(V3 v) {
+  double n = sqrt(dot3(v, v));
+  return {{v.x[0] / n, v.x[1] / n, v.x[2] / n}};
+}
+// transpose(P^-1) diag(l) P^-1
+OHG_HD M3 congruent_diag3(const M3& p, V3 l) {
+  M3 pi = inv3(p);
+  return mm3(mm3(tr3(pi), diag3(l)), pi);
+}
+
+OHG_HD M2 intersect2(M2 m1, M2 m2, bool* ok);
+
+// Two metrics of rank 2 in 3D reduced to the plane of the first one's
+// non-degenerate eigenvectors u and v, intersected there and lifted back:
+// P (3x2) = [u v]; P (intersect(P^T m1 P, P^T m2 P)) P^T (cases 3.a and 4.a)
+OHG_HD M3 intersect_in_plane3(const M3& m1, const M3& m2, V3 u, V3 v, bool* ok) {
+  V3 p[2] = {u, v};
+  M2 mb[2];
+  for (int k = 0; k < 2; ++k) {
+    const M3& m = k == 0 ? m1 : m2;
+    for (int j = 0; j < 2; ++j) {
+      V3 x = mv3(m, p[j]);  // column j of m P
+      // column j of P^T (m P): sum over the 3 columns of P^T
+      V2 c;
+      for (int i = 0; i < 2; ++i) c.x[i] = p[i].x[0] * x.x[0];
+      for (int r = 1; r < 3; ++r)
+        for (int i = 0; i < 2; ++i) c.x[i] = c.x[i] + p[i].x[r] * x.x[r];
+      mb[k].c[j] = c;
+    }
+  }
+  M2 mi = intersect2(mb[0], mb[1], ok);
+  // Y (2x3) = mi P^T: column r = mi[0] P^T[r][0] + mi[1] P^T[r][1]
+  V2 y[3];
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < 2; ++i)
+      y[r].x[i] = mi.c[0].x[i] * p[0].x[r] + mi.c[1].x[i] * p[1].x[r];
+  M3 out;
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < 3; ++i) out.c[r].x[i] = p[0].x[i] * y[r].x[0] + p[1].x[i] * y[r].x[1];
+  return out;
+}
+
+// Barral's case 5: one eigenvalue of each 2D metric below 1e-10
+OHG_HD M2 intersect_degen2(const M2& m1, const Eig2& d1, const int* g1, const M2& m2,
+                           const Eig2& d2, const int* g2) {
+  V2 u1 = {{0, 0}}, v1 = {{0, 0}}, v2 = {{0, 0}};
+  double l1 = -1.0, l2 = -1.0;
+  for (int i = 0; i < 2; ++i) {
+    if (g1[i]) {
+      v1 = d1.q.c[i];
+    } else {
+      u1 = d1.q.c[i];
+      l1 = d1.l.x[i];
+    }
+    if (g2[i]) v2 = d2.q.c[i];
+    else l2 = d2.l.x[i];
+  }
+  if (dot2(v1, v2) < kEps) return scale2(outer2(u1, u1), max2d(l1, l2));  // 5.a
+  M2 p;  // 5.b
+  p.c[0] = v1;
+  p.c[1] = v2;
+  M2 pi = inv2(p);
+  V2 l;
+  l.x[0] = dot2(v1, mv2(m2, v1));
+  l.x[1] = dot2(v2, mv2(m1, v2));
+  return mm2(mm2(tr2(pi), diag2(l)), pi);
+}
+
+// Barral's cases 2-4 in 3D; m1 is the less degenerate metric (n1 <= n2)
+OHG_HD M3 intersect_degen3(const M3& m1, const Eig3& d1, const int* g1, int n1, const M3& m2,
+                           const Eig3& d2, const int* g2, int n2, bool* ok) {
+  const V3 z = {{0, 0, 0}};
+  if (n1 == 2 && n2 == 2) {
+    V3 u1 = z, u2 = z;
+    double l1 = -1.0, l2 = -1.0;
+    for (int i = 0; i < 3; ++i) {
+      if (!g1[i]) {
+        u1 = d1.q.c[i];
+        l1 = d1.l.x[i];
+      }
+      if (!g2[i]) {
+        u2 = d2.q.c[i];
+        l2 = d2.l.x[i];
+      }
+    }
+    V3 u = cross3(u1, u2);
+    if (dot3(u, u) < kEps) return scale3(outer3(u1, u1), max2d(l1, l2));  // 2.a
+    u = normalize3(u);  // 2.b
+    V3 e1 = cross3(u1, u), e2 = cross3(u2, u);
+    M3 p;
+    p.c[0] = e1;
+    p.c[1] = e2;
+    p.c[2] = u;
+    V3 l = {{dot3(e1, mv3(m2, e1)), dot3(e2, mv3(m1, e2)), 0.0}};
+    return congruent_diag3(p, l);
+  }
+  if (n1 == 1 && n2 == 2) {
+    V3 u1 = z, v1 = z, w1 = z, u2 = z, v2 = z, w2 = z;
+    bool found_u1 = false, found_v2 = false;
+    for (int i = 0; i < 3; ++i) {
+      if (g1[i]) {
+        w1 = d1.q.c[i];
+      } else if (found_u1) {
+        v1 = d1.q.c[i];
+      } else {
+        u1 = d1.q.c[i];
+        found_u1 = true;
+      }
+      if (!g2[i]) {
+        u2 = d2.q.c[i];
+      } else if (found_v2) {
+        w2 = d2.q.c[i];
+      } else {
+        v2 = d2.q.c[i];
+        found_v2 = true;
+      }
+    }
+    if (dot3(u2, w1) < kEps) return intersect_in_plane3(m1, m2, u1, v1, ok);  // 3.a
+    M3 p;  // 3.b
+    p.c[0] = v2;
+    p.c[1] = w2;
+    p.c[2] = w1;
+    V3 l = {{dot3(p.c[0], mv3(m1, p.c[0])), dot3(p.c[1], mv3(m1, p.c[1])),
+             dot3(p.c[2], mv3(m2, p.c[2]))}};
+    return congruent_diag3(p, l);
+  }
+  if (n1 == 1 && n2 == 1) {
+    V3 u1 = z, v1 = z, w1 = z, w2 = z;
+    bool found_u1 = false;
+    for (int i = 0; i < 3; ++i) {
+      if (g1[i]) {
+        w1 = d1.q.c[i];
+      } else if (found_u1) {
+        v1 = d1.q.c[i];
+      } else {
+        u1 = d1.q.c[i];
+        found_u1 = true;
+      }
+      if (g2[i]) w2 = d2.q.c[i];
+    }
+    V3 w = cross3(w1, w2);
+    if (dot3(w, w) < kEps) return intersect_in_plane3(m1, m2, u1, v1, ok);  // 4.a
+    w = normalize3(w);  // 4.b
+    M3 p;
+    p.c[0] = w1;
+    p.c[1] = w2;
+    p.c[2] = w;
+    V3 l = {{dot3(p.c[0], mv3(m2, p.c[0])), dot3(p.c[1], mv3(m1, p.c[1])),
+             max2d(dot3(p.c[2], mv3(m1, p.c[2])), dot3(p.c[2], mv3(m2, p.c[2])))}};
+    return congruent_diag3(p, l);
+  }
+  return m1;
+}
+
+OHG_HD M3 intersect3(M3 m1, M3 m2, bool* ok) {
   Eig3 d1 = eigen3(m1), d2 = eigen3(m2);
   *ok = *ok && d1.ok && d2.ok;
-  int n1 = 0, n2 = 0;
+  int g1[3], g2[3], n1 = 0, n2 = 0;
   for (int i = 0; i < 3; ++i) {
-    n1 += d1.l.x[i] < kEps;
-    n2 += d2.l.x[i] < kEps;
+    g1[i] = d1.l.x[i] < kEps;
+    g2[i] = d2.l.x[i] < kEps;
+    n1 += g1[i];
+    n2 += g2[i];
   }
   if (n1 > n2) {
     M3 t = m1;
@@ -148,15 +325,17 @@ OHG_HD M3 intersect3(M3 m1, M3 m2, bool* degen, bool* ok) {
     Eig3 te = d1;
     d1 = d2;
     d2 = te;
+    for (int i = 0; i < 3; ++i) {
+      int tg = g1[i];
+      g1[i] = g2[i];
+      g2[i] = tg;
+    }
     int tn = n1;
     n1 = n2;
     n2 = tn;
   }
   if (n1 == 3) return zero3();
-  if (n1 != 0) {
-    *degen = true;
-    return m1;
-  }
+  if (n1 != 0) return intersect_degen3(m1, d1, g1, n1, m2, d2, g2, n2, ok);
   V3 s, is;
   for (int i = 0; i < 3; ++i) {
     s.x[i] = sqrt(d1.l.x[i]);
@@ -172,13 +351,15 @@ OHG_HD M3 intersect3(M3 m1, M3 m2, bool* degen, bool* ok) {
   M3 mib = compose_ortho3(db.q, l);
   return mm3(mm3(tr3(m1_sqrt), mib), m1_sqrt);
 }
-OHG_HD M2 intersect2(M2 m1, M2 m2, bool* degen, bool* ok) {
+OHG_HD M2 intersect2(M2 m1, M2 m2, bool* ok) {
   Eig2 d1 = eigen2(m1), d2 = eigen2(m2);
   *ok = *ok && d1.ok && d2.ok;
-  int n1 = 0, n2 = 0;
+  int g1[2], g2[2], n1 = 0, n2 = 0;
   for (int i = 0; i < 2; ++i) {
-    n1 += d1.l.x[i] < kEps;
-    n2 += d2.l.x[i] < kEps;
+    g1[i] = d1.l.x[i] < kEps;
+    g2[i] = d2.l.x[i] < kEps;
+    n1 += g1[i];
+    n2 += g2[i];
   }
   if (n1 > n2) {
     M2 t = m1;
@@ -187,15 +368,17 @@ OHG_HD M2 intersect2(M2 m1, M2 m2, bool* degen, bool* ok) {
     Eig2 te = d1;
     d1 = d2;
     d2 = te;
+    for (int i = 0; i < 2; ++i) {
+      int tg = g1[i];
+      g1[i] = g2[i];
+      g2[i] = tg;
+    }
     int tn = n1;
     n1 = n2;
     n2 = tn;
   }
   if (n1 == 2) return zero2();
-  if (n1 != 0) {
-    *degen = true;
-    return m1;
-  }
+  if (n1 != 0) return intersect_degen2(m1, d1, g1, m2, d2, g2);
   V2 s, is;
   for (int i = 0; i < 2; ++i) {
     s.x[i] = sqrt(d1.l.x[i]);
@@ -499,6 +682,60 @@ double exact_sum(const Arr<double>& a) {
 }  // namespace
 
 // ------------------------------------------------------------ entry points
+// find_polynomial_roots of n monic cubics (coefficients a_0, a_1, a_2 each;
+// src/Omega_h_eigen.hpp:21-85), one thread per cubic
+void cubic_roots_batch(LO n, const double* coeffs_p, double eps, int* nroots_p, double* roots_p,
+                       int* mults_p) {
+  auto cf = cview(coeffs_p, n * 3);
+  auto nr = view(nroots_p, n);
+  auto rv = view(roots_p, n * 3);
+  auto mu = view(mults_p, n * 3);
+  pfor(n, [=] __device__(LO i) {
+    double rt[3];
+    int ml[3];
+    nr[i] = cubic_roots(cf[i * 3], cf[i * 3 + 1], cf[i * 3 + 2], eps, rt, ml);
+    for (int k = 0; k < 3; ++k) {
+      rv[i * 3 + k] = rt[k];
+      mu[i * 3 + k] = ml[k];
+    }
+  });
+}
+
+// decompose_eigen (src/Omega_h_eigen.hpp:278-293) of n dim x dim matrices
+// stored by columns; q by columns (the eigenvectors), l the eigenvalues
+void decompose_eigen_batch(int dim, LO n, const double* m_p, double* q_p, double* l_p) {
+  int mm = dim * dim;
+  auto a = cview(m_p, n * mm);
+  auto q = view(q_p, n * mm);
+  auto l = view(l_p, n * dim);
+  int* st = ctx().d_status;
+  pfor(n, [=] __device__(LO i) {
+    bool ok;
+    if (dim == 3) {
+      M3 m;
+      for (int j = 0; j < 3; ++j)
+        for (int r = 0; r < 3; ++r) m.c[j].x[r] = a[i * 9 + j * 3 + r];
+      Eig3 e = eigen3(m);
+      ok = e.ok;
+      for (int j = 0; j < 3; ++j) {
+        for (int r = 0; r < 3; ++r) q[i * 9 + j * 3 + r] = e.q.c[j].x[r];
+        l[i * 3 + j] = e.l.x[j];
+      }
+    } else {
+      M2 m;
+      for (int j = 0; j < 2; ++j)
+        for (int r = 0; r < 2; ++r) m.c[j].x[r] = a[i * 4 + j * 2 + r];
+      Eig2 e = eigen2(m);
+      ok = e.ok;
+      for (int j = 0; j < 2; ++j) {
+        for (int r = 0; r < 2; ++r) q[i * 4 + j * 2 + r] = e.q.c[j].x[r];
+        l[i * 2 + j] = e.l.x[j];
+      }
+    }
+    if (!ok) raise_status(st, ST_NUMERIC);
+  });
+}
+
 void intersect_metrics(int dim, LO n, const double* a_p, const double* b_p, double* out_p) {
   int mc = mcomps(dim);
   auto a = cview(a_p, n * mc);
@@ -506,12 +743,12 @@ void intersect_metrics(int dim, LO n, const double* a_p, const double* b_p, doub
   auto o = view(out_p, n * mc);
   int* st = ctx().d_status;
   pfor(n, [=] __device__(LO i) {
-    bool degen = false, ok = true;
+    bool ok = true;
     if (dim == 3)
-      unsymm3(intersect3(symm3(&a[i * 6]), symm3(&b[i * 6]), &degen, &ok), &o[i * 6]);
+      unsymm3(intersect3(symm3(&a[i * 6]), symm3(&b[i * 6]), &ok), &o[i * 6]);
     else
-      unsymm2(intersect2(symm2(&a[i * 3]), symm2(&b[i * 3]), &degen, &ok), &o[i * 3]);
-    if (degen || !ok) raise_status(st, ST_NUMERIC);
+      unsymm2(intersect2(symm2(&a[i * 3]), symm2(&b[i * 3]), &ok), &o[i * 3]);
+    if (!ok) raise_status(st, ST_NUMERIC);
   });
 }
 
@@ -615,7 +852,7 @@ Arr<double> limit_metric_gradation(Mesh& m, const Arr<double>& v2m, double max_r
     auto in = cview(cur);
     auto o = view(next);
     pfor(m.nverts(), [=] __device__(LO v) {
-      bool degen = false, ok = true;
+      bool ok = true;
       if (dim == 3) {
         M3 mm = symm3(&in[v * 6]);
         V3 x = {{c[v * 3], c[v * 3 + 1], c[v * 3 + 2]}};
@@ -627,7 +864,7 @@ Arr<double> limit_metric_gradation(Mesh& m, const Arr<double>& v2m, double max_r
           V3 vec = sub3(ax, x);
           double dist = sqrt(metric_product3(am, vec));
           double h = 1.0 + dist * max_rate;
-          mm = intersect3(mm, scale3(am, 1.0 / (h * h)), &degen, &ok);
+          mm = intersect3(mm, scale3(am, 1.0 / (h * h)), &ok);
         }
         unsymm3(mm, &o[v * 6]);
       } else {
@@ -641,11 +878,11 @@ Arr<double> limit_metric_gradation(Mesh& m, const Arr<double>& v2m, double max_r
           V2 mv = mv2(am, vec);
           double dist = sqrt(vec.x[0] * mv.x[0] + vec.x[1] * mv.x[1]);
           double h = 1.0 + dist * max_rate;
-          mm = intersect2(mm, scale2(am, 1.0 / (h * h)), &degen, &ok);
+          mm = intersect2(mm, scale2(am, 1.0 / (h * h)), &ok);
         }
         unsymm2(mm, &o[v * 3]);
       }
-      if (degen || !ok) raise_status(st, ST_NUMERIC);
+      if (!ok) raise_status(st, ST_NUMERIC);
     });
     ++i;
     // are_close over all values (rel_diff_with_floor, src/Omega_h_scalar.hpp:266-277)

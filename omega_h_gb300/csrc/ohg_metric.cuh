@@ -34,6 +34,9 @@ struct MetricInput {
   int nsmoothing_steps = 0;
 };
 
+void cubic_roots_batch(LO n, const double* coeffs, double eps, int* nroots, double* roots,
+                       int* mults);
+void decompose_eigen_batch(int dim, LO n, const double* m, double* q, double* l);
 void intersect_metrics(int dim, LO n, const double* a, const double* b, double* out);
 void clamp_metrics(int dim, LO n, const double* m, double h_min, double h_max, double* out);
 void hessian_metrics(int dim, LO n, const double* hessians, double eps, double* out);

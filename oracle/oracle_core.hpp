@@ -29,6 +29,31 @@
 
 namespace orc {
 
+// The libm functions on the path.  Built with -DORC_CR_LIBM=<mask> (bits:
+// 1 cbrt, 2 acos, 4 cos, 8 log, 16 exp) the selected ones are replaced by
+// the long-double function rounded to double (correctly rounded unless the
+// extended result lies within its own error of a halfway point): test
+// infrastructure for measuring how the reference's results depend on the
+// last ulp of each function.
+#ifndef ORC_CR_LIBM
+#define ORC_CR_LIBM 0
+#endif
+inline double orc_cbrt(double x) {
+  return (ORC_CR_LIBM & 1) ? double(cbrtl((long double)x)) : std::cbrt(x);
+}
+inline double orc_acos(double x) {
+  return (ORC_CR_LIBM & 2) ? double(acosl((long double)x)) : std::acos(x);
+}
+inline double orc_cos(double x) {
+  return (ORC_CR_LIBM & 4) ? double(cosl((long double)x)) : std::cos(x);
+}
+inline double orc_log(double x) {
+  return (ORC_CR_LIBM & 8) ? double(logl((long double)x)) : std::log(x);
+}
+inline double orc_exp(double x) {
+  return (ORC_CR_LIBM & 16) ? double(expl((long double)x)) : std::exp(x);
+}
+
 typedef std::int32_t LO;
 typedef std::int64_t GO;
 typedef std::int8_t I8;
@@ -250,7 +275,7 @@ const double EQUILATERAL_TET = 0.1178511301977579;
 const double EQUILATERAL_TRI = 0.4330127018922193;
 
 inline double anisotropic_edge_length(double la, double lb) {
-  if (std::abs(la - lb) > 1e-3) return (la - lb) / (std::log(la / lb));
+  if (std::abs(la - lb) > 1e-3) return (la - lb) / (orc_log(la / lb));
   return (la + lb) / 2.;
 }
 inline double edge_length3(const double* p0, const double* p1, const double* m0,
@@ -281,7 +306,7 @@ inline double tet_quality(const Vec3 p[4], const Mat3& m) {
   for (int i = 0; i < 6; ++i) msl += metric_product3(m, ev[i]);
   msl = msl / 6;
   double x = s / EQUILATERAL_TET;
-  return std::cbrt(x * x) / msl;
+  return orc_cbrt(x * x) / msl;
 }
 inline double tri_quality(const Vec2 p[3], const Mat2& m) {
   Vec2 b0 = {{p[1][0] - p[0][0], p[1][1] - p[0][1]}};

@@ -37,8 +37,8 @@ static Roots3 cubic_roots(double a_0, double a_1, double a_2, double eps) {
   double D = cube(Q) + square(R);
   double shift = -a_2 / 3.;
   if (D >= 0.0) {
-    double S = std::cbrt(R + std::sqrt(D));
-    double T = std::cbrt(R - std::sqrt(D));
+    double S = orc_cbrt(R + std::sqrt(D));
+    double T = orc_cbrt(R - std::sqrt(D));
     double B = S + T;
     double z_1 = shift + B;
     double z_23_real = shift - (1. / 2.) * B;
@@ -46,11 +46,11 @@ static Roots3 cubic_roots(double a_0, double a_1, double a_2, double eps) {
     roots[1] = roots[2] = z_23_real;
   } else {
     double cos_theta = R / std::sqrt(-cube(Q));
-    double theta = std::acos(clampd(cos_theta, -1.0, 1.0));
+    double theta = orc_acos(clampd(cos_theta, -1.0, 1.0));
     double radius = 2. * std::sqrt(-Q);
-    roots[0] = radius * std::cos((theta) / 3.) + shift;
-    roots[1] = radius * std::cos((theta + 2. * PI) / 3.) + shift;
-    roots[2] = radius * std::cos((theta - 2. * PI) / 3.) + shift;
+    roots[0] = radius * orc_cos((theta) / 3.) + shift;
+    roots[1] = radius * orc_cos((theta + 2. * PI) / 3.) + shift;
+    roots[2] = radius * orc_cos((theta - 2. * PI) / 3.) + shift;
   }
   mults[0] = mults[1] = mults[2] = 1;
   if (std::abs(roots[0] - roots[1]) < eps) {
@@ -181,12 +181,12 @@ static Mat3 compose_ortho3(const Mat3& q, Vec3 l) {
 }
 Mat3 log_spd3(Mat3 m) {
   Decomp3 d = decompose_eigen3(m);
-  for (int i = 0; i < 3; ++i) d.l[i] = std::log(d.l[i]);
+  for (int i = 0; i < 3; ++i) d.l[i] = orc_log(d.l[i]);
   return compose_ortho3(d.q, d.l);
 }
 Mat3 exp_spd3(Mat3 m) {
   Decomp3 d = decompose_eigen3(m);
-  for (int i = 0; i < 3; ++i) d.l[i] = std::exp(d.l[i]);
+  for (int i = 0; i < 3; ++i) d.l[i] = orc_exp(d.l[i]);
   return compose_ortho3(d.q, d.l);
 }
 // average_metric of two metrics, has_degen = false (src/Omega_h_metric.hpp:120-150)
@@ -281,12 +281,12 @@ static Mat2 compose_ortho2(const Mat2& q, Vec2 l) {
 }
 Mat2 log_spd2(Mat2 m) {
   Decomp2 d = decompose_eigen2(m);
-  for (int i = 0; i < 2; ++i) d.l[i] = std::log(d.l[i]);
+  for (int i = 0; i < 2; ++i) d.l[i] = orc_log(d.l[i]);
   return compose_ortho2(d.q, d.l);
 }
 Mat2 exp_spd2(Mat2 m) {
   Decomp2 d = decompose_eigen2(m);
-  for (int i = 0; i < 2; ++i) d.l[i] = std::exp(d.l[i]);
+  for (int i = 0; i < 2; ++i) d.l[i] = orc_exp(d.l[i]);
   return compose_ortho2(d.q, d.l);
 }
 void average_metric2(const double* m0, const double* m1, double* out) {

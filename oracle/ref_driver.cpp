@@ -23,6 +23,7 @@
 #include <Omega_h_mark.hpp>
 #include <Omega_h_mesh.hpp>
 #include <Omega_h_metric.hpp>
+#include <Omega_h_metric_intersect.hpp>
 #include <Omega_h_modify.hpp>
 #include <Omega_h_quality.hpp>
 #include <Omega_h_refine.hpp>
@@ -39,6 +40,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -350,7 +352,90 @@ static void dump_metric_tools(Mesh* mesh) {
   dump("mt_generated", generate_metrics(mesh, in));
 }
 
+// "intersect": intersect_metrics on seeded pairs of partially degenerate
+// metrics (rank 1 and 2 in 3D, rank 1 in 2D), in random orientations and in
+// shared eigenbases, plus the reference's unit-test cases; inputs and the
+// reference's outputs packed (xx, yy, zz, yx, zy, zx) / (xx, yy, yx)
+template <Int dim>
+static Tensor<dim> random_rotation(std::mt19937_64& g) {
+  std::normal_distribution<double> nd(0.0, 1.0);
+  Tensor<dim> q;
+  // Gram-Schmidt on Gaussian columns
+  for (Int j = 0; j < dim; ++j) {
+    Vector<dim> v;
+    for (Int i = 0; i < dim; ++i) v[i] = nd(g);
+    for (Int k = 0; k < j; ++k) v = v - (v * q[k]) * q[k];
+    q[j] = normalize(v);
+  }
+  return q;
+}
+template <Int dim>
+static void dump_degenerate_intersections(std::mt19937_64& g) {
+  std::uniform_real_distribution<double> ud(0.25, 4.0);
+  std::vector<Tensor<dim>> as, bs;
+  const int npairs = 96;
+  for (int p = 0; p < npairs; ++p) {
+    Tensor<dim> qa = random_rotation<dim>(g);
+    // a third of the pairs share the eigenbasis (up to a permutation of it)
+    Tensor<dim> qb = (p % 3 == 0) ? qa : random_rotation<dim>(g);
+    if (p % 3 == 0 && dim == 3 && (p / 3) % 2) {
+      auto t = qb[0];
+      qb[0] = qb[2];
+      qb[2] = t;
+    }
+    int ra = (dim == 2) ? 1 : 1 + int(g() % 2);
+    int rb = (dim == 2) ? 1 : 1 + int(g() % 2);
+    Vector<dim> la, lb;
+    for (Int i = 0; i < dim; ++i) {
+      la[i] = i < ra ? ud(g) : 0.0;
+      lb[i] = i < rb ? ud(g) : 0.0;
+    }
+    as.push_back(compose_ortho(qa, la));
+    bs.push_back(compose_ortho(qb, lb));
+  }
+  if (dim == 3) {
+    // src/unit_math.cpp:221-252
+    double cases[6][2][3] = {{{1, 0, 0}, {0, 0, 1}}, {{1, 0, 0}, {2, 0, 0}},
+        {{1, 0, 0}, {2, 1, 0}}, {{1, 0, 0}, {0, 1, 2}}, {{1, 0, 2}, {2, 0, 1}},
+        {{1, 0, 2}, {2, 1, 0}}};
+    for (auto& c : cases) {
+      Vector<dim> a, b;
+      for (Int i = 0; i < dim; ++i) {
+        a[i] = c[0][i];
+        b[i] = c[1][i];
+      }
+      as.push_back(diagonal(a));
+      bs.push_back(diagonal(b));
+    }
+  }
+  LO n = LO(as.size());
+  int nc = symm_ncomps(dim);
+  HostWrite<Real> ha(n * nc), hb(n * nc), ho(n * nc);
+  for (LO i = 0; i < n; ++i) {
+    auto o = intersect_metrics(as[i], bs[i]);
+    auto va = symm2vector(as[i]), vb = symm2vector(bs[i]), vo = symm2vector(o);
+    for (int k = 0; k < nc; ++k) {
+      ha[i * nc + k] = va[k];
+      hb[i * nc + k] = vb[k];
+      ho[i * nc + k] = vo[k];
+    }
+  }
+  std::string pre = "di" + std::to_string(dim) + "_";
+  dump(pre + "a", Reals(ha.write()));
+  dump(pre + "b", Reals(hb.write()));
+  dump(pre + "out", Reals(ho.write()));
+}
+
 int main(int argc, char** argv) {
+  if (argc == 3 && std::string(argv[1]) == "intersect") {
+    g_out = argv[2];
+    g_manifest = std::fopen((g_out + "/manifest.txt").c_str(), "w");
+    std::mt19937_64 g(20261204);
+    dump_degenerate_intersections<2>(g);
+    dump_degenerate_intersections<3>(g);
+    std::fclose(g_manifest);
+    return 0;
+  }
   if (argc < 7) {
     std::fprintf(stderr,
         "usage: %s DIM N METRIC SEED MIN_QUAL_ALLOWED OUTDIR [nopass]\n",

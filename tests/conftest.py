@@ -42,6 +42,25 @@ ADAPT_CASES = {
     "sq32_blayer_adapt": (2, 32, 2, 5, 0.3),
 }
 BIG_CASE = ("box64_shock", (3, 64, 1, 2024, 0.2))
+# one pass at full size against digests of the reference's mesh after it:
+# the two boundary-layer workloads of the FP32-screening tier and a 64^3
+# box whose pass refines, coarsens and swaps
+SCALE_CASES = {
+    "sq1024_blayer": (2, 1024, 2, 3, 0.3),
+    "box48_blayer": (3, 48, 2, 3, 0.2),
+    "box64_sine": (3, 64, 3, 469, 0.2),
+}
+# the first 8 meshes of the batched workload's seeded list (isotropic sine)
+BATCH_CASES = {
+    "batch_m0_n17": (3, 17, 3, 1504059971, 0.2),
+    "batch_m1_n32": (3, 32, 3, 1942236769, 0.2),
+    "batch_m2_n24": (3, 24, 3, 2040772436, 0.2),
+    "batch_m3_n6": (3, 6, 3, 529044838, 0.2),
+    "batch_m4_n8": (3, 8, 3, 930072621, 0.2),
+    "batch_m5_n30": (3, 30, 3, 1543323540, 0.2),
+    "batch_m6_n4": (3, 4, 3, 881660342, 0.2),
+    "batch_m7_n27": (3, 27, 3, 664364275, 0.2),
+}
 # arrays that are metadata, not per-stage outputs
 SKIP_KEYS = ("meta_json", "swap3d_tables", "opts", "opts_values", "r_rep2md")
 
@@ -93,16 +112,36 @@ def run_oracle(driver, spec, mode=""):
 # Real-valued tolerances.  Every real computed before the first metric
 # interpolation (lengths, qualities, cavity qualities of the input mesh) must
 # agree within STRICT_RTOL.  The log-Euclidean metric average (one closed-form
-# 3x3 eigensolve per logarithm and exponential) is ill-conditioned where two
-# eigenvalues (nearly) coincide, e.g. the two tangential sizes of the shock
-# metric: there a one-ulp difference between CUDA's and glibc's cbrt/acos/cos
-# in the cubic root solve moves a double root by O(sqrt(ulp)) before the two
-# roots are merged.  Interpolated metric tensors are therefore compared
-# relative to their largest component (INTERP_TENSOR_RTOL), and every real
-# computed from them afterwards within INTERP_RTOL.  Integers stay bit-exact.
+# 3x3 eigensolve per logarithm and exponential) is ill-conditioned where the
+# averaged metric has a nearly triple eigenvalue: the shock metric's two equal
+# tangential sizes meet a normal size that the log-mean brings close to them.
+# There the characteristic polynomial's single root moves by about
+# ulp / gap^2 and its eigenvector by ulp / gap^3.  The only libm call whose
+# last ulp reaches this on the workloads is cbrt (Cardano's branch, taken for
+# every metric with an exact double eigenvalue): replacing glibc's cbrt alone
+# by a correctly rounded one moves midpoint metrics by 5e-8 of their
+# largest entry, while correctly rounded log, exp, acos and cos leave every
+# array within 4e-14 (test_libm_sensitivity.py).  glibc's cbrt is not
+# correctly rounded, CUDA's is a different function again, and the
+# reference's own algorithm on the aarch64 glibc differs from its x86-64
+# goldens by 4e-10 on box12_shock.  Interpolated metric tensors are
+# therefore compared relative to their largest component
+# (INTERP_TENSOR_RTOL), and every real computed from them afterwards within
+# INTERP_RTOL.  Integers stay bit-exact.
 STRICT_RTOL = 1e-12
 INTERP_TENSOR_RTOL = 1e-6
 INTERP_RTOL = 1e-7
+
+
+# Over the full adapt loop's many refine and coarsen rounds, a one-ulp
+# difference in cbrt (inside the cubic solve of the metric interpolation and
+# in every element quality) can break a tie between exactly equal edge
+# lengths the other way, and the collapse then goes along the other edge.
+# The reference itself does this between platforms: its own algorithm on the
+# aarch64 glibc differs from its x86-64 result on 6 of box8_iso_adapt's
+# 84,580 edges.  Such cases are held to the fraction of connectivity entries
+# that may differ; the rest are bit-exact in every integer.
+LIBM_TIE_SENSITIVE = {"box8_iso_adapt": 1e-3}
 
 
 def interp_dependent(key):
@@ -112,9 +151,10 @@ def interp_dependent(key):
         not key.startswith(("in_", "r_"))
 
 
-def compare_arrays(expected, got, keys=None, rtol=STRICT_RTOL):
+def compare_arrays(expected, got, keys=None, rtol=STRICT_RTOL, interp=True):
     """Bit-exact for integer arrays, relative error <= rtol for reals (with
-    the interpolation tolerances above for interpolation-dependent arrays).
+    the interpolation tolerances above for interpolation-dependent arrays,
+    unless interp is False).
     Returns (list of failures, max real relative error, count of real values
     that are not bitwise equal)."""
     fails = []
@@ -133,15 +173,15 @@ def compare_arrays(expected, got, keys=None, rtol=STRICT_RTOL):
         if a.dtype.kind == "f":
             if a.size:
                 nreal_diff += int(np.sum(a != b))
-                interp = interp_dependent(k) and rtol == STRICT_RTOL
-                if interp and (k.endswith("metric") or k.endswith("metrics")) and a.size % 6 == 0:
+                interp_k = interp and interp_dependent(k) and rtol == STRICT_RTOL
+                if interp_k and (k.endswith("metric") or k.endswith("metrics")) and a.size % 6 == 0:
                     A, B = a.reshape(-1, 6), b.reshape(-1, 6)
                     nrm = np.maximum(np.max(np.abs(A), axis=1), 1e-300)
                     err = float(np.max(np.max(np.abs(A - B), axis=1) / nrm))
                     tol = INTERP_TENSOR_RTOL
                 else:
                     err = float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-300)))
-                    tol = INTERP_RTOL if interp else rtol
+                    tol = INTERP_RTOL if interp_k else rtol
                 maxerr = max(maxerr, err)
                 if not err <= tol:
                     fails.append(f"{k}: max rel err {err:.3e} > {tol:.0e}")
@@ -152,7 +192,20 @@ def compare_arrays(expected, got, keys=None, rtol=STRICT_RTOL):
     return fails, maxerr, nreal_diff
 
 
-def compare_digest(digest, got, rtol=1e-12):
+def digest_refined(digest):
+    """Whether the reference's pass behind a digest refined (its dump
+    driver prints the pass flags), i.e. whether its output reals passed
+    through the log-Euclidean metric average."""
+    words = digest["driver_stdout"].split()
+    return words[words.index("flags") + 1] == "1"
+
+
+def compare_digest(digest, got, rtol=STRICT_RTOL, interp=False, errs=None):
+    """Integer arrays by sha256; real arrays on their sampled entries, min
+    and max.  interp: the pass refined, so every output real depends on an
+    interpolated metric and gets the interpolation tolerances (metric
+    tensors relative to each sampled tensor's largest entry).  errs, if a
+    dict, receives the max sampled error per real array."""
     import hashlib
     fails = []
     for k, v in digest["arrays"].items():
@@ -169,11 +222,21 @@ def compare_digest(digest, got, rtol=1e-12):
         elif a.size:
             idx = np.array(v["sample_idx"], dtype=np.int64)
             s = np.array(v["sample"])
-            err = float(np.max(np.abs(a[idx] - s) / np.maximum(np.abs(s), 1e-300)))
-            if not err <= rtol:
-                fails.append(f"{k}: sampled rel err {err:.3e}")
+            tol = rtol
+            if interp and "sample_row_scale" in v:
+                scale = np.maximum(np.array(v["sample_row_scale"]), 1e-300)
+                tol = INTERP_TENSOR_RTOL
+            else:
+                scale = np.maximum(np.abs(s), 1e-300)
+                if interp:
+                    tol = INTERP_RTOL
+            err = float(np.max(np.abs(a[idx] - s) / scale))
+            if errs is not None:
+                errs[k] = err
+            if not err <= tol:
+                fails.append(f"{k}: sampled rel err {err:.3e} > {tol:.0e}")
             for stat in ("min", "max"):
                 e = abs(getattr(a, stat)() - v[stat]) / max(abs(v[stat]), 1e-300)
-                if not e <= rtol:
+                if not e <= max(tol, rtol):
                     fails.append(f"{k}: {stat} rel err {e:.3e}")
     return fails

@@ -68,6 +68,24 @@ CASES = {
     "sq32_shock_adapt": (2, 32, 1, 5, 0.3, True, "adapt"),
     "sq32_blayer_adapt": (2, 32, 2, 5, 0.3, True, "adapt"),
     "box8_sine_scalar_adapt": (3, 8, 13, 5, 0.2, True, "adapt"),
+    # one pass at full size, the mesh after it only (digests): the two
+    # boundary-layer workloads of the FP32-screening tier (2D 1024^2,
+    # 2,097,152 triangles; 3D 48^3, 663,552 tets) and a 64^3 box whose pass
+    # refines, coarsens and swaps (isotropic sine, seed 469: h0 0.0204,
+    # amplitude 0.39; 1,572,864 tets in, 2,184,560 out)
+    "sq1024_blayer": (2, 1024, 2, 3, 0.3, False, "nostages"),
+    "box48_blayer": (3, 48, 2, 3, 0.2, False, "nostages"),
+    "box64_sine": (3, 64, 3, 469, 0.2, False, "nostages"),
+    # the first 8 meshes of the batched workload's seeded list (1024 boxes,
+    # n log-uniform in [4, 40], isotropic sine metric, seed 7)
+    "batch_m0_n17": (3, 17, 3, 1504059971, 0.2, False, "nostages"),
+    "batch_m1_n32": (3, 32, 3, 1942236769, 0.2, False, "nostages"),
+    "batch_m2_n24": (3, 24, 3, 2040772436, 0.2, False, "nostages"),
+    "batch_m3_n6": (3, 6, 3, 529044838, 0.2, False, "nostages"),
+    "batch_m4_n8": (3, 8, 3, 930072621, 0.2, False, "nostages"),
+    "batch_m5_n30": (3, 30, 3, 1543323540, 0.2, False, "nostages"),
+    "batch_m6_n4": (3, 4, 3, 881660342, 0.2, False, "nostages"),
+    "batch_m7_n27": (3, 27, 3, 664364275, 0.2, False, "nostages"),
 }
 
 
@@ -108,6 +126,22 @@ def run_metric_case(name, spec):
     os.makedirs(os.path.join(HERE, "metric"), exist_ok=True)
     np.savez_compressed(os.path.join(HERE, "metric", name + ".npz"), **arrs)
     print(name, out.stdout.strip())
+
+
+def run_intersect_case():
+    """The reference's intersect_metrics on seeded partially degenerate metric
+    pairs (Barral's cases) and on its unit-test pairs."""
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([os.path.join(ROOT, "oracle/_ref/ref_driver"), "intersect", tmp],
+                       check=True, capture_output=True, text=True)
+        arrs = {}
+        with open(os.path.join(tmp, "manifest.txt")) as f:
+            for line in f:
+                key, dt, count = line.split()
+                arrs[key] = np.fromfile(os.path.join(tmp, key + ".bin"), dtype=np.dtype(dt))
+    os.makedirs(os.path.join(HERE, "metric"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "metric", "degenerate_intersections.npz"), **arrs)
+    print("degenerate_intersections", {k: v.size for k, v in arrs.items()})
 
 
 def run_osh_case(name, spec):
@@ -179,6 +213,12 @@ def run_case(name, spec):
                                 "max": float(a.max()) if a.size else 0.0,
                                 "sample_idx": idx.tolist(),
                                 "sample": a[idx].tolist()}
+                ncomp = (6 if dim == 3 else 3) if key.endswith("metric") else 1
+                if ncomp > 1 and a.size % ncomp == 0 and a.size:
+                    # the largest entry of each sampled entry's tensor: the
+                    # scale interpolated metrics are compared against
+                    rows = np.abs(a.reshape(-1, ncomp)).max(axis=1)
+                    digests[key]["sample_row_scale"] = rows[idx // ncomp].tolist()
             else:
                 digests[key] = {"dtype": a.dtype.str, "count": int(a.size),
                                 "sha256": hashlib.sha256(
@@ -198,7 +238,11 @@ def main():
     if not a.ref or not os.path.isdir(a.ref):
         sys.exit(f"reference sources not found: pass --ref or set OMEGA_H_REFERENCE_SRC")
     build_ref(a.ref)
-    for name in a.cases or list(CASES) + list(OSH_CASES) + ["metric:" + k for k in METRIC_CASES]:
+    for name in a.cases or list(CASES) + list(OSH_CASES) + ["metric:" + k for k in METRIC_CASES] + \
+            ["intersect"]:
+        if name == "intersect":
+            run_intersect_case()
+            continue
         if name.startswith("metric:"):
             run_metric_case(name[7:], METRIC_CASES[name[7:]])
         elif name in OSH_CASES:

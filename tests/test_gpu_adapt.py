@@ -5,7 +5,8 @@ throughout."""
 import numpy as np
 import pytest
 
-from conftest import ADAPT_CASES, INTERP_RTOL, compare_arrays, load_golden, run_oracle
+from conftest import (ADAPT_CASES, INTERP_RTOL, LIBM_TIE_SENSITIVE, compare_arrays,
+                      load_golden, run_oracle)
 
 pytestmark = pytest.mark.gpu
 
@@ -35,16 +36,6 @@ def _adapt(ctx, dim, n, kind, seed, mqa):
     return r, out
 
 
-# Over many rounds, every refine interpolates metrics through log and exp,
-# where CUDA's and glibc's results differ by an ulp in about 0.1 % of
-# arguments.  On a symmetric box, edges of exactly equal length are common,
-# and choose_rails breaks such ties by quality: a one-ulp difference can send
-# a collapse along the other edge of a tie.  These cases are therefore held
-# to the fraction of connectivity entries that may differ (measured: 16 of
-# 84,580 edges for box8_iso_adapt, after 11 refines and 12 coarsens); array
-# sizes, reals and operator counts stay checked.  The other cases are
-# bit-exact in every integer.
-LIBM_TIE_SENSITIVE = {"box8_iso_adapt": 1e-3}
 
 
 @pytest.mark.parametrize("case", sorted(ADAPT_CASES))

@@ -18,7 +18,8 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden", "metric")
-CASES = sorted(f[:-4] for f in os.listdir(GOLD) if f.endswith(".npz"))
+DEGENERATE = "degenerate_intersections"
+CASES = sorted(f[:-4] for f in os.listdir(GOLD) if f.endswith(".npz") and f[:-4] != DEGENERATE)
 from conftest import INTERP_RTOL, INTERP_TENSOR_RTOL  # noqa: E402
 
 TOL = INTERP_TENSOR_RTOL
@@ -185,3 +186,37 @@ def test_intersection_properties(ctx):
     ra, rb = (q(G) / q(A)).min(), (q(G) / q(B)).min()
     print(f"intersection vs operands: smallest ratios {ra:.12f} {rb:.12f}")
     assert ra >= 1 - 1e-9 and rb >= 1 - 1e-9
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_degenerate_intersections_match_reference(ctx, dim):
+    """Barral's degenerate cases (src/Omega_h_metric_intersect.hpp:25-212) on
+    seeded pairs of rank-1 and rank-2 metrics, in random orientations and in
+    shared eigenbases, plus the reference's unit-test pairs, against the
+    reference's own intersect_metrics.  Where the reference's 2D case 5.b
+    meets parallel null directions its result is not finite, and so must
+    ours be at the same entries."""
+    import torch
+    from omega_h_gb300 import _lib
+    import ctypes
+    g = dict(np.load(os.path.join(GOLD, DEGENERATE + ".npz")))
+    nc = 6 if dim == 3 else 3
+    a = torch.tensor(g[f"di{dim}_a"]).cuda()
+    b = torch.tensor(g[f"di{dim}_b"]).cuda()
+    want = g[f"di{dim}_out"].reshape(-1, nc)
+    n = want.shape[0]
+    out = torch.empty(n * nc, dtype=torch.float64, device="cuda")
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    _lib.call("ohg_intersect_metrics", ctx.handle, dim, n, P(a), P(b), P(out))
+    got = out.cpu().numpy().reshape(-1, nc)
+    fin = np.isfinite(want)
+    assert np.array_equal(fin, np.isfinite(got))
+    assert np.array_equal(np.isnan(want), np.isnan(got))
+    rows = fin.all(axis=1)
+    w, o = want[rows], got[rows]
+    scale = np.maximum(np.abs(w).max(axis=1, keepdims=True), 1e-300)
+    err = float((np.abs(w - o) / scale).max())
+    nbit = int(np.sum(np.any(w.view(np.uint64) != o.view(np.uint64), axis=1)))
+    print(f"{dim}D degenerate intersections: {rows.sum()} finite of {n}, max error {err:.2e}, "
+          f"{nbit} not bitwise equal")
+    assert err <= TOL

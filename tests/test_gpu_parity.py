@@ -5,9 +5,9 @@ of every integer array and sampled reals) and against the oracle on seeds
 without fixtures.  Integers bit-exact; reals within 1e-12 relative."""
 import pytest
 
-from conftest import (BIG_CASE, SCALAR_CASES, SMALL_CASES, SMALL_CASES_2D, compare_arrays,
-                      compare_digest,
-                      load_digest, load_golden, run_oracle)
+from conftest import (BATCH_CASES, BIG_CASE, SCALAR_CASES, SCALE_CASES, SMALL_CASES,
+                      SMALL_CASES_2D, compare_arrays, compare_digest, digest_refined, load_digest,
+                      load_golden, run_oracle)
 
 ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D, **SCALAR_CASES}
 
@@ -44,6 +44,48 @@ def test_gpu_full_size_pass_matches_reference_digest():
     fails = compare_digest(load_digest(name), got)
     assert not fails, fails[:12]
     assert list(got["pass_flags"]) == [0, 1, 1]
+
+
+@pytest.mark.parametrize("case", sorted(SCALE_CASES) + sorted(BATCH_CASES))
+def test_gpu_pass_matches_reference_digest(case):
+    """One pass at full size (2D 1024^2 and 3D 48^3 boundary layers, a 64^3
+    box that refines) and on the first 8 meshes of the batched workload,
+    against the reference's mesh after its pass: every integer array by
+    sha256, reals by sampled entries."""
+    import gpu_dump
+    spec = {**SCALE_CASES, **BATCH_CASES}[case]
+    dg = load_digest(case)
+    got = gpu_dump.run(*spec, stages=False)
+    errs = {}
+    fails = compare_digest(dg, got, interp=digest_refined(dg), errs=errs)
+    print(f"{case}: refined {digest_refined(dg)}, max sampled real errors "
+          + ", ".join(f"{k} {v:.1e}" for k, v in sorted(errs.items())))
+    assert not fails, fails[:12]
+
+
+def test_gpu_batched_union_matches_reference_digests():
+    """The first 8 meshes of the batched workload run as one union pass
+    (ohg_adapt_pass_batch); each part against the reference's own pass."""
+    import gpu_dump
+    from omega_h_gb300.mesh import Context, Mesh, adapt_opts, adapt_pass_batch
+    ctx = Context(0)
+    names = sorted(BATCH_CASES)
+    ms = []
+    for name in names:
+        dim, n, kind, seed, _ = BATCH_CASES[name]
+        m = Mesh.build_box(ctx, dim, n)
+        m.apply_workload(n, seed, kind)
+        ms.append(m)
+    adapt_pass_batch(ctx, ms, adapt_opts(3, min_quality_allowed=0.2))
+    fails = []
+    for name, m in zip(names, ms):
+        out = {}
+        gpu_dump.dump_mesh(m, "out_", out, with_length=True, with_quality=True)
+        dg = load_digest(name)
+        fails += [f"{name}: {f}" for f in compare_digest(dg, out, interp=digest_refined(dg))]
+        m.close()
+    ctx.close()
+    assert not fails, fails[:12]
 
 
 @pytest.mark.parametrize("spec", [(3, 10, 3, 5, 0.2), (3, 9, 1, 99, 0.25), (3, 14, 2, 11, 0.2),
