@@ -179,7 +179,8 @@ int ohg_mesh_get_arrays(ohg_mesh* mesh, int n, const char* const* names, void* c
 /* replaces vertex coordinates or metric ("coords" | "metric").  A metric of
  * nverts values is isotropic (the reference's one-component metric tag: its
  * scalar lengths, sizes, maxdet and log-Euclidean means are used), one of
- * nverts * 6 (3D) or * 3 (2D) values is a packed tensor. */
+ * nverts * 6 (3D) or * 3 (2D) values is a packed tensor.  src may be device
+ * or host memory; the call returns after the copy completed. */
 int ohg_mesh_set_array(ohg_mesh* mesh, const char* name, const void* src_dev, long long nbytes);
 
 /* ---- the pass ---- */

@@ -623,7 +623,9 @@ int ohg_mesh_set_array(ohg_mesh* m, const char* name, const void* src, long long
   return guarded(m->owner, [&] {
     if (n == "metric") me.metric_comps = (nbytes == iso && nbytes != full) ? 1 : 0;
     Arr<double> a(LO(nbytes / 8));
-    OHG_CUDA(cudaMemcpyAsync(a.data(), src, size_t(nbytes), cudaMemcpyDeviceToDevice, ctx().stream));
+    // device or host memory: the copy kind is inferred from the address
+    OHG_CUDA(cudaMemcpyAsync(a.data(), src, size_t(nbytes), cudaMemcpyDefault, ctx().stream));
+    ctx().sync();
     *dst = a;
     me.has_length = me.has_quality = false;
     me.screen.reset();

@@ -194,8 +194,10 @@ def test_degenerate_intersections_match_reference(ctx, dim):
     seeded pairs of rank-1 and rank-2 metrics, in random orientations and in
     shared eigenbases, plus the reference's unit-test pairs, against the
     reference's own intersect_metrics.  Where the reference's 2D case 5.b
-    meets parallel null directions its result is not finite, and so must
-    ours be at the same entries."""
+    meets parallel null directions (its test is v1 . v2 < 1e-10, so equal
+    directions go to 5.b) it inverts a singular matrix: the result is
+    infinite, not a number or huge depending on the last bit of the
+    eigenvectors, and so must ours blow up on exactly those pairs."""
     import torch
     from omega_h_gb300 import _lib
     import ctypes
@@ -209,10 +211,13 @@ def test_degenerate_intersections_match_reference(ctx, dim):
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     _lib.call("ohg_intersect_metrics", ctx.handle, dim, n, P(a), P(b), P(out))
     got = out.cpu().numpy().reshape(-1, nc)
-    fin = np.isfinite(want)
-    assert np.array_equal(fin, np.isfinite(got))
-    assert np.array_equal(np.isnan(want), np.isnan(got))
-    rows = fin.all(axis=1)
+
+    def blown_up(x):
+        with np.errstate(invalid="ignore"):
+            return ~np.isfinite(x).all(axis=1) | (np.nan_to_num(np.abs(x), nan=0.0).max(axis=1) > 1e8)
+
+    assert np.array_equal(blown_up(want), blown_up(got))
+    rows = ~blown_up(want)
     w, o = want[rows], got[rows]
     scale = np.maximum(np.abs(w).max(axis=1, keepdims=True), 1e-300)
     err = float((np.abs(w - o) / scale).max())
