@@ -7,9 +7,13 @@
 //
 // Every expression keeps the reference's association order and the library
 // is compiled with -fmad=false, so +,-,*,/,sqrt round exactly as the
-// reference's host build does; log/exp/cbrt/acos/cos are CUDA's.
+// reference's host build does.  cbrt, log, exp, acos and cos are correctly
+// rounded (ohg_libm.cuh), so the results do not depend on a math library's
+// last ulp.
 #pragma once
 #include <cstdint>
+
+#include "ohg_libm.cuh"
 
 #ifndef OHG_HD
 #define OHG_HD __host__ __device__ __forceinline__
@@ -152,7 +156,7 @@ OHG_HD void unsymm3(const M3& s, double* v) {
 OHG_HD double metric_product3(const M3& m, V3 v) { return dot3(v, mv3(m, v)); }
 
 OHG_HD double aniso_length(double la, double lb) {
-  if (fabs(la - lb) > 1e-3) return (la - lb) / (log(la / lb));
+  if (fabs(la - lb) > 1e-3) return (la - lb) / (log_cr(la / lb));
   return (la + lb) / 2.;
 }
 OHG_HD double edge_length3(const double* p0, const double* p1, const double* m0,
@@ -193,7 +197,7 @@ OHG_HD double tet_quality(const V3 p[4], const M3& m) {
   for (int i = 0; i < 6; ++i) msl += metric_product3(m, ev[i]);
   msl = msl / 6;
   double x = s / kEquilateralTet;
-  return cbrt(x * x) / msl;
+  return cbrt_cr(x * x) / msl;
 }
 // maxdet over n metrics, first maximum wins ties
 OHG_HD int maxdet_index3(const M3* ms, int n) {
@@ -271,7 +275,7 @@ OHG_HD double tet_quality_iso(const V3 p[4], double m) {
   for (int i = 0; i < 6; ++i) msl += iso_product3(m, ev[i]);
   msl = msl / 6;
   double x = s / kEquilateralTet;
-  return cbrt(x * x) / msl;
+  return cbrt_cr(x * x) / msl;
 }
 OHG_HD double tri_quality_iso(const double p[3][2], double m) {
   double b00 = p[1][0] - p[0][0], b01 = p[1][1] - p[0][1];
@@ -286,12 +290,12 @@ OHG_HD double tri_quality_iso(const double p[3][2], double m) {
   double x = s / kEquilateralTri;
   return x / msl;
 }
-OHG_HD double iso_log(double m) { return fabs(m) <= 1e-10 ? log(0.0) : log(m); }
+OHG_HD double iso_log(double m) { return fabs(m) <= 1e-10 ? log_cr(0.0) : log_cr(m); }
 OHG_HD double average_metric_iso(double a, double b) {
   double am = 0.0 + iso_log(a);
   am = am + iso_log(b);
   am = am / 2;
-  return fabs(am) <= 1e-10 ? exp(0.0) : exp(am);
+  return fabs(am) <= 1e-10 ? exp_cr(0.0) : exp_cr(am);
 }
 
 // the determinant the maxdet choice compares: the tensor's, or the scalar
@@ -377,18 +381,18 @@ OHG_HD int cubic_roots(double a_0, double a_1, double a_2, double eps, double rt
   double D = cube(Q) + sq(R);
   double shift = -a_2 / 3.;
   if (D >= 0.0) {
-    double S = cbrt(R + sqrt(D));
-    double T = cbrt(R - sqrt(D));
+    double S = cbrt_cr(R + sqrt(D));
+    double T = cbrt_cr(R - sqrt(D));
     double B = S + T;
     rt[0] = shift + B;
     rt[1] = rt[2] = shift - (1. / 2.) * B;
   } else {
     double ct = R / sqrt(-cube(Q));
-    double theta = acos(min2d(max2d(ct, -1.0), 1.0));
+    double theta = acos_cr(min2d(max2d(ct, -1.0), 1.0));
     double radius = 2. * sqrt(-Q);
-    rt[0] = radius * cos((theta) / 3.) + shift;
-    rt[1] = radius * cos((theta + 2. * PI) / 3.) + shift;
-    rt[2] = radius * cos((theta - 2. * PI) / 3.) + shift;
+    rt[0] = radius * cos_cr((theta) / 3.) + shift;
+    rt[1] = radius * cos_cr((theta + 2. * PI) / 3.) + shift;
+    rt[2] = radius * cos_cr((theta - 2. * PI) / 3.) + shift;
   }
   mult[0] = mult[1] = mult[2] = 1;
   if (fabs(rt[0] - rt[1]) < eps) {
@@ -491,7 +495,7 @@ OHG_HD bool average_metric3(const double* m0, const double* m1, double* out) {
   for (int k = 0; k < 2; ++k) {
     Eig3 e = eigen3(symm3(k == 0 ? m0 : m1));
     ok = ok && e.ok;
-    for (int i = 0; i < 3; ++i) e.l.x[i] = log(e.l.x[i]);
+    for (int i = 0; i < 3; ++i) e.l.x[i] = log_cr(e.l.x[i]);
     M3 L = compose_ortho3(e.q, e.l);
     for (int j = 0; j < 3; ++j)
       for (int i = 0; i < 3; ++i) am.c[j].x[i] = am.c[j].x[i] + L.c[j].x[i];
@@ -500,7 +504,7 @@ OHG_HD bool average_metric3(const double* m0, const double* m1, double* out) {
     for (int i = 0; i < 3; ++i) am.c[j].x[i] = am.c[j].x[i] / 2;
   Eig3 e = eigen3(am);
   ok = ok && e.ok;
-  for (int i = 0; i < 3; ++i) e.l.x[i] = exp(e.l.x[i]);
+  for (int i = 0; i < 3; ++i) e.l.x[i] = exp_cr(e.l.x[i]);
   unsymm3(compose_ortho3(e.q, e.l), out);
   return ok;
 }
@@ -620,7 +624,7 @@ OHG_HD bool average_metric2(const double* m0, const double* m1, double* out) {
   for (int k = 0; k < 2; ++k) {
     Eig2 e = eigen2(symm2(k == 0 ? m0 : m1));
     ok = ok && e.ok;
-    for (int i = 0; i < 2; ++i) e.l.x[i] = log(e.l.x[i]);
+    for (int i = 0; i < 2; ++i) e.l.x[i] = log_cr(e.l.x[i]);
     M2 L = compose_ortho2(e.q, e.l);
     for (int j = 0; j < 2; ++j)
       for (int i = 0; i < 2; ++i) am.c[j].x[i] = am.c[j].x[i] + L.c[j].x[i];
@@ -629,7 +633,7 @@ OHG_HD bool average_metric2(const double* m0, const double* m1, double* out) {
     for (int i = 0; i < 2; ++i) am.c[j].x[i] = am.c[j].x[i] / 2;
   Eig2 e = eigen2(am);
   ok = ok && e.ok;
-  for (int i = 0; i < 2; ++i) e.l.x[i] = exp(e.l.x[i]);
+  for (int i = 0; i < 2; ++i) e.l.x[i] = exp_cr(e.l.x[i]);
   M2 r = compose_ortho2(e.q, e.l);
   out[0] = r.c[0].x[0];
   out[1] = r.c[1].x[1];

@@ -61,13 +61,13 @@ OHG_HD M3 inv3(const M3& a) {
 OHG_HD M3 log_spd3(const M3& m, bool* ok) {
   Eig3 e = eigen3(m);
   *ok = *ok && e.ok;
-  for (int i = 0; i < 3; ++i) e.l.x[i] = log(e.l.x[i]);
+  for (int i = 0; i < 3; ++i) e.l.x[i] = log_cr(e.l.x[i]);
   return compose_ortho3(e.q, e.l);
 }
 OHG_HD M3 exp_spd3(const M3& m, bool* ok) {
   Eig3 e = eigen3(m);
   *ok = *ok && e.ok;
-  for (int i = 0; i < 3; ++i) e.l.x[i] = exp(e.l.x[i]);
+  for (int i = 0; i < 3; ++i) e.l.x[i] = exp_cr(e.l.x[i]);
   return compose_ortho3(e.q, e.l);
 }
 OHG_HD double max_norm3(const M3& a) {
@@ -108,13 +108,13 @@ OHG_HD M2 inv2(const M2& m) {
 OHG_HD M2 log_spd2(const M2& m, bool* ok) {
   Eig2 e = eigen2(m);
   *ok = *ok && e.ok;
-  for (int i = 0; i < 2; ++i) e.l.x[i] = log(e.l.x[i]);
+  for (int i = 0; i < 2; ++i) e.l.x[i] = log_cr(e.l.x[i]);
   return compose_ortho2(e.q, e.l);
 }
 OHG_HD M2 exp_spd2(const M2& m, bool* ok) {
   Eig2 e = eigen2(m);
   *ok = *ok && e.ok;
-  for (int i = 0; i < 2; ++i) e.l.x[i] = exp(e.l.x[i]);
+  for (int i = 0; i < 2; ++i) e.l.x[i] = exp_cr(e.l.x[i]);
   return compose_ortho2(e.q, e.l);
 }
 OHG_HD double max_norm2(const M2& a) {
@@ -521,7 +521,7 @@ OHG_HD void average2(const double* const* ms, int n, bool has_degen, double* out
 double typical_unit_simplex_size(int dim) { return dim == 3 ? 0.0838934100219 : 0.377645136635; }
 double equilateral_simplex_size(int dim) { return dim == 3 ? 0.1178511301977579 : 0.4330127018922193; }
 // power(x, 2, dim) of src/Omega_h_scalar.hpp: x^(2/dim)
-double power_2_over(double x, int dim) { return dim == 3 ? std::cbrt(x * x) : x; }
+double power_2_over(double x, int dim) { return dim == 3 ? cbrt_cr(x * x) : x; }
 
 // per-vertex metrics from per-element ones (project_metrics,
 // src/Omega_h_metric.cpp:222-252): log-Euclidean mean over the elements of
@@ -628,7 +628,7 @@ Arr<double> size_isos(int dim, LO n, const double* m_p) {
   auto o = view(out);
   pfor(n, [=] __device__(LO i) {
     if (dim == 3) {
-      o[i] = cbrt(det3(symm3(&mm[i * 6])));
+      o[i] = cbrt_cr(det3(symm3(&mm[i * 6])));
     } else {
       M2 s = symm2(&mm[i * 3]);
       o[i] = sqrt(s.c[0].x[0] * s.c[1].x[1] - s.c[1].x[0] * s.c[0].x[1]);

@@ -23,8 +23,9 @@
 //  * bound arithmetic itself is done in round-to-nearest on non-negative
 //    terms and inflated by (1 + 2^-15), which covers the relative error of
 //    the at most ~200 roundings along any chain;
-//  * cbrtf, logf (CUDA: at most 1 ulp) and the double cbrt/log (at most 1
-//    ulp) are covered by widening their results by 2^-20 / 2^-15 relative;
+//  * cbrtf, logf (CUDA: at most 1 ulp) and the double cbrt and log
+//    (correctly rounded) are covered by widening their results by
+//    2^-20 / 2^-15 relative;
 //  * anything non-finite widens the interval to [-inf, +inf].
 #pragma once
 #include <cfloat>
@@ -365,7 +366,7 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
   float ey = __fmaf_rn(fabsf(y), kC1, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
   ey = __fmul_rn(ey, kInflate);
   // cbrt over [y - ey, y + ey] from one cbrtf (at most 1 ulp; the double
-  // cbrt at most 1 ulp too): with d = ey / y,
+  // cbrt is correctly rounded): with d = ey / y,
   //   (1 + d)^(1/3) <= 1 + d/3 and (1 - d)^(1/3) >= 1 - d/3 - d^2 (d <= 1/2)
   float r_lo, r_hi;
   if (!(y < 1e30f) || !(ey < 1e30f)) return widen_all();  // keeps __fdividef in range
@@ -417,7 +418,7 @@ __device__ __forceinline__ double tet_quality_exact(const ScreenView& s, View<co
   }
   msl = msl / 6;
   double x = sz / kEquilateralTet;
-  return cbrt(x * x) / msl;
+  return cbrt_cr(x * x) / msl;
 }
 
 // ------------------------------------------------------------ 2D

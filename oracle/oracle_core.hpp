@@ -17,6 +17,8 @@
 #include <utility>
 #include <vector>
 
+#include "../omega_h_gb300/csrc/ohg_libm.cuh"
+
 // Independent per-entity loops run on all host threads when built with
 // OpenMP, as the reference's parallel_for does in its OpenMP build; every
 // iteration writes only its own outputs, so results do not depend on the
@@ -30,29 +32,20 @@
 namespace orc {
 
 // The libm functions on the path.  Built with -DORC_CR_LIBM=<mask> (bits:
-// 1 cbrt, 2 acos, 4 cos, 8 log, 16 exp) the selected ones are replaced by
-// the long-double function rounded to double (correctly rounded unless the
-// extended result lies within its own error of a halfway point): test
-// infrastructure for measuring how the reference's results depend on the
-// last ulp of each function.
+// 1 cbrt, 2 acos, 4 cos, 8 log, 16 exp) the selected ones are replaced by the
+// library's correctly rounded functions (ohg_libm.cuh, the functions the GPU
+// path calls).  Test infrastructure: with all five (mask 31) it is the
+// reference's algorithm with the GPU path's elementary functions; with some
+// of them it measures how the reference's results depend on the last ulp of
+// each function.
 #ifndef ORC_CR_LIBM
 #define ORC_CR_LIBM 0
 #endif
-inline double orc_cbrt(double x) {
-  return (ORC_CR_LIBM & 1) ? double(cbrtl((long double)x)) : std::cbrt(x);
-}
-inline double orc_acos(double x) {
-  return (ORC_CR_LIBM & 2) ? double(acosl((long double)x)) : std::acos(x);
-}
-inline double orc_cos(double x) {
-  return (ORC_CR_LIBM & 4) ? double(cosl((long double)x)) : std::cos(x);
-}
-inline double orc_log(double x) {
-  return (ORC_CR_LIBM & 8) ? double(logl((long double)x)) : std::log(x);
-}
-inline double orc_exp(double x) {
-  return (ORC_CR_LIBM & 16) ? double(expl((long double)x)) : std::exp(x);
-}
+inline double orc_cbrt(double x) { return (ORC_CR_LIBM & 1) ? ohg::cbrt_cr(x) : std::cbrt(x); }
+inline double orc_acos(double x) { return (ORC_CR_LIBM & 2) ? ohg::acos_cr(x) : std::acos(x); }
+inline double orc_cos(double x) { return (ORC_CR_LIBM & 4) ? ohg::cos_cr(x) : std::cos(x); }
+inline double orc_log(double x) { return (ORC_CR_LIBM & 8) ? ohg::log_cr(x) : std::log(x); }
+inline double orc_exp(double x) { return (ORC_CR_LIBM & 16) ? ohg::exp_cr(x) : std::exp(x); }
 
 typedef std::int32_t LO;
 typedef std::int64_t GO;

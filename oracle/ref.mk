@@ -53,4 +53,34 @@ $(OUT)/libomega_h_ref.a: $(OBJS)
 $(OUT)/ref_driver: oracle/ref_driver.cpp omega_h_gb300/csrc/ohg_workload.hpp $(OUT)/libomega_h_ref.a
 	$(CXX) $(CXXFLAGS) -Ioracle oracle/ref_driver.cpp $(OUT)/libomega_h_ref.a -o $@
 
-.PHONY: all
+# The reference's OpenMP backend (the reference's -DOmega_h_USE_OpenMP=ON, with
+# CMake's Release flags -O3 -DNDEBUG):
+# the same sources with OMEGA_H_USE_OPENMP defined and -fopenmp, into
+# oracle/_ref/omp/, for timing the reference's own parallel build.
+#   make -f oracle/ref.mk REF=<reference source checkout> omp -j8
+OMP := $(OUT)/omp
+OMP_CXXFLAGS := -O3 -DNDEBUG -std=c++17 -ffp-contract=off -fno-fast-math -w -fopenmp \
+            -I$(OMP)/include -I$(REF)/src -I$(REF)/tpl -Iomega_h_gb300/csrc
+OMP_OBJS := $(patsubst %,$(OMP)/obj/Omega_h_%.o,$(SRC_NAMES))
+
+$(OMP)/include/Omega_h_config.h:
+	mkdir -p $(OMP)/include $(OMP)/obj
+	printf '%s\n' '#ifndef OMEGA_H_CONFIG_H' '#define OMEGA_H_CONFIG_H' \
+	  '#define OMEGA_H_VERSION_MAJOR 9' '#define OMEGA_H_VERSION_MINOR 34' \
+	  '#define OMEGA_H_VERSION_PATCH 13' '#define OMEGA_H_SEMVER "9.34.13"' \
+	  '#define OMEGA_H_USE_OPENMP' \
+	  '#define OMEGA_H_CXX_FLAGS ""' '#define OMEGA_H_CMAKE_ARGS ""' '#define OMEGA_H_COMMIT ""' \
+	  '#endif' > $@
+
+$(OMP)/obj/%.o: $(REF)/src/%.cpp $(OMP)/include/Omega_h_config.h
+	$(CXX) $(OMP_CXXFLAGS) -c $< -o $@
+
+$(OMP)/libomega_h_ref.a: $(OMP_OBJS)
+	ar rcs $@ $^
+
+$(OMP)/ref_driver: oracle/ref_driver.cpp omega_h_gb300/csrc/ohg_workload.hpp $(OMP)/libomega_h_ref.a
+	$(CXX) $(OMP_CXXFLAGS) -Ioracle oracle/ref_driver.cpp $(OMP)/libomega_h_ref.a -o $@
+
+omp: $(OMP)/ref_driver
+
+.PHONY: all omp

@@ -63,6 +63,22 @@ def test_full_adapt_matches_reference(ctx, oracle_driver, case):
     assert [r[k] for k in names] == [int(x) for x in want]
 
 
+@pytest.mark.parametrize("case", sorted(ADAPT_CASES))
+def test_full_adapt_matches_oracle_with_the_same_cube_root(ctx, oracle_cr_driver, case):
+    """The full loop against the reference's algorithm run on the host with
+    the GPU path's correctly rounded cube root: every integer of the final
+    mesh bit-exact (box8_iso_adapt included) and every real within 1e-12."""
+    r, got = _adapt(ctx, *ADAPT_CASES[case])
+    want = run_oracle(oracle_cr_driver, ADAPT_CASES[case], mode="adapt")
+    keys = [k for k in want if k.startswith("out_") and k in got]
+    fails, maxerr, ndiff = compare_arrays(want, got, keys=keys, interp=False)
+    print(f"{case}: max real rel err {maxerr:.2e}, {ndiff} reals not bitwise equal")
+    assert not fails, fails[:10]
+    names = ["did", "quality_satisfied", "refines", "coarsens", "swaps", "sliver_coarsens",
+             "length_rounds"]
+    assert [r[k] for k in names] == [int(x) for x in want["adapt_result"]]
+
+
 def test_full_adapt_screened_equals_fp64(ctx):
     outs = []
     for screening in (True, False):

