@@ -2,10 +2,12 @@
 // device, so that the same argument gives the same double on either side
 // (every step is an IEEE operation or an explicit fused multiply-add).
 //
-// cbrt_cr: the cube root rounded to nearest.  A Newton iterate gives a
-// significand within a few units of the answer; the answer is then decided
-// exactly, in 192-bit integer arithmetic, by comparing the cubes of the
-// halfway points between neighbouring doubles with the argument.  With the
+// cbrt_cr: the cube root rounded to nearest.  Newton iterates, the last one
+// with its residual computed in double-double, give the answer within about
+// 2^-88; when that is not far enough from a halfway point to settle the
+// rounding, the answer is decided exactly, in 192-bit integer arithmetic, by
+// comparing the cubes of the halfway points between neighbouring doubles
+// with the argument.  With the
 // argument reduced to m in [1, 8) (m = M 2^-52, M an integer below 2^55)
 // and a candidate y = C 2^-52 in [1, 2], the halfway point (2C+1) 2^-53 lies
 // below cbrt(m) exactly when (2C+1)^3 < M 2^107.  The left side is odd and
@@ -18,7 +20,9 @@
 // extending the available precision", Numer. Math. 18, 1971) to a relative
 // error near 2^-90 before the one final rounding, which is therefore the
 // correct rounding unless the exact value lies within about 2^-90 of a
-// halfway point between doubles.
+// halfway point between doubles.  A quick evaluation to about 2^-69 comes
+// first; it is returned when Ziv's rounding test shows that its error cannot
+// change the rounding (nearly always), else the accurate one decides.
 //   log: x = 2^E f, f in [sqrt(1/2), sqrt(2)); with c = j/256 nearest f and
 //   inv = the double nearest 1/c, log x = E ln 2 + log(1/inv) + log1p(r),
 //   r = f inv - 1 exactly (|r| < 2^-8.4), log1p(r) = 2 atanh(r / (2 + r)).
@@ -46,59 +50,13 @@
 #define OHG_LIBM_TAB(name) ohg_libm_h_##name
 #endif
 
-namespace ohg {
-
-// 64 x 64 -> 128-bit product
-OHG_HD void mul_64x64(std::uint64_t a, std::uint64_t b, std::uint64_t* hi, std::uint64_t* lo) {
-#ifdef __CUDA_ARCH__
-  *lo = a * b;
-  *hi = __umul64hi(a, b);
-#else
-  unsigned __int128 p = (unsigned __int128)a * b;
-  *lo = std::uint64_t(p);
-  *hi = std::uint64_t(p >> 64);
+// The quick evaluations are on by default; OHG_LIBM_QUICK=0 leaves only the
+// accurate ones (a test hook: both must give the same doubles).
+#ifndef OHG_LIBM_QUICK
+#define OHG_LIBM_QUICK 1
 #endif
-}
 
-// a^3 < M 2^107 for odd a < 2^55 and M < 2^55, exactly
-OHG_HD bool cube_below(std::uint64_t a, std::uint64_t M) {
-  std::uint64_t sh, sl;  // a^2 = sh 2^64 + sl (< 2^110)
-  mul_64x64(a, a, &sh, &sl);
-  std::uint64_t lh, ll, hh, hl;  // sl a and sh a; a^3 = (hh, hl + lh, ll) in 64-bit words
-  mul_64x64(sl, a, &lh, &ll);
-  mul_64x64(sh, a, &hh, &hl);
-  std::uint64_t w1 = lh + hl;
-  std::uint64_t w2 = hh + (w1 < lh ? 1u : 0u);
-  // M 2^107 = (M >> 21) 2^128 + (M << 43 mod 2^64) 2^64
-  std::uint64_t r2 = M >> 21, r1 = M << 43;
-  if (w2 != r2) return w2 < r2;
-  if (w1 != r1) return w1 < r1;
-  return false;  // equal high words: a^3 has a nonzero (odd) low word, M 2^107 none
-}
-
-OHG_HD double cbrt_cr(double x) {
-  if (x == 0.0 || !(x == x) || x - x != 0.0) return x + x;  // zero (sign kept), NaN, inf
-  double ax = fabs(x);
-  int e;
-  double f = frexp(ax, &e);  // ax = f 2^e, f in [0.5, 1), subnormals included
-  int E = e - 1;             // ax = (2f) 2^E with 2f in [1, 2)
-  int k = E >= 0 ? E / 3 : -((2 - E) / 3);
-  int r = E - 3 * k;  // 0, 1 or 2
-  double m = ldexp(2.0 * f, r);  // in [1, 8); the cube root of ax is cbrt(m) 2^k
-  double y = double(cbrtf(float(m)));
-  y = y - (y * y * y - m) / (3.0 * y * y);
-  y = y - (y * y * y - m) / (3.0 * y * y);
-  const std::uint64_t one = std::uint64_t(1) << 52, two = std::uint64_t(1) << 53;
-  double ys = ldexp(y, 52);
-  std::uint64_t C = ys <= double(one) ? one : ys >= double(two) ? two : std::uint64_t(ys);
-  std::uint64_t M = std::uint64_t(ldexp(m, 52));
-  // raise C while the halfway point above it is below cbrt(m), lower it while
-  // the halfway point below it is above; a few steps at most
-  for (int it = 0; it < 8 && C < two && cube_below(2 * C + 1, M); ++it) ++C;
-  for (int it = 0; it < 8 && C > one && !cube_below(2 * C - 1, M); ++it) --C;
-  double res = ldexp(double(C), k - 52);
-  return x < 0.0 ? -res : res;
-}
+namespace ohg {
 
 // ------------------------------------------------------------ double-double
 struct DD {
@@ -152,10 +110,92 @@ OHG_HD DD dd_div(DD a, DD b) {
   return dd_add(q, DD{q3, 0.0});
 }
 
+// Whether the exact value, known to lie within err of the normalised pair
+// hi + lo (hi = fl(hi + lo), hi normal), rounds to hi: it must stay strictly
+// between the halfway points around hi (the one below |hi| is closer when
+// |hi| is a power of two).  This is the rounding test of Ziv's strategy:
+// a quick evaluation is returned when the test passes, else an accurate one
+// decides.
+OHG_HD bool rounds_to_hi(double hi, double lo, double err) {
+  if (!(fabs(hi) >= 0x1p-1020) || !(fabs(hi) <= 0x1p1020)) return false;
+  int e = ilogb(hi);
+  double half_up = ldexp(1.0, e - 53);
+  bool pow2 = fabs(hi) == ldexp(1.0, e);
+  bool toward_zero = (lo < 0.0) == (hi > 0.0);
+  double margin = (toward_zero && pow2) ? 0.5 * half_up : half_up;
+  return fabs(lo) + err < margin;
+}
+
+// ------------------------------------------------------------ cbrt
+// 64 x 64 -> 128-bit product
+OHG_HD void mul_64x64(std::uint64_t a, std::uint64_t b, std::uint64_t* hi, std::uint64_t* lo) {
+#ifdef __CUDA_ARCH__
+  *lo = a * b;
+  *hi = __umul64hi(a, b);
+#else
+  unsigned __int128 p = (unsigned __int128)a * b;
+  *lo = std::uint64_t(p);
+  *hi = std::uint64_t(p >> 64);
+#endif
+}
+
+// a^3 < M 2^107 for odd a < 2^55 and M < 2^55, exactly
+OHG_HD bool cube_below(std::uint64_t a, std::uint64_t M) {
+  std::uint64_t sh, sl;  // a^2 = sh 2^64 + sl (< 2^110)
+  mul_64x64(a, a, &sh, &sl);
+  std::uint64_t lh, ll, hh, hl;  // sl a and sh a; a^3 = (hh, hl + lh, ll) in 64-bit words
+  mul_64x64(sl, a, &lh, &ll);
+  mul_64x64(sh, a, &hh, &hl);
+  std::uint64_t w1 = lh + hl;
+  std::uint64_t w2 = hh + (w1 < lh ? 1u : 0u);
+  // M 2^107 = (M >> 21) 2^128 + (M << 43 mod 2^64) 2^64
+  std::uint64_t r2 = M >> 21, r1 = M << 43;
+  if (w2 != r2) return w2 < r2;
+  if (w1 != r1) return w1 < r1;
+  return false;  // equal high words: a^3 has a nonzero (odd) low word, M 2^107 none
+}
+
+OHG_HD double cbrt_cr(double x) {
+  if (x == 0.0 || !(x == x) || x - x != 0.0) return x + x;  // zero (sign kept), NaN, inf
+  double ax = fabs(x);
+  int e;
+  double f = frexp(ax, &e);  // ax = f 2^e, f in [0.5, 1), subnormals included
+  int E = e - 1;             // ax = (2f) 2^E with 2f in [1, 2)
+  int k = E >= 0 ? E / 3 : -((2 - E) / 3);
+  int r = E - 3 * k;  // 0, 1 or 2
+  double m = ldexp(2.0 * f, r);  // in [1, 8); the cube root of ax is cbrt(m) 2^k
+  double y = double(cbrtf(float(m)));
+  y = y - (y * y * y - m) / (3.0 * y * y);  // within about 2^-45 relative
+  {
+    // one more Newton step with the residual y^3 - m computed to about
+    // 2^-104 relative: y - res / (3 y^2) as a pair, within about 2^-88
+    DD y2 = two_prod(y, y);
+    DD y3 = two_prod(y2.hi, y);
+    double res = ((y3.hi - m) + y3.lo) + y2.lo * y;
+    DD z = fast_two_sum(y, -res / (3.0 * y2.hi));
+    if (OHG_LIBM_QUICK && z.hi >= 1.0 && z.hi < 2.0 && rounds_to_hi(z.hi, z.lo, 0x1p-80)) {
+      double r1 = ldexp(z.hi, k);
+      return x < 0.0 ? -r1 : r1;
+    }
+    y = z.hi;
+  }
+  const std::uint64_t one = std::uint64_t(1) << 52, two = std::uint64_t(1) << 53;
+  double ys = ldexp(y, 52);
+  std::uint64_t C = ys <= double(one) ? one : ys >= double(two) ? two : std::uint64_t(ys);
+  std::uint64_t M = std::uint64_t(ldexp(m, 52));
+  // raise C while the halfway point above it is below cbrt(m), lower it while
+  // the halfway point below it is above; a few steps at most
+  for (int it = 0; it < 8 && C < two && cube_below(2 * C + 1, M); ++it) ++C;
+  for (int it = 0; it < 8 && C > one && !cube_below(2 * C - 1, M); ++it) --C;
+  double res = ldexp(double(C), k - 52);
+  return x < 0.0 ? -res : res;
+}
+
 // ------------------------------------------------------------ log
 OHG_HD double log_cr(double x) {
   if (!(x > 0.0)) return x == 0.0 ? -INFINITY : NAN;  // zero, negative, NaN
   if (x - x != 0.0) return x;                            // +inf
+  if (x == 1.0) return 0.0;
   int e;
   double f = 2.0 * frexp(x, &e);  // x = f 2^(e-1), f in [1, 2), subnormals included
   int E = e - 1;
@@ -168,6 +208,28 @@ OHG_HD double log_cr(double x) {
   double inv = OHG_LIBM_TAB(log_inv)[j - OHG_LOG_J0];
   DD p = two_prod(f, inv);
   DD r = two_sum(p.hi - 1.0, p.lo);  // f inv - 1, exactly
+  double Ed = double(E);
+  DD L = {OHG_LIBM_TAB(log_hi)[j - OHG_LOG_J0], OHG_LIBM_TAB(log_lo)[j - OHG_LOG_J0]};
+  {
+    // quick evaluation, within 2^-69 relative: E ln2 + L + r - r^2/2 with the
+    // leading terms added exactly, the series from r^3 on in double
+    double rh = r.hi, rl = r.lo;
+    DD q = two_prod(rh, rh);
+    double p3 = (rh * q.hi) *
+                (1.0 / 3.0 +
+                 rh * (-1.0 / 4.0 +
+                       rh * (1.0 / 5.0 +
+                             rh * (-1.0 / 6.0 +
+                                   rh * (1.0 / 7.0 + rh * (-1.0 / 8.0 + rh * (1.0 / 9.0 - rh / 10.0)))))));
+    DD a = two_sum(Ed * OHG_LN2_HI, L.hi);
+    DD b = two_sum(a.hi, rh);
+    DD c = two_sum(b.hi, -0.5 * q.hi);
+    double lo = ((a.lo + b.lo) + c.lo) +
+                ((Ed * OHG_LN2_MID + L.lo) + ((rl - 0.5 * q.lo) + ((rl * q.hi - rh * rl) + p3)));
+    DD y = fast_two_sum(c.hi, lo);
+    if (OHG_LIBM_QUICK && rounds_to_hi(y.hi, y.lo, 0x1p-66 * fabs(y.hi))) return y.hi;
+  }
+  // accurate evaluation, within about 2^-90:
   // log1p(r) = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...), s = r / (2 + r)
   DD s = dd_div(r, dd_add(DD{2.0, 0.0}, r));
   DD s2 = dd_mul(s, s);
@@ -178,10 +240,8 @@ OHG_HD double log_cr(double x) {
   const DD two_thirds = {0.66666666666666663, 3.7007434154171883e-17};
   DD l1p = dd_add(DD{2.0 * s.hi, 2.0 * s.lo}, dd_add(dd_mul(s3, two_thirds), DD{tail, 0.0}));
   // E ln 2: E HI exact (|E| < 2^11), E MID exact by two_prod, E LO rounded
-  double Ed = double(E);
   DD eln2 = dd_add(DD{Ed * OHG_LN2_HI, 0.0}, two_prod(Ed, OHG_LN2_MID));
   eln2 = dd_add(eln2, DD{Ed * OHG_LN2_LO, 0.0});
-  DD L = {OHG_LIBM_TAB(log_hi)[j - OHG_LOG_J0], OHG_LIBM_TAB(log_lo)[j - OHG_LOG_J0]};
   DD res = dd_add(dd_add(eln2, L), l1p);
   return res.hi + res.lo;
 }
@@ -198,6 +258,27 @@ OHG_HD double exp_cr(double x) {
   DD r = two_sum(a, -pm.hi);
   r.lo = (r.lo - pm.lo) - kd * OHG_LN2_128_LO;
   r = fast_two_sum(r.hi, r.lo);
+  long long k = (long long)kd;
+  int jj = int(k & 127);
+  int q = int((k - jj) / 128);
+  DD T = {OHG_LIBM_TAB(exp_hi)[jj], OHG_LIBM_TAB(exp_lo)[jj]};
+  if (q > -1000 && q < 1000) {
+    // quick evaluation, within 2^-69 relative: T (1 + r + r^2/2 + ...) with
+    // T, T r and T r^2/2 added exactly, the rest in double
+    double rh = r.hi, rl = r.lo;
+    DD sq = two_prod(rh, rh);
+    double p3 = (rh * sq.hi) *
+                (1.0 / 6.0 + rh * (1.0 / 24.0 + rh * (1.0 / 120.0 + rh * (1.0 / 720.0 + rh / 5040.0))));
+    DD a = two_prod(T.hi, rh);
+    DD b = two_sum(T.hi, a.hi);
+    DD c = two_prod(T.hi, 0.5 * sq.hi);
+    DD d = two_sum(b.hi, c.hi);
+    double lo = ((b.lo + d.lo) + (a.lo + c.lo)) +
+                (T.lo + (T.hi * ((rl + 0.5 * sq.lo) + (rh * rl + p3)) + T.lo * rh));
+    DD y = fast_two_sum(d.hi, lo);
+    if (OHG_LIBM_QUICK && rounds_to_hi(y.hi, y.lo, 0x1p-66 * fabs(y.hi))) return ldexp(y.hi, q);
+  }
+  // accurate evaluation, within about 2^-90:
   // exp(r) - 1 = r + r^2/2 + r^3/6 + r^4 (1/24 + r/120 + ...), |r| < 2^-8.5
   DD r2 = dd_mul(r, r);
   DD r3 = dd_mul(r2, r);
@@ -207,10 +288,6 @@ OHG_HD double exp_cr(double x) {
                  rh * (1.0 / 120.0 + rh * (1.0 / 720.0 + rh * (1.0 / 5040.0 + rh / 40320.0))));
   const DD sixth = {0.16666666666666666, 9.2518585385429707e-18};
   DD em1 = dd_add(r, dd_add(DD{0.5 * r2.hi, 0.5 * r2.lo}, dd_add(dd_mul(r3, sixth), DD{tail, 0.0})));
-  long long k = (long long)kd;
-  int jj = int(k & 127);
-  int q = int((k - jj) / 128);
-  DD T = {OHG_LIBM_TAB(exp_hi)[jj], OHG_LIBM_TAB(exp_lo)[jj]};
   DD res = dd_add(T, dd_mul(T, em1));
   double y = res.hi + res.lo;
   if (q > 1000) return 2.0 * ldexp(y, q - 1);  // keeps ldexp's argument in range
