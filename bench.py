@@ -47,24 +47,33 @@ BATCH = {"workload": "batch1024_sine", "meshes": 1024, "n_min": 4, "n_max": 40, 
 # Serving workload: Poisson arrivals; half 2D squares (n log-uniform in
 # [16, 1024]), half 3D boxes (n log-uniform in [4, 64]); metric family
 # uniform over isotropic sine, shock and boundary layer; 1 to 3 passes per
-# request; 150 GB admission budget.  A bounded sample of the stream is served
-# at each rate so the run stays within minutes.
-SERVE = {"workload": "serve_mix", "requests": 160, "rates_per_s": [50.0, 200.0, 800.0],
+# request; 150 GB admission budget.  Requests arrive as box specifications:
+# each mesh is built on the device when its request is admitted (served) or
+# arrives (plain), inside its latency, and freed when it is done.  The
+# default run serves the first requests of the seeded 20,000-request stream
+# (the count per rate below; the saturating rate is last);
+# --serve-requests 20000 serves the whole stream at the saturating rate.
+SERVE = {"workload": "serve_mix", "stream_requests": 20000,
+         "rates_per_s": [50.0, 200.0, 800.0], "requests_per_rate": [250, 1000, 2000],
          "budget_gb": 150.0, "seed": 11, "slots_per_dim": 2}
 
 
-def serve_specs(sv=SERVE):
+def serve_specs(sv=SERVE, count=None):
+    """(dim, n, metric kind, seed, passes) of the seeded stream's first
+    ``count`` requests, and their exponential inter-arrival gaps (unit mean)."""
     import numpy as np
     rng = np.random.default_rng(sv["seed"])
     out = []
-    for _ in range(sv["requests"]):
+    total = sv["stream_requests"]
+    for _ in range(total):
         dim = 2 if rng.uniform() < 0.5 else 3
         lo, hi = (16, 1024) if dim == 2 else (4, 64)
         n = int(np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1)))), lo, hi))
         kind = int(rng.choice([3, 1, 2]))
         out.append((dim, n, kind, int(rng.integers(1, 2 ** 31)), int(rng.integers(1, 4))))
-    gaps = rng.exponential(1.0, sv["requests"])
-    return out, gaps
+    gaps = rng.exponential(1.0, total)
+    count = total if count is None else count
+    return out[:count], gaps[:count]
 
 
 def batch_specs(b=BATCH):
@@ -85,6 +94,9 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
+    ap.add_argument("--serve-requests", type=int, default=0,
+                    help="requests served at the saturating rate (default: the bounded "
+                         "sample; 20000 serves the whole stream)")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the boundary-layer precision workloads")
     ap.add_argument("--no-tools", action="store_true", help="skip the .osh and metric tools")
@@ -425,67 +437,53 @@ def run_batch(ctx, lib_stream, flush, args):
 
 def run_serve(ctx, args, slots_per_dim=None):
     """The serving workload at each arrival rate: continuous batching against
-    one request at a time, the same requests (resident meshes cloned from the
-    same bases) and the same arrival times.  Batching routes each request to
-    one of slots_per_dim contexts of its dimension; their union passes
-    overlap on the device."""
+    one request at a time, on the same requests and arrival times.  Each
+    request's mesh is built on the device at admission (served) or arrival
+    (plain) and freed when it is done.  Batching routes each request to one
+    of slots_per_dim contexts of its dimension, each with its own step loop;
+    admission counts device bytes measured by calibrate()."""
     import numpy as np
-    from omega_h_gb300.mesh import Mesh
-    from omega_h_gb300.serve import Request, route, serve, serve_one_at_a_time, summary
     from omega_h_gb300.mesh import Context
+    from omega_h_gb300.serve import Request, calibrate, serve, serve_one_at_a_time, summary
     k = slots_per_dim or SERVE["slots_per_dim"]
-    specs, gaps = serve_specs()
     extra = [Context(ctx.device) for _ in range(2 * k - 1)]
     slots = {3: [ctx] + extra[:k - 1], 2: extra[k - 1:]}
-    ctxs = {3: ctx, 2: slots[2][0]}
-    bases = []
-    for dim, n, kind, seed, _ in specs:
-        m = Mesh.build_box(ctxs[dim], dim, n)
-        m.apply_workload(n, seed, kind)
-        bases.append(m)
-    elements = sum(m.nelems() for m in bases)
-    dims = [sp[0] for sp in specs]
-    where = route(dims, [b.nelems() * sp[4] for b, sp in zip(bases, specs)],
-                  {d: len(c) for d, c in slots.items()})
+    bpe, peak = calibrate({d: c[0] for d, c in slots.items()})
+    counts = list(SERVE["requests_per_rate"])
+    if args.serve_requests:
+        counts = [min(c, args.serve_requests) for c in counts[:-1]] + [args.serve_requests]
 
-    def stream(rate, routed):
+    def stream(rate, count):
+        specs, gaps = serve_specs(count=count)
         arr = np.cumsum(gaps) / rate
         arr -= arr[0]
-        reqs = []
-        for i, (b, sp) in enumerate(zip(bases, specs)):
-            h = ctypes.c_void_p()
-            target = slots[sp[0]][where[i]] if routed else ctxs[sp[0]]
-            _lib_call("ohg_mesh_clone_to", b.handle, target.handle, ctypes.byref(h))
-            reqs.append(Request(rid=i, arrival=float(arr[i]), mesh=Mesh(target, h),
-                                passes=sp[4]))
-        return reqs
+        return [Request(rid=i, arrival=float(arr[i]), passes=p, dim=d, n=n, kind=kk, seed=sd)
+                for i, (d, n, kk, sd, p) in enumerate(specs)]
 
-    # warm both paths once on a few requests
-    for fn, routed in ((lambda r: serve(ctx, r), True), (lambda r: serve_one_at_a_time(ctx, r), False)):
-        w = stream(1e9, routed)[:6]
-        fn(w)
-        for r in w:
-            r.mesh.close()
+    # warm both paths on a few requests
+    serve(slots, stream(1e9, 6), bytes_per_element=bpe, pass_peak=peak, release=True)
+    serve_one_at_a_time(ctx, stream(1e9, 6), release=True)
     rates = []
-    for rate in SERVE["rates_per_s"]:
-        res = {}
-        for name, fn, routed in (
-                ("served", lambda r: serve(ctx, r, budget_bytes=SERVE["budget_gb"] * 1e9), True),
-                ("plain", lambda r: serve_one_at_a_time(ctx, r), False)):
-            reqs = stream(rate, routed)
-            out = fn(reqs)
-            res[name] = summary(out)
-            for r in out:
-                r.mesh.close()
-        res["rate_per_s"] = rate
-        res["served_over_plain"] = res["served"]["elements_per_s"] / max(res["plain"]["elements_per_s"], 1e-9)
+    for rate, count in zip(SERVE["rates_per_s"], counts):
+        res = {"rate_per_s": rate, "requests": count}
+        reqs = stream(rate, count)
+        out = serve(slots, reqs, budget_bytes=SERVE["budget_gb"] * 1e9, bytes_per_element=bpe,
+                    pass_peak=peak, release=True)
+        res["served"] = summary(out)
+        res["served"]["build_p50_ms"] = float(np.median([(r.built - r.admitted) * 1e3 for r in out]))
+        reqs = stream(rate, count)
+        out = serve_one_at_a_time(ctx, reqs, release=True)
+        res["plain"] = summary(out)
+        res["served_over_plain"] = res["served"]["elements_per_s"] / \
+            max(res["plain"]["elements_per_s"], 1e-9)
         rates.append(res)
-    for m in bases:
-        m.close()
     for c in extra:
         c.close()
-    return {"workload": SERVE["workload"], "requests": len(specs), "elements": elements,
-            "budget_gb": SERVE["budget_gb"], "slots_per_dim": k, "rates": rates}
+    return {"workload": SERVE["workload"], "stream_requests": SERVE["stream_requests"],
+            "budget_gb": SERVE["budget_gb"], "slots_per_dim": k,
+            "calibrated_bytes_per_element": bpe, "calibrated_pass_peak_over_resident": peak,
+            "meshes": "built on the device at admission (served) or arrival (plain), freed "
+                      "when done", "rates": rates}
 
 
 def _lib_call(name, *a):

@@ -161,6 +161,17 @@ int ohg_osh_zlib(int* available);
 int ohg_mesh_destroy(ohg_mesh* mesh);
 int ohg_mesh_dim(ohg_mesh* mesh, int* out);
 int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);
+/* Device memory held by a mesh: its arrays, derived adjacencies and caches,
+ * each buffer once (no counterpart in the reference; the serving loop's
+ * admission counts it). */
+int ohg_mesh_device_bytes(ohg_mesh* mesh, long long* bytes);
+/* The device's stream-ordered memory pool, which every context of the device
+ * in this process draws from: bytes in use, bytes reserved from the device,
+ * and the high-water mark of bytes in use (reset to the current use when
+ * reset_high is nonzero).  It neither waits on nor touches the context's
+ * stream, so any host thread may call it.  No counterpart in the reference. */
+int ohg_context_pool_bytes(ohg_context* ctx, int reset_high, long long* used,
+                           long long* reserved, long long* used_high);
 /* Size in bytes of a named mesh array, then a copy of it into caller device
  * memory.  Names: coords, metric, length, quality, ev2v_<d>, down_<d>,
  * downcodes_<d>, class_dim_<d>, class_id_<d>, global_<d>, up_a2ab_<lo><hi>,

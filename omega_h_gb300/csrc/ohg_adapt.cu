@@ -3,6 +3,7 @@
 #include <math_constants.h>
 
 #include <cfloat>
+#include <set>
 #include <cmath>
 
 #include "ohg_adapt.cuh"
@@ -2180,6 +2181,41 @@ static void swap_loops(Mesh& m, const LO* edges_p, LO n, Arr<int>& lsize, Arr<LO
     for (int k = 0; k < size; ++k) lv[i * 7 + k] = t0[k];
     ls[i] = size;
   });
+}
+
+// device bytes held by a mesh: every array it references (stored and
+// derived adjacencies, fields, cached lengths and qualities, screening data),
+// each buffer counted once (the parts of a split union share buffers)
+std::size_t mesh_device_bytes(const Mesh& m) {
+  std::set<const Buf*> seen;
+  std::size_t total = 0;
+  auto add = [&](const std::shared_ptr<Buf>& b) {
+    if (b && seen.insert(b.get()).second) total += b->bytes;
+  };
+  add(m.coords.buf);
+  add(m.metric.buf);
+  add(m.length.buf);
+  add(m.quality.buf);
+  for (int d = 0; d < 4; ++d) {
+    add(m.class_dim[d].buf);
+    add(m.class_id[d].buf);
+  }
+  for (const auto* cache : {&m.adj, &m.adj_any_order})
+    for (const auto& kv : *cache) {
+      add(kv.second.a2ab.buf);
+      add(kv.second.ab2b.buf);
+      add(kv.second.codes.buf);
+    }
+  for (const auto& t : m.extra_tags) add(t.bytes.buf);
+  if (m.screen) {
+    add(m.screen->xh.buf);
+    add(m.screen->xl.buf);
+    add(m.screen->ma.buf);
+    add(m.screen->mb.buf);
+    add(m.screen->dkey.buf);
+    add(m.screen->sdet.buf);
+  }
+  return total;
 }
 
 void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO* loop_verts) {

@@ -45,6 +45,8 @@ void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* q
 Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers);
 // swap2d_qualities (src/Omega_h_swap2d_qualities.cpp:15-81)
 void swap2d_qualities(Mesh& m, double max_length_allowed, const LO* c2e, LO n, double* quals);
+// device bytes held by a mesh (each buffer once)
+std::size_t mesh_device_bytes(const Mesh& m);
 // swap3d::find_loop per edge: ring size (0 outside 3..7), the edge's two
 // vertices, and up to 7 loop vertices per edge
 void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO* loop_verts);

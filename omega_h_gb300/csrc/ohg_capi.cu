@@ -442,6 +442,40 @@ int ohg_mesh_dim(ohg_mesh* m, int* out) {
   *out = m->mesh.dim;
   return OHG_OK;
 }
+int ohg_mesh_device_bytes(ohg_mesh* m, long long* out) {
+  MESH_GUARD(m);
+  if (!out) return OHG_ERR_INVALID;
+  *out = (long long)mesh_device_bytes(m->mesh);
+  return OHG_OK;
+}
+int ohg_context_pool_bytes(ohg_context* c, int reset_high, long long* used, long long* reserved,
+                           long long* used_high) {
+  if (!c || !used || !reserved || !used_high) {
+    g_err = "ohg_context_pool_bytes: null argument";
+    return OHG_ERR_INVALID;
+  }
+  // a device-level query: it touches neither the context's stream nor its
+  // status word, so any thread may call it while others use the context
+  cudaMemPool_t pool;
+  std::uint64_t u = 0, r = 0, h = 0;
+  cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, c->ctx.device);
+  if (e == cudaSuccess) e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u);
+  if (e == cudaSuccess) e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r);
+  if (e == cudaSuccess) e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &h);
+  if (e == cudaSuccess && reset_high) {
+    std::uint64_t zero = 0;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero);
+  }
+  if (e != cudaSuccess) {
+    g_err = std::string("memory pool query failed: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    return OHG_ERR_CUDA;
+  }
+  *used = (long long)u;
+  *reserved = (long long)r;
+  *used_high = (long long)h;
+  return OHG_OK;
+}
 int ohg_mesh_nents(ohg_mesh* m, int d, int* out) {
   MESH_GUARD(m);
   if (d < 0 || d > m->mesh.dim) return OHG_ERR_INVALID;

@@ -164,15 +164,19 @@ OHG_HD double cbrt_cr(double x) {
   int k = E >= 0 ? E / 3 : -((2 - E) / 3);
   int r = E - 3 * k;  // 0, 1 or 2
   double m = ldexp(2.0 * f, r);  // in [1, 8); the cube root of ax is cbrt(m) 2^k
-  double y = double(cbrtf(float(m)));
-  y = y - (y * y * y - m) / (3.0 * y * y);  // within about 2^-45 relative
+  // w ~ m^(-1/3): a float start and one division-free Newton step
+  // w (4 - m w^3) / 3 (about 2^-45 relative); y = m w^2 ~ m^(1/3)
+  double w = double(1.0f / cbrtf(float(m)));
+  w = (w * (4.0 - m * (w * (w * w)))) * (1.0 / 3.0);
+  double y = m * (w * w);
   {
     // one more Newton step with the residual y^3 - m computed to about
-    // 2^-104 relative: y - res / (3 y^2) as a pair, within about 2^-88
+    // 2^-104 relative and 1 / (3 y^2) taken as w^2 / 3: y - res w^2 / 3 as
+    // a pair, within about 2^-85
     DD y2 = two_prod(y, y);
     DD y3 = two_prod(y2.hi, y);
     double res = ((y3.hi - m) + y3.lo) + y2.lo * y;
-    DD z = fast_two_sum(y, -res / (3.0 * y2.hi));
+    DD z = fast_two_sum(y, -(res * (w * w)) * (1.0 / 3.0));
     if (OHG_LIBM_QUICK && z.hi >= 1.0 && z.hi < 2.0 && rounds_to_hi(z.hi, z.lo, 0x1p-80)) {
       double r1 = ldexp(z.hi, k);
       return x < 0.0 ? -r1 : r1;

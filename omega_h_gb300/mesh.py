@@ -45,6 +45,14 @@ class Context:
         _lib.call("ohg_context_syncs", self.handle, ctypes.byref(v))
         return v.value
 
+    def pool_bytes(self, reset_high=False):
+        """(bytes in use, bytes reserved, high-water mark of bytes in use) of
+        the device's memory pool, which all contexts of the device share."""
+        u, r, h = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.call("ohg_context_pool_bytes", self.handle, 1 if reset_high else 0,
+                  ctypes.byref(u), ctypes.byref(r), ctypes.byref(h))
+        return u.value, r.value, h.value
+
     def allocations(self):
         """Device allocations the library has made on this context."""
         v = ctypes.c_ulonglong()
@@ -157,6 +165,12 @@ class Mesh:
 
     def nelems(self):
         return self.nents(self.dim)
+
+    def device_bytes(self):
+        """Device memory held by the mesh (arrays, adjacencies, caches)."""
+        v = ctypes.c_longlong()
+        _lib.call("ohg_mesh_device_bytes", self.handle, ctypes.byref(v))
+        return v.value
 
     def get(self, name):
         """A copy of a named mesh array as a CUDA tensor."""

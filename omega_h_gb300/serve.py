@@ -1,60 +1,74 @@
 """Serving loop for adapt-pass requests with continuous batching.
 
-Requests arrive over time, each with a device-resident mesh and a number of
-passes.  The loop admits arrived requests in arrival order while their
-estimated device footprint fits the admission budget, and every step runs one
-adapt pass over the disjoint union of all admitted requests of a dimension
-(ohg_adapt_pass_batch): requests that arrive while a step runs join the next
-step, finished requests leave and free their memory.  Because a union pass is
-bit for bit the separate passes, a request's result does not depend on what
-it was batched with.
+A request names a mesh (a box of given dimension and subdivisions with a
+seeded metric family, or a mesh already on the device) and a number of
+passes.  Requests arrive over time.  The loop admits them in arrival order
+while their device footprint fits the admission budget and routes each to a
+slot of its dimension: a context (one stream) with its own step loop on its
+own host thread.  A slot builds the meshes of newly routed requests on the
+device, then runs one adapt pass over the disjoint union of all its
+requests (ohg_adapt_pass_batch), and repeats: requests routed while a step
+runs join that slot's next step, finished requests leave and free their
+memory at once.  Slots do not wait for one another, so a long 3D union does
+not hold back the 2D slots.  Because a union pass is bit for bit the
+separate passes, a request's result does not depend on what it was batched
+with.  The library's calls release the interpreter lock, so the slots' work
+overlaps on the device.
 
-Each request's mesh lives on a context (a slot: one stream and its memory
-pool on the device), chosen when the request is routed; ``route`` spreads a
-stream of requests over the slots of each dimension by the work already sent
-to each.  A step runs one union pass per slot that holds admitted requests,
-all slots at once from a pool of host threads (the library's calls release
-the interpreter lock), so the slots' passes overlap on the device.
+Admission counts device bytes.  Before a mesh exists its footprint is
+estimated from a per-element figure measured on the device (``calibrate``:
+the memory pool's high-water mark over one build and pass); once the slot
+has built it, the reservation becomes the mesh's own device bytes scaled by
+the measured ratio of a pass's peak to the resident mesh.  A request is
+admitted while the larger of the reservations and the pool's bytes in use,
+plus its estimate, stays within the budget.
 
 ``serve_one_at_a_time`` runs the same stream with one request on the device
-at a time and no batching, the baseline the batched loop is measured against.
+at a time and no batching, the baseline the batched loop is measured
+against.  Its latencies include the same mesh builds.
 """
-import concurrent.futures
+import threading
 import time
 from dataclasses import dataclass, field
 
-from .mesh import adapt_opts, adapt_pass_batch
+from .mesh import Mesh, adapt_opts, adapt_pass_batch
 
-# device bytes per element while a mesh is resident and during its pass:
-# arrays of the mesh and its derived adjacencies plus the pass's temporaries
-# (upper estimates; 3D tets carry about 3x the adjacency of 2D triangles)
+# device bytes per element (build and pass peak) used until calibrate()
+# has measured them; upper estimates
 BYTES_PER_ELEMENT = {2: 1200, 3: 2400}
+# peak bytes of a pass over resident bytes, used until calibrate() measures it
+PASS_PEAK_OVER_RESIDENT = {2: 2.5, 3: 2.5}
 
 
 @dataclass
 class Request:
     rid: int
     arrival: float  # seconds from the start of the stream
-    mesh: object  # omega_h_gb300.mesh.Mesh, resident on the device
     passes: int
     dim: int = 0
+    n: int = 0      # subdivisions per axis of the box to build
+    kind: int = 0   # metric family of the box (the library's workload kinds)
+    seed: int = 0
+    mesh: object = None  # omega_h_gb300.mesh.Mesh: given, or built on admission
+    slot: int = -1
     elements_in: int = 0
     admitted: float = -1.0
+    built: float = -1.0
     done: float = -1.0
-    reserved: int = 0  # footprint held from admission to completion
+    reserved: int = 0  # bytes held from admission to completion
     passes_done: int = 0
     element_passes: int = 0
     stats: list = field(default_factory=list)
 
-    def footprint(self):
-        return BYTES_PER_ELEMENT[self.dim] * max(self.elements_in, self.mesh.nelems())
+    def elements(self):
+        if self.mesh is not None:
+            return self.mesh.nelems()
+        return 2 * self.n * self.n if self.dim == 2 else 6 * self.n ** 3
 
-
-def _prepare(reqs):
-    for r in reqs:
-        r.dim = r.mesh.dim
-        r.elements_in = r.mesh.nelems()
-    return sorted(reqs, key=lambda r: (r.arrival, r.rid))
+    def build(self, ctx):
+        m = Mesh.build_box(ctx, self.dim, self.n)
+        m.apply_workload(self.n, self.seed, self.kind)
+        self.mesh = m
 
 
 def route(dims, work, slots):
@@ -70,81 +84,174 @@ def route(dims, work, slots):
     return out
 
 
-def serve(ctx, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter):
-    """Continuous batching.  Returns the requests with admitted/done times
-    (seconds from the stream start) and per-pass union stats.  The slots are
-    the contexts of the requests' meshes (``ctx`` is kept for callers that
-    pass one; the meshes decide)."""
-    reqs = _prepare(requests)
-    slots = []
+def calibrate(ctxs, sizes=None):
+    """Measures, per dimension, the device bytes per element of a mesh's build
+    and pass (the memory pool's high-water mark above its use before) and the
+    ratio of a pass's peak to the resident mesh.  ctxs maps a dimension to a
+    context.  Returns (bytes_per_element, pass_peak_over_resident)."""
+    sizes = sizes or {2: 256, 3: 24}
+    bpe, peak = {}, {}
+    for d, ctx in ctxs.items():
+        r = Request(rid=-1, arrival=0.0, passes=1, dim=d, n=sizes[d], kind=1, seed=1)
+        used0, _, _ = ctx.pool_bytes(reset_high=True)
+        r.build(ctx)
+        resident = r.mesh.device_bytes()
+        r.mesh.adapt_pass(adapt_opts(d))
+        _, _, high = ctx.pool_bytes()
+        n = r.elements()
+        bpe[d] = max(1.0, (high - used0) / n)
+        peak[d] = max(1.0, (high - used0) / max(resident, 1))
+        r.mesh.close()
+    return bpe, peak
+
+
+class _Slot:
+    def __init__(self, ctx, dim, index):
+        self.ctx, self.dim, self.index = ctx, dim, index
+        self.inbox = []
+        self.active = []
+        self.work = 0.0  # element-passes routed and not finished
+
+
+def serve(slots, requests, budget_bytes=150e9, opts=None, clock=time.perf_counter,
+          bytes_per_element=None, pass_peak=None, release=False, trace=None):
+    """Continuous batching.  slots maps a dimension to its contexts (one step
+    loop each).  Returns the requests with admitted/built/done times (seconds
+    from the stream start), per-pass union stats and their slot.  release:
+    free each finished request's mesh at once (else it stays with the
+    request for the caller to read and close; its reservation ends either
+    way).  trace, if a list, receives (seconds, bytes reserved, pool bytes in
+    use) at each admission.  A request whose estimate alone exceeds the
+    budget raises ValueError."""
+    bpe = bytes_per_element or BYTES_PER_ELEMENT
+    peak = pass_peak or PASS_PEAK_OVER_RESIDENT
+    reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
     for r in reqs:
-        if not any(r.mesh.ctx is c for c in slots):
-            slots.append(r.mesh.ctx)
-    pool = concurrent.futures.ThreadPoolExecutor(len(slots)) if len(slots) > 1 else None
-
-    def run_group(dim, group):
-        o = opts[dim] if opts else adapt_opts(dim)
-        n_before = [r.mesh.nelems() for r in group]
-        st = adapt_pass_batch(group[0].mesh.ctx, [r.mesh for r in group], o)
-        for r, nb in zip(group, n_before):
-            r.passes_done += 1
-            r.element_passes += nb
-            r.stats.append(st)
-
+        if r.mesh is not None:
+            r.dim = r.mesh.dim
+        r.elements_in = r.elements()
+    all_slots = {d: [_Slot(c, d, i) for i, c in enumerate(cs)] for d, cs in slots.items()}
+    any_ctx = next(iter(slots.values()))[0]
+    cv = threading.Condition()
+    state = {"reserved": 0, "admitting": True, "error": None}
     t0 = clock()
-    pending = list(reqs)
-    active = []
-    used = 0
-    while pending or active:
-        now = clock() - t0
-        # admit arrived requests in order while they fit
-        while pending and pending[0].arrival <= now and used + pending[0].footprint() <= budget_bytes:
-            r = pending.pop(0)
-            r.admitted = now
-            r.reserved = r.footprint()
-            used += r.reserved
-            active.append(r)
-        if pending and pending[0].arrival <= now and not active and \
-                pending[0].footprint() > budget_bytes:
-            raise ValueError(f"request {pending[0].rid} alone exceeds the admission budget")
-        if not active:
-            time.sleep(max(0.0, pending[0].arrival - now))
-            continue
-        groups = []
-        for c in slots:
-            for d in (2, 3):
-                g = [r for r in active if r.mesh.ctx is c and r.dim == d]
-                if g:
-                    groups.append((d, g))
-        if pool and len(groups) > 1:
-            for f in [pool.submit(run_group, d, g) for d, g in groups]:
-                f.result()
-        else:
-            for d, g in groups:
-                run_group(d, g)
-        now = clock() - t0
-        still = []
-        for r in active:
-            if r.passes_done >= r.passes:
-                r.done = now
-                used -= r.reserved
-            else:
-                still.append(r)
-        active = still
-    if pool:
-        pool.shutdown()
+
+    def estimate(r):
+        return int(bpe[r.dim] * r.elements_in)
+
+    def run_slot(s):
+        o = opts[s.dim] if opts else adapt_opts(s.dim)
+        try:
+            while True:
+                with cv:
+                    while not s.inbox and not s.active and state["admitting"] and \
+                            state["error"] is None:
+                        cv.wait()
+                    if state["error"] is not None:
+                        return
+                    if not s.inbox and not s.active:
+                        return
+                    new, s.inbox = s.inbox, []
+                for r in new:
+                    if r.mesh is None:
+                        r.build(s.ctx)
+                    r.built = clock() - t0
+                    actual = int(r.mesh.device_bytes() * peak[s.dim])
+                    with cv:
+                        state["reserved"] += actual - r.reserved
+                        r.reserved = actual
+                        cv.notify_all()
+                s.active.extend(new)
+                n_before = [r.mesh.nelems() for r in s.active]
+                st = adapt_pass_batch(s.ctx, [r.mesh for r in s.active], o)
+                still = []
+                finished = []
+                for r, nb in zip(s.active, n_before):
+                    r.passes_done += 1
+                    r.element_passes += nb
+                    r.stats.append(st)
+                    if r.passes_done >= r.passes:
+                        r.done = clock() - t0
+                        finished.append(r)
+                        if release:
+                            r.mesh.close()
+                            r.mesh = None
+                    else:
+                        still.append(r)
+                s.active = still
+                with cv:
+                    for r in finished:
+                        state["reserved"] -= r.reserved
+                        s.work -= r.elements_in * r.passes
+                    cv.notify_all()
+        except BaseException as e:  # noqa: BLE001 - reported to the caller
+            with cv:
+                state["error"] = e
+                cv.notify_all()
+
+    threads = [threading.Thread(target=run_slot, args=(s,), daemon=True)
+               for ss in all_slots.values() for s in ss]
+    for th in threads:
+        th.start()
+    try:
+        for r in reqs:
+            est = estimate(r)
+            if est > budget_bytes:
+                raise ValueError(f"request {r.rid} alone exceeds the admission budget")
+            now = clock() - t0
+            if r.arrival > now:
+                time.sleep(r.arrival - now)
+            with cv:
+                while state["error"] is None:
+                    used, _, _ = any_ctx.pool_bytes()
+                    if max(state["reserved"], used) + est <= budget_bytes or \
+                            state["reserved"] == 0:
+                        break
+                    cv.wait(timeout=0.005)
+                if state["error"] is not None:
+                    break
+                cands = all_slots[r.dim]
+                if r.mesh is not None:  # a resident mesh stays on its context
+                    cands = [x for x in cands if x.ctx is r.mesh.ctx]
+                    if not cands:
+                        raise ValueError(f"request {r.rid}: its mesh is on no serving slot")
+                s = min(cands, key=lambda x: x.work)
+                s.work += r.elements_in * r.passes
+                r.slot = s.index
+                r.admitted = clock() - t0
+                r.reserved = est
+                state["reserved"] += est
+                if trace is not None:
+                    trace.append((r.admitted, state["reserved"], used))
+                s.inbox.append(r)
+                cv.notify_all()
+    finally:
+        with cv:
+            state["admitting"] = False
+            cv.notify_all()
+        for th in threads:
+            th.join()
+    if state["error"] is not None:
+        raise state["error"]
     return reqs
 
 
-def serve_one_at_a_time(ctx, requests, opts=None, clock=time.perf_counter):
-    """The same stream, one request at a time, each pass run on its own."""
-    reqs = _prepare(requests)
+def serve_one_at_a_time(ctx, requests, opts=None, clock=time.perf_counter, release=False):
+    """The same stream, one request at a time on one context: built on
+    arrival (or given), each pass run on its own; freed when done if
+    release."""
+    reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
     t0 = clock()
     for r in reqs:
         now = clock() - t0
         if r.arrival > now:
             time.sleep(r.arrival - now)
         r.admitted = clock() - t0
+        if r.mesh is None:
+            r.build(ctx)
+        r.dim = r.mesh.dim
+        r.elements_in = r.mesh.nelems()
+        r.built = clock() - t0
         o = opts[r.dim] if opts else adapt_opts(r.dim)
         for _ in range(r.passes):
             nb = r.mesh.nelems()
@@ -152,6 +259,9 @@ def serve_one_at_a_time(ctx, requests, opts=None, clock=time.perf_counter):
             r.passes_done += 1
             r.element_passes += nb
         r.done = clock() - t0
+        if release:
+            r.mesh.close()
+            r.mesh = None
     return reqs
 
 

@@ -62,7 +62,10 @@ def _arrays(m):
 @pytest.mark.parametrize("slots", [1, 2, 4], ids=["one_ctx", "two_ctx", "four_ctx"])
 @pytest.mark.parametrize("budget", [150e9, 3e7], ids=["roomy", "tight"])
 def test_served_results_equal_results_alone(ctx, ctx2, more, budget, slots):
-    from omega_h_gb300.serve import Request, route, serve, summary
+    """Requests arrive as box specifications; each slot builds its meshes
+    when they are routed to it, runs its own step loop, and the result of
+    every request equals its result alone, bit for bit."""
+    from omega_h_gb300.serve import Request, serve, summary
     alone = []
     for dim, n, kind, seed, passes, _ in STREAM:
         m = _mesh(ctx, dim, n, kind, seed)
@@ -73,14 +76,11 @@ def test_served_results_equal_results_alone(ctx, ctx2, more, budget, slots):
     # slots per dimension: one context for both, one each, or two each
     per_dim = {1: {2: [ctx], 3: [ctx]}, 2: {2: [ctx2], 3: [ctx]},
                4: {2: [ctx2, more[0]], 3: [ctx, more[1]]}}[slots]
-    dims = [d for d, *_ in STREAM]
-    work = [(2 * n * n if d == 2 else 6 * n ** 3) * p for d, n, _, _, p, _ in STREAM]
-    where = route(dims, work, {d: len(c) for d, c in per_dim.items()})
-    reqs = [Request(rid=i, arrival=a, mesh=_mesh(per_dim[d][where[i]], d, n, k, s), passes=p)
+    reqs = [Request(rid=i, arrival=a, passes=p, dim=d, n=n, kind=k, seed=s)
             for i, (d, n, k, s, p, a) in enumerate(STREAM)]
-    ctxs = {d: c[0] for d, c in per_dim.items()}
-    out = serve(ctxs, reqs, budget_bytes=budget)
-    assert all(r.done >= r.admitted >= r.arrival - 1e-9 and r.passes_done == r.passes for r in out)
+    out = serve(per_dim, reqs, budget_bytes=budget)
+    assert all(r.done >= r.built >= r.admitted >= r.arrival - 1e-9 and r.passes_done == r.passes
+               for r in out)
     for r in out:
         got = _arrays(r.mesh)
         want = alone[r.rid]
@@ -90,3 +90,50 @@ def test_served_results_equal_results_alone(ctx, ctx2, more, budget, slots):
         r.mesh.close()
     s = summary(out)
     assert s["requests"] == len(STREAM) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_served_resident_meshes_stay_on_their_context(ctx, ctx2):
+    """Requests may also bring a mesh already on the device; it is served by
+    the slot of its own context and released when asked."""
+    from omega_h_gb300.serve import Request, serve
+    spec = STREAM[:4]
+    alone = []
+    for dim, n, kind, seed, passes, _ in spec:
+        m = _mesh(ctx, dim, n, kind, seed)
+        for _ in range(passes):
+            m.adapt_pass()
+        alone.append(_arrays(m))
+        m.close()
+    slots = {2: [ctx2], 3: [ctx]}
+    reqs = [Request(rid=i, arrival=a, passes=p, mesh=_mesh(slots[d][0], d, n, k, s))
+            for i, (d, n, k, s, p, a) in enumerate(spec)]
+    out = serve(slots, reqs)
+    for r in out:
+        got = _arrays(r.mesh)
+        for k, v in alone[r.rid].items():
+            assert np.array_equal(v.view(np.uint8), got[k].view(np.uint8))
+        r.mesh.close()
+    reqs = [Request(rid=i, arrival=a, passes=p, dim=d, n=n, kind=k, seed=s)
+            for i, (d, n, k, s, p, a) in enumerate(spec)]
+    out = serve(slots, reqs, release=True)
+    assert all(r.mesh is None and r.passes_done == r.passes for r in out)
+
+
+def test_admission_counts_device_bytes(ctx, ctx2):
+    """calibrate() measures bytes per element on the device; with a budget
+    of about two meshes' footprint the loop never holds more than that in
+    reservations, and every request still completes."""
+    from omega_h_gb300.serve import Request, calibrate, serve
+    bpe, peak = calibrate({2: ctx2, 3: ctx})
+    assert all(100 < bpe[d] < 20000 and 1.0 <= peak[d] < 20 for d in (2, 3))
+    reqs = [Request(rid=i, arrival=0.0, passes=1, dim=3, n=12, kind=1, seed=i) for i in range(6)]
+    budget = 2.2 * bpe[3] * 6 * 12 ** 3
+    trace = []
+    out = serve({3: [ctx]}, reqs, budget_bytes=budget, bytes_per_element=bpe, pass_peak=peak,
+                release=True, trace=trace)
+    assert all(r.passes_done == 1 for r in out) and len(trace) == len(reqs)
+    # every admission kept the reservations within the budget
+    assert all(reserved <= budget for _, reserved, _ in trace)
+    # and held requests back: never were all six in flight at once
+    spans = sorted((r.admitted, r.done) for r in out)
+    assert max(sum(1 for b, e in spans if b <= a < e) for a, _ in spans) < len(reqs)
