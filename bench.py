@@ -37,6 +37,10 @@ DOMINANT = "coarsen_filter"
 # untimed passes in which the launch-shape autotuner explores its variants
 AUTOTUNE_PASSES = 4
 DOMINANT_TRAFFIC = 118974208  # bytes per launch on the 64^3 shock pass (ncu dram read + write)
+# FP64 operations per launch of the FP64 output kernels on the 64^3 shock
+# box (ncu: dfma counted twice, dadd and dmul once, per thread instruction;
+# profiles/fp64_outputs_box64_shock.md), for their FP64-pipe fraction
+FP64_FLOPS_PER_LAUNCH = {"lengths": None, "qualities": None}
 # Batched workload: 1024 independent 3D boxes, subdivisions per axis
 # log-uniform integers in [4, 40] (seeded), isotropic sine metric with seeded
 # h0, amplitude and wave vector per mesh
@@ -650,13 +654,23 @@ def run_ours(args):
     achieved = dom_bytes_launch / (dom_avg_ms / 1e3) / 1e9 if dom_avg_ms > 0 else 0.0
     m = clone(base)
     kernels = {}
+    fp64 = ctypes.c_double()
+    _lib.call("ohg_fp64_peak", ctx.handle, 5, ctypes.byref(fp64))
     for stage in ("lengths", "qualities"):
         avg = ctypes.c_float()
         nb = ctypes.c_double()
         _lib.call("ohg_time_stage", m.handle, stage.encode(), 10, ctypes.byref(avg),
                   ctypes.byref(nb))
         kernels[stage] = {"ms": avg.value, "alg_bytes": nb.value,
-                          "gbs": nb.value / (avg.value / 1e3) / 1e9 if avg.value > 0 else None}
+                          "gbs": nb.value / (avg.value / 1e3) / 1e9 if avg.value > 0 else None,
+                          "hbm_frac": (nb.value / (avg.value / 1e3) / 1e9) / peak
+                          if avg.value > 0 else None}
+        fl = FP64_FLOPS_PER_LAUNCH[stage]
+        if fl and avg.value > 0:
+            g = fl / (avg.value / 1e3) / 1e9
+            kernels[stage].update({"fp64_gflops": g, "fp64_frac": g / fp64.value})
+    kernels["fp64_peak_gflops"] = fp64.value
+    kernels["fp64_peak_kind"] = "measured in this run: chains of dependent FP64 FMAs"
     m.close()
 
     cpu = None

@@ -291,6 +291,10 @@ int ohg_find_indset(ohg_mesh* mesh, int ent_dim, const double* quality_dev,
  * compulsory bytes of one launch (each input array read once, each output
  * written once).  A measurement hook with no counterpart in the reference. */
 int ohg_time_stage(ohg_mesh* mesh, const char* stage, int reps, float* avg_ms, double* alg_bytes);
+/* Measurement hook (no counterpart in the reference): the device's FP64
+ * fused multiply-add throughput in GFLOP/s, from chains of dependent FMAs
+ * timed with CUDA events on the context's stream (best of reps launches). */
+int ohg_fp64_peak(ohg_context* ctx, int reps, double* gflops);
 
 /* ---- graph-level kernels (no mesh) ---- */
 /* invert_adj (src/Omega_h_adj.cpp:231-263): outputs nlows+1, nhigh*k, nhigh*k */

@@ -75,6 +75,7 @@ SIGNATURES = {
     "ohg_context_allocations": [c_void_p, P(c_ull)],
     "ohg_context_pool_bytes": [c_void_p, c_int, P(c_ll), P(c_ll), P(c_ll)],
     "ohg_mesh_device_bytes": [c_void_p, P(c_ll)],
+    "ohg_fp64_peak": [c_void_p, c_int, P(c_double)],
     "ohg_context_autotune": [c_void_p, c_int],
     "ohg_context_force_variant": [c_void_p, c_int],
     "ohg_context_tuning": [c_void_p, P(c_int)],

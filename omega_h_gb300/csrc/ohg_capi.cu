@@ -902,6 +902,13 @@ int ohg_find_indset(ohg_mesh* m, int d, const double* q, const signed char* cand
   });
 }
 
+int ohg_fp64_peak(ohg_context* c, int reps, double* gflops) {
+  if (!gflops || reps < 1) {
+    g_err = "ohg_fp64_peak: reps >= 1 and an output are needed";
+    return OHG_ERR_INVALID;
+  }
+  return guarded(c, [&] { *gflops = fp64_peak_gflops(reps); });
+}
 int ohg_time_stage(ohg_mesh* m, const char* stage, int reps, float* avg_ms, double* alg_bytes) {
   MESH_GUARD(m);
   std::string st(stage ? stage : "");

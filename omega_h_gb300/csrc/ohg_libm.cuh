@@ -33,6 +33,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #ifndef OHG_HD
 #ifdef __CUDACC__
@@ -116,11 +117,32 @@ OHG_HD DD dd_div(DD a, DD b) {
 // |hi| is a power of two).  This is the rounding test of Ziv's strategy:
 // a quick evaluation is returned when the test passes, else an accurate one
 // decides.
+// the bits of a double and back
+OHG_HD std::uint64_t d2u(double x) {
+#ifdef __CUDA_ARCH__
+  return std::uint64_t(__double_as_longlong(x));
+#else
+  std::uint64_t u;
+  std::memcpy(&u, &x, sizeof(u));
+  return u;
+#endif
+}
+OHG_HD double u2d(std::uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  std::memcpy(&x, &u, sizeof(x));
+  return x;
+#endif
+}
+
 OHG_HD bool rounds_to_hi(double hi, double lo, double err) {
   if (!(fabs(hi) >= 0x1p-1020) || !(fabs(hi) <= 0x1p1020)) return false;
-  int e = ilogb(hi);
-  double half_up = ldexp(1.0, e - 53);
-  bool pow2 = fabs(hi) == ldexp(1.0, e);
+  std::uint64_t b = d2u(hi) & 0x7fffffffffffffffull;
+  std::uint64_t eb = b >> 52;  // biased exponent, 3 .. 2043 here
+  double half_up = u2d((eb - 53) << 52);  // 2^(exponent - 53): half an ulp of hi
+  bool pow2 = (b & 0xfffffffffffffull) == 0;
   bool toward_zero = (lo < 0.0) == (hi > 0.0);
   double margin = (toward_zero && pow2) ? 0.5 * half_up : half_up;
   return fabs(lo) + err < margin;
@@ -158,12 +180,18 @@ OHG_HD bool cube_below(std::uint64_t a, std::uint64_t M) {
 OHG_HD double cbrt_cr(double x) {
   if (x == 0.0 || !(x == x) || x - x != 0.0) return x + x;  // zero (sign kept), NaN, inf
   double ax = fabs(x);
-  int e;
-  double f = frexp(ax, &e);  // ax = f 2^e, f in [0.5, 1), subnormals included
-  int E = e - 1;             // ax = (2f) 2^E with 2f in [1, 2)
+  int kadj = 0;
+  if (ax < 0x1p-1022) {  // subnormal: scale by 2^162, exactly
+    ax *= 0x1p162;
+    kadj = -54;
+  }
+  std::uint64_t bits = d2u(ax);
+  int E = int(bits >> 52) - 1023;  // ax = g 2^E, g in [1, 2)
   int k = E >= 0 ? E / 3 : -((2 - E) / 3);
   int r = E - 3 * k;  // 0, 1 or 2
-  double m = ldexp(2.0 * f, r);  // in [1, 8); the cube root of ax is cbrt(m) 2^k
+  // m = g 2^r in [1, 8); the cube root of ax is cbrt(m) 2^k
+  double m = u2d((bits & 0xfffffffffffffull) | (std::uint64_t(1023 + r) << 52));
+  k += kadj;
   // w ~ m^(-1/3): a float start and one division-free Newton step
   // w (4 - m w^3) / 3 (about 2^-45 relative); y = m w^2 ~ m^(1/3)
   double w = double(1.0f / cbrtf(float(m)));
@@ -178,7 +206,8 @@ OHG_HD double cbrt_cr(double x) {
     double res = ((y3.hi - m) + y3.lo) + y2.lo * y;
     DD z = fast_two_sum(y, -(res * (w * w)) * (1.0 / 3.0));
     if (OHG_LIBM_QUICK && z.hi >= 1.0 && z.hi < 2.0 && rounds_to_hi(z.hi, z.lo, 0x1p-80)) {
-      double r1 = ldexp(z.hi, k);
+      // z.hi 2^k: the exponent field moves by k (the result is normal)
+      double r1 = u2d(d2u(z.hi) + (std::uint64_t(std::int64_t(k)) << 52));
       return x < 0.0 ? -r1 : r1;
     }
     y = z.hi;

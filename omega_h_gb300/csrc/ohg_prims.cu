@@ -679,6 +679,49 @@ LO count_marked(const Arr<I8>& marks) {
   return c.h_pinned[0];
 }
 
+// ------------------------------------------------------------ FP64 peak
+// Eight independent chains of dependent FP64 fused multiply-adds per thread:
+// the FP64 pipe's throughput, the ceiling of the FP64-bound kernels (their
+// arithmetic keeps the reference's evaluation order in FP64).
+__global__ void __launch_bounds__(256) k_dfma_chains(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = double(threadIdx.x) * 1e-9 + double(k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == -1.0) out[blockIdx.x] = s;  // never true; keeps the chains live
+}
+
+double fp64_peak_gflops(int reps) {
+  Ctx& c = ctx();
+  const int block = 256, iters = 4096;
+  int grid = c.num_sms * 8;
+  Arr<double> sink(grid);
+  cudaEvent_t e0, e1;
+  OHG_CUDA(cudaEventCreate(&e0));
+  OHG_CUDA(cudaEventCreate(&e1));
+  float best = -1.0f;
+  for (int r = 0; r < reps + 1; ++r) {
+    OHG_CUDA(cudaEventRecord(e0, c.stream));
+    k_dfma_chains<<<grid, block, 0, c.stream>>>(sink.data(), iters, 0.9999999, 1e-7);
+    OHG_CUDA(cudaEventRecord(e1, c.stream));
+    OHG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    OHG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (r > 0 && (best < 0.0f || ms < best)) best = ms;  // the first launch warms up
+  }
+  c.launches += unsigned(reps + 1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  double flops = 2.0 * 8.0 * double(iters) * double(grid) * double(block);
+  return flops / (double(best) * 1e-3) / 1e9;
+}
+
 // ------------------------------------------------------------ reductions
 template <class T, class Op>
 __global__ void k_reduce(const T* in, LO n, T init, Op op, T* out) {

@@ -29,6 +29,8 @@ Arr<LO> collect_marked(const Arr<I8>& marks);
 LO count_marked(const Arr<I8>& marks);
 
 LO last(const Arr<LO>& a);
+// FP64 fused multiply-add throughput of the device (GFLOP/s, best of reps)
+double fp64_peak_gflops(int reps);
 // the last element of each array (at most 16) with one host wait
 void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out);
 // indices of nonzero marks given offset_scan of the 0/1 marks and its total

@@ -5,12 +5,14 @@ seeded metric family, or a mesh already on the device) and a number of
 passes.  Requests arrive over time.  The loop admits them in arrival order
 while their device footprint fits the admission budget and routes each to a
 slot of its dimension: a context (one stream) with its own step loop on its
-own host thread.  A slot builds the meshes of newly routed requests on the
-device, then runs one adapt pass over the disjoint union of all its
-requests (ohg_adapt_pass_batch), and repeats: requests routed while a step
-runs join that slot's next step, finished requests leave and free their
-memory at once.  Slots do not wait for one another, so a long 3D union does
-not hold back the 2D slots.  Because a union pass is bit for bit the
+own host thread (slots that share a context share its thread, since a
+context is driven by one thread at a time).  A slot builds the meshes of
+newly routed requests on the device, then runs one adapt pass over the
+disjoint union of all its requests (ohg_adapt_pass_batch), and repeats:
+requests routed while a step runs join that slot's next step, finished
+requests leave and free their memory at once.  Slots on different contexts
+do not wait for one another, so a long 3D union does not hold back the 2D
+slots.  Because a union pass is bit for bit the
 separate passes, a request's result does not depend on what it was batched
 with.  The library's calls release the interpreter lock, so the slots' work
 overlaps on the device.
@@ -139,58 +141,74 @@ def serve(slots, requests, budget_bytes=150e9, opts=None, clock=time.perf_counte
     def estimate(r):
         return int(bpe[r.dim] * r.elements_in)
 
-    def run_slot(s):
+    def step(s, new):
+        """Builds a slot's new meshes, then one union pass over its requests."""
         o = opts[s.dim] if opts else adapt_opts(s.dim)
+        for r in new:
+            if r.mesh is None:
+                r.build(s.ctx)
+            r.built = clock() - t0
+            actual = int(r.mesh.device_bytes() * peak[s.dim])
+            with cv:
+                state["reserved"] += actual - r.reserved
+                r.reserved = actual
+                cv.notify_all()
+        s.active.extend(new)
+        if not s.active:
+            return
+        n_before = [r.mesh.nelems() for r in s.active]
+        st = adapt_pass_batch(s.ctx, [r.mesh for r in s.active], o)
+        still, finished = [], []
+        for r, nb in zip(s.active, n_before):
+            r.passes_done += 1
+            r.element_passes += nb
+            r.stats.append(st)
+            if r.passes_done >= r.passes:
+                r.done = clock() - t0
+                finished.append(r)
+                if release:
+                    r.mesh.close()
+                    r.mesh = None
+            else:
+                still.append(r)
+        s.active = still
+        with cv:
+            for r in finished:
+                state["reserved"] -= r.reserved
+                s.work -= r.elements_in * r.passes
+            cv.notify_all()
+
+    def run_worker(slist):
+        # one host thread per context: a context's stream, status word and
+        # memory are driven by one thread at a time; slots of different
+        # dimensions that share a context take their steps in turn
         try:
             while True:
                 with cv:
-                    while not s.inbox and not s.active and state["admitting"] and \
-                            state["error"] is None:
+                    while not any(x.inbox or x.active for x in slist) and \
+                            state["admitting"] and state["error"] is None:
                         cv.wait()
                     if state["error"] is not None:
                         return
-                    if not s.inbox and not s.active:
+                    if not any(x.inbox or x.active for x in slist):
                         return
-                    new, s.inbox = s.inbox, []
-                for r in new:
-                    if r.mesh is None:
-                        r.build(s.ctx)
-                    r.built = clock() - t0
-                    actual = int(r.mesh.device_bytes() * peak[s.dim])
-                    with cv:
-                        state["reserved"] += actual - r.reserved
-                        r.reserved = actual
-                        cv.notify_all()
-                s.active.extend(new)
-                n_before = [r.mesh.nelems() for r in s.active]
-                st = adapt_pass_batch(s.ctx, [r.mesh for r in s.active], o)
-                still = []
-                finished = []
-                for r, nb in zip(s.active, n_before):
-                    r.passes_done += 1
-                    r.element_passes += nb
-                    r.stats.append(st)
-                    if r.passes_done >= r.passes:
-                        r.done = clock() - t0
-                        finished.append(r)
-                        if release:
-                            r.mesh.close()
-                            r.mesh = None
-                    else:
-                        still.append(r)
-                s.active = still
-                with cv:
-                    for r in finished:
-                        state["reserved"] -= r.reserved
-                        s.work -= r.elements_in * r.passes
-                    cv.notify_all()
+                    news = []
+                    for x in slist:
+                        news.append(x.inbox)
+                        x.inbox = []
+                for x, new in zip(slist, news):
+                    step(x, new)
         except BaseException as e:  # noqa: BLE001 - reported to the caller
             with cv:
                 state["error"] = e
                 cv.notify_all()
 
-    threads = [threading.Thread(target=run_slot, args=(s,), daemon=True)
-               for ss in all_slots.values() for s in ss]
+    workers = {}
+    for ss in all_slots.values():
+        for x in ss:
+            workers.setdefault(id(x.ctx), []).append(x)
+    threads = [threading.Thread(target=run_worker, args=(sl,), daemon=True)
+               for sl in workers.values()]
     for th in threads:
         th.start()
     try:

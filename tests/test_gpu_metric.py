@@ -1,13 +1,14 @@
 """Metric tools on the GPU against the reference's own outputs
 (tests/golden/metric, written by the reference through oracle/ref_driver):
-intersection, clamping, Hessian metrics, implied metrics, gradation
-limiting, the expected element count and generate_metrics.  Every one of
-these goes through the closed-form eigensolve (cbrt, acos, cos) and most
-through log/exp, where CUDA's and glibc's results differ by an ulp; the
-tensors are held to the suite's interpolation tolerance relative to each
-tensor's largest entry, and the expected element count to the one for reals
-derived from interpolated metrics (the measured errors are printed: about
-1e-12 on these cases)."""
+intersection (Barral's degenerate cases included), clamping, Hessian
+metrics, implied metrics, gradation limiting, the expected element count and
+generate_metrics.  Every one of these goes through the closed-form
+eigensolve, whose cube root the library takes correctly rounded while
+glibc's is not (the reference's results depend on that last ulp near
+repeated eigenvalues); the tensors are held to the suite's interpolation
+tolerance relative to each tensor's largest entry, and the expected element
+count to the one for reals derived from interpolated metrics (the measured
+errors are printed: about 1e-12 on these cases)."""
 import json
 import os
 
@@ -56,10 +57,10 @@ def _close(want, got, what, nc):
 
 # Metric kinds with two equal principal sizes (the shock's two tangential
 # sizes, the boundary layer's x and z sizes): every intersection of such
-# metrics solves a cubic with an exact double root, which the closed-form
-# solver resolves only to O(sqrt(ulp)) before merging the roots, so CUDA's
-# and glibc's one-ulp differences give 1e-7-level differences per
-# intersection.  Gradation limiting repeats dozens of intersections per
+# metrics solves a cubic with an exact double root through Cardano's branch,
+# whose result depends on the cube root's last ulp (glibc's is not correctly
+# rounded on half of all arguments), so the two sides differ by about 1e-7
+# per intersection.  Gradation limiting repeats dozens of intersections per
 # vertex per sweep until nothing changes by 1e-3, and on these metrics the
 # reference's own iteration does not settle quickly (188 sweeps for
 # box4_shock): the fixed point it stops at depends on the rounding.  These
