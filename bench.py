@@ -36,11 +36,18 @@ METRIC = "elements/s per adapt pass"
 DOMINANT = "coarsen_filter"
 # untimed passes in which the launch-shape autotuner explores its variants
 AUTOTUNE_PASSES = 4
-DOMINANT_TRAFFIC = 118974208  # bytes per launch on the 64^3 shock pass (ncu dram read + write)
-# FP64 operations per launch of the FP64 output kernels on the 64^3 shock
-# box (ncu: dfma counted twice, dadd and dmul once, per thread instruction;
-# profiles/fp64_outputs_box64_shock.md), for their FP64-pipe fraction
-FP64_FLOPS_PER_LAUNCH = {"lengths": None, "qualities": None}
+# bytes per launch on the 64^3 shock pass: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch of k_coarsen_screen_v<3> (vertices
+# taken 8 at a time, 608 blocks of 256 threads), profiles/coarsen_filter_box64_shock.md;
+# to be captured again whenever that kernel changes
+DOMINANT_TRAFFIC = 124004864 + 18097920
+# FP64 add, multiply and fused multiply-add thread instructions per launch of
+# the FP64 output kernels on the 64^3 shock box, all edges / all tets (ncu:
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), for their
+# FP64-pipe fraction against the measured FMA-chain rate (one such
+# instruction per pipe slot)
+FP64_OPS_PER_LAUNCH = {"lengths": 63905036 + 70059756 + 30746988,
+                       "qualities": 117161842 + 138959394 + 40870410}
 # Batched workload: 1024 independent 3D boxes, subdivisions per axis
 # log-uniform integers in [4, 40] (seeded), isotropic sine metric with seeded
 # h0, amplitude and wave vector per mesh
@@ -98,6 +105,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-workload leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-workload leg")
+    ap.add_argument("--serve-slots", type=int, default=0,
+                    help="serving contexts per dimension (default: SERVE['slots_per_dim'])")
     ap.add_argument("--serve-requests", type=int, default=0,
                     help="requests served at the saturating rate (default: the bounded "
                          "sample; 20000 serves the whole stream)")
@@ -449,7 +458,7 @@ def run_serve(ctx, args, slots_per_dim=None):
     import numpy as np
     from omega_h_gb300.mesh import Context
     from omega_h_gb300.serve import Request, calibrate, serve, serve_one_at_a_time, summary
-    k = slots_per_dim or SERVE["slots_per_dim"]
+    k = slots_per_dim or args.serve_slots or SERVE["slots_per_dim"]
     extra = [Context(ctx.device) for _ in range(2 * k - 1)]
     slots = {3: [ctx] + extra[:k - 1], 2: extra[k - 1:]}
     bpe, peak = calibrate({d: c[0] for d, c in slots.items()})
@@ -665,12 +674,14 @@ def run_ours(args):
                           "gbs": nb.value / (avg.value / 1e3) / 1e9 if avg.value > 0 else None,
                           "hbm_frac": (nb.value / (avg.value / 1e3) / 1e9) / peak
                           if avg.value > 0 else None}
-        fl = FP64_FLOPS_PER_LAUNCH[stage]
-        if fl and avg.value > 0:
-            g = fl / (avg.value / 1e3) / 1e9
-            kernels[stage].update({"fp64_gflops": g, "fp64_frac": g / fp64.value})
+        ops = FP64_OPS_PER_LAUNCH[stage]
+        if avg.value > 0:
+            rate = ops / (avg.value / 1e3) / 1e9  # G instructions / s
+            kernels[stage].update({"fp64_ops_per_launch": ops, "fp64_gops": rate,
+                                   "fp64_pipe_frac": rate / (fp64.value / 2.0)})
     kernels["fp64_peak_gflops"] = fp64.value
-    kernels["fp64_peak_kind"] = "measured in this run: chains of dependent FP64 FMAs"
+    kernels["fp64_peak_kind"] = ("measured in this run: chains of dependent FP64 FMAs; "
+                                 "fp64_pipe_frac divides by half of it (FMA instructions/s)")
     m.close()
 
     cpu = None

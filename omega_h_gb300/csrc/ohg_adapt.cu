@@ -1181,119 +1181,258 @@ __device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, L
   return minq;
 }
 
-// Persistent screening of collapse directions.  Each warp takes chunks of
-// directions (kQueueChunk by default) from a global counter, and each lane takes the next
-// direction of its warp's chunk as soon as its current one is settled, so
-// the lanes stay busy whatever the cavity sizes and early exits (the
-// while-while loop of persistent ray traversal).  A direction whose
-// enclosure of min(1, cavity qualities) straddles the threshold goes to a
-// list for the FP64 stage, with the smallest upper bound of its cavity.
-constexpr int kQueueChunk = 64;
+// ------------------------------------------------------------ vertex-centric screen
+// The same screen, one warp per collapsing vertex v_col.  Every direction
+// that collapses v_col screens the same star of elements with v_col moved
+// onto another neighbour, so the warp stages the star once in shared memory:
+// the neighbours' screening records (local index k+1 for the k-th edge of v's
+// row, 0 for v), each star element as local indices, and one slot per
+// direction.  Lanes then spread over the (direction, element) pairs and
+// reduce each direction's bounds by shared atomic minima of order keys.  A
+// direction's outcome is the sequential one's: it fails when the smallest
+// upper bound is below the threshold, passes when the smallest lower bound
+// reaches it, and is sent to the FP64 list otherwise.  Stars that do not fit
+// the staging arrays are screened direction by direction from global memory.
+constexpr int kVsWarps = kBlock / 32;
+constexpr int kVsMaxLocal = 32, kVsMaxElems = 64;
 
-// The refill step of a persistent warp: lanes with st == 0 take the next
-// items of the warp's chunk, calling start(item), which returns the lane's
-// new state (1: working on the item, 0: the item was settled at once);
-// lanes find st == 2 once the queue is exhausted.  Every lane of the warp
-// calls this.
-struct WarpQueue {
-  long long next = 0, end = 0;
-  template <class Start>
-  __device__ __forceinline__ void refill(int& st, LO nitems, int chunk, unsigned long long* counter,
-                                         Start start) {
-    const unsigned full = 0xffffffffu;
-    const int lane = int(threadIdx.x & 31u);
-    const unsigned below = (1u << lane) - 1u;
-    unsigned needm = __ballot_sync(full, st == 0);
-    while (needm) {
-      if (next >= end) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
-        base = __shfl_sync(full, base, 0);
-        if (base >= (unsigned long long)nitems) {
-          if (st == 0) st = 2;
-          return;
-        }
-        next = (long long)base;
-        end = next + chunk < nitems ? next + chunk : nitems;
-      }
-      int avail = int(end - next);
-      int rank = __popc(needm & below);
-      if (st == 0 && rank < avail) st = start(LO(next + rank));
-      int took = __popc(needm);
-      next += took < avail ? took : avail;
-      needm = __ballot_sync(full, st == 0);
-    }
-  }
-};
-
-struct CoarsenScreenArgs {
-  LO ndirs;
+struct CoarsenVertexArgs {
+  LO nverts;
   int chunk;
   ScreenView sv;
-  LV ev, cv, va, vb;
-  View<const I8> vc;
-  View<const LO> c2e;
+  LV ev, cv, va, vb, ea, eb;
+  View<const I8> vc, ec;
+  View<const LO> e2cand;
   View<const I8> codes;
   View<double> q2;
   float mqa_f;
-  unsigned long long* queue;  // [0] next direction, [1] directions in the list
+  unsigned long long* queue;  // [0] next vertex, [1] directions in the FP64 list
   LO* amb_dir;
   float* amb_mhi;
   unsigned long long* cnt;
 };
 
+// order-preserving int key of a float, and back
+__device__ __forceinline__ int fkey(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fkey_inv(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ void screen_outcome(const CoarsenVertexArgs& a, LO d, float lo, float hi) {
+  if (hi < a.mqa_f) {
+    a.q2[d] = -1.0;  // fails
+  } else if (lo >= a.mqa_f) {
+    a.q2[d] = CUDART_NAN;  // passes on its enclosure
+  } else {
+    LO k = LO(atomicAdd(&a.queue[1], 1ULL));
+    a.amb_dir[k] = d;
+    a.amb_mhi[k] = hi;
+    a.q2[d] = -1.0;  // replaced by the FP64 minimum
+  }
+}
+
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_coarsen_screen(CoarsenScreenArgs a) {
-  constexpr int dim = D;
-  WarpQueue q;
-  int st = 0;  // 0: needs a direction, 1: screening one, 2: done
-  LO d = 0, x = 0, x1 = 0, v_onto = 0;
-  float lo = 1.0f, hi = 1.0f;
+__global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a) {
+  constexpr int NV = D + 1;
+  __shared__ float4 s_h[kVsWarps][kVsMaxLocal], s_l[kVsWarps][kVsMaxLocal];
+  __shared__ float4 s_ma[kVsWarps][kVsMaxLocal], s_mb[kVsWarps][kVsMaxLocal];
+  __shared__ long long s_key[kVsWarps][kVsMaxLocal];
+  __shared__ LO s_gid[kVsWarps][kVsMaxLocal];
+  __shared__ LO s_dir[kVsWarps][kVsMaxLocal];  // direction of local vertex k as v_onto, or -1
+  __shared__ int s_lo[kVsWarps][kVsMaxLocal], s_hi[kVsWarps][kVsMaxLocal];
+  __shared__ unsigned char s_dk[kVsWarps][kVsMaxLocal];  // local indices of the directions
+  __shared__ unsigned s_elem[kVsWarps][kVsMaxElems];     // NV local indices, 8 bits each
+  // per local vertex k: the star elements that do not contain k, i.e. the
+  // cavity of the direction onto k, as a bit set; then those not yet screened
+  __shared__ unsigned long long s_rem[kVsWarps][kVsMaxLocal];
+  const unsigned full = 0xffffffffu;
+  const int w = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31u);
   unsigned nscreen = 0;
+  LO next = 0, end = 0;
   for (;;) {
-    q.refill(st, a.ndirs, a.chunk, &a.queue[0], [&](LO item) {
-      d = item;
-      LO cand = d >> 1;
-      int col = d & 1;
-      if (!collapses(a.codes[cand], col)) {
-        a.q2[d] = -1.0;
-        return 0;
-      }
-      LO e = a.c2e[cand];
-      LO v_col = a.ev[e * 2 + col];
-      v_onto = a.ev[e * 2 + (1 - col)];
-      x = a.va[v_col];
-      x1 = a.va[v_col + 1];
-      lo = hi = 1.0f;
-      if (x < x1) return 1;
-      a.q2[d] = CUDART_NAN;  // empty cavity: min(1) passes
-      return 0;
-    });
-    if (__all_sync(0xffffffffu, st == 2)) break;
-    if (st == 1) {
-      LO vv[4];
-      if (collapse_elem(a.cv, dim, a.vb[x], code_which_down(a.vc[x]), v_onto, vv)) {
-        FIv b = elem_quality_bounds(dim, a.sv, vv);
-        lo = fminf(lo, b.lo);
-        hi = fminf(hi, b.hi);
-        ++nscreen;
-      }
-      ++x;
-      if (hi < a.mqa_f) {
-        a.q2[d] = -1.0;  // fails: the minimum only falls as elements are added
-        st = 0;
-      } else if (x >= x1) {
-        if (lo >= a.mqa_f) {
-          a.q2[d] = CUDART_NAN;  // passes on its enclosure
-        } else {
-          LO k = LO(atomicAdd(&a.queue[1], 1ULL));
-          a.amb_dir[k] = d;
-          a.amb_mhi[k] = hi;
-          a.q2[d] = -1.0;  // replaced by the FP64 minimum
-        }
-        st = 0;
-      }
+    if (next >= end) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&a.queue[0], (unsigned long long)a.chunk);
+      base = __shfl_sync(full, base, 0);
+      if (base >= (unsigned long long)a.nverts) break;
+      next = LO(base);
+      end = next + a.chunk < a.nverts ? next + a.chunk : a.nverts;
     }
+    const LO v = next++;
+    const LO e0 = a.ea[v], ne = a.ea[v + 1] - e0;
+    // the directions with v as v_col; non-collapsing directions of candidate
+    // edges fail outright
+    bool fits = ne + 1 <= kVsMaxLocal;
+    unsigned any = 0;
+    for (LO kb = 0; kb < ne; kb += 32) {
+      LO k = kb + lane;
+      LO dir = -1;
+      if (k < ne) {
+        LO e = a.eb[e0 + k];
+        LO cand = a.e2cand[e];
+        if (cand >= 0) {
+          int col = code_which_down(a.ec[e0 + k]);
+          LO d = cand * 2 + col;
+          if (collapses(a.codes[cand], col)) dir = d;
+          else a.q2[d] = -1.0;
+        }
+        if (fits) s_dir[w][k + 1] = dir;
+      }
+      any |= __ballot_sync(full, dir >= 0);
+    }
+    if (!any) continue;
+    const LO s0 = a.va[v], S = a.va[v + 1] - s0;
+    fits = fits && S <= kVsMaxElems;
+    if (fits) {
+      // stage the local vertices and the star's elements
+      for (LO k = lane; k <= ne; k += 32) {
+        LO u = v;
+        if (k > 0) {
+          LO e = a.eb[e0 + k - 1];
+          u = a.ev[e * 2 + (1 - code_which_down(a.ec[e0 + k - 1]))];
+        }
+        s_gid[w][k] = u;
+        s_h[w][k] = a.sv.xh[u];
+        s_l[w][k] = a.sv.xl[u];
+        s_ma[w][k] = a.sv.ma[u];
+        s_mb[w][k] = a.sv.mb[u];
+        s_key[w][k] = a.sv.dkey[u];
+        s_lo[w][k] = fkey(1.0f);
+        s_hi[w][k] = fkey(1.0f);
+        s_rem[w][k] = S == 64 ? ~0ull : (1ull << S) - 1ull;
+      }
+      __syncwarp();
+      bool found = true;
+      for (LO x = lane; x < S; x += 32) {
+        LO el = a.vb[s0 + x];
+        int pos = code_which_down(a.vc[s0 + x]);
+        unsigned packed = 0;
+        for (int j = 0; j < NV; ++j) {
+          unsigned li = 0;
+          if (j != pos) {
+            LO u = a.cv[el * NV + j];
+            li = 255;
+            for (LO k = 1; k <= ne; ++k)
+              if (s_gid[w][k] == u) li = unsigned(k);
+            if (li == 255) found = false;
+            else atomicAnd(&s_rem[w][li], ~(1ull << x));
+          }
+          packed |= li << (8 * j);
+        }
+        s_elem[w][x] = packed;
+      }
+      fits = __all_sync(full, found);
+      __syncwarp();
+    }
+    if (!fits) {
+      // direction by direction, each lane one direction, from global memory
+      for (LO kb = 0; kb < ne; kb += 32) {
+        LO k = kb + lane;
+        LO d = -1, v_onto = 0;
+        if (k < ne) {
+          LO e = a.eb[e0 + k];
+          LO cand = a.e2cand[e];
+          int col = code_which_down(a.ec[e0 + k]);
+          if (cand >= 0 && collapses(a.codes[cand], col)) {
+            d = cand * 2 + col;
+            v_onto = a.ev[e * 2 + (1 - col)];
+          }
+        }
+        if (d >= 0) {
+          float lo = 1.0f, hi = 1.0f;
+          for (LO x = s0; x < s0 + S && !(hi < a.mqa_f); ++x) {
+            LO vv[4];
+            if (collapse_elem(a.cv, D, a.vb[x], code_which_down(a.vc[x]), v_onto, vv)) {
+              FIv b = elem_quality_bounds(D, a.sv, vv);
+              lo = fminf(lo, b.lo);
+              hi = fminf(hi, b.hi);
+              ++nscreen;
+            }
+          }
+          screen_outcome(a, d, lo, hi);
+        }
+      }
+      __syncwarp();
+      continue;
+    }
+    // the directions' local indices, in order
+    int nd = 0;
+    for (LO kb = 1; kb <= ne; kb += 32) {
+      LO k = kb + lane;
+      bool is = k <= ne && s_dir[w][k] >= 0;
+      unsigned m = __ballot_sync(full, is);
+      if (is) s_dk[w][nd + __popc(m & ((1u << lane) - 1u))] = (unsigned char)k;
+      nd += __popc(m);
+    }
+    __syncwarp();
+    // rounds of (direction, element) pairs over the lanes: each live
+    // direction takes its next 32 / (live directions) cavity elements; a
+    // direction leaves when its cavity is screened or an upper bound fell
+    // below the threshold (its minimum only falls), as the sequential screen
+    // stops at its first failing element
+    int nlive = nd;
+    for (;;) {
+      int kl = lane < nlive ? s_dk[w][lane] : 0;
+      bool alive = lane < nlive && s_rem[w][kl] != 0ull && !(fkey_inv(s_hi[w][kl]) < a.mqa_f);
+      unsigned am = __ballot_sync(full, alive);
+      __syncwarp();
+      if (alive) s_dk[w][__popc(am & ((1u << lane) - 1u))] = (unsigned char)kl;
+      nlive = __popc(am);
+      __syncwarp();
+      if (nlive == 0) break;
+      const int per = 32 / nlive;
+      if (lane < nlive * per) {
+        int i = lane / per, j = lane - i * per;
+        int k = s_dk[w][i];
+        unsigned long long rem = s_rem[w][k];
+        unsigned rlo = unsigned(rem), rhi = unsigned(rem >> 32);
+        int clo = __popc(rlo), x = -1;
+        if (j < clo) x = int(__fns(rlo, 0, j + 1));
+        else if (j - clo < __popc(rhi)) x = 32 + int(__fns(rhi, 0, j - clo + 1));
+        if (x >= 0) {
+          unsigned packed = s_elem[w][x];
+          int li[NV];
+          for (int jj = 0; jj < NV; ++jj) {
+            li[jj] = int((packed >> (8 * jj)) & 255u);
+            if (li[jj] == 0) li[jj] = k;  // v_col moved onto v_onto
+          }
+          int best = 0;
+          long long bk = s_key[w][li[0]];
+          for (int jj = 1; jj < NV; ++jj) {
+            long long kk = s_key[w][li[jj]];
+            if (kk > bk) {
+              best = jj;
+              bk = kk;
+            }
+          }
+          float4 h[NV], l[NV];
+          for (int jj = 0; jj < NV; ++jj) {
+            h[jj] = s_h[w][li[jj]];
+            l[jj] = s_l[w][li[jj]];
+          }
+          FIv b;
+          if constexpr (D == 3) b = tet_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
+          else b = tri_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
+          atomicMin(&s_lo[w][k], fkey(b.lo));
+          atomicMin(&s_hi[w][k], fkey(b.hi));
+          ++nscreen;
+        }
+      }
+      __syncwarp();
+      if (lane < nlive) {  // drop the elements screened in this round
+        int k = s_dk[w][lane];
+        unsigned long long rem = s_rem[w][k];
+        for (int t = 0; t < per && rem; ++t) rem &= rem - 1ull;
+        s_rem[w][k] = rem;
+      }
+      __syncwarp();
+    }
+    for (LO k = 1 + lane; k <= ne; k += 32) {
+      if (s_dir[w][k] >= 0)
+        screen_outcome(a, s_dir[w][k], fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]));
+    }
+    __syncwarp();
   }
   warp_count_full(a.cnt, nscreen);
 }
@@ -1466,18 +1605,30 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   Arr<unsigned long long> queue = fill<unsigned long long>(2, 0ULL);
   Arr<LO> amb_dir(ndirs);
   Arr<float> amb_mhi(ndirs);
-  // tuned launch shape: queue chunk 64 or 32 directions (the results do not
+  // candidate index of each edge (-1: not a candidate), for the vertex rows
+  const Adj& v2e = m.ask_up(0, 1);
+  LO nE = m.nedges();
+  Arr<LO> e2cand(nE);
+  OHG_CUDA(cudaMemsetAsync(e2cand.data(), 0xff, size_t(nE) * sizeof(LO), ctx().stream));
+  {
+    auto e2c = view(e2cand);
+    pfor(n, [=] __device__(LO cand) { e2c[c2e[cand]] = cand; });
+  }
+  // tuned launch shape: vertices taken 8 or 4 at a time (the results do not
   // depend on it); blocks of 256 threads
   Ctx& cx = ctx();
-  int var = cx.tuner.select("coarsen_screen", D, ndirs, 2, 0, cx.stream);
+  int var = cx.tuner.select("coarsen_screen_v", D, nV, 2, 0, cx.stream);
   bool timed = cx.tuner.open >= 0;
-  int block = kBlock, chunk = (var & 1) ? 32 : kQueueChunk;
-  CoarsenScreenArgs args{ndirs, chunk, sv, ev, cv, va, vb, vc, c2e, cview(codes_p, n), q2, mqa_f,
+  int block = kBlock, chunk = (var & 1) ? 4 : 8;
+  CoarsenVertexArgs args{nV,   chunk, sv,   ev,   cv,
+                         va,   vb,    cview(v2e.a2ab), cview(v2e.ab2b), vc,
+                         cview(v2e.codes), cview(e2cand), cview(codes_p, n), q2, mqa_f,
                          queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
+  bytes += double(nE) * 4 + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
   {
     KernelTimer timer("coarsen_filter", bytes);
-    unsigned nb = persistent_blocks(k_coarsen_screen<D>, block, (ndirs + chunk - 1) / chunk);
-    k_coarsen_screen<D><<<nb, block, 0, cx.stream>>>(args);
+    unsigned nb = persistent_blocks(k_coarsen_screen_v<D>, block, (nV + chunk - 1) / chunk);
+    k_coarsen_screen_v<D><<<nb, block, 0, cx.stream>>>(args);
     if (timed) cx.tuner.stop(cx.stream);
     ++cx.launches;
 #ifdef OHG_CHECKED

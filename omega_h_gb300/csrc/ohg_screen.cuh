@@ -238,15 +238,10 @@ __device__ __forceinline__ int maxdet_vertex(const ScreenView& s, const LO vv[4]
   return best;
 }
 
-// Interval of the double tet quality (tet_quality on the maxdet metric).
-__device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {
-  int mi = maxdet_vertex(s, vv);
-  float4 ma = s.ma[vv[mi]], mb = s.mb[vv[mi]];
-  float4 h[4], l[4];
-  for (int i = 0; i < 4; ++i) {
-    h[i] = s.xh[vv[i]];
-    l[i] = s.xl[vv[i]];
-  }
+// Interval of the double tet quality (tet_quality on the maxdet metric), from
+// the four vertices' coordinate pairs and the maxdet vertex's metric record.
+__device__ __forceinline__ FIv tet_quality_bounds_of(const float4 h[4], const float4 l[4],
+                                                     float4 ma, float4 mb) {
   // the six edges in the reference's order; the third, -b1, has the same
   // v^T M v as b1
   float ev[6][3], ee[6];
@@ -391,6 +386,16 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
   return q;
 }
 
+__device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {
+  int mi = maxdet_vertex(s, vv);
+  float4 h[4], l[4];
+  for (int i = 0; i < 4; ++i) {
+    h[i] = s.xh[vv[i]];
+    l[i] = s.xl[vv[i]];
+  }
+  return tet_quality_bounds_of(h, l, s.ma[vv[mi]], s.mb[vv[mi]]);
+}
+
 // The double tet quality with sqrt(det M) and the maxdet choice taken from
 // the per-vertex screening data: the same operations, in the same order, as
 // tet_quality(p, metric of the maxdet vertex), since sqrt(det3(M)) of a
@@ -520,15 +525,9 @@ constexpr float kThirdUp = 0.33333337f;
 // Interval of the double triangle quality (tri_quality on the maxdet metric):
 // x / msl with x = area * sqrt(det M) / s_eq, msl the mean v^T M v of the
 // three edges; a negative size is returned as the size.
-__device__ __forceinline__ FIv tri_quality_bounds(const ScreenView& s, const LO vv[3]) {
-  int mi = maxdet_vertex3(s, vv);
-  float4 ma = s.ma[vv[mi]];
-  float sd = s.mb[vv[mi]].w;
-  float4 h[3], l[3];
-  for (int i = 0; i < 3; ++i) {
-    h[i] = s.xh[vv[i]];
-    l[i] = s.xl[vv[i]];
-  }
+__device__ __forceinline__ FIv tri_quality_bounds_of(const float4 h[3], const float4 l[3],
+                                                     float4 ma, float4 mb) {
+  float sd = mb.w;
   float ev[3][2], ee[3];
   ee[0] = sdiff2(h[1], l[1], h[0], l[0], ev[0]);  // b0
   ee[1] = sdiff2(h[2], l[2], h[1], l[1], ev[1]);
@@ -574,6 +573,16 @@ __device__ __forceinline__ FIv tri_quality_bounds(const ScreenView& s, const LO 
            __fmul_ru(__fdividef(x_hi, msl_lo), 1.0f + 0x1p-21f)};
   if (!finite_iv(q)) return widen_all();
   return q;
+}
+
+__device__ __forceinline__ FIv tri_quality_bounds(const ScreenView& s, const LO vv[3]) {
+  int mi = maxdet_vertex3(s, vv);
+  float4 h[3], l[3];
+  for (int i = 0; i < 3; ++i) {
+    h[i] = s.xh[vv[i]];
+    l[i] = s.xl[vv[i]];
+  }
+  return tri_quality_bounds_of(h, l, s.ma[vv[mi]], s.mb[vv[mi]]);
 }
 
 // The double triangle quality with sqrt(det M) and the maxdet choice taken

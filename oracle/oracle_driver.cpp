@@ -291,11 +291,18 @@ int main(int argc, char** argv) {
     auto t1 = std::chrono::steady_clock::now();
     if (stages) dump_refine_stage(m, o);
     PassResult r;
+    auto since = [](std::chrono::steady_clock::time_point t) {
+      return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
+    };
     r.did_refine = refine_by_size(m, o);
+    double t_ref = since(t1);
     if (stages) dump_mesh(m, "r_out_");
     if (stages) dump_coarsen_stage(m, o);
+    auto t2 = std::chrono::steady_clock::now();
     r.did_coarsen = coarsen_by_size(m, o);
+    double t_coa = since(t2);
     if (stages) dump_mesh(m, "c_out_");
+    auto t3 = std::chrono::steady_clock::now();
     const V<double>& q = m.ask_qualities();
     double minq = q[0];
     for (double x : q) minq = std::min(minq, x);
@@ -303,7 +310,9 @@ int main(int argc, char** argv) {
       if (stages) dump_swap_stage(m, o);
       r.did_swap = swap_edges(m, o);
     }
+    double t_swp = since(t3);
     double t_pass = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+    if (mode == "time") std::printf("refine %.4f coarsen %.4f swap %.4f ", t_ref, t_coa, t_swp);
     dump("pass_flags", V<LO>{r.did_refine, r.did_coarsen, r.did_swap});
     dump_mesh(m, "out_");
     if (g_manifest) std::fclose(g_manifest);
