@@ -66,7 +66,7 @@ BATCH = {"workload": "batch1024_sine", "meshes": 1024, "n_min": 4, "n_max": 40, 
 # --serve-requests 20000 serves the whole stream at the saturating rate.
 SERVE = {"workload": "serve_mix", "stream_requests": 20000,
          "rates_per_s": [50.0, 200.0, 800.0], "requests_per_rate": [250, 1000, 2000],
-         "budget_gb": 150.0, "seed": 11, "slots_per_dim": 2}
+         "budget_gb": 150.0, "seed": 11, "slots_per_dim": 4}
 
 
 def serve_specs(sv=SERVE, count=None):

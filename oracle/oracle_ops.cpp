@@ -887,10 +887,12 @@ bool coarsen_slivers(Mesh& m, const AdaptOpts& o) {
 V<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
   const V<double>& q = m.ask_qualities();
   V<I8> marks(q.size());
+  ORC_PARALLEL_FOR
   for (size_t i = 0; i < q.size(); ++i) marks[i] = q[i] < ceil;
   const Adj& dual = m.ask_adj(m.dim, m.dim);
   for (int l = 0; l < nlayers; ++l) {
     V<I8> nmk(marks.size());
+    ORC_PARALLEL_FOR
     for (size_t e = 0; e < marks.size(); ++e) {
       I8 r = -128;  // fan_reduce MAX starts from the lowest I8
       for (LO j = dual.a2ab[e]; j < dual.a2ab[e + 1]; ++j) r = std::max(r, marks[dual.ab2b[j]]);
@@ -1176,8 +1178,13 @@ bool swap_edges(Mesh& m, const AdaptOpts& o) {
   V<LO> k2p[4], pv2v[4];
   for (int d = 1; d <= 3; ++d) k2p[d].assign((size_t)(nkeys) + 1, 0);
   V<Loop> loops((size_t)(nkeys));
+  // the adjacencies find_loop reads, derived before the parallel loop
+  m.ask_up(1, 3);
+  m.ask_verts_of(1);
+  m.ask_verts_of(3);
+  ORC_PARALLEL_FOR
+  for (LO k = 0; k < nkeys; ++k) loops[k] = find_loop(m, k2e[k]);
   for (LO k = 0; k < nkeys; ++k) {
-    loops[k] = find_loop(m, k2e[k]);
     int n = loops[k].size;
     int npt = swap3d::mesh_size(n), npe = swap3d::nedges(n);
     k2p[1][k + 1] = k2p[1][k] + npe;
@@ -1185,6 +1192,7 @@ bool swap_edges(Mesh& m, const AdaptOpts& o) {
     k2p[3][k + 1] = k2p[3][k] + 2 * npt;
   }
   for (int d = 1; d <= 3; ++d) pv2v[d].resize((size_t)(k2p[d][nkeys]) * (d + 1));
+  ORC_PARALLEL_FOR
   for (LO k = 0; k < nkeys; ++k) {
     const Loop& loop = loops[k];
     int n = loop.size;
