@@ -229,9 +229,14 @@ OHG_HD double log_cr(double x) {
   if (!(x > 0.0)) return x == 0.0 ? -INFINITY : NAN;  // zero, negative, NaN
   if (x - x != 0.0) return x;                            // +inf
   if (x == 1.0) return 0.0;
-  int e;
-  double f = 2.0 * frexp(x, &e);  // x = f 2^(e-1), f in [1, 2), subnormals included
-  int E = e - 1;
+  int E = 0;
+  if (x < 0x1p-1022) {  // subnormal: scale by 2^54, exactly
+    x *= 0x1p54;
+    E = -54;
+  }
+  std::uint64_t bits = d2u(x);
+  E += int(bits >> 52) - 1023;  // x = f 2^E, f in [1, 2)
+  double f = u2d((bits & 0xfffffffffffffull) | (std::uint64_t(1023) << 52));
   if (f >= 1.4142135623730951) {
     f = 0.5 * f;
     E += 1;
@@ -309,7 +314,9 @@ OHG_HD double exp_cr(double x) {
     double lo = ((b.lo + d.lo) + (a.lo + c.lo)) +
                 (T.lo + (T.hi * ((rl + 0.5 * sq.lo) + (rh * rl + p3)) + T.lo * rh));
     DD y = fast_two_sum(d.hi, lo);
-    if (OHG_LIBM_QUICK && rounds_to_hi(y.hi, y.lo, 0x1p-66 * fabs(y.hi))) return ldexp(y.hi, q);
+    // y.hi 2^q: the exponent field moves by q (the result stays normal)
+    if (OHG_LIBM_QUICK && rounds_to_hi(y.hi, y.lo, 0x1p-66 * fabs(y.hi)))
+      return u2d(d2u(y.hi) + (std::uint64_t(std::int64_t(q)) << 52));
   }
   // accurate evaluation, within about 2^-90:
   // exp(r) - 1 = r + r^2/2 + r^3/6 + r^4 (1/24 + r/120 + ...), |r| < 2^-8.5
