@@ -562,6 +562,8 @@ def run_ours(args):
         one_pass(False)
         t, st = one_pass(True)
         print(json.dumps({"profile_pass_ms": t, "pass": st}), flush=True)
+        base.close()
+        ctx.close()  # with OHG_TRACE_SYNCS set, prints the host waits by call site
         return
     for _ in range(args.warmup):
         one_pass(False)

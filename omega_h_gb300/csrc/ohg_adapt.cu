@@ -163,6 +163,40 @@ void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, doub
   });
 }
 
+// The per-face route of the collapse screen: each tet's quality interval
+// from its face opposite slot k (invariants made once) and the vertex at
+// slot k, with the exact FP64 value beside it
+void screen_tets_face(Mesh& m, const LO* tv2v_p, LO n, int k, float* lo_p, float* hi_p,
+                      double* ex_p) {
+  if (m.dim != 3 || k < 0 || k > 3) throw Error(1, "screen_tets_face: a 3D mesh and a slot 0..3");
+  const VertScreen& vs = mesh_screen(m);
+  auto sv = screen_view(vs);
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto tv = cview(tv2v_p, n * 4);
+  auto lo = view(lo_p, n);
+  auto hi = view(hi_p, n);
+  auto ex = view(ex_p, n);
+  pfor(n, [=] __device__(LO i) {
+    LO vv[4];
+    for (int j = 0; j < 4; ++j) vv[j] = tv[i * 4 + j];
+    float4 hf[3], lf[3];
+    int nf = 0;
+    for (int j = 0; j < 4; ++j) {
+      if (j == k) continue;
+      hf[nf] = sv.xh[vv[j]];
+      lf[nf] = sv.xl[vv[j]];
+      ++nf;
+    }
+    int mi = maxdet_vertex(sv, vv);
+    TetFaceInv f = tet_face_invariants(hf, lf, k);
+    FIv b = tet_face_bounds(f, hf, lf, sv.xh[vv[k]], sv.xl[vv[k]], sv.ma[vv[mi]], sv.mb[vv[mi]]);
+    lo[i] = b.lo;
+    hi[i] = b.hi;
+    ex[i] = tet_quality_exact(sv, c, mt, vv);
+  });
+}
+
 void screen_edges(Mesh& m, const LO* ev2v_p, LO n, float* lo_p, float* hi_p, double* ex_p) {
   int dim = m.dim, mc = m.mcomp();
   const VertScreen& vs = mesh_screen(m);
@@ -214,98 +248,215 @@ static float float_at_or_below(double x) {
 
 // ------------------------------------------------------------ indset
 enum { NOT_IN = 0, IN = 1, UNKNOWN = 2 };
-constexpr int kMaxIndsetRounds = 4096;
+// a sweeping thread that has not settled its vertices after this long gives
+// up and raises ST_STALL (with all blocks resident, the highest-ranked
+// undecided vertex settles at its owner's next sweep, so this is a guard)
+constexpr unsigned long long kIndsetLimitNs = 2000000000ull;
+constexpr int kIndsetBlock = 256;
+// in-place rounds over all vertices, one thread each, before the sweep
+constexpr int kIndsetRounds = 2;
+// undecided vertices a sweeping thread keeps in its own list
+constexpr int kIndsetPending = 16;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // find_indset (src/Omega_h_indset.cpp:5-34; its rounds, local_iteration,
 // src/Omega_h_indset_inline.hpp:14-43, and their driver, lines 53-76):
 // a candidate joins when no neighbour has joined and every neighbour not yet
 // excluded ranks below it by (quality, index); it is excluded once a
 // neighbour has joined.  The set these rules settle on is unique: the greedy
-// set by decreasing rank.  The rounds here update one state array in place:
-// a state only ever moves from UNKNOWN to IN or NOT_IN, so a read that
-// misses a neighbour's decision of the same round sees UNKNOWN and can only
-// postpone a decision, never change one (a lower-ranked neighbour cannot
-// join while a higher-ranked one is UNKNOWN).  Decisions then spread within
-// a round along the launch order, and the set is the same as with rounds
-// that read only the previous round's states; the round count depends on
-// the schedule.
-Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands,
-                    int* rounds_out) {
+// set by decreasing rank.  A state only ever moves from UNKNOWN to IN or
+// NOT_IN, and a lower-ranked neighbour cannot join while a higher-ranked one
+// is UNKNOWN, so a read that misses a neighbour's decision can only postpone
+// a decision, never change one: the rules may be applied in any order, with
+// any staleness, and settle on the same set.  Each neighbour's state is read
+// once per decision; the reads of a row are independent (no early exit), so
+// their latencies overlap.  first: the state array has not been initialised
+// (all UNKNOWN), so a neighbour that is no candidate counts as NOT_IN.
+template <bool first>
+__device__ __forceinline__ int indset_decide(LO v, const LO* __restrict__ xa,
+                                             const LO* __restrict__ xb,
+                                             const double* __restrict__ q,
+                                             const I8* __restrict__ cands, volatile I8* s) {
+  LO beg = xa[v], end = xa[v + 1];
+  double qv = q[v];
+  bool joined = false, top = true;
+  // eight neighbours at a time: their numbers, then their states, then the
+  // qualities of the undecided ones, each group of loads issued together
+  for (LO j = beg; j < end; j += 8) {
+    LO u[8];
+    int su[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) u[t] = j + t < end ? xb[j + t] : -1;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      su[t] = NOT_IN;
+      if (u[t] >= 0 && (!first || cands[u[t]])) su[t] = s[u[t]];
+    }
+    double qu[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) qu[t] = su[t] == UNKNOWN ? q[u[t]] : 0.0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      if (su[t] == IN) joined = true;
+      else if (su[t] == UNKNOWN) top = top && ((qu[t] != qv) ? (qu[t] < qv) : (u[t] < v));
+    }
+  }
+  return joined ? NOT_IN : (top ? IN : UNKNOWN);
+}
+
+// The rounds before the sweep: one thread per vertex, plain launches, in
+// decreasing vertex order.  Among equal qualities the higher index ranks
+// first, so decisions spread from high to low indices; with threads in
+// decreasing order, a round's later blocks see what its earlier blocks
+// decided, and a chain of ties advances by more than one step per round.
+template <bool first>
+static void indset_round(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands,
+                         I8* st) {
+  auto xa = g.a2ab.data();
+  auto xb = g.ab2b.data();
+  auto q = quality.data();
+  auto cd = cands.data();
+  pfor(n, [=] __device__(LO i) {
+    LO v = n - 1 - i;
+    volatile I8* s = st;
+    if (first) {
+      if (!cd[v]) {
+        s[v] = NOT_IN;
+        return;
+      }
+    } else if (s[v] != UNKNOWN) {
+      return;
+    }
+    int d = indset_decide<first>(v, xa, xb, q, cd, s);
+    if (d != UNKNOWN) s[v] = I8(d);
+  });
+}
+
+// The sweep that settles the rest: one cooperative launch (all blocks
+// resident).  Each thread owns the vertices first, first + stride, ...; it
+// keeps up to kIndsetPending of its undecided ones in a list and decides
+// what the states it reads allow, sweep after sweep, refilling the list from
+// its vertices when it empties, until all of them are decided.  What is
+// left after the rounds is chains of decisions that wait on one another;
+// one step of a chain costs a sweep of the thread that owns it, so threads
+// own few vertices and a sweep is a few rounds of memory latency.  Since the
+// highest-ranked undecided vertex can always be decided, every sweep of its
+// owner makes progress somewhere.  Threads without progress back off
+// briefly with __nanosleep.  sweeps_acc receives the largest sweep count of
+// any thread.
+__global__ void __launch_bounds__(kIndsetBlock, 4)
+    k_indset_sweep(const LO* __restrict__ xa, const LO* __restrict__ xb,
+                   const double* __restrict__ q, const I8* __restrict__ cands, I8* st, LO n,
+                   int* status, int* sweeps_acc, unsigned* blocks_done, int* call_max) {
+  volatile I8* s = st;
+  LO stride = LO(gridDim.x) * kIndsetBlock;
+  LO scan = LO(blockIdx.x) * kIndsetBlock + LO(threadIdx.x);  // next owned vertex to look at
+  unsigned long long t0 = globaltimer_ns();
+  int sweeps = 0;
+  unsigned nap = 32;
+  LO pend[kIndsetPending];
+  int np = 0;
+  bool stalled = false;
+  for (;;) {
+    // refill the list from the owned vertices, eight state reads at a time
+    while (np < kIndsetPending && scan < n) {
+      I8 sv[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        long long v = (long long)scan + (long long)t * stride;
+        sv[t] = v < n ? s[v] : I8(NOT_IN);
+      }
+      int t = 0;
+      for (; t < 8 && np < kIndsetPending; ++t)
+        if (sv[t] == UNKNOWN) pend[np++] = scan + LO(t) * stride;
+      long long next = (long long)scan + (long long)t * stride;
+      scan = next < n ? LO(next) : n;
+    }
+    if (np == 0) break;
+    bool progress = false;
+    int keep = 0;
+    for (int i = 0; i < np; ++i) {
+      LO v = pend[i];
+      int d = indset_decide<false>(v, xa, xb, q, cands, s);
+      if (d == UNKNOWN) {
+        pend[keep++] = v;
+      } else {
+        s[v] = I8(d);
+        progress = true;
+      }
+    }
+    np = keep;
+    ++sweeps;
+    if (progress) {
+      nap = 32;
+    } else {
+      __nanosleep(nap);
+      if (nap < 256) nap *= 2;
+    }
+    if ((sweeps & 15) == 0 && globaltimer_ns() - t0 > kIndsetLimitNs) {
+      stalled = true;
+      break;
+    }
+  }
+  if (stalled) raise_status(status, ST_STALL);
+  // the call's largest sweep count, added to the accumulator by the last
+  // block to finish
+  int m = __reduce_max_sync(0xffffffffu, sweeps);
+  if ((threadIdx.x & 31u) == 0u) atomicMax(call_max, m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned prev = atomicAdd(blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      atomicAdd(sweeps_acc, atomicAdd(call_max, 0) + kIndsetRounds);
+    }
+  }
+}
+
+Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands) {
   Ctx& c = ctx();
   Arr<I8> a(n);
-  auto cd = cview(cands);
-  // flags[0..kIndsetBatch): a vertex is still UNKNOWN after that round of
-  // the batch; flags[kIndsetBatch]: there was a candidate at all
-  constexpr int kIndsetBatch = 8;
-  Arr<int> flags(kIndsetBatch + 1);
-  OHG_CUDA(cudaMemsetAsync(flags.data(), 0, (kIndsetBatch + 1) * sizeof(int), c.stream));
-  {
-    auto s0 = view(a);
-    int* anyc = flags.data() + kIndsetBatch;
-    pfor(n, [=] __device__(LO i) {
-      s0[i] = cd[i] ? UNKNOWN : NOT_IN;
-      if (cd[i]) *anyc = 1;
-    });
+  if (n == 0) return a;
+  OHG_CUDA(cudaMemsetAsync(a.data(), UNKNOWN, size_t(n), c.stream));
+  indset_round<true>(g, n, quality, cands, a.data());
+  for (int r = 1; r < kIndsetRounds; ++r) indset_round<false>(g, n, quality, cands, a.data());
+  // blocks_done and the call's sweep maximum
+  Arr<unsigned> scratch(2);
+  OHG_CUDA(cudaMemsetAsync(scratch.data(), 0, 2 * sizeof(unsigned), c.stream));
+  static thread_local int per_sm = 0;  // per host thread: no locking
+  if (per_sm == 0) {
+    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_indset_sweep,
+                                                           kIndsetBlock, 0));
+    if (per_sm < 1) per_sm = 1;
   }
-  // Rounds are launched in batches of kIndsetBatch with one flag per round
-  // and one host read per batch: a round after the one that left no vertex
-  // UNKNOWN changes nothing, so the state is the converged one and the
-  // count is taken from the first round whose flag stayed clear.
-  auto xa = cview(g.a2ab);
-  auto xb = cview(g.ab2b);
-  auto q = cview(quality);
-  I8* stp = a.data();
-  int rounds = 0;
-  bool any = true, first = true;
-  while (any) {
-    if (rounds >= kMaxIndsetRounds) throw Error(5, "independent set did not converge");
-    if (!first) OHG_CUDA(cudaMemsetAsync(flags.data(), 0, kIndsetBatch * sizeof(int), c.stream));
-    for (int r = 0; r < kIndsetBatch; ++r) {
-      int* fl = flags.data() + r;
-      pfor(n, [=] __device__(LO v) {
-        volatile I8* s = stp;
-        if (s[v] != UNKNOWN) return;
-        LO beg = xa[v], end = xa[v + 1];
-        for (LO j = beg; j < end; ++j)
-          if (s[xb[j]] == IN) {
-            s[v] = NOT_IN;
-            return;
-          }
-        double qv = q[v];
-        for (LO j = beg; j < end; ++j) {
-          LO u = xb[j];
-          if (s[u] == NOT_IN) continue;
-          double qu = q[u];
-          bool less = (qu != qv) ? (qu < qv) : (u < v);
-          if (!less) {
-            *fl = 1;
-            return;
-          }
-        }
-        s[v] = IN;
-      });
-    }
-    OHG_CUDA(cudaMemcpyAsync(c.h_pinned, flags.data(), (kIndsetBatch + 1) * sizeof(int),
-                             cudaMemcpyDeviceToHost, c.stream));
-    c.sync();
-    if (first && !c.h_pinned[kIndsetBatch]) break;  // no candidate: zero rounds
-    first = false;
-    int done = -1;
-    for (int r = 0; r < kIndsetBatch && done < 0; ++r)
-      if (!c.h_pinned[r]) done = r;
-    if (done >= 0) {
-      rounds += done + 1;
-      any = false;
-    } else {
-      rounds += kIndsetBatch;
-    }
-  }
-  if (rounds_out) *rounds_out += rounds;
+  long long full = (long long)per_sm * c.num_sms;
+  long long need = (n + kIndsetBlock - 1) / kIndsetBlock;
+  unsigned blocks = unsigned(need < full ? need : full);
+  const LO* xa = g.a2ab.data();
+  const LO* xb = g.ab2b.data();
+  const double* q = quality.data();
+  const I8* cd = cands.data();
+  I8* st = a.data();
+  int* status = c.d_status;
+  int* acc = c.d_indset_sweeps;
+  unsigned* done = scratch.data();
+  int* cmax = reinterpret_cast<int*>(scratch.data() + 1);
+  void* args[] = {(void*)&xa, (void*)&xb, (void*)&q,      (void*)&cd,   (void*)&st,
+                  (void*)&n,  (void*)&status, (void*)&acc, (void*)&done, (void*)&cmax};
+  OHG_CUDA(cudaLaunchCooperativeKernel((const void*)k_indset_sweep, dim3(blocks),
+                                       dim3(kIndsetBlock), args, 0, c.stream));
+  ++c.launches;
   return a;
 }
-Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& q, const Arr<I8>& cands, int* rounds) {
+Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& q, const Arr<I8>& cands) {
   if (d == m.dim) return cands;
-  return find_indset(m.ask_adj(d, d), m.nents[d], q, cands, rounds);
+  return find_indset(m.ask_adj(d, d), m.nents[d], q, cands);
 }
 
 // ------------------------------------------------------------ marks
@@ -862,7 +1013,7 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* s
     });
   }
   if (!get_elem(anyg, 0)) return false;
-  Arr<I8> keys = find_indset(m, EDGE, eq, initial, &st->indset_rounds);
+  Arr<I8> keys = find_indset(m, EDGE, eq, initial);
   Arr<LO> k2e = collect_marked(keys);
   LO nkeys = k2e.size();
   st->refine_keys = nkeys;
@@ -1193,8 +1344,14 @@ __device__ double collapse_min_exact(const ScreenView& sv, RV c, RV mt, LV cv, L
 // upper bound is below the threshold, passes when the smallest lower bound
 // reaches it, and is sent to the FP64 list otherwise.  Stars that do not fit
 // the staging arrays are screened direction by direction from global memory.
-constexpr int kVsWarps = kBlock / 32;
+// blocks of the vertex-centric screen: 128 threads, so that the 3D kernel's
+// per-element invariants fit the static shared memory of a block
+constexpr int kVsBlock = 128;
+constexpr int kVsWarps = kVsBlock / 32;
 constexpr int kVsMaxLocal = 32, kVsMaxElems = 64;
+// 3D stars staged with their per-element invariants: at most 48 elements
+// (larger stars take the per-direction path), so that six blocks fit an SM
+constexpr int kVsMaxElems3 = 48;
 
 struct CoarsenVertexArgs {
   LO nverts;
@@ -1233,8 +1390,15 @@ __device__ __forceinline__ void screen_outcome(const CoarsenVertexArgs& a, LO d,
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a) {
+__global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexArgs a) {
   constexpr int NV = D + 1;
+  // 3D: per star element, the invariants of its face opposite the
+  // collapsing vertex (tet_face_invariants), the slot of that vertex and the
+  // face's first maxdet slot
+  constexpr int kMaxE = D == 3 ? kVsMaxElems3 : kVsMaxElems;
+  constexpr int kInv = D == 3 ? kVsMaxElems3 : 1;
+  __shared__ TetFaceInv s_inv[kVsWarps][kInv];
+  __shared__ unsigned char s_slot[kVsWarps][kInv];  // slot | first maxdet face slot << 4
   __shared__ float4 s_h[kVsWarps][kVsMaxLocal], s_l[kVsWarps][kVsMaxLocal];
   __shared__ float4 s_ma[kVsWarps][kVsMaxLocal], s_mb[kVsWarps][kVsMaxLocal];
   __shared__ long long s_key[kVsWarps][kVsMaxLocal];
@@ -1242,7 +1406,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a
   __shared__ LO s_dir[kVsWarps][kVsMaxLocal];  // direction of local vertex k as v_onto, or -1
   __shared__ int s_lo[kVsWarps][kVsMaxLocal], s_hi[kVsWarps][kVsMaxLocal];
   __shared__ unsigned char s_dk[kVsWarps][kVsMaxLocal];  // local indices of the directions
-  __shared__ unsigned s_elem[kVsWarps][kVsMaxElems];     // NV local indices, 8 bits each
+  __shared__ unsigned s_elem[kVsWarps][kMaxE];     // NV local indices, 8 bits each
   // per local vertex k: the star elements that do not contain k, i.e. the
   // cavity of the direction onto k, as a bit set; then those not yet screened
   __shared__ unsigned long long s_rem[kVsWarps][kVsMaxLocal];
@@ -1283,7 +1447,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a
     }
     if (!any) continue;
     const LO s0 = a.va[v], S = a.va[v + 1] - s0;
-    fits = fits && S <= kVsMaxElems;
+    fits = fits && S <= kMaxE;
     if (fits) {
       // stage the local vertices and the star's elements
       for (LO k = lane; k <= ne; k += 32) {
@@ -1308,6 +1472,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a
         LO el = a.vb[s0 + x];
         int pos = code_which_down(a.vc[s0 + x]);
         unsigned packed = 0;
+        bool here = true;
         for (int j = 0; j < NV; ++j) {
           unsigned li = 0;
           if (j != pos) {
@@ -1315,12 +1480,33 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a
             li = 255;
             for (LO k = 1; k <= ne; ++k)
               if (s_gid[w][k] == u) li = unsigned(k);
-            if (li == 255) found = false;
+            if (li == 255) here = false;
             else atomicAnd(&s_rem[w][li], ~(1ull << x));
           }
           packed |= li << (8 * j);
         }
         s_elem[w][x] = packed;
+        found = found && here;
+        if constexpr (D == 3) {
+          if (here) {
+            // the face's slots in order, without the collapsing vertex's
+            int j0 = pos == 0 ? 1 : 0, j1 = pos <= 1 ? 2 : 1, j2 = pos <= 2 ? 3 : 2;
+            int f0 = int((packed >> (8 * j0)) & 255u), f1 = int((packed >> (8 * j1)) & 255u),
+                f2 = int((packed >> (8 * j2)) & 255u);
+            float4 hf[3] = {s_h[w][f0], s_h[w][f1], s_h[w][f2]};
+            float4 lf[3] = {s_l[w][f0], s_l[w][f1], s_l[w][f2]};
+            long long k0 = s_key[w][f0], k1 = s_key[w][f1], k2 = s_key[w][f2];
+            int fb = j0;
+            long long kb = k0;
+            if (k1 > kb) {
+              fb = j1;
+              kb = k1;
+            }
+            if (k2 > kb) fb = j2;
+            s_inv[w][x] = tet_face_invariants(hf, lf, pos);
+            s_slot[w][x] = (unsigned char)(pos | (fb << 4));
+          }
+        }
       }
       fits = __all_sync(full, found);
       __syncwarp();
@@ -1392,28 +1578,46 @@ __global__ void __launch_bounds__(kBlock) k_coarsen_screen_v(CoarsenVertexArgs a
         else if (j - clo < __popc(rhi)) x = 32 + int(__fns(rhi, 0, j - clo + 1));
         if (x >= 0) {
           unsigned packed = s_elem[w][x];
-          int li[NV];
-          for (int jj = 0; jj < NV; ++jj) {
-            li[jj] = int((packed >> (8 * jj)) & 255u);
-            if (li[jj] == 0) li[jj] = k;  // v_col moved onto v_onto
-          }
-          int best = 0;
-          long long bk = s_key[w][li[0]];
-          for (int jj = 1; jj < NV; ++jj) {
-            long long kk = s_key[w][li[jj]];
-            if (kk > bk) {
-              best = jj;
-              bk = kk;
-            }
-          }
-          float4 h[NV], l[NV];
-          for (int jj = 0; jj < NV; ++jj) {
-            h[jj] = s_h[w][li[jj]];
-            l[jj] = s_l[w][li[jj]];
-          }
           FIv b;
-          if constexpr (D == 3) b = tet_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
-          else b = tri_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
+          if constexpr (D == 3) {
+            // the face's vertices in slot order, the vertex moved onto at
+            // the collapsing vertex's slot; maxdet as in slot order: the
+            // face's first maximum against k, k first on a tie if its slot
+            // comes first
+            unsigned sl = s_slot[w][x];
+            int pos = int(sl & 15u), fb = int(sl >> 4);
+            int j0 = pos == 0 ? 1 : 0, j1 = pos <= 1 ? 2 : 1, j2 = pos <= 2 ? 3 : 2;
+            int f0 = int((packed >> (8 * j0)) & 255u), f1 = int((packed >> (8 * j1)) & 255u),
+                f2 = int((packed >> (8 * j2)) & 255u);
+            float4 hf[3] = {s_h[w][f0], s_h[w][f1], s_h[w][f2]};
+            float4 lf[3] = {s_l[w][f0], s_l[w][f1], s_l[w][f2]};
+            int lfb = int((packed >> (8 * fb)) & 255u);
+            long long kf = s_key[w][lfb], kp = s_key[w][k];
+            int best = (kp > kf || (kp == kf && pos < fb)) ? k : lfb;
+            b = tet_face_bounds(s_inv[w][x], hf, lf, s_h[w][k], s_l[w][k], s_ma[w][best],
+                                s_mb[w][best]);
+          } else {
+            int li[NV];
+            for (int jj = 0; jj < NV; ++jj) {
+              li[jj] = int((packed >> (8 * jj)) & 255u);
+              if (li[jj] == 0) li[jj] = k;  // v_col moved onto v_onto
+            }
+            int best = 0;
+            long long bk = s_key[w][li[0]];
+            for (int jj = 1; jj < NV; ++jj) {
+              long long kk = s_key[w][li[jj]];
+              if (kk > bk) {
+                best = jj;
+                bk = kk;
+              }
+            }
+            float4 h[NV], l[NV];
+            for (int jj = 0; jj < NV; ++jj) {
+              h[jj] = s_h[w][li[jj]];
+              l[jj] = s_l[w][li[jj]];
+            }
+            b = tri_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
+          }
           atomicMin(&s_lo[w][k], fkey(b.lo));
           atomicMin(&s_hi[w][k], fkey(b.hi));
           ++nscreen;
@@ -1619,7 +1823,7 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   Ctx& cx = ctx();
   int var = cx.tuner.select("coarsen_screen_v", D, nV, 2, 0, cx.stream);
   bool timed = cx.tuner.open >= 0;
-  int block = kBlock, chunk = (var & 1) ? 4 : 8;
+  int block = kVsBlock, chunk = (var & 1) ? 4 : 8;
   CoarsenVertexArgs args{nV,   chunk, sv,   ev,   cv,
                          va,   vb,    cview(v2e.a2ab), cview(v2e.ab2b), vc,
                          cview(v2e.codes), cview(e2cand), cview(codes_p, n), q2, mqa_f,
@@ -2059,7 +2263,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   else
     choose_rails(m, c2e.data(), c2e.size(), codes.data(), q2.data(), vc.data(), vq.data(),
                  vr.data());
-  Arr<I8> vkeys = find_indset(m, VERT, vq, vc, &st->indset_rounds);
+  Arr<I8> vkeys = find_indset(m, VERT, vq, vc);
   Arr<LO> k2v = collect_marked(vkeys);
   LO nkeys = k2v.size();
   st->coarsen_keys = nkeys;
@@ -2851,7 +3055,7 @@ static Arr<LO> swap_keys(Mesh& m, Arr<LO> c2e, Arr<double> cq, PassStats* st) {
   cq = unmap(kept, cq, 1);
   Arr<I8> is_cand = mark_image(c2e, ne);
   Arr<double> edge_q = map_onto(cq, c2e, ne, -1.0, 1);
-  Arr<I8> keys = find_indset(m, EDGE, edge_q, is_cand, &st->indset_rounds);
+  Arr<I8> keys = find_indset(m, EDGE, edge_q, is_cand);
   Arr<LO> k2e = collect_marked(keys);
   st->swap_keys = k2e.size();
   return k2e;
@@ -3135,6 +3339,7 @@ PassStats adapt_pass(Mesh& m, const AdaptOpts& o) {
   OHG_CUDA(cudaEventCreate(&e3));
   // each operator of the pass runs on a ghosted mesh (partitioning state
   // only: one part has no ghosts to exchange)
+  OHG_CUDA(cudaMemsetAsync(c.d_indset_sweeps, 0, sizeof(int), c.stream));
   OHG_CUDA(cudaEventRecord(e0, c.stream));
   m.parting = 1;
   st.did_refine = refine_by_size(m, o, &st);
@@ -3146,7 +3351,10 @@ PassStats adapt_pass(Mesh& m, const AdaptOpts& o) {
   st.min_quality = min_f64(m.ask_qualities());
   if (st.min_quality < o.min_quality_desired) st.did_swap = swap_edges(m, o, &st);
   OHG_CUDA(cudaEventRecord(e3, c.stream));
+  OHG_CUDA(cudaMemcpyAsync(c.h_indset_sweeps, c.d_indset_sweeps, sizeof(int),
+                           cudaMemcpyDeviceToHost, c.stream));
   c.sync();
+  st.indset_rounds = *c.h_indset_sweeps;
   OHG_CUDA(cudaEventElapsedTime(&st.ms_refine, e0, e1));
   OHG_CUDA(cudaEventElapsedTime(&st.ms_coarsen, e1, e2));
   OHG_CUDA(cudaEventElapsedTime(&st.ms_swap, e2, e3));

@@ -22,11 +22,10 @@ struct PassStats {
 
 // independent set over a conflict graph (src/Omega_h_indset.cpp,
 // src/Omega_h_indset_inline.hpp); quality ties broken by entity number,
-// which is the global number on one device
-Arr<I8> find_indset(const Adj& graph, LO n, const Arr<double>& quality, const Arr<I8>& cands,
-                    int* rounds);
-Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& quality, const Arr<I8>& cands,
-                    int* rounds = nullptr);
+// which is the global number on one device.  No host wait: the call's
+// sweep count is added to the context's device counter d_indset_sweeps.
+Arr<I8> find_indset(const Adj& graph, LO n, const Arr<double>& quality, const Arr<I8>& cands);
+Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& quality, const Arr<I8>& cands);
 
 // stage kernels (each fills caller memory of the stated size)
 void refine_qualities(Mesh& m, const LO* cands2edges, LO n, const double* midmetrics,
@@ -39,6 +38,8 @@ void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* ou
 // FP32 enclosures of the FP64 quality of arbitrary vertex 4-tuples and of
 // the FP64 metric length of vertex pairs, with the FP64 values (3D)
 void screen_tets(Mesh& m, const LO* tv2v, LO n, float* lo, float* hi, double* exact);
+void screen_tets_face(Mesh& m, const LO* tv2v, LO n, int slot, float* lo, float* hi,
+                      double* exact);
 void screen_edges(Mesh& m, const LO* ev2v, LO n, float* lo, float* hi, double* exact);
 void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,
                   I8* vert_cands, double* vert_quals, GO* vert_rails);

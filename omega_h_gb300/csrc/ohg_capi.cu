@@ -819,6 +819,12 @@ int ohg_screen_tet_qualities(ohg_mesh* m, const int* tv2v, int n, float* lo, flo
   MESH_GUARD(m);
   return guarded(m->owner, [&] { screen_tets(m->mesh, tv2v, n, lo, hi, exact); });
 }
+int ohg_screen_tet_qualities_face(ohg_mesh* m, const int* tv2v, int n, int slot, float* lo,
+                                  float* hi, double* exact) {
+  MESH_GUARD(m);
+  if (n < 0 || slot < 0 || slot > 3) return OHG_ERR_INVALID;
+  return guarded(m->owner, [&] { screen_tets_face(m->mesh, tv2v, n, slot, lo, hi, exact); });
+}
 int ohg_screen_edge_lengths(ohg_mesh* m, const int* ev2v, int n, float* lo, float* hi,
                             double* exact) {
   MESH_GUARD(m);
@@ -894,11 +900,15 @@ int ohg_find_indset(ohg_mesh* m, int d, const double* q, const signed char* cand
   MESH_GUARD(m);
   return guarded(m->owner, [&] {
     LO n = m->mesh.nents[d];
-    int r = 0;
+    Ctx& x = ctx();
+    OHG_CUDA(cudaMemsetAsync(x.d_indset_sweeps, 0, sizeof(int), x.stream));
     Arr<I8> res = find_indset(m->mesh, d, Arr<double>::wrap(const_cast<double*>(q), n),
-                              Arr<I8>::wrap(const_cast<I8*>(cands), n), &r);
-    OHG_CUDA(cudaMemcpyAsync(out, res.data(), size_t(n), cudaMemcpyDeviceToDevice, ctx().stream));
-    if (rounds) *rounds = r;
+                              Arr<I8>::wrap(const_cast<I8*>(cands), n));
+    OHG_CUDA(cudaMemcpyAsync(out, res.data(), size_t(n), cudaMemcpyDeviceToDevice, x.stream));
+    OHG_CUDA(cudaMemcpyAsync(x.h_indset_sweeps, x.d_indset_sweeps, sizeof(int),
+                             cudaMemcpyDeviceToHost, x.stream));
+    x.sync();
+    if (rounds) *rounds = d == m->mesh.dim ? 0 : *x.h_indset_sweeps;
   });
 }
 
@@ -1017,11 +1027,15 @@ int ohg_find_indset_graph(ohg_context* c, int n, const int* xa, const int* xb, c
     Adj g;
     g.a2ab = Arr<LO>::wrap(const_cast<LO*>(xa), n + 1);
     g.ab2b = Arr<LO>::wrap(const_cast<LO*>(xb), 0);
-    int r = 0;
+    Ctx& x = ctx();
+    OHG_CUDA(cudaMemsetAsync(x.d_indset_sweeps, 0, sizeof(int), x.stream));
     Arr<I8> res = find_indset(g, n, Arr<double>::wrap(const_cast<double*>(q), n),
-                              Arr<I8>::wrap(const_cast<I8*>(cands), n), &r);
-    OHG_CUDA(cudaMemcpyAsync(out, res.data(), size_t(n), cudaMemcpyDeviceToDevice, ctx().stream));
-    if (rounds) *rounds = r;
+                              Arr<I8>::wrap(const_cast<I8*>(cands), n));
+    OHG_CUDA(cudaMemcpyAsync(out, res.data(), size_t(n), cudaMemcpyDeviceToDevice, x.stream));
+    OHG_CUDA(cudaMemcpyAsync(x.h_indset_sweeps, x.d_indset_sweeps, sizeof(int),
+                             cudaMemcpyDeviceToHost, x.stream));
+    x.sync();
+    if (rounds) *rounds = *x.h_indset_sweeps;
   });
 }
 int ohg_sort_by_keys(ohg_context* c, const void* keys, int n, int width, int kb, int* perm) {

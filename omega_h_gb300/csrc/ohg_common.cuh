@@ -100,12 +100,20 @@ struct Ctx {
   int num_sms = 0;  // streaming multiprocessors of the device
   std::uint64_t launches = 0;
   std::uint64_t syncs = 0;  // host waits on the stream (sizes and flags read back)
+  // host waits per source line of the caller, kept when the environment sets
+  // OHG_TRACE_SYNCS and printed to stderr when the context is destroyed
+  bool trace_syncs = false;
+  std::map<std::pair<std::string, int>, std::uint64_t> sync_sites;
   std::uint64_t allocs = 0;  // device allocations made through dev_alloc
   // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
   int screening = 1;
   // screening counters: cavity tets screened, tets recomputed in FP64,
   // edge lengths screened, edge lengths recomputed in FP64
   unsigned long long* d_screen_counts = nullptr;
+  // independent-set sweeps (the largest sweep count of any thread, summed
+  // over the calls since the counter was last cleared) and its pinned copy
+  int* d_indset_sweeps = nullptr;
+  int* h_indset_sweeps = nullptr;
   // opt-in timing of named kernels: CUDA events on the context's stream
   // around each launch, resolved when read (no synchronisation in between)
   bool time_kernels = false;
@@ -120,7 +128,7 @@ struct Ctx {
   ~Ctx();
   Ctx(const Ctx&) = delete;
   Ctx& operator=(const Ctx&) = delete;
-  void sync();
+  void sync(const char* file = __builtin_FILE(), int line = __builtin_LINE());
   // reads and clears the device status word (synchronises the stream)
   int take_status();
 };

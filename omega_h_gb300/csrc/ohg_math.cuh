@@ -486,27 +486,43 @@ OHG_HD M3 compose_ortho3(const M3& q, V3 l) {
   for (int i = 0; i < 3; ++i) d.c[i].x[i] = l.x[i];
   return mm3(mm3(q, d), tr3(q));
 }
-// exp(mean(log M0, log M1)) for two packed metrics
-OHG_HD bool average_metric3(const double* m0, const double* m1, double* out) {
+// log M of a packed metric (linearize_metric, src/Omega_h_metric.hpp:105-125)
+// as the full 3x3 matrix, column by column; false if the eigendecomposition
+// failed
+OHG_HD bool log_metric3(const double* m, double* L9) {
+  Eig3 e = eigen3(symm3(m));
+  for (int i = 0; i < 3; ++i) e.l.x[i] = log_cr(e.l.x[i]);
+  M3 L = compose_ortho3(e.q, e.l);
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) L9[j * 3 + i] = L.c[j].x[i];
+  return e.ok;
+}
+// exp(mean of two log metrics) (average_metric, src/Omega_h_metric.hpp:
+// 127-150): the sum starts from zero and adds L0, then L1, as the reference
+// accumulates it
+OHG_HD bool average_log_metrics3(const double* L0, const double* L1, double* out) {
   M3 am;
   for (int j = 0; j < 3; ++j)
     for (int i = 0; i < 3; ++i) am.c[j].x[i] = 0.0;
-  bool ok = true;
   for (int k = 0; k < 2; ++k) {
-    Eig3 e = eigen3(symm3(k == 0 ? m0 : m1));
-    ok = ok && e.ok;
-    for (int i = 0; i < 3; ++i) e.l.x[i] = log_cr(e.l.x[i]);
-    M3 L = compose_ortho3(e.q, e.l);
+    const double* L = k == 0 ? L0 : L1;
     for (int j = 0; j < 3; ++j)
-      for (int i = 0; i < 3; ++i) am.c[j].x[i] = am.c[j].x[i] + L.c[j].x[i];
+      for (int i = 0; i < 3; ++i) am.c[j].x[i] = am.c[j].x[i] + L[j * 3 + i];
   }
   for (int j = 0; j < 3; ++j)
     for (int i = 0; i < 3; ++i) am.c[j].x[i] = am.c[j].x[i] / 2;
   Eig3 e = eigen3(am);
-  ok = ok && e.ok;
   for (int i = 0; i < 3; ++i) e.l.x[i] = exp_cr(e.l.x[i]);
   unsymm3(compose_ortho3(e.q, e.l), out);
-  return ok;
+  return e.ok;
+}
+// exp(mean(log M0, log M1)) for two packed metrics
+OHG_HD bool average_metric3(const double* m0, const double* m1, double* out) {
+  double L0[9], L1[9];
+  bool ok0 = log_metric3(m0, L0);
+  bool ok1 = log_metric3(m1, L1);
+  bool ok2 = average_log_metrics3(L0, L1, out);
+  return ok0 && ok1 && ok2;
 }
 
 // ------------------------------------------------------------ eigen (2x2)

@@ -1215,6 +1215,30 @@ void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
       LO e = all ? a : ed[a];
       o[a] = average_metric_iso(mt[ev[e * 2]], mt[ev[e * 2 + 1]]);
     });
+  } else if (m.dim == 3 && 2LL * n >= (long long)m.nverts()) {
+    // many edges: each vertex's log metric once, then one eigendecomposition
+    // per edge instead of three (the same doubles: log_metric3 is a function
+    // of the vertex's metric alone)
+    LO nv = m.nverts();
+    Arr<double> logs(LO(9) * nv);
+    auto lg = view(logs);
+    pfor(nv, [=] __device__(LO v) {
+      double L[9];
+      if (!log_metric3(&mt[v * 6], L)) raise_status(st, ST_NUMERIC);
+      for (int k = 0; k < 9; ++k) lg[v * 9 + k] = L[k];
+    });
+    auto lc = cview(logs);
+    pfor(n, [=] __device__(LO a) {
+      LO e = all ? a : ed[a];
+      LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
+      double L0[9], L1[9], r[6];
+      for (int k = 0; k < 9; ++k) {
+        L0[k] = lc[v0 * 9 + k];
+        L1[k] = lc[v1 * 9 + k];
+      }
+      if (!average_log_metrics3(L0, L1, r)) raise_status(st, ST_NUMERIC);
+      for (int k = 0; k < 6; ++k) o[a * 6 + k] = r[k];
+    });
   } else if (m.dim == 3) {
     pfor(n, [=] __device__(LO a) {
       LO e = all ? a : ed[a];

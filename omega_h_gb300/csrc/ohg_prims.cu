@@ -1,5 +1,6 @@
 // Scan, compaction, reduction and radix-sort kernels.
 #include <cfloat>
+#include <cstdlib>
 #include <mutex>
 
 #include "ohg_prims.cuh"
@@ -30,13 +31,25 @@ Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaMallocHost(&h_pinned, kPinnedInts * sizeof(int)));
   OHG_CUDA(cudaMalloc(&d_screen_counts, 4 * sizeof(unsigned long long)));
   OHG_CUDA(cudaMemset(d_screen_counts, 0, 4 * sizeof(unsigned long long)));
+  OHG_CUDA(cudaMalloc(&d_indset_sweeps, sizeof(int)));
+  OHG_CUDA(cudaMemset(d_indset_sweeps, 0, sizeof(int)));
+  OHG_CUDA(cudaMallocHost(&h_indset_sweeps, sizeof(int)));
   cudaMemPool_t pool;
   OHG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
   std::uint64_t thr = ~std::uint64_t(0);
   OHG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  const char* tr = std::getenv("OHG_TRACE_SYNCS");
+  trace_syncs = tr && *tr && *tr != '0';
 }
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
+  if (trace_syncs) {
+    std::fprintf(stderr, "ohg: host waits by call site (%llu in all)\n",
+                 (unsigned long long)syncs);
+    for (auto& kv : sync_sites)
+      std::fprintf(stderr, "ohg:   %s:%d %llu\n", kv.first.first.c_str(), kv.first.second,
+                   (unsigned long long)kv.second);
+  }
   tuner.release();
   for (auto& k : kernel_launches) {
     cudaEventDestroy(k.start);
@@ -44,12 +57,15 @@ Ctx::~Ctx() {
   }
   cudaFree(d_status);
   cudaFree(d_screen_counts);
+  cudaFree(d_indset_sweeps);
+  cudaFreeHost(h_indset_sweeps);
   if (d_swap_tables) cudaFree(d_swap_tables);
   cudaFreeHost(h_pinned);
   cudaStreamDestroy(stream);
 }
-void Ctx::sync() {
+void Ctx::sync(const char* file, int line) {
   ++syncs;
+  if (trace_syncs) ++sync_sites[{file, line}];
   OHG_CUDA(cudaStreamSynchronize(stream));
   if (!tuner.pending.empty()) tuner.resolve();
 }
@@ -613,17 +629,17 @@ static void check_no_stall(const Ctx& c) {
                    "are not used");
 }
 
-LO last(const Arr<LO>& a) {
+LO last(const Arr<LO>& a, const char* file, int line) {
   Ctx& c = ctx();
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, a.data() + a.size() - 1, sizeof(LO),
                            cudaMemcpyDeviceToHost, c.stream));
   queue_status_read(c);
-  c.sync();
+  c.sync(file, line);
   check_no_stall(c);
   return c.h_pinned[0];
 }
 
-void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out) {
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out, const char* file, int line) {
   Ctx& c = ctx();
   int n = int(arrs.size());
   if (n > kPinnedStatusSlot) throw Error(8, "read_lasts: too many arrays");
@@ -631,7 +647,7 @@ void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out) {
     OHG_CUDA(cudaMemcpyAsync(c.h_pinned + i, arrs[i]->data() + arrs[i]->size() - 1, sizeof(LO),
                              cudaMemcpyDeviceToHost, c.stream));
   queue_status_read(c);
-  c.sync();
+  c.sync(file, line);
   check_no_stall(c);
   for (int i = 0; i < n; ++i) out[i] = c.h_pinned[i];
 }
@@ -650,7 +666,7 @@ Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt) {
 
 // indices of the nonzero marks in increasing order: one compaction launch
 // and one read of the count; the result keeps its n-slot buffer
-Arr<LO> collect_marked(const Arr<I8>& marks) {
+Arr<LO> collect_marked(const Arr<I8>& marks, const char* file, int line) {
   LO n = marks.size();
   if (n == 0) return Arr<LO>(0);
   Ctx& c = ctx();
@@ -660,12 +676,12 @@ Arr<LO> collect_marked(const Arr<I8>& marks) {
   launch_lookback<I8, true>(marks.data(), n, out.data(), st, &cnt);
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
   queue_status_read(c);
-  c.sync();
+  c.sync(file, line);
   check_no_stall(c);
   out.n = c.h_pinned[0];
   return out;
 }
-LO count_marked(const Arr<I8>& marks) {
+LO count_marked(const Arr<I8>& marks, const char* file, int line) {
   LO n = marks.size();
   if (n == 0) return 0;
   Ctx& c = ctx();
@@ -674,7 +690,7 @@ LO count_marked(const Arr<I8>& marks) {
   launch_lookback<I8, true>(marks.data(), n, nullptr, st, &cnt);
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
   queue_status_read(c);
-  c.sync();
+  c.sync(file, line);
   check_no_stall(c);
   return c.h_pinned[0];
 }

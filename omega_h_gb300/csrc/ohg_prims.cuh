@@ -25,14 +25,17 @@ LO offset_scan_fixed_limit();
 void scan_wait_limit_selftest(const LO* counts, LO n, LO* out);
 
 // indices of nonzero marks (collect_marked, src/Omega_h_map.cpp:174-185)
-Arr<LO> collect_marked(const Arr<I8>& marks);
-LO count_marked(const Arr<I8>& marks);
+Arr<LO> collect_marked(const Arr<I8>& marks, const char* file = __builtin_FILE(),
+                       int line = __builtin_LINE());
+LO count_marked(const Arr<I8>& marks, const char* file = __builtin_FILE(),
+                int line = __builtin_LINE());
 
-LO last(const Arr<LO>& a);
+LO last(const Arr<LO>& a, const char* file = __builtin_FILE(), int line = __builtin_LINE());
 // FP64 fused multiply-add throughput of the device (GFLOP/s, best of reps)
 double fp64_peak_gflops(int reps);
 // the last element of each array (at most 16) with one host wait
-void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out);
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out,
+                const char* file = __builtin_FILE(), int line = __builtin_LINE());
 // indices of nonzero marks given offset_scan of the 0/1 marks and its total
 Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt);
 

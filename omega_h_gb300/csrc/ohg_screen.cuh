@@ -240,6 +240,116 @@ __device__ __forceinline__ int maxdet_vertex(const ScreenView& s, const LO vv[4]
 
 // Interval of the double tet quality (tet_quality on the maxdet metric), from
 // the four vertices' coordinate pairs and the maxdet vertex's metric record.
+// Running sums over a tet's edges v (float) with error bounds e for the mean
+// squared metric length: G = sum v v^T, H = the off-diagonal of sum |v||v|^T,
+// W = sum e |v| and sum e^2.  Each entry is a sum of at most six products,
+// whose float rounding bound (gamma_6) holds in any order of accumulation.
+struct GramAcc {
+  float gxx = 0.0f, gyy = 0.0f, gzz = 0.0f, gxy = 0.0f, gyz = 0.0f, gzx = 0.0f;
+  float hxy = 0.0f, hyz = 0.0f, hzx = 0.0f;
+  float wx = 0.0f, wy = 0.0f, wz = 0.0f, esq = 0.0f;
+  __device__ __forceinline__ void add(const float v[3], float e) {
+    float ax = fabsf(v[0]), ay = fabsf(v[1]), az = fabsf(v[2]);
+    gxx = __fmaf_rn(v[0], v[0], gxx);
+    gyy = __fmaf_rn(v[1], v[1], gyy);
+    gzz = __fmaf_rn(v[2], v[2], gzz);
+    gxy = __fmaf_rn(v[0], v[1], gxy);
+    gyz = __fmaf_rn(v[1], v[2], gyz);
+    gzx = __fmaf_rn(v[2], v[0], gzx);
+    hxy = __fmaf_rn(ax, ay, hxy);
+    hyz = __fmaf_rn(ay, az, hyz);
+    hzx = __fmaf_rn(az, ax, hzx);
+    wx = __fmaf_rn(e, ax, wx);
+    wy = __fmaf_rn(e, ay, wy);
+    wz = __fmaf_rn(e, az, wz);
+    esq = __fmaf_rn(e, e, esq);
+  }
+};
+
+// The quality interval from the triple product T (six times the signed
+// volume, against the double T by at most eT) and the edge sums of G.
+__device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc& G, float4 ma,
+                                               float4 mb) {
+  // rs = T / 6 (here T times float(1/6): one more rounding, so kC2), s = rs * sqrt(det M)
+  float rs = __fmul_rn(T, kSixth);
+  float ers = __fmaf_rn(fabsf(rs), kC2, __fmul_rn(eT, kSixthUp));
+  float sd = mb.w;
+  float sv = __fmul_rn(rs, sd);
+  float es = __fmaf_rn(fabsf(sv), kC2, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
+  es = __fmul_rn(es, kInflate);
+  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
+  if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
+  float s_lo = __fsub_rd(sv, es);
+  // mean squared metric length: the sum over the six edges of v^T M v is
+  // the contraction M : G with G = sum v v^T.  Its float evaluation differs
+  // from the exact value for the float edges and float metric by at most
+  // (gamma_6 for G, gamma_4 for the contraction) times
+  // asum = sum |v|^T |M| |v| = |M| : (sum |v| |v|^T); the metric's
+  // conversion to float adds u asum and the double evaluation far less
+  // (12.2 u asum in all).  The edge errors e_i perturb the sum by at most
+  // sum 2 e_i 1^T |M| |v_i| + e_i^2 S0 = 2 c . w + S0 sum e_i^2, with c the
+  // column sums of |M| and w = sum e_i |v_i|.
+  float mxx = ma.x, myy = ma.y, mzz = ma.z, myx = ma.w, mzy = mb.x, mzx = mb.y;
+  float dg = __fmaf_rn(mzz, G.gzz, __fmaf_rn(myy, G.gyy, __fmul_rn(mxx, G.gxx)));
+  float od = __fmaf_rn(mzx, G.gzx, __fmaf_rn(mzy, G.gyz, __fmul_rn(myx, G.gxy)));
+  float msum = __fmaf_rn(2.0f, od, dg);
+  float axx = fabsf(mxx), ayy = fabsf(myy), azz = fabsf(mzz), ayx = fabsf(myx), azy = fabsf(mzy),
+        azx = fabsf(mzx);
+  float adg = __fmaf_rn(azz, G.gzz, __fmaf_rn(ayy, G.gyy, __fmul_rn(axx, G.gxx)));
+  float aod = __fmaf_rn(azx, G.hzx, __fmaf_rn(azy, G.hyz, __fmul_rn(ayx, G.hxy)));
+  float asum = __fmaf_rn(2.0f, aod, adg);
+  float cx = __fadd_rn(__fadd_rn(axx, ayx), azx);
+  float cy = __fadd_rn(__fadd_rn(ayx, ayy), azy);
+  float cz = __fadd_rn(__fadd_rn(azx, azy), azz);
+  float cw = __fmaf_rn(cz, G.wz, __fmaf_rn(cy, G.wy, __fmul_rn(cx, G.wx)));
+  float pert = __fmul_rn(__fmaf_rn(2.0f, cw, __fmul_rn(mb.z, G.esq)), 1.0f + kU);
+  float msl = __fmul_rn(msum, kSixth);
+  float emsl = __fmaf_rn(fabsf(msl), kC2,
+                         __fmul_rn(__fmaf_rn(12.2f * kU, asum, __fadd_rn(pert, 16.0f * kTiny)),
+                                   kSixthUp));
+  emsl = __fmul_rn(emsl, kInflate);
+  float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
+  // the range keeps __fdividef within its documented 2-ulp error
+  if (!(msl_lo > 1e-30f) || !(msl_hi < 1e30f)) return widen_all();
+  if (s_lo < 0.0f) {
+    // sign of the size not settled: the value is either s (>= s_lo) or a
+    // non-negative quality
+    return {s_lo, INFINITY};
+  }
+  // x = s / 0.1178511301977579, y = x * x
+  float x = __fmul_rn(sv, 8.485281374238571f);
+  float ex = __fmaf_rn(fabsf(x), kC2, __fmul_rn(es, 8.4853f));
+  float y = __fmul_rn(x, x);
+  float ey = __fmaf_rn(fabsf(y), kC1, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
+  ey = __fmul_rn(ey, kInflate);
+  // cbrt over [y - ey, y + ey] from one cbrtf (at most 1 ulp; the double
+  // cbrt is correctly rounded): with d = ey / y,
+  //   (1 + d)^(1/3) <= 1 + d/3 and (1 - d)^(1/3) >= 1 - d/3 - d^2 (d <= 1/2)
+  float r_lo, r_hi;
+  if (!(y < 1e30f) || !(ey < 1e30f)) return widen_all();  // keeps __fdividef in range
+  if (!(y > 1e-30f)) {
+    r_lo = 0.0f;
+    r_hi = __fmul_ru(cbrtf(__fadd_ru(fmaxf(y, 0.0f), ey)), 1.0f + 0x1p-20f);
+  } else {
+    float cy = cbrtf(y);
+    float d = __fmul_ru(__fdividef(ey, y), 1.0f + 0x1p-21f);
+    r_hi = __fmul_ru(__fmul_ru(cy, 1.0f + 0x1p-21f), __fmaf_ru(d, 0.33333334f, 1.0f));
+    if (d <= 0.5f) {
+      float f = __fsub_rd(__fmaf_rd(-d, 0.33333334f, 1.0f), __fmul_ru(d, d));
+      r_lo = __fmul_rd(__fmul_rd(cy, 1.0f - 0x1p-21f), f);
+    } else {
+      r_lo = 0.0f;
+    }
+  }
+  // q = r / msl; __fdividef is within 2 ulp for divisors in [2^-126, 2^126]
+  FIv q = {__fmul_rd(__fdividef(r_lo, msl_hi), 1.0f - 0x1p-21f),
+           __fmul_ru(__fdividef(r_hi, msl_lo), 1.0f + 0x1p-21f)};
+  if (!finite_iv(q)) return widen_all();
+  return q;
+}
+
+// Interval of the double tet quality (tet_quality on the maxdet metric), from
+// the four vertices' coordinate pairs and the maxdet vertex's metric record.
 __device__ __forceinline__ FIv tet_quality_bounds_of(const float4 h[4], const float4 l[4],
                                                      float4 ma, float4 mb) {
   // the six edges in the reference's order; the third, -b1, has the same
@@ -287,103 +397,125 @@ __device__ __forceinline__ FIv tet_quality_bounds_of(const float4 h[4], const fl
       6.0f, __fmaf_rn(__fmul_rn(e0, e1), __fadd_rn(n2, e2),
                       __fmaf_rn(__fmul_rn(e0, e2), n1, __fmul_rn(__fmul_rn(e1, e2), n0))));
   float eT = __fmaf_rn(5.1f * kU, P, __fadd_rn(__fadd_rn(first, second), kTiny));
-  // rs = T / 6 (here T times float(1/6): one more rounding, so kC2), s = rs * sqrt(det M)
-  float rs = __fmul_rn(T, kSixth);
-  float ers = __fmaf_rn(fabsf(rs), kC2, __fmul_rn(eT, kSixthUp));
-  float sd = mb.w;
-  float sv = __fmul_rn(rs, sd);
-  float es = __fmaf_rn(fabsf(sv), kC2, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
-  es = __fmul_rn(es, kInflate);
-  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
-  if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
-  float s_lo = __fsub_rd(sv, es);
-  // mean squared metric length: the sum over the six edges of v^T M v is
-  // the contraction M : G with G = sum v v^T.  Its float evaluation differs
-  // from the exact value for the float edges and float metric by at most
-  // (gamma_6 for G, gamma_4 for the contraction) times
-  // asum = sum |v|^T |M| |v| = |M| : (sum |v| |v|^T); the metric's
-  // conversion to float adds u asum and the double evaluation far less
-  // (12.2 u asum in all).  The edge errors e_i perturb the sum by at most
-  // sum 2 e_i 1^T |M| |v_i| + e_i^2 S0 = 2 c . w + S0 sum e_i^2, with c the
-  // column sums of |M| and w = sum e_i |v_i|.
-  float gxx = 0.0f, gyy = 0.0f, gzz = 0.0f, gxy = 0.0f, gyz = 0.0f, gzx = 0.0f;
-  float hxy = 0.0f, hyz = 0.0f, hzx = 0.0f;
-  float wx = 0.0f, wy = 0.0f, wz = 0.0f, esq = 0.0f;
+  GramAcc G;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    const float* v = ev[i];
-    float ax = fabsf(v[0]), ay = fabsf(v[1]), az = fabsf(v[2]), e = ee[i];
-    gxx = __fmaf_rn(v[0], v[0], gxx);
-    gyy = __fmaf_rn(v[1], v[1], gyy);
-    gzz = __fmaf_rn(v[2], v[2], gzz);
-    gxy = __fmaf_rn(v[0], v[1], gxy);
-    gyz = __fmaf_rn(v[1], v[2], gyz);
-    gzx = __fmaf_rn(v[2], v[0], gzx);
-    hxy = __fmaf_rn(ax, ay, hxy);
-    hyz = __fmaf_rn(ay, az, hyz);
-    hzx = __fmaf_rn(az, ax, hzx);
-    wx = __fmaf_rn(e, ax, wx);
-    wy = __fmaf_rn(e, ay, wy);
-    wz = __fmaf_rn(e, az, wz);
-    esq = __fmaf_rn(e, e, esq);
-  }
-  float mxx = ma.x, myy = ma.y, mzz = ma.z, myx = ma.w, mzy = mb.x, mzx = mb.y;
-  float dg = __fmaf_rn(mzz, gzz, __fmaf_rn(myy, gyy, __fmul_rn(mxx, gxx)));
-  float od = __fmaf_rn(mzx, gzx, __fmaf_rn(mzy, gyz, __fmul_rn(myx, gxy)));
-  float msum = __fmaf_rn(2.0f, od, dg);
-  float axx = fabsf(mxx), ayy = fabsf(myy), azz = fabsf(mzz), ayx = fabsf(myx), azy = fabsf(mzy),
-        azx = fabsf(mzx);
-  float adg = __fmaf_rn(azz, gzz, __fmaf_rn(ayy, gyy, __fmul_rn(axx, gxx)));
-  float aod = __fmaf_rn(azx, hzx, __fmaf_rn(azy, hyz, __fmul_rn(ayx, hxy)));
-  float asum = __fmaf_rn(2.0f, aod, adg);
-  float cx = __fadd_rn(__fadd_rn(axx, ayx), azx);
-  float cy = __fadd_rn(__fadd_rn(ayx, ayy), azy);
-  float cz = __fadd_rn(__fadd_rn(azx, azy), azz);
-  float cw = __fmaf_rn(cz, wz, __fmaf_rn(cy, wy, __fmul_rn(cx, wx)));
-  float pert = __fmul_rn(__fmaf_rn(2.0f, cw, __fmul_rn(mb.z, esq)), 1.0f + kU);
-  float msl = __fmul_rn(msum, kSixth);
-  float emsl = __fmaf_rn(fabsf(msl), kC2,
-                         __fmul_rn(__fmaf_rn(12.2f * kU, asum, __fadd_rn(pert, 16.0f * kTiny)),
-                                   kSixthUp));
-  emsl = __fmul_rn(emsl, kInflate);
-  float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
-  // the range keeps __fdividef within its documented 2-ulp error
-  if (!(msl_lo > 1e-30f) || !(msl_hi < 1e30f)) return widen_all();
-  if (s_lo < 0.0f) {
-    // sign of the size not settled: the value is either s (>= s_lo) or a
-    // non-negative quality
-    return {s_lo, INFINITY};
-  }
-  // x = s / 0.1178511301977579, y = x * x
-  float x = __fmul_rn(sv, 8.485281374238571f);
-  float ex = __fmaf_rn(fabsf(x), kC2, __fmul_rn(es, 8.4853f));
-  float y = __fmul_rn(x, x);
-  float ey = __fmaf_rn(fabsf(y), kC1, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
-  ey = __fmul_rn(ey, kInflate);
-  // cbrt over [y - ey, y + ey] from one cbrtf (at most 1 ulp; the double
-  // cbrt is correctly rounded): with d = ey / y,
-  //   (1 + d)^(1/3) <= 1 + d/3 and (1 - d)^(1/3) >= 1 - d/3 - d^2 (d <= 1/2)
-  float r_lo, r_hi;
-  if (!(y < 1e30f) || !(ey < 1e30f)) return widen_all();  // keeps __fdividef in range
-  if (!(y > 1e-30f)) {
-    r_lo = 0.0f;
-    r_hi = __fmul_ru(cbrtf(__fadd_ru(fmaxf(y, 0.0f), ey)), 1.0f + 0x1p-20f);
+  for (int i = 0; i < 6; ++i) G.add(ev[i], ee[i]);
+  return tet_bounds_tail(T, eT, G, ma, mb);
+}
+
+// The same interval for the tets of a collapse, with the parts that do not
+// depend on the vertex moved onto computed once per element.
+//
+// A star element of the collapsing vertex keeps the face opposite that
+// vertex's slot k; the new tet puts the vertex p moved onto at slot k.  With
+// the face's vertices f0, f1, f2 in slot order, the triple product of the
+// reference, det[x1 - x0, x2 - x0, x3 - x0] in slot order, equals
+// (u x w) . (p - f0) with (u, w) = (f2 - f0, f1 - f0) for k even and
+// (f1 - f0, f2 - f0) for k odd (expand the determinant along the column of
+// p).  So n = u x w, its absolute-value form and the face's three edges'
+// Gram sums are invariants of the element.
+//
+// The float evaluation of (u x w) . d has the same structure, and the same
+// rounding bound 5.1 u P with P = |d| . (|u| x |w|)_abs, as the reference
+// order's (b0 x b1) . b2; its input perturbation is bounded as there, with
+// the first-order terms e_u sum|w x d|_abs <= e_u |w|_1 |d|_1 (likewise for
+// w) and e_d sum (|u| x |w|)_abs.  The double value differs from the exact
+// triple product of the exact coordinate differences by at most
+// 8.1 u_double P_ref (five roundings of the evaluation and one per edge
+// difference), P_ref <= 6 L^3 with L bounding every edge component of the
+// new tet: 2^-47 L^3 covers it.
+struct TetFaceInv {
+  float4 a, b, c, d, e, f;
+  // a = (n, sum (|u| x |w|)_abs), b = ((|u| x |w|)_abs, e_u |w|_1 + e_w |u|_1),
+  // c = (e_u e_w, e_u |w|_inf + e_w |u|_inf, L of the face edges, sum e^2),
+  // d..f = the face edges' Gram sums (gxx gyy gzz gxy | gyz gzx hxy hyz |
+  // hzx wx wy wz)
+};
+
+__device__ __forceinline__ TetFaceInv tet_face_invariants(const float4 h[3], const float4 l[3],
+                                                          int k) {
+  float u[3], w[3], t[3];
+  float eu, ew;
+  if (k & 1) {
+    eu = sdiff3(h[1], l[1], h[0], l[0], u);
+    ew = sdiff3(h[2], l[2], h[0], l[0], w);
   } else {
-    float cy = cbrtf(y);
-    float d = __fmul_ru(__fdividef(ey, y), 1.0f + 0x1p-21f);
-    r_hi = __fmul_ru(__fmul_ru(cy, 1.0f + 0x1p-21f), __fmaf_ru(d, 0.33333334f, 1.0f));
-    if (d <= 0.5f) {
-      float f = __fsub_rd(__fmaf_rd(-d, 0.33333334f, 1.0f), __fmul_ru(d, d));
-      r_lo = __fmul_rd(__fmul_rd(cy, 1.0f - 0x1p-21f), f);
-    } else {
-      r_lo = 0.0f;
-    }
+    eu = sdiff3(h[2], l[2], h[0], l[0], u);
+    ew = sdiff3(h[1], l[1], h[0], l[0], w);
   }
-  // q = r / msl; __fdividef is within 2 ulp for divisors in [2^-126, 2^126]
-  FIv q = {__fmul_rd(__fdividef(r_lo, msl_hi), 1.0f - 0x1p-21f),
-           __fmul_ru(__fdividef(r_hi, msl_lo), 1.0f + 0x1p-21f)};
-  if (!finite_iv(q)) return widen_all();
-  return q;
+  float et = sdiff3(h[2], l[2], h[1], l[1], t);
+  float n0 = __fmaf_rn(u[1], w[2], -__fmul_rn(u[2], w[1]));
+  float n1 = __fmaf_rn(u[2], w[0], -__fmul_rn(u[0], w[2]));
+  float n2 = __fmaf_rn(u[0], w[1], -__fmul_rn(u[1], w[0]));
+  float au[3] = {fabsf(u[0]), fabsf(u[1]), fabsf(u[2])};
+  float aw[3] = {fabsf(w[0]), fabsf(w[1]), fabsf(w[2])};
+  float A0 = __fmaf_rn(au[1], aw[2], __fmul_rn(au[2], aw[1]));
+  float A1 = __fmaf_rn(au[2], aw[0], __fmul_rn(au[0], aw[2]));
+  float A2 = __fmaf_rn(au[0], aw[1], __fmul_rn(au[1], aw[0]));
+  float cuw = __fadd_rn(__fadd_rn(A0, A1), A2);
+  float nu = fmaxf(au[0], fmaxf(au[1], au[2]));
+  float nw = fmaxf(aw[0], fmaxf(aw[1], aw[2]));
+  float nt = fmaxf(fabsf(t[0]), fmaxf(fabsf(t[1]), fabsf(t[2])));
+  float u1 = __fadd_rn(__fadd_rn(au[0], au[1]), au[2]);
+  float w1 = __fadd_rn(__fadd_rn(aw[0], aw[1]), aw[2]);
+  float K1 = __fmaf_rn(eu, w1, __fmul_rn(ew, u1));
+  float E2a = __fmul_rn(eu, ew);
+  float E2b = __fmaf_rn(eu, nw, __fmul_rn(ew, nu));
+  float L = fmaxf(__fadd_rn(nu, eu), fmaxf(__fadd_rn(nw, ew), __fadd_rn(nt, et)));
+  GramAcc G;
+  G.add(u, eu);
+  G.add(w, ew);
+  G.add(t, et);
+  TetFaceInv r;
+  r.a = make_float4(n0, n1, n2, cuw);
+  r.b = make_float4(A0, A1, A2, K1);
+  r.c = make_float4(E2a, E2b, L, G.esq);
+  r.d = make_float4(G.gxx, G.gyy, G.gzz, G.gxy);
+  r.e = make_float4(G.gyz, G.gzx, G.hxy, G.hyz);
+  r.f = make_float4(G.hzx, G.wx, G.wy, G.wz);
+  return r;
+}
+
+// Interval of the double quality of the tet that puts p at the slot the
+// invariants were made for; hf/lf the face vertices in slot order, ma/mb the
+// metric record of the new tet's maxdet vertex.
+__device__ __forceinline__ FIv tet_face_bounds(const TetFaceInv& f, const float4 hf[3],
+                                               const float4 lf[3], float4 hp, float4 lp,
+                                               float4 ma, float4 mb) {
+  float d0[3], d1[3], d2[3];
+  float e0 = sdiff3(hp, lp, hf[0], lf[0], d0);
+  float e1 = sdiff3(hp, lp, hf[1], lf[1], d1);
+  float e2 = sdiff3(hp, lp, hf[2], lf[2], d2);
+  float T = __fmaf_rn(f.a.z, d0[2], __fmaf_rn(f.a.y, d0[1], __fmul_rn(f.a.x, d0[0])));
+  float P = __fmaf_rn(fabsf(d0[2]), f.b.z, __fmaf_rn(fabsf(d0[1]), f.b.y,
+                                                     __fmul_rn(fabsf(d0[0]), f.b.x)));
+  float n_d = fmaxf(fabsf(d0[0]), fmaxf(fabsf(d0[1]), fabsf(d0[2])));
+  float d_1 = __fadd_rn(__fadd_rn(fabsf(d0[0]), fabsf(d0[1])), fabsf(d0[2]));
+  float first = __fmaf_rn(f.b.w, d_1, __fmul_rn(e0, f.a.w));
+  float second = __fmul_rn(6.0f, __fmaf_rn(f.c.x, __fadd_rn(n_d, e0), __fmul_rn(e0, f.c.y)));
+  float n1 = fmaxf(fabsf(d1[0]), fmaxf(fabsf(d1[1]), fabsf(d1[2])));
+  float n2 = fmaxf(fabsf(d2[0]), fmaxf(fabsf(d2[1]), fabsf(d2[2])));
+  float L = fmaxf(f.c.z, fmaxf(__fadd_rn(n_d, e0), fmaxf(__fadd_rn(n1, e1), __fadd_rn(n2, e2))));
+  float dbl = __fmul_rn(0x1p-47f, __fmul_rn(L, __fmul_rn(L, L)));
+  float eT = __fmaf_rn(5.1f * kU, P, __fadd_rn(__fadd_rn(__fadd_rn(first, second), dbl), kTiny));
+  GramAcc G;
+  G.gxx = f.d.x;
+  G.gyy = f.d.y;
+  G.gzz = f.d.z;
+  G.gxy = f.d.w;
+  G.gyz = f.e.x;
+  G.gzx = f.e.y;
+  G.hxy = f.e.z;
+  G.hyz = f.e.w;
+  G.hzx = f.f.x;
+  G.wx = f.f.y;
+  G.wy = f.f.z;
+  G.wz = f.f.w;
+  G.esq = f.c.w;
+  G.add(d0, e0);
+  G.add(d1, e1);
+  G.add(d2, e2);
+  return tet_bounds_tail(T, eT, G, ma, mb);
 }
 
 __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {

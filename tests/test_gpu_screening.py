@@ -89,6 +89,47 @@ def test_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     m.close()
 
 
+@pytest.mark.parametrize("n,kind,seed", [(12, 0, 1), (16, 1, 7), (16, 2, 3), (16, 13, 4)])
+def test_face_route_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
+    """The collapse screen's route: invariants of the face opposite one slot,
+    then the vertex at that slot, for every slot, on the mesh's tets, their
+    mirror images and tets with one vertex moved to a far vertex (arbitrary
+    shapes, slivers, inversions).  The intervals must hold the FP64 value as
+    the reference evaluates it, in its slot order."""
+    import torch
+    from omega_h_gb300 import _lib
+    m = _mesh(ctx, n, kind, seed)
+    tv = m.get("ev2v_3").view(-1, 4)
+    nt = tv.shape[0]
+    nv = m.nents(0)
+    g = torch.Generator().manual_seed(seed)
+    col = torch.randint(0, 4, (nt,), generator=g).cuda()
+    rows = torch.arange(nt, device=tv.device)
+    mixed = tv.clone()
+    far = torch.randint(0, nv - 1, (nt,), generator=g).cuda()
+    mixed[rows, col] = ((tv[rows, col].long() + 1 + far) % nv).to(tv.dtype)
+    tets = torch.cat([tv, tv[:, [1, 0, 2, 3]], mixed]).contiguous()
+    lo0, hi0, ex0 = _screen(m, "ohg_screen_tet_qualities", tets, 4)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    nn = tets.shape[0]
+    for slot in range(4):
+        lo = torch.empty(nn, dtype=torch.float32, device="cuda")
+        hi = torch.empty_like(lo)
+        ex = torch.empty(nn, dtype=torch.float64, device="cuda")
+        _lib.call("ohg_screen_tet_qualities_face", m.handle, P(tets), nn, slot, P(lo), P(hi),
+                  P(ex))
+        torch.cuda.synchronize()
+        lo, hi, ex = (lo.cpu().numpy().astype(np.float64), hi.cpu().numpy().astype(np.float64),
+                      ex.cpu().numpy())
+        assert np.array_equal(ex, ex0)
+        _check_enclosure(lo, hi, ex, f"tet qualities, face route, slot {slot}")
+        # no wider than a few times the direct route's interval
+        fin = np.isfinite(lo) & np.isfinite(hi) & np.isfinite(lo0) & np.isfinite(hi0) & (ex > 0)
+        r = (hi[fin] - lo[fin]) / np.maximum(hi0[fin] - lo0[fin], 1e-300)
+        assert np.median(r) < 2.0
+    m.close()
+
+
 @pytest.mark.parametrize("n,kind,seed", [(32, 0, 1), (48, 1, 7), (40, 2, 3), (64, 3, 5),
                                          (48, 13, 6)])
 def test_2d_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
