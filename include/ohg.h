@@ -242,10 +242,11 @@ int ohg_screen_tet_qualities(ohg_mesh* mesh, const int* tv2v_dev, int n, float* 
                              float* hi_dev, double* exact_dev);
 /* the same intervals by the collapse screen's per-face route: the face
  * opposite vertex slot `slot` (0..3) of each tet taken as fixed, its
- * invariants made once, and the vertex at `slot` as the one moved onto
- * (a 3D mesh only; exposed for checking it) */
+ * invariants made once, and the vertex at `slot` as the one moved onto;
+ * cubed != 0: [lo, hi] bounds the cube of the quality, as the 3D collapse
+ * screen compares it (a 3D mesh only; exposed for checking it) */
 int ohg_screen_tet_qualities_face(ohg_mesh* mesh, const int* tv2v_dev, int n, int slot,
-                                  float* lo_dev, float* hi_dev, double* exact_dev);
+                                  int cubed, float* lo_dev, float* hi_dev, double* exact_dev);
 /* the same for the metric length (edge_length, src/Omega_h_shape.hpp:112-157)
  * of n vertex pairs */
 int ohg_screen_edge_lengths(ohg_mesh* mesh, const int* ev2v_dev, int n, float* lo_dev,

@@ -143,8 +143,8 @@ SIGNATURES = {
     "ohg_collect_marked": [c_void_p, c_void_p, c_int, c_void_p, c_void_p],
     "ohg_selftest_scan_wait_limit": [c_void_p, c_void_p, c_int, c_void_p],
     "ohg_screen_tet_qualities": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
-    "ohg_screen_tet_qualities_face": [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
-                                      c_void_p],
+    "ohg_screen_tet_qualities_face": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p,
+                                      c_void_p, c_void_p],
     "ohg_screen_edge_lengths": [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p],
     "ohg_context_set_screening": [c_void_p, c_int],
     "ohg_context_time_kernels": [c_void_p, c_int],

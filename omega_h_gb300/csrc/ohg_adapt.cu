@@ -164,10 +164,11 @@ void screen_tets(Mesh& m, const LO* tv2v_p, LO n, float* lo_p, float* hi_p, doub
 }
 
 // The per-face route of the collapse screen: each tet's quality interval
-// from its face opposite slot k (invariants made once) and the vertex at
-// slot k, with the exact FP64 value beside it
-void screen_tets_face(Mesh& m, const LO* tv2v_p, LO n, int k, float* lo_p, float* hi_p,
-                      double* ex_p) {
+// (cubed: the interval of its cube) from its face opposite slot k
+// (invariants made once) and the vertex at slot k, with the exact FP64
+// value beside it
+void screen_tets_face(Mesh& m, const LO* tv2v_p, LO n, int k, bool cubed, float* lo_p,
+                      float* hi_p, double* ex_p) {
   if (m.dim != 3 || k < 0 || k > 3) throw Error(1, "screen_tets_face: a 3D mesh and a slot 0..3");
   const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
@@ -190,7 +191,10 @@ void screen_tets_face(Mesh& m, const LO* tv2v_p, LO n, int k, float* lo_p, float
     }
     int mi = maxdet_vertex(sv, vv);
     TetFaceInv f = tet_face_invariants(hf, lf, k);
-    FIv b = tet_face_bounds(f, hf, lf, sv.xh[vv[k]], sv.xl[vv[k]], sv.ma[vv[mi]], sv.mb[vv[mi]]);
+    FIv b = cubed ? tet_face_bounds<true>(f, hf, lf, sv.xh[vv[k]], sv.xl[vv[k]], sv.ma[vv[mi]],
+                                          sv.mb[vv[mi]])
+                  : tet_face_bounds<false>(f, hf, lf, sv.xh[vv[k]], sv.xl[vv[k]], sv.ma[vv[mi]],
+                                           sv.mb[vv[mi]]);
     lo[i] = b.lo;
     hi[i] = b.hi;
     ex[i] = tet_quality_exact(sv, c, mt, vv);
@@ -511,19 +515,30 @@ struct ModifyOut {
 
 // modify_ents_adapt / modify_ents / modify_conn (src/Omega_h_modify.cpp:20-70,
 // 141-517) for one entity dimension; global numbers equal local numbers on
-// one device, so the local numbering is the global numbering
-static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
-                                   const Arr<LO>& keys2kds, const Arr<LO>& keys2prods,
-                                   const Arr<LO>& prod_verts2verts,
-                                   const Arr<LO>& old_lows2new_lows) {
+// one device, so the local numbering is the global numbering.
+//
+// In two phases: plan_modify finds the kept entities, the representatives
+// and the new numbering's offsets on the device; the three sizes it needs
+// (kept, new, products) are the last elements of three of its arrays, so an
+// operator plans every dimension first and reads all their sizes with one
+// host wait (plan_sizes); apply_modify then builds the dimension.
+struct ModifyPlan {
+  bool some_mod = false;
+  Arr<I8> same;
+  Arr<LO> same_offs, reps, offs;
+  LO sizes[3] = {0, 0, 0};  // kept, new, products
+};
+static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>& keys2kds,
+                              const Arr<LO>& keys2prods) {
   LO nkeys = keys2kds.size();
-  ModifyOut out;
+  ModifyPlan pl;
   LO nold = om.nents[ent_dim];
-  // entities kept as they are (0/1 marks and their offsets); the three sizes
-  // this function needs (kept, new, products) are read back together below
+  // entities kept as they are (0/1 marks and their offsets)
   bool some_mod = ent_dim >= key_dim;
-  Arr<I8> same, km;
-  Arr<LO> same_offs;
+  pl.some_mod = some_mod;
+  Arr<I8> km;
+  Arr<I8>& same = pl.same;
+  Arr<LO>& same_offs = pl.same_offs;
   if (some_mod) {
     km = mark_image(keys2kds, om.nents[key_dim]);
     Arr<I8> mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
@@ -534,7 +549,7 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     same_offs = offset_scan(same);
   }
   // representatives (get_mods2reps, src/Omega_h_modify.cpp:163-195)
-  Arr<LO> reps;
+  Arr<LO>& reps = pl.reps;
   if (key_dim == ent_dim) {
     reps = keys2kds;
   } else {
@@ -615,13 +630,47 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
     auto kp = cview(keys2prods);
     pfor(nkeys, [=] __device__(LO k) { atomicAdd(&ct[r[k]], kp[k + 1] - kp[k]); });
   }
-  Arr<LO> offs = offset_scan(counts);
-  LO sizes[3] = {nold, 0, 0};  // kept, new, products
-  if (some_mod) {
-    read_lasts({&same_offs, &offs, &keys2prods}, sizes);
-  } else {
-    read_lasts({&offs, &keys2prods}, sizes + 1);
+  pl.offs = offset_scan(counts);
+  pl.sizes[0] = nold;
+  return pl;
+}
+
+// the sizes of several plans with one host wait (keys2prods[i] belongs to
+// plans[i]); status, if given, receives the device status word read in the
+// same wait (not cleared)
+static void plan_sizes(const std::vector<ModifyPlan*>& plans,
+                       const std::vector<const Arr<LO>*>& keys2prods, int* status = nullptr) {
+  std::vector<const Arr<LO>*> arrs;
+  std::vector<LO*> dst;
+  for (size_t i = 0; i < plans.size(); ++i) {
+    ModifyPlan& pl = *plans[i];
+    if (pl.some_mod) {
+      arrs.push_back(&pl.same_offs);
+      dst.push_back(&pl.sizes[0]);
+    }
+    arrs.push_back(&pl.offs);
+    dst.push_back(&pl.sizes[1]);
+    arrs.push_back(keys2prods[i]);
+    dst.push_back(&pl.sizes[2]);
   }
+  std::vector<LO> got(arrs.size());
+  read_lasts(arrs, got.data(), status);
+  for (size_t i = 0; i < arrs.size(); ++i) *dst[i] = got[i];
+}
+
+static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, const ModifyPlan& pl,
+                              const Arr<LO>& keys2kds, const Arr<LO>& keys2prods,
+                              const Arr<LO>& prod_verts2verts,
+                              const Arr<LO>& old_lows2new_lows) {
+  LO nkeys = keys2kds.size();
+  ModifyOut out;
+  LO nold = om.nents[ent_dim];
+  bool some_mod = pl.some_mod;
+  const Arr<I8>& same = pl.same;
+  const Arr<LO>& same_offs = pl.same_offs;
+  const Arr<LO>& reps = pl.reps;
+  const Arr<LO>& offs = pl.offs;
+  const LO* sizes = pl.sizes;
   LO nnew = sizes[1];
   out.same2old = some_mod ? collect_marked_offs(same, same_offs, sizes[0]) : iota(nold);
   bool has_order = key_dim > ent_dim;
@@ -724,6 +773,16 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
   }
   nm.set_ents(ent_dim, std::move(nd));
   return out;
+}
+
+static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
+                                   const Arr<LO>& keys2kds, const Arr<LO>& keys2prods,
+                                   const Arr<LO>& prod_verts2verts,
+                                   const Arr<LO>& old_lows2new_lows) {
+  ModifyPlan pl = plan_modify(om, ent_dim, key_dim, keys2kds, keys2prods);
+  plan_sizes({&pl}, {&keys2prods});
+  return apply_modify(om, nm, ent_dim, key_dim, pl, keys2kds, keys2prods, prod_verts2verts,
+                      old_lows2new_lows);
 }
 
 // transfer_common (src/Omega_h_transfer.cpp:160-180)
@@ -1125,6 +1184,10 @@ void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8*
     int nccs = simplex_degree(cd, cd - 1);
     pfor(n, [=] __device__(LO c) {
       I8 code = in[c];
+      if (!code) {
+        out[c] = 0;
+        return;
+      }
       LO e = c2e[c];
       for (LO x = ea[e]; x < ea[e + 1]; ++x) {
         LO el = eb[x];
@@ -1363,6 +1426,9 @@ struct CoarsenVertexArgs {
   View<const I8> codes;
   View<double> q2;
   float mqa_f;
+  // cubes of the threshold, rounded down and up (3D screens the cube of the
+  // quality)
+  float mqa3_dn, mqa3_up;
   unsigned long long* queue;  // [0] next vertex, [1] directions in the FP64 list
   LO* amb_dir;
   float* amb_mhi;
@@ -1376,15 +1442,18 @@ __device__ __forceinline__ int fkey(float f) {
 }
 __device__ __forceinline__ float fkey_inv(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
-__device__ __forceinline__ void screen_outcome(const CoarsenVertexArgs& a, LO d, float lo, float hi) {
-  if (hi < a.mqa_f) {
+// cubed: lo and hi bound the cube of the quality; the FP64 list takes the
+// upper bound of the quality itself (a cube root rounded up)
+__device__ __forceinline__ void screen_outcome(const CoarsenVertexArgs& a, LO d, float lo, float hi,
+                                               bool cubed) {
+  if (cubed ? hi < a.mqa3_dn : hi < a.mqa_f) {
     a.q2[d] = -1.0;  // fails
-  } else if (lo >= a.mqa_f) {
+  } else if (cubed ? lo >= a.mqa3_up : lo >= a.mqa_f) {
     a.q2[d] = CUDART_NAN;  // passes on its enclosure
   } else {
     LO k = LO(atomicAdd(&a.queue[1], 1ULL));
     a.amb_dir[k] = d;
-    a.amb_mhi[k] = hi;
+    a.amb_mhi[k] = cubed ? __fmul_ru(cbrtf(hi), 1.0f + 0x1p-20f) : hi;
     a.q2[d] = -1.0;  // replaced by the FP64 minimum
   }
 }
@@ -1399,6 +1468,8 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
   constexpr int kInv = D == 3 ? kVsMaxElems3 : 1;
   __shared__ TetFaceInv s_inv[kVsWarps][kInv];
   __shared__ unsigned char s_slot[kVsWarps][kInv];  // slot | first maxdet face slot << 4
+  // (element, direction) pairs queued for screening: element * 32 + direction
+  __shared__ unsigned short s_q[kVsWarps][64];
   __shared__ float4 s_h[kVsWarps][kVsMaxLocal], s_l[kVsWarps][kVsMaxLocal];
   __shared__ float4 s_ma[kVsWarps][kVsMaxLocal], s_mb[kVsWarps][kVsMaxLocal];
   __shared__ long long s_key[kVsWarps][kVsMaxLocal];
@@ -1407,9 +1478,6 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
   __shared__ int s_lo[kVsWarps][kVsMaxLocal], s_hi[kVsWarps][kVsMaxLocal];
   __shared__ unsigned char s_dk[kVsWarps][kVsMaxLocal];  // local indices of the directions
   __shared__ unsigned s_elem[kVsWarps][kMaxE];     // NV local indices, 8 bits each
-  // per local vertex k: the star elements that do not contain k, i.e. the
-  // cavity of the direction onto k, as a bit set; then those not yet screened
-  __shared__ unsigned long long s_rem[kVsWarps][kVsMaxLocal];
   const unsigned full = 0xffffffffu;
   const int w = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31u);
   unsigned nscreen = 0;
@@ -1464,7 +1532,6 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
         s_key[w][k] = a.sv.dkey[u];
         s_lo[w][k] = fkey(1.0f);
         s_hi[w][k] = fkey(1.0f);
-        s_rem[w][k] = S == 64 ? ~0ull : (1ull << S) - 1ull;
       }
       __syncwarp();
       bool found = true;
@@ -1481,7 +1548,6 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
             for (LO k = 1; k <= ne; ++k)
               if (s_gid[w][k] == u) li = unsigned(k);
             if (li == 255) here = false;
-            else atomicAnd(&s_rem[w][li], ~(1ull << x));
           }
           packed |= li << (8 * j);
         }
@@ -1536,7 +1602,7 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
               ++nscreen;
             }
           }
-          screen_outcome(a, d, lo, hi);
+          screen_outcome(a, d, lo, hi, false);
         }
       }
       __syncwarp();
@@ -1552,38 +1618,52 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
       nd += __popc(m);
     }
     __syncwarp();
-    // rounds of (direction, element) pairs over the lanes: each live
-    // direction takes its next 32 / (live directions) cavity elements; a
-    // direction leaves when its cavity is screened or an upper bound fell
-    // below the threshold (its minimum only falls), as the sequential screen
-    // stops at its first failing element
-    int nlive = nd;
+    // (element, direction) pairs, element by element: pair p = x * nd + t
+    // is direction t on element x.  A pair whose element contains the vertex
+    // moved onto is not in the direction's cavity.  Every direction walks
+    // its cavity in element order, and one whose upper bound fell below the
+    // threshold skips the rest (its minimum only falls, as the sequential
+    // screen stops at its first failing element); a direction that is not
+    // skipped is screened in full, so its bounds do not depend on the
+    // schedule.  The warp scans the pairs 32 at a time and queues the ones
+    // to screen in shared memory (ballot compaction); it screens 32 queued
+    // pairs at a time, one per lane.
+    constexpr bool cubed = D == 3;
+    const float fail_below = cubed ? a.mqa3_dn : a.mqa_f;
+    const int npairs = S * nd;
+    const float rnd = 1.0f / float(nd);
+    int p0 = 0, qn = 0;
     for (;;) {
-      int kl = lane < nlive ? s_dk[w][lane] : 0;
-      bool alive = lane < nlive && s_rem[w][kl] != 0ull && !(fkey_inv(s_hi[w][kl]) < a.mqa_f);
-      unsigned am = __ballot_sync(full, alive);
+      while (qn < 32 && p0 < npairs) {
+        int p = p0 + lane;
+        bool take = false;
+        int x = 0, t = 0;
+        if (p < npairs) {
+          x = int((float(p) + 0.5f) * rnd);  // p / nd: exact for p < 2^12, nd <= 32
+          t = p - x * nd;
+          int k = s_dk[w][t];
+          take = __vcmpeq4(s_elem[w][x], unsigned(k) * 0x01010101u) == 0u &&  // not v_onto's
+                 !(fkey_inv(s_hi[w][k]) < fail_below);
+        }
+        unsigned m = __ballot_sync(full, take);
+        if (take) s_q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)(x * 32 + t);
+        qn += __popc(m);
+        p0 += 32;
+      }
+      if (qn == 0) break;
       __syncwarp();
-      if (alive) s_dk[w][__popc(am & ((1u << lane) - 1u))] = (unsigned char)kl;
-      nlive = __popc(am);
-      __syncwarp();
-      if (nlive == 0) break;
-      const int per = 32 / nlive;
-      if (lane < nlive * per) {
-        int i = lane / per, j = lane - i * per;
-        int k = s_dk[w][i];
-        unsigned long long rem = s_rem[w][k];
-        unsigned rlo = unsigned(rem), rhi = unsigned(rem >> 32);
-        int clo = __popc(rlo), x = -1;
-        if (j < clo) x = int(__fns(rlo, 0, j + 1));
-        else if (j - clo < __popc(rhi)) x = 32 + int(__fns(rhi, 0, j - clo + 1));
-        if (x >= 0) {
+      const int nq = qn < 32 ? qn : 32;
+      if (lane < nq) {
+        unsigned qe = s_q[w][lane];
+        int x = int(qe >> 5), t = int(qe & 31u);
+        int k = s_dk[w][t];
+        if (!(fkey_inv(s_hi[w][k]) < fail_below)) {
           unsigned packed = s_elem[w][x];
           FIv b;
           if constexpr (D == 3) {
-            // the face's vertices in slot order, the vertex moved onto at
-            // the collapsing vertex's slot; maxdet as in slot order: the
-            // face's first maximum against k, k first on a tie if its slot
-            // comes first
+            // the face's vertices in slot order, the vertex moved onto at the
+            // collapsing vertex's slot; maxdet as in slot order: the face's
+            // first maximum against k, k first on a tie if its slot comes first
             unsigned sl = s_slot[w][x];
             int pos = int(sl & 15u), fb = int(sl >> 4);
             int j0 = pos == 0 ? 1 : 0, j1 = pos <= 1 ? 2 : 1, j2 = pos <= 2 ? 3 : 2;
@@ -1594,8 +1674,8 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
             int lfb = int((packed >> (8 * fb)) & 255u);
             long long kf = s_key[w][lfb], kp = s_key[w][k];
             int best = (kp > kf || (kp == kf && pos < fb)) ? k : lfb;
-            b = tet_face_bounds(s_inv[w][x], hf, lf, s_h[w][k], s_l[w][k], s_ma[w][best],
-                                s_mb[w][best]);
+            b = tet_face_bounds<true>(s_inv[w][x], hf, lf, s_h[w][k], s_l[w][k], s_ma[w][best],
+                                      s_mb[w][best]);
           } else {
             int li[NV];
             for (int jj = 0; jj < NV; ++jj) {
@@ -1624,17 +1704,17 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
         }
       }
       __syncwarp();
-      if (lane < nlive) {  // drop the elements screened in this round
-        int k = s_dk[w][lane];
-        unsigned long long rem = s_rem[w][k];
-        for (int t = 0; t < per && rem; ++t) rem &= rem - 1ull;
-        s_rem[w][k] = rem;
-      }
+      // move the rest of the queue (fewer than 32) to its front
+      const int rest = qn - nq;
+      unsigned short mv = lane < rest ? s_q[w][nq + lane] : (unsigned short)0;
+      __syncwarp();
+      if (lane < rest) s_q[w][lane] = mv;
+      qn = rest;
       __syncwarp();
     }
     for (LO k = 1 + lane; k <= ne; k += 32) {
       if (s_dir[w][k] >= 0)
-        screen_outcome(a, s_dir[w][k], fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]));
+        screen_outcome(a, s_dir[w][k], fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]), cubed);
     }
     __syncwarp();
   }
@@ -1798,6 +1878,11 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   auto q2 = view(q2_p, n * 2);
   unsigned long long* cnt = ctx().d_screen_counts;
   float mqa_f = float_at_or_above(mqa);  // for float x: x >= mqa <=> x >= mqa_f
+  // floats below and above the exact cube of mqa (the double product is
+  // within 2.1 u_double of it)
+  double mqa3 = mqa * mqa * mqa;
+  float mqa3_dn = float_at_or_below(mqa3 * (1.0 - 0x1p-50));
+  float mqa3_up = float_at_or_above(mqa3 * (1.0 + 0x1p-50));
   // algorithmic bytes: candidates in and codes and q2 out, the candidate
   // edges' vertices, vertex-to-element rows, element vertices and the
   // per-vertex screening data, each read once
@@ -1827,7 +1912,8 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   CoarsenVertexArgs args{nV,   chunk, sv,   ev,   cv,
                          va,   vb,    cview(v2e.a2ab), cview(v2e.ab2b), vc,
                          cview(v2e.codes), cview(e2cand), cview(codes_p, n), q2, mqa_f,
-                         queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
+                         mqa3_dn, mqa3_up, queue.data(), amb_dir.data(), amb_mhi.data(),
+                         &cnt[0]};
   bytes += double(nE) * 4 + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
   {
     KernelTimer timer("coarsen_filter", bytes);
@@ -2201,18 +2287,31 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Arr<I8> codes0 = unmap(c2e, ecodes, 1);
   Arr<I8> codes(c2e.size());
   check_collapse_class(m, c2e.data(), c2e.size(), codes0.data(), codes.data());
-  filter_cands(c2e, codes, nullptr);
-  if (c2e.size() == 0) return false;
-  m.parting = 1;  // ghosted once candidates pass the class check (src/Omega_h_coarsen.cpp:159-164)
+  // The exposure and overshoot checks run on the same list: a candidate
+  // that failed the class check has code 0, which they pass through at
+  // once, so one compaction after the three gives the list the reference
+  // gets by compacting after each (src/Omega_h_coarsen.cpp:159-176).  Whether
+  // any candidate passed the class check (the mesh is then ghosted) is read
+  // with that compaction's count.
+  Arr<int> any_class = fill<int>(1, 0);
+  {
+    auto cd = cview(codes);
+    int* ac = any_class.data();
+    pfor(c2e.size(), [=] __device__(LO i) {
+      if (cd[i]) *ac = 1;
+    });
+  }
   Arr<I8> codes2(c2e.size());
   check_collapse_exposure(m, c2e.data(), c2e.size(), codes.data(), codes2.data());
-  codes = codes2;
-  filter_cands(c2e, codes, nullptr);
-  codes2 = Arr<I8>(c2e.size());
   prevent_coarsen_overshoot(m, allowed ? o.max_length_allowed : o.max_length_desired, c2e.data(),
-                            c2e.size(), codes.data(), codes2.data());
-  codes = codes2;
-  filter_cands(c2e, codes, nullptr);
+                            c2e.size(), codes2.data(), codes.data());
+  int passed_class = 0;
+  {
+    Arr<LO> keep = collect_marked(codes, any_class.data(), &passed_class);
+    c2e = unmap(keep, c2e, 1);
+    codes = unmap(keep, codes, 1);
+  }
+  if (passed_class) m.parting = 1;  // ghosted once candidates pass the class check
   if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
@@ -2337,31 +2436,52 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   nm.metric_comps = m.metric_comps;
   nm.class_sets = m.class_sets;
   Arr<LO> ov2nv, old_lows2new;
+  // find_coarsen_domains: live d-entities around each key vertex, for every
+  // dimension, and every dimension's modify plan, before one host wait for
+  // all their sizes
+  Arr<LO> k2ps[4];
+  ModifyPlan plans[4];
+  k2ps[0] = fill<LO>(nkeys + 1, 0);
+  for (int d = 1; d <= dim; ++d) {
+    const Adj& v2d = m.ask_up(0, d);
+    auto va = cview(v2d.a2ab);
+    auto vb = cview(v2d.ab2b);
+    auto dd = cview(dead[d]);
+    auto kv = cview(k2v);
+    // one warp per key: the lanes stride the key vertex's row (rows of
+    // tens of entries, which one thread would walk alone)
+    Arr<LO> cnt(nkeys);
+    auto ct = view(cnt);
+    group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+      if (k < 0) return;
+      LO v = kv[k], n2 = 0;
+      for (LO x = va[v] + gl; x < va[v + 1]; x += 32) n2 += !dd[vb[x]];
+      n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
+      if (gl == 0) ct[k] = n2;
+    });
+    k2ps[d] = offset_scan(cnt);
+  }
+  {
+    std::vector<ModifyPlan*> pls;
+    std::vector<const Arr<LO>*> kps;
+    for (int d = 0; d <= dim; ++d) {
+      plans[d] = plan_modify(m, d, VERT, k2v, k2ps[d]);
+      pls.push_back(&plans[d]);
+      kps.push_back(&k2ps[d]);
+    }
+    plan_sizes(pls, kps);
+  }
   for (int d = 0; d <= dim; ++d) {
-    Arr<LO> k2p, pv2v, kd2d;
-    if (d == VERT) {
-      k2p = fill<LO>(nkeys + 1, 0);
-    } else {
-      // find_coarsen_domains: live d-entities around each key vertex
+    const Arr<LO>& k2p = k2ps[d];
+    Arr<LO> pv2v, kd2d;
+    if (d != VERT) {
       const Adj& v2d = m.ask_up(0, d);
       auto va = cview(v2d.a2ab);
       auto vb = cview(v2d.ab2b);
       auto vcd = cview(v2d.codes);
       auto dd = cview(dead[d]);
       auto kv = cview(k2v);
-      // one warp per key: the lanes stride the key vertex's row (rows of
-      // tens of entries, which one thread would walk alone)
-      Arr<LO> cnt(nkeys);
-      auto ct = view(cnt);
-      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
-        if (k < 0) return;
-        LO v = kv[k], n2 = 0;
-        for (LO x = va[v] + gl; x < va[v + 1]; x += 32) n2 += !dd[vb[x]];
-        n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
-        if (gl == 0) ct[k] = n2;
-      });
-      k2p = offset_scan(cnt);
-      LO nprod = last(k2p);
+      LO nprod = plans[d].sizes[2];
       kd2d = Arr<LO>(nprod);
       int nccv = d + 1;
       pv2v = Arr<LO>(nprod * nccv);
@@ -2398,7 +2518,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
         }
       });
     }
-    ModifyOut mo = modify_ents_adapt(m, nm, d, VERT, k2v, k2p, pv2v, old_lows2new);
+    ModifyOut mo = apply_modify(m, nm, d, VERT, plans[d], k2v, k2p, pv2v, old_lows2new);
     LO nnew = nm.nents[d];
     if (d == VERT) ov2nv = mo.old2new;
     xfer_class(m, nm, d, mo, nnew, nullptr, nullptr, kd2d.data());
@@ -2445,6 +2565,24 @@ bool coarsen_slivers(Mesh& m, const AdaptOpts& o, PassStats* st) {
 enum { SW_NMESH, SW_NTRI, SW_NUTRI, SW_NEDGE, SW_NUEDGE, SW_OTRI, SW_OMESH, SW_OUEDGE, SW_OE2U };
 constexpr int kSwapHdr = 8 * 9;
 constexpr int kMaxUniqTris = 35, kMaxUniqEdges = 26;
+
+// the largest product counts of one key over the 3..7-gons: edges,
+// triangles and tets (npe, npt + 2 npe, 2 npt)
+static void swap3d_max_products(int out[4]) {
+  out[0] = 0;
+  out[1] = out[2] = out[3] = 0;
+  int p = 0;
+  while (p < OHG_SWAP3D_TABLE_LEN) {
+    int nm = OHG_SWAP3D_TABLE[p + 1], nt = OHG_SWAP3D_TABLE[p + 2],
+        nu = OHG_SWAP3D_TABLE[p + 3];
+    p += 4 + nu * 3 + nm * nt;
+    int ne = OHG_SWAP3D_TABLE[p], nue = OHG_SWAP3D_TABLE[p + 1];
+    p += 2 + nue * 2 + nm * ne;
+    out[1] = std::max(out[1], ne);
+    out[2] = std::max(out[2], nt + 2 * ne);
+    out[3] = std::max(out[3], 2 * nt);
+  }
+}
 
 static View<const int> swap_tables() {
   Ctx& c = ctx();
@@ -3049,12 +3187,23 @@ static Arr<LO> swap_keys(Mesh& m, Arr<LO> c2e, Arr<double> cq, PassStats* st) {
       kp[i] = q[i] > old;
     });
   }
-  Arr<LO> kept = collect_marked(keep);
-  if (kept.size() == 0) return Arr<LO>(0);
-  c2e = unmap(kept, c2e, 1);
-  cq = unmap(kept, cq, 1);
-  Arr<I8> is_cand = mark_image(c2e, ne);
-  Arr<double> edge_q = map_onto(cq, c2e, ne, -1.0, 1);
+  // the improving candidates marked on the edges directly (no compaction
+  // and no host wait: without any, the independent set is empty)
+  Arr<I8> is_cand = fill<I8>(ne, 0);
+  Arr<double> edge_q = fill<double>(ne, -1.0);
+  {
+    auto ce = cview(c2e);
+    auto q = cview(cq);
+    auto kp = cview(keep);
+    auto ic = view(is_cand);
+    auto eq = view(edge_q);
+    pfor(nc, [=] __device__(LO i) {
+      if (kp[i]) {
+        ic[ce[i]] = 1;
+        eq[ce[i]] = q[i];
+      }
+    });
+  }
   Arr<I8> keys = find_indset(m, EDGE, edge_q, is_cand);
   Arr<LO> k2e = collect_marked(keys);
   st->swap_keys = k2e.size();
@@ -3063,7 +3212,8 @@ static Arr<LO> swap_keys(Mesh& m, Arr<LO> c2e, Arr<double> cq, PassStats* st) {
 
 // modify + transfer_swap: every product inherits the key edge's
 // classification; lengths and qualities of products are re-measured
-static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2v) {
+static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2v,
+                         bool check_rings) {
   int dim = m.dim;
   LO nkeys = k2e.size();
   Mesh nm;
@@ -3078,8 +3228,24 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
   nm.class_dim[0] = m.class_dim[0];
   nm.class_id[0] = m.class_id[0];
   Arr<LO> old_lows2new = iota(m.nverts());
+  // every dimension's plan, then one wait for their sizes and the status
+  // word (an invalid edge ring raised ST_TOPOLOGY while the products were
+  // written)
+  ModifyPlan plans[4];
+  {
+    std::vector<ModifyPlan*> pls;
+    std::vector<const Arr<LO>*> kps;
+    for (int d = 1; d <= dim; ++d) {
+      plans[d] = plan_modify(m, d, EDGE, k2e, k2p[d]);
+      pls.push_back(&plans[d]);
+      kps.push_back(&k2p[d]);
+    }
+    int status = 0;
+    plan_sizes(pls, kps, &status);
+    if (check_rings && (status & ST_TOPOLOGY)) throw Error(10, "edge swap found an invalid edge ring");
+  }
   for (int d = 1; d <= dim; ++d) {
-    ModifyOut mo = modify_ents_adapt(m, nm, d, EDGE, k2e, k2p[d], pv2v[d], old_lows2new);
+    ModifyOut mo = apply_modify(m, nm, d, EDGE, plans[d], k2e, k2p[d], pv2v[d], old_lows2new);
     LO nnew = nm.nents[d];
     LO np = mo.prods2new.size();
     Arr<I8> pcd(np);
@@ -3148,7 +3314,7 @@ static bool swap_edges_2d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2
       }
     });
   }
-  swap_rebuild(m, k2e, k2p, pv2v);
+  swap_rebuild(m, k2e, k2p, pv2v, false);
   return true;
 }
 
@@ -3183,9 +3349,15 @@ static bool swap_edges_3d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2
       c3[k] = 2 * npt;
     });
   }
+  // products' vertices sized by the tables' largest product counts per key
+  // (no host wait; the exact counts come with the rebuild's sizes)
+  int maxp[4];
+  swap3d_max_products(maxp);
   for (int d = 1; d <= 3; ++d) {
     k2p[d] = offset_scan(cnt[d]);
-    pv2v[d] = Arr<LO>(last(k2p[d]) * (d + 1));
+    long long cap = (long long)nkeys * maxp[d] * (d + 1);
+    if (cap > 0x7fffffffLL) throw Error(8, "edge swap: too many products");
+    pv2v[d] = Arr<LO>(LO(cap));
   }
   {
     auto ls = cview(lsize);
@@ -3248,8 +3420,7 @@ static bool swap_edges_3d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2
       }
     });
   }
-  if (ctx().take_status() & ST_TOPOLOGY) throw Error(10, "edge swap found an invalid edge ring");
-  swap_rebuild(m, k2e, k2p, pv2v);
+  swap_rebuild(m, k2e, k2p, pv2v, true);
   return true;
 }
 

@@ -38,7 +38,7 @@ void coarsen_qualities(Mesh& m, const LO* c2e, LO n, const I8* codes, double* ou
 // FP32 enclosures of the FP64 quality of arbitrary vertex 4-tuples and of
 // the FP64 metric length of vertex pairs, with the FP64 values (3D)
 void screen_tets(Mesh& m, const LO* tv2v, LO n, float* lo, float* hi, double* exact);
-void screen_tets_face(Mesh& m, const LO* tv2v, LO n, int slot, float* lo, float* hi,
+void screen_tets_face(Mesh& m, const LO* tv2v, LO n, int slot, bool cubed, float* lo, float* hi,
                       double* exact);
 void screen_edges(Mesh& m, const LO* ev2v, LO n, float* lo, float* hi, double* exact);
 void choose_rails(Mesh& m, const LO* c2e, LO n, const I8* codes, const double* quals2,

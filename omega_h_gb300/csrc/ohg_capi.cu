@@ -819,11 +819,12 @@ int ohg_screen_tet_qualities(ohg_mesh* m, const int* tv2v, int n, float* lo, flo
   MESH_GUARD(m);
   return guarded(m->owner, [&] { screen_tets(m->mesh, tv2v, n, lo, hi, exact); });
 }
-int ohg_screen_tet_qualities_face(ohg_mesh* m, const int* tv2v, int n, int slot, float* lo,
-                                  float* hi, double* exact) {
+int ohg_screen_tet_qualities_face(ohg_mesh* m, const int* tv2v, int n, int slot, int cubed,
+                                  float* lo, float* hi, double* exact) {
   MESH_GUARD(m);
   if (n < 0 || slot < 0 || slot > 3) return OHG_ERR_INVALID;
-  return guarded(m->owner, [&] { screen_tets_face(m->mesh, tv2v, n, slot, lo, hi, exact); });
+  return guarded(m->owner,
+                 [&] { screen_tets_face(m->mesh, tv2v, n, slot, cubed != 0, lo, hi, exact); });
 }
 int ohg_screen_edge_lengths(ohg_mesh* m, const int* ev2v, int n, float* lo, float* hi,
                             double* exact) {

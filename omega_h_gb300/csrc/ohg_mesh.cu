@@ -524,7 +524,7 @@ static Adj edges_across_tris(const Adj& f2e, const Adj& e2f, LO ne) {
   pfor(ne, [=] __device__(LO e) { dg[e] = 2 * (ea[e + 1] - ea[e]); });
   g.a2ab = offset_scan(deg);
   g.has_a2ab = true;
-  g.ab2b = Arr<LO>(last(g.a2ab));
+  g.ab2b = Arr<LO>(2 * e2f.ab2b.size());  // two edges per (edge, triangle) use
   auto ga = cview(g.a2ab);
   auto ef = cview(e2f.ab2b);
   auto efc = cview(e2f.codes);
@@ -564,7 +564,7 @@ static Adj add_edges(const Adj& g1, const Adj& g2, LO nv) {
   pfor(nv, [=] __device__(LO v) { dg[v] = (a1[v + 1] - a1[v]) + (a2[v + 1] - a2[v]); });
   g.a2ab = offset_scan(deg);
   g.has_a2ab = true;
-  g.ab2b = Arr<LO>(last(g.a2ab));
+  g.ab2b = Arr<LO>(g1.ab2b.size() + g2.ab2b.size());
   auto ga = cview(g.a2ab);
   auto b1 = cview(g1.ab2b);
   auto b2 = cview(g2.ab2b);

@@ -639,7 +639,8 @@ LO last(const Arr<LO>& a, const char* file, int line) {
   return c.h_pinned[0];
 }
 
-void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out, const char* file, int line) {
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out, int* status, const char* file,
+                int line) {
   Ctx& c = ctx();
   int n = int(arrs.size());
   if (n > kPinnedStatusSlot) throw Error(8, "read_lasts: too many arrays");
@@ -650,6 +651,7 @@ void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out, const char* fi
   c.sync(file, line);
   check_no_stall(c);
   for (int i = 0; i < n; ++i) out[i] = c.h_pinned[i];
+  if (status) *status = c.h_pinned[kPinnedStatusSlot];
 }
 
 Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt) {
@@ -667,18 +669,34 @@ Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt) {
 // indices of the nonzero marks in increasing order: one compaction launch
 // and one read of the count; the result keeps its n-slot buffer
 Arr<LO> collect_marked(const Arr<I8>& marks, const char* file, int line) {
+  return collect_marked(marks, nullptr, nullptr, file, line);
+}
+Arr<LO> collect_marked(const Arr<I8>& marks, const int* extra_dev, int* extra_host,
+                       const char* file, int line) {
   LO n = marks.size();
-  if (n == 0) return Arr<LO>(0);
   Ctx& c = ctx();
+  if (n == 0) {
+    if (extra_dev) {
+      OHG_CUDA(cudaMemcpyAsync(c.h_pinned + 1, extra_dev, sizeof(int), cudaMemcpyDeviceToHost,
+                               c.stream));
+      c.sync(file, line);
+      *extra_host = c.h_pinned[1];
+    }
+    return Arr<LO>(0);
+  }
   Arr<LO> out(n);
   Arr<unsigned long long> st;
   LO* cnt = nullptr;
   launch_lookback<I8, true>(marks.data(), n, out.data(), st, &cnt);
   OHG_CUDA(cudaMemcpyAsync(c.h_pinned, cnt, sizeof(LO), cudaMemcpyDeviceToHost, c.stream));
+  if (extra_dev)
+    OHG_CUDA(cudaMemcpyAsync(c.h_pinned + 1, extra_dev, sizeof(int), cudaMemcpyDeviceToHost,
+                             c.stream));
   queue_status_read(c);
   c.sync(file, line);
   check_no_stall(c);
   out.n = c.h_pinned[0];
+  if (extra_dev) *extra_host = c.h_pinned[1];
   return out;
 }
 LO count_marked(const Arr<I8>& marks, const char* file, int line) {

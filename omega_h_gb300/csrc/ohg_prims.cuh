@@ -27,6 +27,9 @@ void scan_wait_limit_selftest(const LO* counts, LO n, LO* out);
 // indices of nonzero marks (collect_marked, src/Omega_h_map.cpp:174-185)
 Arr<LO> collect_marked(const Arr<I8>& marks, const char* file = __builtin_FILE(),
                        int line = __builtin_LINE());
+// the same, with *extra_host = *extra_dev read in the same wait
+Arr<LO> collect_marked(const Arr<I8>& marks, const int* extra_dev, int* extra_host,
+                       const char* file = __builtin_FILE(), int line = __builtin_LINE());
 LO count_marked(const Arr<I8>& marks, const char* file = __builtin_FILE(),
                 int line = __builtin_LINE());
 
@@ -34,7 +37,9 @@ LO last(const Arr<LO>& a, const char* file = __builtin_FILE(), int line = __buil
 // FP64 fused multiply-add throughput of the device (GFLOP/s, best of reps)
 double fp64_peak_gflops(int reps);
 // the last element of each array (at most 16) with one host wait
-void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out,
+// (status, if given, receives the device status word read in the same wait;
+// it is not cleared)
+void read_lasts(const std::vector<const Arr<LO>*>& arrs, LO* out, int* status = nullptr,
                 const char* file = __builtin_FILE(), int line = __builtin_LINE());
 // indices of nonzero marks given offset_scan of the 0/1 marks and its total
 Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt);

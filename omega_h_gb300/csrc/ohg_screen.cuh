@@ -238,8 +238,6 @@ __device__ __forceinline__ int maxdet_vertex(const ScreenView& s, const LO vv[4]
   return best;
 }
 
-// Interval of the double tet quality (tet_quality on the maxdet metric), from
-// the four vertices' coordinate pairs and the maxdet vertex's metric record.
 // Running sums over a tet's edges v (float) with error bounds e for the mean
 // squared metric length: G = sum v v^T, H = the off-diagonal of sum |v||v|^T,
 // W = sum e |v| and sum e^2.  Each entry is a sum of at most six products,
@@ -266,10 +264,18 @@ struct GramAcc {
   }
 };
 
-// The quality interval from the triple product T (six times the signed
-// volume, against the double T by at most eT) and the edge sums of G.
-__device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc& G, float4 ma,
-                                               float4 mb) {
+// The parts of a tet quality interval from the triple product T (six times
+// the signed volume, against the double T by at most eT) and the edge sums
+// of G: the size s = T/6 sqrt(det M) within es, the mean squared length msl
+// within [msl_lo, msl_hi], and y = (s / s_equilateral)^2 within ey.  The
+// return value says which case holds: 0 the parts are valid (s settled
+// non-negative), 1 unbounded, 2 the size is surely negative (the quality is
+// s itself: [s_lo, s_hi]), 3 the size's sign is not settled.
+struct TetTail {
+  float sv, es, msl_lo, msl_hi, y, ey;
+};
+__device__ __forceinline__ int tet_tail_parts(float T, float eT, const GramAcc& G, float4 ma,
+                                              float4 mb, TetTail& o) {
   // rs = T / 6 (here T times float(1/6): one more rounding, so kC2), s = rs * sqrt(det M)
   float rs = __fmul_rn(T, kSixth);
   float ers = __fmaf_rn(fabsf(rs), kC2, __fmul_rn(eT, kSixthUp));
@@ -277,8 +283,10 @@ __device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc&
   float sv = __fmul_rn(rs, sd);
   float es = __fmaf_rn(fabsf(sv), kC2, __fmul_rn(__fmul_rn(ers, fabsf(sd)), 1.0f + 0x1p-20f));
   es = __fmul_rn(es, kInflate);
-  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return widen_all();
-  if (__fadd_ru(sv, es) < 0.0f) return {__fsub_rd(sv, es), __fadd_ru(sv, es)};  // negative size
+  o.sv = sv;
+  o.es = es;
+  if (!(fabsf(sv) <= FLT_MAX) || !(es <= FLT_MAX)) return 1;
+  if (__fadd_ru(sv, es) < 0.0f) return 2;  // negative size
   float s_lo = __fsub_rd(sv, es);
   // mean squared metric length: the sum over the six edges of v^T M v is
   // the contraction M : G with G = sum v v^T.  Its float evaluation differs
@@ -308,25 +316,37 @@ __device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc&
                          __fmul_rn(__fmaf_rn(12.2f * kU, asum, __fadd_rn(pert, 16.0f * kTiny)),
                                    kSixthUp));
   emsl = __fmul_rn(emsl, kInflate);
-  float msl_lo = __fsub_rd(msl, emsl), msl_hi = __fadd_ru(msl, emsl);
+  o.msl_lo = __fsub_rd(msl, emsl);
+  o.msl_hi = __fadd_ru(msl, emsl);
   // the range keeps __fdividef within its documented 2-ulp error
-  if (!(msl_lo > 1e-30f) || !(msl_hi < 1e30f)) return widen_all();
-  if (s_lo < 0.0f) {
-    // sign of the size not settled: the value is either s (>= s_lo) or a
-    // non-negative quality
-    return {s_lo, INFINITY};
-  }
+  if (!(o.msl_lo > 1e-30f) || !(o.msl_hi < 1e30f)) return 1;
+  if (s_lo < 0.0f) return 3;
   // x = s / 0.1178511301977579, y = x * x
   float x = __fmul_rn(sv, 8.485281374238571f);
   float ex = __fmaf_rn(fabsf(x), kC2, __fmul_rn(es, 8.4853f));
   float y = __fmul_rn(x, x);
   float ey = __fmaf_rn(fabsf(y), kC1, __fmul_rn(ex, __fmaf_rn(2.0f, fabsf(x), ex)));
-  ey = __fmul_rn(ey, kInflate);
+  o.y = y;
+  o.ey = __fmul_rn(ey, kInflate);
+  if (!(y < 1e30f) || !(o.ey < 1e30f)) return 1;  // keeps __fdividef in range
+  return 0;
+}
+
+// The quality interval: q = cbrt(y) / msl.
+__device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc& G, float4 ma,
+                                               float4 mb) {
+  TetTail t;
+  int c = tet_tail_parts(T, eT, G, ma, mb, t);
+  if (c == 1) return widen_all();
+  if (c == 2) return {__fsub_rd(t.sv, t.es), __fadd_ru(t.sv, t.es)};
+  // sign of the size not settled: the value is either s (>= s_lo) or a
+  // non-negative quality
+  if (c == 3) return {__fsub_rd(t.sv, t.es), INFINITY};
+  float y = t.y, ey = t.ey;
   // cbrt over [y - ey, y + ey] from one cbrtf (at most 1 ulp; the double
   // cbrt is correctly rounded): with d = ey / y,
   //   (1 + d)^(1/3) <= 1 + d/3 and (1 - d)^(1/3) >= 1 - d/3 - d^2 (d <= 1/2)
   float r_lo, r_hi;
-  if (!(y < 1e30f) || !(ey < 1e30f)) return widen_all();  // keeps __fdividef in range
   if (!(y > 1e-30f)) {
     r_lo = 0.0f;
     r_hi = __fmul_ru(cbrtf(__fadd_ru(fmaxf(y, 0.0f), ey)), 1.0f + 0x1p-20f);
@@ -342,8 +362,33 @@ __device__ __forceinline__ FIv tet_bounds_tail(float T, float eT, const GramAcc&
     }
   }
   // q = r / msl; __fdividef is within 2 ulp for divisors in [2^-126, 2^126]
-  FIv q = {__fmul_rd(__fdividef(r_lo, msl_hi), 1.0f - 0x1p-21f),
-           __fmul_ru(__fdividef(r_hi, msl_lo), 1.0f + 0x1p-21f)};
+  FIv q = {__fmul_rd(__fdividef(r_lo, t.msl_hi), 1.0f - 0x1p-21f),
+           __fmul_ru(__fdividef(r_hi, t.msl_lo), 1.0f + 0x1p-21f)};
+  if (!finite_iv(q)) return widen_all();
+  return q;
+}
+
+// The cube of the quality interval, without a cube root: q^3 = y / msl^3
+// is monotone in q, so minima and comparisons with a threshold's cube carry
+// over.  The double quality is fl(cbrt(Y) / M) with Y the double y and M the
+// double msl (correctly rounded cbrt, rounded division: within 2 u_double of
+// cbrt(Y) / M), so its cube lies within (1 +- 6.1 u_double) of Y / M^3;
+// [y_lo, y_hi] holds Y and [msl_lo, msl_hi] holds M.  The float quotient
+// (__fdividef, 2 ulp, divisor kept in [1e-30, 1e30]) is widened by 2^-20.
+// A surely negative size gives [-inf, 0] (the quality is negative); an
+// unsettled sign [-inf, inf].
+__device__ __forceinline__ FIv tet_bounds_tail_cubed(float T, float eT, const GramAcc& G,
+                                                     float4 ma, float4 mb) {
+  TetTail t;
+  int c = tet_tail_parts(T, eT, G, ma, mb, t);
+  if (c == 1 || c == 3) return widen_all();
+  if (c == 2) return {-INFINITY, 0.0f};
+  if (!(t.msl_lo > 1e-10f) || !(t.msl_hi < 1e10f)) return widen_all();
+  float y_lo = fmaxf(__fsub_rd(t.y, t.ey), 0.0f), y_hi = __fadd_ru(t.y, t.ey);
+  float m3_hi = __fmul_ru(__fmul_ru(t.msl_hi, t.msl_hi), t.msl_hi);
+  float m3_lo = __fmul_rd(__fmul_rd(t.msl_lo, t.msl_lo), t.msl_lo);
+  FIv q = {__fmul_rd(__fdividef(y_lo, m3_hi), 1.0f - 0x1p-20f),
+           __fmul_ru(__fdividef(y_hi, m3_lo), 1.0f + 0x1p-20f)};
   if (!finite_iv(q)) return widen_all();
   return q;
 }
@@ -477,8 +522,9 @@ __device__ __forceinline__ TetFaceInv tet_face_invariants(const float4 h[3], con
 }
 
 // Interval of the double quality of the tet that puts p at the slot the
-// invariants were made for; hf/lf the face vertices in slot order, ma/mb the
-// metric record of the new tet's maxdet vertex.
+// invariants were made for (cubed: of its cube); hf/lf the face vertices in
+// slot order, ma/mb the metric record of the new tet's maxdet vertex.
+template <bool cubed>
 __device__ __forceinline__ FIv tet_face_bounds(const TetFaceInv& f, const float4 hf[3],
                                                const float4 lf[3], float4 hp, float4 lp,
                                                float4 ma, float4 mb) {
@@ -515,7 +561,7 @@ __device__ __forceinline__ FIv tet_face_bounds(const TetFaceInv& f, const float4
   G.add(d0, e0);
   G.add(d1, e1);
   G.add(d2, e2);
-  return tet_bounds_tail(T, eT, G, ma, mb);
+  return cubed ? tet_bounds_tail_cubed(T, eT, G, ma, mb) : tet_bounds_tail(T, eT, G, ma, mb);
 }
 
 __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {

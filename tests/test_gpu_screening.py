@@ -112,21 +112,35 @@ def test_face_route_enclosures_contain_the_fp64_values(ctx, n, kind, seed):
     lo0, hi0, ex0 = _screen(m, "ohg_screen_tet_qualities", tets, 4)
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     nn = tets.shape[0]
-    for slot in range(4):
+    def face(slot, cubed):
         lo = torch.empty(nn, dtype=torch.float32, device="cuda")
         hi = torch.empty_like(lo)
         ex = torch.empty(nn, dtype=torch.float64, device="cuda")
-        _lib.call("ohg_screen_tet_qualities_face", m.handle, P(tets), nn, slot, P(lo), P(hi),
-                  P(ex))
+        _lib.call("ohg_screen_tet_qualities_face", m.handle, P(tets), nn, slot, int(cubed),
+                  P(lo), P(hi), P(ex))
         torch.cuda.synchronize()
-        lo, hi, ex = (lo.cpu().numpy().astype(np.float64), hi.cpu().numpy().astype(np.float64),
-                      ex.cpu().numpy())
+        return (lo.cpu().numpy().astype(np.float64), hi.cpu().numpy().astype(np.float64),
+                ex.cpu().numpy())
+
+    for slot in range(4):
+        lo, hi, ex = face(slot, False)
         assert np.array_equal(ex, ex0)
         _check_enclosure(lo, hi, ex, f"tet qualities, face route, slot {slot}")
         # no wider than a few times the direct route's interval
         fin = np.isfinite(lo) & np.isfinite(hi) & np.isfinite(lo0) & np.isfinite(hi0) & (ex > 0)
         r = (hi[fin] - lo[fin]) / np.maximum(hi0[fin] - lo0[fin], 1e-300)
         assert np.median(r) < 2.0
+        # the cube of the quality, as the 3D collapse screen takes it: the
+        # double cube of ex is within 2.1 u_double of the exact one
+        lo3, hi3, _ = face(slot, True)
+        c = ex ** 3
+        bad = ~((lo3 <= c * (1 + 4.7e-16 * np.sign(c))) & (c * (1 - 4.7e-16 * np.sign(c)) <= hi3))
+        assert not bad.any(), f"slot {slot}: {int(bad.sum())} cubes outside their interval"
+        # a settled negative size gives [-inf, 0], an unsettled sign or an
+        # unbounded case [-inf, inf]; a positive quality's cube is >= 0
+        neg, pos = ex < 0, ex > 0
+        assert ((hi3[neg] <= 0) | ~np.isfinite(hi3[neg])).all()
+        assert ((lo3[pos] >= 0) | ~np.isfinite(lo3[pos])).all()
     m.close()
 
 
