@@ -281,50 +281,91 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // once per decision; the reads of a row are independent (no early exit), so
 // their latencies overlap.  first: the state array has not been initialised
 // (all UNKNOWN), so a neighbour that is no candidate counts as NOT_IN.
+// Eight neighbours u[0..8) (-1: none) folded into a decision: their states,
+// then the qualities of the undecided ones, each group of loads issued
+// together.  first: the state array has not been initialised (all UNKNOWN),
+// so a neighbour that is no candidate counts as NOT_IN.
 template <bool first>
-__device__ __forceinline__ int indset_decide(LO v, const LO* __restrict__ xa,
-                                             const LO* __restrict__ xb,
-                                             const double* __restrict__ q,
-                                             const I8* __restrict__ cands, volatile I8* s) {
-  LO beg = xa[v], end = xa[v + 1];
-  double qv = q[v];
-  bool joined = false, top = true;
-  // eight neighbours at a time: their numbers, then their states, then the
-  // qualities of the undecided ones, each group of loads issued together
-  for (LO j = beg; j < end; j += 8) {
-    LO u[8];
-    int su[8];
+__device__ __forceinline__ void indset_fold(LO v, double qv, const LO u[8],
+                                            const double* __restrict__ q,
+                                            const I8* __restrict__ cands, volatile I8* s,
+                                            bool& joined, bool& top) {
+  int su[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) u[t] = j + t < end ? xb[j + t] : -1;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      su[t] = NOT_IN;
-      if (u[t] >= 0 && (!first || cands[u[t]])) su[t] = s[u[t]];
-    }
-    double qu[8];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) qu[t] = su[t] == UNKNOWN ? q[u[t]] : 0.0;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      if (su[t] == IN) joined = true;
-      else if (su[t] == UNKNOWN) top = top && ((qu[t] != qv) ? (qu[t] < qv) : (u[t] < v));
-    }
+  for (int t = 0; t < 8; ++t) {
+    su[t] = NOT_IN;
+    if (u[t] >= 0 && (!first || cands[u[t]])) su[t] = s[u[t]];
   }
-  return joined ? NOT_IN : (top ? IN : UNKNOWN);
+  double qu[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) qu[t] = su[t] == UNKNOWN ? q[u[t]] : 0.0;
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    if (su[t] == IN) joined = true;
+    else if (su[t] == UNKNOWN) top = top && ((qu[t] != qv) ? (qu[t] < qv) : (u[t] < v));
+  }
 }
+
+// A conflict graph given by rows (CSR)
+struct CsrGraph {
+  const LO* xa;
+  const LO* xb;
+  template <bool first>
+  __device__ __forceinline__ int decide(LO v, const double* __restrict__ q,
+                                        const I8* __restrict__ cands, volatile I8* s) const {
+    LO beg = xa[v], end = xa[v + 1];
+    double qv = q[v];
+    bool joined = false, top = true;
+    for (LO j = beg; j < end; j += 8) {
+      LO u[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) u[t] = j + t < end ? xb[j + t] : -1;
+      indset_fold<first>(v, qv, u, q, cands, s, joined, top);
+    }
+    return joined ? NOT_IN : (top ? IN : UNKNOWN);
+  }
+};
+
+// Edges that share an element (the star of an edge, src/Omega_h_star.cpp),
+// walked through the edge's elements and their edges: no graph is built.
+// An edge shared by several of the elements is read once per element, which
+// does not change a decision.
+struct EdgeStarGraph {
+  const LO* ea;   // edge -> element rows
+  const LO* eb;
+  const LO* le;   // element -> edges, nle per element
+  int nle;
+  template <bool first>
+  __device__ __forceinline__ int decide(LO v, const double* __restrict__ q,
+                                        const I8* __restrict__ cands, volatile I8* s) const {
+    LO beg = ea[v], end = ea[v + 1];
+    double qv = q[v];
+    bool joined = false, top = true;
+    for (LO x = beg; x < end; ++x) {
+      LO el = eb[x];
+      LO u[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        LO f = t < nle ? le[el * nle + t] : -1;
+        u[t] = f == v ? -1 : f;
+      }
+      indset_fold<first>(v, qv, u, q, cands, s, joined, top);
+    }
+    return joined ? NOT_IN : (top ? IN : UNKNOWN);
+  }
+};
 
 // The rounds before the sweep: one thread per vertex, plain launches, in
 // decreasing vertex order.  Among equal qualities the higher index ranks
 // first, so decisions spread from high to low indices; with threads in
 // decreasing order, a round's later blocks see what its earlier blocks
 // decided, and a chain of ties advances by more than one step per round.
-template <bool first>
-static void indset_round(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands,
+template <bool first, class G>
+static void indset_round(const G& g, LO n, const Arr<double>& quality, const Arr<I8>& cands,
                          I8* st) {
-  auto xa = g.a2ab.data();
-  auto xb = g.ab2b.data();
   auto q = quality.data();
   auto cd = cands.data();
+  G gr = g;
   pfor(n, [=] __device__(LO i) {
     LO v = n - 1 - i;
     volatile I8* s = st;
@@ -336,7 +377,7 @@ static void indset_round(const Adj& g, LO n, const Arr<double>& quality, const A
     } else if (s[v] != UNKNOWN) {
       return;
     }
-    int d = indset_decide<first>(v, xa, xb, q, cd, s);
+    int d = gr.template decide<first>(v, q, cd, s);
     if (d != UNKNOWN) s[v] = I8(d);
   });
 }
@@ -353,10 +394,10 @@ static void indset_round(const Adj& g, LO n, const Arr<double>& quality, const A
 // owner makes progress somewhere.  Threads without progress back off
 // briefly with __nanosleep.  sweeps_acc receives the largest sweep count of
 // any thread.
+template <class G>
 __global__ void __launch_bounds__(kIndsetBlock, 4)
-    k_indset_sweep(const LO* __restrict__ xa, const LO* __restrict__ xb,
-                   const double* __restrict__ q, const I8* __restrict__ cands, I8* st, LO n,
-                   int* status, int* sweeps_acc, unsigned* blocks_done, int* call_max) {
+    k_indset_sweep(G g, const double* __restrict__ q, const I8* __restrict__ cands, I8* st,
+                   LO n, int* status, int* sweeps_acc, unsigned* blocks_done, int* call_max) {
   volatile I8* s = st;
   LO stride = LO(gridDim.x) * kIndsetBlock;
   LO scan = LO(blockIdx.x) * kIndsetBlock + LO(threadIdx.x);  // next owned vertex to look at
@@ -386,7 +427,7 @@ __global__ void __launch_bounds__(kIndsetBlock, 4)
     int keep = 0;
     for (int i = 0; i < np; ++i) {
       LO v = pend[i];
-      int d = indset_decide<false>(v, xa, xb, q, cands, s);
+      int d = g.template decide<false>(v, q, cands, s);
       if (d == UNKNOWN) {
         pend[keep++] = v;
       } else {
@@ -423,7 +464,8 @@ __global__ void __launch_bounds__(kIndsetBlock, 4)
   }
 }
 
-Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands) {
+template <class G>
+static Arr<I8> find_indset_on(const G& g, LO n, const Arr<double>& quality, const Arr<I8>& cands) {
   Ctx& c = ctx();
   Arr<I8> a(n);
   if (n == 0) return a;
@@ -433,17 +475,16 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
   // blocks_done and the call's sweep maximum
   Arr<unsigned> scratch(2);
   OHG_CUDA(cudaMemsetAsync(scratch.data(), 0, 2 * sizeof(unsigned), c.stream));
-  static thread_local int per_sm = 0;  // per host thread: no locking
+  static thread_local int per_sm = 0;  // per host thread and graph type: no locking
   if (per_sm == 0) {
-    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_indset_sweep,
+    OHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_indset_sweep<G>,
                                                            kIndsetBlock, 0));
     if (per_sm < 1) per_sm = 1;
   }
   long long full = (long long)per_sm * c.num_sms;
   long long need = (n + kIndsetBlock - 1) / kIndsetBlock;
   unsigned blocks = unsigned(need < full ? need : full);
-  const LO* xa = g.a2ab.data();
-  const LO* xb = g.ab2b.data();
+  G gr = g;
   const double* q = quality.data();
   const I8* cd = cands.data();
   I8* st = a.data();
@@ -451,15 +492,27 @@ Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8
   int* acc = c.d_indset_sweeps;
   unsigned* done = scratch.data();
   int* cmax = reinterpret_cast<int*>(scratch.data() + 1);
-  void* args[] = {(void*)&xa, (void*)&xb, (void*)&q,      (void*)&cd,   (void*)&st,
-                  (void*)&n,  (void*)&status, (void*)&acc, (void*)&done, (void*)&cmax};
-  OHG_CUDA(cudaLaunchCooperativeKernel((const void*)k_indset_sweep, dim3(blocks),
+  void* args[] = {(void*)&gr, (void*)&q,      (void*)&cd,  (void*)&st,   (void*)&n,
+                  (void*)&status, (void*)&acc, (void*)&done, (void*)&cmax};
+  OHG_CUDA(cudaLaunchCooperativeKernel((const void*)k_indset_sweep<G>, dim3(blocks),
                                        dim3(kIndsetBlock), args, 0, c.stream));
   ++c.launches;
   return a;
 }
+
+Arr<I8> find_indset(const Adj& g, LO n, const Arr<double>& quality, const Arr<I8>& cands) {
+  return find_indset_on(CsrGraph{g.a2ab.data(), g.ab2b.data()}, n, quality, cands);
+}
 Arr<I8> find_indset(Mesh& m, int d, const Arr<double>& q, const Arr<I8>& cands) {
   if (d == m.dim) return cands;
+  if (d == EDGE) {
+    // edges sharing an element, walked through the elements: the edge graph
+    // (tens of entries per edge) is not built
+    const Adj& e2el = m.ask_up_any_order(EDGE, m.dim);  // membership only: row order is free
+    EdgeStarGraph g{e2el.a2ab.data(), e2el.ab2b.data(), m.ask_down(m.dim, EDGE).ab2b.data(),
+                    simplex_degree(m.dim, EDGE)};
+    return find_indset_on(g, m.nents[EDGE], q, cands);
+  }
   return find_indset(m.ask_adj(d, d), m.nents[d], q, cands);
 }
 
@@ -3097,15 +3150,36 @@ Arr<I8> mark_sliver_layers(Mesh& m, double ceil, int nlayers) {
     auto s = view(a);
     pfor(ne, [=] __device__(LO i) { s[i] = qq[i] < ceil; });
   }
-  const Adj& dual = m.ask_adj(m.dim, m.dim);
-  auto da = cview(dual.a2ab);
-  auto db = cview(dual.ab2b);
+  // the dual graph (elements across their sides) as a fixed-width table:
+  // the other element across each side of e, -1 on the boundary (a side of
+  // a simplicial mesh has at most two elements), so no sizes are read back
+  int nse = m.dim + 1;
+  Arr<LO> across(ne * nse);
+  {
+    auto es = cview(m.ask_down(m.dim, m.dim - 1).ab2b);
+    const Adj& s2e = m.ask_up_any_order(m.dim - 1, m.dim);  // a maximum: row order is free
+    auto sa = cview(s2e.a2ab);
+    auto sb = cview(s2e.ab2b);
+    auto ac = view(across);
+    pfor(ne, [=] __device__(LO e) {
+      for (int k = 0; k < nse; ++k) {
+        LO sd = es[e * nse + k], other = -1;
+        for (LO x = sa[sd]; x < sa[sd + 1]; ++x)
+          if (sb[x] != e) other = sb[x];
+        ac[e * nse + k] = other;
+      }
+    });
+  }
+  auto ac = cview(across);
   for (int l = 0; l < nlayers; ++l) {
     auto o = cview(a);
     auto nw = view(b);
     pfor(ne, [=] __device__(LO e) {
       int r = -128;
-      for (LO x = da[e]; x < da[e + 1]; ++x) r = max(r, int(o[db[x]]));
+      for (int k = 0; k < nse; ++k) {
+        LO f = ac[e * nse + k];
+        if (f >= 0) r = max(r, int(o[f]));
+      }
       nw[e] = I8(r);
     });
     std::swap(a, b);

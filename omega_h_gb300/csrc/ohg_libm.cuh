@@ -337,7 +337,8 @@ OHG_HD double exp_cr(double x) {
 // ------------------------------------------------------------ sin, cos
 // sin and cos of a double-double a with |a| <= pi/4 + 2^-7: a = c + t with
 // c = j/64 from the table and |t| <= 2^-7, then the addition formulas with
-// the Taylor series of sin t and cos t.
+// the Taylor series of sin t and cos t.  sn or cs may be null: only the
+// other one is formed.
 OHG_HD void sincos_dd(DD a, DD* sn, DD* cs) {
   bool neg = a.hi < 0.0;
   if (neg) a = dd_neg(a);
@@ -359,10 +360,29 @@ OHG_HD void sincos_dd(DD a, DD* sn, DD* cs) {
                                       dd_add(dd_mul(t4, inv24), DD{c6, 0.0})));
   DD S = {OHG_LIBM_TAB(sin_hi)[j], OHG_LIBM_TAB(sin_lo)[j]};
   DD C = {OHG_LIBM_TAB(cos_hi)[j], OHG_LIBM_TAB(cos_lo)[j]};
-  DD s_ = dd_add(dd_mul(S, ct), dd_mul(C, st));
-  DD c_ = dd_add(dd_mul(C, ct), dd_neg(dd_mul(S, st)));
-  *sn = neg ? dd_neg(s_) : s_;
-  *cs = c_;
+  if (sn) {
+    DD s_ = dd_add(dd_mul(S, ct), dd_mul(C, st));
+    *sn = neg ? dd_neg(s_) : s_;
+  }
+  if (cs) *cs = dd_add(dd_mul(C, ct), dd_neg(dd_mul(S, st)));
+}
+
+// sin and cos of a double w with |w| <= pi/4 + 2^-7 in plain double
+// arithmetic, the same table and series to degree 7: to a few units of
+// 2^-53, for Newton steps whose result is refined in double-double.
+OHG_HD void sincos_d(double w, double* sn, double* cs) {
+  bool neg = w < 0.0;
+  double a = neg ? -w : w;
+  int j = int(rint(a * 64.0));
+  j = j < 0 ? 0 : j > 51 ? 51 : j;
+  double t = a - double(j) * (1.0 / 64.0);  // exact
+  double t2 = t * t;
+  double st = fma(t * t2, fma(t2, fma(t2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), t);
+  double ct = fma(t2, fma(t2, fma(t2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+  double S = OHG_LIBM_TAB(sin_hi)[j], C = OHG_LIBM_TAB(cos_hi)[j];
+  double s_ = fma(S, ct, C * st);
+  *sn = neg ? -s_ : s_;
+  *cs = fma(C, ct, -(S * st));
 }
 
 // cos x, correctly rounded for |x| <= 2^20 (the reduction by multiples of
@@ -383,23 +403,28 @@ OHG_HD double cos_cr(double x) {
     r.lo = (r.lo - pm.lo) - kd * OHG_PIO2_LO;
     r = fast_two_sum(r.hi, r.lo);
   }
-  DD sn, cs;
-  sincos_dd(r, &sn, &cs);
   long long q = (long long)fmod(kd, 4.0);
-  DD v = q == 0 ? cs : q == 1 ? dd_neg(sn) : q == 2 ? dd_neg(cs) : sn;
+  DD v;
+  if (q & 1) {
+    sincos_dd(r, &v, nullptr);  // cos(r + k pi/2) = -+ sin r
+    if (q == 1) v = dd_neg(v);
+  } else {
+    sincos_dd(r, nullptr, &v);
+    if (q == 2) v = dd_neg(v);
+  }
   return v.hi + v.lo;
 }
 
 // asin z for |z| <= 0.5 + 2^-10 as a double-double: a series start refined
 // by Newton's iteration on sin w = z (cos w >= 0.85 there), twice in double
-// and once in double-double.
+// (sincos_d) and once in double-double.
 OHG_HD DD asin_dd_small(DD z) {
   double zh = z.hi, z2 = zh * zh;
   double w = zh * (1.0 + z2 * (1.0 / 6.0 + z2 * (3.0 / 40.0 + z2 * (15.0 / 336.0))));
   for (int it = 0; it < 2; ++it) {
-    DD sn, cs;
-    sincos_dd(DD{w, 0.0}, &sn, &cs);
-    w = w + (zh - sn.hi) / cs.hi;
+    double sn, cs;
+    sincos_d(w, &sn, &cs);
+    w = w + (zh - sn) / cs;
   }
   DD sn, cs;
   DD wd = {w, 0.0};
