@@ -1482,6 +1482,13 @@ struct CoarsenVertexArgs {
   // cubes of the threshold, rounded down and up (3D screens the cube of the
   // quality)
   float mqa3_dn, mqa3_up;
+  // prevent_coarsen_overshoot in the same kernel (overshoot): a direction
+  // whose new edges reach max_length gets q2 = -1 and is not screened
+  bool overshoot;
+  double max_length;
+  float ov_thr, ov_tdn;
+  RV c, mt;
+  int mc;
   unsigned long long* queue;  // [0] next vertex, [1] directions in the FP64 list
   LO* amb_dir;
   float* amb_mhi;
@@ -1531,6 +1538,10 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
   __shared__ int s_lo[kVsWarps][kVsMaxLocal], s_hi[kVsWarps][kVsMaxLocal];
   __shared__ unsigned char s_dk[kVsWarps][kVsMaxLocal];  // local indices of the directions
   __shared__ unsigned s_elem[kVsWarps][kMaxE];     // NV local indices, 8 bits each
+  // per local vertex: which end of its edge with v is v (the new edge to the
+  // vertex moved onto keeps the edge's orientation), and whether the
+  // direction onto it overshoots
+  __shared__ unsigned char s_end[kVsWarps][kVsMaxLocal], s_over[kVsWarps][kVsMaxLocal];
   const unsigned full = 0xffffffffu;
   const int w = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31u);
   unsigned nscreen = 0;
@@ -1585,6 +1596,8 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
         s_key[w][k] = a.sv.dkey[u];
         s_lo[w][k] = fkey(1.0f);
         s_hi[w][k] = fkey(1.0f);
+        s_end[w][k] = k > 0 ? (unsigned char)code_which_down(a.ec[e0 + k - 1]) : 0;
+        s_over[w][k] = 0;
       }
       __syncwarp();
       bool found = true;
@@ -1644,6 +1657,45 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
             v_onto = a.ev[e * 2 + (1 - col)];
           }
         }
+        if (d >= 0 && a.overshoot) {
+          // prevent_coarsen_overshoot for this direction, as the separate
+          // kernel decides it
+          LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
+          unsigned nl = 0, nx = 0;
+          for (LO x = e0; x < e0 + ne; ++x) {
+            LO e2 = a.eb[x];
+            int ein = code_which_down(a.ec[x]), eout = 1 - ein;
+            LO nv[2];
+            nv[ein] = v_onto;
+            nv[eout] = a.ev[e2 * 2 + eout];
+            if (nv[eout] == v_onto) continue;  // the collapsing edge
+            float qlo[2], qhi[2];
+            bool qok = edge_q_bounds_d(D, a.sv, nv[0], nv[1], qlo, qhi);
+            int side = len_cut_side(qlo, qhi, qok, cut);
+            ++nl;
+            bool over;
+            if (side != 0) {
+              over = side > 0;
+            } else {
+              FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+              if (L.lo >= a.ov_thr) {
+                over = true;
+              } else if (L.hi < a.ov_thr) {
+                over = false;
+              } else {
+                over = edge_len_v(D, a.c, a.mt, a.mc, nv[0], nv[1]) >= a.max_length;
+                ++nx;
+              }
+            }
+            if (over) {
+              a.q2[d] = -1.0;
+              d = -1;
+              break;
+            }
+          }
+          atomicAdd(&a.cnt[2], (unsigned long long)nl);
+          if (nx) atomicAdd(&a.cnt[3], (unsigned long long)nx);
+        }
         if (d >= 0) {
           float lo = 1.0f, hi = 1.0f;
           for (LO x = s0; x < s0 + S && !(hi < a.mqa_f); ++x) {
@@ -1681,6 +1733,49 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
     // schedule.  The warp scans the pairs 32 at a time and queues the ones
     // to screen in shared memory (ballot compaction); it screens 32 queued
     // pairs at a time, one per lane.
+    if (a.overshoot) {
+      // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49):
+      // the new edges from each direction's vertex moved onto to v's other
+      // neighbours, (direction, neighbour) pairs over the lanes; a direction
+      // with a new edge at or above max_length does not collapse.  Its
+      // outcome does not depend on which over-long edge is found first.
+      const LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
+      const int npo = nd * ne;
+      const float rne = 1.0f / float(ne);
+      unsigned nl = 0, nx = 0;
+      for (int p = lane; p < npo; p += 32) {
+        int t = int((float(p) + 0.5f) * rne);  // p / ne: exact for p < 2^12, ne <= 31
+        int wl = p - t * ne + 1;
+        int k = s_dk[w][t];
+        if (wl == k || s_over[w][k]) continue;
+        // the new edge keeps the orientation of v's edge to wl, with k for v
+        int ein = s_end[w][wl];
+        int ia = ein == 0 ? k : wl, ib = ein == 0 ? wl : k;
+        float qlo[2], qhi[2];
+        bool qok = edge_q_bounds_rec<D>(s_h[w][ia], s_l[w][ia], s_ma[w][ia], s_mb[w][ia],
+                                        s_h[w][ib], s_l[w][ib], s_ma[w][ib], s_mb[w][ib], qlo, qhi);
+        int side = len_cut_side(qlo, qhi, qok, cut);
+        ++nl;
+        bool over;
+        if (side != 0) {
+          over = side > 0;
+        } else {
+          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+          if (L.lo >= a.ov_thr) {
+            over = true;
+          } else if (L.hi < a.ov_thr) {
+            over = false;
+          } else {
+            over = edge_len_v(D, a.c, a.mt, a.mc, s_gid[w][ia], s_gid[w][ib]) >= a.max_length;
+            ++nx;
+          }
+        }
+        if (over) s_over[w][k] = 1;
+      }
+      warp_count_full(&a.cnt[2], nl);
+      warp_count_full(&a.cnt[3], nx);
+      __syncwarp();
+    }
     constexpr bool cubed = D == 3;
     const float fail_below = cubed ? a.mqa3_dn : a.mqa_f;
     const int npairs = S * nd;
@@ -1696,7 +1791,7 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
           t = p - x * nd;
           int k = s_dk[w][t];
           take = __vcmpeq4(s_elem[w][x], unsigned(k) * 0x01010101u) == 0u &&  // not v_onto's
-                 !(fkey_inv(s_hi[w][k]) < fail_below);
+                 !s_over[w][k] && !(fkey_inv(s_hi[w][k]) < fail_below);
         }
         unsigned m = __ballot_sync(full, take);
         if (take) s_q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)(x * 32 + t);
@@ -1766,8 +1861,13 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
       __syncwarp();
     }
     for (LO k = 1 + lane; k <= ne; k += 32) {
-      if (s_dir[w][k] >= 0)
-        screen_outcome(a, s_dir[w][k], fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]), cubed);
+      LO d = s_dir[w][k];
+      if (d < 0) continue;
+      if (s_over[w][k]) {
+        a.q2[d] = -1.0;  // overshoots: does not collapse
+      } else {
+        screen_outcome(a, d, fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]), cubed);
+      }
     }
     __syncwarp();
   }
@@ -1914,7 +2014,7 @@ void prevent_coarsen_overshoot(Mesh& m, double max_length, const LO* c2e_p, LO n
 // choose_rails_lazy needs it).
 template <int D>
 static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,
-                                  double* q2_p) {
+                                  double* q2_p, double max_length) {
   constexpr int dim = D;
   const VertScreen& vs = mesh_screen(m);
   auto sv = screen_view(vs);
@@ -1962,11 +2062,14 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   int var = cx.tuner.select("coarsen_screen_v", D, nV, 2, 0, cx.stream);
   bool timed = cx.tuner.open >= 0;
   int block = kVsBlock, chunk = (var & 1) ? 4 : 8;
+  bool overshoot = max_length >= 0.0;
+  float ov_thr = overshoot ? float_at_or_above(max_length) : 0.0f;
+  float ov_tdn = overshoot ? float_at_or_below(max_length) : 0.0f;
   CoarsenVertexArgs args{nV,   chunk, sv,   ev,   cv,
                          va,   vb,    cview(v2e.a2ab), cview(v2e.ab2b), vc,
                          cview(v2e.codes), cview(e2cand), cview(codes_p, n), q2, mqa_f,
-                         mqa3_dn, mqa3_up, queue.data(), amb_dir.data(), amb_mhi.data(),
-                         &cnt[0]};
+                         mqa3_dn, mqa3_up, overshoot, max_length, ov_thr, ov_tdn, c, mt,
+                         m.mcomp(), queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
   bytes += double(nE) * 4 + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
   {
     KernelTimer timer("coarsen_filter", bytes);
@@ -2075,12 +2178,15 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
     codes[cand] = code;
   });
 }
+// max_length >= 0: prevent_coarsen_overshoot with that limit in the same
+// kernel, before the quality screen (a direction that overshoots gets
+// q2 = -1 and loses its collapse bit)
 static void coarsen_filter_lazy(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, double mqa,
-                                double* q2_p) {
+                                double* q2_p, double max_length = -1.0) {
   if (m.dim == 3)
-    coarsen_filter_lazy_d<3>(m, c2e_p, n, codes_p, mqa, q2_p);
+    coarsen_filter_lazy_d<3>(m, c2e_p, n, codes_p, mqa, q2_p, max_length);
   else
-    coarsen_filter_lazy_d<2>(m, c2e_p, n, codes_p, mqa, q2_p);
+    coarsen_filter_lazy_d<2>(m, c2e_p, n, codes_p, mqa, q2_p, max_length);
 }
 
 // FP64 minima min(1, cavity qualities) of K collapse cavities (v_col[k] onto
@@ -2356,8 +2462,14 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   }
   Arr<I8> codes2(c2e.size());
   check_collapse_exposure(m, c2e.data(), c2e.size(), codes.data(), codes2.data());
-  prevent_coarsen_overshoot(m, allowed ? o.max_length_allowed : o.max_length_desired, c2e.data(),
-                            c2e.size(), codes2.data(), codes.data());
+  // with screening, prevent_coarsen_overshoot runs inside the quality
+  // screen (it stages the same neighbours); otherwise here
+  bool lazy = ctx().screening && !improve;
+  double max_len = allowed ? o.max_length_allowed : o.max_length_desired;
+  if (lazy)
+    codes = codes2;
+  else
+    prevent_coarsen_overshoot(m, max_len, c2e.data(), c2e.size(), codes2.data(), codes.data());
   int passed_class = 0;
   {
     Arr<LO> keep = collect_marked(codes, any_class.data(), &passed_class);
@@ -2368,9 +2480,9 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
-  bool lazy = ctx().screening && !improve;
   if (lazy) {
-    coarsen_filter_lazy(m, c2e.data(), nc, codes.data(), o.min_quality_allowed, q2.data());
+    coarsen_filter_lazy(m, c2e.data(), nc, codes.data(), o.min_quality_allowed, q2.data(),
+                        max_len);
   } else {
     coarsen_qualities(m, c2e.data(), nc, codes.data(), q2.data());
     // the worst element quality at each vertex now (graph_reduce MIN)

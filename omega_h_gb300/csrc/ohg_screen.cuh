@@ -819,6 +819,43 @@ __device__ __forceinline__ bool edge_q_bounds_d(int dim, const ScreenView& s, LO
   return dim == 3 ? edge_q_bounds3(s, a, b, lo, hi) : edge_q_bounds2(s, a, b, lo, hi);
 }
 
+// edge_q_bounds3 / edge_q_bounds2 from the two ends' records (coordinate
+// pairs and metric records, end a first): the same operations
+template <int D>
+__device__ __forceinline__ bool edge_q_bounds_rec(float4 ha, float4 la, float4 maa, float4 mba,
+                                                  float4 hb, float4 lb, float4 mab, float4 mbb,
+                                                  float lo[2], float hi[2]) {
+  bool ok = true;
+  if constexpr (D == 3) {
+    float v[3];
+    float e = sdiff3(hb, lb, ha, la, v);  // p1 - p0 with p0 = a
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      float4 ma = k == 0 ? maa : mab, mb = k == 0 ? mba : mbb;
+      float A, S1;
+      float q = mprod(ma, mb, v, A, S1);
+      float qe = __fmul_rn(mprod_err(A, S1, mb.z, e), kInflate);
+      lo[k] = __fsub_rd(q, qe);
+      hi[k] = __fadd_ru(q, qe);
+      ok = ok && lo[k] > 0.0f && hi[k] <= FLT_MAX;
+    }
+  } else {
+    float v[2];
+    float e = sdiff2(hb, lb, ha, la, v);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      float4 ma = k == 0 ? maa : mab;
+      float A, S1;
+      float q = mprod2(ma, v, A, S1);
+      float qe = __fmul_rn(mprod2_err(A, S1, ma.w, e), kInflate);
+      lo[k] = __fsub_rd(q, qe);
+      hi[k] = __fadd_ru(q, qe);
+      ok = ok && lo[k] > 0.0f && hi[k] <= FLT_MAX;
+    }
+  }
+  return ok;
+}
+
 // builds the per-vertex screening data of a mesh of dimension dim
 VertScreen build_vert_screen(const Arr<double>& coords, const Arr<double>& metric, LO nverts,
                              int dim = 3);
