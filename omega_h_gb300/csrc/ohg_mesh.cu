@@ -165,21 +165,24 @@ Adj invert_adj(const Adj& down, int k, LO nlows, bool sorted) {
   Arr<LO> deg = fill<LO>(nlows, 0);
   auto hl2l = cview(down.ab2b);
   auto dg = view(deg);
-  pfor(nhl, [=] __device__(LO hl) { atomicAdd(&dg[hl2l[hl]], 1); });
+  // each use's rank within its row is the count's atomic return value, kept
+  // for the fill (one round of atomics instead of two)
+  Arr<LO> rank(nhl);
+  auto rk = view(rank);
+  pfor(nhl, [=] __device__(LO hl) { rk[hl] = atomicAdd(&dg[hl2l[hl]], 1); });
   Adj up;
   up.a2ab = offset_scan(deg);
   up.has_a2ab = true;
   up.ab2b = Arr<LO>(nhl);
   up.codes = Arr<I8>(nhl);
   up.has_codes = true;
-  // slots by atomics; each slot holds the use index hl and the use's down
-  // code (flip, rotation) packed as hl * 8 + code, read here where the
-  // reads of the down arrays are coalesced
-  // (beyond 2^28 uses the key is hl alone and the code is read afterwards)
+  // each slot holds the use index hl and the use's down code (flip,
+  // rotation) packed as hl * 8 + code, read here where the reads of the down
+  // arrays are coalesced (beyond 2^28 uses the key is hl alone and the code
+  // is read afterwards)
   bool packed = nhl < (1 << 28);
-  Arr<LO> pos = fill<LO>(nlows, 0);
   auto off = cview(up.a2ab);
-  auto ps = view(pos);
+  auto rc = cview(rank);
   auto lh2hl = view(up.ab2b);
   bool has_dc = down.has_codes;
   auto dc = cview(down.codes);
@@ -189,7 +192,7 @@ Adj invert_adj(const Adj& down, int k, LO nlows, bool sorted) {
     pfor(nhl, [=] __device__(LO hl) {
       LO l = hl2l[hl];
       int c = has_dc ? int(dc[hl] & 7) : 0;
-      LO j = off[l] + atomicAdd(&ps[l], 1);
+      LO j = off[l] + rc[hl];
       lh2hl[j] = hl / k;
       uc[j] = make_code(c & 1, (c >> 1) & 3, hl % k);
     });
@@ -198,7 +201,7 @@ Adj invert_adj(const Adj& down, int k, LO nlows, bool sorted) {
   pfor(nhl, [=] __device__(LO hl) {
     LO l = hl2l[hl];
     LO c = has_dc ? LO(dc[hl] & 7) : 0;
-    lh2hl[off[l] + atomicAdd(&ps[l], 1)] = packed ? hl * 8 + c : hl;
+    lh2hl[off[l] + rc[hl]] = packed ? hl * 8 + c : hl;
   });
   // rows sorted by high entity (sort_by_high_index)
   sort_rows_by_high(nlows, up.a2ab, up.ab2b, up.codes, k,
