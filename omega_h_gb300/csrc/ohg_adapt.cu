@@ -2515,8 +2515,13 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       cd[i] = code;
     });
   }
-  filter_cands(c2e, codes, &q2);
-  if (c2e.size() == 0) return false;
+  // choose_rails_lazy skips candidates whose directions all failed (code
+  // 0), so with screening the list is not compacted here (no host wait); a
+  // pass where none survives then finds no key below
+  if (!lazy) {
+    filter_cands(c2e, codes, &q2);
+    if (c2e.size() == 0) return false;
+  }
   LO nv = m.nverts();
   Arr<I8> vc(nv);
   Arr<double> vq(nv);
@@ -2530,6 +2535,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Arr<I8> vkeys = find_indset(m, VERT, vq, vc);
   Arr<LO> k2v = collect_marked(vkeys);
   LO nkeys = k2v.size();
+  if (nkeys == 0) return false;  // no candidate survived (the set of any is not empty)
   st->coarsen_keys = nkeys;
   // find_rails (src/Omega_h_collapse_rail.cpp:79-108) and the vertices onto
   Arr<LO> r2e(nkeys);
@@ -2913,8 +2919,12 @@ void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO
 //     hold its minimum: those triangles are evaluated in FP64;
 //  3. the FP64 minima of those triangulations give the reference's choice
 //     and quality, the first one winning ties.
+// improving_only (the pass): a candidate whose best triangulation's upper
+// bound is below the worst current quality around its edge cannot pass
+// filter_swap_improve; it gets quality -DBL_MAX and no FP64 work.
 static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, LO n,
-                                      double* quals_p, I8* configs_p) {
+                                      double* quals_p, I8* configs_p,
+                                      bool improving_only = false) {
   int mc = m.mcomp();  // metric components per vertex (1: isotropic)
   auto tab = swap_tables();
   Arr<int> lsize;
@@ -2973,18 +2983,50 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
       int size = ls[i];
       unsigned ns = 0;
       {
+        // the triangle's two tets (t0, t1, t2, end 1) and (t0, t2, t1, end 0)
+        // share the face opposite slot 3: its invariants once, the second
+        // tet's normal the first's negated (its face edges in swapped order);
+        // the bounds are of the cube of the quality, a monotone scale for
+        // every comparison below
         int otri = tab[size * 9 + SW_OTRI];
-        LO tet[4];
-        for (int k = 0; k < 3; ++k) tet[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+        LO f[3];
+        for (int k = 0; k < 3; ++k) f[k] = lv[i * 7 + tab[otri + u * 3 + k]];
+        float4 hf[3] = {sv.xh[f[0]], sv.xh[f[1]], sv.xh[f[2]]};
+        float4 lf[3] = {sv.xl[f[0]], sv.xl[f[1]], sv.xl[f[2]]};
+        long long k0 = sv.dkey[f[0]], k1 = sv.dkey[f[1]], k2 = sv.dkey[f[2]];
+        TetFaceInv inv = tet_face_invariants(hf, lf, 3);
         float lo = 1.0f, hi = 1.0f;
         for (int tt = 0; tt < 2; ++tt) {
-          tet[3] = le[i * 2 + (1 - tt)];
-          FIv b = tet_quality_bounds(sv, tet);
+          LO pv = le[i * 2 + (1 - tt)];
+          // maxdet in slot order: (f0, f1, f2, p) or (f0, f2, f1, p)
+          LO sa = f[0], sb = tt == 0 ? f[1] : f[2], sc = tt == 0 ? f[2] : f[1];
+          long long ka = k0, kb = tt == 0 ? k1 : k2, kc = tt == 0 ? k2 : k1, kp = sv.dkey[pv];
+          LO best = sa;
+          long long bk = ka;
+          if (kb > bk) {
+            best = sb;
+            bk = kb;
+          }
+          if (kc > bk) {
+            best = sc;
+            bk = kc;
+          }
+          if (kp > bk) best = pv;
+          FIv b;
+          if (tt == 0) {
+            b = tet_face_bounds<true>(inv, hf, lf, sv.xh[pv], sv.xl[pv], sv.ma[best],
+                                      sv.mb[best]);
+          } else {
+            TetFaceInv neg = inv;
+            neg.a.x = -inv.a.x;
+            neg.a.y = -inv.a.y;
+            neg.a.z = -inv.a.z;
+            float4 hs[3] = {hf[0], hf[2], hf[1]}, ls2[3] = {lf[0], lf[2], lf[1]};
+            b = tet_face_bounds<true>(neg, hs, ls2, sv.xh[pv], sv.xl[pv], sv.ma[best],
+                                      sv.mb[best]);
+          }
           lo = fminf(lo, b.lo);
           hi = fminf(hi, b.hi);
-          LO sw = tet[1];
-          tet[1] = tet[2];
-          tet[2] = sw;
         }
         tb[idx] = make_float2(lo, hi);
         ns = 2;
@@ -3034,6 +3076,31 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   }
   auto tb = cview(tbnd);
   auto ov = cview(over);
+  // the cube of the worst current quality around each candidate edge,
+  // rounded down (improving_only)
+  Arr<float> old3;
+  if (improving_only) {
+    old3 = Arr<float>(n);
+    auto o3 = view(old3);
+    auto eq = cview(m.ask_qualities());
+    const Adj& e2t = m.ask_up_any_order(1, 3);  // a minimum: row order is free
+    auto ea = cview(e2t.a2ab);
+    auto eb = cview(e2t.ab2b);
+    auto ce = cview(c2e_p, n);
+    pfor(n, [=] __device__(LO i) {
+      LO e = ce[i];
+      double old = DBL_MAX;
+      for (LO x = ea[e]; x < ea[e + 1]; ++x) old = min2d(old, eq[eb[x]]);
+      // largest float at or below old, then its cube rounded down: for a
+      // negative old the cube is negative and no candidate is skipped
+      float f = float(old);
+      if (double(f) > old) f = nextafterf(f, -INFINITY);
+      float c3 = f > 0.0f ? __fmul_rd(__fmul_rd(f, f), f) : -INFINITY;
+      o3[i] = old >= DBL_MAX ? -INFINITY : c3;
+    });
+  }
+  auto o3 = cview(old3);
+  bool improving = improving_only;
   {
     auto nd = view(need);
     auto lst = view(lstar);
@@ -3059,6 +3126,7 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
         L = fmaxf(L, mlo);
       }
       unsigned long long mask = 0;
+      float best_hi = -INFINITY;
       for (int mesh = 0; mesh < nmeshes; ++mesh) {
         bool valid = true;
         for (int e = 0; e < nedges; ++e)
@@ -3068,10 +3136,17 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
         for (int t = 0; t < ntris; ++t)
           mhi = fminf(mhi, tb[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]].y);
         if (!(mhi >= L && mhi > 0.0f)) continue;
+        best_hi = fmaxf(best_hi, mhi);
         for (int t = 0; t < ntris; ++t) {
           int u = tab[omsh + mesh * ntris + t];
           if (tb[i * kMaxUniqTris + u].x <= mhi) mask |= 1ull << u;
         }
+      }
+      // cannot beat the worst current quality: no FP64 work (L = +inf
+      // marks it for the selection below)
+      if (improving && best_hi < o3[i]) {
+        mask = 0;
+        L = INFINITY;
       }
       nd[i] = mask;
       lst[i] = L;
@@ -3137,6 +3212,11 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     int nmeshes = h[SW_NMESH], ntris = h[SW_NTRI], nedges = h[SW_NEDGE];
     int omsh = h[SW_OMESH], oe2u = h[SW_OE2U];
     float L = lst[i];
+    if (L == INFINITY) {  // cannot improve (improving_only)
+      configs[i] = -1;
+      quals[i] = -DBL_MAX;
+      return;
+    }
     for (int mesh = 0; mesh < nmeshes; ++mesh) {
       bool valid = true;
       for (int e = 0; e < nedges; ++e)
@@ -3509,7 +3589,11 @@ static bool swap_edges_3d(Mesh& m, const AdaptOpts& o, PassStats* st, Arr<LO> c2
   LO nc = c2e.size();
   Arr<double> cq(nc);
   Arr<I8> cc(nc);
-  swap3d_qualities(m, o.max_length_allowed, c2e.data(), nc, cq.data(), cc.data());
+  if (ctx().screening)
+    swap3d_qualities_screened(m, o.max_length_allowed, c2e.data(), nc, cq.data(), cc.data(),
+                              true);
+  else
+    swap3d_qualities(m, o.max_length_allowed, c2e.data(), nc, cq.data(), cc.data());
   LO ne = m.nedges();
   Arr<I8> econfig = map_onto(cc, c2e, ne, I8(-1), 1);
   Arr<LO> k2e = swap_keys(m, c2e, cq, st);
