@@ -653,17 +653,22 @@ static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>&
         }
       });
     } else if (ent_dim > key_dim) {
-      const Adj& up = om.ask_up(key_dim, ent_dim);
+      // the first entry of an upward row sorted by high entity is the row's
+      // smallest entity: its minimum over the row in any order, so the rows
+      // need no sort for this
+      const Adj& up = om.ask_up_any_order(key_dim, ent_dim);
       auto ua = cview(up.a2ab);
       auto ub = cview(up.ab2b);
       int* stw = ctx().d_status;
       pfor(nkeys, [=] __device__(LO k) {
-        LO b = ua[kd[k]];
-        if (b == ua[kd[k] + 1]) {
+        LO b = ua[kd[k]], e = ua[kd[k] + 1];
+        if (b == e) {
           raise_status(stw, ST_TOPOLOGY);
           r[k] = 0;
         } else {
-          r[k] = ub[b];
+          LO mn = ub[b];
+          for (LO x = b + 1; x < e; ++x) mn = min(mn, ub[x]);
+          r[k] = mn;
         }
       });
     } else {
@@ -892,7 +897,11 @@ static void xfer_class(Mesh& om, Mesh& nm, int d, const ModifyOut& mo, LO nnew, 
   nm.class_id[d] = ci;
 }
 
-static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& mo) {
+// pv2v: the products' vertex tuples in the new numbering, if at hand (the
+// products' qualities are then measured from them, without deriving the new
+// mesh's element-to-vertex list)
+static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& mo,
+                                   const Arr<LO>* pv2v = nullptr) {
   LO np = mo.prods2new.size();
   if (d == EDGE && om.has_length) {
     Arr<double> pl(np);
@@ -902,7 +911,10 @@ static void xfer_lengths_qualities(Mesh& om, Mesh& nm, int d, const ModifyOut& m
   }
   if (d == om.dim && om.has_quality) {
     Arr<double> pq(np);
-    measure_qualities(nm, mo.prods2new.data(), np, pq.data());
+    if (pv2v && pv2v->size() >= np * (d + 1))
+      measure_qualities_tuples(nm, pv2v->data(), np, pq.data());
+    else
+      measure_qualities(nm, mo.prods2new.data(), np, pq.data());
     nm.quality = xfer(om.quality, mo, nm.nents[d], pq, 1);
     nm.has_quality = true;
   }
@@ -1175,7 +1187,7 @@ static bool refine(Mesh& m, const AdaptOpts& o, const Arr<LO>& c2e, PassStats* s
       mident_metrics(m, k2e.data(), nkeys, pm.data());
       nm.metric = xfer(m.metric, mo, nnew, pm, mc);
     }
-    xfer_lengths_qualities(m, nm, d, mo);
+    xfer_lengths_qualities(m, nm, d, mo, &pv2v);
     old_lows2new = mo.old2new;
   }
   m = std::move(nm);
@@ -1733,49 +1745,6 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
     // schedule.  The warp scans the pairs 32 at a time and queues the ones
     // to screen in shared memory (ballot compaction); it screens 32 queued
     // pairs at a time, one per lane.
-    if (a.overshoot) {
-      // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49):
-      // the new edges from each direction's vertex moved onto to v's other
-      // neighbours, (direction, neighbour) pairs over the lanes; a direction
-      // with a new edge at or above max_length does not collapse.  Its
-      // outcome does not depend on which over-long edge is found first.
-      const LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
-      const int npo = nd * ne;
-      const float rne = 1.0f / float(ne);
-      unsigned nl = 0, nx = 0;
-      for (int p = lane; p < npo; p += 32) {
-        int t = int((float(p) + 0.5f) * rne);  // p / ne: exact for p < 2^12, ne <= 31
-        int wl = p - t * ne + 1;
-        int k = s_dk[w][t];
-        if (wl == k || s_over[w][k]) continue;
-        // the new edge keeps the orientation of v's edge to wl, with k for v
-        int ein = s_end[w][wl];
-        int ia = ein == 0 ? k : wl, ib = ein == 0 ? wl : k;
-        float qlo[2], qhi[2];
-        bool qok = edge_q_bounds_rec<D>(s_h[w][ia], s_l[w][ia], s_ma[w][ia], s_mb[w][ia],
-                                        s_h[w][ib], s_l[w][ib], s_ma[w][ib], s_mb[w][ib], qlo, qhi);
-        int side = len_cut_side(qlo, qhi, qok, cut);
-        ++nl;
-        bool over;
-        if (side != 0) {
-          over = side > 0;
-        } else {
-          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
-          if (L.lo >= a.ov_thr) {
-            over = true;
-          } else if (L.hi < a.ov_thr) {
-            over = false;
-          } else {
-            over = edge_len_v(D, a.c, a.mt, a.mc, s_gid[w][ia], s_gid[w][ib]) >= a.max_length;
-            ++nx;
-          }
-        }
-        if (over) s_over[w][k] = 1;
-      }
-      warp_count_full(&a.cnt[2], nl);
-      warp_count_full(&a.cnt[3], nx);
-      __syncwarp();
-    }
     constexpr bool cubed = D == 3;
     const float fail_below = cubed ? a.mqa3_dn : a.mqa_f;
     const int npairs = S * nd;
@@ -1791,7 +1760,7 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
           t = p - x * nd;
           int k = s_dk[w][t];
           take = __vcmpeq4(s_elem[w][x], unsigned(k) * 0x01010101u) == 0u &&  // not v_onto's
-                 !s_over[w][k] && !(fkey_inv(s_hi[w][k]) < fail_below);
+                 !(fkey_inv(s_hi[w][k]) < fail_below);
         }
         unsigned m = __ballot_sync(full, take);
         if (take) s_q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)(x * 32 + t);
@@ -1858,6 +1827,53 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
       __syncwarp();
       if (lane < rest) s_q[w][lane] = mv;
       qn = rest;
+      __syncwarp();
+    }
+    if (a.overshoot) {
+      // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
+      // for the directions the quality screen has not failed: the new edges
+      // from each direction's vertex moved onto to v's other neighbours,
+      // (direction, neighbour) pairs over the lanes; a direction with a new
+      // edge at or above max_length does not collapse.  The two checks are
+      // both required of a direction, so either order gives the same
+      // decisions; this order skips the edges of the many directions that
+      // fail on quality.  Its outcome does not depend on which over-long
+      // edge is found first.
+      const LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
+      const int npo = nd * ne;
+      const float rne = 1.0f / float(ne);
+      unsigned nl = 0, nx = 0;
+      for (int p = lane; p < npo; p += 32) {
+        int t = int((float(p) + 0.5f) * rne);  // p / ne: exact for p < 2^12, ne <= 31
+        int wl = p - t * ne + 1;
+        int k = s_dk[w][t];
+        if (wl == k || s_over[w][k] || fkey_inv(s_hi[w][k]) < fail_below) continue;
+        // the new edge keeps the orientation of v's edge to wl, with k for v
+        int ein = s_end[w][wl];
+        int ia = ein == 0 ? k : wl, ib = ein == 0 ? wl : k;
+        float qlo[2], qhi[2];
+        bool qok = edge_q_bounds_rec<D>(s_h[w][ia], s_l[w][ia], s_ma[w][ia], s_mb[w][ia],
+                                        s_h[w][ib], s_l[w][ib], s_ma[w][ib], s_mb[w][ib], qlo, qhi);
+        int side = len_cut_side(qlo, qhi, qok, cut);
+        ++nl;
+        bool over;
+        if (side != 0) {
+          over = side > 0;
+        } else {
+          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+          if (L.lo >= a.ov_thr) {
+            over = true;
+          } else if (L.hi < a.ov_thr) {
+            over = false;
+          } else {
+            over = edge_len_v(D, a.c, a.mt, a.mc, s_gid[w][ia], s_gid[w][ib]) >= a.max_length;
+            ++nx;
+          }
+        }
+        if (over) s_over[w][k] = 1;
+      }
+      warp_count_full(&a.cnt[2], nl);
+      warp_count_full(&a.cnt[3], nx);
       __syncwarp();
     }
     for (LO k = 1 + lane; k <= ne; k += 32) {
@@ -2697,7 +2713,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       nm.coords = xfer(m.coords, mo, nnew, Arr<double>(), dim);
       nm.metric = xfer(m.metric, mo, nnew, Arr<double>(), m.mcomp());
     }
-    xfer_lengths_qualities(m, nm, d, mo);
+    xfer_lengths_qualities(m, nm, d, mo, &pv2v);
     old_lows2new = mo.old2new;
   }
   m = std::move(nm);
@@ -3531,7 +3547,7 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
       });
     }
     xfer_class(m, nm, d, mo, nnew, pcd.data(), pci.data(), nullptr);
-    xfer_lengths_qualities(m, nm, d, mo);
+    xfer_lengths_qualities(m, nm, d, mo, &pv2v[d]);
     old_lows2new = mo.old2new;
   }
   m = std::move(nm);

@@ -1204,6 +1204,31 @@ void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out) {
   });
 }
 
+// measure_qualities of na elements given by their vertex tuples (dim + 1
+// each, in the element's own order): a rebuild's products, whose tuples are
+// the rows the new mesh's element-to-vertex list would give them
+void measure_qualities_tuples(Mesh& m, const LO* tuples, LO na, double* out) {
+  int dim = m.dim, mc = m.mcomp();
+  auto tv = cview(tuples, na * (dim + 1));
+  auto c = cview(m.coords);
+  auto mt = cview(m.metric);
+  auto o = view(out, na);
+  if (dim == 3 && na > 0) {
+    const VertScreen& vs = mesh_screen(m);
+    auto sv = screen_view(vs);
+    pfor(na, [=] __device__(LO a) {
+      LO v[4] = {tv[a * 4], tv[a * 4 + 1], tv[a * 4 + 2], tv[a * 4 + 3]};
+      o[a] = tet_quality_exact(sv, c, mt, v);
+    });
+    return;
+  }
+  pfor(na, [=] __device__(LO a) {
+    LO v[4];
+    for (int k = 0; k <= dim; ++k) v[k] = tv[a * (dim + 1) + k];
+    o[a] = elem_quality_dev(dim, mc, c, mt, v);
+  });
+}
+
 // get_mident_metrics (src/Omega_h_metric.cpp:56-104) for edges
 void mident_metrics(Mesh& m, const LO* edges, LO n, double* out) {
   auto ev = cview(m.ask_verts_of(1));

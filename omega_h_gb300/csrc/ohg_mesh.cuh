@@ -105,6 +105,8 @@ bool zlib_available();
 // measurement kernels
 void measure_edges_metric(Mesh& m, const LO* a2e, LO na, double* out);
 void measure_qualities(Mesh& m, const LO* a2e, LO na, double* out);
+// the same for elements given by vertex tuples (dim + 1 each)
+void measure_qualities_tuples(Mesh& m, const LO* tuples, LO na, double* out);
 void mident_metrics(Mesh& m, const LO* edges, LO n, double* out);
 
 }  // namespace ohg
