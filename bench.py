@@ -42,7 +42,7 @@ AUTOTUNE_PASSES = 4
 # vertices taken 8 at a time, 912 blocks of 128 threads),
 # profiles/coarsen_filter_box64_shock.md; to be captured again whenever that
 # kernel changes
-DOMINANT_TRAFFIC = 123762944 + 17990912
+DOMINANT_TRAFFIC = 123543296 + 18275584
 # FP64 add, multiply and fused multiply-add thread instructions per launch of
 # the FP64 output kernels on the 64^3 shock box, all edges / all tets (ncu:
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), for their
