@@ -2229,26 +2229,39 @@ static void collapse_minima_exact_d(Mesh& m, const ScreenView& sv, const Arr<LO>
   Arr<float> mhi(K);
   Arr<LO> cnt(K);
   {
+    // kCavityLanes lanes per cavity; in 3D the bounds are of the cube of
+    // the quality (no cube root), a monotone scale for the selection
+    // lo <= min hi below
     auto lo = view(lo_at);
     auto mh = view(mhi);
     auto ct = view(cnt);
-    pfor(K, [=] __device__(LO k) {
+    constexpr int G = kCavityLanes;
+    group_for(G, K, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+      if (k < 0) return;
       LO v = vcv[k], onto = vov[k];
+      LO x0 = ta[v], x1 = ta[v + 1];
       float min_hi = 1.0f;
-      for (LO x = ta[v]; x < ta[v + 1]; ++x) {
+      for (LO x = x0 + gl; x < x1; x += G) {
         LO vv[4];
         if (!collapse_elem(cv, dim, tb[x], code_which_down(tc[x]), onto, vv)) {
           lo[x] = INFINITY;
           continue;
         }
-        FIv b = elem_quality_bounds(dim, sv, vv);
+        FIv b = D == 3 ? tet_quality_bounds<true>(sv, vv) : elem_quality_bounds(dim, sv, vv);
         lo[x] = b.lo;
         min_hi = fminf(min_hi, b.hi);
       }
+#pragma unroll
+      for (int j = G / 2; j > 0; j >>= 1) min_hi = fminf(min_hi, __shfl_xor_sync(gm, min_hi, j, G));
+      __syncwarp(gm);
       LO n = 0;
-      for (LO x = ta[v]; x < ta[v + 1]; ++x) n += lo[x] <= min_hi;
-      mh[k] = min_hi;
-      ct[k] = n;
+      for (LO x = x0 + gl; x < x1; x += G) n += lo[x] <= min_hi;
+#pragma unroll
+      for (int j = G / 2; j > 0; j >>= 1) n += __shfl_xor_sync(gm, n, j, G);
+      if (gl == 0) {
+        mh[k] = min_hi;
+        ct[k] = n;
+      }
     });
   }
   Arr<LO> offs = offset_scan(cnt);

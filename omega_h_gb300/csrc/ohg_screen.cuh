@@ -395,6 +395,7 @@ __device__ __forceinline__ FIv tet_bounds_tail_cubed(float T, float eT, const Gr
 
 // Interval of the double tet quality (tet_quality on the maxdet metric), from
 // the four vertices' coordinate pairs and the maxdet vertex's metric record.
+template <bool cubed = false>
 __device__ __forceinline__ FIv tet_quality_bounds_of(const float4 h[4], const float4 l[4],
                                                      float4 ma, float4 mb) {
   // the six edges in the reference's order; the third, -b1, has the same
@@ -445,7 +446,7 @@ __device__ __forceinline__ FIv tet_quality_bounds_of(const float4 h[4], const fl
   GramAcc G;
 #pragma unroll
   for (int i = 0; i < 6; ++i) G.add(ev[i], ee[i]);
-  return tet_bounds_tail(T, eT, G, ma, mb);
+  return cubed ? tet_bounds_tail_cubed(T, eT, G, ma, mb) : tet_bounds_tail(T, eT, G, ma, mb);
 }
 
 // The same interval for the tets of a collapse, with the parts that do not
@@ -564,6 +565,7 @@ __device__ __forceinline__ FIv tet_face_bounds(const TetFaceInv& f, const float4
   return cubed ? tet_bounds_tail_cubed(T, eT, G, ma, mb) : tet_bounds_tail(T, eT, G, ma, mb);
 }
 
+template <bool cubed = false>
 __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO vv[4]) {
   int mi = maxdet_vertex(s, vv);
   float4 h[4], l[4];
@@ -571,7 +573,7 @@ __device__ __forceinline__ FIv tet_quality_bounds(const ScreenView& s, const LO 
     h[i] = s.xh[vv[i]];
     l[i] = s.xl[vv[i]];
   }
-  return tet_quality_bounds_of(h, l, s.ma[vv[mi]], s.mb[vv[mi]]);
+  return tet_quality_bounds_of<cubed>(h, l, s.ma[vv[mi]], s.mb[vv[mi]]);
 }
 
 // The double tet quality with sqrt(det M) and the maxdet choice taken from
