@@ -1498,6 +1498,7 @@ struct CoarsenVertexArgs {
   // whose new edges reach max_length gets q2 = -1 and is not screened
   bool overshoot;
   double max_length;
+  RV elen;  // FP64 edge lengths (the rail choice's order)
   float ov_thr, ov_tdn;
   RV c, mt;
   int mc;
@@ -1554,6 +1555,9 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
   // vertex moved onto keeps the edge's orientation), and whether the
   // direction onto it overshoots
   __shared__ unsigned char s_end[kVsWarps][kVsMaxLocal], s_over[kVsWarps][kVsMaxLocal];
+  // direction index of each local vertex, and the current length group's
+  // directions (local indices)
+  __shared__ unsigned char s_dt[kVsWarps][kVsMaxLocal], s_gk[kVsWarps][kVsMaxLocal];
   const unsigned full = 0xffffffffu;
   const int w = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31u);
   unsigned nscreen = 0;
@@ -1731,7 +1735,11 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
       LO k = kb + lane;
       bool is = k <= ne && s_dir[w][k] >= 0;
       unsigned m = __ballot_sync(full, is);
-      if (is) s_dk[w][nd + __popc(m & ((1u << lane) - 1u))] = (unsigned char)k;
+      if (is) {
+        int t = nd + __popc(m & ((1u << lane) - 1u));
+        s_dk[w][t] = (unsigned char)k;
+        s_dt[w][k] = (unsigned char)t;
+      }
       nd += __popc(m);
     }
     __syncwarp();
@@ -1747,139 +1755,178 @@ __global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexA
     // pairs at a time, one per lane.
     constexpr bool cubed = D == 3;
     const float fail_below = cubed ? a.mqa3_dn : a.mqa_f;
-    const int npairs = S * nd;
-    const float rnd = 1.0f / float(nd);
-    int p0 = 0, qn = 0;
-    for (;;) {
-      while (qn < 32 && p0 < npairs) {
-        int p = p0 + lane;
-        bool take = false;
-        int x = 0, t = 0;
-        if (p < npairs) {
-          x = int((float(p) + 0.5f) * rnd);  // p / nd: exact for p < 2^12, nd <= 32
-          t = p - x * nd;
-          int k = s_dk[w][t];
-          take = __vcmpeq4(s_elem[w][x], unsigned(k) * 0x01010101u) == 0u &&  // not v_onto's
-                 !(fkey_inv(s_hi[w][k]) < fail_below);
-        }
-        unsigned m = __ballot_sync(full, take);
-        if (take) s_q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)(x * 32 + t);
-        qn += __popc(m);
-        p0 += 32;
-      }
-      if (qn == 0) break;
+    const float pass_from = cubed ? a.mqa3_up : a.mqa_f;
+    // choose_rails (src/Omega_h_collapse_rail.cpp:19-77) takes at each vertex
+    // the shortest edge whose collapse passes (ties by quality), so the
+    // directions are screened in groups of equal length, shortest first:
+    // once a group holds a direction that surely passes (its lower bound
+    // clears the threshold and it does not overshoot), no longer direction
+    // can be the rail, and those are not screened (q2 = -1: they do not
+    // collapse, which leaves the rail choice as it is).  A group whose
+    // directions only straddle the threshold does not end the search: their
+    // FP64 minima decide later.
+    // The first two groups go one at a time and the rest together: each
+    // round costs its own pass over the star, and the search ends within
+    // the first two groups at most vertices.
+    double mylen = INFINITY;
+    if (lane < nd) mylen = a.elen[a.eb[e0 + s_dk[w][lane] - 1]];
+    unsigned todo = nd >= 32 ? full : ((1u << nd) - 1u), skipped = 0u;
+    for (int round = 0; todo; ++round) {
+      double ml = ((todo >> lane) & 1u) ? mylen : INFINITY;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ml = fmin(ml, __shfl_xor_sync(full, ml, o));
+      const unsigned grp =
+          round < 2 ? __ballot_sync(full, ((todo >> lane) & 1u) && mylen == ml) : todo;
+      todo &= ~grp;
+      const int ng = __popc(grp);
+      if ((grp >> lane) & 1u) s_gk[w][__popc(grp & ((1u << lane) - 1u))] = s_dk[w][lane];
       __syncwarp();
-      const int nq = qn < 32 ? qn : 32;
-      if (lane < nq) {
-        unsigned qe = s_q[w][lane];
-        int x = int(qe >> 5), t = int(qe & 31u);
-        int k = s_dk[w][t];
-        if (!(fkey_inv(s_hi[w][k]) < fail_below)) {
-          unsigned packed = s_elem[w][x];
-          FIv b;
-          if constexpr (D == 3) {
-            // the face's vertices in slot order, the vertex moved onto at the
-            // collapsing vertex's slot; maxdet as in slot order: the face's
-            // first maximum against k, k first on a tie if its slot comes first
-            unsigned sl = s_slot[w][x];
-            int pos = int(sl & 15u), fb = int(sl >> 4);
-            int j0 = pos == 0 ? 1 : 0, j1 = pos <= 1 ? 2 : 1, j2 = pos <= 2 ? 3 : 2;
-            int f0 = int((packed >> (8 * j0)) & 255u), f1 = int((packed >> (8 * j1)) & 255u),
-                f2 = int((packed >> (8 * j2)) & 255u);
-            float4 hf[3] = {s_h[w][f0], s_h[w][f1], s_h[w][f2]};
-            float4 lf[3] = {s_l[w][f0], s_l[w][f1], s_l[w][f2]};
-            int lfb = int((packed >> (8 * fb)) & 255u);
-            long long kf = s_key[w][lfb], kp = s_key[w][k];
-            int best = (kp > kf || (kp == kf && pos < fb)) ? k : lfb;
-            b = tet_face_bounds<true>(s_inv[w][x], hf, lf, s_h[w][k], s_l[w][k], s_ma[w][best],
-                                      s_mb[w][best]);
-          } else {
-            int li[NV];
-            for (int jj = 0; jj < NV; ++jj) {
-              li[jj] = int((packed >> (8 * jj)) & 255u);
-              if (li[jj] == 0) li[jj] = k;  // v_col moved onto v_onto
-            }
-            int best = 0;
-            long long bk = s_key[w][li[0]];
-            for (int jj = 1; jj < NV; ++jj) {
-              long long kk = s_key[w][li[jj]];
-              if (kk > bk) {
-                best = jj;
-                bk = kk;
+      const int npairs = S * ng;
+      const float rnd = 1.0f / float(ng);
+      int p0 = 0, qn = 0;
+      for (;;) {
+        while (qn < 32 && p0 < npairs) {
+          int p = p0 + lane;
+          bool take = false;
+          int x = 0, t = 0;
+          if (p < npairs) {
+            x = int((float(p) + 0.5f) * rnd);  // p / ng: exact for p < 2^12, ng <= 32
+            t = p - x * ng;
+            int k = s_gk[w][t];
+            take = __vcmpeq4(s_elem[w][x], unsigned(k) * 0x01010101u) == 0u &&  // not v_onto's
+                   !(fkey_inv(s_hi[w][k]) < fail_below);
+          }
+          unsigned m = __ballot_sync(full, take);
+          if (take) s_q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)(x * 32 + t);
+          qn += __popc(m);
+          p0 += 32;
+        }
+        if (qn == 0) break;
+        __syncwarp();
+        const int nq = qn < 32 ? qn : 32;
+        if (lane < nq) {
+          unsigned qe = s_q[w][lane];
+          int x = int(qe >> 5), t = int(qe & 31u);
+          int k = s_gk[w][t];
+          if (!(fkey_inv(s_hi[w][k]) < fail_below)) {
+            unsigned packed = s_elem[w][x];
+            FIv b;
+            if constexpr (D == 3) {
+              // the face's vertices in slot order, the vertex moved onto at the
+              // collapsing vertex's slot; maxdet as in slot order: the face's
+              // first maximum against k, k first on a tie if its slot comes first
+              unsigned sl = s_slot[w][x];
+              int pos = int(sl & 15u), fb = int(sl >> 4);
+              int j0 = pos == 0 ? 1 : 0, j1 = pos <= 1 ? 2 : 1, j2 = pos <= 2 ? 3 : 2;
+              int f0 = int((packed >> (8 * j0)) & 255u), f1 = int((packed >> (8 * j1)) & 255u),
+                  f2 = int((packed >> (8 * j2)) & 255u);
+              float4 hf[3] = {s_h[w][f0], s_h[w][f1], s_h[w][f2]};
+              float4 lf[3] = {s_l[w][f0], s_l[w][f1], s_l[w][f2]};
+              int lfb = int((packed >> (8 * fb)) & 255u);
+              long long kf = s_key[w][lfb], kp = s_key[w][k];
+              int best = (kp > kf || (kp == kf && pos < fb)) ? k : lfb;
+              b = tet_face_bounds<true>(s_inv[w][x], hf, lf, s_h[w][k], s_l[w][k], s_ma[w][best],
+                                        s_mb[w][best]);
+            } else {
+              int li[NV];
+              for (int jj = 0; jj < NV; ++jj) {
+                li[jj] = int((packed >> (8 * jj)) & 255u);
+                if (li[jj] == 0) li[jj] = k;  // v_col moved onto v_onto
               }
+              int best = 0;
+              long long bk = s_key[w][li[0]];
+              for (int jj = 1; jj < NV; ++jj) {
+                long long kk = s_key[w][li[jj]];
+                if (kk > bk) {
+                  best = jj;
+                  bk = kk;
+                }
+              }
+              float4 h[NV], l[NV];
+              for (int jj = 0; jj < NV; ++jj) {
+                h[jj] = s_h[w][li[jj]];
+                l[jj] = s_l[w][li[jj]];
+              }
+              b = tri_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
             }
-            float4 h[NV], l[NV];
-            for (int jj = 0; jj < NV; ++jj) {
-              h[jj] = s_h[w][li[jj]];
-              l[jj] = s_l[w][li[jj]];
-            }
-            b = tri_quality_bounds_of(h, l, s_ma[w][li[best]], s_mb[w][li[best]]);
+            atomicMin(&s_lo[w][k], fkey(b.lo));
+            atomicMin(&s_hi[w][k], fkey(b.hi));
+            ++nscreen;
           }
-          atomicMin(&s_lo[w][k], fkey(b.lo));
-          atomicMin(&s_hi[w][k], fkey(b.hi));
-          ++nscreen;
         }
+        __syncwarp();
+        // move the rest of the queue (fewer than 32) to its front
+        const int rest = qn - nq;
+        unsigned short mv = lane < rest ? s_q[w][nq + lane] : (unsigned short)0;
+        __syncwarp();
+        if (lane < rest) s_q[w][lane] = mv;
+        qn = rest;
+        __syncwarp();
       }
-      __syncwarp();
-      // move the rest of the queue (fewer than 32) to its front
-      const int rest = qn - nq;
-      unsigned short mv = lane < rest ? s_q[w][nq + lane] : (unsigned short)0;
-      __syncwarp();
-      if (lane < rest) s_q[w][lane] = mv;
-      qn = rest;
-      __syncwarp();
-    }
-    if (a.overshoot) {
-      // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
-      // for the directions the quality screen has not failed: the new edges
-      // from each direction's vertex moved onto to v's other neighbours,
-      // (direction, neighbour) pairs over the lanes; a direction with a new
-      // edge at or above max_length does not collapse.  The two checks are
-      // both required of a direction, so either order gives the same
-      // decisions; this order skips the edges of the many directions that
-      // fail on quality.  Its outcome does not depend on which over-long
-      // edge is found first.
-      const LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
-      const int npo = nd * ne;
-      const float rne = 1.0f / float(ne);
-      unsigned nl = 0, nx = 0;
-      for (int p = lane; p < npo; p += 32) {
-        int t = int((float(p) + 0.5f) * rne);  // p / ne: exact for p < 2^12, ne <= 31
-        int wl = p - t * ne + 1;
-        int k = s_dk[w][t];
-        if (wl == k || s_over[w][k] || fkey_inv(s_hi[w][k]) < fail_below) continue;
-        // the new edge keeps the orientation of v's edge to wl, with k for v
-        int ein = s_end[w][wl];
-        int ia = ein == 0 ? k : wl, ib = ein == 0 ? wl : k;
-        float qlo[2], qhi[2];
-        bool qok = edge_q_bounds_rec<D>(s_h[w][ia], s_l[w][ia], s_ma[w][ia], s_mb[w][ia],
-                                        s_h[w][ib], s_l[w][ib], s_ma[w][ib], s_mb[w][ib], qlo, qhi);
-        int side = len_cut_side(qlo, qhi, qok, cut);
-        ++nl;
-        bool over;
-        if (side != 0) {
-          over = side > 0;
-        } else {
-          FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
-          if (L.lo >= a.ov_thr) {
-            over = true;
-          } else if (L.hi < a.ov_thr) {
-            over = false;
+      if (a.overshoot) {
+        // prevent_coarsen_overshoot (src/Omega_h_coarsen_overshoot.cpp:11-49)
+        // for the directions the quality screen has not failed: the new edges
+        // from each direction's vertex moved onto to v's other neighbours,
+        // (direction, neighbour) pairs over the lanes; a direction with a new
+        // edge at or above max_length does not collapse.  The two checks are
+        // both required of a direction, so either order gives the same
+        // decisions; this order skips the edges of the many directions that
+        // fail on quality.  Its outcome does not depend on which over-long
+        // edge is found first.
+        const LenCut cut = len_cut(a.ov_tdn, a.ov_thr);
+        const int npo = ng * ne;
+        const float rne = 1.0f / float(ne);
+        unsigned nl = 0, nx = 0;
+        for (int p = lane; p < npo; p += 32) {
+          int t = int((float(p) + 0.5f) * rne);  // p / ne: exact for p < 2^12, ne <= 31
+          int wl = p - t * ne + 1;
+          int k = s_gk[w][t];
+          if (wl == k || s_over[w][k] || fkey_inv(s_hi[w][k]) < fail_below) continue;
+          // the new edge keeps the orientation of v's edge to wl, with k for v
+          int ein = s_end[w][wl];
+          int ia = ein == 0 ? k : wl, ib = ein == 0 ? wl : k;
+          float qlo[2], qhi[2];
+          bool qok = edge_q_bounds_rec<D>(s_h[w][ia], s_l[w][ia], s_ma[w][ia], s_mb[w][ia],
+                                          s_h[w][ib], s_l[w][ib], s_ma[w][ib], s_mb[w][ib], qlo, qhi);
+          int side = len_cut_side(qlo, qhi, qok, cut);
+          ++nl;
+          bool over;
+          if (side != 0) {
+            over = side > 0;
           } else {
-            over = edge_len_v(D, a.c, a.mt, a.mc, s_gid[w][ia], s_gid[w][ib]) >= a.max_length;
-            ++nx;
+            FIv L = qok ? len_from_q(qlo, qhi) : widen_all();
+            if (L.lo >= a.ov_thr) {
+              over = true;
+            } else if (L.hi < a.ov_thr) {
+              over = false;
+            } else {
+              over = edge_len_v(D, a.c, a.mt, a.mc, s_gid[w][ia], s_gid[w][ib]) >= a.max_length;
+              ++nx;
+            }
           }
+          if (over) s_over[w][k] = 1;
         }
-        if (over) s_over[w][k] = 1;
+        warp_count_full(&a.cnt[2], nl);
+        warp_count_full(&a.cnt[3], nx);
+        __syncwarp();
       }
-      warp_count_full(&a.cnt[2], nl);
-      warp_count_full(&a.cnt[3], nx);
-      __syncwarp();
+      // a surely passing direction ends the search
+      bool sure = false;
+      if (lane < ng) {
+        int k = s_gk[w][lane];
+        sure = !s_over[w][k] && fkey_inv(s_lo[w][k]) >= pass_from;
+      }
+      if (__any_sync(full, sure)) {
+        skipped = todo;
+        break;
+      }
     }
     for (LO k = 1 + lane; k <= ne; k += 32) {
       LO d = s_dir[w][k];
       if (d < 0) continue;
-      if (s_over[w][k]) {
+      if ((skipped >> s_dt[w][k]) & 1u) {
+        a.q2[d] = -1.0;  // longer than a surely passing direction: not the rail
+      } else if (s_over[w][k]) {
         a.q2[d] = -1.0;  // overshoots: does not collapse
       } else {
         screen_outcome(a, d, fkey_inv(s_lo[w][k]), fkey_inv(s_hi[w][k]), cubed);
@@ -2084,8 +2131,9 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
   CoarsenVertexArgs args{nV,   chunk, sv,   ev,   cv,
                          va,   vb,    cview(v2e.a2ab), cview(v2e.ab2b), vc,
                          cview(v2e.codes), cview(e2cand), cview(codes_p, n), q2, mqa_f,
-                         mqa3_dn, mqa3_up, overshoot, max_length, ov_thr, ov_tdn, c, mt,
-                         m.mcomp(), queue.data(), amb_dir.data(), amb_mhi.data(), &cnt[0]};
+                         mqa3_dn, mqa3_up, overshoot, max_length, cview(m.ask_lengths()), ov_thr,
+                         ov_tdn, c, mt, m.mcomp(), queue.data(), amb_dir.data(), amb_mhi.data(),
+                         &cnt[0]};
   bytes += double(nE) * 4 + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
   {
     KernelTimer timer("coarsen_filter", bytes);
