@@ -2134,7 +2134,9 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
                          mqa3_dn, mqa3_up, overshoot, max_length, cview(m.ask_lengths()), ov_thr,
                          ov_tdn, c, mt, m.mcomp(), queue.data(), amb_dir.data(), amb_mhi.data(),
                          &cnt[0]};
-  bytes += double(nE) * 4 + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
+  // the edge-to-candidate map, the vertex-to-edge rows and the FP64 edge
+  // lengths (the rail order)
+  bytes += double(nE) * (4 + 8) + double(nV + 1) * 4 + double(v2e.ab2b.size()) * 5;
   {
     KernelTimer timer("coarsen_filter", bytes);
     unsigned nb = persistent_blocks(k_coarsen_screen_v<D>, block, (nV + chunk - 1) / chunk);
