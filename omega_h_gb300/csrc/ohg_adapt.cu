@@ -652,6 +652,43 @@ static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>&
           r[k] = LO(b);
         }
       });
+    } else if (ent_dim == FACE && key_dim == EDGE && om.dim == 3 &&
+               !om.adj.count({EDGE, FACE}) && !om.adj_any_order.count({EDGE, FACE})) {
+      // the faces containing a key edge are, in each tet around it, the two
+      // tet faces that hold both of the edge's vertices: the representative,
+      // the smallest such face, without inverting the face-to-edge lists
+      const Adj& e2t = om.ask_up_any_order(EDGE, REGION);
+      auto ea = cview(e2t.a2ab);
+      auto eb = cview(e2t.ab2b);
+      auto ec = cview(e2t.codes);
+      auto tf = cview(om.ask_down(REGION, FACE).ab2b);
+      int* stw = ctx().d_status;
+      pfor(nkeys, [=] __device__(LO k) {
+        LO e = kd[k];
+        LO mn = -1;
+        for (LO x = ea[e]; x < ea[e + 1]; ++x) {
+          LO t = eb[x];
+          int j = code_which_down(ec[x]);
+          int va = down_template(3, 1, j, 0), vb = down_template(3, 1, j, 1);
+          for (int f = 0; f < 4; ++f) {
+            bool ha = false, hb = false;
+            for (int q = 0; q < 3; ++q) {
+              int fv = down_template(3, 2, f, q);
+              ha = ha || fv == va;
+              hb = hb || fv == vb;
+            }
+            if (ha && hb) {
+              LO face = tf[t * 4 + f];
+              if (mn < 0 || face < mn) mn = face;
+            }
+          }
+        }
+        if (mn < 0) {
+          raise_status(stw, ST_TOPOLOGY);
+          mn = 0;
+        }
+        r[k] = mn;
+      });
     } else if (ent_dim > key_dim) {
       // the first entry of an upward row sorted by high entity is the row's
       // smallest entity: its minimum over the row in any order, so the rows
@@ -2504,6 +2541,37 @@ static void filter_cands(Arr<LO>& c2e, Arr<I8>& codes, Arr<double>* q2) {
   if (q2) *q2 = unmap(keep, *q2, 2);
 }
 
+// The faces around a vertex v of a tet mesh, from v's tets: each tet holds v
+// in one slot, and its three faces other than the one opposite that slot
+// contain v.  Every face around v is found this way, once per tet that holds
+// it (one or two).  For rows of up to 32 tets, lane l of a warp takes tet
+// beg + l; the face ids go to F (-1 where there is none) and keep[] marks
+// each face's first occurrence in (lane, slot) order.
+__device__ __forceinline__ void faces_around_lane(LO v, LO beg, LO end, int lane, LV tb,
+                                                  View<const I8> tc, LV tf, LO F[3],
+                                                  bool keep[3]) {
+  for (int i = 0; i < 3; ++i) F[i] = -1;
+  LO x = beg + lane;
+  if (x < end) {
+    LO t = tb[x];
+    int sv = code_which_down(tc[x]);
+    int q = 0;
+    for (int f = 0; f < 4; ++f) {
+      bool has = false;
+      for (int j = 0; j < 3; ++j) has = has || down_template(3, 2, f, j) == sv;
+      if (has) F[q++] = tf[t * 4 + f];
+    }
+  }
+  for (int i = 0; i < 3; ++i) keep[i] = F[i] >= 0;
+  for (int src = 0; src < 32; ++src) {
+    for (int j = 0; j < 3; ++j) {
+      LO o = __shfl_sync(0xffffffffu, F[j], src);
+      for (int i = 0; i < 3; ++i)
+        if (o == F[i] && (src < lane || (src == lane && j < i))) keep[i] = false;
+    }
+  }
+}
+
 // coarsen_verts + coarsen (src/Omega_h_coarsen.cpp:29-176): collapse the
 // marked vertices along their edges.  allowed: overshoot limit
 // max_length_allowed instead of max_length_desired; improve: keep only
@@ -2692,23 +2760,65 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Arr<LO> k2ps[4];
   ModifyPlan plans[4];
   k2ps[0] = fill<LO>(nkeys + 1, 0);
+  // In 3D the faces around a key vertex come from its tets (faces_around_lane)
+  // when the vertex-to-face rows are not built: their ascending order is the
+  // sorted row's, without inverting and sorting the face-to-vertex lists.
+  bool faces_by_tets = dim == 3 && !m.adj.count({VERT, FACE});
   for (int d = 1; d <= dim; ++d) {
-    const Adj& v2d = m.ask_up(0, d);
-    auto va = cview(v2d.a2ab);
-    auto vb = cview(v2d.ab2b);
     auto dd = cview(dead[d]);
     auto kv = cview(k2v);
-    // one warp per key: the lanes stride the key vertex's row (rows of
-    // tens of entries, which one thread would walk alone)
     Arr<LO> cnt(nkeys);
     auto ct = view(cnt);
-    group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
-      if (k < 0) return;
-      LO v = kv[k], n2 = 0;
-      for (LO x = va[v] + gl; x < va[v + 1]; x += 32) n2 += !dd[vb[x]];
-      n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
-      if (gl == 0) ct[k] = n2;
-    });
+    if (d == FACE && faces_by_tets) {
+      const Adj& v2t = m.ask_up(0, 3);
+      auto ta = cview(v2t.a2ab);
+      auto tb = cview(v2t.ab2b);
+      auto tc = cview(v2t.codes);
+      auto tf = cview(m.ask_down(3, 2).ab2b);
+      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+        if (k < 0) return;
+        LO v = kv[k], beg = ta[v], end = ta[v + 1];
+        LO n2 = 0;
+        if (end - beg <= 32) {
+          LO F[3];
+          bool keep[3];
+          faces_around_lane(v, beg, end, gl, tb, tc, tf, F, keep);
+          for (int i = 0; i < 3; ++i) n2 += keep[i] && !dd[F[i]];
+          n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
+        } else if (gl == 0) {
+          // a long row: one lane, each face counted at its first occurrence
+          for (LO x = beg; x < end; ++x) {
+            LO t = tb[x];
+            int sv = code_which_down(tc[x]);
+            for (int f = 0; f < 4; ++f) {
+              bool has = false;
+              for (int j = 0; j < 3; ++j) has = has || down_template(3, 2, f, j) == sv;
+              if (!has) continue;
+              LO F = tf[t * 4 + f];
+              bool first = true;
+              for (LO y = beg; y < x && first; ++y)
+                for (int g = 0; g < 4; ++g)
+                  if (tf[tb[y] * 4 + g] == F) first = false;
+              n2 += first && !dd[F];
+            }
+          }
+        }
+        if (gl == 0) ct[k] = n2;
+      });
+    } else {
+      const Adj& v2d = m.ask_up(0, d);
+      auto va = cview(v2d.a2ab);
+      auto vb = cview(v2d.ab2b);
+      // one warp per key: the lanes stride the key vertex's row (rows of
+      // tens of entries, which one thread would walk alone)
+      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+        if (k < 0) return;
+        LO v = kv[k], n2 = 0;
+        for (LO x = va[v] + gl; x < va[v + 1]; x += 32) n2 += !dd[vb[x]];
+        n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
+        if (gl == 0) ct[k] = n2;
+      });
+    }
     k2ps[d] = offset_scan(cnt);
   }
   {
@@ -2724,7 +2834,87 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   for (int d = 0; d <= dim; ++d) {
     const Arr<LO>& k2p = k2ps[d];
     Arr<LO> pv2v, kd2d;
-    if (d != VERT) {
+    if (d == FACE && faces_by_tets) {
+      const Adj& v2t = m.ask_up(0, 3);
+      auto ta = cview(v2t.a2ab);
+      auto tb = cview(v2t.ab2b);
+      auto tc = cview(v2t.codes);
+      auto tf = cview(m.ask_down(3, 2).ab2b);
+      auto dd = cview(dead[d]);
+      auto kv = cview(k2v);
+      LO nprod = plans[d].sizes[2];
+      kd2d = Arr<LO>(nprod);
+      pv2v = Arr<LO>(nprod * 3);
+      auto kp = cview(k2p);
+      auto cv = cview(m.ask_verts_of(2));
+      auto ko = cview(k2onto);
+      auto o2n = cview(ov2nv);
+      auto kd = view(kd2d);
+      auto pv = view(pv2v);
+      // the live faces in ascending order (the sorted row's order): each
+      // one's rank among the live faces gives its product slot
+      group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
+        if (k < 0) return;
+        LO v = kv[k], beg = ta[v], end = ta[v + 1], p = kp[k];
+        auto put = [&](LO q, LO F) {
+          kd[q] = F;
+          for (int ccv = 0; ccv < 3; ++ccv) {
+            LO fv = cv[F * 3 + ccv];
+            pv[q * 3 + ccv] = o2n[fv == v ? ko[k] : fv];
+          }
+        };
+        if (end - beg <= 32) {
+          LO F[3];
+          bool keep[3];
+          faces_around_lane(v, beg, end, gl, tb, tc, tf, F, keep);
+          LO L[3];  // the live faces kept here (-1: none)
+          for (int i = 0; i < 3; ++i) L[i] = keep[i] && !dd[F[i]] ? F[i] : -1;
+          LO rank[3] = {0, 0, 0};
+          for (int src = 0; src < 32; ++src)
+            for (int j = 0; j < 3; ++j) {
+              LO o = __shfl_sync(0xffffffffu, L[j], src);
+              for (int i = 0; i < 3; ++i) rank[i] += o >= 0 && o < L[i];
+            }
+          for (int i = 0; i < 3; ++i)
+            if (L[i] >= 0) put(p + rank[i], L[i]);
+        } else if (gl == 0) {
+          // a long row: one lane; a face's slot is the number of live first
+          // occurrences with a smaller id
+          for (LO x = beg; x < end; ++x) {
+            LO t = tb[x];
+            int sv = code_which_down(tc[x]);
+            for (int f = 0; f < 4; ++f) {
+              bool has = false;
+              for (int j = 0; j < 3; ++j) has = has || down_template(3, 2, f, j) == sv;
+              if (!has) continue;
+              LO F = tf[t * 4 + f];
+              bool first = true;
+              for (LO y = beg; y < x && first; ++y)
+                for (int g = 0; g < 4; ++g)
+                  if (tf[tb[y] * 4 + g] == F) first = false;
+              if (!first || dd[F]) continue;
+              LO r = 0;
+              for (LO y = beg; y < end; ++y) {
+                int sy = code_which_down(tc[y]);
+                for (int g = 0; g < 4; ++g) {
+                  bool hg = false;
+                  for (int j = 0; j < 3; ++j) hg = hg || down_template(3, 2, g, j) == sy;
+                  if (!hg) continue;
+                  LO G = tf[tb[y] * 4 + g];
+                  if (G >= F || dd[G]) continue;
+                  bool gfirst = true;
+                  for (LO z = beg; z < y && gfirst; ++z)
+                    for (int h = 0; h < 4; ++h)
+                      if (tf[tb[z] * 4 + h] == G) gfirst = false;
+                  r += gfirst;
+                }
+              }
+              put(p + r, F);
+            }
+          }
+        }
+      });
+    } else if (d != VERT) {
       const Adj& v2d = m.ask_up(0, d);
       auto va = cview(v2d.a2ab);
       auto vb = cview(v2d.ab2b);
