@@ -1269,10 +1269,75 @@ void check_collapse_class(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8* co
   });
 }
 
+// The tet's local edge between local vertices a and b, as 4 bits at
+// 4 * (a * 4 + b) of the returned word (from the edge template)
+static unsigned long long tet_edge_lookup() {
+  unsigned long long t = 0;
+  for (int j = 0; j < 6; ++j) {
+    int a = down_template(3, 1, j, 0), b = down_template(3, 1, j, 1);
+    t |= (unsigned long long)j << (4 * (a * 4 + b));
+    t |= (unsigned long long)j << (4 * (b * 4 + a));
+  }
+  return t;
+}
+__device__ __forceinline__ int tet_edge_between(unsigned long long lut, int a, int b) {
+  return int((lut >> (4 * (a * 4 + b))) & 15u);
+}
+
 // check_collapse_exposure (src/Omega_h_check_collapse.cpp:69-119)
 void check_collapse_exposure(Mesh& m, const LO* c2e_p, LO n, const I8* ci_p, I8* co_p) {
-  Arr<I8> tmp(n);
   auto c2e = cview(c2e_p, n);
+  if (m.dim == 3) {
+    // Both steps in one walk of the edge's tets.  The faces around the edge
+    // are, in each tet around it, the two tet faces that hold the edge: face
+    // {col, onto, w} is the one opposite the tet's fourth vertex, and its
+    // side opposite onto is the tet edge {col, w}.  A face shared by two
+    // tets is checked twice, with the same outcome; the steps only clear
+    // bits, so their order does not change the result.
+    const Adj& e2t = m.ask_up_any_order(EDGE, REGION);
+    auto ea = cview(e2t.a2ab);
+    auto eb = cview(e2t.ab2b);
+    auto ecc = cview(e2t.codes);
+    auto tf = cview(m.ask_down(REGION, FACE).ab2b);
+    auto te = cview(m.ask_down(REGION, EDGE).ab2b);
+    auto edim = cview(m.class_dim[EDGE]);
+    auto fdim = cview(m.class_dim[FACE]);
+    auto tdim = cview(m.class_dim[REGION]);
+    auto in = cview(ci_p, n);
+    auto out = view(co_p, n);
+    unsigned long long lut = tet_edge_lookup();
+    pfor(n, [=] __device__(LO c) {
+      I8 code = in[c];
+      if (!code) {
+        out[c] = 0;
+        return;
+      }
+      LO e = c2e[c];
+      for (LO x = ea[e]; x < ea[e + 1]; ++x) {
+        LO t = eb[x];
+        int cce = code_which_down(ecc[x]), rot = code_rotation(ecc[x]);
+        int l0 = down_template(3, 1, cce, rot), l1 = down_template(3, 1, cce, rot ^ 1);
+        // the tet's two other vertices, and each one's face with the edge
+        int w0 = -1, w1 = -1;
+        for (int k = 0; k < 4; ++k)
+          if (k != l0 && k != l1) (w0 < 0 ? w0 : w1) = k;
+        int tcd = tdim[t];
+        int fw0 = fdim[tf[t * 4 + opposite_template(3, 0, w1)]];  // {l0, l1, w0}
+        int fw1 = fdim[tf[t * 4 + opposite_template(3, 0, w0)]];  // {l0, l1, w1}
+        for (int col = 0; col < 2; ++col) {
+          if (!collapses(code, col)) continue;
+          int lc = col ? l1 : l0, lo = col ? l0 : l1;
+          bool bad = fdim[tf[t * 4 + opposite_template(3, 0, lo)]] != tcd ||
+                     edim[te[t * 6 + tet_edge_between(lut, lc, w0)]] != fw0 ||
+                     edim[te[t * 6 + tet_edge_between(lut, lc, w1)]] != fw1;
+          if (bad) code = dont_collapse(code, col);
+        }
+      }
+      out[c] = code;
+    });
+    return;
+  }
+  Arr<I8> tmp(n);
   View<const I8> in = cview(ci_p, n);
   for (int cd = 2; cd <= m.dim; ++cd) {
     View<I8> out = cd == m.dim ? view(co_p, n) : view(tmp);
@@ -1569,7 +1634,7 @@ __device__ __forceinline__ void screen_outcome(const CoarsenVertexArgs& a, LO d,
 }
 
 template <int D>
-__global__ void __launch_bounds__(kVsBlock, 6) k_coarsen_screen_v(CoarsenVertexArgs a) {
+__global__ void __launch_bounds__(kVsBlock, 7) k_coarsen_screen_v(CoarsenVertexArgs a) {
   constexpr int NV = D + 1;
   // 3D: per star element, the invariants of its face opposite the
   // collapsing vertex (tet_face_invariants), the slot of that vertex and the
@@ -2724,7 +2789,41 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   Arr<I8> dead[4];
   dead[1] = mark_image(r2e, ne);
   for (int d = 2; d <= dim; ++d) dead[d] = fill<I8>(m.nents[d], 0);
-  for (int cd = dim; cd > EDGE; --cd) {
+  if (dim == 3) {
+    // both steps in one walk of the rail's tets: each tet dies with its face
+    // opposite onto; of the two faces holding the rail, {col, onto, w}, each
+    // dies with its side opposite onto, the tet edge {col, w}
+    const Adj& e2t = m.ask_up_any_order(EDGE, REGION);
+    auto ea = cview(e2t.a2ab);
+    auto eb = cview(e2t.ab2b);
+    auto ecc = cview(e2t.codes);
+    auto tf = cview(m.ask_down(REGION, FACE).ab2b);
+    auto te = cview(m.ask_down(REGION, EDGE).ab2b);
+    auto re = cview(r2e);
+    auto rd = cview(rdir);
+    auto d3 = view(dead[3]);
+    auto d2 = view(dead[2]);
+    auto d1 = view(dead[1]);
+    unsigned long long lut = tet_edge_lookup();
+    pfor(nkeys, [=] __device__(LO r) {
+      LO e = re[r];
+      int onto = 1 - rd[r];
+      for (LO x = ea[e]; x < ea[e + 1]; ++x) {
+        LO t = eb[x];
+        int cce = code_which_down(ecc[x]), rot = code_rotation(ecc[x]);
+        int lo = down_template(3, 1, cce, rot ^ onto);
+        int lc = down_template(3, 1, cce, rot ^ (1 - onto));
+        d3[t] = 1;
+        d2[tf[t * 4 + opposite_template(3, 0, lo)]] = 1;
+        for (int w = 0; w < 4; ++w) {
+          if (w == lo || w == lc) continue;
+          d2[tf[t * 4 + opposite_template(3, 0, 6 - lo - lc - w)]] = 1;
+          d1[te[t * 6 + tet_edge_between(lut, lc, w)]] = 1;
+        }
+      }
+    });
+  }
+  for (int cd = dim; cd > EDGE && dim != 3; --cd) {
     const Adj& e2c = m.ask_up_any_order(1, cd);  // marks only: row order is free
     auto ea = cview(e2c.a2ab);
     auto eb = cview(e2c.ab2b);
