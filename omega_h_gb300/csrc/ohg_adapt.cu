@@ -2249,90 +2249,47 @@ static void coarsen_filter_lazy_d(Mesh& m, const LO* c2e_p, LO n, I8* codes_p, d
     checked_after_launch(__FILE__, __LINE__);
 #endif
   }
-  // FP64 minima of the straddling directions: the elements whose lower bound
-  // does not exceed the smallest upper bound become (direction, element)
-  // pairs in one dense list, evaluated in full warps, reduced by an atomic
-  // minimum on order keys (the minimum of a set of doubles does not depend
-  // on the order of evaluation)
-  unsigned long long hq[2];
+  // FP64 minima of the straddling directions: of each one's cavity, the
+  // elements whose lower bound does not exceed the smallest upper bound are
+  // evaluated in FP64 and reduced to their minimum (the minimum of a set of
+  // doubles does not depend on the order of evaluation).  One group of lanes
+  // per direction, the directions' number read on the device: no host wait
+  // for it.
   {
-    OHG_CUDA(cudaMemcpyAsync(cx.h_pinned, queue.data() + 1, sizeof(unsigned long long),
-                             cudaMemcpyDeviceToHost, cx.stream));
-    cx.sync();
-    std::memcpy(&hq[1], cx.h_pinned, sizeof(unsigned long long));
-  }
-  LO K = LO(hq[1]);
-  if (K > 0) {
+    const unsigned long long* qn = queue.data() + 1;
     auto ad = cview(amb_dir);
     auto am = cview(amb_mhi);
     constexpr int G = kCavityLanes;
-    // elements of each cavity that need FP64
-    Arr<LO> pcount(K);
-    auto pc = view(pcount);
-    group_for(G, K, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
-      if (k < 0) return;
-      LO d = ad[k], e = c2e[d >> 1];
-      int col = d & 1;
-      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
-      float mh = am[k];
-      LO x1 = va[v_col + 1], np = 0;
-      for (LO xb = va[v_col]; xb < x1; xb += G) {
-        LO x = xb + gl;
-        LO vv[4];
-        if (x < x1 && collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv) &&
-            elem_quality_bounds(dim, sv, vv).lo <= mh)
-          ++np;
-      }
-#pragma unroll
-      for (int j = G / 2; j > 0; j >>= 1) np += __shfl_xor_sync(gm, np, j, G);
-      if (gl == 0) pc[k] = np;
-    });
-    Arr<LO> poff = offset_scan(pcount);
-    LO P = last(poff);
-    Arr<LO> pk(P), px(P);
-    auto po = cview(poff);
-    auto pkv = view(pk);
-    auto pxv = view(px);
-    group_for(G, K, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
-      if (k < 0) return;
-      LO d = ad[k], e = c2e[d >> 1];
-      int col = d & 1;
-      LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
-      float mh = am[k];
-      LO x1 = va[v_col + 1], at = po[k];
-      unsigned glt = gm & ((1u << (threadIdx.x & 31u)) - 1u);
-      for (LO xb = va[v_col]; xb < x1; xb += G) {
-        LO x = xb + gl;
-        LO vv[4];
-        bool need = x < x1 && collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv) &&
-                    elem_quality_bounds(dim, sv, vv).lo <= mh;
-        unsigned bits = __ballot_sync(gm, need) & gm;
-        if (need) {
-          LO slot = at + __popc(bits & glt);
-          pkv[slot] = k;
-          pxv[slot] = x;
+    LO slots = LO(std::min<long long>(ndirs, (long long)cx.num_sms * (2048 / G)));
+    group_for(G, slots, kBlock, [=] __device__(LO s, int gl, unsigned gm) {
+      if (s < 0) return;
+      LO K = LO(*qn);
+      unsigned nfp64 = 0;
+      for (LO k = s; k < K; k += slots) {
+        LO d = ad[k], e = c2e[d >> 1];
+        int col = d & 1;
+        LO v_col = ev[e * 2 + col], v_onto = ev[e * 2 + (1 - col)];
+        float mh = am[k];
+        long long best = order_key(1.0);
+        LO x1 = va[v_col + 1];
+        for (LO xb = va[v_col]; xb < x1; xb += G) {
+          LO x = xb + gl;
+          LO vv[4];
+          if (x < x1 && collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv) &&
+              elem_quality_bounds(dim, sv, vv).lo <= mh) {
+            long long q = order_key(elem_quality_exact(dim, sv, c, mt, vv));
+            best = q < best ? q : best;
+            ++nfp64;
+          }
         }
-        at += __popc(bits);
+#pragma unroll
+        for (int j = G / 2; j > 0; j >>= 1) {
+          long long o = __shfl_xor_sync(gm, best, j, G);
+          best = o < best ? o : best;
+        }
+        if (gl == 0) q2[ad[k]] = key_to_double(best);
       }
-    });
-    Arr<long long> kmin = fill<long long>(K, order_key(1.0));
-    auto km = view(kmin);
-    auto pkc = cview(pk);
-    auto pxc = cview(px);
-    pfor(P, [=] __device__(LO i) {
-      LO k = pkc[i], x = pxc[i];
-      LO d = ad[k], e = c2e[d >> 1];
-      int col = d & 1;
-      LO v_onto = ev[e * 2 + (1 - col)];
-      LO vv[4];
-      collapse_elem(cv, dim, vb[x], code_which_down(vc[x]), v_onto, vv);
-      atomicMin(&km[k], order_key(elem_quality_exact(dim, sv, c, mt, vv)));
-    });
-    auto kmc = cview(kmin);
-    unsigned long long nfp64 = (unsigned long long)P;
-    pfor(K, [=] __device__(LO k) {
-      q2[ad[k]] = key_to_double(kmc[k]);
-      if (k == 0) cnt[1] += nfp64;
+      warp_count(&cnt[1], nfp64);
     });
   }
   // the decisions: a direction passes on its enclosure (NaN) or on its FP64
@@ -2655,6 +2612,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
     pfor(ne, [=] __device__(LO e) { ec[e] = I8((v[ev[e * 2]] ? 1 : 0) | (v[ev[e * 2 + 1]] ? 2 : 0)); });
   }
   Arr<LO> c2e = collect_marked(ecodes);
+  if (c2e.size() == 0) return false;
   Arr<I8> codes0 = unmap(c2e, ecodes, 1);
   Arr<I8> codes(c2e.size());
   check_collapse_class(m, c2e.data(), c2e.size(), codes0.data(), codes.data());
@@ -2682,14 +2640,17 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
     codes = codes2;
   else
     prevent_coarsen_overshoot(m, max_len, c2e.data(), c2e.size(), codes2.data(), codes.data());
+  // With screening the list is not compacted here: the screen and
+  // choose_rails_lazy pass over candidates with code 0, and whether any
+  // candidate passed the class check is read with the keys' count below.
   int passed_class = 0;
-  {
+  if (!lazy) {
     Arr<LO> keep = collect_marked(codes, any_class.data(), &passed_class);
     c2e = unmap(keep, c2e, 1);
     codes = unmap(keep, codes, 1);
+    if (passed_class) m.parting = 1;  // ghosted once candidates pass the class check
+    if (c2e.size() == 0) return false;
   }
-  if (passed_class) m.parting = 1;  // ghosted once candidates pass the class check
-  if (c2e.size() == 0) return false;
   LO nc = c2e.size();
   Arr<double> q2(nc * 2);
   if (lazy) {
@@ -2745,7 +2706,9 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
     choose_rails(m, c2e.data(), c2e.size(), codes.data(), q2.data(), vc.data(), vq.data(),
                  vr.data());
   Arr<I8> vkeys = find_indset(m, VERT, vq, vc);
-  Arr<LO> k2v = collect_marked(vkeys);
+  Arr<LO> k2v = lazy ? collect_marked(vkeys, any_class.data(), &passed_class)
+                     : collect_marked(vkeys);
+  if (lazy && passed_class) m.parting = 1;
   LO nkeys = k2v.size();
   if (nkeys == 0) return false;  // no candidate survived (the set of any is not empty)
   st->coarsen_keys = nkeys;
@@ -3290,6 +3253,29 @@ void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO
 // improving_only (the pass): a candidate whose best triangulation's upper
 // bound is below the worst current quality around its edge cannot pass
 // filter_swap_improve; it gets quality -DBL_MAX and no FP64 work.
+// f(i) for every i below a count that is on the device (*n_dev, at most
+// bound), in a grid-stride loop over a grid of resident size: the count
+// needs no host wait
+template <class F>
+__global__ void k_for_dev_count(const LO* n_dev, F f) {
+  LO n = *n_dev;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    f(LO(i));
+}
+template <class F>
+static void pfor_dev_count(const LO* n_dev, LO bound, F f) {
+  if (bound <= 0) return;
+  Ctx& c = ctx();
+  long long full = (long long)c.num_sms * (2048 / kBlock);
+  long long need = ((long long)bound + kBlock - 1) / kBlock;
+  k_for_dev_count<<<unsigned(need < full ? need : full), kBlock, 0, c.stream>>>(n_dev, f);
+  ++c.launches;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
+}
+
 static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, LO n,
                                       double* quals_p, I8* configs_p,
                                       bool improving_only = false) {
@@ -3527,9 +3513,11 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     Arr<LO> tcnt(n);
     auto tc = view(tcnt);
     pfor(n, [=] __device__(LO i) { tc[i] = __popcll(nd[i]); });
+    // the list is sized by its bound (every unique triangle of every
+    // candidate) and walked up to its count on the device: no host wait
     Arr<LO> toff = offset_scan(tcnt);
-    LO ntot = last(toff);
-    Arr<LO> ent(ntot);
+    LO bound = n * kMaxUniqTris;
+    Arr<LO> ent(bound);
     auto of = cview(toff);
     auto en = view(ent);
     pfor(n, [=] __device__(LO i) {
@@ -3543,7 +3531,7 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     });
     auto q = view(tq);
     auto enc = cview(ent);
-    pfor(ntot, [=] __device__(LO j) {
+    pfor_dev_count(toff.data() + n, bound, [=] __device__(LO j) {
       LO idx = enc[j];
       LO i = idx / kMaxUniqTris;
       int u = idx % kMaxUniqTris;
@@ -4157,12 +4145,20 @@ PassStats adapt_pass(Mesh& m, const AdaptOpts& o) {
   st.did_coarsen = coarsen_by_size(m, o, &st);
   OHG_CUDA(cudaEventRecord(e2, c.stream));
   m.parting = 1;
-  st.min_quality = min_f64(m.ask_qualities());
-  if (st.min_quality < o.min_quality_desired) st.did_swap = swap_edges(m, o, &st);
+  // adapt() swaps only while the worst quality is below min_quality_desired
+  // (src/Omega_h_adapt.cpp:196); with none below it, swap_edges finds no
+  // candidate (its candidates are the sliver layers of those elements) and
+  // changes nothing.  So the worst quality is only reported: it is read at
+  // the pass's last host wait, not before the swap.
+  Arr<double> minq = min_f64_dev(m.ask_qualities());
+  OHG_CUDA(cudaMemcpyAsync(c.h_pass_min, minq.data(), sizeof(double), cudaMemcpyDeviceToHost,
+                           c.stream));
+  st.did_swap = swap_edges(m, o, &st);
   OHG_CUDA(cudaEventRecord(e3, c.stream));
   OHG_CUDA(cudaMemcpyAsync(c.h_indset_sweeps, c.d_indset_sweeps, sizeof(int),
                            cudaMemcpyDeviceToHost, c.stream));
   c.sync();
+  st.min_quality = *c.h_pass_min;
   st.indset_rounds = *c.h_indset_sweeps;
   OHG_CUDA(cudaEventElapsedTime(&st.ms_refine, e0, e1));
   OHG_CUDA(cudaEventElapsedTime(&st.ms_coarsen, e1, e2));

@@ -114,6 +114,7 @@ struct Ctx {
   // over the calls since the counter was last cleared) and its pinned copy
   int* d_indset_sweeps = nullptr;
   int* h_indset_sweeps = nullptr;
+  double* h_pass_min = nullptr;  // pinned: a pass's worst quality, read at its end
   // opt-in timing of named kernels: CUDA events on the context's stream
   // around each launch, resolved when read (no synchronisation in between)
   bool time_kernels = false;

@@ -34,6 +34,7 @@ Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaMalloc(&d_indset_sweeps, sizeof(int)));
   OHG_CUDA(cudaMemset(d_indset_sweeps, 0, sizeof(int)));
   OHG_CUDA(cudaMallocHost(&h_indset_sweeps, sizeof(int)));
+  OHG_CUDA(cudaMallocHost(&h_pass_min, sizeof(double)));
   cudaMemPool_t pool;
   OHG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
   std::uint64_t thr = ~std::uint64_t(0);
@@ -59,6 +60,7 @@ Ctx::~Ctx() {
   cudaFree(d_screen_counts);
   cudaFree(d_indset_sweeps);
   cudaFreeHost(h_indset_sweeps);
+  cudaFreeHost(h_pass_min);
   if (d_swap_tables) cudaFree(d_swap_tables);
   cudaFreeHost(h_pinned);
   cudaStreamDestroy(stream);
@@ -771,8 +773,9 @@ __global__ void k_reduce(const T* in, LO n, T init, Op op, T* out) {
   }
   if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
+// the reduction of a into a one-element device array (no host wait)
 template <class T, class Op>
-static T reduce(const Arr<T>& a, T init, Op op) {
+static Arr<T> reduce_dev(const Arr<T>& a, T init, Op op) {
   Ctx& c = ctx();
   LO n = a.size();
   int nb = int(std::min<LO>(1024, (n + kBlock - 1) / kBlock));
@@ -785,7 +788,11 @@ static T reduce(const Arr<T>& a, T init, Op op) {
 #ifdef OHG_CHECKED
   checked_after_launch(__FILE__, __LINE__);
 #endif
-  return get_elem(fin, 0);
+  return fin;
+}
+template <class T, class Op>
+static T reduce(const Arr<T>& a, T init, Op op) {
+  return get_elem(reduce_dev(a, init, op), 0);
 }
 struct MaxOp {
   template <class T>
@@ -798,6 +805,7 @@ struct MinOp {
 I8 max_i8(const Arr<I8>& a) { return reduce<I8>(a, I8(-128), MaxOp()); }
 LO max_lo(const Arr<LO>& a) { return reduce<LO>(a, LO(-2147483647 - 1), MaxOp()); }
 double min_f64(const Arr<double>& a) { return reduce<double>(a, DBL_MAX, MinOp()); }
+Arr<double> min_f64_dev(const Arr<double>& a) { return reduce_dev<double>(a, DBL_MAX, MinOp()); }
 double max_f64(const Arr<double>& a) { return reduce<double>(a, -DBL_MAX, MaxOp()); }
 
 // ------------------------------------------------------------ radix sort

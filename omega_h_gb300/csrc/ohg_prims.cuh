@@ -47,6 +47,7 @@ Arr<LO> collect_marked_offs(const Arr<I8>& marks, const Arr<LO>& offs, LO cnt);
 // reductions (synchronise the stream)
 I8 max_i8(const Arr<I8>& a);
 double min_f64(const Arr<double>& a);
+Arr<double> min_f64_dev(const Arr<double>& a);  // no host wait
 double max_f64(const Arr<double>& a);
 LO max_lo(const Arr<LO>& a);
 
