@@ -39,10 +39,11 @@ AUTOTUNE_PASSES = 4
 # bytes per launch on the 64^3 shock pass: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of k_coarsen_screen_v<3> (overshoot
 # check and quality screen, directions by rail length; per-face invariants,
-# cubed tail, queued pairs; vertices taken 8 at a time, 912 blocks of 128
-# threads), profiles/coarsen_filter_box64_shock.md; to be captured again
-# whenever that kernel changes
-DOMINANT_TRAFFIC = 139202048 + 19366656
+# cubed tail, queued pairs, one pass over the local vertices per element;
+# vertices taken 8 at a time, 1064 blocks of 128 threads, 7 per SM),
+# profiles/coarsen_filter_box64_shock.md; to be captured again whenever that
+# kernel changes
+DOMINANT_TRAFFIC = 139600896 + 20408320
 # FP64 add, multiply and fused multiply-add thread instructions per launch of
 # the FP64 output kernels on the 64^3 shock box, all edges / all tets (ncu:
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), for their

@@ -1724,16 +1724,22 @@ __global__ void __launch_bounds__(kVsBlock, 7) k_coarsen_screen_v(CoarsenVertexA
         int pos = code_which_down(a.vc[s0 + x]);
         unsigned packed = 0;
         bool here = true;
+        // the element's other vertices among the local ones: one pass over
+        // the local list for all of them (v itself, slot pos, is local 0)
+        LO u[NV];
+        unsigned li[NV];
         for (int j = 0; j < NV; ++j) {
-          unsigned li = 0;
-          if (j != pos) {
-            LO u = a.cv[el * NV + j];
-            li = 255;
-            for (LO k = 1; k <= ne; ++k)
-              if (s_gid[w][k] == u) li = unsigned(k);
-            if (li == 255) here = false;
-          }
-          packed |= li << (8 * j);
+          u[j] = j != pos ? a.cv[el * NV + j] : LO(-1);
+          li[j] = j != pos ? 255u : 0u;
+        }
+        for (LO k = 1; k <= ne; ++k) {
+          LO g = s_gid[w][k];
+          for (int j = 0; j < NV; ++j)
+            if (u[j] == g) li[j] = unsigned(k);
+        }
+        for (int j = 0; j < NV; ++j) {
+          if (li[j] == 255u) here = false;
+          packed |= li[j] << (8 * j);
         }
         s_elem[w][x] = packed;
         found = found && here;
