@@ -1,4 +1,5 @@
 // The C ABI (include/ohg.h) over the device mesh and operators.
+#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -471,7 +472,9 @@ int ohg_context_pool_bytes(ohg_context* c, int reset_high, long long* used, long
     cudaGetLastError();
     return OHG_ERR_CUDA;
   }
-  *used = (long long)u;
+  // blocks the contexts keep for reuse are not in use by any array
+  long long cached = g_cached_device_bytes.load();
+  *used = std::max(0LL, (long long)u - cached);
   *reserved = (long long)r;
   *used_high = (long long)h;
   return OHG_OK;

@@ -7,8 +7,10 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <atomic>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -90,6 +92,26 @@ struct Tuner {
 constexpr int kPinnedInts = 32;
 constexpr int kPinnedStatusSlot = kPinnedInts - 1;
 
+// Freed device blocks kept for reuse, by size class: a host-side cache in
+// front of the stream-ordered pool, whose allocation calls cost about 3 µs
+// of host time each over a pass's few hundred arrays of mixed sizes.  Every
+// block belongs to one context and is used on its stream only, so a block
+// freed (its last use enqueued) may serve the next allocation at once, as
+// the pool itself would.  Blocks past the cap go back to the pool.
+struct DevCache {
+  std::mutex mu;
+  std::unordered_map<size_t, std::vector<void*>> lists;
+  size_t bytes = 0;
+  size_t cap = size_t(2) << 30;
+  bool open = true;
+  cudaStream_t stream = nullptr;
+  void* take(size_t cls);
+  bool put(void* p, size_t cls);
+  void release();  // every cached block back to the pool (stream-ordered)
+};
+// device bytes held in the caches of all contexts (not in use by arrays)
+extern std::atomic<long long> g_cached_device_bytes;
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -104,6 +126,13 @@ struct Ctx {
   // OHG_TRACE_SYNCS and printed to stderr when the context is destroyed
   bool trace_syncs = false;
   std::map<std::pair<std::string, int>, std::uint64_t> sync_sites;
+  // with the trace: host time blocked in each site's waits (nanoseconds)
+  std::map<std::pair<std::string, int>, std::uint64_t> sync_wait_ns;
+  // and the host time from the previous wait's return to this one (the
+  // host issuing the work in between), with the launches issued in it
+  std::map<std::pair<std::string, int>, std::uint64_t> sync_issue_ns, sync_issue_launches;
+  std::int64_t trace_last_ns = -1;
+  std::uint64_t trace_last_launches = 0;
   std::uint64_t allocs = 0;  // device allocations made through dev_alloc
   // FP32 screening with exact FP64 recheck (1, default) or FP64 throughout (0)
   int screening = 1;
@@ -115,6 +144,7 @@ struct Ctx {
   int* d_indset_sweeps = nullptr;
   int* h_indset_sweeps = nullptr;
   double* h_pass_min = nullptr;  // pinned: a pass's worst quality, read at its end
+  std::shared_ptr<DevCache> cache = std::make_shared<DevCache>();
   // opt-in timing of named kernels: CUDA events on the context's stream
   // around each launch, resolved when read (no synchronisation in between)
   bool time_kernels = false;
@@ -140,8 +170,9 @@ void set_ctx(Ctx* c);
 
 struct Buf {
   void* p = nullptr;
-  size_t bytes = 0;
+  size_t bytes = 0;  // the block's size class
   cudaStream_t stream = nullptr;
+  std::shared_ptr<DevCache> cache;  // the owning context's (kept past its end)
   ~Buf();
 };
 
@@ -165,7 +196,9 @@ struct Arr {
   }
 };
 
-void* dev_alloc(size_t bytes);
+// a device block of at least bytes (rounded up to its size class, which
+// bytes receives), from the context's cache or its pool
+void* dev_alloc(size_t& bytes);
 
 template <class T>
 void Arr<T>::alloc(LO count) {
@@ -174,7 +207,9 @@ void Arr<T>::alloc(LO count) {
   size_t bytes = size_t(count > 0 ? count : 1) * sizeof(T);
   buf->p = dev_alloc(bytes);
   buf->bytes = bytes;
-  buf->stream = ctx().stream;
+  Ctx& c = ctx();
+  buf->stream = c.stream;
+  buf->cache = c.cache;
   ptr = static_cast<T*>(buf->p);
 }
 

@@ -1,5 +1,6 @@
 // Scan, compaction, reduction and radix-sort kernels.
 #include <cfloat>
+#include <chrono>
 #include <cstdlib>
 #include <mutex>
 
@@ -25,6 +26,7 @@ void set_ctx(Ctx* c) { g_ctx = c; }
 Ctx::Ctx(int dev) : device(dev) {
   OHG_CUDA(cudaSetDevice(dev));
   OHG_CUDA(cudaStreamCreate(&stream));  // blocking: ordered with the legacy default stream
+  cache->stream = stream;
   OHG_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   OHG_CUDA(cudaMalloc(&d_status, sizeof(int)));
   OHG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
@@ -44,12 +46,20 @@ Ctx::Ctx(int dev) : device(dev) {
 }
 Ctx::~Ctx() {
   cudaStreamSynchronize(stream);
+  cache->release();
+  {
+    std::lock_guard<std::mutex> g(cache->mu);
+    cache->open = false;  // arrays that outlive the context free to the pool
+  }
+  cudaStreamSynchronize(stream);
   if (trace_syncs) {
     std::fprintf(stderr, "ohg: host waits by call site (%llu in all)\n",
                  (unsigned long long)syncs);
     for (auto& kv : sync_sites)
-      std::fprintf(stderr, "ohg:   %s:%d %llu\n", kv.first.first.c_str(), kv.first.second,
-                   (unsigned long long)kv.second);
+      std::fprintf(stderr, "ohg:   %s:%d %llu (%.3f ms blocked, %.3f ms issuing %llu launches before)\n",
+                   kv.first.first.c_str(), kv.first.second, (unsigned long long)kv.second,
+                   double(sync_wait_ns[kv.first]) * 1e-6, double(sync_issue_ns[kv.first]) * 1e-6,
+                   (unsigned long long)sync_issue_launches[kv.first]);
   }
   tuner.release();
   for (auto& k : kernel_launches) {
@@ -67,8 +77,25 @@ Ctx::~Ctx() {
 }
 void Ctx::sync(const char* file, int line) {
   ++syncs;
-  if (trace_syncs) ++sync_sites[{file, line}];
-  OHG_CUDA(cudaStreamSynchronize(stream));
+  if (trace_syncs) {
+    ++sync_sites[{file, line}];
+    auto ns = [] {
+      return std::int64_t(std::chrono::duration_cast<std::chrono::nanoseconds>(
+                              std::chrono::steady_clock::now().time_since_epoch())
+                              .count());
+    };
+    std::int64_t t0 = ns();
+    if (trace_last_ns >= 0) {
+      sync_issue_ns[{file, line}] += std::uint64_t(t0 - trace_last_ns);
+      sync_issue_launches[{file, line}] += launches - trace_last_launches;
+    }
+    OHG_CUDA(cudaStreamSynchronize(stream));
+    trace_last_ns = ns();
+    trace_last_launches = launches;
+    sync_wait_ns[{file, line}] += std::uint64_t(trace_last_ns - t0);
+  } else {
+    OHG_CUDA(cudaStreamSynchronize(stream));
+  }
   if (!tuner.pending.empty()) tuner.resolve();
 }
 
@@ -172,11 +199,55 @@ int Ctx::take_status() {
   return h_pinned[0];
 }
 
-void* dev_alloc(size_t bytes) {
-  void* p = nullptr;
+std::atomic<long long> g_cached_device_bytes{0};
+
+// size classes: multiples of 512 bytes up to 4 KiB, then four classes per
+// power of two (at most a quarter over the request)
+static size_t size_class(size_t b) {
+  if (b <= 4096) return (b + 511) & ~size_t(511);
+  size_t p = size_t(1) << (63 - __builtin_clzll((unsigned long long)b));
+  size_t step = p / 4;
+  return (b + step - 1) / step * step;
+}
+void* DevCache::take(size_t cls) {
+  std::lock_guard<std::mutex> g(mu);
+  auto it = lists.find(cls);
+  if (it == lists.end() || it->second.empty()) return nullptr;
+  void* p = it->second.back();
+  it->second.pop_back();
+  bytes -= cls;
+  g_cached_device_bytes -= (long long)cls;
+  return p;
+}
+bool DevCache::put(void* p, size_t cls) {
+  std::lock_guard<std::mutex> g(mu);
+  if (!open || bytes + cls > cap) return false;
+  lists[cls].push_back(p);
+  bytes += cls;
+  g_cached_device_bytes += (long long)cls;
+  return true;
+}
+void DevCache::release() {
+  std::lock_guard<std::mutex> g(mu);
+  for (auto& kv : lists)
+    for (void* p : kv.second) cudaFreeAsync(p, stream);
+  lists.clear();
+  g_cached_device_bytes -= (long long)bytes;
+  bytes = 0;
+}
+void* dev_alloc(size_t& bytes) {
   Ctx& c = ctx();
   ++c.allocs;
+  bytes = size_class(bytes);
+  if (void* q = c.cache->take(bytes)) return q;
+  void* p = nullptr;
   cudaError_t e = cudaMallocAsync(&p, bytes, c.stream);
+  if (e != cudaSuccess) {
+    // the cached blocks back to the pool, then once more
+    cudaGetLastError();
+    c.cache->release();
+    e = cudaMallocAsync(&p, bytes, c.stream);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     throw Error(6, "device allocation of " + std::to_string(bytes) + " bytes failed");
@@ -184,7 +255,9 @@ void* dev_alloc(size_t bytes) {
   return p;
 }
 Buf::~Buf() {
-  if (p) cudaFreeAsync(p, stream);
+  if (!p) return;
+  if (cache && cache->put(p, bytes)) return;
+  cudaFreeAsync(p, stream);
 }
 
 // ------------------------------------------------------------ scan
