@@ -166,10 +166,10 @@ int ohg_mesh_nents(ohg_mesh* mesh, int dim, int* out);
  * admission counts it). */
 int ohg_mesh_device_bytes(ohg_mesh* mesh, long long* bytes);
 /* The device's stream-ordered memory pool, which every context of the device
- * in this process draws from: bytes in use by arrays (the blocks the
- * contexts keep for reuse, up to 2 GiB each, are not counted), bytes
- * reserved from the device, and the high-water mark of bytes drawn from the
- * pool (reset to the current draw when reset_high is nonzero).  It neither waits on nor touches the context's
+ * in this process draws from: bytes in use (including the freed blocks each
+ * context keeps for reuse, up to 2 GiB per context), bytes reserved from
+ * the device, and the high-water mark of bytes in use (reset to the current
+ * use when reset_high is nonzero).  It neither waits on nor touches the context's
  * stream, so any host thread may call it.  No counterpart in the reference. */
 int ohg_context_pool_bytes(ohg_context* ctx, int reset_high, long long* used,
                            long long* reserved, long long* used_high);

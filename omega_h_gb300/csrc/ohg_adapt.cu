@@ -232,6 +232,29 @@ __device__ __forceinline__ void warp_count_full(unsigned long long* p, unsigned 
   if ((threadIdx.x & 31u) == 0u && tot) atomicAdd(p, (unsigned long long)tot);
 }
 
+// f(i) for every i below a count that is on the device (*n_dev, at most
+// bound), in a grid-stride loop over a grid of resident size: the count
+// needs no host wait
+template <class F>
+__global__ void k_for_dev_count(const LO* n_dev, F f) {
+  LO n = *n_dev;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    f(LO(i));
+}
+template <class F>
+static void pfor_dev_count(const LO* n_dev, LO bound, F f) {
+  if (bound <= 0) return;
+  Ctx& c = ctx();
+  long long full = (long long)c.num_sms * (2048 / kBlock);
+  long long need = ((long long)bound + kBlock - 1) / kBlock;
+  k_for_dev_count<<<unsigned(need < full ? need : full), kBlock, 0, c.stream>>>(n_dev, f);
+  ++c.launches;
+#ifdef OHG_CHECKED
+  checked_after_launch(__FILE__, __LINE__);
+#endif
+}
+
 // lanes per collapse direction in the cavity screens (both directions of a
 // candidate must fit in one warp: at most 16)
 constexpr int kCavityLanes = 8;
@@ -2832,6 +2855,10 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   // when the vertex-to-face rows are not built: their ascending order is the
   // sorted row's, without inverting and sorting the face-to-vertex lists.
   bool faces_by_tets = dim == 3 && !m.adj.count({VERT, FACE});
+  // per key with at most 32 tets, its live faces in ascending order (at
+  // most 96), found by the count below and copied out by the fill
+  constexpr int kFaceLoc = 96;
+  Arr<LO> face_loc(faces_by_tets ? nkeys * kFaceLoc : 0);
   for (int d = 1; d <= dim; ++d) {
     auto dd = cview(dead[d]);
     auto kv = cview(k2v);
@@ -2843,6 +2870,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       auto tb = cview(v2t.ab2b);
       auto tc = cview(v2t.codes);
       auto tf = cview(m.ask_down(3, 2).ab2b);
+      auto fl = view(face_loc);
       group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
         if (k < 0) return;
         LO v = kv[k], beg = ta[v], end = ta[v + 1];
@@ -2851,7 +2879,21 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
           LO F[3];
           bool keep[3];
           faces_around_lane(v, beg, end, gl, tb, tc, tf, F, keep);
-          for (int i = 0; i < 3; ++i) n2 += keep[i] && !dd[F[i]];
+          // the live faces kept here (-1: none), each placed at its rank
+          // among the live faces (the sorted row's order)
+          LO L[3];
+          for (int i = 0; i < 3; ++i) L[i] = keep[i] && !dd[F[i]] ? F[i] : -1;
+          LO rank[3] = {0, 0, 0};
+          for (int src = 0; src < 32; ++src)
+            for (int j = 0; j < 3; ++j) {
+              LO o = __shfl_sync(0xffffffffu, L[j], src);
+              for (int i = 0; i < 3; ++i) rank[i] += o >= 0 && o < L[i];
+            }
+          for (int i = 0; i < 3; ++i) {
+            if (L[i] < 0) continue;
+            fl[k * kFaceLoc + rank[i]] = L[i];
+            ++n2;
+          }
           n2 = LO(__reduce_add_sync(gm, unsigned(n2)));
         } else if (gl == 0) {
           // a long row: one lane, each face counted at its first occurrence
@@ -2919,6 +2961,7 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
       auto o2n = cview(ov2nv);
       auto kd = view(kd2d);
       auto pv = view(pv2v);
+      auto fl = cview(face_loc);
       // the live faces in ascending order (the sorted row's order): each
       // one's rank among the live faces gives its product slot
       group_for(32, nkeys, kBlock, [=] __device__(LO k, int gl, unsigned gm) {
@@ -2932,19 +2975,9 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
           }
         };
         if (end - beg <= 32) {
-          LO F[3];
-          bool keep[3];
-          faces_around_lane(v, beg, end, gl, tb, tc, tf, F, keep);
-          LO L[3];  // the live faces kept here (-1: none)
-          for (int i = 0; i < 3; ++i) L[i] = keep[i] && !dd[F[i]] ? F[i] : -1;
-          LO rank[3] = {0, 0, 0};
-          for (int src = 0; src < 32; ++src)
-            for (int j = 0; j < 3; ++j) {
-              LO o = __shfl_sync(0xffffffffu, L[j], src);
-              for (int i = 0; i < 3; ++i) rank[i] += o >= 0 && o < L[i];
-            }
-          for (int i = 0; i < 3; ++i)
-            if (L[i] >= 0) put(p + rank[i], L[i]);
+          // the count placed them in order
+          LO nf = kp[k + 1] - p;
+          for (LO r = gl; r < nf; r += 32) put(p + r, fl[k * kFaceLoc + r]);
         } else if (gl == 0) {
           // a long row: one lane; a face's slot is the number of live first
           // occurrences with a smaller id
@@ -3259,29 +3292,6 @@ void swap3d_find_loops(Mesh& m, const LO* edges, LO n, int* sizes, LO* eev2v, LO
 // improving_only (the pass): a candidate whose best triangulation's upper
 // bound is below the worst current quality around its edge cannot pass
 // filter_swap_improve; it gets quality -DBL_MAX and no FP64 work.
-// f(i) for every i below a count that is on the device (*n_dev, at most
-// bound), in a grid-stride loop over a grid of resident size: the count
-// needs no host wait
-template <class F>
-__global__ void k_for_dev_count(const LO* n_dev, F f) {
-  LO n = *n_dev;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    f(LO(i));
-}
-template <class F>
-static void pfor_dev_count(const LO* n_dev, LO bound, F f) {
-  if (bound <= 0) return;
-  Ctx& c = ctx();
-  long long full = (long long)c.num_sms * (2048 / kBlock);
-  long long need = ((long long)bound + kBlock - 1) / kBlock;
-  k_for_dev_count<<<unsigned(need < full ? need : full), kBlock, 0, c.stream>>>(n_dev, f);
-  ++c.launches;
-#ifdef OHG_CHECKED
-  checked_after_launch(__FILE__, __LINE__);
-#endif
-}
-
 static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, LO n,
                                       double* quals_p, I8* configs_p,
                                       bool improving_only = false) {
@@ -3539,6 +3549,9 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     auto enc = cview(ent);
     pfor_dev_count(toff.data() + n, bound, [=] __device__(LO j) {
       LO idx = enc[j];
+      // an entry no tile wrote (only after a scan tile gave up its wait,
+      // which the pass reports as an error) is skipped, not followed
+      if (idx < 0 || idx >= bound) return;
       LO i = idx / kMaxUniqTris;
       int u = idx % kMaxUniqTris;
       int size = ls[i];

@@ -1,5 +1,4 @@
 // The C ABI (include/ohg.h) over the device mesh and operators.
-#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -472,9 +471,9 @@ int ohg_context_pool_bytes(ohg_context* c, int reset_high, long long* used, long
     cudaGetLastError();
     return OHG_ERR_CUDA;
   }
-  // blocks the contexts keep for reuse are not in use by any array
-  long long cached = g_cached_device_bytes.load();
-  *used = std::max(0LL, (long long)u - cached);
+  // blocks the contexts keep for reuse count as in use, as the pool counts
+  // them: the high-water mark, taken by the pool, includes them too
+  *used = (long long)u;
   *reserved = (long long)r;
   *used_high = (long long)h;
   return OHG_OK;

@@ -7,7 +7,6 @@
 
 #include <cstdint>
 #include <cstdio>
-#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -109,8 +108,6 @@ struct DevCache {
   bool put(void* p, size_t cls);
   void release();  // every cached block back to the pool (stream-ordered)
 };
-// device bytes held in the caches of all contexts (not in use by arrays)
-extern std::atomic<long long> g_cached_device_bytes;
 
 struct Ctx {
   int device = 0;

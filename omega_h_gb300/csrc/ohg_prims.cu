@@ -199,8 +199,6 @@ int Ctx::take_status() {
   return h_pinned[0];
 }
 
-std::atomic<long long> g_cached_device_bytes{0};
-
 // size classes: multiples of 512 bytes up to 4 KiB, then four classes per
 // power of two (at most a quarter over the request)
 static size_t size_class(size_t b) {
@@ -216,7 +214,6 @@ void* DevCache::take(size_t cls) {
   void* p = it->second.back();
   it->second.pop_back();
   bytes -= cls;
-  g_cached_device_bytes -= (long long)cls;
   return p;
 }
 bool DevCache::put(void* p, size_t cls) {
@@ -224,7 +221,6 @@ bool DevCache::put(void* p, size_t cls) {
   if (!open || bytes + cls > cap) return false;
   lists[cls].push_back(p);
   bytes += cls;
-  g_cached_device_bytes += (long long)cls;
   return true;
 }
 void DevCache::release() {
@@ -232,7 +228,6 @@ void DevCache::release() {
   for (auto& kv : lists)
     for (void* p : kv.second) cudaFreeAsync(p, stream);
   lists.clear();
-  g_cached_device_bytes -= (long long)bytes;
   bytes = 0;
 }
 void* dev_alloc(size_t& bytes) {
