@@ -3345,9 +3345,10 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   auto ei = cview(eitem);
   {
     auto tb = view(tbnd);
-    pfor(n * kMaxUniqTris, [=] __device__(LO item) {
-      if (item >= to[n]) return;
+    // the items up to their count on the device, in a grid of resident size
+    pfor_dev_count(tioff.data() + n, n * kMaxUniqTris, [=] __device__(LO item) {
       LO i = ti[item];
+      if (i < 0 || i >= n) return;  // unwritten only after a scan tile gave up its wait
       int u = int(item - to[i]);
       LO idx = i * kMaxUniqTris + u;
       int size = ls[i];
@@ -3410,9 +3411,9 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
     // floats t_dn <= max_len < t_up for the end-length cut (strict above)
     float tup = float_at_or_above(max_len);
     if (double(tup) == max_len) tup = std::nextafter(tup, INFINITY);
-    pfor(n * kMaxUniqEdges, [=] __device__(LO item) {
-      if (item >= eo[n]) return;
+    pfor_dev_count(eioff.data() + n, n * kMaxUniqEdges, [=] __device__(LO item) {
       LO i = ei[item];
+      if (i < 0 || i >= n) return;  // unwritten only after a scan tile gave up its wait
       int u = int(item - eo[i]);
       LO idx = i * kMaxUniqEdges + u;
       int size = ls[i];
