@@ -996,17 +996,25 @@ void refine_qualities(Mesh& m, const LO* c2e_p, LO n, const double* mid_p, doubl
   auto c2e = cview(c2e_p, n);
   auto mid = cview(mid_p, n * mc);
   auto out = view(out_p, n);
-  pfor(n, [=] __device__(LO cand) {
+  // 8 lanes per candidate over its (element, child) pairs, then the minimum
+  // across the lanes (a minimum does not depend on the order: no child
+  // quality is NaN or -0)
+  constexpr int G = 8;
+  group_for(G, n, kBlock, [=] __device__(LO cand, int gl, unsigned gm) {
+    if (cand < 0) return;
     LO e = c2e[cand];
     LO v0 = ev[e * 2], v1 = ev[e * 2 + 1];
     double midp[3];
     for (int j = 0; j < dim; ++j) midp[j] = (c[v0 * dim + j] + c[v1 * dim + j]) / 2.;
     double minq = 1.0;
-    for (LO x = ea[e]; x < ea[e + 1]; ++x) {
+    LO np = 2 * (ea[e + 1] - ea[e]);
+    for (LO pi = gl; pi < np; pi += G) {
+      LO x = ea[e] + pi / 2;
       LO el = eb[x];
       I8 code = ec[x];
       int cce = code_which_down(code), rot = code_rotation(code);
-      for (int eev = 0; eev < 2; ++eev) {
+      {
+        int eev = int(pi & 1);
         int ccv = down_template(dim, 1, cce, eev ^ rot);
         int ccs = opposite_template(dim, 0, ccv);
         LO sv[3];
@@ -1030,7 +1038,9 @@ void refine_qualities(Mesh& m, const LO* c2e_p, LO n, const double* mid_p, doubl
         minq = min2d(minq, q);
       }
     }
-    out[cand] = minq;
+#pragma unroll
+    for (int j = G / 2; j > 0; j >>= 1) minq = min2d(minq, __shfl_xor_sync(gm, minq, j, G));
+    if (gl == 0) out[cand] = minq;
   });
 }
 
