@@ -3485,18 +3485,25 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
   {
     auto nd = view(need);
     auto lst = view(lstar);
-    pfor(n, [=] __device__(LO i) {
+    // 8 lanes per candidate over its triangulations; the floats are combined
+    // by max, min and or, which do not depend on the order (the bounds are
+    // only compared, so the sign of a zero does not matter)
+    constexpr int G = 8;
+    group_for(G, n, kBlock, [=] __device__(LO i, int gl, unsigned gm) {
+      if (i < 0) return;
       int size = ls[i];
       if (size < 3) {
-        nd[i] = 0;
-        lst[i] = INFINITY;
+        if (gl == 0) {
+          nd[i] = 0;
+          lst[i] = INFINITY;
+        }
         return;
       }
       const int* h = &tab[size * 9];
       int nmeshes = h[SW_NMESH], ntris = h[SW_NTRI], nedges = h[SW_NEDGE];
       int omsh = h[SW_OMESH], oe2u = h[SW_OE2U];
       float L = -INFINITY;
-      for (int mesh = 0; mesh < nmeshes; ++mesh) {
+      for (int mesh = gl; mesh < nmeshes; mesh += G) {
         bool valid = true;
         for (int e = 0; e < nedges; ++e)
           if (ov[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]]) valid = false;
@@ -3506,9 +3513,11 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
           mlo = fminf(mlo, tb[i * kMaxUniqTris + tab[omsh + mesh * ntris + t]].x);
         L = fmaxf(L, mlo);
       }
+#pragma unroll
+      for (int j = G / 2; j > 0; j >>= 1) L = fmaxf(L, __shfl_xor_sync(gm, L, j, G));
       unsigned long long mask = 0;
       float best_hi = -INFINITY;
-      for (int mesh = 0; mesh < nmeshes; ++mesh) {
+      for (int mesh = gl; mesh < nmeshes; mesh += G) {
         bool valid = true;
         for (int e = 0; e < nedges; ++e)
           if (ov[i * kMaxUniqEdges + tab[oe2u + mesh * nedges + e]]) valid = false;
@@ -3523,14 +3532,21 @@ static void swap3d_qualities_screened(Mesh& m, double max_len, const LO* c2e_p, 
           if (tb[i * kMaxUniqTris + u].x <= mhi) mask |= 1ull << u;
         }
       }
+#pragma unroll
+      for (int j = G / 2; j > 0; j >>= 1) {
+        best_hi = fmaxf(best_hi, __shfl_xor_sync(gm, best_hi, j, G));
+        mask |= __shfl_xor_sync(gm, mask, j, G);
+      }
       // cannot beat the worst current quality: no FP64 work (L = +inf
       // marks it for the selection below)
       if (improving && best_hi < o3[i]) {
         mask = 0;
         L = INFINITY;
       }
-      nd[i] = mask;
-      lst[i] = L;
+      if (gl == 0) {
+        nd[i] = mask;
+        lst[i] = L;
+      }
     });
   }
   auto nd = cview(need);
