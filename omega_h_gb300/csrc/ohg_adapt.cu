@@ -604,8 +604,10 @@ struct ModifyPlan {
   Arr<LO> same_offs, reps, offs;
   LO sizes[3] = {0, 0, 0};  // kept, new, products
 };
+// key_marks, if given, is mark_image(keys2kds, om.nents[key_dim]): the same
+// for every dimension of one rebuild, so its caller makes it once
 static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>& keys2kds,
-                              const Arr<LO>& keys2prods) {
+                              const Arr<LO>& keys2prods, const Arr<I8>* key_marks = nullptr) {
   LO nkeys = keys2kds.size();
   ModifyPlan pl;
   LO nold = om.nents[ent_dim];
@@ -615,14 +617,26 @@ static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>&
   Arr<I8> km;
   Arr<I8>& same = pl.same;
   Arr<LO>& same_offs = pl.same_offs;
+  // get_rep_counts (src/Omega_h_modify.cpp:210-243) starts from the kept
+  // marks (1 each without modified entities); the keys' products are added
+  // below
+  Arr<LO> counts(nold);
   if (some_mod) {
-    km = mark_image(keys2kds, om.nents[key_dim]);
+    km = key_marks ? *key_marks : mark_image(keys2kds, om.nents[key_dim]);
     Arr<I8> mods_ent = ent_dim == key_dim ? km : mark_up(om, key_dim, ent_dim, km);
     same = Arr<I8>(nold);
     auto me = cview(mods_ent);
     auto sm = view(same);
-    pfor(nold, [=] __device__(LO e) { sm[e] = !me[e]; });
+    auto ct = view(counts);
+    pfor(nold, [=] __device__(LO e) {
+      I8 k = !me[e];
+      sm[e] = k;
+      ct[e] = LO(k);
+    });
     same_offs = offset_scan(same);
+  } else {
+    auto ct = view(counts);
+    pfor(nold, [=] __device__(LO e) { ct[e] = 1; });
   }
   // representatives (get_mods2reps, src/Omega_h_modify.cpp:163-195)
   Arr<LO>& reps = pl.reps;
@@ -737,13 +751,10 @@ static ModifyPlan plan_modify(Mesh& om, int ent_dim, int key_dim, const Arr<LO>&
       pfor(nkeys, [=] __device__(LO k) { r[k] = dn[kd[k] * deg]; });
     }
   }
-  // get_rep_counts (src/Omega_h_modify.cpp:210-243): integer sums, so the
+  // the keys' products onto their representatives: integer sums, so the
   // atomics give a deterministic result
-  Arr<LO> counts(nold);
   {
     auto ct = view(counts);
-    auto sm = cview(same);
-    pfor(nold, [=] __device__(LO e) { ct[e] = some_mod ? LO(sm[e]) : 1; });
     auto r = cview(reps);
     auto kp = cview(keys2prods);
     pfor(nkeys, [=] __device__(LO k) { atomicAdd(&ct[r[k]], kp[k + 1] - kp[k]); });
@@ -2944,8 +2955,9 @@ static bool coarsen_verts(Mesh& m, const AdaptOpts& o, const Arr<I8>& vm, bool a
   {
     std::vector<ModifyPlan*> pls;
     std::vector<const Arr<LO>*> kps;
+    Arr<I8> key_marks = mark_image(k2v, m.nverts());
     for (int d = 0; d <= dim; ++d) {
-      plans[d] = plan_modify(m, d, VERT, k2v, k2ps[d]);
+      plans[d] = plan_modify(m, d, VERT, k2v, k2ps[d], &key_marks);
       pls.push_back(&plans[d]);
       kps.push_back(&k2ps[d]);
     }
@@ -3903,8 +3915,9 @@ static void swap_rebuild(Mesh& m, const Arr<LO>& k2e, Arr<LO>* k2p, Arr<LO>* pv2
   {
     std::vector<ModifyPlan*> pls;
     std::vector<const Arr<LO>*> kps;
+    Arr<I8> key_marks = mark_image(k2e, m.nedges());
     for (int d = 1; d <= dim; ++d) {
-      plans[d] = plan_modify(m, d, EDGE, k2e, k2p[d]);
+      plans[d] = plan_modify(m, d, EDGE, k2e, k2p[d], &key_marks);
       pls.push_back(&plans[d]);
       kps.push_back(&k2p[d]);
     }
