@@ -918,20 +918,28 @@ static ModifyOut modify_ents_adapt(Mesh& om, Mesh& nm, int ent_dim, int key_dim,
 template <class T>
 static Arr<T> xfer(const Arr<T>& old, const ModifyOut& mo, LO nnew, const Arr<T>& prod, int w) {
   Arr<T> nd(nnew * w);
-  if (prod.size()) map_into(prod, mo.prods2new, nd, w);
+  // one launch: the products' values first, then the kept entities'
+  LO np = prod.size() ? mo.prods2new.size() : 0;
+  auto p2n = cview(mo.prods2new);
+  auto pv = cview(prod);
   auto s2o = cview(mo.same2old);
   auto s2n = cview(mo.same2new);
   auto o = cview(old);
   auto d = view(nd);
-  pfor(mo.same2old.size(), [=] __device__(LO i) {
-    for (int j = 0; j < w; ++j) d[s2n[i] * w + j] = o[s2o[i] * w + j];
+  pfor(np + mo.same2old.size(), [=] __device__(LO i) {
+    if (i < np) {
+      for (int j = 0; j < w; ++j) d[p2n[i] * w + j] = pv[i * w + j];
+    } else {
+      LO k = i - np;
+      for (int j = 0; j < w; ++j) d[s2n[k] * w + j] = o[s2o[k] * w + j];
+    }
   });
   return nd;
 }
 
 // class_dim and class_id of dimension d together, as xfer does for each:
 // products take their values (pcd/pci, or those of the old entities kd2d),
-// kept entities their old ones; two launches for both arrays
+// kept entities their old ones; one launch for both arrays
 static void xfer_class(Mesh& om, Mesh& nm, int d, const ModifyOut& mo, LO nnew, const I8* pcd,
                        const LO* pci, const LO* kd2d) {
   Arr<I8> cd(nnew);
@@ -941,28 +949,28 @@ static void xfer_class(Mesh& om, Mesh& nm, int d, const ModifyOut& mo, LO nnew, 
   auto ncd = view(cd);
   auto nci = view(ci);
   LO np = mo.prods2new.size();
-  if (np) {
-    auto p2n = cview(mo.prods2new);
-    auto kd = cview(kd2d, kd2d ? np : 0);
-    auto pd = cview(pcd, pcd ? np : 0);
-    auto pi = cview(pci, pci ? np : 0);
-    bool gather = kd2d != nullptr;
-    pfor(np, [=] __device__(LO p) {
-      LO q = p2n[p];
-      if (gather) {
-        ncd[q] = ocd[kd[p]];
-        nci[q] = oci[kd[p]];
-      } else {
-        ncd[q] = pd[p];
-        nci[q] = pi[p];
-      }
-    });
-  }
+  auto p2n = cview(mo.prods2new);
+  auto kd = cview(kd2d, kd2d ? np : 0);
+  auto pd = cview(pcd, pcd ? np : 0);
+  auto pi = cview(pci, pci ? np : 0);
+  bool gather = kd2d != nullptr;
   auto s2o = cview(mo.same2old);
   auto s2n = cview(mo.same2new);
-  pfor(mo.same2old.size(), [=] __device__(LO i) {
-    ncd[s2n[i]] = ocd[s2o[i]];
-    nci[s2n[i]] = oci[s2o[i]];
+  pfor(np + mo.same2old.size(), [=] __device__(LO i) {
+    if (i < np) {
+      LO q = p2n[i];
+      if (gather) {
+        ncd[q] = ocd[kd[i]];
+        nci[q] = oci[kd[i]];
+      } else {
+        ncd[q] = pd[i];
+        nci[q] = pi[i];
+      }
+    } else {
+      LO k = i - np;
+      ncd[s2n[k]] = ocd[s2o[k]];
+      nci[s2n[k]] = oci[s2o[k]];
+    }
   });
   nm.class_dim[d] = cd;
   nm.class_id[d] = ci;
