@@ -801,7 +801,32 @@ static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, cons
   const Arr<LO>& offs = pl.offs;
   const LO* sizes = pl.sizes;
   LO nnew = sizes[1];
-  out.same2old = some_mod ? collect_marked_offs(same, same_offs, sizes[0]) : iota(nold);
+  // the kept entities' old and new numbers and the old-to-new map, in one
+  // launch (collect_marked_offs, unmap and map_onto of the same marks)
+  {
+    LO nsame = some_mod ? sizes[0] : nold;
+    out.same2old = Arr<LO>(nsame);
+    out.same2new = Arr<LO>(nsame);
+    out.old2new = Arr<LO>(nold);
+    auto sm = cview(same);
+    auto so = cview(same_offs);
+    auto of = cview(offs);
+    auto s2o = view(out.same2old);
+    auto s2n = view(out.same2new);
+    auto o2n = view(out.old2new);
+    pfor(nold, [=] __device__(LO e) {
+      bool kept = !some_mod || sm[e];
+      if (!kept) {
+        o2n[e] = -1;
+        return;
+      }
+      LO i = some_mod ? so[e] : e;
+      LO q = of[e];
+      s2o[i] = e;
+      s2n[i] = q;
+      o2n[e] = q;
+    });
+  }
   bool has_order = key_dim > ent_dim;
   Arr<LO> order;
   if (has_order) {
@@ -830,7 +855,6 @@ static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, cons
       }
     });
   }
-  out.same2new = unmap(out.same2old, offs, 1);
   out.prods2new = Arr<LO>(sizes[2]);
   {
     auto of = cview(offs);
@@ -846,7 +870,6 @@ static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, cons
       for (LO p = kp[k]; p < kp[k + 1]; ++p) p2n[p] = offset++;
     });
   }
-  out.old2new = map_onto(out.same2new, out.same2old, nold, LO(-1), 1);
   if (ent_dim == VERT) {
     nm.nents[0] = nnew;
     return out;
