@@ -881,7 +881,7 @@ static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, cons
   Adj nd;
   // zero-filled so that every slot holds a valid index even if a caller's
   // keys were not independent (the writes below would then overlap)
-  nd.ab2b = fill<LO>(nnew * deg, 0);
+  nd.ab2b = Arr<LO>(nnew * deg);  // every entry written below
   LO nprods = out.prods2new.size();
   Adj pd;
   if (ld > VERT) {
@@ -898,30 +898,47 @@ static ModifyOut apply_modify(Mesh& om, Mesh& nm, int ent_dim, int key_dim, cons
   } else {
     pd.ab2b = prod_verts2verts;
   }
-  map_into(pd.ab2b, out.prods2new, nd.ab2b, deg);
+  // the new down adjacency and its codes in one launch: every new entity is
+  // a product (its sides and codes as found) or a kept entity (its old
+  // sides renumbered, its old codes)
+  bool codes = ld > VERT;
+  if (codes) {
+    nd.codes = Arr<I8>(nnew * deg);
+    nd.has_codes = true;
+  }
   {
+    LO np = out.prods2new.size(), ns = out.same2old.size();
+    auto p2n = cview(out.prods2new);
+    auto pb = cview(pd.ab2b);
+    auto pc = cview(pd.codes);
     auto s2o = cview(out.same2old);
     auto s2n = cview(out.same2new);
     auto ob = cview(od.ab2b);
+    auto oc = cview(od.codes);
     auto l2n = cview(old_lows2new_lows);
     auto nb = view(nd.ab2b);
+    auto nc = view(nd.codes);
     int* stw = ctx().d_status;
-    pfor(out.same2old.size(), [=] __device__(LO i) {
+    pfor(np + ns, [=] __device__(LO i) {
+      if (i < np) {
+        LO q = p2n[i];
+        for (int k = 0; k < deg; ++k) {
+          nb[q * deg + k] = pb[i * deg + k];
+          if (codes) nc[q * deg + k] = pc[i * deg + k];
+        }
+        return;
+      }
+      LO j = i - np, o = s2o[j], q = s2n[j];
       for (int k = 0; k < deg; ++k) {
-        LO l = l2n[ob[s2o[i] * deg + k]];
+        LO l = l2n[ob[o * deg + k]];
         if (l < 0) {
           raise_status(stw, ST_TOPOLOGY);
           l = 0;
         }
-        nb[s2n[i] * deg + k] = l;
+        nb[q * deg + k] = l;
+        if (codes) nc[q * deg + k] = oc[o * deg + k];
       }
     });
-  }
-  if (ld > VERT) {
-    nd.codes = fill<I8>(nnew * deg, 0);
-    nd.has_codes = true;
-    map_into(unmap(out.same2old, od.codes, deg), out.same2new, nd.codes, deg);
-    map_into(pd.codes, out.prods2new, nd.codes, deg);
   }
   nm.set_ents(ent_dim, std::move(nd));
   return out;
